@@ -1,0 +1,326 @@
+"""Benchmark: ms per RK3 step of the IBM channel (256^3, 1000 spheres D=16dx).
+
+Default run: N=1 GPU, the plain FP64 drop-in path, seeded synthetic inputs
+(perturbed Poiseuille channel, random non-overlapping spheres).  Prints one
+JSON line.  `--impl reference` times the CPU restatement of the reference
+(the oracle, OpenMP on all host cores) on the same workload.
+
+Under torchrun (N>1) every rank runs an independent replica of the case on
+its own GPU ("replicas only": the single-GPU step does not shard); timing is
+max over ranks after a barrier.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ms per RK3 step, 256³ channel+1000 spheres: mixed+learned vs plain FP64 GPU"
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+def sphere_box(case) -> int:
+    return int(round(2 * case.radius * case.dxi + 5)) ** 3
+
+
+def s_fp(case) -> float:
+    import math
+    r = (case.radius - 0.3 / case.dxi) * case.dxi
+    return 4.0 / 3.0 * math.pi * ((r + 1.5) ** 3 - (r - 1.5) ** 3)
+
+
+def algorithmic_bytes(case, w: int = 8) -> dict:
+    """Reference dataflow model per RK3 step: 3 x [32 N + 27 S_fp np + 3 box np] words."""
+    n = case.itot * case.jtot * case.ktot
+    dense = 3 * 32 * n * w
+    ibm = 3 * 27 * s_fp(case) * case.np * w
+    sph = 3 * 3 * sphere_box(case) * case.np * w
+    return {"dense": dense, "ibm": ibm, "sphere": sph, "total": dense + ibm + sph,
+            "predictor": (10 + 13 + 10) * n * w, "projection": 3 * 21 * n * w}
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    from interparts_mpich_gb300 import IBMSolver
+    from interparts_mpich_gb300 import build as b
+    from interparts_mpich_gb300.cases import channel_case
+
+    torch.cuda.set_device(local)
+    if rank == 0 or ws > 1:
+        b.build()
+    barrier(ws)
+    case = channel_case(args.n, args.np, seed=1234)
+    solver = IBMSolver(case)
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    fields = case.initial_fields()
+    solver.setup(fields)
+    dt = 0.5 * solver.chkdt()  # frozen dt (0.5 dtmax at t=0, main.f90:151-154)
+    ncell = case.itot * case.jtot * case.ktot
+    # warm-up
+    for _ in range(args.warmup):
+        solver.rk3_step(dt)
+    solver.sync()
+    # per-phase timing of one extra step (events inside the library)
+    phases = solver.timed_step(dt)
+    torch.cuda.synchronize()
+    launches0 = solver.launch_count()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            solver.run(dt, args.steps)
+            ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = solver.launch_count() - launches0
+    ms_max = max_over_ranks(ms, ws)
+    solver.sync()
+    tot, divmax, _ = solver.chkdiv()
+
+    # end-to-end through the C ABI with host buffers: set u,v,w,p + particles
+    # from pinned host memory, one step, read u,v,w,p + particles back
+    e2e = None
+    if args.e2e_steps > 0:
+        pin = {k: torch.empty(case.shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T for k in "uvwp"}
+        cur = solver.get_fields()
+        for k in "uvwp":
+            pin[k][...] = cur[k]
+        ps = solver.get_particles(lagrangian=True)
+        h2d = 4 * pin["u"].nbytes
+        d2h = 4 * pin["u"].nbytes
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            solver.set_fields(pin["u"], pin["v"], pin["w"], pin["p"])
+            solver.set_particles(ps)
+            solver.rk3_step(dt)
+            f = solver.get_fields()
+            ps = solver.get_particles(lagrangian=True)
+            for k in "uvwp":
+                pin[k][...] = f[k]
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        e2e = {"value": round(max_over_ranks(e2e_ms, ws), 4), "unit": "ms/step",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+    solver.close()
+    return case, dt, ms_max, phases, launches, clk.summary(), e2e, ncell, divmax
+
+
+def cpu_baseline(args, case_fn):
+    """The oracle restatement timed on the host cores on one RK3 step of the workload."""
+    from oracle.oracle import OracleSolver, load
+
+    lib, _ = load()
+    cores = lib.orc_set_threads(os.cpu_count() or 1)
+    case = case_fn()
+    o = OracleSolver(case)
+    o.setup()
+    dt = 0.5 * o.chkdt()
+    t0 = time.perf_counter()
+    o.rk3_step(dt)
+    t = (time.perf_counter() - t0) * 1e3
+    o.close()
+    return {"value": round(t, 1), "unit": "ms/step", "cores": int(cores), "kind": "port",
+            "sample": f"1 RK3 step of the same {case.itot}^3 / {case.np}-sphere case (oracle restatement, OpenMP)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--np", type=int, default=1000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_init()
+
+    from interparts_mpich_gb300.cases import channel_case
+
+    config = {"workload": f"channel {args.n}^3, {args.np} spheres D=16dx, perturbed Poiseuille Re_b=5600, "
+                          f"Nl=3, dt=0.5 dtmax frozen", "grid": [args.n] * 3, "spheres": args.np,
+              "l2_policy": "inputs larger than L2 (each field 137 MB > 129 MB L2)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle.oracle import OracleSolver, load
+        lib, _ = load()
+        cores = lib.orc_set_threads(os.cpu_count() or 1)
+        case = channel_case(args.n, args.np, seed=1234)
+        o = OracleSolver(case)
+        o.setup()
+        dt = 0.5 * o.chkdt()
+        nsteps = min(args.steps, 2)
+        o.rk3_step(dt)  # one untimed warm-up step (bounded sample)
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            o.rk3_step(dt)
+        ms = (time.perf_counter() - t0) * 1e3 / nsteps
+        sample = f"{nsteps} RK3 steps after 1 warm-up step of the same case (oracle restatement, OpenMP)"
+        line = {"metric": METRIC, "value": round(ms, 1), "unit": "ms/step", "impl": "reference", "n_gpus": 0,
+                "steps": nsteps, "warmup": 1, "ms_per_step": round(ms, 1), "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": round(ms, 1), "unit": "ms/step", "cores": int(cores), "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": round(ms, 1), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    case, dt, ms, phases, launches, clocks, e2e, ncell, divmax = run_ours(args, ws, rank, local)
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    ab = algorithmic_bytes(case)
+    # dominant phase roofline (per-phase CUDA-event times of one step)
+    names = ["predictor", "ibm", "projection", "newton_euler"]
+    byts = {"predictor": ab["predictor"], "ibm": ab["ibm"], "projection": ab["projection"],
+            "newton_euler": ab["sphere"]}
+    dom = max(range(4), key=lambda q: phases[q])
+    achieved = byts[names[dom]] / (phases[dom] * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+        "form": "plain FP64 (drop-in)",
+        "mcell_steps_per_s": round(args.gpus * ncell / (ms * 1e-3) / 1e6, 1),
+        "phases_ms": {n: round(t, 4) for n, t in zip(names, phases)},
+        "hbm_roofline_frac_step": round(ab["total"] / (ms * 1e-3) / 1e9 / hbm, 4),
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800"},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "chkdiv_max": divmax,
+        "dt": dt,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args, lambda: channel_case(args.n, args.np, seed=1234))
+        except Exception as ex:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

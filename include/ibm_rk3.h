@@ -1,0 +1,204 @@
+/*
+ * ibm_rk3.h -- C ABI of the GB300-native immersed-boundary RK3 substep.
+ *
+ * This is the drop-in boundary for the InterPartS hot path (one RK3 substep
+ * of a particle-resolved channel DNS: momentum predictor, multidirect IBM
+ * forcing, FFT/tridiagonal pressure projection, sphere integrals, soft-sphere
+ * collisions with lubrication, Newton-Euler update).  A single-rank Fortran
+ * main program binds these entry points through ISO_C_BINDING; every call
+ * replaces one reference subroutine (or one block of the reference driver),
+ * cited beside it as file:line within the reference project.
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, doubles, ints.
+ *   - Every entry point returns an int status: IBM_OK (0) or a negative code;
+ *     ibm_last_error() gives a message for the last failing call.
+ *   - Host field arrays use the reference layout exactly: Fortran order
+ *     (i fastest) with one ghost layer, shape (0:itot+1, 0:jtot+1, 0:ktot+1),
+ *     i.e. (itot+2)*(jtot+2)*(ktot+2) doubles (mod_common, common.f90:4-8).
+ *   - All state lives on the GPU between calls; set/get copy it.
+ *   - One host thread per context; all work is ordered on the context stream.
+ *   - No MPI: the 2-D pencil decomposition of the reference collapses to one
+ *     rank with dims=(1,1); halos become periodic index wrap in x and y.
+ */
+#ifndef IBM_RK3_H
+#define IBM_RK3_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IBM_ABI_VERSION 1
+
+/* status codes */
+#define IBM_OK                 0
+#define IBM_E_INVALID        (-1)  /* bad argument or size                        */
+#define IBM_E_CUDA           (-2)  /* CUDA runtime error                          */
+#define IBM_E_NOMEM          (-3)  /* device allocation failed                    */
+#define IBM_E_CONTACT_OVERFLOW (-4)/* a particle exceeded nqmax contacts          */
+#define IBM_E_NOT_CONVERGED  (-5)  /* bounded iteration gave up                   */
+#define IBM_E_DIVERGENCE     (-6)  /* chkdiv total divergence above 1e-3          */
+#define IBM_E_STATE          (-7)  /* call out of order (e.g. no fields set yet)  */
+
+/* boundary condition types for the z walls (param.f90:33-34, bound.f90:17-65) */
+#define IBM_BC_NOSLIP   0
+#define IBM_BC_FREESLIP 1
+
+/* arithmetic forms of the step */
+#define IBM_MODE_PLAIN_FP64    0   /* drop-in: FP64 everywhere                    */
+#define IBM_MODE_MIXED         1   /* FP32 bulk passes, FP64 where required       */
+#define IBM_MODE_MIXED_LEARNED 2   /* MIXED + learned forcing correction          */
+
+/*
+ * Run parameters: mod_gridsize (gridsize.f90:6-26), the &parameters namelist
+ * (param.f90:66-86) and the Lagrangian force-point table read by coordsfp
+ * (coordsfp.f90:21-29).  Derived constants (init.f90:74-243) are computed
+ * inside ibm_create exactly as derived_parameters does.
+ */
+typedef struct ibm_params {
+  int    itot, jtot, ktot;     /* grid cells                                   */
+  double lx, ly, lz;           /* domain size                                  */
+  double visc;                 /* kinematic viscosity                          */
+  double radius;               /* sphere radius                                */
+  double ratiorho;             /* particle/fluid density ratio                 */
+  int    bc_top, bc_bot;       /* IBM_BC_*                                     */
+  int    particle_rotation;    /* 0/1 (param.f90:52)                           */
+  int    np;                   /* number of spheres (gridsize.f90 np)          */
+  int    nl;                   /* Lagrangian points per sphere (must equal the
+                                  value derived_parameters computes, main.f90:118-132) */
+  const double *thetarc;       /* [nl] polar angle of each point               */
+  const double *phirc;         /* [nl] azimuth of each point                   */
+  double radfp;                /* radius of the force-point shell              */
+  int    nb_copies;            /* 9: single-rank reference collision loop over the
+                                  self-neighbour copies nb=0..8 (intgr_nwtn_eulr.f90:358);
+                                  1: only nb=0                                 */
+  int    mode;                 /* IBM_MODE_*                                   */
+} ibm_params;
+
+/*
+ * Particle state, structure of arrays, host pointers.  Mirrors the reference
+ * derived type `particle` (common.f90:35-71) plus the RK accumulators `rkp`
+ * (common.f90:97-105).  Per-particle arrays have np entries; contact arrays
+ * have np*nqmax entries (particle-major: [p*nqmax + q]); nb has np*9 entries
+ * ([p*9 + nb], the neighbour flags ap(p)%nb(0:8)); rkp has np*19 entries in
+ * the field order of particle_sumrk.  nqmax = min(np+2, 15) (param.f90:100).
+ * Lagrangian arrays (np*nl, [p*nl + l]) are optional on set (may be NULL:
+ * they are then regenerated from the centres as coordsfp does).
+ */
+typedef struct ibm_particles {
+  double *x, *y, *z, *theta, *phi;
+  double *u, *v, *w, *omx, *omy, *omz, *omtheta;
+  double *intu, *intv, *intw, *intomx, *intomy, *intomz;
+  double *colfx, *colfy, *colfz, *coltx, *colty, *coltz;
+  double *fxltot, *fyltot, *fzltot, *torqxltot, *torqyltot, *torqzltot, *torqtheta;
+  int    *qmax;                /* [np]                                         */
+  int    *firstc;              /* [np*nqmax] partner ids (np+1, np+2 = walls)  */
+  double *cdx, *cdy, *cdz, *cdxt, *cdyt, *cdzt, *cdut, *cdvt, *cdwt, *cpsi; /* [np*nqmax] */
+  int    *nb;                  /* [np*9]                                       */
+  int    *mslv;                /* [np] master id (= particle id 1..np)         */
+  double *rkp;                 /* [np*19]                                      */
+  double *xfp, *yfp, *zfp, *ul, *vl, *wl, *fxl, *fyl, *fzl; /* [np*nl]         */
+} ibm_particles;
+
+typedef struct ibm_ctx ibm_ctx;
+
+/* --- context ------------------------------------------------------------ */
+
+/* Creates a context on the current CUDA device and computes the derived
+ * parameters (init.f90:74-243) and the solver tables (initsolver,
+ * initsolver.f90:10-66).  Replaces the set-up part of program interpt
+ * (main.f90:95-195) for one rank.  Returns NULL on failure (see
+ * ibm_last_error(NULL)). */
+ibm_ctx *ibm_create(const ibm_params *params);
+int      ibm_destroy(ibm_ctx *ctx);
+const char *ibm_last_error(const ibm_ctx *ctx);
+int      ibm_abi_version(void);
+/* nqmax and nl as used by the context (param.f90:100, init.f90:129). */
+int      ibm_sizes(const ibm_ctx *ctx, int *nqmax, int *nl, int *ncells);
+
+/* --- state transfer ------------------------------------------------------ */
+
+/* Fields u,v,w,p (unew..pnew) and the RK right-hand side kept between stages
+ * (durkold.., main.f90:49), reference layout (0:i1,0:j1,0:k1).  Any of durk,
+ * dvrk, dwrk may be NULL (taken as zero, as main.f90:218-220 does). */
+int ibm_set_fields(ibm_ctx *ctx, const double *u, const double *v, const double *w,
+                   const double *p, const double *durk, const double *dvrk,
+                   const double *dwrk);
+int ibm_get_fields(ibm_ctx *ctx, double *u, double *v, double *w, double *p,
+                   double *durk, double *dvrk, double *dwrk);
+/* Forced intermediate velocity dudt/dvdt/dwdt after the IBM loop (the input
+ * of fillps, main.f90:356-357). */
+int ibm_get_intermediate(ibm_ctx *ctx, double *dudt, double *dvdt, double *dwdt);
+
+int ibm_set_particles(ibm_ctx *ctx, const ibm_particles *ps);
+int ibm_get_particles(ibm_ctx *ctx, ibm_particles *ps);
+
+/* coordsfp (coordsfp.f90:10-124) followed by intgr_over_sphere(1..3)
+ * (main.f90:202-206): Lagrangian points, dVlagr/dVeul and the initial
+ * sphere integrals.  vol_calc (may be NULL) receives the type-1 volume of
+ * particle 1 (intgr_over_sphere.f90:607-622). */
+int ibm_init_particles(ibm_ctx *ctx, double *vol_calc);
+
+/* --- one reference subroutine per call ---------------------------------- */
+
+/* rk1/rk2/rk3 (rk3.f90:13-329) incl. momxp..momzad (mom.f90:8-231):
+ * predictor dudt and the stored RHS.  rkiter in 1..3. */
+int ibm_rk_predict(ibm_ctx *ctx, int rkiter, double dt);
+
+/* IBM block of the driver (main.f90:286-338): dudtf=dudt, then for
+ * ibmiter=0..nl_iter-1: eulr2lagr, complagrforces/updtlagrforces,
+ * lagr2eulr, updtintermediatevel; dudt=dudtf.  nl_iter = 3 in the reference. */
+int ibm_forcing_loop(ibm_ctx *ctx, double dt, int nl_iter);
+
+/* bounduvw(dudt), fillps, solver2d, boundp, correc, bounduvw(unew),
+ * pnew+=p, boundp(pnew)  (main.f90:356-372). */
+int ibm_project(ibm_ctx *ctx, int rkiter, double dt);
+
+/* intgr_nwtn_eulr (intgr_nwtn_eulr.f90:12-1514) on one rank. */
+int ibm_newton_euler(ibm_ctx *ctx, int rkiter, double dt);
+
+/* One full RK3 time step: rkiter=1..3 of the above (main.f90:268-413). */
+int ibm_rk3_step(ibm_ctx *ctx, double dt);
+/* nsteps consecutive RK3 steps with a fixed dt. */
+int ibm_run(ibm_ctx *ctx, double dt, int nsteps);
+
+/* --- diagnostics ----------------------------------------------------------- */
+
+/* chkdiv (chkdiv.f90:7-61): total and max |div| of (unew,vnew,wnew) and the
+ * 1-based (i,j,k) of the maximum.  Returns IBM_E_DIVERGENCE when tot > 1e-3
+ * (the reference aborts there) after filling the outputs. */
+int ibm_chkdiv(ibm_ctx *ctx, double *divtot, double *divmax, int ijk[3]);
+/* chkdt (chkdt.f90:6-273): stability limit dtmax. */
+int ibm_chkdt(ibm_ctx *ctx, double *dtmax);
+/* Lagrangian no-slip residual |U_l - u~_l| after the last forcing pass:
+ * max and rms over all points. */
+int ibm_slip_residual(ibm_ctx *ctx, double *maxres, double *rmsres);
+/* wallshearnew/wallshearold (rk3.f90:88-103) and the IBM mean-force
+ * diagnostics of updtintermediatevel (forcing.f90:445-463) of the last pass. */
+int ibm_diagnostics(ibm_ctx *ctx, double *wallshearnew, double *wallshearold,
+                    double forcetot[3]);
+
+/* --- streams and timing ------------------------------------------------------ */
+
+/* Runs all further work of the context on the given cudaStream_t (NULL:
+ * back to a private stream).  Lets a host program time the library with
+ * its own CUDA events on the launching stream. */
+int ibm_set_stream(ibm_ctx *ctx, void *cuda_stream);
+/* ibm_rk3_step with CUDA events around the four phases (see
+ * ibm_phase_times); synchronises once per substep. */
+int ibm_timed_step(ibm_ctx *ctx, double dt);
+
+/* Milliseconds of the last ibm_rk3_step/ibm_run per phase (fluid predictor,
+ * IBM loop, projection, Newton-Euler), measured with CUDA events on the
+ * context stream, like the per-phase MPI_WTIME report (main.f90:396-410).
+ * ms must hold 4 doubles. */
+int ibm_phase_times(ibm_ctx *ctx, double ms[4]);
+/* Number of kernels the library launched since the context was created. */
+long long ibm_launch_count(const ibm_ctx *ctx);
+/* Device synchronisation of the context stream. */
+int ibm_sync(ibm_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IBM_RK3_H */

@@ -1,0 +1,384 @@
+// fluid_kernels.cu -- momentum predictor, velocity correction, boundary
+// conditions, layout conversion and the chkdiv/chkdt reductions.
+//
+// One thread per interior cell; x/y neighbours by periodic wrap, z ghosts
+// stored.  All arithmetic follows the reference expression order; FP64
+// fused multiply-add contraction is allowed (differences at 1 ulp level).
+#include "kernels.cuh"
+
+namespace ibmk {
+
+// ---------------------------------------------------------------------------
+// Momentum predictor: rk1/rk2/rk3 (rk3.f90:13-329) fused with momxp..momzad
+// (mom.f90:8-231).  STAGE 1: dudt = u + f1*gradp; dudt += f1*RHS; rhs_old=RHS
+// STAGE 2/3: dudt = u + f1*gradp; dudt += (f2*RHS - f3*rhs_old); stage 2
+// stores rhs_old = RHS.  The output goes straight into the forcing buffer
+// (dudtf == dudt on entry of the IBM loop, main.f90:288-306).
+// ---------------------------------------------------------------------------
+template <typename T, int STAGE>
+__global__ void __launch_bounds__(256) k_predict(Geo g, const T *__restrict__ u, const T *__restrict__ v,
+                                                 const T *__restrict__ w, const T *__restrict__ p,
+                                                 T *__restrict__ ru, T *__restrict__ rv, T *__restrict__ rw,
+                                                 T *__restrict__ fu, T *__restrict__ fv, T *__restrict__ fw,
+                                                 T f1, T f2, T f3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;
+  if (i >= g.I || j >= g.J) return;
+  const int ip = i + 1 == g.I ? 0 : i + 1, im = i == 0 ? g.I - 1 : i - 1;
+  const int jp = j + 1 == g.J ? 0 : j + 1, jm = j == 0 ? g.J - 1 : j - 1;
+  const long PL = g.plane;
+  const long c = fidx(g, i, j, k);
+  const long rj = (long)k * g.J;  // row base helpers
+  auto at = [&](int ii, int jj, int kk) -> long { return ((long)kk * g.J + jj) * g.I + ii; };
+  (void)rj;
+  const T dxi = (T)g.dxi, dyi = (T)g.dyi, dzi = (T)g.dzi, visc = (T)g.visc;
+  const T q = (T)0.25;
+  // u-neighbourhood
+  const T U0 = u[c], Uip = u[at(ip, j, k)], Uim = u[at(im, j, k)], Ujp = u[at(i, jp, k)], Ujm = u[at(i, jm, k)];
+  const T Ukp = u[c + PL], Ukm = u[c - PL];
+  const T V0 = v[c], Vip = v[at(ip, j, k)], Vim = v[at(im, j, k)], Vjp = v[at(i, jp, k)], Vjm = v[at(i, jm, k)];
+  const T Vkp = v[c + PL], Vkm = v[c - PL];
+  const T W0 = w[c], Wip = w[at(ip, j, k)], Wim = w[at(im, j, k)], Wjp = w[at(i, jp, k)], Wjm = w[at(i, jm, k)];
+  const T Wkp = w[c + PL], Wkm = w[c - PL];
+  // diagonal neighbours
+  const T Vipjm = v[at(ip, jm, k)], Wipkm = w[at(ip, j, k - 1)];
+  const T Uimjp = u[at(im, jp, k)], Wjpkm = w[at(i, jp, k - 1)];
+  const T Uimkp = u[at(im, j, k + 1)], Vjmkp = v[at(i, jm, k + 1)];
+  // momxad (mom.f90:21-50)
+  T ru_new;
+  {
+    const T uuip = q * (Uip + U0) * (Uip + U0);
+    const T uuim = q * (Uim + U0) * (Uim + U0);
+    const T uvjp = q * (Ujp + U0) * (Vip + V0);
+    const T uvjm = q * (Ujm + U0) * (Vipjm + Vjm);
+    const T uwkp = q * (Ukp + U0) * (Wip + W0);
+    const T uwkm = q * (Ukm + U0) * (Wipkm + Wkm);
+    const T dudxp = (Uip - U0) * dxi, dudxm = (U0 - Uim) * dxi;
+    const T dudyp = (Ujp - U0) * dyi, dudym = (U0 - Ujm) * dyi;
+    const T dudzp = (Ukp - U0) * dzi, dudzm = (U0 - Ukm) * dzi;
+    ru_new = dxi * (-uuip + uuim) + visc * (dudxp - dudxm) * dxi + dyi * (-uvjp + uvjm) +
+             visc * (dudyp - dudym) * dyi + dzi * (-uwkp + uwkm) + visc * (dudzp - dudzm) * dzi;
+  }
+  T rv_new;
+  {  // momyad (mom.f90:94-123)
+    const T uvip = q * (U0 + Ujp) * (V0 + Vip);
+    const T uvim = q * (Uim + Uimjp) * (V0 + Vim);
+    const T vvjp = q * (V0 + Vjp) * (V0 + Vjp);
+    const T vvjm = q * (V0 + Vjm) * (V0 + Vjm);
+    const T wvkp = q * (W0 + Wjp) * (Vkp + V0);
+    const T wvkm = q * (Wkm + Wjpkm) * (Vkm + V0);
+    const T dvdxp = (Vip - V0) * dxi, dvdxm = (V0 - Vim) * dxi;
+    const T dvdyp = (Vjp - V0) * dyi, dvdym = (V0 - Vjm) * dyi;
+    const T dvdzp = (Vkp - V0) * dzi, dvdzm = (V0 - Vkm) * dzi;
+    rv_new = dxi * (-uvip + uvim) + visc * (dvdxp - dvdxm) * dxi + dyi * (-vvjp + vvjm) +
+             visc * (dvdyp - dvdym) * dyi + dzi * (-wvkp + wvkm) + visc * (dvdzp - dvdzm) * dzi;
+  }
+  T rw_new;
+  {  // momzad (mom.f90:170-199)
+    const T uwip = q * (W0 + Wip) * (U0 + Ukp);
+    const T uwim = q * (W0 + Wim) * (Uim + Uimkp);
+    const T vwjp = q * (W0 + Wjp) * (V0 + Vkp);
+    const T vwjm = q * (W0 + Wjm) * (Vjm + Vjmkp);
+    const T wwkp = q * (W0 + Wkp) * (W0 + Wkp);
+    const T wwkm = q * (W0 + Wkm) * (W0 + Wkm);
+    const T dwdxp = (Wip - W0) * dxi, dwdxm = (W0 - Wim) * dxi;
+    const T dwdyp = (Wjp - W0) * dyi, dwdym = (W0 - Wjm) * dyi;
+    const T dwdzp = (Wkp - W0) * dzi, dwdzm = (W0 - Wkm) * dzi;
+    rw_new = dxi * (-uwip + uwim) + visc * (dwdxp - dwdxm) * dxi + dyi * (-vwjp + vwjm) +
+             visc * (dwdyp - dwdym) * dyi + dzi * (-wwkp + wwkm) + visc * (dwdzp - dwdzm) * dzi;
+  }
+  // pressure gradient (momxp/momyp/momzp)
+  const T P0 = p[c];
+  const T gx = -dxi * (p[at(ip, j, k)] - P0);
+  const T gy = -dyi * (p[at(i, jp, k)] - P0);
+  const T gz = -dzi * (p[c + PL] - P0);
+  T du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
+  if (STAGE == 1) {
+    du = du + f1 * ru_new;
+    dv = dv + f1 * rv_new;
+    dw = dw + f1 * rw_new;
+  } else {
+    du = du + (f2 * ru_new - f3 * ru[c]);
+    dv = dv + (f2 * rv_new - f3 * rv[c]);
+    dw = dw + (f2 * rw_new - f3 * rw[c]);
+  }
+  fu[c] = du;
+  fv[c] = dv;
+  fw[c] = dw;
+  if (STAGE != 3) {
+    ru[c] = ru_new;
+    rv[c] = rv_new;
+    rw[c] = rw_new;
+  }
+}
+
+template <typename T>
+void launch_predict(cudaStream_t s, const Geo &g, int stage, const T *u, const T *v, const T *w, const T *p,
+                    T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3) {
+  dim3 blk(64, 4, 1);
+  dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
+  if (stage == 1)
+    k_predict<T, 1><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+  else if (stage == 2)
+    k_predict<T, 2><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+  else
+    k_predict<T, 3><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+}
+template void launch_predict<double>(cudaStream_t, const Geo &, int, const double *, const double *,
+                                     const double *, const double *, double *, double *, double *, double *,
+                                     double *, double *, double, double, double);
+template void launch_predict<float>(cudaStream_t, const Geo &, int, const float *, const float *, const float *,
+                                    const float *, float *, float *, float *, float *, float *, float *, double,
+                                    double, double);
+
+// ---------------------------------------------------------------------------
+// correc (correc.f90:11-42) + pnew += p (main.f90:369-371) + bounduvw(unew)
+// and boundp(pnew) z-ghosts (bound.f90:11-107).  phi holds the Poisson
+// solution on planes 1..K; its Neumann ghost p(k1)=p(kmax) is implied.
+// ---------------------------------------------------------------------------
+template <typename T, typename TP>
+__global__ void __launch_bounds__(256) k_correc(Geo g, const T *__restrict__ fu, const T *__restrict__ fv,
+                                                const T *__restrict__ fw, const T *__restrict__ phi,
+                                                T *__restrict__ u, T *__restrict__ v, T *__restrict__ w,
+                                                TP *__restrict__ pn, double fi_, double fj_, double fk_) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;
+  if (i >= g.I || j >= g.J) return;
+  const int ip = i + 1 == g.I ? 0 : i + 1;
+  const int jp = j + 1 == g.J ? 0 : j + 1;
+  const long PL = g.plane;
+  const long c = fidx(g, i, j, k);
+  const T fi = (T)fi_, fj = (T)fj_, fk = (T)fk_;
+  const T P0 = phi[c];
+  const T Pip = phi[fidx(g, ip, j, k)];
+  const T Pjp = phi[fidx(g, i, jp, k)];
+  const T Pkp = (k == g.K) ? P0 : phi[c + PL];
+  const T un = fu[c] - fi * (Pip - P0);
+  const T vn = fv[c] - fj * (Pjp - P0);
+  const T wn = (k == g.K) ? (T)0 : fw[c] - fk * (Pkp - P0);
+  u[c] = un;
+  v[c] = vn;
+  w[c] = wn;
+  const TP pnn = pn[c] + (TP)P0;
+  pn[c] = pnn;
+  if (k == g.K) {
+    const T sg = g.bc_top == IBM_BC_NOSLIP ? (T)-1 : (T)1;
+    u[c + PL] = sg * un;
+    v[c + PL] = sg * vn;
+    pn[c + PL] = pnn;
+  }
+  if (k == 1) {
+    const T sg = g.bc_bot == IBM_BC_NOSLIP ? (T)-1 : (T)1;
+    u[c - PL] = sg * un;
+    v[c - PL] = sg * vn;
+    w[c - PL] = (T)0;
+    pn[c - PL] = pnn;
+  }
+}
+
+template <typename T, typename TP>
+void launch_correc(cudaStream_t s, const Geo &g, const T *fu, const T *fv, const T *fw, const T *phi, T *u, T *v,
+                   T *w, TP *pn, double fi, double fj, double fk) {
+  dim3 blk(64, 4, 1);
+  dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
+  k_correc<T, TP><<<grd, blk, 0, s>>>(g, fu, fv, fw, phi, u, v, w, pn, fi, fj, fk);
+}
+template void launch_correc<double, double>(cudaStream_t, const Geo &, const double *, const double *,
+                                            const double *, const double *, double *, double *, double *,
+                                            double *, double, double, double);
+template void launch_correc<float, double>(cudaStream_t, const Geo &, const float *, const float *,
+                                           const float *, const float *, float *, float *, float *, double *,
+                                           double, double, double);
+
+// ---------------------------------------------------------------------------
+// Layout conversion between the reference host layout (0:i1,0:j1,0:k1) and
+// the device layout.  to_dev: dev(i,j,k) = ref(i+1,j+1,k).  to_ref fills the
+// x/y ghosts with the periodic values, as bounduvw/boundp leave them.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_ref_to_dev(Geo g, const double *__restrict__ ref, T *__restrict__ dev) {
+  const long n = g.nfield;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.I);
+    const int j = (int)((t / g.I) % g.J);
+    const int k = (int)(t / g.plane);
+    const long r = (long)(i + 1) + (long)(g.I + 2) * ((j + 1) + (long)(g.J + 2) * k);
+    dev[t] = (T)ref[r];
+  }
+}
+template <typename T>
+__global__ void k_dev_to_ref(Geo g, const T *__restrict__ dev, double *__restrict__ ref) {
+  const long n = (long)(g.I + 2) * (g.J + 2) * (g.K + 2);
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % (g.I + 2));
+    const int j = (int)((t / (g.I + 2)) % (g.J + 2));
+    const int k = (int)(t / ((long)(g.I + 2) * (g.J + 2)));
+    const int id = wrapm(i - 1, g.I), jd = wrapm(j - 1, g.J);
+    ref[t] = (double)dev[fidx(g, id, jd, k)];
+  }
+}
+template <typename T>
+void launch_ref_to_dev(cudaStream_t s, const Geo &g, const double *ref, T *dev) {
+  k_ref_to_dev<T><<<1216, 256, 0, s>>>(g, ref, dev);
+}
+template <typename T>
+void launch_dev_to_ref(cudaStream_t s, const Geo &g, const T *dev, double *ref) {
+  k_dev_to_ref<T><<<1216, 256, 0, s>>>(g, dev, ref);
+}
+template void launch_ref_to_dev<double>(cudaStream_t, const Geo &, const double *, double *);
+template void launch_ref_to_dev<float>(cudaStream_t, const Geo &, const double *, float *);
+template void launch_dev_to_ref<double>(cudaStream_t, const Geo &, const double *, double *);
+template void launch_dev_to_ref<float>(cudaStream_t, const Geo &, const float *, double *);
+
+// ---------------------------------------------------------------------------
+// chkdiv (chkdiv.f90:7-61): block partials of sum(div) and (max|div|, first
+// linear index), combined in a fixed order by a single block.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_div_partial(Geo g, const double *__restrict__ u,
+                                                     const double *__restrict__ v, const double *__restrict__ w,
+                                                     double *__restrict__ psum, double *__restrict__ pmax,
+                                                     long long *__restrict__ ploc) {
+  const long n = (long)g.I * g.J * g.K;
+  double s = 0., m = -1.;
+  long long loc = -1;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.I), j = (int)((t / g.I) % g.J), k = (int)(t / g.plane) + 1;
+    const long c = fidx(g, i, j, k);
+    const double div = (w[c] - w[c - g.plane]) * g.dzi + (v[c] - v[fidx(g, i, wrapm(j - 1, g.J), k)]) * g.dyi +
+                       (u[c] - u[fidx(g, wrapm(i - 1, g.I), j, k)]) * g.dxi;
+    s += div;
+    const double a = fabs(div);
+    if (a > m) { m = a; loc = t; }
+  }
+  __shared__ double ss[256], sm[256];
+  __shared__ long long sl[256];
+  ss[threadIdx.x] = s; sm[threadIdx.x] = m; sl[threadIdx.x] = loc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      ss[threadIdx.x] += ss[threadIdx.x + o];
+      const double m2 = sm[threadIdx.x + o];
+      const long long l2 = sl[threadIdx.x + o];
+      if (m2 > sm[threadIdx.x] || (m2 == sm[threadIdx.x] && l2 >= 0 && (sl[threadIdx.x] < 0 || l2 < sl[threadIdx.x]))) {
+        sm[threadIdx.x] = m2; sl[threadIdx.x] = l2;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { psum[blockIdx.x] = ss[0]; pmax[blockIdx.x] = sm[0]; ploc[blockIdx.x] = sl[0]; }
+}
+__global__ void k_div_final(int nb, const double *psum, const double *pmax, const long long *ploc, double *out) {
+  if (threadIdx.x != 0) return;
+  double s = 0., m = -1.;
+  long long l = -1;
+  for (int b = 0; b < nb; ++b) {
+    s += psum[b];
+    if (pmax[b] > m || (pmax[b] == m && ploc[b] >= 0 && (l < 0 || ploc[b] < l))) { m = pmax[b]; l = ploc[b]; }
+  }
+  out[0] = s; out[1] = m; out[2] = (double)l;
+}
+void launch_chkdiv(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w,
+                   double *scratch, double *out) {
+  const int nb = 608;
+  double *psum = scratch, *pmax = scratch + nb;
+  long long *ploc = (long long *)(scratch + 2 * nb);
+  k_div_partial<<<nb, 256, 0, s>>>(g, u, v, w, psum, pmax, ploc);
+  k_div_final<<<1, 32, 0, s>>>(nb, psum, pmax, ploc, out);
+}
+
+// chkdt (chkdt.f90:6-273): min over the three staggered components.
+__global__ void __launch_bounds__(256) k_dt_partial(Geo g, const double *__restrict__ u,
+                                                    const double *__restrict__ v, const double *__restrict__ w,
+                                                    double *__restrict__ pmin) {
+  const long n = (long)g.I * g.J * g.K;
+  double m = 899999.;
+  const double dxi = g.dxi, dyi = g.dyi, dzi = g.dzi;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.I), j = (int)((t / g.I) % g.J), k = (int)(t / g.plane) + 1;
+    const int ip = wrapm(i + 1, g.I), im = wrapm(i - 1, g.I), jp = wrapm(j + 1, g.J), jm = wrapm(j - 1, g.J);
+    auto U = [&](int a, int b, int c) { return u[fidx(g, a, b, c)]; };
+    auto V = [&](int a, int b, int c) { return v[fidx(g, a, b, c)]; };
+    auto W = [&](int a, int b, int c) { return w[fidx(g, a, b, c)]; };
+    const double dxi2 = dxi * dxi + dyi * dyi + dzi * dzi;
+    const double dt1 = 1.65 / (4. * g.visc * dxi2);
+    for (int comp = 0; comp < 3; ++comp) {
+      double u2, v2, w2, tt;
+      if (comp == 0) {
+        u2 = U(i, j, k) * U(i, j, k);
+        tt = 0.25 * (V(i, j, k) + V(i, jm, k) + V(ip, j, k) + V(ip, jm, k)); v2 = tt * tt;
+        tt = 0.25 * (W(i, j, k) + W(i, j, k - 1) + W(ip, j, k) + W(ip, j, k - 1)); w2 = tt * tt;
+      } else if (comp == 1) {
+        tt = 0.25 * (U(i, j, k) + U(i, jp, k) + U(im, jp, k) + U(im, j, k)); u2 = tt * tt;
+        v2 = V(i, j, k) * V(i, j, k);
+        tt = 0.25 * (W(i, j, k) + W(i, jp, k) + W(i, jp, k - 1) + W(i, j, k - 1)); w2 = tt * tt;
+      } else {
+        tt = 0.25 * (U(i, j, k) + U(im, j, k) + U(im, j, k + 1) + U(i, j, k + 1)); u2 = tt * tt;
+        tt = 0.25 * (V(i, j, k) + V(i, jm, k) + V(i, jm, k + 1) + V(i, j, k + 1)); v2 = tt * tt;
+        w2 = W(i, j, k) * W(i, j, k);
+      }
+      const double velo = sqrt(u2 + v2 + w2);
+      double dt2;
+      if (fabs(velo) > 1.e-12) dt2 = sqrt(3.) / (sqrt(u2) * dxi + sqrt(v2) * dyi + sqrt(w2) * dzi);
+      else dt2 = 99999.;
+      m = fmin(m, fmin(dt1, dt2));
+    }
+  }
+  __shared__ double sm[256];
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sm[threadIdx.x] = fmin(sm[threadIdx.x], sm[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) pmin[blockIdx.x] = sm[0];
+}
+__global__ void k_min_final(int nb, const double *p, double *out) {
+  if (threadIdx.x != 0) return;
+  double m = 899999.;
+  for (int b = 0; b < nb; ++b) m = fmin(m, p[b]);
+  out[0] = m;
+}
+void launch_chkdt(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w,
+                  double *scratch, double *out) {
+  const int nb = 608;
+  k_dt_partial<<<nb, 256, 0, s>>>(g, u, v, w, scratch);
+  k_min_final<<<1, 32, 0, s>>>(nb, scratch, out);
+}
+
+// wall shear of rk1/rk2/rk3 (rk3.f90:80-103): sum over the wall planes.
+__global__ void k_wallshear(Geo g, const double *__restrict__ v, double *out) {
+  __shared__ double sm[512];
+  double s = 0.;
+  const long PL = g.plane;
+  for (long t = threadIdx.x; t < PL; t += blockDim.x) {
+    const long top = (long)g.K * PL + t, bot = PL + t;
+    s = s + g.visc * (v[top + PL] - v[top]) * g.dzi * (1. / g.dxi) * (1. / g.dyi) -
+        g.visc * (v[bot] - v[bot - PL]) * g.dzi * (1. / g.dxi) * (1. / g.dyi);
+  }
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sm[0];
+}
+void launch_wallshear(cudaStream_t s, const Geo &g, const double *v, double *out) {
+  k_wallshear<<<1, 512, 0, s>>>(g, v, out);
+}
+
+// convert / copy helpers for the mixed form
+__global__ void k_d2f(long n, const double *__restrict__ a, float *__restrict__ b) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    b[t] = (float)a[t];
+}
+__global__ void k_f2d(long n, const float *__restrict__ a, double *__restrict__ b) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    b[t] = (double)a[t];
+}
+void launch_d2f(cudaStream_t s, long n, const double *a, float *b) { k_d2f<<<1216, 256, 0, s>>>(n, a, b); }
+void launch_f2d(cudaStream_t s, long n, const float *a, double *b) { k_f2d<<<1216, 256, 0, s>>>(n, a, b); }
+
+}  // namespace ibmk

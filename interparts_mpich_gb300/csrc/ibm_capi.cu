@@ -1,0 +1,794 @@
+// ibm_capi.cu -- the C ABI of include/ibm_rk3.h: context set-up (derived
+// parameters, solver tables), state transfer and the per-subroutine entry
+// points that sequence the kernels on the context stream.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+using namespace ibmk;
+
+namespace {
+thread_local std::string g_create_error;
+const double PI = 3.141592653589793238462643383279502884;
+
+bool make_plan(int n, FftPlan &pl) {
+  pl.nst = 0;
+  while (n % 4 == 0 && n > 1) { pl.rad[pl.nst++] = 4; n /= 4; if (pl.nst >= 16) return false; }
+  while (n % 2 == 0 && n > 1) { pl.rad[pl.nst++] = 2; n /= 2; if (pl.nst >= 16) return false; }
+  while (n % 3 == 0 && n > 1) { pl.rad[pl.nst++] = 3; n /= 3; if (pl.nst >= 16) return false; }
+  return n == 1;
+}
+}  // namespace
+
+struct ibm_ctx {
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  ibm_params prm{};
+  std::vector<double> thetarc, phirc;
+  Geo g{};
+  PartGeo pg{};
+  int mode = IBM_MODE_PLAIN_FP64;
+  int nq = 0;
+  // derived (init.f90:74-243)
+  double offset = 0, volp = 0, mominert = 0, rkab[3] = {0, 0, 0};
+  // FP64 fields
+  double *u = nullptr, *v = nullptr, *w = nullptr, *p = nullptr;
+  double *ru = nullptr, *rv = nullptr, *rw = nullptr;
+  double *fu = nullptr, *fv = nullptr, *fw = nullptr, *phi = nullptr;
+  void *spec = nullptr;
+  double *zt = nullptr;
+  void *twM = nullptr, *twN = nullptr, *twJ = nullptr;
+  FftPlan plx{}, ply{};
+  // particles
+  IbmBuffers ib{};
+  PartBuffers pb{};
+  // misc
+  double *scratch = nullptr;   // reduction partials
+  double *dout = nullptr;      // small device results
+  double *href = nullptr;      // device staging buffer in the reference layout
+  double *hpin = nullptr;      // pinned host results
+  bool have_fields = false, have_particles = false, particles_ready = false;
+  long long launches = 0;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double phase_ms[4] = {0, 0, 0, 0};
+  double wall_raw[3] = {0, 0, 0};
+  double dt_last = 0;
+};
+
+namespace {
+
+int set_err(ibm_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+int cuda_err(ibm_ctx *c, cudaError_t e, const char *where) {
+  if (e == cudaSuccess) return IBM_OK;
+  return set_err(c, e == cudaErrorMemoryAllocation ? IBM_E_NOMEM : IBM_E_CUDA,
+                 std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                          \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_err(c, e_, #call); \
+  } while (0)
+#define LAUNCHED(n)                                                     \
+  do {                                                                  \
+    c->launches += (n);                                                 \
+    cudaError_t e_ = cudaGetLastError();                                \
+    if (e_ != cudaSuccess) return cuda_err(c, e_, "kernel launch");     \
+  } while (0)
+
+template <typename T>
+int dalloc(ibm_ctx *c, T **ptr, size_t n) {
+  cudaError_t e = cudaMalloc((void **)ptr, n * sizeof(T) + 256);
+  if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc");
+  e = cudaMemsetAsync(*ptr, 0, n * sizeof(T) + 256, c->stream);
+  return cuda_err(c, e, "cudaMemset");
+}
+
+void derived(ibm_ctx *c) {
+  const ibm_params &P = c->prm;
+  Geo &g = c->g;
+  g.I = P.itot; g.J = P.jtot; g.K = P.ktot; g.MX = P.itot / 2 + 1;
+  g.plane = (long)g.I * g.J;
+  g.nfield = (long)(g.K + 2) * g.plane;
+  g.lx = P.lx; g.ly = P.ly; g.lz = P.lz;
+  g.dxi = P.itot / P.lx; g.dyi = P.jtot / P.ly; g.dzi = P.ktot / P.lz;
+  g.dx = 1. / g.dxi; g.dy = 1. / g.dyi; g.dz = 1. / g.dzi;
+  g.visc = P.visc;
+  g.bc_top = P.bc_top; g.bc_bot = P.bc_bot;
+  c->offset = (std::sqrt(3. * (1.5 * 1.5))) / g.dxi + 0.01 / g.dxi;
+  c->volp = (4. / 3.) * PI * std::pow(P.radius, 3.);
+  c->mominert = (2. / 5.) * c->volp * std::pow(P.radius, 2.);
+  c->rkab[0] = 32. / 60. + 0.;
+  c->rkab[1] = 25. / 60. + (-17. / 60.);
+  c->rkab[2] = 45. / 60. + (-25. / 60.);
+  c->nq = std::min(P.np + 2, 15);
+  PartGeo &pg = c->pg;
+  pg.np = P.np; pg.nl = P.nl; pg.nq = c->nq;
+  pg.nb_copies = P.nb_copies == 1 ? 1 : 9;
+  pg.rotation = P.particle_rotation;
+  pg.radius = P.radius; pg.radfp = P.radfp; pg.offset = c->offset;
+  // dVlagr of the outer shell and dVeul (coordsfp.f90:84-90)
+  pg.dVlagr = ((4. / 3.) * PI * std::pow(P.radfp + 0.5 / g.dxi, 3.) -
+               (4. / 3.) * PI * std::pow(P.radfp - 0.5 / g.dxi, 3.)) / (1. * P.nl);
+  pg.dVeul = 1. / (g.dxi * g.dyi * g.dzi);
+  pg.lx = g.lx; pg.ly = g.ly; pg.lz = g.lz;
+  pg.dxi = g.dxi; pg.dyi = g.dyi; pg.dzi = g.dzi; pg.dx = g.dx; pg.dy = g.dy; pg.dz = g.dz;
+  const double gacc = -9.81;  // param.f90:102-104
+  pg.gacc[0] = gacc * std::cos(PI / 2.);
+  pg.gacc[1] = gacc * std::cos(PI / 2.);
+  pg.gacc[2] = gacc * std::sin(PI / 2.);
+  for (int r = 0; r < 3; ++r) pg.rkab[r] = c->rkab[r];
+  pg.volp = c->volp; pg.ratiorho = P.ratiorho; pg.mominert = c->mominert;
+  // collision / lubrication constants (init.f90:137-241, param.f90:114-120)
+  const double Nstretch = 8, dt_estim = 0.05, en = 0.97, et = 0.10, muc = 0.;
+  const double meffn_ss = P.ratiorho * c->volp / 2., mefft_ss = 2. / 7. * meffn_ss;
+  const double meffn_sw = P.ratiorho * c->volp, mefft_sw = 2. / 7. * meffn_sw;
+  pg.kn_ss = (PI * PI + std::pow(std::fabs(std::log(en)), 2.)) * meffn_ss / std::pow(Nstretch * dt_estim, 2.);
+  pg.kt_ss = (PI * PI + std::pow(std::fabs(std::log(et)), 2.)) * mefft_ss / std::pow(Nstretch * dt_estim, 2.);
+  pg.etan_ss = -2. * (std::log(en)) * meffn_ss / (Nstretch * dt_estim);
+  pg.etat_ss = -2. * (std::log(et)) * mefft_ss / (Nstretch * dt_estim);
+  pg.muc_ss = muc;
+  pg.kn_sw = (PI * PI + std::pow(std::fabs(std::log(en)), 2.)) * meffn_sw / std::pow(Nstretch * dt_estim, 2.);
+  pg.kt_sw = (PI * PI + std::pow(std::fabs(std::log(et)), 2.)) * mefft_sw / std::pow(Nstretch * dt_estim, 2.);
+  pg.etan_sw = -2. * (std::log(en)) * meffn_sw / (Nstretch * dt_estim);
+  pg.etat_sw = -2. * (std::log(et)) * mefft_sw / (Nstretch * dt_estim);
+  pg.muc_sw = muc;
+  pg.coeff_f = 6. * PI * P.visc * P.radius;
+  const double eps_ini_pp = 0.025, eps_sat_pp = 0.001, eps_ini_pw = 0.075, eps_sat_pw = 0.001;
+  const double a11_ini_pp = -(1. / 4. * std::pow(eps_ini_pp, -1.)) + 9. / 40. * std::log(eps_ini_pp) +
+                            3. / 112. * eps_ini_pp * std::log(eps_ini_pp);
+  const double a11_sat_pp = -(1. / 4. * std::pow(eps_sat_pp, -1.)) + 9. / 40. * std::log(eps_sat_pp) +
+                            3. / 112. * eps_sat_pp * std::log(eps_sat_pp);
+  pg.a11a_ini_pp = a11_ini_pp - .995;
+  pg.a11b_ini_pp = -a11_ini_pp + .350;
+  pg.a11a_sat_pp = a11_sat_pp - .995;
+  pg.a11b_sat_pp = -a11_sat_pp + .350;
+  pg.a11_ini_pw = -(1. / eps_ini_pw) + 1. / 5. * std::log(eps_ini_pw) + 1. / 21. * eps_ini_pw * std::log(eps_ini_pw) - .9713;
+  pg.a11_sat_pw = -(1. / eps_sat_pw) + 1. / 5. * std::log(eps_sat_pw) + 1. / 21. * eps_sat_pw * std::log(eps_sat_pw) - .9713;
+  pg.I = g.I; pg.J = g.J; pg.K = g.K;
+}
+
+// twiddles and the Thomas pivots (initsolver.f90:10-66)
+int build_solver_tables(ibm_ctx *c) {
+  const Geo &g = c->g;
+  const int I = g.I, J = g.J, K = g.K, M = I / 2, MX = g.MX;
+  std::vector<double2> twM(M), twN(M + 1), twJ(J);
+  for (int t = 0; t < M; ++t) twM[t] = make_double2(std::cos(2. * PI * t / M), -std::sin(2. * PI * t / M));
+  for (int t = 0; t <= M; ++t) twN[t] = make_double2(std::cos(2. * PI * t / I), -std::sin(2. * PI * t / I));
+  for (int t = 0; t < J; ++t) twJ[t] = make_double2(std::cos(2. * PI * t / J), -std::sin(2. * PI * t / J));
+  int st;
+  if ((st = dalloc(c, (double2 **)&c->twM, M))) return st;
+  if ((st = dalloc(c, (double2 **)&c->twN, M + 1))) return st;
+  if ((st = dalloc(c, (double2 **)&c->twJ, J))) return st;
+  CK(cudaMemcpyAsync(c->twM, twM.data(), M * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->twN, twN.data(), (M + 1) * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->twJ, twJ.data(), J * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  // tridiagonal matrix with Neumann rows
+  std::vector<double> a(K + 1), b(K + 1), cc(K + 1);
+  for (int k = 1; k <= K; ++k) { a[k] = g.dzi * g.dzi; cc[k] = g.dzi * g.dzi; b[k] = -(a[k] + cc[k]); }
+  b[1] = b[1] + a[1]; b[K] = b[K] + cc[K]; a[1] = 0.; cc[K] = 0.;
+  // eigenvalues in the reference's expression order
+  std::vector<double> xrt(MX), yrt(J / 2 + 1);
+  xrt[0] = 0.;
+  for (int k = 1; k < MX; ++k) {
+    const double s = std::sin(double(2 * k) * PI / (2. * I));
+    xrt[k] = -4. * g.dxi * g.dxi * (s * s);
+  }
+  if (I % 2 == 0) xrt[M] = -4. * g.dxi * g.dxi;
+  yrt[0] = 0.;
+  for (int k = 1; k <= J / 2; ++k) {
+    const double s = std::sin(double(2 * k) * PI / (2. * J));
+    yrt[k] = -4. * g.dyi * g.dyi * (s * s);
+  }
+  if (J % 2 == 0) yrt[J / 2] = -4. * g.dyi * g.dyi;
+  const long zst = (long)(J / 2 + 1) * MX;
+  std::vector<double> z((size_t)zst * K);
+  for (int ky = 0; ky <= J / 2; ++ky)
+    for (int kx = 0; kx < MX; ++kx) {
+      const double xy = xrt[kx] + yrt[ky];
+      double zz = 1. / (b[1] + xy);
+      double d = cc[1] * zz;
+      z[(size_t)ky * MX + kx] = zz;
+      for (int k = 2; k <= K - 1; ++k) {
+        const double bb = b[k] + xy;
+        zz = 1. / (bb - a[k] * d);
+        d = cc[k] * zz;
+        z[(size_t)(k - 1) * zst + (size_t)ky * MX + kx] = zz;
+      }
+      const double bb = b[K] + xy;
+      z[(size_t)(K - 1) * zst + (size_t)ky * MX + kx] = bb - a[K] * d;
+    }
+  if ((st = dalloc(c, &c->zt, z.size()))) return st;
+  CK(cudaMemcpyAsync(c->zt, z.data(), z.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
+int alloc_all(ibm_ctx *c) {
+  const Geo &g = c->g;
+  const size_t nf = (size_t)g.nfield;
+  int st;
+  for (double **f : {&c->u, &c->v, &c->w, &c->p, &c->ru, &c->rv, &c->rw, &c->fu, &c->fv, &c->fw, &c->phi})
+    if ((st = dalloc(c, f, nf))) return st;
+  if ((st = dalloc(c, (double2 **)&c->spec, (size_t)g.K * g.J * g.MX))) return st;
+  if ((st = dalloc(c, &c->scratch, 4096))) return st;
+  if ((st = dalloc(c, &c->dout, 64))) return st;
+  CK(cudaMallocHost((void **)&c->hpin, 64 * sizeof(double)));
+  const int np = c->pg.np, nl = c->pg.nl, nq = c->nq;
+  if (np > 0) {
+    const size_t npl = (size_t)np * nl;
+    for (double **f : {&c->ib.xfp, &c->ib.yfp, &c->ib.zfp, &c->ib.ul, &c->ib.vl, &c->ib.wl, &c->ib.dudtl,
+                       &c->ib.dvdtl, &c->ib.dwdtl, &c->ib.fxl, &c->ib.fyl, &c->ib.fzl})
+      if ((st = dalloc(c, f, npl))) return st;
+    if ((st = dalloc(c, &c->ib.st, npl))) return st;
+    if ((st = dalloc(c, &c->ib.nla, np))) return st;
+    if ((st = dalloc(c, &c->pb.pf, (size_t)PF_N * np))) return st;
+    if ((st = dalloc(c, &c->pb.cf, (size_t)CF_N * np * nq))) return st;
+    if ((st = dalloc(c, &c->pb.qmax, np))) return st;
+    if ((st = dalloc(c, &c->pb.firstc, (size_t)np * nq))) return st;
+    if ((st = dalloc(c, &c->pb.ofirstc, (size_t)np * nq))) return st;
+    if ((st = dalloc(c, &c->pb.nb, (size_t)np * 9))) return st;
+    if ((st = dalloc(c, &c->pb.mslv, np))) return st;
+    if ((st = dalloc(c, &c->pb.rkp, (size_t)RK_N * np))) return st;
+    if ((st = dalloc(c, &c->pb.sincos, (size_t)4 * nl))) return st;
+    if ((st = dalloc(c, &c->pb.err, 4))) return st;
+    if ((st = dalloc(c, &c->pb.red, (size_t)4 * np))) return st;
+    if ((st = dalloc(c, &c->ib.diag, 8))) return st;
+    c->ib.pf = c->pb.pf;
+    c->ib.err = c->pb.err;
+    std::vector<double> sc((size_t)4 * nl);
+    for (int l = 0; l < nl; ++l) {
+      sc[l] = std::sin(c->thetarc[l]);
+      sc[nl + l] = std::cos(c->thetarc[l]);
+      sc[2 * nl + l] = std::sin(c->phirc[l]);
+      sc[3 * nl + l] = std::cos(c->phirc[l]);
+    }
+    CK(cudaMemcpyAsync(c->pb.sincos, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  return IBM_OK;
+}
+
+int check_flags(ibm_ctx *c) {
+  if (c->pg.np == 0) return IBM_OK;
+  int h[4];
+  CK(cudaMemcpyAsync(h, c->pb.err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (h[2]) return set_err(c, IBM_E_INVALID, "a Lagrangian point left the grid (non-finite or beyond the walls)");
+  if (h[1]) return set_err(c, IBM_E_CONTACT_OVERFLOW, "a particle exceeded nqmax contacts (param.f90:100)");
+  if (h[0]) return set_err(c, IBM_E_CONTACT_OVERFLOW, "more than 64 interaction candidates for one particle");
+  return IBM_OK;
+}
+
+int predict(ibm_ctx *c, int rkiter, double dt) {
+  const Geo &g = c->g;
+  launch_wallshear(c->stream, g, c->v, c->dout + 8 + (rkiter - 1));
+  LAUNCHED(1);
+  double f1, f2 = 0, f3 = 0;
+  if (rkiter == 1) f1 = dt * (32. / 60.);
+  else if (rkiter == 2) { f1 = dt * (8. / 60.); f2 = dt * (25. / 60.); f3 = dt * (17. / 60.); }
+  else { f1 = dt * (20. / 60.); f2 = dt * (45. / 60.); f3 = dt * (25. / 60.); }
+  launch_predict<double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv, c->fw, f1,
+                         f2, f3);
+  LAUNCHED(1);
+  return IBM_OK;
+}
+
+int forcing(ibm_ctx *c, double dt, int nl_iter) {
+  if (c->pg.np == 0 || nl_iter <= 0) return IBM_OK;
+  const Geo &g = c->g;
+  launch_ibm_stencil<double>(c->stream, g, c->pg, c->ib);
+  LAUNCHED(1);
+  for (int it = 0; it < nl_iter; ++it) {
+    launch_ibm_interp_force<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0 ? 1 : 0);
+    LAUNCHED(1);
+    if (it == 0) {  // dwdtf(:,:,k1) carries only S(F) (interp_spread.f90:267-269)
+      launch_zero_plane<double>(c->stream, g, c->fw, g.K + 1);
+      LAUNCHED(1);
+    }
+    launch_ibm_spread<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0);
+    LAUNCHED(1);
+  }
+  return IBM_OK;
+}
+
+int project(ibm_ctx *c, int rkiter, double dt) {
+  const Geo &g = c->g;
+  const double dti = 1. / (c->rkab[rkiter - 1] * dt);
+  int nl = 0;
+  launch_poisson<double>(c->stream, g, c->plx, c->ply, c->fu, c->fv, c->fw, c->spec, c->phi, c->twM, c->twN, c->twJ,
+                         c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl);
+  LAUNCHED(nl);
+  const double factor = c->rkab[rkiter - 1] * dt;
+  launch_correc<double, double>(c->stream, g, c->fu, c->fv, c->fw, c->phi, c->u, c->v, c->w, c->p, factor * g.dxi,
+                                factor * g.dyi, factor * g.dzi);
+  LAUNCHED(1);
+  return IBM_OK;
+}
+
+int newton_euler(ibm_ctx *c, int rkiter, double dt) {
+  if (c->pg.np == 0) return IBM_OK;
+  launch_save_old(c->stream, c->pg, c->pb);
+  LAUNCHED(1);
+  launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
+  LAUNCHED(1);
+  for (int iter = 0; iter <= 1; ++iter) {
+    launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt);
+    LAUNCHED(2);
+  }
+  launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 0);
+  LAUNCHED(1);
+  return IBM_OK;
+}
+
+int ready(ibm_ctx *c) {
+  if (!c) return IBM_E_INVALID;
+  if (!c->have_fields) return set_err(c, IBM_E_STATE, "ibm_set_fields has not been called");
+  if (c->pg.np > 0 && !c->particles_ready)
+    return set_err(c, IBM_E_STATE, "particles not initialised (ibm_set_particles + ibm_init_particles)");
+  return IBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ibm_abi_version(void) { return IBM_ABI_VERSION; }
+
+const char *ibm_last_error(const ibm_ctx *c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+ibm_ctx *ibm_create(const ibm_params *P) {
+  g_create_error.clear();
+  if (!P) { g_create_error = "null params"; return nullptr; }
+  if (P->itot < 4 || P->jtot < 4 || P->ktot < 3 || P->itot % 2) {
+    g_create_error = "grid must have even itot >= 4, jtot >= 4, ktot >= 3";
+    return nullptr;
+  }
+  if (!(P->lx > 0 && P->ly > 0 && P->lz > 0 && P->visc > 0)) { g_create_error = "lx, ly, lz, visc must be > 0"; return nullptr; }
+  if (P->np < 0 || (P->np > 0 && (P->nl <= 0 || !P->thetarc || !P->phirc || !(P->radius > 0)))) {
+    g_create_error = "np > 0 requires nl > 0, thetarc, phirc and radius > 0";
+    return nullptr;
+  }
+  if (P->mode != IBM_MODE_PLAIN_FP64) { g_create_error = "only IBM_MODE_PLAIN_FP64 is available in this build"; return nullptr; }
+  if (P->np > 0) {
+    // nl must equal nint(pi/3*(12*((radius-retrac)*dxi)^2+1)) (main.f90:118-132)
+    const double dxi = P->itot / P->lx, retrac = 0.3 / dxi;
+    const int nl = (int)std::lround((PI / 3.) * (12. * std::pow((P->radius - retrac) * dxi, 2) + 1.));
+    if (nl != P->nl) {
+      g_create_error = "nl = " + std::to_string(P->nl) + " does not match the derived value " + std::to_string(nl) +
+                       " (main.f90:118-132)";
+      return nullptr;
+    }
+  }
+  ibm_ctx *c = new ibm_ctx();
+  c->prm = *P;
+  if (P->np > 0) {
+    c->thetarc.assign(P->thetarc, P->thetarc + P->nl);
+    c->phirc.assign(P->phirc, P->phirc + P->nl);
+  }
+  c->prm.thetarc = nullptr;
+  c->prm.phirc = nullptr;
+  c->mode = P->mode;
+  derived(c);
+  if (!make_plan(c->g.I / 2, c->plx) || !make_plan(c->g.J, c->ply)) {
+    g_create_error = "itot/2 and jtot must be products of 2 and 3";
+    delete c;
+    return nullptr;
+  }
+  cudaGetDevice(&c->device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    g_create_error = "cudaStreamCreate failed (no CUDA device?)";
+    delete c;
+    return nullptr;
+  }
+  c->own_stream = true;
+  for (auto &e : c->ev) cudaEventCreate(&e);
+  int st = alloc_all(c);
+  if (st == IBM_OK) st = build_solver_tables(c);
+  if (st == IBM_OK && (poisson_set_smem_limits<double>() != 0 || poisson_set_smem_limits<float>() != 0))
+    st = set_err(c, IBM_E_CUDA, "cudaFuncSetAttribute failed");
+  if (st == IBM_OK) st = cuda_err(c, cudaStreamSynchronize(c->stream), "create");
+  if (st != IBM_OK) {
+    g_create_error = c->err;
+    ibm_destroy(c);
+    return nullptr;
+  }
+  return c;
+}
+
+int ibm_destroy(ibm_ctx *c) {
+  if (!c) return IBM_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void *ptrs[] = {c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv, c->fw, c->phi, c->spec, c->zt, c->twM,
+                  c->twN, c->twJ, c->scratch, c->dout, c->href, c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl,
+                  c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
+                  c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
+                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  if (c->hpin) cudaFreeHost(c->hpin);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return IBM_OK;
+}
+
+int ibm_sizes(const ibm_ctx *c, int *nqmax, int *nl, int *ncells) {
+  if (!c) return IBM_E_INVALID;
+  if (nqmax) *nqmax = c->nq;
+  if (nl) *nl = c->pg.nl;
+  if (ncells) *ncells = (c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  return IBM_OK;
+}
+
+int ibm_set_stream(ibm_ctx *c, void *stream) {
+  if (!c) return IBM_E_INVALID;
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->own_stream = stream == nullptr;
+  if (stream) c->stream = (cudaStream_t)stream;
+  else CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  return IBM_OK;
+}
+
+static int ensure_href(ibm_ctx *c) {
+  if (c->href) return IBM_OK;
+  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  CK(cudaMalloc((void **)&c->href, n * sizeof(double)));
+  return IBM_OK;
+}
+
+static int upload_field(ibm_ctx *c, const double *h, double *d) {
+  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  if (!h) {
+    CK(cudaMemsetAsync(d, 0, (size_t)c->g.nfield * sizeof(double), c->stream));
+    return IBM_OK;
+  }
+  CK(cudaMemcpyAsync(c->href, h, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_ref_to_dev<double>(c->stream, c->g, c->href, d);
+  LAUNCHED(1);
+  return IBM_OK;
+}
+static int download_field(ibm_ctx *c, const double *d, double *h) {
+  if (!h) return IBM_OK;
+  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  launch_dev_to_ref<double>(c->stream, c->g, d, c->href);
+  LAUNCHED(1);
+  CK(cudaMemcpyAsync(h, c->href, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
+int ibm_set_fields(ibm_ctx *c, const double *u, const double *v, const double *w, const double *p, const double *durk,
+                   const double *dvrk, const double *dwrk) {
+  if (!c) return IBM_E_INVALID;
+  if (!u || !v || !w || !p) return set_err(c, IBM_E_INVALID, "u, v, w and p are required");
+  int st;
+  if ((st = ensure_href(c))) return st;
+  const double *hs[7] = {u, v, w, p, durk, dvrk, dwrk};
+  double *ds[7] = {c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw};
+  for (int f = 0; f < 7; ++f)
+    if ((st = upload_field(c, hs[f], ds[f]))) return st;
+  // dudtf starts from zero (module storage), in particular its k1 plane
+  for (double *f : {c->fu, c->fv, c->fw}) CK(cudaMemsetAsync(f, 0, (size_t)c->g.nfield * sizeof(double), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_fields = true;
+  return IBM_OK;
+}
+
+int ibm_get_fields(ibm_ctx *c, double *u, double *v, double *w, double *p, double *durk, double *dvrk, double *dwrk) {
+  if (!c) return IBM_E_INVALID;
+  int st;
+  if ((st = ensure_href(c))) return st;
+  const double *ds[7] = {c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw};
+  double *hs[7] = {u, v, w, p, durk, dvrk, dwrk};
+  for (int f = 0; f < 7; ++f)
+    if ((st = download_field(c, ds[f], hs[f]))) return st;
+  return IBM_OK;
+}
+
+int ibm_get_intermediate(ibm_ctx *c, double *du, double *dv, double *dw) {
+  if (!c) return IBM_E_INVALID;
+  int st;
+  if ((st = ensure_href(c))) return st;
+  if ((st = download_field(c, c->fu, du))) return st;
+  if ((st = download_field(c, c->fv, dv))) return st;
+  return download_field(c, c->fw, dw);
+}
+
+static const double *const *pf_host_ptrs(const ibm_particles *s, const double **arr) {
+  const double *a[31] = {s->x, s->y, s->z, s->theta, s->phi, s->u, s->v, s->w, s->omx, s->omy, s->omz, s->omtheta,
+                         s->intu, s->intv, s->intw, s->intomx, s->intomy, s->intomz, s->colfx, s->colfy, s->colfz,
+                         s->coltx, s->colty, s->coltz, s->fxltot, s->fyltot, s->fzltot, s->torqxltot, s->torqyltot,
+                         s->torqzltot, s->torqtheta};
+  for (int f = 0; f < 31; ++f) arr[f] = a[f];
+  return arr;
+}
+
+int ibm_set_particles(ibm_ctx *c, const ibm_particles *s) {
+  if (!c || !s) return IBM_E_INVALID;
+  const int np = c->pg.np, nq = c->nq, nl = c->pg.nl;
+  if (np == 0) { c->have_particles = true; c->particles_ready = true; return IBM_OK; }
+  const double *arr[31];
+  pf_host_ptrs(s, arr);
+  std::vector<double> pf((size_t)PF_N * np, 0.);
+  for (int f = 0; f < 31; ++f) {
+    if (!arr[f]) return set_err(c, IBM_E_INVALID, "particle array missing");
+    std::memcpy(&pf[(size_t)f * np], arr[f], np * sizeof(double));
+  }
+  CK(cudaMemcpyAsync(c->pb.pf, pf.data(), pf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  std::vector<double> cf((size_t)CF_N * np * nq, 0.);
+  const double *carr[10] = {s->cdx, s->cdy, s->cdz, s->cdxt, s->cdyt, s->cdzt, s->cdut, s->cdvt, s->cdwt, s->cpsi};
+  for (int f = 0; f < 10; ++f)
+    if (carr[f]) std::memcpy(&cf[(size_t)f * np * nq], carr[f], (size_t)np * nq * sizeof(double));
+  CK(cudaMemcpyAsync(c->pb.cf, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (!s->qmax || !s->firstc || !s->nb || !s->mslv || !s->rkp)
+    return set_err(c, IBM_E_INVALID, "qmax, firstc, nb, mslv and rkp are required");
+  for (int p = 0; p < np; ++p) {
+    if (s->qmax[p] < 0 || s->qmax[p] > nq) return set_err(c, IBM_E_INVALID, "qmax outside 0..nqmax");
+    if (s->mslv[p] != p + 1) return set_err(c, IBM_E_INVALID, "mslv must be the particle id p+1 on one rank");
+    for (int n = 0; n < 9; ++n)
+      if (s->nb[(size_t)p * 9 + n] != 0 && s->nb[(size_t)p * 9 + n] != 1) return set_err(c, IBM_E_INVALID, "nb flags must be 0/1");
+  }
+  CK(cudaMemcpyAsync(c->pb.qmax, s->qmax, np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->pb.firstc, s->firstc, (size_t)np * nq * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->pb.ofirstc, s->firstc, (size_t)np * nq * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->pb.nb, s->nb, (size_t)np * 9 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->pb.mslv, s->mslv, np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  std::vector<double> rk((size_t)RK_N * np);
+  for (int p = 0; p < np; ++p)
+    for (int t = 0; t < RK_N; ++t) rk[(size_t)p * RK_N + t] = s->rkp[(size_t)p * RK_N + t];
+  CK(cudaMemcpyAsync(c->pb.rkp, rk.data(), rk.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->pb.err, 0, 4 * sizeof(int), c->stream));
+  if (s->xfp && s->yfp && s->zfp && s->ul && s->vl && s->wl) {
+    const size_t npl = (size_t)np * nl;
+    const double *la[6] = {s->xfp, s->yfp, s->zfp, s->ul, s->vl, s->wl};
+    double *ld[6] = {c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl, c->ib.wl};
+    for (int f = 0; f < 6; ++f) CK(cudaMemcpyAsync(ld[f], la[f], npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (s->fxl && s->fyl && s->fzl) {
+      CK(cudaMemcpyAsync(c->ib.fxl, s->fxl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->ib.fyl, s->fyl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->ib.fzl, s->fzl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+    std::vector<int> nla(np, nl);
+    CK(cudaMemcpyAsync(c->ib.nla, nla.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    c->particles_ready = true;
+  } else {
+    launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 2);
+    LAUNCHED(1);
+    c->particles_ready = true;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_particles = true;
+  return IBM_OK;
+}
+
+int ibm_get_particles(ibm_ctx *c, ibm_particles *s) {
+  if (!c || !s) return IBM_E_INVALID;
+  const int np = c->pg.np, nq = c->nq, nl = c->pg.nl;
+  if (np == 0) return IBM_OK;
+  std::vector<double> pf((size_t)PF_N * np);
+  CK(cudaMemcpyAsync(pf.data(), c->pb.pf, pf.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<double> cf((size_t)CF_N * np * nq);
+  CK(cudaMemcpyAsync(cf.data(), c->pb.cf, cf.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<double> rk((size_t)RK_N * np);
+  CK(cudaMemcpyAsync(rk.data(), c->pb.rkp, rk.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (s->qmax) CK(cudaMemcpyAsync(s->qmax, c->pb.qmax, np * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (s->firstc) CK(cudaMemcpyAsync(s->firstc, c->pb.firstc, (size_t)np * nq * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (s->nb) CK(cudaMemcpyAsync(s->nb, c->pb.nb, (size_t)np * 9 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (s->mslv) CK(cudaMemcpyAsync(s->mslv, c->pb.mslv, np * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  const size_t npl = (size_t)np * nl;
+  const double *ls[9] = {c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl, c->ib.wl, c->ib.fxl, c->ib.fyl, c->ib.fzl};
+  double *lh[9] = {s->xfp, s->yfp, s->zfp, s->ul, s->vl, s->wl, s->fxl, s->fyl, s->fzl};
+  for (int f = 0; f < 9; ++f)
+    if (lh[f]) CK(cudaMemcpyAsync(lh[f], ls[f], npl * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double *arr[31] = {s->x, s->y, s->z, s->theta, s->phi, s->u, s->v, s->w, s->omx, s->omy, s->omz, s->omtheta,
+                     s->intu, s->intv, s->intw, s->intomx, s->intomy, s->intomz, s->colfx, s->colfy, s->colfz,
+                     s->coltx, s->colty, s->coltz, s->fxltot, s->fyltot, s->fzltot, s->torqxltot, s->torqyltot,
+                     s->torqzltot, s->torqtheta};
+  for (int f = 0; f < 31; ++f)
+    if (arr[f]) std::memcpy(arr[f], &pf[(size_t)f * np], np * sizeof(double));
+  double *carr[10] = {s->cdx, s->cdy, s->cdz, s->cdxt, s->cdyt, s->cdzt, s->cdut, s->cdvt, s->cdwt, s->cpsi};
+  for (int f = 0; f < 10; ++f)
+    if (carr[f]) std::memcpy(carr[f], &cf[(size_t)f * np * nq], (size_t)np * nq * sizeof(double));
+  if (s->rkp) std::memcpy(s->rkp, rk.data(), rk.size() * sizeof(double));
+  return check_flags(c);
+}
+
+int ibm_init_particles(ibm_ctx *c, double *vol_calc) {
+  if (!c) return IBM_E_INVALID;
+  if (!c->have_fields) return set_err(c, IBM_E_STATE, "ibm_set_fields has not been called");
+  if (c->pg.np == 0) { c->particles_ready = true; if (vol_calc) *vol_calc = 0.; return IBM_OK; }
+  if (!c->have_particles) return set_err(c, IBM_E_STATE, "ibm_set_particles has not been called");
+  launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 1);
+  LAUNCHED(1);
+  launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 1);
+  LAUNCHED(1);
+  double vol = 0.;
+  CK(cudaMemcpyAsync(&vol, c->pb.red, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
+  LAUNCHED(1);
+  CK(cudaStreamSynchronize(c->stream));
+  if (vol_calc) *vol_calc = vol;
+  c->particles_ready = true;
+  return IBM_OK;
+}
+
+int ibm_rk_predict(ibm_ctx *c, int rkiter, double dt) {
+  int st;
+  if ((st = ready(c))) return st;
+  if (rkiter < 1 || rkiter > 3) return set_err(c, IBM_E_INVALID, "rkiter must be 1..3");
+  c->dt_last = dt;
+  return predict(c, rkiter, dt);
+}
+int ibm_forcing_loop(ibm_ctx *c, double dt, int nl_iter) {
+  int st;
+  if ((st = ready(c))) return st;
+  return forcing(c, dt, nl_iter);
+}
+int ibm_project(ibm_ctx *c, int rkiter, double dt) {
+  int st;
+  if ((st = ready(c))) return st;
+  if (rkiter < 1 || rkiter > 3) return set_err(c, IBM_E_INVALID, "rkiter must be 1..3");
+  return project(c, rkiter, dt);
+}
+int ibm_newton_euler(ibm_ctx *c, int rkiter, double dt) {
+  int st;
+  if ((st = ready(c))) return st;
+  if (rkiter < 1 || rkiter > 3) return set_err(c, IBM_E_INVALID, "rkiter must be 1..3");
+  return newton_euler(c, rkiter, dt);
+}
+
+static int step_once(ibm_ctx *c, double dt, bool timed) {
+  int st;
+  float ms[4] = {0, 0, 0, 0};
+  for (int rkiter = 1; rkiter <= 3; ++rkiter) {
+    if (timed) CK(cudaEventRecord(c->ev[0], c->stream));
+    if ((st = predict(c, rkiter, dt))) return st;
+    if (timed) CK(cudaEventRecord(c->ev[1], c->stream));
+    if ((st = forcing(c, dt, 3))) return st;
+    if (timed) CK(cudaEventRecord(c->ev[2], c->stream));
+    if ((st = project(c, rkiter, dt))) return st;
+    if (timed) CK(cudaEventRecord(c->ev[3], c->stream));
+    if ((st = newton_euler(c, rkiter, dt))) return st;
+    if (timed) {
+      CK(cudaEventRecord(c->ev[4], c->stream));
+      CK(cudaEventSynchronize(c->ev[4]));
+      for (int q = 0; q < 4; ++q) {
+        float t = 0;
+        cudaEventElapsedTime(&t, c->ev[q], c->ev[q + 1]);
+        ms[q] += t;
+      }
+    }
+  }
+  if (timed)
+    for (int q = 0; q < 4; ++q) c->phase_ms[q] = ms[q];
+  c->dt_last = dt;
+  return IBM_OK;
+}
+
+int ibm_rk3_step(ibm_ctx *c, double dt) {
+  int st;
+  if ((st = ready(c))) return st;
+  return step_once(c, dt, false);
+}
+
+int ibm_run(ibm_ctx *c, double dt, int nsteps) {
+  int st;
+  if ((st = ready(c))) return st;
+  for (int s = 0; s < nsteps; ++s)
+    if ((st = step_once(c, dt, false))) return st;
+  return IBM_OK;
+}
+
+int ibm_timed_step(ibm_ctx *c, double dt) {
+  int st;
+  if ((st = ready(c))) return st;
+  return step_once(c, dt, true);
+}
+
+int ibm_chkdiv(ibm_ctx *c, double *divtot, double *divmax, int ijk[3]) {
+  if (!c) return IBM_E_INVALID;
+  launch_chkdiv(c->stream, c->g, c->u, c->v, c->w, c->scratch, c->dout);
+  LAUNCHED(2);
+  CK(cudaMemcpyAsync(c->hpin, c->dout, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const double tot = c->hpin[0], mx = c->hpin[1];
+  const long long loc = (long long)c->hpin[2];
+  if (divtot) *divtot = tot;
+  if (divmax) *divmax = mx;
+  if (ijk) {
+    if (loc >= 0) {
+      ijk[0] = (int)(loc % c->g.I) + 1;
+      ijk[1] = (int)((loc / c->g.I) % c->g.J) + 1;
+      ijk[2] = (int)(loc / c->g.plane) + 1;
+    } else {
+      ijk[0] = ijk[1] = ijk[2] = 0;
+    }
+  }
+  if (tot > 1.e-3) return set_err(c, IBM_E_DIVERGENCE, "total divergence > 1e-3 (chkdiv.f90:51-58)");
+  return IBM_OK;
+}
+
+int ibm_chkdt(ibm_ctx *c, double *dtmax) {
+  if (!c || !dtmax) return IBM_E_INVALID;
+  launch_chkdt(c->stream, c->g, c->u, c->v, c->w, c->scratch, c->dout);
+  LAUNCHED(2);
+  CK(cudaMemcpyAsync(c->hpin, c->dout, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *dtmax = c->hpin[0];
+  return IBM_OK;
+}
+
+int ibm_slip_residual(ibm_ctx *c, double *maxres, double *rmsres) {
+  if (!c) return IBM_E_INVALID;
+  if (c->pg.np == 0) { if (maxres) *maxres = 0; if (rmsres) *rmsres = 0; return IBM_OK; }
+  // re-interpolate the forced field (valid between ibm_forcing_loop and ibm_project)
+  launch_ibm_interp_force<double>(c->stream, c->g, c->pg, c->ib, c->fu, c->fv, c->fw, 1., -1);
+  LAUNCHED(1);
+  launch_slip_residual(c->stream, c->pg, c->ib, c->dout + 16);
+  LAUNCHED(1);
+  CK(cudaMemcpyAsync(c->hpin, c->dout + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  std::vector<int> nla(c->pg.np);
+  CK(cudaMemcpy(nla.data(), c->ib.nla, c->pg.np * sizeof(int), cudaMemcpyDeviceToHost));
+  long n = 0;
+  for (int q : nla) n += q;
+  if (maxres) *maxres = c->hpin[0];
+  if (rmsres) *rmsres = n ? std::sqrt(c->hpin[1] / n) : 0.;
+  return IBM_OK;
+}
+
+int ibm_diagnostics(ibm_ctx *c, double *wsn, double *wso, double ft[3]) {
+  if (!c) return IBM_E_INVALID;
+  double raw[3];
+  CK(cudaMemcpyAsync(raw, c->dout + 8, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  // rk3.f90:99-103, 213-217, 321-325 for the last completed stage sequence
+  const double dt = c->dt_last;
+  const double dVeul = (1. / c->g.dxi) * (1. / c->g.dyi) * (1. / c->g.dzi);
+  const double nt = (double)c->g.I * c->g.J * c->g.K;
+  const double old1 = raw[0] / (dVeul * nt);
+  const double old2 = raw[1] / (dVeul * nt);
+  const double new3 = ((dt * (45. / 60.)) / dt) * raw[2] / (dVeul * nt) - ((dt * (25. / 60.)) / dt) * old2;
+  (void)old1;
+  if (wsn) *wsn = new3;
+  if (wso) *wso = old2;
+  if (ft) {
+    ft[0] = ft[1] = ft[2] = 0.;
+    const int np = c->pg.np;
+    if (np > 0) {
+      std::vector<double> f((size_t)3 * np);
+      CK(cudaMemcpy(f.data(), c->pb.pf + (size_t)PF_FXLTOT * np, 3 * np * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int q = 0; q < 3; ++q)
+        for (int p = 0; p < np; ++p) ft[q] += f[(size_t)q * np + p];
+    }
+  }
+  return IBM_OK;
+}
+
+int ibm_phase_times(ibm_ctx *c, double ms[4]) {
+  if (!c || !ms) return IBM_E_INVALID;
+  for (int q = 0; q < 4; ++q) ms[q] = c->phase_ms[q];
+  return IBM_OK;
+}
+
+long long ibm_launch_count(const ibm_ctx *c) { return c ? c->launches : 0; }
+
+int ibm_sync(ibm_ctx *c) {
+  if (!c) return IBM_E_INVALID;
+  CK(cudaStreamSynchronize(c->stream));
+  return check_flags(c);
+}
+
+}  // extern "C"

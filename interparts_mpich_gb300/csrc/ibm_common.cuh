@@ -1,0 +1,90 @@
+// ibm_common.cuh -- device data layout and helpers shared by the kernels.
+//
+// HBM layout (one rank, periodic x/y, walls in z):
+//   cell fields   F[(k*J + j)*I + i], i in [0,I), j in [0,J), k in [0,K+1]
+//                 -> reference F(i+1, j+1, k); the x/y ghosts of the
+//                 reference are replaced by periodic index wrap, the z ghost
+//                 planes k=0 and k=K+1 are stored.
+//   spectra       S[(k*J + ky)*MX + kx], complex, kx in [0, I/2], MX = I/2+1,
+//                 k in [0,K) (reference k-1).
+//   particles     scalar state pf[f*np + p] (field-major), contact arrays
+//                 [p*nq + q], Lagrangian arrays [p*nl + l].
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ibm_rk3.h"
+
+#define IBM_PI 3.141592653589793238462643383279502884
+
+// particle scalar fields (order of the reference type `particle`, then the
+// force totals, then the old-state copy `op`)
+enum PField {
+  PF_X, PF_Y, PF_Z, PF_THETA, PF_PHI, PF_U, PF_V, PF_W, PF_OMX, PF_OMY, PF_OMZ, PF_OMTHETA,
+  PF_INTU, PF_INTV, PF_INTW, PF_INTOMX, PF_INTOMY, PF_INTOMZ,
+  PF_COLFX, PF_COLFY, PF_COLFZ, PF_COLTX, PF_COLTY, PF_COLTZ,
+  PF_FXLTOT, PF_FYLTOT, PF_FZLTOT, PF_TQX, PF_TQY, PF_TQZ, PF_TQTHETA,
+  // old state (op), same order as the first 24 fields
+  PF_OX, PF_OY, PF_OZ, PF_OTHETA, PF_OPHI, PF_OU, PF_OV, PF_OW, PF_OOMX, PF_OOMY, PF_OOMZ, PF_OOMTHETA,
+  PF_OINTU, PF_OINTV, PF_OINTW, PF_OINTOMX, PF_OINTOMY, PF_OINTOMZ,
+  PF_OCOLFX, PF_OCOLFY, PF_OCOLFZ, PF_OCOLTX, PF_OCOLTY, PF_OCOLTZ,
+  // snapshot of the collision pass (anb(:,0)): x,y,z,u,v,w,omx,omy,omz
+  PF_SX, PF_SY, PF_SZ, PF_SU, PF_SV, PF_SW, PF_SOMX, PF_SOMY, PF_SOMZ,
+  PF_N
+};
+// contact arrays: current and old
+enum CField { CF_DX, CF_DY, CF_DZ, CF_DXT, CF_DYT, CF_DZT, CF_DUT, CF_DVT, CF_DWT, CF_PSI,
+              CF_ODX, CF_ODY, CF_ODZ, CF_ODXT, CF_ODYT, CF_ODZT, CF_ODUT, CF_ODVT, CF_ODWT, CF_N };
+// rkp accumulators (particle_sumrk, common.f90:97-105)
+enum RKField { RK_FX, RK_FY, RK_FZ, RK_TX, RK_TY, RK_TZ, RK_TT, RK_CFX, RK_CFY, RK_CFZ,
+               RK_CTX, RK_CTY, RK_CTZ, RK_DUDT, RK_DVDT, RK_DWDT, RK_DOMX, RK_DOMY, RK_DOMZ, RK_N };
+
+// Per-point stencil of the 3-point delta (interp_spread.f90:76-130), cached
+// once per substep because the points do not move during the forcing loop.
+struct PointStencil {
+  int ilow, jlow, klow, ilows, jlows, klows;  // reference indices
+  double phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
+};
+
+// Constants of one context, passed by value to the kernels.
+struct Geo {
+  int I, J, K, MX;            // grid, MX = I/2+1
+  long plane, nfield;         // I*J, (K+2)*I*J
+  double lx, ly, lz, dxi, dyi, dzi, dx, dy, dz, visc;
+  int bc_top, bc_bot;
+};
+
+struct PartGeo {
+  int np, nl, nq, nb_copies, rotation;
+  double radius, radfp, offset, dVlagr, dVeul, lx, ly, lz, dxi, dyi, dzi, dx, dy, dz;
+  double gacc[3], rkab[3], volp, ratiorho, mominert;
+  double kn_ss, etan_ss, kt_ss, etat_ss, muc_ss, kn_sw, etan_sw, kt_sw, etat_sw, muc_sw;
+  double coeff_f, a11a_ini_pp, a11b_ini_pp, a11a_sat_pp, a11b_sat_pp, a11_ini_pw, a11_sat_pw;
+  int I, J, K;
+};
+
+__host__ __device__ inline long fidx(const Geo &g, int i, int j, int k) {
+  return ((long)k * g.J + j) * g.I + i;
+}
+__device__ __forceinline__ int wrapm(int i, int n) {  // i in [-n, 2n)
+  return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
+// Roma-Peskin 3-point regularised delta times h (kernel.f90:7-25)
+__device__ __forceinline__ double delta3(double r) {
+  const double ar = fabs(r);
+  if (ar > 1.5) return 0.;
+  if (ar > 0.5) return (1. / 6.) * (5. - 3. * ar - sqrt(-3. * ((1. - ar) * (1. - ar)) + 1.));
+  return (1. / 3.) * (1. + sqrt(-3. * (r * r) + 1.));
+}
+__device__ __forceinline__ float delta3f(float r) {
+  const float ar = fabsf(r);
+  if (ar > 1.5f) return 0.f;
+  if (ar > 0.5f) return (1.f / 6.f) * (5.f - 3.f * ar - sqrtf(-3.f * ((1.f - ar) * (1.f - ar)) + 1.f));
+  return (1.f / 3.f) * (1.f + sqrtf(-3.f * (r * r) + 1.f));
+}
+// Fortran NINT (half away from zero)
+__device__ __forceinline__ int fnint(double x) { return (int)round(x); }
+
+// launch helpers (the host side counts every launch)
+#define IBM_CHECK_LAUNCH() cudaGetLastError()

@@ -1,0 +1,251 @@
+// ibm_kernels.cu -- multidirect immersed-boundary forcing on the Lagrangian
+// points: eulr2lagr (interp_spread.f90:12-228), complagrforces /
+// updtlagrforces (forcing.f90:9-391) and lagr2eulr (interp_spread.f90:230-474).
+//
+// Compiled without FMA contraction so the stencil indices, delta weights and
+// point forces follow the reference roundings.
+//
+// Spreading is incremental: lagr2eulr rebuilds dudtf = dudtold + S(F) with
+// the cumulative point force F every pass (zeroing and re-adding the whole
+// field).  By linearity of S, dudtf after pass n equals the pass n-1 field
+// plus S(F_n - F_{n-1}); the GPU adds only S(dF) over the points' footprint,
+// so no full-field pass is needed.  The one plane that the reference never
+// refreshes from dwdt, dwdtf(:,:,k1), is zeroed before the first spread of
+// a substep so it carries S(F) exactly as in the reference.
+#include "kernels.cuh"
+
+namespace ibmk {
+
+// stencil of one point (interp_spread.f90:76-130): same arithmetic as the
+// reference, single rank (zstart = 1)
+__global__ void __launch_bounds__(256) k_ibm_stencil(Geo g, PartGeo pg, IbmBuffers b) {
+  const long n = (long)pg.np * pg.nl;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t / pg.nl), l = (int)(t - (long)p * pg.nl);
+    if (l >= b.nla[p]) continue;
+    const double xfp = b.xfp[t], yfp = b.yfp[t], zfp = b.zfp[t];
+    double coorxfp = xfp * g.dxi - (double)((long)floor((xfp - 0.5 * g.dx) / g.lx) * g.I) - (1 - 1);
+    double cooryfp = yfp * g.dyi - (double)((long)floor((yfp - 0.5 * g.dy) / g.ly) * g.J) - (1 - 1);
+    double coorzfp = zfp * g.dzi;
+    // Guard: a point outside the grid (or a non-finite position) would index
+    // outside the arrays; flag it and park the point at a safe location.
+    if (!(coorxfp >= 0. && coorxfp <= g.I + 1.) || !(cooryfp >= 0. && cooryfp <= g.J + 1.) ||
+        !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
+      atomicExch(&b.err[2], 1);
+      coorxfp = 1.; cooryfp = 1.; coorzfp = 1.5;
+    }
+    PointStencil s;
+    s.ilows = fnint(coorxfp) - 1;
+    s.jlows = fnint(cooryfp) - 1;
+    s.klows = max(fnint(coorzfp) - 1, 1);
+    s.ilow = (int)floor(coorxfp);
+    s.jlow = (int)floor(cooryfp);
+    s.klow = max(min((int)floor(coorzfp), g.K - 2), 1);
+    for (int m = 0; m < 3; ++m) {
+      s.phix[m] = delta3(1. * s.ilows + m - coorxfp);
+      s.phiy[m] = delta3(1. * s.jlows + m - cooryfp);
+      s.phiz[m] = delta3(1. * s.klows + m - coorzfp);
+      s.phixh[m] = delta3(1. * s.ilow + m - .5 - coorxfp);
+      s.phiyh[m] = delta3(1. * s.jlow + m - .5 - cooryfp);
+      s.phizh[m] = delta3(1. * s.klow + m - .5 - coorzfp);
+    }
+    b.st[t] = s;
+  }
+}
+
+template <typename T>
+void launch_ibm_stencil(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b) {
+  k_ibm_stencil<<<1216, 256, 0, s>>>(g, pg, b);
+}
+template void launch_ibm_stencil<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers);
+template void launch_ibm_stencil<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers);
+
+// interpolation of the three staggered components at point t
+template <typename T>
+__device__ __forceinline__ void interp_point(const Geo &g, const PointStencil &s, const T *__restrict__ fu,
+                                             const T *__restrict__ fv, const T *__restrict__ fw, double &ou,
+                                             double &ov, double &ow) {
+  double au = 0., av = 0., aw = 0.;
+  int ix[3], ixh[3], jy[3], jyh[3];
+  for (int m = 0; m < 3; ++m) {
+    ix[m] = wrapm(s.ilows + m - 1, g.I);
+    ixh[m] = wrapm(s.ilow + m - 1, g.I);
+    jy[m] = wrapm(s.jlows + m - 1, g.J);
+    jyh[m] = wrapm(s.jlow + m - 1, g.J);
+  }
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i)
+        au = au + (double)fu[fidx(g, ix[i], jyh[j], s.klow + k)] * s.phix[i] * s.phiyh[j] * s.phizh[k];
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i)
+        av = av + (double)fv[fidx(g, ixh[i], jy[j], s.klow + k)] * s.phixh[i] * s.phiy[j] * s.phizh[k];
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i)
+        aw = aw + (double)fw[fidx(g, ixh[i], jyh[j], s.klows + k)] * s.phixh[i] * s.phiyh[j] * s.phiz[k];
+  ou = au; ov = av; ow = aw;
+}
+
+// eulr2lagr + complagrforces/updtlagrforces for one particle per block:
+// interpolation, point force update and the per-particle force/torque sums.
+template <typename T>
+__global__ void __launch_bounds__(256) k_ibm_interp_force(Geo g, PartGeo pg, IbmBuffers b, const T *__restrict__ fu,
+                                                          const T *__restrict__ fv, const T *__restrict__ fw,
+                                                          double dti, int first) {
+  const int p = blockIdx.x;
+  const int nla = b.nla[p];
+  const double *pf = b.pf;
+  const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
+  double sfx = 0, sfy = 0, sfz = 0, stx = 0, sty = 0, stz = 0;
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const long t = (long)p * pg.nl + l;
+    const PointStencil s = b.st[t];
+    double iu, iv, iw;
+    interp_point<T>(g, s, fu, fv, fw, iu, iv, iw);
+    b.dudtl[t] = iu; b.dvdtl[t] = iv; b.dwdtl[t] = iw;
+    if (first < 0) continue;  // interpolation only (slip residual)
+    double fx, fy, fz;
+    if (first) {
+      fx = (b.ul[t] - iu) * dti;
+      fy = (b.vl[t] - iv) * dti;
+      fz = (b.wl[t] - iw) * dti;
+    } else {
+      fx = b.fxl[t] + (b.ul[t] - iu) * dti;
+      fy = b.fyl[t] + (b.vl[t] - iv) * dti;
+      fz = b.fzl[t] + (b.wl[t] - iw) * dti;
+    }
+    b.fxl[t] = fx; b.fyl[t] = fy; b.fzl[t] = fz;
+    const double rx = b.xfp[t] - px, ry = b.yfp[t] - py, rz = b.zfp[t] - pz;
+    sfx += fx; sfy += fy; sfz += fz;
+    stx = stx + ry * fz - rz * fy;
+    sty = sty + rz * fx - rx * fz;
+    stz = stz + rx * fy - ry * fx;
+  }
+  __shared__ double red[6][256];
+  red[0][threadIdx.x] = sfx; red[1][threadIdx.x] = sfy; red[2][threadIdx.x] = sfz;
+  red[3][threadIdx.x] = stx; red[4][threadIdx.x] = sty; red[5][threadIdx.x] = stz;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && first >= 0) {
+    double *pw = b.pf;
+    const double dV = pg.dVlagr;
+    const double tx = red[3][0] * dV, ty = red[4][0] * dV, tz = red[5][0] * dV;
+    pw[PF_FXLTOT * pg.np + p] = red[0][0] * dV;
+    pw[PF_FYLTOT * pg.np + p] = red[1][0] * dV;
+    pw[PF_FZLTOT * pg.np + p] = red[2][0] * dV;
+    pw[PF_TQX * pg.np + p] = tx;
+    pw[PF_TQY * pg.np + p] = ty;
+    pw[PF_TQZ * pg.np + p] = tz;
+    const double phi = pw[PF_PHI * pg.np + p];
+    pw[PF_TQTHETA * pg.np + p] = (ty * cos(phi)) - (tx * sin(phi));
+  }
+}
+
+template <typename T>
+void launch_ibm_interp_force(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const T *fu, const T *fv,
+                             const T *fw, double dt, int first) {
+  if (pg.np == 0) return;
+  k_ibm_interp_force<T><<<pg.np, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, first);
+}
+template void launch_ibm_interp_force<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, const double *,
+                                              const double *, const double *, double, int);
+template void launch_ibm_interp_force<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, const float *,
+                                             const float *, const float *, double, int);
+
+// lagr2eulr increment: spread dF = (U_l - u~_l)/dt with the reference
+// coefficient order F*coeff0*phix*phiy*phiz (interp_spread.f90:329-355)
+template <typename T>
+__global__ void __launch_bounds__(256) k_ibm_spread(Geo g, PartGeo pg, IbmBuffers b, T *__restrict__ fu,
+                                                    T *__restrict__ fv, T *__restrict__ fw, double dti,
+                                                    double coeff0) {
+  const long n = (long)pg.np * pg.nl;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(t / pg.nl), l = (int)(t - (long)p * pg.nl);
+    if (l >= b.nla[p]) continue;
+    const PointStencil s = b.st[t];
+    const double dfx = (b.ul[t] - b.dudtl[t]) * dti;
+    const double dfy = (b.vl[t] - b.dvdtl[t]) * dti;
+    const double dfz = (b.wl[t] - b.dwdtl[t]) * dti;
+    int ix[3], ixh[3], jy[3], jyh[3];
+    for (int m = 0; m < 3; ++m) {
+      ix[m] = wrapm(s.ilows + m - 1, g.I);
+      ixh[m] = wrapm(s.ilow + m - 1, g.I);
+      jy[m] = wrapm(s.jlows + m - 1, g.J);
+      jyh[m] = wrapm(s.jlow + m - 1, g.J);
+    }
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+          atomicAdd(&fu[fidx(g, ix[i], jyh[j], s.klow + k)], (T)(dfx * coeff0 * s.phix[i] * s.phiyh[j] * s.phizh[k]));
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+          atomicAdd(&fv[fidx(g, ixh[i], jy[j], s.klow + k)], (T)(dfy * coeff0 * s.phixh[i] * s.phiy[j] * s.phizh[k]));
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+          atomicAdd(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)], (T)(dfz * coeff0 * s.phixh[i] * s.phiyh[j] * s.phiz[k]));
+  }
+}
+
+template <typename T>
+void launch_ibm_spread(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, T *fu, T *fv, T *fw, double dt,
+                       int first) {
+  (void)first;
+  if (pg.np == 0) return;
+  const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
+  k_ibm_spread<T><<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0);
+}
+template void launch_ibm_spread<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, double *, double *,
+                                        double *, double, int);
+template void launch_ibm_spread<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, float *, float *,
+                                       float *, double, int);
+
+template <typename T>
+__global__ void k_zero_plane(Geo g, T *f, int k) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < g.plane; t += (long)gridDim.x * blockDim.x)
+    f[(long)k * g.plane + t] = (T)0;
+}
+template <typename T>
+void launch_zero_plane(cudaStream_t s, const Geo &g, T *f, int k) {
+  k_zero_plane<T><<<152, 256, 0, s>>>(g, f, k);
+}
+template void launch_zero_plane<double>(cudaStream_t, const Geo &, double *, int);
+template void launch_zero_plane<float>(cudaStream_t, const Geo &, float *, int);
+
+// |U_l - u~_l| statistics (max, sum of squares, count) over all points,
+// using the interpolation stored by the last pass.
+__global__ void k_slip_residual(PartGeo pg, IbmBuffers b, double *out) {
+  __shared__ double smax[256], ssum[256];
+  double mx = 0., sm = 0.;
+  const long n = (long)pg.np * pg.nl;
+  for (long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int p = (int)(t / pg.nl), l = (int)(t - (long)p * pg.nl);
+    if (l >= b.nla[p]) continue;
+    const double ex = b.ul[t] - b.dudtl[t], ey = b.vl[t] - b.dvdtl[t], ez = b.wl[t] - b.dwdtl[t];
+    const double r2 = ex * ex + ey * ey + ez * ez;
+    mx = fmax(mx, sqrt(r2));
+    sm += r2;
+  }
+  smax[threadIdx.x] = mx; ssum[threadIdx.x] = sm;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+      ssum[threadIdx.x] += ssum[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[0] = smax[0]; out[1] = ssum[0]; }
+}
+void launch_slip_residual(cudaStream_t s, const PartGeo &pg, IbmBuffers b, double *out) {
+  k_slip_residual<<<1, 256, 0, s>>>(pg, b, out);
+}
+
+}  // namespace ibmk

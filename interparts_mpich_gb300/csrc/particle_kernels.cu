@@ -1,0 +1,677 @@
+// particle_kernels.cu -- rigid-sphere side of the substep on one rank:
+// intgr_over_sphere (intgr_over_sphere.f90:12-625), the collision /
+// lubrication pass with its integer contact lists (intgr_nwtn_eulr.f90:326-605,
+// collisions.f90:10-438), the Newton-Euler update (:607-667), sumrk3
+// (:1586-1669), the periodic wrap and neighbour flags (:702-714, :1051-1090)
+// and the new Lagrangian points (:1438-1485).
+//
+// Compiled without FMA contraction: these are few, sequential-per-particle
+// operations whose roundings are kept equal to the reference so that the
+// integer contact lists (firstc/qmax) come out identical.
+#include "kernels.cuh"
+
+namespace ibmk {
+
+#define PF(f) b.pf[(long)(f) * np + p]
+#define CFA(f, q) b.cf[((long)(f) * np + p) * nq + (q)]
+
+// ---------------------------------------------------------------------------
+// new -> old (intgr_nwtn_eulr.f90:77-118)
+// ---------------------------------------------------------------------------
+__global__ void k_save_old(PartGeo pg, PartBuffers b) {
+  const int np = pg.np, nq = pg.nq;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np || b.mslv[p] <= 0) return;
+  for (int f = PF_X; f <= PF_COLTZ; ++f) PF(f + (PF_OX - PF_X)) = PF(f);
+  for (int q = 0; q < nq; ++q)
+    for (int f = CF_DX; f <= CF_DWT; ++f) CFA(f + (CF_ODX - CF_DX), q) = CFA(f, q);
+}
+void launch_save_old(cudaStream_t s, const PartGeo &pg, PartBuffers b) {
+  if (pg.np == 0) return;
+  k_save_old<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b);
+}
+
+// ---------------------------------------------------------------------------
+// intgr_over_sphere.  One block per particle; the self-neighbour copies of a
+// particle near the periodic edges integrate the wrapped part of the box
+// (intgr_over_sphere.f90:84-112 and :298-313).  type 1 = volume, type 2 =
+// integral of u (intu..), type 3 = integral of r x u (intomx..), type 23 =
+// types 2 and 3 in one sweep (they read the same fields).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void copy_shift_sphere(int nbrecv, double lx, double ly, double &x, double &y) {
+  switch (nbrecv) {
+    case 1: x = x + lx; break;
+    case 2: x = x + lx; y = y - ly; break;
+    case 3: y = y - ly; break;
+    case 4: x = x - lx; y = y - ly; break;
+    case 5: x = x - lx; break;
+    case 6: x = x - lx; y = y + ly; break;
+    case 7: y = y + ly; break;
+    case 8: x = x + lx; y = y + ly; break;
+    default: break;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffers b, const T *__restrict__ u,
+                                                    const T *__restrict__ v, const T *__restrict__ w, int type) {
+  const int np = pg.np;
+  const int p = blockIdx.x;
+  if (b.mslv[p] == 0) return;
+  const double radius = pg.radius, dVeul = pg.dVeul;
+  const double dx = 1. / g.dxi, dy = 1. / g.dyi, dz = 1. / g.dzi;
+  const double radin = radius - 2. * dx;
+  const double radin2 = radin * radin;
+  double ax[9], ay[9], az[9];
+  ax[0] = PF(PF_X); ay[0] = PF(PF_Y); az[0] = PF(PF_Z);
+  for (int n = 1; n < 9; ++n) { ax[n] = 0; ay[n] = 0; az[n] = 0; }
+  const int *nbf = b.nb + (long)p * 9;
+  for (int nb = 1; nb <= 8; ++nb) {
+    int nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8;
+    if (b.mslv[p] > 0 && nbf[nb] == 1) {
+      ax[nbrecv] = ax[0]; ay[nbrecv] = ay[0]; az[nbrecv] = az[0];
+      copy_shift_sphere(nbrecv, g.lx, g.ly, ax[nbrecv], ay[nbrecv]);
+    }
+  }
+  __shared__ double red[6][256];
+  double tot[6] = {0, 0, 0, 0, 0, 0};  // thread 0: per-copy sums added in nb order
+  double cps[9][6];
+  for (int n = 0; n < 9; ++n) for (int q = 0; q < 6; ++q) cps[n][q] = 0.;
+  for (int nb = 0; nb <= 8; ++nb) {
+    const bool go = (nb == 0 && b.mslv[p] > 0) || (nb > 0 && b.mslv[p] > 0 && nbf[nb] == 1);
+    if (!go) continue;
+    int nbrecv = nb;
+    if (nb > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
+    const double cx = ax[nbrecv], cy = ay[nbrecv], cz = az[nbrecv];
+    int ilow = fnint((cx - radius) * g.dxi - 2.), ihigh = fnint((cx + radius) * g.dxi + 2.);
+    int jlow = fnint((cy - radius) * g.dyi - 2.), jhigh = fnint((cy + radius) * g.dyi + 2.);
+    int klow = fnint((cz - radius) * g.dzi - 2.), khigh = fnint((cz + radius) * g.dzi + 2.);
+    if (ilow < 1) ilow = 1;
+    if (jlow < 1) jlow = 1;
+    if (klow < 1) klow = 1;
+    if (ihigh > g.I) ihigh = g.I;
+    if (jhigh > g.J) jhigh = g.J;
+    if (khigh > g.K) khigh = g.K;
+    const int ni = ihigh - ilow + 1, nj = jhigh - jlow + 1, nk = khigh - klow + 1;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    if (ni > 0 && nj > 0 && nk > 0) {
+      const long ncell = (long)ni * nj * nk;
+      for (int comp = 0; comp < 3; ++comp) {
+        const T *F = comp == 0 ? u : (comp == 1 ? v : w);
+        for (long t = threadIdx.x; t < ncell; t += blockDim.x) {
+          const int i = ilow + (int)(t % ni);
+          const int j = jlow + (int)((t / ni) % nj);
+          const int k = klow + (int)(t / ((long)ni * nj));
+          double coorzmin, coorzplus, coorymin, cooryplus, coorxmin, coorxplus;
+          if (comp < 2) { coorzmin = (k - 1) * dz; coorzplus = k * dz; }
+          else { coorzmin = (k - 0.5) * dz; coorzplus = (k + 0.5) * dz; }
+          if (comp == 1) { coorymin = 0. + (j - 0.5) * dy; cooryplus = 0. + (j + 0.5) * dy; }
+          else { coorymin = 0. + (j - 1) * dy; cooryplus = 0. + j * dy; }
+          if (comp == 0) { coorxmin = 0. + (i - 0.5) * dx; coorxplus = 0. + (i + 0.5) * dx; }
+          else { coorxmin = 0. + (i - 1) * dx; coorxplus = 0. + i * dx; }
+          const double dzp2 = (coorzplus - cz) * (coorzplus - cz);
+          const double dyp2 = (cooryplus - cy) * (cooryplus - cy);
+          const double dxp2 = (coorxplus - cx) * (coorxplus - cx);
+          const double dist2 = dxp2 + dyp2 + dzp2;
+          double frac = 1.;
+          bool full = dist2 < radin2;
+          if (!full) {
+            const double dxm2 = (coorxmin - cx) * (coorxmin - cx);
+            const double dym2 = (coorymin - cy) * (coorymin - cy);
+            const double dzm2 = (coorzmin - cz) * (coorzmin - cz);
+            // exact shortcuts: every corner outside -> sum1 = 0 (no
+            // contribution); every corner inside -> sum1 == sum2 (frac = 1)
+            const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
+            if (sqrt(mind2) >= radius) continue;
+            const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
+            if (!(sqrt(maxd2) < radius)) {
+              double sg[8];
+              sg[0] = radius - sqrt(dxm2 + dym2 + dzm2);
+              sg[1] = radius - sqrt(dxm2 + dyp2 + dzm2);
+              sg[2] = radius - sqrt(dxp2 + dyp2 + dzm2);
+              sg[3] = radius - sqrt(dxp2 + dym2 + dzm2);
+              sg[4] = radius - sqrt(dxm2 + dym2 + dzp2);
+              sg[5] = radius - sqrt(dxm2 + dyp2 + dzp2);
+              sg[6] = radius - sqrt(dxp2 + dyp2 + dzp2);
+              sg[7] = radius - sqrt(dxp2 + dym2 + dzp2);
+              double sum1 = 0., sum2 = 0.;
+              for (int cp = 0; cp < 8; ++cp) {
+                if (sg[cp] > 0.) sum1 = sum1 + sg[cp];
+                sum2 = sum2 + fabs(sg[cp]);
+              }
+              frac = sum1 / sum2;
+            }
+          }
+          const double f = (double)F[fidx(g, i - 1, j - 1, k)];
+          if (type == 1) {
+            acc[comp] += full ? dVeul : frac * dVeul;
+          } else {
+            if (type == 2 || type == 23) acc[comp] += full ? f * dVeul : f * frac * dVeul;
+            if (type == 3 || type == 23) {
+              const double rx = 0. + (i - 0.5) * dx - cx;
+              const double ry = 0. + (j - 0.5) * dy - cy;
+              const double rz = (k - 0.5) * dz - cz;
+              const int o = (type == 23) ? 3 : 0;
+              if (comp == 0) {
+                if (full) { acc[o + 1] = acc[o + 1] + rz * f * dVeul; acc[o + 2] = acc[o + 2] - ry * f * dVeul; }
+                else { acc[o + 1] = acc[o + 1] + rz * f * frac * dVeul; acc[o + 2] = acc[o + 2] - ry * f * frac * dVeul; }
+              } else if (comp == 1) {
+                if (full) { acc[o + 0] = acc[o + 0] - rz * f * dVeul; acc[o + 2] = acc[o + 2] + rx * f * dVeul; }
+                else { acc[o + 0] = acc[o + 0] - rz * f * frac * dVeul; acc[o + 2] = acc[o + 2] + rx * f * frac * dVeul; }
+              } else {
+                if (full) { acc[o + 0] = acc[o + 0] + ry * f * dVeul; acc[o + 1] = acc[o + 1] - rx * f * dVeul; }
+                else { acc[o + 0] = acc[o + 0] + ry * f * frac * dVeul; acc[o + 1] = acc[o + 1] - rx * f * frac * dVeul; }
+              }
+            }
+          }
+        }
+      }
+    }
+    for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o)
+        for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0)
+      for (int q = 0; q < 6; ++q) cps[nbrecv][q] = red[q][0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int n = 0; n <= 8; ++n)
+      for (int q = 0; q < 6; ++q) tot[q] = tot[q] + cps[n][q];
+    if (type == 1) {
+      b.red[p] = tot[0];  // volume of the u-cells (intgr_over_sphere.f90:607-622)
+      PF(PF_INTU) = tot[0]; PF(PF_INTV) = tot[1]; PF(PF_INTW) = tot[2];
+    } else if (type == 2) {
+      PF(PF_INTU) = tot[0]; PF(PF_INTV) = tot[1]; PF(PF_INTW) = tot[2];
+    } else if (type == 3) {
+      PF(PF_INTOMX) = tot[0]; PF(PF_INTOMY) = tot[1]; PF(PF_INTOMZ) = tot[2];
+    } else {
+      PF(PF_INTU) = tot[0]; PF(PF_INTV) = tot[1]; PF(PF_INTW) = tot[2];
+      PF(PF_INTOMX) = tot[3]; PF(PF_INTOMY) = tot[4]; PF(PF_INTOMZ) = tot[5];
+    }
+  }
+}
+
+template <typename T>
+void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,
+                             const T *w, int type) {
+  if (pg.np == 0) return;
+  k_sphere_int<T><<<pg.np, 256, 0, s>>>(g, pg, b, u, v, w, type);
+}
+template void launch_sphere_integrals<double>(cudaStream_t, const Geo &, const PartGeo &, PartBuffers,
+                                              const double *, const double *, const double *, int);
+template void launch_sphere_integrals<float>(cudaStream_t, const Geo &, const PartGeo &, PartBuffers, const float *,
+                                             const float *, const float *, int);
+
+// ---------------------------------------------------------------------------
+// collisions / lubrication (collisions.f90).  Only the normal contact force
+// and the normal lubrication force are applied (collisions.f90:199-205,
+// 430-432); the tangential history is still evolved and stored.
+// ---------------------------------------------------------------------------
+__device__ void d_lubrication(const PartGeo &pg, double pu, double pv, double pw, int idq, double nx, double ny,
+                              double nz, double eps, double u_nb, double v_nb, double w_nb, double &cfx, double &cfy,
+                              double &cfz) {
+  const double u1a = pu * nx + pv * ny + pw * nz;
+  const double u1b = u_nb * nx + v_nb * ny + w_nb * nz;
+  double f1;
+  if (idq > pg.np) {
+    double a11;
+    if (eps < 0.001) a11 = pg.a11_sat_pw;
+    else a11 = -(1. / eps) + 1. / 5. * log(eps) + 1. / 21. * eps * log(eps) - .9713;
+    f1 = (a11 * u1a);
+    f1 = pg.coeff_f * (f1 - (pg.a11_ini_pw * u1a));
+  } else {
+    double a11a, a11b;
+    if (eps < 0.001) { a11a = pg.a11a_sat_pp; a11b = pg.a11b_sat_pp; }
+    else {
+      const double a11 = -(1. / 4. * pow(eps, -1.)) + 9. / 40. * log(eps) + 3. / 112. * eps * log(eps);
+      a11a = a11 - .995;
+      a11b = -a11 + .350;
+    }
+    f1 = (a11a * u1a + a11b * u1b);
+    f1 = pg.coeff_f * (f1 - (pg.a11a_ini_pp * u1a + pg.a11b_ini_pp * u1b));
+  }
+  cfx = cfx + f1 * nx;
+  cfy = cfy + f1 * ny;
+  cfz = cfz + f1 * nz;
+}
+
+struct PState {  // the particle's own state held in registers by the collision thread
+  double u, v, w, omx, omy, omz, colfx, colfy, colfz;
+};
+
+__device__ void d_collisions(const PartGeo &pg, PartBuffers &b, int p, PState &S, int qq, int idq, double dist,
+                             double deltax, double deltay, double deltaz, double u_nb, double v_nb, double w_nb,
+                             double omx_nb, double omy_nb, double omz_nb, double dtsub, double rkab) {
+  const int np = pg.np, nq = pg.nq;
+  const double radius = pg.radius;
+  const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
+  double deltan, kn, etan, kt, etat, muc;
+  if (idq <= np) {
+    deltan = 2 * radius - dist; kn = pg.kn_ss; kt = pg.kt_ss; etan = pg.etan_ss; etat = pg.etat_ss; muc = pg.muc_ss;
+  } else {
+    deltan = radius - dist; kn = pg.kn_sw; kt = pg.kt_sw; etan = pg.etan_sw; etat = pg.etat_sw; muc = pg.muc_sw;
+  }
+  const double dun = (S.u + (S.omy * radius * nz) - (S.omz * radius * ny)) -
+                     (u_nb + (omy_nb * radius * (-nz)) - (omz_nb * radius * (-ny)));
+  const double dvn = (S.v - (S.omx * radius * nz) + (S.omz * radius * nx)) -
+                     (v_nb - (omx_nb * radius * (-nz)) + (omz_nb * radius * (-nx)));
+  const double dwn = (S.w + (S.omx * radius * ny) - (S.omy * radius * nx)) -
+                     (w_nb + (omx_nb * radius * (-ny)) - (omy_nb * radius * (-nx)));
+  const double vabs = dun * nx + dvn * ny + dwn * nz;
+  const double fxn = -(kn * (deltan * nx)) - etan * (vabs * nx);
+  const double fyn = -(kn * (deltan * ny)) - etan * (vabs * ny);
+  const double fzn = -(kn * (deltan * nz)) - etan * (vabs * nz);
+  const double dut = dun - vabs * nx, dvt = dvn - vabs * ny, dwt = dwn - vabs * nz;
+  const double vtabs = sqrt(dut * dut + dvt * dvt + dwt * dwt);
+  const int q = qq - 1;
+  const double odx = CFA(CF_ODX, q), ody = CFA(CF_ODY, q), odz = CFA(CF_ODZ, q);
+  const double distold = sqrt(odx * odx + ody * ody + odz * odz);
+  double nxold, nyold, nzold;
+  if (distold == 0) { nxold = nx; nyold = ny; nzold = nz; }
+  else { nxold = odx / distold; nyold = ody / distold; nzold = odz / distold; }
+  double dxt, dyt, dzt;
+  if (b.firstc[(long)p * nq + q] == idq) {
+    double hx = ny * nzold - nyold * nz;
+    double hy = nz * nxold - nzold * nx;
+    double hz = nx * nyold - nxold * ny;
+    const double aa = sqrt(hx * hx + hy * hy + hz * hz);
+    const double cc = cos(asin(aa));
+    const double bb = 1. - cc;
+    if (aa == 0.) { hx = 0.; hy = 0.; hz = 0.; }
+    else { hx = hx / aa; hy = hy / aa; hz = hz / aa; }
+    const double h11 = bb * (hx * hx) + cc, h12 = bb * hx * hy - aa * hz, h13 = bb * hx * hz + aa * hy;
+    const double h21 = bb * hx * hy + aa * hz, h22 = bb * (hy * hy) + cc, h23 = bb * hy * hz - aa * hx;
+    const double h31 = bb * hx * hz - aa * hy, h32 = bb * hy * hz + aa * hx, h33 = bb * (hz * hz) + cc;
+    const double oxt = CFA(CF_ODXT, q), oyt = CFA(CF_ODYT, q), ozt = CFA(CF_ODZT, q);
+    const double out_ = CFA(CF_ODUT, q), ovt = CFA(CF_ODVT, q), owt = CFA(CF_ODWT, q);
+    dxt = oxt * h11 + oyt * h21 + ozt * h31 + 0.5 * dtsub * rkab * (dut + out_ * h11 + ovt * h21 + owt * h31);
+    dyt = oxt * h12 + oyt * h22 + ozt * h32 + 0.5 * dtsub * rkab * (dvt + out_ * h12 + ovt * h22 + owt * h32);
+    dzt = oxt * h13 + oyt * h23 + ozt * h33 + 0.5 * dtsub * rkab * (dwt + out_ * h13 + ovt * h23 + owt * h33);
+  } else {
+    CFA(CF_PSI, q) = vtabs / fabs(vabs);
+    dxt = 0.; dyt = 0.; dzt = 0.;
+  }
+  double fxt = -(kt * dxt) - (etat * dut);
+  double fyt = -(kt * dyt) - (etat * dvt);
+  double fzt = -(kt * dzt) - (etat * dwt);
+  const double fnabs = sqrt(fxn * fxn + fyn * fyn + fzn * fzn);
+  double ftabs = sqrt(fxt * fxt + fyt * fyt + fzt * fzt);
+  const double tx = -fxt / ftabs, ty = -fyt / ftabs, tz = -fzt / ftabs;
+  if (!(ftabs <= muc * fnabs)) {
+    dxt = muc * fnabs * tx / kt;
+    dyt = muc * fnabs * ty / kt;
+    dzt = muc * fnabs * tz / kt;
+  }
+  S.colfx = S.colfx + fxn;
+  S.colfy = S.colfy + fyn;
+  S.colfz = S.colfz + fzn;
+  CFA(CF_DX, q) = deltax; CFA(CF_DY, q) = deltay; CFA(CF_DZ, q) = deltaz;
+  CFA(CF_DXT, q) = dxt; CFA(CF_DYT, q) = dyt; CFA(CF_DZT, q) = dzt;
+  CFA(CF_DUT, q) = dut; CFA(CF_DVT, q) = dvt; CFA(CF_DWT, q) = dwt;
+}
+
+__device__ void d_remove_contact(const PartGeo &pg, PartBuffers &b, int p, int i, int &qlast) {
+  const int np = pg.np, nq = pg.nq;
+  const int a = i - 1, l = qlast - 1;
+  int *fc = b.firstc + (long)p * nq, *ofc = b.ofirstc + (long)p * nq;
+  if (qlast > 1) {
+    fc[a] = fc[l];
+    for (int f : {CF_DXT, CF_DYT, CF_DZT, CF_DUT, CF_DVT, CF_DWT}) CFA(f, a) = CFA(f, l);
+    ofc[a] = ofc[l];
+    for (int f : {CF_ODXT, CF_ODYT, CF_ODZT, CF_ODUT, CF_ODVT, CF_ODWT}) CFA(f, a) = CFA(f, l);
+  }
+  fc[l] = 0;
+  ofc[l] = 0;
+  for (int f = CF_DX; f <= CF_DWT; ++f) CFA(f, l) = 0.;
+  for (int f = CF_ODX; f <= CF_ODWT; ++f) CFA(f, l) = 0.;
+  qlast = qlast - 1;
+}
+__device__ void d_new_contact(const PartGeo &pg, PartBuffers &b, int p, int slot) {
+  const int np = pg.np, nq = pg.nq;
+  const int s = slot - 1;
+  for (int f = CF_DX; f <= CF_DWT; ++f) CFA(f, s) = 0.;
+  for (int f = CF_ODX; f <= CF_ODWT; ++f) CFA(f, s) = 0.;
+}
+
+// position of particle copy nb in the collision loop on one rank
+// (intgr_nwtn_eulr.f90:223-322, coords=(0,0), dims=(1,1))
+__device__ __forceinline__ void copy_shift_coll(int nb, double lx, double ly, double &x, double &y) {
+  const double boundleftnb = lx, boundrightnb = 0., boundbacknb = 0., boundfrontnb = ly;
+  switch (nb) {
+    case 1: if (x < boundleftnb) x = x + lx; break;
+    case 2: if (x < boundleftnb) x = x + lx; if (y > boundbacknb) y = y - ly; break;
+    case 3: if (y > boundbacknb) y = y - ly; break;
+    case 4: if (x > boundrightnb) x = x - lx; if (y > boundbacknb) y = y - ly; break;
+    case 5: if (x > boundrightnb) x = x - lx; break;
+    case 6: if (x > boundrightnb) x = x - lx; if (y < boundfrontnb) y = y + ly; break;
+    case 7: if (y < boundfrontnb) y = y + ly; break;
+    case 8: if (x < boundleftnb) x = x + lx; if (y < boundfrontnb) y = y + ly; break;
+    default: break;
+  }
+}
+__device__ __forceinline__ double minimg(double a0, double a1, double a2) {
+  double m = a0;
+  if (fabs(a1) < fabs(m)) m = a1;
+  if (fabs(a2) < fabs(m)) m = a2;
+  return m;
+}
+
+#define COLL_WARPS 4
+#define COLL_CAP 64
+
+// snapshot of the collision iteration (anb(:,0), intgr_nwtn_eulr.f90:153-206)
+__global__ void k_snapshot(PartGeo pg, PartBuffers b) {
+  const int np = pg.np;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const bool m = b.mslv[p] > 0;
+  PF(PF_SX) = m ? PF(PF_X) : 0.; PF(PF_SY) = m ? PF(PF_Y) : 0.; PF(PF_SZ) = m ? PF(PF_Z) : 0.;
+  PF(PF_SU) = m ? PF(PF_U) : 0.; PF(PF_SV) = m ? PF(PF_V) : 0.; PF(PF_SW) = m ? PF(PF_W) : 0.;
+  PF(PF_SOMX) = m ? PF(PF_OMX) : 0.; PF(PF_SOMY) = m ? PF(PF_OMY) : 0.; PF(PF_SOMZ) = m ? PF(PF_OMZ) : 0.;
+}
+
+// One warp per particle: a coarse FP32 periodic-distance filter selects the
+// partners that can interact (lubrication range, contact, or listed in
+// firstc); lane 0 then walks them in the reference (nb, q) order, handles
+// the walls, integrates Newton-Euler and accumulates sumrk3.
+__global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, PartBuffers b, int iter, int rkiter,
+                                                                   double dt) {
+  __shared__ int cand[COLL_WARPS][COLL_CAP];
+  __shared__ int ncand[COLL_WARPS];
+  const int np = pg.np, nq = pg.nq;
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int p = blockIdx.x * COLL_WARPS + wid;
+  if (p >= np) return;
+  if (lane == 0) ncand[wid] = 0;
+  __syncwarp();
+  const double radius = pg.radius;
+  const int qmax0 = b.qmax[p];
+  const int *fc = b.firstc + (long)p * nq;
+  const float thr = 2.1f * (float)radius;
+  const float thr2 = thr * thr;
+  const float lxf = (float)pg.lx, lyf = (float)pg.ly;
+  const float pxf = (float)PF(PF_SX), pyf = (float)PF(PF_SY), pzf = (float)PF(PF_SZ);
+  for (int base = 0; base < np; base += 32) {
+    const int q = base + lane;
+    bool c = false;
+    if (q < np && q != p && b.mslv[q] > 0) {
+      float dxf = fabsf((float)b.pf[(long)PF_SX * np + q] - pxf);
+      float dyf = fabsf((float)b.pf[(long)PF_SY * np + q] - pyf);
+      const float dzf = (float)b.pf[(long)PF_SZ * np + q] - pzf;
+      dxf = fminf(dxf, fabsf(lxf - dxf));
+      dyf = fminf(dyf, fabsf(lyf - dyf));
+      c = dxf * dxf + dyf * dyf + dzf * dzf < thr2;
+      for (int i = 0; i < qmax0 && !c; ++i) c = (fc[i] == b.mslv[q]);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, c);
+    if (c) {
+      const int pos = ncand[wid] + __popc(m & ((1u << lane) - 1u));
+      if (pos < COLL_CAP) cand[wid][pos] = q;
+    }
+    __syncwarp();
+    if (lane == 0) ncand[wid] += __popc(m);
+    __syncwarp();
+  }
+  if (lane != 0) return;
+  int nc = ncand[wid];
+  if (nc > COLL_CAP) { atomicExch(&b.err[0], 1); nc = COLL_CAP; }
+  if (b.mslv[p] <= 0) return;
+  const int idp = b.mslv[p];
+  const double rkab = pg.rkab[rkiter - 1];
+  const int itermax = 1;
+  PState S;
+  S.u = PF(PF_U); S.v = PF(PF_V); S.w = PF(PF_W); S.omx = PF(PF_OMX); S.omy = PF(PF_OMY); S.omz = PF(PF_OMZ);
+  S.colfx = 0.; S.colfy = 0.; S.colfz = 0.;
+  const double px = PF(PF_X), py = PF(PF_Y), pz = PF(PF_Z);
+  int qlast = b.qmax[p];
+  int *fcw = b.firstc + (long)p * nq, *ofcw = b.ofirstc + (long)p * nq;
+  // (i) other particles, nb-outer / q-inner as in the reference
+  for (int nb = 0; nb < pg.nb_copies; ++nb) {
+    for (int ci = 0; ci < nc; ++ci) {
+      const int q = cand[wid][ci];
+      if (idp == b.mslv[q]) continue;
+      if (!(b.mslv[q] > 0)) continue;
+      const int idq = b.mslv[q];
+      double qx = b.pf[(long)PF_SX * np + q], qy = b.pf[(long)PF_SY * np + q];
+      const double qz = b.pf[(long)PF_SZ * np + q];
+      copy_shift_coll(nb, pg.lx, pg.ly, qx, qy);
+      const double deltaz = qz - pz;
+      const double deltax = minimg(qx - px, qx - pg.lx - px, qx + pg.lx - px);
+      const double deltay = minimg(qy - py, qy - pg.ly - py, qy + pg.ly - py);
+      const double dist = sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
+      const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
+      const double eps = (dist - 2. * radius) / radius;
+      const double qu = b.pf[(long)PF_SU * np + q], qv = b.pf[(long)PF_SV * np + q], qw = b.pf[(long)PF_SW * np + q];
+      if ((eps < 0.025) && (eps > 0.))
+        d_lubrication(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, qu, qv, qw, S.colfx, S.colfy, S.colfz);
+      int qq = 0;
+      const int qm = b.qmax[p];
+      for (int i = 1; i <= qm; ++i) {
+        if (idq == fcw[i - 1]) {
+          if (dist < (2. * radius)) {
+            qq = i;
+            d_collisions(pg, b, p, S, qq, idq, dist, deltax, deltay, deltaz, qu, qv, qw,
+                         b.pf[(long)PF_SOMX * np + q], b.pf[(long)PF_SOMY * np + q], b.pf[(long)PF_SOMZ * np + q],
+                         dt, rkab);
+          } else if (iter == itermax) {
+            d_remove_contact(pg, b, p, i, qlast);
+          }
+        }
+      }
+      if (qq == 0 && dist < (2. * radius)) {
+        qlast = qlast + 1;
+        if (qlast > nq) { atomicExch(&b.err[1], 1); qlast = nq; continue; }
+        qq = qlast;
+        d_new_contact(pg, b, p, qq);
+        d_collisions(pg, b, p, S, qq, idq, dist, deltax, deltay, deltaz, qu, qv, qw,
+                     b.pf[(long)PF_SOMX * np + q], b.pf[(long)PF_SOMY * np + q], b.pf[(long)PF_SOMZ * np + q],
+                     dt, rkab);
+        fcw[qlast - 1] = idq;
+        ofcw[qlast - 1] = idq;
+      }
+      b.qmax[p] = qlast;
+    }
+  }
+  // (ii) walls (intgr_nwtn_eulr.f90:503-603)
+  const int botw = np + 1, topw = np + 2;
+  const int qm_w = b.qmax[p];
+  for (int qw_ = botw; qw_ <= topw; ++qw_) {
+    const int idq = qw_;
+    const double deltax = 0., deltay = 0., deltaz = (qw_ - botw) * pg.lz - pz;
+    const double dist = sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
+    const double deltan = radius - dist;
+    const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
+    int qq = 0;
+    const double eps = -deltan / radius;
+    if ((eps < 0.075) && (eps > 0.))
+      d_lubrication(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, 0., 0., 0., S.colfx, S.colfy, S.colfz);
+    for (int i = 1; i <= qm_w; ++i) {
+      if (idq == fcw[i - 1]) {
+        qq = i;
+        if (dist < radius) {
+          d_collisions(pg, b, p, S, qq, idq, dist, deltax, deltay, deltaz, 0., 0., 0., 0., 0., 0., dt, rkab);
+        } else if (iter == itermax) {
+          d_remove_contact(pg, b, p, i, qlast);
+        }
+      }
+    }
+    if ((qq == 0) && (dist < radius)) {
+      qlast = qlast + 1;
+      if (qlast > nq) { atomicExch(&b.err[1], 1); qlast = nq; continue; }
+      qq = qlast;
+      d_new_contact(pg, b, p, qq);
+      d_collisions(pg, b, p, S, qq, idq, dist, deltax, deltay, deltaz, 0., 0., 0., 0., 0., 0., dt, rkab);
+      fcw[qlast - 1] = idq;
+      ofcw[qlast - 1] = idq;
+    }
+  }
+  b.qmax[p] = qlast;
+  // Newton-Euler (intgr_nwtn_eulr.f90:611-667); colflg is reset to 0 first
+  const double colflgx = 0., colflgy = 0., colflgz = 0.;
+  const double vol = pg.volp, rr = pg.ratiorho;  // ap%vol, ap%ratiorho (coordsfp.f90:96-102)
+  const double vr = vol * rr;
+  const double ou = PF(PF_OU), ov = PF(PF_OV), ow = PF(PF_OW);
+  double nu = ou + (1 - colflgx) * ((-1.) * dt * (PF(PF_FXLTOT)) / vr + (PF(PF_INTU) - PF(PF_OINTU)) / vr) +
+              rkab * dt * pg.gacc[0] * (1. - (1. / rr)) + rkab * 0.5 * dt * (S.colfx + PF(PF_OCOLFX)) / vr;
+  PF(PF_X) = PF(PF_OX) + rkab * 0.5 * dt * (nu + ou);
+  double nv = ov + (1 - colflgy) * ((-1.) * dt * (PF(PF_FYLTOT)) / vr + (PF(PF_INTV) - PF(PF_OINTV)) / vr) +
+              rkab * dt * pg.gacc[1] * (1. - (1. / rr)) + rkab * 0.5 * dt * (S.colfy + PF(PF_OCOLFY)) / vr;
+  PF(PF_Y) = PF(PF_OY) + rkab * 0.5 * dt * (nv + ov);
+  double nw = ow + (1 - colflgz) * ((-1.) * dt * (PF(PF_FZLTOT)) / vr + (PF(PF_INTW) - PF(PF_OINTW)) / vr) +
+              rkab * dt * pg.gacc[2] * (1. - (1. / rr)) + rkab * 0.5 * dt * (S.colfz + PF(PF_OCOLFZ)) / vr;
+  PF(PF_Z) = PF(PF_OZ) + rkab * 0.5 * dt * (nw + ow);
+  PF(PF_U) = nu; PF(PF_V) = nv; PF(PF_W) = nw;
+  PF(PF_COLFX) = S.colfx; PF(PF_COLFY) = S.colfy; PF(PF_COLFZ) = S.colfz;
+  PF(PF_COLTX) = 0.; PF(PF_COLTY) = 0.; PF(PF_COLTZ) = 0.;
+  double omx, omy, omz;
+  if (pg.rotation) {
+    const double mr = pg.mominert * rr;
+    omx = PF(PF_OOMX) + (-1.) * dt * PF(PF_TQX) / mr + (PF(PF_INTOMX) - PF(PF_OINTOMX)) / mr +
+          rkab * 0.5 * dt * (PF(PF_COLTX) + PF(PF_OCOLTX)) / mr;
+    omy = PF(PF_OOMY) + (-1.) * dt * PF(PF_TQY) / mr + (PF(PF_INTOMY) - PF(PF_OINTOMY)) / mr +
+          rkab * 0.5 * dt * (PF(PF_COLTY) + PF(PF_OCOLTY)) / mr;
+    omz = PF(PF_OOMZ) + (-1.) * dt * PF(PF_TQZ) / mr + (PF(PF_INTOMZ) - PF(PF_OINTOMZ)) / mr +
+          rkab * 0.5 * dt * (PF(PF_COLTZ) + PF(PF_OCOLTZ)) / mr;
+  } else {
+    omx = 0.0; omy = 0.0; omz = 0.0;
+  }
+  PF(PF_OMX) = omx; PF(PF_OMY) = omy; PF(PF_OMZ) = omz;
+  const double phi = PF(PF_OPHI) + 0.5 * rkab * dt * (omz + PF(PF_OOMZ));
+  PF(PF_PHI) = phi;
+  const double omtheta = (omy * cos(phi)) - (omx * sin(phi));
+  PF(PF_OMTHETA) = omtheta;
+  PF(PF_THETA) = PF(PF_OTHETA) + rkab * 0.5 * dt * (omtheta + PF(PF_OOMTHETA));
+  // sumrk3 (intgr_nwtn_eulr.f90:1586-1669)
+  double *r = b.rkp + (long)p * RK_N;
+  if (rkiter == 1)
+    for (int t = 0; t < RK_N; ++t) r[t] = 0.;
+  const double dpdy_new = 0.;
+  r[RK_FX] = r[RK_FX] + (-1.) * PF(PF_FXLTOT) + (PF(PF_INTU) - PF(PF_OINTU)) / dt;
+  r[RK_FY] = r[RK_FY] + (-1.) * PF(PF_FYLTOT) + (PF(PF_INTV) - PF(PF_OINTV)) / dt;
+  r[RK_FZ] = r[RK_FZ] + (-1.) * PF(PF_FZLTOT) + (PF(PF_INTW) - PF(PF_OINTW)) / dt;
+  r[RK_TX] = r[RK_TX] + (-1.) * PF(PF_TQX) + (PF(PF_INTOMX) - PF(PF_OINTOMX)) / dt;
+  r[RK_TY] = r[RK_TY] + (-1.) * PF(PF_TQY) + (PF(PF_INTOMY) - PF(PF_OINTOMY)) / dt;
+  r[RK_TZ] = r[RK_TZ] + (-1.) * PF(PF_TQZ) + (PF(PF_INTOMZ) - PF(PF_OINTOMZ)) / dt;
+  r[RK_TT] = r[RK_TT] + (-1.) * (-dpdy_new * pg.dVlagr);
+  r[RK_CFX] = r[RK_CFX] + 0.5 * rkab * (S.colfx + PF(PF_OCOLFX));
+  r[RK_CFY] = r[RK_CFY] + 0.5 * rkab * (S.colfy + PF(PF_OCOLFY));
+  r[RK_CFZ] = r[RK_CFZ] + 0.5 * rkab * (S.colfz + PF(PF_OCOLFZ));
+  r[RK_CTX] = r[RK_CTX] + 0.5 * rkab * (PF(PF_COLTX) + PF(PF_OCOLTX));
+  r[RK_CTY] = r[RK_CTY] + 0.5 * rkab * (PF(PF_COLTY) + PF(PF_OCOLTY));
+  r[RK_CTZ] = r[RK_CTZ] + 0.5 * rkab * (PF(PF_COLTZ) + PF(PF_OCOLTZ));
+  r[RK_DUDT] = r[RK_DUDT] + (nu - ou) / dt;
+  r[RK_DVDT] = r[RK_DVDT] + (nv - ov) / dt;
+  r[RK_DWDT] = r[RK_DWDT] + (nw - ow) / dt;
+}
+
+void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt) {
+  if (pg.np == 0) return;
+  k_snapshot<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b);
+  k_collide_update<<<(pg.np + COLL_WARPS - 1) / COLL_WARPS, 32 * COLL_WARPS, 0, s>>>(pg, b, iter, rkiter, dt);
+}
+
+// ---------------------------------------------------------------------------
+// periodic correction (:702-714), neighbour flags (:1051-1090, one rank) and
+// new Lagrangian points with their rigid-body velocity (:1438-1485).
+// One block per particle; the compaction of points flagged `isout` keeps the
+// reference order.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_ne_finalize(PartGeo pg, PartBuffers b, IbmBuffers ib, int init) {
+  const int np = pg.np;
+  const int p = blockIdx.x;
+  __shared__ double sx, sy, sz, su, sv, sw, somx, somy, somz;
+  __shared__ int wcount[4];
+  __shared__ int base;
+  // init: 0 = after Newton-Euler, 1 = initial set-up (initparticles +
+  // coordsfp), 2 = Lagrangian points only (restart with given flags)
+  if (threadIdx.x == 0) {
+    if (init == 1) b.mslv[p] = p + 1;
+    double x = PF(PF_X), y = PF(PF_Y);
+    if (b.mslv[p] > 0 && init == 0) {
+      if (x > pg.lx) x = x - pg.lx;
+      if (x < 0.) x = x + pg.lx;
+      if (y > pg.ly) y = y - pg.ly;
+      if (y < 0.) y = y + pg.ly;
+      PF(PF_X) = x; PF(PF_Y) = y;
+    }
+    const double ro = pg.radius + pg.offset;
+    const double leftb = 0., rightb = pg.lx, frontb = 0., backb = pg.ly;
+    int *nbf = b.nb + (long)p * 9;
+    if (init != 2) {
+    for (int n = 0; n < 9; ++n) nbf[n] = 0;
+    double dist;
+    if (x > (rightb - ro)) nbf[1] = 1;
+    dist = sqrt((rightb - x) * (rightb - x) + (frontb - y) * (frontb - y));
+    if (fabs(dist) < ro) nbf[2] = 1;
+    if (y < (frontb + ro)) nbf[3] = 1;
+    dist = sqrt((leftb - x) * (leftb - x) + (frontb - y) * (frontb - y));
+    if (fabs(dist) < ro) nbf[4] = 1;
+    if (x < (leftb + ro)) nbf[5] = 1;
+    dist = sqrt((leftb - x) * (leftb - x) + (backb - y) * (backb - y));
+    if (fabs(dist) < ro) nbf[6] = 1;
+    if (y > (backb - ro)) nbf[7] = 1;
+    dist = sqrt((rightb - x) * (rightb - x) + (backb - y) * (backb - y));
+    if (fabs(dist) < ro) nbf[8] = 1;
+    }
+    if (init == 0) {
+      double *r = b.rkp + (long)p * RK_N;
+      r[RK_DOMX] = 0.; r[RK_DOMY] = 0.; r[RK_DOMZ] = 0.;
+    }
+    sx = x; sy = y; sz = PF(PF_Z); su = PF(PF_U); sv = PF(PF_V); sw = PF(PF_W);
+    somx = PF(PF_OMX); somy = PF(PF_OMY); somz = PF(PF_OMZ);
+    base = 0;
+  }
+  __syncthreads();
+  const int nl = pg.nl;
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  for (int l0 = 0; l0 < nl; l0 += blockDim.x) {
+    const int l = l0 + threadIdx.x;
+    bool keep = false;
+    double xfploc = 0, yfploc = 0, zfploc = 0;
+    if (l < nl && b.mslv[p] != 0) {
+      const double st = b.sincos[l], ct = b.sincos[nl + l], sp = b.sincos[2 * nl + l], cp = b.sincos[3 * nl + l];
+      xfploc = sx + pg.radfp * st * cp;
+      yfploc = sy + pg.radfp * st * sp;
+      zfploc = sz + pg.radfp * ct;
+      double isperiodx = 0., isperiody = 0.;
+      if (xfploc < 0. + 0.5 * pg.dx) isperiodx = 1.;
+      if (xfploc >= pg.lx + 0.5 * pg.dx) isperiodx = -1.;
+      if (yfploc < 0. + 0.5 * pg.dy) isperiody = 1.;
+      if (yfploc >= pg.ly + 0.5 * pg.dy) isperiody = -1.;
+      bool isout = false;
+      const double coorxfp = (xfploc + isperiodx * pg.lx - 0.) * pg.dxi;
+      if (fnint(coorxfp) < 1 || fnint(coorxfp) > pg.I) isout = true;
+      const double cooryfp = (yfploc + isperiody * pg.ly - 0.) * pg.dyi;
+      if (fnint(cooryfp) < 1 || fnint(cooryfp) > pg.J) isout = true;
+      keep = !isout;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wcount[wid] = __popc(m);
+    __syncthreads();
+    int off = base;
+    for (int q = 0; q < wid; ++q) off += wcount[q];
+    off += __popc(m & ((1u << lane) - 1u));
+    if (keep) {
+      const long t = (long)p * nl + off;
+      ib.xfp[t] = xfploc; ib.yfp[t] = yfploc; ib.zfp[t] = zfploc;
+      ib.ul[t] = su + somy * (zfploc - sz) - somz * (yfploc - sy);
+      ib.vl[t] = sv + somz * (xfploc - sx) - somx * (zfploc - sz);
+      ib.wl[t] = sw + somx * (yfploc - sy) - somy * (xfploc - sx);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) for (int q = 0; q < (int)(blockDim.x / 32); ++q) base += wcount[q];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ib.nla[p] = b.mslv[p] != 0 ? base : 0;
+}
+
+void launch_ne_finalize(cudaStream_t s, const PartGeo &pg, PartBuffers b, IbmBuffers ib, int init) {
+  if (pg.np == 0) return;
+  k_ne_finalize<<<pg.np, 128, 0, s>>>(pg, b, ib, init);
+}
+
+}  // namespace ibmk

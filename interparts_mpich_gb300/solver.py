@@ -1,0 +1,195 @@
+"""Host-side mirror of the reference driver API over the C ABI.
+
+IBMSolver exposes one method per reference subroutine of the hot path
+(rk1/rk2/rk3, the IBM forcing loop, the projection, intgr_nwtn_eulr, chkdiv,
+chkdt) with the reference's argument meaning.  Errors from the library raise
+IBMError with the library's message.  The CUDA library must be built
+(interparts_mpich_gb300.build.build()); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+from ._abi import ParticleState, bind, dptr
+from .cases import Case
+
+_LIB = None
+_FN = None
+
+
+class IBMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "_build" / "libibm_rk3.so"
+
+
+def load_library(path: str | Path | None = None):
+    """Load libibm_rk3.so (built in-tree).  Raises if it is missing."""
+    global _LIB, _FN
+    if _LIB is not None and path is None:
+        return _LIB, _FN
+    p = Path(path) if path else library_path()
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: run interparts_mpich_gb300.build.build() first")
+    lib = C.CDLL(str(p))
+    fn = bind(lib, "ibm_")
+    if path is None:
+        _LIB, _FN = lib, fn
+    return lib, fn
+
+
+class IBMSolver:
+    """One simulation context (fields + particles) on the current GPU."""
+
+    def __init__(self, case: Case, mode: int = _abi.IBM_MODE_PLAIN_FP64, backend=None):
+        self.case = case
+        if backend is None:
+            _, self.fn = load_library()
+        else:
+            self.fn = backend
+        self._params = case.params(mode)
+        self.ctx = self.fn["create"](C.byref(self._params))
+        if not self.ctx:
+            msg = self.fn["last_error"](None)
+            raise IBMError(_abi.IBM_E_INVALID, msg.decode() if msg else "create failed")
+        nq, nl, nc = C.c_int(), C.c_int(), C.c_int()
+        self._chk(self.fn["sizes"](self.ctx, C.byref(nq), C.byref(nl), C.byref(nc)))
+        self.nq, self.nl, self.ncells = nq.value, nl.value, nc.value
+
+    def _chk(self, st: int):
+        if st != _abi.IBM_OK:
+            msg = self.fn["last_error"](self.ctx)
+            raise IBMError(st, msg.decode() if msg else "")
+        return st
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.fn["destroy"](self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- state ------------------------------------------------------------------
+    def _field_arrays(self):
+        return [np.zeros(self.case.shape, order="F") for _ in range(7)]
+
+    def set_fields(self, u, v, w, p, durk=None, dvrk=None, dwrk=None):
+        arrs = [np.asfortranarray(a, np.float64) if a is not None else None for a in (u, v, w, p, durk, dvrk, dwrk)]
+        for a in arrs:
+            if a is not None and a.shape != self.case.shape:
+                raise ValueError(f"field shape {a.shape} != {self.case.shape}")
+        self._chk(self.fn["set_fields"](self.ctx, *[dptr(a) for a in arrs]))
+
+    def get_fields(self) -> dict[str, np.ndarray]:
+        arrs = self._field_arrays()
+        self._chk(self.fn["get_fields"](self.ctx, *[dptr(a) for a in arrs]))
+        return dict(zip(["u", "v", "w", "p", "durk", "dvrk", "dwrk"], arrs))
+
+    def get_intermediate(self) -> dict[str, np.ndarray]:
+        arrs = self._field_arrays()[:3]
+        self._chk(self.fn["get_intermediate"](self.ctx, *[dptr(a) for a in arrs]))
+        return dict(zip(["dudt", "dvdt", "dwdt"], arrs))
+
+    def set_particles(self, ps: ParticleState):
+        s = ps.struct()
+        self._chk(self.fn["set_particles"](self.ctx, C.byref(s)))
+
+    def get_particles(self, lagrangian: bool = True) -> ParticleState:
+        ps = ParticleState(self.case.np, self.nq, self.nl, lagrangian=lagrangian)
+        s = ps.struct()
+        self._chk(self.fn["get_particles"](self.ctx, C.byref(s)))
+        return ps
+
+    def init_particles(self) -> float:
+        vol = C.c_double()
+        self._chk(self.fn["init_particles"](self.ctx, C.byref(vol)))
+        return vol.value
+
+    def setup(self, fields: dict | None = None, particles: ParticleState | None = None) -> float:
+        """Cold start as program interpt does (main.f90:142-206)."""
+        f = fields or self.case.initial_fields()
+        self.set_fields(f["u"], f["v"], f["w"], f["p"], f.get("durk"), f.get("dvrk"), f.get("dwrk"))
+        ps = particles or self.case.initial_particles(lagrangian=False)
+        self.set_particles(ps)
+        return self.init_particles()
+
+    # ---- reference subroutines -------------------------------------------------------
+    def rk(self, rkiter: int, dt: float):
+        """rk1/rk2/rk3 (rk3.f90:13-329)."""
+        self._chk(self.fn["rk_predict"](self.ctx, rkiter, dt))
+
+    def forcing_loop(self, dt: float, nl_iter: int = 3):
+        """IBM loop of the driver (main.f90:286-338)."""
+        self._chk(self.fn["forcing_loop"](self.ctx, dt, nl_iter))
+
+    def project(self, rkiter: int, dt: float):
+        """fillps, solver2d, correc and pnew += p (main.f90:356-372)."""
+        self._chk(self.fn["project"](self.ctx, rkiter, dt))
+
+    def intgr_nwtn_eulr(self, rkiter: int, dt: float):
+        """intgr_nwtn_eulr (intgr_nwtn_eulr.f90:12-1514)."""
+        self._chk(self.fn["newton_euler"](self.ctx, rkiter, dt))
+
+    def rk3_step(self, dt: float):
+        self._chk(self.fn["rk3_step"](self.ctx, dt))
+
+    def run(self, dt: float, nsteps: int):
+        self._chk(self.fn["run"](self.ctx, dt, nsteps))
+
+    def timed_step(self, dt: float) -> list[float]:
+        self._chk(self.fn["timed_step"](self.ctx, dt))
+        ms = (C.c_double * 4)()
+        self._chk(self.fn["phase_times"](self.ctx, ms))
+        return list(ms)
+
+    def chkdiv(self) -> tuple[float, float, tuple[int, int, int]]:
+        tot, mx = C.c_double(), C.c_double()
+        ijk = (C.c_int * 3)()
+        st = self.fn["chkdiv"](self.ctx, C.byref(tot), C.byref(mx), ijk)
+        if st not in (_abi.IBM_OK, _abi.IBM_E_DIVERGENCE):
+            self._chk(st)
+        return tot.value, mx.value, tuple(ijk)
+
+    def chkdt(self) -> float:
+        d = C.c_double()
+        self._chk(self.fn["chkdt"](self.ctx, C.byref(d)))
+        return d.value
+
+    def slip_residual(self) -> tuple[float, float]:
+        mx, rms = C.c_double(), C.c_double()
+        self._chk(self.fn["slip_residual"](self.ctx, C.byref(mx), C.byref(rms)))
+        return mx.value, rms.value
+
+    def diagnostics(self) -> dict:
+        wn, wo = C.c_double(), C.c_double()
+        ft = (C.c_double * 3)()
+        self._chk(self.fn["diagnostics"](self.ctx, C.byref(wn), C.byref(wo), ft))
+        return {"wallshearnew": wn.value, "wallshearold": wo.value, "forcetot": list(ft)}
+
+    def set_stream(self, stream_handle: int | None):
+        self._chk(self.fn["set_stream"](self.ctx, C.c_void_p(stream_handle or 0)))
+
+    def launch_count(self) -> int:
+        return int(self.fn["launch_count"](self.ctx)) if "launch_count" in self.fn else 0
+
+    def sync(self):
+        if "sync" in self.fn:
+            self._chk(self.fn["sync"](self.ctx))
