@@ -1,0 +1,119 @@
+"""Pins of the CPU oracle against the reference's own invariants and known
+values (the reference ships no golden outputs for this path):
+
+* kerneltest: integral of the 3-point delta = 1 (kernel.f90:43-63, printed
+  by main.f90:145-146);
+* the regularised delta's values and moments (kernel.f90:7-25);
+* nl = nlmax of the shipped case tests/1003 (gridsize: nlmax=55 for
+  radius 0.005, 128 cells on lx=0.27) and 746 for D = 16 dx
+  (init.f90:127-129, checked at main.f90:118-132);
+* VFFTPACK semantics documented in fft.f:693-760 (forward) and fft.f:1-80
+  (backward): half-complex layout, sqrt(1/N) scaling, backward(forward) = id;
+* sphere volume check of intgr_over_sphere(1) (intgr_over_sphere.f90:607-622);
+* divergence after the projection (chkdiv.f90:7-61);
+* master-count conservation (intgr_nwtn_eulr.f90:1384-1396);
+* the committed golden fixture (tests/golden/make_golden.py).
+"""
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from interparts_mpich_gb300.cases import Case, derived_nl
+from oracle.oracle import OracleSolver, load
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return load()[0]
+
+
+def test_kerneltest(lib):
+    s = lib.orc_kerneltest()
+    assert abs(s - 1.0) < 1e-6, s
+
+
+def test_kernel_values_and_moments(lib):
+    k = lib.orc_kernel
+    assert k(0.0) == pytest.approx(2.0 / 3.0, abs=1e-16)
+    assert k(0.5) == pytest.approx(0.5, abs=1e-16) and k(-0.5) == pytest.approx(0.5, abs=1e-16)
+    assert k(1.5) == 0.0 and k(-1.7) == 0.0
+    rng = np.random.default_rng(0)
+    for x in rng.uniform(-0.5, 0.5, 50):
+        js = np.arange(-3, 4)
+        w = np.array([k(x - j) for j in js])
+        assert abs(w.sum() - 1.0) < 1e-14
+        assert abs(np.sum((x - js) * w)) < 1e-14
+
+
+def test_nl_pins(lib):
+    assert lib.orc_nl(0.005, 128 / 0.27) == 55      # tests/1003: gridsize nlmax = 55
+    assert lib.orc_nl(8.0 / 256, 256.0) == 746      # D = 16 dx
+    assert derived_nl(0.005, 128 / 0.27) == 55
+    assert derived_nl(8.0 / 256, 256.0) == 746
+
+
+@pytest.mark.parametrize("n", [8, 12, 16, 24])
+def test_vrfft_semantics(lib, n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n)
+    r = x.copy()
+    lib.orc_vrfft(r.ctypes.data_as(C.POINTER(C.c_double)), n, 1)
+    j = np.arange(n)
+    s = math.sqrt(1.0 / n)
+    assert r[0] == pytest.approx(s * x.sum(), abs=1e-13)
+    for k in range(1, (n - 1) // 2 + 1):
+        assert r[2 * k - 1] == pytest.approx(s * np.sum(x * np.cos(2 * np.pi * j * k / n)), abs=1e-13)
+        assert r[2 * k] == pytest.approx(-s * np.sum(x * np.sin(2 * np.pi * j * k / n)), abs=1e-13)
+    if n % 2 == 0:
+        assert r[n - 1] == pytest.approx(s * np.sum(x * (-1.0) ** j), abs=1e-13)
+    lib.orc_vrfft(r.ctypes.data_as(C.POINTER(C.c_double)), n, -1)
+    assert np.max(np.abs(r - x)) < 1e-13
+
+
+def test_sphere_volume():
+    errs = []
+    for n in (32, 64):
+        c = Case(name="vol", itot=n, jtot=n, ktot=n, radius=8.0 / 64, np=1, flow="pur", perturb=0.0,
+                 centres=np.array([[0.5, 0.5, 0.5]]))
+        vol = OracleSolver(c).setup()
+        exact = 4.0 / 3.0 * math.pi * c.radius ** 3
+        errs.append(abs(vol - exact) / exact)
+    assert errs[1] < 0.01            # D = 16 dx: within 1 %
+    assert errs[1] < errs[0]         # converges with resolution
+
+
+def small(n=24, nsp=3, seed=5):
+    return Case(name="pin", itot=n, jtot=n, ktot=n, radius=3.0 / n, np=nsp, visc=1.0 / 400.0, seed=seed)
+
+
+def test_projection_divergence_and_masters():
+    c = small()
+    o = OracleSolver(c)
+    o.setup()
+    dt = 0.5 * o.chkdt()
+    o.run(dt, 2)
+    tot, mx, _ = o.chkdiv()
+    assert mx < 1e-11 and abs(tot) < 1e-10
+    ps = o.get_particles()
+    assert np.array_equal(ps.mslv, np.arange(1, c.np + 1))
+
+
+def test_golden_fixture():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    ref = np.load(GOLDEN / "oracle_small.npz")
+    out = mg.generate()
+    for k in ref.files:
+        a, b = out[k], ref[k]
+        if a.dtype.kind in "iu":
+            assert np.array_equal(a, b), k
+        else:
+            assert np.max(np.abs(a - b)) <= 1e-13 * max(1.0, np.max(np.abs(b))), k
