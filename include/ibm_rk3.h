@@ -198,6 +198,25 @@ long long ibm_launch_count(const ibm_ctx *ctx);
 /* Device synchronisation of the context stream. */
 int ibm_sync(ibm_ctx *ctx);
 
+/* --- allocation-free variant ------------------------------------------------ */
+
+/* chkdiv for callers that cannot allocate device memory (no counterpart in the
+ * reference).  A host program whose fields already live on the GPU under its
+ * own memory manager, that runs under a fixed device-memory budget, or that is
+ * at a point where cudaMalloc is not allowed passes its own device arrays u, v,
+ * w in the reference layout (0:itot+1, 0:jtot+1, 0:ktot+1), the inverse grid
+ * spacings, and a device output of 5 doubles {total divergence, max |div|,
+ * i, j, k of the maximum (1-based)}.  Work is queued on cuda_stream (NULL =
+ * default stream) and not synchronised.  The call allocates nothing: its
+ * per-plane partial sums live in a static device array of 4096 records
+ * (96 KiB, held by every GPU that loads the library), so ktot > 4096 returns
+ * IBM_E_INVALID.  All calls share that array: calls that overlap on the GPU
+ * race.  The first call on each device looks the array up with
+ * cudaGetSymbolAddress; make it before any stream capture. */
+int ibm_chkdiv_noalloc(const double *u, const double *v, const double *w,
+                       int itot, int jtot, int ktot, double dxi, double dyi, double dzi,
+                       double *out5, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

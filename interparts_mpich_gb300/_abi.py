@@ -148,6 +148,8 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "phase_times": (C.c_int, [ctx, c_double_p]),
         "launch_count": (C.c_longlong, [ctx]),
         "sync": (C.c_int, [ctx]),
+        "chkdiv_noalloc": (C.c_int, [c_double_p, c_double_p, c_double_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                     C.c_double, C.c_double, c_double_p, C.c_void_p]),
     }
     table = {}
     for name, (res, args) in list(sig.items()) + list(optional.items()):
