@@ -46,11 +46,13 @@ def barrier(ws):
 
 
 def max_over_ranks(x: float, ws: int) -> float:
+    """Max over the replicas (the slowest rank sets the job time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -146,30 +148,23 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
             "predictor": (10 + 13 + 10) * n * w, "projection": 3 * 21 * n * w}
 
 
-def run_ours(args, ws, rank, local):
+def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
+    """Times one arithmetic form on the channel case: K steps between CUDA
+    events on the library's stream, plus the per-phase times of one step."""
     import torch
 
     from interparts_mpich_gb300 import IBMSolver
-    from interparts_mpich_gb300 import build as b
     from interparts_mpich_gb300.cases import channel_case
 
-    torch.cuda.set_device(local)
-    if rank == 0 or ws > 1:
-        b.build()
-    barrier(ws)
     case = channel_case(args.n, args.np, seed=1234)
-    solver = IBMSolver(case)
+    solver = IBMSolver(case, mode=mode)
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
-    fields = case.initial_fields()
-    solver.setup(fields)
+    solver.setup(case.initial_fields())
     dt = 0.5 * solver.chkdt()  # frozen dt (0.5 dtmax at t=0, main.f90:151-154)
-    ncell = case.itot * case.jtot * case.ktot
-    # warm-up
     for _ in range(args.warmup):
         solver.rk3_step(dt)
     solver.sync()
-    # per-phase timing of one extra step (events inside the library)
     phases = solver.timed_step(dt)
     torch.cuda.synchronize()
     launches0 = solver.launch_count()
@@ -189,12 +184,11 @@ def run_ours(args, ws, rank, local):
     launches = solver.launch_count() - launches0
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
-    tot, divmax, _ = solver.chkdiv()
-
-    # end-to-end through the C ABI with host buffers: set u,v,w,p + particles
-    # from pinned host memory, one step, read u,v,w,p + particles back
+    _, divmax, _ = solver.chkdiv()
     e2e = None
-    if args.e2e_steps > 0:
+    if with_e2e and args.e2e_steps > 0:
+        # end to end through the C ABI with host buffers: u,v,w,p and the
+        # particle state from pinned host memory, one step, read back
         pin = {k: torch.empty(case.shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T for k in "uvwp"}
         cur = solver.get_fields()
         for k in "uvwp":
@@ -208,16 +202,15 @@ def run_ours(args, ws, rank, local):
             solver.set_fields(pin["u"], pin["v"], pin["w"], pin["p"])
             solver.set_particles(ps)
             solver.rk3_step(dt)
-            f = solver.get_fields()
+            solver.get_fields(out=pin)
             ps = solver.get_particles(lagrangian=True)
-            for k in "uvwp":
-                pin[k][...] = f[k]
         torch.cuda.synchronize()
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
         e2e = {"value": round(max_over_ranks(e2e_ms, ws), 4), "unit": "ms/step",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
     solver.close()
-    return case, dt, ms_max, phases, launches, clk.summary(), e2e, ncell, divmax
+    return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
+            "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax}
 
 
 def cpu_baseline(args, case_fn):
@@ -248,6 +241,7 @@ def main():
     ap.add_argument("--np", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -284,36 +278,55 @@ def main():
         print(json.dumps(line))
         return
 
-    case, dt, ms, phases, launches, clocks, e2e, ncell, divmax = run_ours(args, ws, rank, local)
+    import torch
+
+    from interparts_mpich_gb300 import IBM_MODE_MIXED, IBM_MODE_PLAIN_FP64
+    from interparts_mpich_gb300 import build as b
+
+    torch.cuda.set_device(local)
+    b.build()
+    barrier(ws)
+    forms = {"plain": IBM_MODE_PLAIN_FP64, "mixed": IBM_MODE_MIXED}
+    wanted = ["plain", "mixed"] if args.form == "both" else [args.form]
+    head = "mixed" if "mixed" in wanted else "plain"
+    res = {f: run_form(args, ws, rank, local, forms[f], with_e2e=(f == head)) for f in wanted}
     if rank != 0:
         return
+    r = res[head]
+    case = r["case"]
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
+    w = 8 if head == "plain" else 4
     ab = algorithmic_bytes(case)
-    # dominant phase roofline (per-phase CUDA-event times of one step)
     names = ["predictor", "ibm", "projection", "newton_euler"]
     byts = {"predictor": ab["predictor"], "ibm": ab["ibm"], "projection": ab["projection"],
             "newton_euler": ab["sphere"]}
+    phases = r["phases"]
     dom = max(range(4), key=lambda q: phases[q])
     achieved = byts[names[dom]] / (phases[dom] * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
-        "form": "plain FP64 (drop-in)",
-        "mcell_steps_per_s": round(args.gpus * ncell / (ms * 1e-3) / 1e6, 1),
-        "phases_ms": {n: round(t, 4) for n, t in zip(names, phases)},
-        "hbm_roofline_frac_step": round(ab["total"] / (ms * 1e-3) / 1e9 / hbm, 4),
-        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": hbm,
-                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
+        "metric": METRIC, "value": round(r["ms"], 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(r["ms"], 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if head == "plain" else "f32+f64", "data": "synthetic",
+        "config": config,
+        "form": {"plain": "plain FP64 (drop-in)", "mixed": "mixed FP32/FP64"}[head],
+        "forms": {f: {"ms_per_step": round(x["ms"], 4),
+                      "mcell_steps_per_s": round(args.gpus * x["ncell"] / (x["ms"] * 1e-3) / 1e6, 1),
+                      "phases_ms": {n: round(t, 4) for n, t in zip(names, x["phases"])},
+                      "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"])} for f, x in res.items()},
+        "mcell_steps_per_s": round(args.gpus * r["ncell"] / (r["ms"] * 1e-3) / 1e6, 1),
+        "hbm_roofline_frac_step": round(ab["total"] / (r["ms"] * 1e-3) / 1e9 / hbm, 4),
+        "roofline": {"bound": "hbm", "kernel": names[dom] + " phase", "achieved": round(achieved * w / 8, 1),
+                     "peak": hbm, "unit": "GB/s", "frac": round(achieved * w / 8 / hbm, 4), "traffic": None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800"},
-        "gpu_launches": int(launches),
-        "clocks": clocks,
-        "chkdiv_max": divmax,
-        "dt": dt,
+        "gpu_launches": int(r["launches"]),
+        "clocks": r["clocks"],
+        "dt": r["dt"],
     }
-    if e2e:
-        line["e2e"] = e2e
+    if "plain" in res and "mixed" in res:
+        line["speedup_mixed_vs_plain"] = round(res["plain"]["ms"] / res["mixed"]["ms"], 3)
+    if r["e2e"]:
+        line["e2e"] = r["e2e"]
     if not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args, lambda: channel_case(args.n, args.np, seed=1234))

@@ -88,14 +88,76 @@ __device__ C *fft_smem(C *a, C *b, int M, int nseq, int es, int ss, const FftPla
   return a;
 }
 
+// Compile-time specialisation of the same Stockham stages for the lengths
+// used by the configurations: the index arithmetic (divisions by the
+// butterfly count and the sub-transform size) becomes shifts and constant
+// multiplies.  Radix order as in the runtime plan: 4s, then 2, then 3.
+template <int M, int Ns, typename C>
+__device__ __forceinline__ C *fft_stages_ct(C *a, C *b, int nseq, int ss, const C *__restrict__ tw, int inv) {
+  if constexpr (Ns >= M) {
+    return a;
+  } else {
+    constexpr int rem = M / Ns;
+    constexpr int R = (rem % 4 == 0) ? 4 : ((rem % 2 == 0) ? 2 : 3);
+    constexpr int nb = M / R;
+    constexpr int twst = M / (Ns * R);
+    for (int t = threadIdx.x; t < nb * nseq; t += blockDim.x) {
+      const int sq = t / nb, jb = t - sq * nb;
+      const C *src = a + (long)sq * ss;
+      C *dst = b + (long)sq * ss;
+      const int kk = jb % Ns;
+      C v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        C x = src[jb + r * nb];
+        if (r > 0 && kk > 0) {
+          C wt = tw[kk * twst * r];
+          if (inv) wt = cconj(wt);
+          x = cmul(x, wt);
+        }
+        v[r] = x;
+      }
+      if constexpr (R == 2) dft2(v);
+      else if constexpr (R == 4) dft4(v, inv);
+      else dft3(v, inv);
+      const int idxD = (jb / Ns) * Ns * R + kk;
+#pragma unroll
+      for (int r = 0; r < R; ++r) dst[idxD + r * Ns] = v[r];
+    }
+    __syncthreads();
+    return fft_stages_ct<M, Ns * R, C>(b, a, nseq, ss, tw, inv);
+  }
+}
+
+// unit-stride sequences (es = 1); lengths without a specialisation use the
+// runtime plan
+template <typename C>
+__device__ C *fft_smem1(C *a, C *b, int M, int nseq, int ss, const FftPlan &pl, const C *__restrict__ tw, int inv) {
+  switch (M) {
+    case 16: return fft_stages_ct<16, 1, C>(a, b, nseq, ss, tw, inv);
+    case 24: return fft_stages_ct<24, 1, C>(a, b, nseq, ss, tw, inv);
+    case 32: return fft_stages_ct<32, 1, C>(a, b, nseq, ss, tw, inv);
+    case 48: return fft_stages_ct<48, 1, C>(a, b, nseq, ss, tw, inv);
+    case 64: return fft_stages_ct<64, 1, C>(a, b, nseq, ss, tw, inv);
+    case 96: return fft_stages_ct<96, 1, C>(a, b, nseq, ss, tw, inv);
+    case 128: return fft_stages_ct<128, 1, C>(a, b, nseq, ss, tw, inv);
+    case 192: return fft_stages_ct<192, 1, C>(a, b, nseq, ss, tw, inv);
+    case 256: return fft_stages_ct<256, 1, C>(a, b, nseq, ss, tw, inv);
+    case 384: return fft_stages_ct<384, 1, C>(a, b, nseq, ss, tw, inv);
+    case 512: return fft_stages_ct<512, 1, C>(a, b, nseq, ss, tw, inv);
+    case 768: return fft_stages_ct<768, 1, C>(a, b, nseq, ss, tw, inv);
+    default: return fft_smem<C>(a, b, M, nseq, 1, ss, pl, tw, inv);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // fillps + forward real FFT along x.  One CTA handles ROWS rows (j,k).
 // Reads the forced predictor (fu,fv,fw) with the bounduvw(dudt) wall values
 // w(0)=w(kmax)=0 applied (and stored back into fw plane K).
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(128) k_fillps_fftx(Geo g, FftPlan plx, const T *__restrict__ fu,
-                                                     const T *__restrict__ fv, T *__restrict__ fw,
+template <typename TIn, typename T, typename TA, bool DF = false>
+__global__ void __launch_bounds__(128) k_fillps_fftx(Geo g, FftPlan plx, const TIn *__restrict__ fu,
+                                                     const TIn *__restrict__ fv, TIn *__restrict__ fw,
                                                      typename cpx<T>::t *__restrict__ S,
                                                      const typename cpx<T>::t *__restrict__ twM,
                                                      const typename cpx<T>::t *__restrict__ twN, double dtidxi,
@@ -107,6 +169,10 @@ __global__ void __launch_bounds__(128) k_fillps_fftx(Geo g, FftPlan plx, const T
   C *B = A + rows * M;
   const int row0 = blockIdx.x * rows;
   const int nrow = g.J * g.K;
+  const float fx_hi = (float)dtidxi, fx_lo = (float)(dtidxi - (double)fx_hi);
+  const float fy_hi = (float)dtidyi, fy_lo = (float)(dtidyi - (double)fy_hi);
+  const float fz_hi = (float)dtidzi, fz_lo = (float)(dtidzi - (double)fz_hi);
+  (void)fx_lo; (void)fy_lo; (void)fz_lo;
   // 1. right-hand side, packed z_m = x_{2m} + i x_{2m+1}
   for (int t = threadIdx.x; t < rows * g.I; t += blockDim.x) {
     const int r = t / g.I, i = t - r * g.I;
@@ -115,18 +181,38 @@ __global__ void __launch_bounds__(128) k_fillps_fftx(Geo g, FftPlan plx, const T
     if (row < nrow) {
       const int j = row % g.J, k = row / g.J + 1;
       const long c = fidx(g, i, j, k);
-      const T wk = (k == g.K) ? (T)0 : fw[c];
-      const T wkm = fw[c - g.plane];  // plane 0 holds w(0)=0
-      if (k == g.K) fw[c] = (T)0;
-      const T vjm = fv[fidx(g, i, j == 0 ? g.J - 1 : j - 1, k)];
-      const T uim = fu[fidx(g, i == 0 ? g.I - 1 : i - 1, j, k)];
-      val = ((wk - wkm) * (T)dtidzi + (fv[c] - vjm) * (T)dtidyi + (fu[c] - uim) * (T)dtidxi);
+      if constexpr (DF) {
+        // divergence residual in double-float arithmetic: exact differences
+        // of the FP32 velocities, products with the split FP64 factors
+        const float wk = (k == g.K) ? 0.f : (float)fw[c];
+        const float wkm = (float)fw[c - g.plane];
+        if (k == g.K) fw[c] = (TIn)0;
+        const float vjm = (float)fv[fidx(g, i, j == 0 ? g.J - 1 : j - 1, k)];
+        const float uim = (float)fu[fidx(g, i == 0 ? g.I - 1 : i - 1, j, k)];
+        float dh, dl, th, tl, sh, sl;
+        two_sum(wk, -wkm, dh, dl);
+        df_mul(dh, dl, fz_hi, fz_lo, sh, sl);
+        two_sum((float)fv[c], -vjm, dh, dl);
+        df_mul(dh, dl, fy_hi, fy_lo, th, tl);
+        df_add(sh, sl, th, tl, sh, sl);
+        two_sum((float)fu[c], -uim, dh, dl);
+        df_mul(dh, dl, fx_hi, fx_lo, th, tl);
+        df_add(sh, sl, th, tl, sh, sl);
+        val = (T)(sh + sl);
+      } else {
+        const TA wk = (k == g.K) ? (TA)0 : (TA)fw[c];
+        const TA wkm = (TA)fw[c - g.plane];  // plane 0 holds w(0)=0
+        if (k == g.K) fw[c] = (TIn)0;
+        const TA vjm = (TA)fv[fidx(g, i, j == 0 ? g.J - 1 : j - 1, k)];
+        const TA uim = (TA)fu[fidx(g, i == 0 ? g.I - 1 : i - 1, j, k)];
+        val = (T)((wk - wkm) * (TA)dtidzi + ((TA)fv[c] - vjm) * (TA)dtidyi + ((TA)fu[c] - uim) * (TA)dtidxi);
+      }
     }
     T *Ar = reinterpret_cast<T *>(A + r * M);
     Ar[i] = val;
   }
   __syncthreads();
-  C *Z = fft_smem<C>(A, B, M, rows, 1, M, plx, twM, 0);
+  C *Z = fft_smem1<C>(A, B, M, rows, M, plx, twM, 0);
   // 2. unpack to X_k, k = 0..M  (X_k = E_k + W_N^k O_k)
   for (int t = threadIdx.x; t < rows * (M + 1); t += blockDim.x) {
     const int r = t / (M + 1), kx = t - r * (M + 1);
@@ -148,22 +234,25 @@ __global__ void __launch_bounds__(256) k_ffty(Geo g, FftPlan ply, typename cpx<T
                                               const typename cpx<T>::t *__restrict__ twJ, int cols, int inv) {
   typedef typename cpx<T>::t C;
   extern __shared__ unsigned char smraw[];
+  // each column is stored contiguously (row length J+1 to spread the banks),
+  // so the Stockham stages access shared memory with unit stride
+  const int LD = g.J + 1;
   C *A = reinterpret_cast<C *>(smraw);
-  C *B = A + g.J * cols;
+  C *B = A + LD * cols;
   const int kx0 = blockIdx.x * cols;
   const int k = blockIdx.y;
   C *plane = S + (long)k * g.J * g.MX;
   for (int t = threadIdx.x; t < g.J * cols; t += blockDim.x) {
     const int jy = t / cols, cx = t - jy * cols;
     const int kx = kx0 + cx;
-    A[jy * cols + cx] = (kx < g.MX) ? plane[(long)jy * g.MX + kx] : cmk<C>((T)0, (T)0);
+    A[cx * LD + jy] = (kx < g.MX) ? plane[(long)jy * g.MX + kx] : cmk<C>((T)0, (T)0);
   }
   __syncthreads();
-  C *Y = fft_smem<C>(A, B, g.J, cols, cols, 1, ply, twJ, inv);
+  C *Y = fft_smem1<C>(A, B, g.J, cols, LD, ply, twJ, inv);
   for (int t = threadIdx.x; t < g.J * cols; t += blockDim.x) {
     const int jy = t / cols, cx = t - jy * cols;
     const int kx = kx0 + cx;
-    if (kx < g.MX) plane[(long)jy * g.MX + kx] = Y[jy * cols + cx];
+    if (kx < g.MX) plane[(long)jy * g.MX + kx] = Y[cx * LD + jy];
   }
 }
 
@@ -172,6 +261,7 @@ __global__ void __launch_bounds__(256) k_ffty(Geo g, FftPlan ply, typename cpx<T
 template <typename T>
 __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__restrict__ S,
                                                 const double *__restrict__ zt, double a2, double scale) {
+  // the recurrence always runs in FP64 (also for an FP32 spectrum)
   typedef typename cpx<T>::t C;
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long ncol = (long)g.MX * g.J;
@@ -182,40 +272,67 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
   const double *z = zt + (long)kyy * g.MX + kx;
   const long sstride = (long)g.J * g.MX;
   C *s = S + t;
-  const T A2 = (T)a2;
-  // forward elimination
-  C prev = cscale(s[0], (T)scale);
-  {
-    const T z0 = (T)z[0];
-    prev = cscale(prev, z0);
-    s[0] = prev;
-  }
-  for (int k = 1; k < g.K - 1; ++k) {
-    const T zk = (T)z[k * zstride];
-    C cur = cscale(s[k * sstride], (T)scale);
-    cur = cscale(csub(cur, cscale(prev, A2)), zk);
-    s[k * sstride] = cur;
-    prev = cur;
-  }
-  {
-    const int k = g.K - 1;
-    const T den = (T)z[k * zstride];
-    C cur = cscale(s[k * sstride], (T)scale);
-    if (den != (T)0) {
-      cur = csub(cur, cscale(prev, A2));
-      cur = cmk<C>(cur.x / den, cur.y / den);
-    } else {
-      cur = cmk<C>((T)0, (T)0);
+  // The recurrence is a dependent chain over k; loads of the next planes
+  // are issued in groups of PF so that several are in flight at once.
+  constexpr int PF = 8;
+  auto ld = [&](int k) -> double2 { const C v = s[k * sstride]; return make_double2((double)v.x * scale, (double)v.y * scale); };
+  auto st = [&](int k, double2 v) { C o; o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; s[k * sstride] = o; };
+  const int K = g.K;
+  double2 prev = make_double2(0., 0.);
+  for (int k0 = 0; k0 < K; k0 += PF) {
+    double2 buf[PF];
+    double zb[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k0 + q;
+      if (k < K) { buf[q] = ld(k); zb[q] = z[(long)k * zstride]; }
     }
-    s[k * sstride] = cur;
-    prev = cur;
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k0 + q;
+      if (k >= K) break;
+      double2 cur = buf[q];
+      if (k == 0) {
+        cur = make_double2(cur.x * zb[q], cur.y * zb[q]);
+      } else if (k < K - 1) {
+        cur = make_double2((cur.x - a2 * prev.x) * zb[q], (cur.y - a2 * prev.y) * zb[q]);
+      } else {
+        const double den = zb[q];
+        if (den != 0.) cur = make_double2((cur.x - a2 * prev.x) / den, (cur.y - a2 * prev.y) / den);
+        else cur = make_double2(0., 0.);
+      }
+      buf[q] = cur;
+      prev = cur;
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q)
+      if (k0 + q < K) st(k0 + q, buf[q]);
   }
   // back substitution, d(k) = c(k)*z(k) with c(k) = dzi^2 for k < kmax
-  for (int k = g.K - 2; k >= 0; --k) {
-    const T d = A2 * (T)z[k * zstride];
-    C cur = csub(s[k * sstride], cscale(prev, d));
-    s[k * sstride] = cur;
-    prev = cur;
+  for (int k1 = K - 2; k1 >= 0; k1 -= PF) {
+    double2 buf[PF];
+    double zb[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k1 - q;
+      if (k >= 0) {
+        const C v = s[k * sstride];
+        buf[q] = make_double2((double)v.x, (double)v.y);
+        zb[q] = z[(long)k * zstride];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k1 - q;
+      if (k < 0) break;
+      const double d = a2 * zb[q];
+      const double2 cur = make_double2(buf[q].x - d * prev.x, buf[q].y - d * prev.y);
+      buf[q] = cur;
+      prev = cur;
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q)
+      if (k1 - q >= 0) st(k1 - q, buf[q]);
   }
 }
 
@@ -247,7 +364,7 @@ __global__ void __launch_bounds__(128) k_ifftx(Geo g, FftPlan plx, const typenam
     A[r * M + kx] = cadd(E, cmk<C>(-O.y, O.x));  // E + i O
   }
   __syncthreads();
-  C *Z = fft_smem<C>(A, B, M, rows, 1, M, plx, twM, 1);
+  C *Z = fft_smem1<C>(A, B, M, rows, M, plx, twM, 1);
   for (int t = threadIdx.x; t < rows * g.I; t += blockDim.x) {
     const int r = t / g.I, i = t - r * g.I;
     const int row = row0 + r;
@@ -258,20 +375,29 @@ __global__ void __launch_bounds__(128) k_ifftx(Geo g, FftPlan plx, const typenam
   }
 }
 
-template <typename T>
-void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const T *fu, const T *fv,
-                    T *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
-                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches) {
+template <typename TIn, typename T>
+void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
+                    const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
+                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64) {
   typedef typename cpx<T>::t C;
   C *S = reinterpret_cast<C *>(spec);
   const int M = g.I / 2;
   const int rows = g.I <= 256 ? 4 : 2;
   const int nrow = g.J * g.K;
   size_t smx = (size_t)2 * rows * M * sizeof(C);
-  k_fillps_fftx<T><<<(nrow + rows - 1) / rows, 128, smx, s>>>(g, plx, fu, fv, fw, S, (const C *)twM,
-                                                               (const C *)twN, dtidxi, dtidyi, dtidzi, rows);
+  if (res64 && sizeof(TIn) == 4)
+    k_fillps_fftx<TIn, T, float, true><<<(nrow + rows - 1) / rows, 128, smx, s>>>(
+        g, plx, fu, fv, fw, S, (const C *)twM, (const C *)twN, dtidxi, dtidyi, dtidzi, rows);
+  else if (res64)
+    k_fillps_fftx<TIn, T, double><<<(nrow + rows - 1) / rows, 128, smx, s>>>(g, plx, fu, fv, fw, S, (const C *)twM,
+                                                                            (const C *)twN, dtidxi, dtidyi, dtidzi,
+                                                                            rows);
+  else
+    k_fillps_fftx<TIn, T, TIn><<<(nrow + rows - 1) / rows, 128, smx, s>>>(g, plx, fu, fv, fw, S, (const C *)twM,
+                                                                         (const C *)twN, dtidxi, dtidyi, dtidzi,
+                                                                         rows);
   const int cols = 8;
-  size_t smy = (size_t)2 * g.J * cols * sizeof(C);
+  size_t smy = (size_t)2 * (g.J + 1) * cols * sizeof(C);
   dim3 gy((g.MX + cols - 1) / cols, g.K);
   k_ffty<T><<<gy, 256, smy, s>>>(g, ply, S, (const C *)twJ, cols, 0);
   const long ncol = (long)g.MX * g.J;
@@ -285,20 +411,28 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
 
 template <typename T>
 int poisson_set_smem_limits() {
-  typedef typename cpx<T>::t C;
-  (void)sizeof(C);
-  cudaError_t e1 = cudaFuncSetAttribute(k_fillps_fftx<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaError_t e2 = cudaFuncSetAttribute(k_ffty<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaError_t e3 = cudaFuncSetAttribute(k_ifftx<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
+  cudaError_t e[4];
+  e[0] = cudaFuncSetAttribute(k_fillps_fftx<T, T, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (sizeof(T) == 4)
+    if (cudaFuncSetAttribute(k_fillps_fftx<T, T, float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024) != cudaSuccess)
+      return -1;
+  e[1] = cudaFuncSetAttribute(k_fillps_fftx<T, T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  e[2] = cudaFuncSetAttribute(k_ffty<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  e[3] = cudaFuncSetAttribute(k_ifftx<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  for (cudaError_t x : e)
+    if (x != cudaSuccess) return -1;
+  return 0;
 }
 
-template void launch_poisson<double>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &, const double *,
-                                     const double *, double *, void *, double *, const void *, const void *,
-                                     const void *, const double *, double, double, double, int *);
-template void launch_poisson<float>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &, const float *,
-                                    const float *, float *, void *, float *, const void *, const void *,
-                                    const void *, const double *, double, double, double, int *);
+template void launch_poisson<double, double>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
+                                             const double *, const double *, double *, void *, double *,
+                                             const void *, const void *, const void *, const double *, double, double,
+                                             double, int *, bool);
+template void launch_poisson<float, float>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
+                                           const float *, const float *, float *, void *, float *, const void *,
+                                           const void *, const void *, const double *, double, double, double, int *,
+                                           bool);
 template int poisson_set_smem_limits<double>();
 template int poisson_set_smem_limits<float>();
 

@@ -15,9 +15,9 @@ namespace ibmk {
 // stores rhs_old = RHS.  The output goes straight into the forcing buffer
 // (dudtf == dudt on entry of the IBM loop, main.f90:288-306).
 // ---------------------------------------------------------------------------
-template <typename T, int STAGE>
-__global__ void __launch_bounds__(256) k_predict(Geo g, const T *__restrict__ u, const T *__restrict__ v,
-                                                 const T *__restrict__ w, const T *__restrict__ p,
+template <typename TU, typename T, int STAGE>
+__global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u, const TU *__restrict__ v,
+                                                 const TU *__restrict__ w, const TU *__restrict__ p,
                                                  T *__restrict__ ru, T *__restrict__ rv, T *__restrict__ rw,
                                                  T *__restrict__ fu, T *__restrict__ fv, T *__restrict__ fw,
                                                  T f1, T f2, T f3) {
@@ -35,16 +35,19 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const T *__restrict__ u,
   const T dxi = (T)g.dxi, dyi = (T)g.dyi, dzi = (T)g.dzi, visc = (T)g.visc;
   const T q = (T)0.25;
   // u-neighbourhood
-  const T U0 = u[c], Uip = u[at(ip, j, k)], Uim = u[at(im, j, k)], Ujp = u[at(i, jp, k)], Ujm = u[at(i, jm, k)];
-  const T Ukp = u[c + PL], Ukm = u[c - PL];
-  const T V0 = v[c], Vip = v[at(ip, j, k)], Vim = v[at(im, j, k)], Vjp = v[at(i, jp, k)], Vjm = v[at(i, jm, k)];
-  const T Vkp = v[c + PL], Vkm = v[c - PL];
-  const T W0 = w[c], Wip = w[at(ip, j, k)], Wim = w[at(im, j, k)], Wjp = w[at(i, jp, k)], Wjm = w[at(i, jm, k)];
-  const T Wkp = w[c + PL], Wkm = w[c - PL];
+  const T U0 = (T)u[c], Uip = (T)u[at(ip, j, k)], Uim = (T)u[at(im, j, k)], Ujp = (T)u[at(i, jp, k)],
+          Ujm = (T)u[at(i, jm, k)];
+  const T Ukp = (T)u[c + PL], Ukm = (T)u[c - PL];
+  const T V0 = (T)v[c], Vip = (T)v[at(ip, j, k)], Vim = (T)v[at(im, j, k)], Vjp = (T)v[at(i, jp, k)],
+          Vjm = (T)v[at(i, jm, k)];
+  const T Vkp = (T)v[c + PL], Vkm = (T)v[c - PL];
+  const T W0 = (T)w[c], Wip = (T)w[at(ip, j, k)], Wim = (T)w[at(im, j, k)], Wjp = (T)w[at(i, jp, k)],
+          Wjm = (T)w[at(i, jm, k)];
+  const T Wkp = (T)w[c + PL], Wkm = (T)w[c - PL];
   // diagonal neighbours
-  const T Vipjm = v[at(ip, jm, k)], Wipkm = w[at(ip, j, k - 1)];
-  const T Uimjp = u[at(im, jp, k)], Wjpkm = w[at(i, jp, k - 1)];
-  const T Uimkp = u[at(im, j, k + 1)], Vjmkp = v[at(i, jm, k + 1)];
+  const T Vipjm = (T)v[at(ip, jm, k)], Wipkm = (T)w[at(ip, j, k - 1)];
+  const T Uimjp = (T)u[at(im, jp, k)], Wjpkm = (T)w[at(i, jp, k - 1)];
+  const T Uimkp = (T)u[at(im, j, k + 1)], Vjmkp = (T)v[at(i, jm, k + 1)];
   // momxad (mom.f90:21-50)
   T ru_new;
   {
@@ -89,10 +92,10 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const T *__restrict__ u,
              visc * (dwdyp - dwdym) * dyi + dzi * (-wwkp + wwkm) + visc * (dwdzp - dwdzm) * dzi;
   }
   // pressure gradient (momxp/momyp/momzp)
-  const T P0 = p[c];
-  const T gx = -dxi * (p[at(ip, j, k)] - P0);
-  const T gy = -dyi * (p[at(i, jp, k)] - P0);
-  const T gz = -dzi * (p[c + PL] - P0);
+  const T P0 = (T)p[c];
+  const T gx = -dxi * ((T)p[at(ip, j, k)] - P0);
+  const T gy = -dyi * ((T)p[at(i, jp, k)] - P0);
+  const T gz = -dzi * ((T)p[c + PL] - P0);
   T du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
   if (STAGE == 1) {
     du = du + f1 * ru_new;
@@ -113,35 +116,38 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const T *__restrict__ u,
   }
 }
 
-template <typename T>
-void launch_predict(cudaStream_t s, const Geo &g, int stage, const T *u, const T *v, const T *w, const T *p,
+template <typename TU, typename T>
+void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
                     T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3) {
   dim3 blk(64, 4, 1);
   dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
   if (stage == 1)
-    k_predict<T, 1><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+    k_predict<TU, T, 1><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
   else if (stage == 2)
-    k_predict<T, 2><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+    k_predict<TU, T, 2><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
   else
-    k_predict<T, 3><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+    k_predict<TU, T, 3><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
 }
-template void launch_predict<double>(cudaStream_t, const Geo &, int, const double *, const double *,
-                                     const double *, const double *, double *, double *, double *, double *,
-                                     double *, double *, double, double, double);
-template void launch_predict<float>(cudaStream_t, const Geo &, int, const float *, const float *, const float *,
-                                    const float *, float *, float *, float *, float *, float *, float *, double,
-                                    double, double);
+template void launch_predict<double, double>(cudaStream_t, const Geo &, int, const double *, const double *,
+                                             const double *, const double *, double *, double *, double *,
+                                             double *, double *, double *, double, double, double);
+template void launch_predict<float, float>(cudaStream_t, const Geo &, int, const float *, const float *,
+                                           const float *, const float *, float *, float *, float *, float *,
+                                           float *, float *, double, double, double);
 
 // ---------------------------------------------------------------------------
 // correc (correc.f90:11-42) + pnew += p (main.f90:369-371) + bounduvw(unew)
 // and boundp(pnew) z-ghosts (bound.f90:11-107).  phi holds the Poisson
 // solution on planes 1..K; its Neumann ghost p(k1)=p(kmax) is implied.
 // ---------------------------------------------------------------------------
-template <typename T, typename TP>
-__global__ void __launch_bounds__(256) k_correc(Geo g, const T *__restrict__ fu, const T *__restrict__ fv,
-                                                const T *__restrict__ fw, const T *__restrict__ phi,
-                                                T *__restrict__ u, T *__restrict__ v, T *__restrict__ w,
-                                                TP *__restrict__ pn, double fi_, double fj_, double fk_) {
+template <typename TF, typename TPh, typename TU>
+__global__ void __launch_bounds__(256) k_correc(Geo g, const TF *fu, const TF *fv, const TF *fw,
+                                                const TPh *__restrict__ phi, TU *u, TU *v, TU *w,
+                                                double *__restrict__ pn, float *__restrict__ pn32, double fi_,
+                                                double fj_, double fk_) {
+  // fu may alias u (the defect correction updates the state in place: each
+  // thread reads and writes only its own cell of u/v/w)
+  typedef TU T;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z + 1;
@@ -151,23 +157,25 @@ __global__ void __launch_bounds__(256) k_correc(Geo g, const T *__restrict__ fu,
   const long PL = g.plane;
   const long c = fidx(g, i, j, k);
   const T fi = (T)fi_, fj = (T)fj_, fk = (T)fk_;
-  const T P0 = phi[c];
-  const T Pip = phi[fidx(g, ip, j, k)];
-  const T Pjp = phi[fidx(g, i, jp, k)];
-  const T Pkp = (k == g.K) ? P0 : phi[c + PL];
-  const T un = fu[c] - fi * (Pip - P0);
-  const T vn = fv[c] - fj * (Pjp - P0);
-  const T wn = (k == g.K) ? (T)0 : fw[c] - fk * (Pkp - P0);
+  const T P0 = (T)phi[c];
+  const T Pip = (T)phi[fidx(g, ip, j, k)];
+  const T Pjp = (T)phi[fidx(g, i, jp, k)];
+  const T Pkp = (k == g.K) ? P0 : (T)phi[c + PL];
+  const T un = (T)fu[c] - fi * (Pip - P0);
+  const T vn = (T)fv[c] - fj * (Pjp - P0);
+  const T wn = (k == g.K) ? (T)0 : (T)fw[c] - fk * (Pkp - P0);
   u[c] = un;
   v[c] = vn;
   w[c] = wn;
-  const TP pnn = pn[c] + (TP)P0;
+  const double pnn = pn[c] + (double)phi[c];
   pn[c] = pnn;
+  if (pn32) pn32[c] = (float)pnn;
   if (k == g.K) {
     const T sg = g.bc_top == IBM_BC_NOSLIP ? (T)-1 : (T)1;
     u[c + PL] = sg * un;
     v[c + PL] = sg * vn;
     pn[c + PL] = pnn;
+    if (pn32) pn32[c + PL] = (float)pnn;
   }
   if (k == 1) {
     const T sg = g.bc_bot == IBM_BC_NOSLIP ? (T)-1 : (T)1;
@@ -175,22 +183,95 @@ __global__ void __launch_bounds__(256) k_correc(Geo g, const T *__restrict__ fu,
     v[c - PL] = sg * vn;
     w[c - PL] = (T)0;
     pn[c - PL] = pnn;
+    if (pn32) pn32[c - PL] = (float)pnn;
   }
 }
 
-template <typename T, typename TP>
-void launch_correc(cudaStream_t s, const Geo &g, const T *fu, const T *fv, const T *fw, const T *phi, T *u, T *v,
-                   T *w, TP *pn, double fi, double fj, double fk) {
+template <typename TF, typename TPh, typename TU>
+void launch_correc(cudaStream_t s, const Geo &g, const TF *fu, const TF *fv, const TF *fw, const TPh *phi, TU *u,
+                   TU *v, TU *w, double *pn, float *pn32, double fi, double fj, double fk) {
   dim3 blk(64, 4, 1);
   dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
-  k_correc<T, TP><<<grd, blk, 0, s>>>(g, fu, fv, fw, phi, u, v, w, pn, fi, fj, fk);
+  k_correc<TF, TPh, TU><<<grd, blk, 0, s>>>(g, fu, fv, fw, phi, u, v, w, pn, pn32, fi, fj, fk);
 }
-template void launch_correc<double, double>(cudaStream_t, const Geo &, const double *, const double *,
-                                            const double *, const double *, double *, double *, double *,
-                                            double *, double, double, double);
-template void launch_correc<float, double>(cudaStream_t, const Geo &, const float *, const float *,
-                                           const float *, const float *, float *, float *, float *, double *,
-                                           double, double, double);
+template void launch_correc<double, double, double>(cudaStream_t, const Geo &, const double *, const double *,
+                                                    const double *, const double *, double *, double *, double *,
+                                                    double *, float *, double, double, double);
+template void launch_correc<float, float, float>(cudaStream_t, const Geo &, const float *, const float *,
+                                                 const float *, const float *, float *, float *, float *, double *,
+                                                 float *, double, double, double);
+
+// Mixed form of the same update: FP32 velocity; pnew carried as the
+// double-float pair (ph, pl), ph doubling as the FP32 pressure that the
+// predictor reads.  fu may alias u (defect correction in place).
+__global__ void __launch_bounds__(256) k_correc_mixed(Geo g, const float *fu, const float *fv, const float *fw,
+                                                      const float *__restrict__ phi, float *u, float *v, float *w,
+                                                      float *__restrict__ ph, float *__restrict__ pl, float fi,
+                                                      float fj, float fk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;
+  if (i >= g.I || j >= g.J) return;
+  const int ip = i + 1 == g.I ? 0 : i + 1;
+  const int jp = j + 1 == g.J ? 0 : j + 1;
+  const long PL = g.plane;
+  const long c = fidx(g, i, j, k);
+  const float P0 = phi[c];
+  const float Pip = phi[fidx(g, ip, j, k)];
+  const float Pjp = phi[fidx(g, i, jp, k)];
+  const float Pkp = (k == g.K) ? P0 : phi[c + PL];
+  const float un = fu[c] - fi * (Pip - P0);
+  const float vn = fv[c] - fj * (Pjp - P0);
+  const float wn = (k == g.K) ? 0.f : fw[c] - fk * (Pkp - P0);
+  u[c] = un;
+  v[c] = vn;
+  w[c] = wn;
+  float sh, sl;
+  df_add(ph[c], pl[c], P0, 0.f, sh, sl);
+  ph[c] = sh;
+  pl[c] = sl;
+  if (k == g.K) {
+    const float sg = g.bc_top == IBM_BC_NOSLIP ? -1.f : 1.f;
+    u[c + PL] = sg * un;
+    v[c + PL] = sg * vn;
+    ph[c + PL] = sh;
+    pl[c + PL] = sl;
+  }
+  if (k == 1) {
+    const float sg = g.bc_bot == IBM_BC_NOSLIP ? -1.f : 1.f;
+    u[c - PL] = sg * un;
+    v[c - PL] = sg * vn;
+    w[c - PL] = 0.f;
+    ph[c - PL] = sh;
+    pl[c - PL] = sl;
+  }
+}
+void launch_correc_mixed(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
+                         const float *phi, float *u, float *v, float *w, float *ph, float *pl, double fi, double fj,
+                         double fk) {
+  dim3 blk(64, 4, 1);
+  dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
+  k_correc_mixed<<<grd, blk, 0, s>>>(g, fu, fv, fw, phi, u, v, w, ph, pl, (float)fi, (float)fj, (float)fk);
+}
+
+// double-float pair <-> FP64 array
+__global__ void k_df_to_d(long n, const float *__restrict__ h, const float *__restrict__ l, double *__restrict__ d) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    d[t] = (double)h[t] + (double)l[t];
+}
+__global__ void k_d_to_df(long n, const double *__restrict__ d, float *__restrict__ h, float *__restrict__ l) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const float hh = (float)d[t];
+    h[t] = hh;
+    l[t] = (float)(d[t] - (double)hh);
+  }
+}
+void launch_df_to_d(cudaStream_t s, long n, const float *h, const float *l, double *d) {
+  k_df_to_d<<<1216, 256, 0, s>>>(n, h, l, d);
+}
+void launch_d_to_df(cudaStream_t s, long n, const double *d, float *h, float *l) {
+  k_d_to_df<<<1216, 256, 0, s>>>(n, d, h, l);
+}
 
 // ---------------------------------------------------------------------------
 // Layout conversion between the reference host layout (0:i1,0:j1,0:k1) and
@@ -236,8 +317,9 @@ template void launch_dev_to_ref<float>(cudaStream_t, const Geo &, const float *,
 // chkdiv (chkdiv.f90:7-61): block partials of sum(div) and (max|div|, first
 // linear index), combined in a fixed order by a single block.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_div_partial(Geo g, const double *__restrict__ u,
-                                                     const double *__restrict__ v, const double *__restrict__ w,
+template <typename T>
+__global__ void __launch_bounds__(256) k_div_partial(Geo g, const T *__restrict__ u,
+                                                     const T *__restrict__ v, const T *__restrict__ w,
                                                      double *__restrict__ psum, double *__restrict__ pmax,
                                                      long long *__restrict__ ploc) {
   const long n = (long)g.I * g.J * g.K;
@@ -246,8 +328,9 @@ __global__ void __launch_bounds__(256) k_div_partial(Geo g, const double *__rest
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.I), j = (int)((t / g.I) % g.J), k = (int)(t / g.plane) + 1;
     const long c = fidx(g, i, j, k);
-    const double div = (w[c] - w[c - g.plane]) * g.dzi + (v[c] - v[fidx(g, i, wrapm(j - 1, g.J), k)]) * g.dyi +
-                       (u[c] - u[fidx(g, wrapm(i - 1, g.I), j, k)]) * g.dxi;
+    const double div = ((double)w[c] - (double)w[c - g.plane]) * g.dzi +
+                       ((double)v[c] - (double)v[fidx(g, i, wrapm(j - 1, g.J), k)]) * g.dyi +
+                       ((double)u[c] - (double)u[fidx(g, wrapm(i - 1, g.I), j, k)]) * g.dxi;
     s += div;
     const double a = fabs(div);
     if (a > m) { m = a; loc = t; }
@@ -279,18 +362,23 @@ __global__ void k_div_final(int nb, const double *psum, const double *pmax, cons
   }
   out[0] = s; out[1] = m; out[2] = (double)l;
 }
-void launch_chkdiv(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w,
-                   double *scratch, double *out) {
+template <typename T>
+void launch_chkdiv(cudaStream_t s, const Geo &g, const T *u, const T *v, const T *w, double *scratch, double *out) {
   const int nb = 608;
   double *psum = scratch, *pmax = scratch + nb;
   long long *ploc = (long long *)(scratch + 2 * nb);
-  k_div_partial<<<nb, 256, 0, s>>>(g, u, v, w, psum, pmax, ploc);
+  k_div_partial<T><<<nb, 256, 0, s>>>(g, u, v, w, psum, pmax, ploc);
   k_div_final<<<1, 32, 0, s>>>(nb, psum, pmax, ploc, out);
 }
+template void launch_chkdiv<double>(cudaStream_t, const Geo &, const double *, const double *, const double *,
+                                    double *, double *);
+template void launch_chkdiv<float>(cudaStream_t, const Geo &, const float *, const float *, const float *, double *,
+                                   double *);
 
 // chkdt (chkdt.f90:6-273): min over the three staggered components.
-__global__ void __launch_bounds__(256) k_dt_partial(Geo g, const double *__restrict__ u,
-                                                    const double *__restrict__ v, const double *__restrict__ w,
+template <typename T>
+__global__ void __launch_bounds__(256) k_dt_partial(Geo g, const T *__restrict__ u,
+                                                    const T *__restrict__ v, const T *__restrict__ w,
                                                     double *__restrict__ pmin) {
   const long n = (long)g.I * g.J * g.K;
   double m = 899999.;
@@ -298,9 +386,9 @@ __global__ void __launch_bounds__(256) k_dt_partial(Geo g, const double *__restr
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.I), j = (int)((t / g.I) % g.J), k = (int)(t / g.plane) + 1;
     const int ip = wrapm(i + 1, g.I), im = wrapm(i - 1, g.I), jp = wrapm(j + 1, g.J), jm = wrapm(j - 1, g.J);
-    auto U = [&](int a, int b, int c) { return u[fidx(g, a, b, c)]; };
-    auto V = [&](int a, int b, int c) { return v[fidx(g, a, b, c)]; };
-    auto W = [&](int a, int b, int c) { return w[fidx(g, a, b, c)]; };
+    auto U = [&](int a, int b, int c) { return (double)u[fidx(g, a, b, c)]; };
+    auto V = [&](int a, int b, int c) { return (double)v[fidx(g, a, b, c)]; };
+    auto W = [&](int a, int b, int c) { return (double)w[fidx(g, a, b, c)]; };
     const double dxi2 = dxi * dxi + dyi * dyi + dzi * dzi;
     const double dt1 = 1.65 / (4. * g.visc * dxi2);
     for (int comp = 0; comp < 3; ++comp) {
@@ -340,22 +428,28 @@ __global__ void k_min_final(int nb, const double *p, double *out) {
   for (int b = 0; b < nb; ++b) m = fmin(m, p[b]);
   out[0] = m;
 }
-void launch_chkdt(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w,
-                  double *scratch, double *out) {
+template <typename T>
+void launch_chkdt(cudaStream_t s, const Geo &g, const T *u, const T *v, const T *w, double *scratch, double *out) {
   const int nb = 608;
-  k_dt_partial<<<nb, 256, 0, s>>>(g, u, v, w, scratch);
+  k_dt_partial<T><<<nb, 256, 0, s>>>(g, u, v, w, scratch);
   k_min_final<<<1, 32, 0, s>>>(nb, scratch, out);
 }
+template void launch_chkdt<double>(cudaStream_t, const Geo &, const double *, const double *, const double *,
+                                   double *, double *);
+template void launch_chkdt<float>(cudaStream_t, const Geo &, const float *, const float *, const float *, double *,
+                                  double *);
 
-// wall shear of rk1/rk2/rk3 (rk3.f90:80-103): sum over the wall planes.
-__global__ void k_wallshear(Geo g, const double *__restrict__ v, double *out) {
-  __shared__ double sm[512];
+// wall shear of rk1/rk2/rk3 (rk3.f90:80-103): sum over the wall planes,
+// block partials combined in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(256) k_wallshear_partial(Geo g, const T *__restrict__ v, double *__restrict__ part) {
+  __shared__ double sm[256];
   double s = 0.;
   const long PL = g.plane;
-  for (long t = threadIdx.x; t < PL; t += blockDim.x) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < PL; t += (long)gridDim.x * blockDim.x) {
     const long top = (long)g.K * PL + t, bot = PL + t;
-    s = s + g.visc * (v[top + PL] - v[top]) * g.dzi * (1. / g.dxi) * (1. / g.dyi) -
-        g.visc * (v[bot] - v[bot - PL]) * g.dzi * (1. / g.dxi) * (1. / g.dyi);
+    s = s + g.visc * ((double)v[top + PL] - (double)v[top]) * g.dzi * (1. / g.dxi) * (1. / g.dyi) -
+        g.visc * ((double)v[bot] - (double)v[bot - PL]) * g.dzi * (1. / g.dxi) * (1. / g.dyi);
   }
   sm[threadIdx.x] = s;
   __syncthreads();
@@ -363,11 +457,22 @@ __global__ void k_wallshear(Geo g, const double *__restrict__ v, double *out) {
     if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[0] = sm[0];
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
 }
-void launch_wallshear(cudaStream_t s, const Geo &g, const double *v, double *out) {
-  k_wallshear<<<1, 512, 0, s>>>(g, v, out);
+__global__ void k_sum_final(int nb, const double *__restrict__ part, double *out) {
+  if (threadIdx.x != 0) return;
+  double s = 0.;
+  for (int b = 0; b < nb; ++b) s += part[b];
+  out[0] = s;
 }
+template <typename T>
+void launch_wallshear(cudaStream_t s, const Geo &g, const T *v, double *scratch, double *out) {
+  const int nb = 64;
+  k_wallshear_partial<T><<<nb, 256, 0, s>>>(g, v, scratch);
+  k_sum_final<<<1, 32, 0, s>>>(nb, scratch, out);
+}
+template void launch_wallshear<double>(cudaStream_t, const Geo &, const double *, double *, double *);
+template void launch_wallshear<float>(cudaStream_t, const Geo &, const float *, double *, double *);
 
 // convert / copy helpers for the mixed form
 __global__ void k_d2f(long n, const double *__restrict__ a, float *__restrict__ b) {

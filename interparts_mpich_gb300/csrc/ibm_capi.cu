@@ -43,6 +43,13 @@ struct ibm_ctx {
   double *ru = nullptr, *rv = nullptr, *rw = nullptr;
   double *fu = nullptr, *fv = nullptr, *fw = nullptr, *phi = nullptr;
   void *spec = nullptr;
+  // mixed form: FP32 predictor, RHS, Poisson work arrays
+  bool mixed = false;
+  float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr, *p32 = nullptr;  // FP32 state
+  float *plo32 = nullptr;  // pnew = p32 + plo32 (double-float); p is the FP64 staging copy
+  float *ru32 = nullptr, *rv32 = nullptr, *rw32 = nullptr;
+  float *fu32 = nullptr, *fv32 = nullptr, *fw32 = nullptr, *phi32 = nullptr;
+  void *spec32 = nullptr, *twM32 = nullptr, *twN32 = nullptr, *twJ32 = nullptr;
   double *zt = nullptr;
   void *twM = nullptr, *twN = nullptr, *twJ = nullptr;
   FftPlan plx{}, ply{};
@@ -54,6 +61,20 @@ struct ibm_ctx {
   double *dout = nullptr;      // small device results
   double *href = nullptr;      // device staging buffer in the reference layout
   double *hpin = nullptr;      // pinned host results
+  // learned forcing (IBM_MODE_MIXED_LEARNED)
+  MlpTrainBuffers mt{};        // model (params, Adam moments, BF16 copies) + training batch buffers
+  int mt_cap = 0;              // batch capacity of mt
+  float *norm = nullptr;       // [198]: feature mean, 1/sigma; target mean, sigma
+  __nv_bfloat16 *lx = nullptr; // [np*nl][96] standardised features
+  float *ly = nullptr, *ldf = nullptr;  // [np*nl][3] network output, force increment
+  double *ls = nullptr;        // learn state, see k_ibm_res_gate
+  int *gate = nullptr;
+  HarvestArgs hv{};
+  int hv_passes = 0;
+  bool harvesting = false, learn_on = false, model_ready = false, stats_ready = false;
+  __nv_bfloat16 *tx = nullptr; // staged training set
+  float *tt = nullptr;
+  int tcap = 0, train_step = 0;
   bool have_fields = false, have_particles = false, particles_ready = false;
   long long launches = 0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -91,6 +112,62 @@ int dalloc(ibm_ctx *c, T **ptr, size_t n) {
   if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc");
   e = cudaMemsetAsync(*ptr, 0, n * sizeof(T) + 256, c->stream);
   return cuda_err(c, e, "cudaMemset");
+}
+
+void free_mlp_batch(MlpTrainBuffers &B) {
+  void *q[] = {B.x, B.t, B.y, B.z1, B.z2, B.h1, B.h2, B.dz1, B.dz2};
+  for (void *p : q)
+    if (p) cudaFree(p);
+  B.x = nullptr; B.t = B.y = B.z1 = B.z2 = nullptr; B.h1 = B.h2 = B.dz1 = B.dz2 = nullptr;
+}
+// training batch buffers for nb rows (rounded up to the 64-row tile)
+int alloc_mlp_batch(ibm_ctx *c, MlpTrainBuffers &B, int nb) {
+  const size_t n = ((size_t)nb + 63) / 64 * 64;
+  int st;
+  if ((st = dalloc(c, &B.x, n * 96))) return st;
+  for (float **f : {&B.t, &B.y})
+    if ((st = dalloc(c, f, n * 3))) return st;
+  for (float **f : {&B.z1, &B.z2})
+    if ((st = dalloc(c, f, n * 128))) return st;
+  for (__nv_bfloat16 **f : {&B.h1, &B.h2, &B.dz1, &B.dz2})
+    if ((st = dalloc(c, f, n * 128))) return st;
+  return IBM_OK;
+}
+// model buffers (params, moments, gradient, BF16 copies) of a scratch model
+int alloc_mlp_model(ibm_ctx *c, MlpTrainBuffers &B) {
+  int st;
+  for (float **f : {&B.params, &B.m, &B.v, &B.grad})
+    if ((st = dalloc(c, f, mlp_nparam()))) return st;
+  if ((st = dalloc(c, &B.loss, 4))) return st;
+  for (__nv_bfloat16 **f : {&B.w1b, &B.w2b, &B.w2tb})
+    if ((st = dalloc(c, f, 128 * 128))) return st;
+  return IBM_OK;
+}
+void free_mlp_model(MlpTrainBuffers &B) {
+  void *q[] = {B.params, B.m, B.v, B.grad, B.loss, B.w1b, B.w2b, B.w2tb};
+  for (void *p : q)
+    if (p) cudaFree(p);
+}
+
+// He-style initial weights (deterministic counter-based normal deviates)
+void init_mlp_params(std::vector<float> &w, unsigned seed) {
+  const int sizes[6] = {128 * 96, 128, 128 * 128, 128, 3 * 128, 3};
+  const double scale[6] = {std::sqrt(2. / 96.), 0., std::sqrt(2. / 128.), 0., 0.1 * std::sqrt(1. / 128.), 0.};
+  uint64_t x = 0x9E3779B97F4A7C15ULL ^ ((uint64_t)seed << 17);
+  auto next = [&x]() {  // splitmix64
+    uint64_t z = (x += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  };
+  w.clear();
+  for (int b = 0; b < 6; ++b)
+    for (int q = 0; q < sizes[b]; ++q) {
+      const double u1 = ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+      const double u2 = ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+      const double nrm = std::sqrt(-2. * std::log(u1)) * std::cos(2. * PI * u2);  // Box-Muller
+      w.push_back((float)(scale[b] * nrm));
+    }
 }
 
 void derived(ibm_ctx *c) {
@@ -155,6 +232,15 @@ void derived(ibm_ctx *c) {
   pg.a11_ini_pw = -(1. / eps_ini_pw) + 1. / 5. * std::log(eps_ini_pw) + 1. / 21. * eps_ini_pw * std::log(eps_ini_pw) - .9713;
   pg.a11_sat_pw = -(1. / eps_sat_pw) + 1. / 5. * std::log(eps_sat_pw) + 1. / 21. * eps_sat_pw * std::log(eps_sat_pw) - .9713;
   pg.I = g.I; pg.J = g.J; pg.K = g.K;
+  // smallest double x with sqrt(x) >= radius (sqrt is correctly rounded and
+  // monotone on host and device alike)
+  double t = P.radius * P.radius;
+  if (std::sqrt(t) >= P.radius) {
+    while (t > 0 && std::sqrt(std::nextafter(t, 0.)) >= P.radius) t = std::nextafter(t, 0.);
+  } else {
+    while (!(std::sqrt(t) >= P.radius)) t = std::nextafter(t, 1e300);
+  }
+  pg.rthr = t;
 }
 
 // twiddles and the Thomas pivots (initsolver.f90:10-66)
@@ -172,6 +258,19 @@ int build_solver_tables(ibm_ctx *c) {
   CK(cudaMemcpyAsync(c->twM, twM.data(), M * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->twN, twN.data(), (M + 1) * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->twJ, twJ.data(), J * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  if (c->mixed) {
+    std::vector<float2> fM(M), fN(M + 1), fJ(J);
+    for (int t = 0; t < M; ++t) fM[t] = make_float2((float)twM[t].x, (float)twM[t].y);
+    for (int t = 0; t <= M; ++t) fN[t] = make_float2((float)twN[t].x, (float)twN[t].y);
+    for (int t = 0; t < J; ++t) fJ[t] = make_float2((float)twJ[t].x, (float)twJ[t].y);
+    if ((st = dalloc(c, (float2 **)&c->twM32, M))) return st;
+    if ((st = dalloc(c, (float2 **)&c->twN32, M + 1))) return st;
+    if ((st = dalloc(c, (float2 **)&c->twJ32, J))) return st;
+    CK(cudaMemcpyAsync(c->twM32, fM.data(), M * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->twN32, fN.data(), (M + 1) * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->twJ32, fJ.data(), J * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
   // tridiagonal matrix with Neumann rows
   std::vector<double> a(K + 1), b(K + 1), cc(K + 1);
   for (int k = 1; k <= K; ++k) { a[k] = g.dzi * g.dzi; cc[k] = g.dzi * g.dzi; b[k] = -(a[k] + cc[k]); }
@@ -217,9 +316,19 @@ int alloc_all(ibm_ctx *c) {
   const Geo &g = c->g;
   const size_t nf = (size_t)g.nfield;
   int st;
-  for (double **f : {&c->u, &c->v, &c->w, &c->p, &c->ru, &c->rv, &c->rw, &c->fu, &c->fv, &c->fw, &c->phi})
-    if ((st = dalloc(c, f, nf))) return st;
-  if ((st = dalloc(c, (double2 **)&c->spec, (size_t)g.K * g.J * g.MX))) return st;
+  if ((st = dalloc(c, &c->p, nf))) return st;
+  if (!c->mixed) {
+    for (double **f : {&c->u, &c->v, &c->w})
+      if ((st = dalloc(c, f, nf))) return st;
+    for (double **f : {&c->ru, &c->rv, &c->rw, &c->fu, &c->fv, &c->fw, &c->phi})
+      if ((st = dalloc(c, f, nf))) return st;
+    if ((st = dalloc(c, (double2 **)&c->spec, (size_t)g.K * g.J * g.MX))) return st;
+  } else {
+    for (float **f : {&c->u32, &c->v32, &c->w32, &c->p32, &c->plo32, &c->ru32, &c->rv32, &c->rw32, &c->fu32, &c->fv32,
+                      &c->fw32, &c->phi32})
+      if ((st = dalloc(c, f, nf))) return st;
+    if ((st = dalloc(c, (float2 **)&c->spec32, (size_t)g.K * g.J * g.MX))) return st;
+  }
   if ((st = dalloc(c, &c->scratch, 4096))) return st;
   if ((st = dalloc(c, &c->dout, 64))) return st;
   CK(cudaMallocHost((void **)&c->hpin, 64 * sizeof(double)));
@@ -229,7 +338,11 @@ int alloc_all(ibm_ctx *c) {
     for (double **f : {&c->ib.xfp, &c->ib.yfp, &c->ib.zfp, &c->ib.ul, &c->ib.vl, &c->ib.wl, &c->ib.dudtl,
                        &c->ib.dvdtl, &c->ib.dwdtl, &c->ib.fxl, &c->ib.fyl, &c->ib.fzl})
       if ((st = dalloc(c, f, npl))) return st;
-    if ((st = dalloc(c, &c->ib.st, npl))) return st;
+    if (c->mixed) {
+      if ((st = dalloc(c, &c->ib.st32, npl))) return st;
+    } else {
+      if ((st = dalloc(c, &c->ib.st, npl))) return st;
+    }
     if ((st = dalloc(c, &c->ib.nla, np))) return st;
     if ((st = dalloc(c, &c->pb.pf, (size_t)PF_N * np))) return st;
     if ((st = dalloc(c, &c->pb.cf, (size_t)CF_N * np * nq))) return st;
@@ -254,6 +367,26 @@ int alloc_all(ibm_ctx *c) {
     }
     CK(cudaMemcpyAsync(c->pb.sincos, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   }
+  if (c->mode == IBM_MODE_MIXED_LEARNED) {
+    const int npar = mlp_nparam();
+    for (float **f : {&c->mt.params, &c->mt.m, &c->mt.v, &c->mt.grad})
+      if ((st = dalloc(c, f, npar))) return st;
+    if ((st = dalloc(c, &c->mt.loss, 4))) return st;
+    for (__nv_bfloat16 **f : {&c->mt.w1b, &c->mt.w2b, &c->mt.w2tb})
+      if ((st = dalloc(c, f, 128 * 128))) return st;
+    if ((st = dalloc(c, &c->norm, 198))) return st;
+    if ((st = dalloc(c, &c->ls, 8))) return st;
+    if ((st = dalloc(c, &c->gate, 4))) return st;
+    const double ls0[8] = {0, 0, 0, 1.5, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(c->ls, ls0, sizeof(ls0), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (np > 0) {
+      const size_t npl = (size_t)np * nl;
+      if ((st = dalloc(c, &c->lx, npl * 96))) return st;
+      if ((st = dalloc(c, &c->ly, npl * 3))) return st;
+      if ((st = dalloc(c, &c->ldf, npl * 3))) return st;
+    }
+  }
   return IBM_OK;
 }
 
@@ -263,6 +396,7 @@ int check_flags(ibm_ctx *c) {
   CK(cudaMemcpyAsync(h, c->pb.err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   if (h[2]) return set_err(c, IBM_E_INVALID, "a Lagrangian point left the grid (non-finite or beyond the walls)");
+  if (h[3]) return set_err(c, IBM_E_INVALID, "sphere integration box wider than 128 cells");
   if (h[1]) return set_err(c, IBM_E_CONTACT_OVERFLOW, "a particle exceeded nqmax contacts (param.f90:100)");
   if (h[0]) return set_err(c, IBM_E_CONTACT_OVERFLOW, "more than 64 interaction candidates for one particle");
   return IBM_OK;
@@ -270,21 +404,88 @@ int check_flags(ibm_ctx *c) {
 
 int predict(ibm_ctx *c, int rkiter, double dt) {
   const Geo &g = c->g;
-  launch_wallshear(c->stream, g, c->v, c->dout + 8 + (rkiter - 1));
-  LAUNCHED(1);
+  if (c->mixed) launch_wallshear<float>(c->stream, g, c->v32, c->scratch, c->dout + 8 + (rkiter - 1));
+  else launch_wallshear<double>(c->stream, g, c->v, c->scratch, c->dout + 8 + (rkiter - 1));
+  LAUNCHED(2);
   double f1, f2 = 0, f3 = 0;
   if (rkiter == 1) f1 = dt * (32. / 60.);
   else if (rkiter == 2) { f1 = dt * (8. / 60.); f2 = dt * (25. / 60.); f3 = dt * (17. / 60.); }
   else { f1 = dt * (20. / 60.); f2 = dt * (45. / 60.); f3 = dt * (25. / 60.); }
-  launch_predict<double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv, c->fw, f1,
-                         f2, f3);
+  if (c->mixed)
+    launch_predict<float, float>(c->stream, g, rkiter, c->u32, c->v32, c->w32, c->p32, c->ru32, c->rv32, c->rw32,
+                                 c->fu32, c->fv32, c->fw32, f1, f2, f3);
+  else
+    launch_predict<double, double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv,
+                                   c->fw, f1, f2, f3);
   LAUNCHED(1);
+  return IBM_OK;
+}
+
+int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
+  // one plain sweep, one inference, then the plain passes only where the
+  // no-slip residual exceeds fallback_ratio x the plain method's
+  const Geo &g = c->g;
+  const long npts = (long)c->pg.np * c->pg.nl;
+  launch_ibm_stencil_f(c->stream, g, c->pg, c->ib);
+  launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 1);
+  launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
+  launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt);
+  LAUNCHED(4);
+  HarvestArgs none{};
+  launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->norm, c->norm + 96, c->lx,
+                        none);
+  launch_mlp_forward(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly, nullptr, nullptr,
+                     nullptr, nullptr, 0);
+  launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
+  launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf);
+  launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
+  launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 0);
+  LAUNCHED(7);
+  for (int it = 1; it < nl_iter; ++it) {
+    launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 0, c->gate);
+    launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate);
+    LAUNCHED(2);
+  }
   return IBM_OK;
 }
 
 int forcing(ibm_ctx *c, double dt, int nl_iter) {
   if (c->pg.np == 0 || nl_iter <= 0) return IBM_OK;
   const Geo &g = c->g;
+  if (c->mixed) {
+    if (c->learn_on && !c->harvesting && nl_iter >= 2) return forcing_learned(c, dt, nl_iter);
+    const long npts = (long)c->pg.np * c->pg.nl;
+    const int npass = c->harvesting ? std::max(nl_iter, c->hv_passes) : nl_iter;
+    launch_ibm_stencil_f(c->stream, g, c->pg, c->ib);
+    LAUNCHED(1);
+    for (int it = 0; it < npass; ++it) {
+      launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, it == 0 ? 1 : 0);
+      LAUNCHED(1);
+      if (it == 0) {
+        launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
+        LAUNCHED(1);
+      }
+      launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt);
+      LAUNCHED(1);
+      if (c->harvesting && it == 0) {
+        c->hv.phase = (c->hv.phase + 1) % c->hv.stride;
+        launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, nullptr, nullptr,
+                              c->hv);
+        LAUNCHED(1);
+      }
+      if (c->harvesting && it == nl_iter - 1) {
+        // the plain method's residual at its own number of passes
+        launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
+        launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 1);
+        LAUNCHED(3);
+      }
+    }
+    if (c->harvesting) {
+      launch_ibm_harvest_targets(c->stream, c->ib, c->hv, dt);
+      LAUNCHED(2);
+    }
+    return IBM_OK;
+  }
   launch_ibm_stencil<double>(c->stream, g, c->pg, c->ib);
   LAUNCHED(1);
   for (int it = 0; it < nl_iter; ++it) {
@@ -304,12 +505,32 @@ int project(ibm_ctx *c, int rkiter, double dt) {
   const Geo &g = c->g;
   const double dti = 1. / (c->rkab[rkiter - 1] * dt);
   int nl = 0;
-  launch_poisson<double>(c->stream, g, c->plx, c->ply, c->fu, c->fv, c->fw, c->spec, c->phi, c->twM, c->twN, c->twJ,
-                         c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl);
-  LAUNCHED(nl);
   const double factor = c->rkab[rkiter - 1] * dt;
-  launch_correc<double, double>(c->stream, g, c->fu, c->fv, c->fw, c->phi, c->u, c->v, c->w, c->p, factor * g.dxi,
-                                factor * g.dyi, factor * g.dzi);
+  if (c->mixed) {
+    // FP32 solve of fillps(u*), FP64 Thomas; correction into the FP64 state
+    launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
+                                 c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl);
+    LAUNCHED(nl);
+    launch_correc_mixed(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
+                        factor * g.dxi, factor * g.dyi, factor * g.dzi);
+    LAUNCHED(1);
+    // one defect correction: the divergence residual of the corrected state,
+    // evaluated in FP64, drives a second solve; its pressure is accumulated
+    // into the FP64 pnew
+    nl = 0;
+    launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->u32, c->v32, c->w32, c->spec32, c->phi32, c->twM32,
+                                 c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl, true);
+    LAUNCHED(nl);
+    launch_correc_mixed(c->stream, g, c->u32, c->v32, c->w32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
+                        factor * g.dxi, factor * g.dyi, factor * g.dzi);
+    LAUNCHED(1);
+    return IBM_OK;
+  }
+  launch_poisson<double, double>(c->stream, g, c->plx, c->ply, c->fu, c->fv, c->fw, c->spec, c->phi, c->twM, c->twN,
+                                 c->twJ, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl);
+  LAUNCHED(nl);
+  launch_correc<double, double, double>(c->stream, g, c->fu, c->fv, c->fw, c->phi, c->u, c->v, c->w, c->p, nullptr,
+                                        factor * g.dxi, factor * g.dyi, factor * g.dzi);
   LAUNCHED(1);
   return IBM_OK;
 }
@@ -318,7 +539,8 @@ int newton_euler(ibm_ctx *c, int rkiter, double dt) {
   if (c->pg.np == 0) return IBM_OK;
   launch_save_old(c->stream, c->pg, c->pb);
   LAUNCHED(1);
-  launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
+  if (c->mixed) launch_sphere_integrals<float>(c->stream, c->g, c->pg, c->pb, c->u32, c->v32, c->w32, 23);
+  else launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
   LAUNCHED(1);
   for (int iter = 0; iter <= 1; ++iter) {
     launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt);
@@ -357,7 +579,10 @@ ibm_ctx *ibm_create(const ibm_params *P) {
     g_create_error = "np > 0 requires nl > 0, thetarc, phirc and radius > 0";
     return nullptr;
   }
-  if (P->mode != IBM_MODE_PLAIN_FP64) { g_create_error = "only IBM_MODE_PLAIN_FP64 is available in this build"; return nullptr; }
+  if (P->mode != IBM_MODE_PLAIN_FP64 && P->mode != IBM_MODE_MIXED && P->mode != IBM_MODE_MIXED_LEARNED) {
+    g_create_error = "mode must be IBM_MODE_PLAIN_FP64, IBM_MODE_MIXED or IBM_MODE_MIXED_LEARNED";
+    return nullptr;
+  }
   if (P->np > 0) {
     // nl must equal nint(pi/3*(12*((radius-retrac)*dxi)^2+1)) (main.f90:118-132)
     const double dxi = P->itot / P->lx, retrac = 0.3 / dxi;
@@ -368,6 +593,10 @@ ibm_ctx *ibm_create(const ibm_params *P) {
       return nullptr;
     }
   }
+  if ((long long)P->np * P->nl >= (1LL << 31) || (long long)(P->itot + 2) * (P->jtot + 2) * (P->ktot + 2) >= (1LL << 40)) {
+    g_create_error = "problem too large (np*nl must be < 2^31)";
+    return nullptr;
+  }
   ibm_ctx *c = new ibm_ctx();
   c->prm = *P;
   if (P->np > 0) {
@@ -377,6 +606,7 @@ ibm_ctx *ibm_create(const ibm_params *P) {
   c->prm.thetarc = nullptr;
   c->prm.phirc = nullptr;
   c->mode = P->mode;
+  c->mixed = P->mode != IBM_MODE_PLAIN_FP64;
   derived(c);
   if (!make_plan(c->g.I / 2, c->plx) || !make_plan(c->g.J, c->ply)) {
     g_create_error = "itot/2 and jtot must be products of 2 and 3";
@@ -393,7 +623,8 @@ ibm_ctx *ibm_create(const ibm_params *P) {
   for (auto &e : c->ev) cudaEventCreate(&e);
   int st = alloc_all(c);
   if (st == IBM_OK) st = build_solver_tables(c);
-  if (st == IBM_OK && (poisson_set_smem_limits<double>() != 0 || poisson_set_smem_limits<float>() != 0))
+  if (st == IBM_OK && (poisson_set_smem_limits<double>() != 0 || poisson_set_smem_limits<float>() != 0 ||
+                       mlp_set_smem_limits() != 0))
     st = set_err(c, IBM_E_CUDA, "cudaFuncSetAttribute failed");
   if (st == IBM_OK) st = cuda_err(c, cudaStreamSynchronize(c->stream), "create");
   if (st != IBM_OK) {
@@ -411,9 +642,17 @@ int ibm_destroy(ibm_ctx *c) {
                   c->twN, c->twJ, c->scratch, c->dout, c->href, c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl,
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
-                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red};
+                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
+                  c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.st32, c->u32, c->v32,
+                  c->w32, c->p32, c->plo32};
   for (void *q : ptrs)
     if (q) cudaFree(q);
+  void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
+                   c->norm, c->ls, c->gate, c->lx, c->ly, c->ldf, c->hv.feat, c->hv.pidx, c->hv.targ,
+                   c->hv.count, c->tx, c->tt};
+  for (void *q : lptrs)
+    if (q) cudaFree(q);
+  free_mlp_batch(c->mt);
   if (c->hpin) cudaFreeHost(c->hpin);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -468,6 +707,16 @@ static int download_field(ibm_ctx *c, const double *d, double *h) {
   return IBM_OK;
 }
 
+static int download_field32(ibm_ctx *c, const float *d, double *h) {
+  if (!h) return IBM_OK;
+  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  launch_dev_to_ref<float>(c->stream, c->g, d, c->href);
+  LAUNCHED(1);
+  CK(cudaMemcpyAsync(h, c->href, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
 int ibm_set_fields(ibm_ctx *c, const double *u, const double *v, const double *w, const double *p, const double *durk,
                    const double *dvrk, const double *dwrk) {
   if (!c) return IBM_E_INVALID;
@@ -476,10 +725,32 @@ int ibm_set_fields(ibm_ctx *c, const double *u, const double *v, const double *w
   if ((st = ensure_href(c))) return st;
   const double *hs[7] = {u, v, w, p, durk, dvrk, dwrk};
   double *ds[7] = {c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw};
-  for (int f = 0; f < 7; ++f)
-    if ((st = upload_field(c, hs[f], ds[f]))) return st;
-  // dudtf starts from zero (module storage), in particular its k1 plane
-  for (double *f : {c->fu, c->fv, c->fw}) CK(cudaMemsetAsync(f, 0, (size_t)c->g.nfield * sizeof(double), c->stream));
+  if (!c->mixed) {
+    for (int f = 0; f < 7; ++f)
+      if ((st = upload_field(c, hs[f], ds[f]))) return st;
+  } else {
+    if ((st = upload_field(c, p, c->p))) return st;
+    launch_d_to_df(c->stream, c->g.nfield, c->p, c->p32, c->plo32);
+    LAUNCHED(1);
+  }
+  if (c->mixed) {
+    float *d32[6] = {c->u32, c->v32, c->w32, c->ru32, c->rv32, c->rw32};
+    const double *h32[6] = {u, v, w, durk, dvrk, dwrk};
+    for (int f = 0; f < 6; ++f) {
+      if (h32[f]) {
+        const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+        CK(cudaMemcpyAsync(c->href, h32[f], n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        launch_ref_to_dev<float>(c->stream, c->g, c->href, d32[f]);
+        LAUNCHED(1);
+      } else {
+        CK(cudaMemsetAsync(d32[f], 0, (size_t)c->g.nfield * sizeof(float), c->stream));
+      }
+    }
+    for (float *f : {c->fu32, c->fv32, c->fw32}) CK(cudaMemsetAsync(f, 0, (size_t)c->g.nfield * sizeof(float), c->stream));
+  } else {
+    // dudtf starts from zero (module storage), in particular its k1 plane
+    for (double *f : {c->fu, c->fv, c->fw}) CK(cudaMemsetAsync(f, 0, (size_t)c->g.nfield * sizeof(double), c->stream));
+  }
   CK(cudaStreamSynchronize(c->stream));
   c->have_fields = true;
   return IBM_OK;
@@ -491,8 +762,20 @@ int ibm_get_fields(ibm_ctx *c, double *u, double *v, double *w, double *p, doubl
   if ((st = ensure_href(c))) return st;
   const double *ds[7] = {c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw};
   double *hs[7] = {u, v, w, p, durk, dvrk, dwrk};
-  for (int f = 0; f < 7; ++f)
-    if ((st = download_field(c, ds[f], hs[f]))) return st;
+  if (!c->mixed) {
+    for (int f = 0; f < 7; ++f)
+      if ((st = download_field(c, ds[f], hs[f]))) return st;
+    return IBM_OK;
+  }
+  if (p) {
+    launch_df_to_d(c->stream, c->g.nfield, c->p32, c->plo32, c->p);
+    LAUNCHED(1);
+  }
+  if ((st = download_field(c, c->p, p))) return st;
+  const float *d32[6] = {c->u32, c->v32, c->w32, c->ru32, c->rv32, c->rw32};
+  double *h32[6] = {u, v, w, durk, dvrk, dwrk};
+  for (int f = 0; f < 6; ++f)
+    if ((st = download_field32(c, d32[f], h32[f]))) return st;
   return IBM_OK;
 }
 
@@ -500,6 +783,11 @@ int ibm_get_intermediate(ibm_ctx *c, double *du, double *dv, double *dw) {
   if (!c) return IBM_E_INVALID;
   int st;
   if ((st = ensure_href(c))) return st;
+  if (c->mixed) {
+    if ((st = download_field32(c, c->fu32, du))) return st;
+    if ((st = download_field32(c, c->fv32, dv))) return st;
+    return download_field32(c, c->fw32, dw);
+  }
   if ((st = download_field(c, c->fu, du))) return st;
   if ((st = download_field(c, c->fv, dv))) return st;
   return download_field(c, c->fw, dw);
@@ -612,11 +900,13 @@ int ibm_init_particles(ibm_ctx *c, double *vol_calc) {
   if (!c->have_particles) return set_err(c, IBM_E_STATE, "ibm_set_particles has not been called");
   launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 1);
   LAUNCHED(1);
-  launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 1);
+  if (c->mixed) launch_sphere_integrals<float>(c->stream, c->g, c->pg, c->pb, c->u32, c->v32, c->w32, 1);
+  else launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 1);
   LAUNCHED(1);
   double vol = 0.;
   CK(cudaMemcpyAsync(&vol, c->pb.red, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
+  if (c->mixed) launch_sphere_integrals<float>(c->stream, c->g, c->pg, c->pb, c->u32, c->v32, c->w32, 23);
+  else launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
   LAUNCHED(1);
   CK(cudaStreamSynchronize(c->stream));
   if (vol_calc) *vol_calc = vol;
@@ -699,7 +989,8 @@ int ibm_timed_step(ibm_ctx *c, double dt) {
 
 int ibm_chkdiv(ibm_ctx *c, double *divtot, double *divmax, int ijk[3]) {
   if (!c) return IBM_E_INVALID;
-  launch_chkdiv(c->stream, c->g, c->u, c->v, c->w, c->scratch, c->dout);
+  if (c->mixed) launch_chkdiv<float>(c->stream, c->g, c->u32, c->v32, c->w32, c->scratch, c->dout);
+  else launch_chkdiv<double>(c->stream, c->g, c->u, c->v, c->w, c->scratch, c->dout);
   LAUNCHED(2);
   CK(cudaMemcpyAsync(c->hpin, c->dout, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -722,7 +1013,8 @@ int ibm_chkdiv(ibm_ctx *c, double *divtot, double *divmax, int ijk[3]) {
 
 int ibm_chkdt(ibm_ctx *c, double *dtmax) {
   if (!c || !dtmax) return IBM_E_INVALID;
-  launch_chkdt(c->stream, c->g, c->u, c->v, c->w, c->scratch, c->dout);
+  if (c->mixed) launch_chkdt<float>(c->stream, c->g, c->u32, c->v32, c->w32, c->scratch, c->dout);
+  else launch_chkdt<double>(c->stream, c->g, c->u, c->v, c->w, c->scratch, c->dout);
   LAUNCHED(2);
   CK(cudaMemcpyAsync(c->hpin, c->dout, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -734,7 +1026,8 @@ int ibm_slip_residual(ibm_ctx *c, double *maxres, double *rmsres) {
   if (!c) return IBM_E_INVALID;
   if (c->pg.np == 0) { if (maxres) *maxres = 0; if (rmsres) *rmsres = 0; return IBM_OK; }
   // re-interpolate the forced field (valid between ibm_forcing_loop and ibm_project)
-  launch_ibm_interp_force<double>(c->stream, c->g, c->pg, c->ib, c->fu, c->fv, c->fw, 1., -1);
+  if (c->mixed) launch_ibm_interp_force_f(c->stream, c->g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, 1., -1);
+  else launch_ibm_interp_force<double>(c->stream, c->g, c->pg, c->ib, c->fu, c->fv, c->fw, 1., -1);
   LAUNCHED(1);
   launch_slip_residual(c->stream, c->pg, c->ib, c->dout + 16);
   LAUNCHED(1);
@@ -789,6 +1082,236 @@ int ibm_sync(ibm_ctx *c) {
   if (!c) return IBM_E_INVALID;
   CK(cudaStreamSynchronize(c->stream));
   return check_flags(c);
+}
+
+/* --- learned forcing -------------------------------------------------------- */
+
+int ibm_harvest(ibm_ctx *c, int capacity, int stride, int passes) {
+  if (!c) return IBM_E_INVALID;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "harvesting needs IBM_MODE_MIXED_LEARNED");
+  if (capacity < 0 || (capacity > 0 && (stride < 1 || passes < 0))) return set_err(c, IBM_E_INVALID, "bad harvest arguments");
+  if (capacity == 0) {
+    c->harvesting = false;
+    return IBM_OK;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  void *old[] = {c->hv.feat, c->hv.pidx, c->hv.targ, c->hv.count};
+  for (void *q : old)
+    if (q) cudaFree(q);
+  c->hv = HarvestArgs{};
+  int st;
+  if ((st = dalloc(c, &c->hv.feat, (size_t)capacity * 96))) return st;
+  if ((st = dalloc(c, &c->hv.pidx, (size_t)capacity))) return st;
+  if ((st = dalloc(c, &c->hv.targ, (size_t)capacity * 3))) return st;
+  if ((st = dalloc(c, &c->hv.count, 2))) return st;
+  c->hv.cap = capacity;
+  c->hv.stride = stride;
+  c->hv.phase = 0;
+  c->hv_passes = passes;
+  c->harvesting = true;
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
+int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsigned seed, int reinit, double *loss) {
+  if (!c) return IBM_E_INVALID;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "training needs IBM_MODE_MIXED_LEARNED");
+  if (nsteps < 0 || batch < 1 || !(lr > 0)) return set_err(c, IBM_E_INVALID, "bad training arguments");
+  if (!c->hv.count) return set_err(c, IBM_E_STATE, "no harvested samples (ibm_harvest)");
+  int cnt[2];
+  CK(cudaMemcpyAsync(cnt, c->hv.count, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const int n = cnt[1];
+  if (n < 1) return set_err(c, IBM_E_STATE, "no harvested samples (ibm_harvest)");
+  if (reinit || !c->stats_ready) {
+    // standardisation from the samples (host, once), fresh weights and moments
+    std::vector<float> f((size_t)n * 96), t((size_t)n * 3);
+    CK(cudaMemcpy(f.data(), c->hv.feat, f.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(t.data(), c->hv.targ, t.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    std::vector<float> nrm(198);
+    for (int q = 0; q < 99; ++q) {
+      const int nc = q < 96 ? 96 : 3;
+      const float *a = q < 96 ? f.data() + q : t.data() + (q - 96);
+      double s = 0, s2 = 0;
+      for (int r = 0; r < n; ++r) s += a[(size_t)r * nc];
+      const double mu = s / n;
+      for (int r = 0; r < n; ++r) s2 += (a[(size_t)r * nc] - mu) * (a[(size_t)r * nc] - mu);
+      const double sd = std::sqrt(s2 / n);
+      if (q < 96) {
+        nrm[q] = (float)mu;
+        nrm[96 + q] = sd > 1e-30 ? (float)(1. / sd) : 0.f;
+      } else {
+        nrm[192 + (q - 96)] = (float)mu;
+        nrm[195 + (q - 96)] = sd > 1e-30 ? (float)sd : 1.f;
+      }
+    }
+    CK(cudaMemcpy(c->norm, nrm.data(), nrm.size() * sizeof(float), cudaMemcpyHostToDevice));
+    std::vector<float> w;
+    init_mlp_params(w, seed);
+    CK(cudaMemcpy(c->mt.params, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemsetAsync(c->mt.m, 0, w.size() * sizeof(float), c->stream));
+    CK(cudaMemsetAsync(c->mt.v, 0, w.size() * sizeof(float), c->stream));
+    launch_mlp_refresh(c->stream, c->mt.params, c->mt.w1b, c->mt.w2b, c->mt.w2tb);
+    LAUNCHED(1);
+    c->train_step = 0;
+    c->stats_ready = true;
+  }
+  if (c->tcap < n) {
+    if (c->tx) cudaFree(c->tx);
+    if (c->tt) cudaFree(c->tt);
+    c->tx = nullptr; c->tt = nullptr; c->tcap = 0;
+    int st;
+    if ((st = dalloc(c, &c->tx, (size_t)n * 96))) return st;
+    if ((st = dalloc(c, &c->tt, (size_t)n * 3))) return st;
+    c->tcap = n;
+  }
+  launch_mlp_stage(c->stream, n, c->hv.feat, c->hv.targ, c->norm, c->norm + 96, c->norm + 192, c->norm + 195, c->tx,
+                   c->tt);
+  LAUNCHED(1);
+  if (c->mt_cap < batch) {
+    CK(cudaStreamSynchronize(c->stream));
+    free_mlp_batch(c->mt);
+    c->mt_cap = 0;
+    int st;
+    if ((st = alloc_mlp_batch(c, c->mt, batch))) return st;
+    c->mt_cap = batch;
+  }
+  for (int q = 0; q < nsteps; ++q) {
+    ++c->train_step;
+    launch_mlp_gather(c->stream, n, c->tx, c->tt, batch, seed, c->train_step, c->mt.x, c->mt.t);
+    launch_mlp_train_step(c->stream, c->mt, batch, c->train_step, (float)lr);
+    LAUNCHED(8);
+  }
+  float l = 0.f;
+  CK(cudaMemcpyAsync(&l, c->mt.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (loss) *loss = l;
+  c->model_ready = true;
+  c->learn_on = true;
+  return IBM_OK;
+}
+
+int ibm_set_forcing_model(ibm_ctx *c, const float *params, const float *norm) {
+  if (!c || !params || !norm) return IBM_E_INVALID;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "a model needs IBM_MODE_MIXED_LEARNED");
+  CK(cudaMemcpyAsync(c->mt.params, params, mlp_nparam() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->norm, norm, 198 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->mt.m, 0, mlp_nparam() * sizeof(float), c->stream));
+  CK(cudaMemsetAsync(c->mt.v, 0, mlp_nparam() * sizeof(float), c->stream));
+  launch_mlp_refresh(c->stream, c->mt.params, c->mt.w1b, c->mt.w2b, c->mt.w2tb);
+  LAUNCHED(1);
+  CK(cudaStreamSynchronize(c->stream));
+  c->train_step = 0;
+  c->stats_ready = c->model_ready = c->learn_on = true;
+  return IBM_OK;
+}
+
+int ibm_get_forcing_model(ibm_ctx *c, float *params, float *norm) {
+  if (!c) return IBM_E_INVALID;
+  if (!c->model_ready) return set_err(c, IBM_E_STATE, "no model (ibm_train_forcing_model or ibm_set_forcing_model)");
+  if (params) CK(cudaMemcpyAsync(params, c->mt.params, mlp_nparam() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  if (norm) CK(cudaMemcpyAsync(norm, c->norm, 198 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
+int ibm_learned_config(ibm_ctx *c, int enable, double fallback_ratio, double plain_rms_ref) {
+  if (!c) return IBM_E_INVALID;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "needs IBM_MODE_MIXED_LEARNED");
+  if (enable && !c->model_ready) return set_err(c, IBM_E_STATE, "no model to enable");
+  if (!(fallback_ratio > 0) || plain_rms_ref < 0) return set_err(c, IBM_E_INVALID, "bad learned-forcing settings");
+  double h[8];
+  CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  h[3] = fallback_ratio;
+  if (plain_rms_ref > 0) { h[1] = plain_rms_ref; h[2] = 1.; }
+  CK(cudaMemcpyAsync(c->ls, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->learn_on = enable != 0;
+  return IBM_OK;
+}
+
+int ibm_learned_stats(ibm_ctx *c, double stats[6]) {
+  if (!c || !stats) return IBM_E_INVALID;
+  for (int q = 0; q < 6; ++q) stats[q] = 0.;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return IBM_OK;
+  double h[8];
+  int cnt[2] = {0, 0};
+  CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if (c->hv.count) CK(cudaMemcpyAsync(cnt, c->hv.count, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  stats[0] = h[0];
+  stats[1] = h[2] > 0 ? h[1] / h[2] : 0.;
+  stats[2] = h[3];
+  stats[3] = h[4];
+  stats[4] = h[5];
+  stats[5] = cnt[1];
+  return IBM_OK;
+}
+
+// test hooks on a scratch model: the library's forward/backward kernels on a
+// caller batch, for the check against a CPU reference
+static int mlp_scratch(ibm_ctx *c, const float *params, const float *x, const float *t, int nb, MlpTrainBuffers &B) {
+  int st;
+  if ((st = alloc_mlp_model(c, B))) return st;
+  if ((st = alloc_mlp_batch(c, B, nb))) return st;
+  std::vector<float> tmp;
+  CK(cudaMemcpyAsync(B.params, params, mlp_nparam() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  float *xf = nullptr;
+  if ((st = dalloc(c, &xf, (size_t)nb * 96))) return st;
+  CK(cudaMemcpyAsync(xf, x, (size_t)nb * 96 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  launch_f2bf(c->stream, (long)nb * 96, xf, B.x);
+  CK(cudaMemcpyAsync(B.t, t, (size_t)nb * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  launch_mlp_refresh(c->stream, B.params, B.w1b, B.w2b, B.w2tb);
+  LAUNCHED(2);
+  CK(cudaStreamSynchronize(c->stream));
+  cudaFree(xf);
+  return IBM_OK;
+}
+
+int ibm_mlp_gradient(ibm_ctx *c, const float *params, const float *x, const float *t, int nb, float *grad,
+                     float *loss, float *y) {
+  if (!c || !params || !x || !t || nb < 1) return IBM_E_INVALID;
+  MlpTrainBuffers B{};
+  int st = mlp_scratch(c, params, x, t, nb, B);
+  if (st == IBM_OK) {
+    launch_mlp_grad(c->stream, B, nb);
+    c->launches += 5;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && grad)
+      e = cudaMemcpyAsync(grad, B.grad, mlp_nparam() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, B.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && y)
+      e = cudaMemcpyAsync(y, B.y, (size_t)nb * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    st = cuda_err(c, e, "ibm_mlp_gradient");
+  }
+  cudaStreamSynchronize(c->stream);
+  free_mlp_batch(B);
+  free_mlp_model(B);
+  return st;
+}
+
+int ibm_mlp_fit(ibm_ctx *c, const float *params_in, const float *x, const float *t, int nb, int nsteps, double lr,
+                float *params_out, float *losses) {
+  if (!c || !params_in || !x || !t || nb < 1 || nsteps < 0 || !(lr > 0)) return IBM_E_INVALID;
+  MlpTrainBuffers B{};
+  int st = mlp_scratch(c, params_in, x, t, nb, B);
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; st == IBM_OK && e == cudaSuccess && q < nsteps; ++q) {
+    launch_mlp_train_step(c->stream, B, nb, q + 1, (float)lr);
+    c->launches += 6;
+    e = cudaGetLastError();
+    if (e == cudaSuccess && losses) e = cudaMemcpyAsync(losses + q, B.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  }
+  if (st == IBM_OK && e == cudaSuccess && params_out)
+    e = cudaMemcpyAsync(params_out, B.params, mlp_nparam() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if (st == IBM_OK && e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (st == IBM_OK) st = cuda_err(c, e, "ibm_mlp_fit");
+  cudaStreamSynchronize(c->stream);
+  free_mlp_batch(B);
+  free_mlp_model(B);
+  return st;
 }
 
 }  // extern "C"

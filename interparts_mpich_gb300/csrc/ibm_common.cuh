@@ -46,6 +46,12 @@ struct PointStencil {
   double phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
 };
 
+// FP32 weights of the same stencil for the mixed form
+struct PointStencilF {
+  int ilow, jlow, klow, ilows, jlows, klows;
+  float phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
+};
+
 // Constants of one context, passed by value to the kernels.
 struct Geo {
   int I, J, K, MX;            // grid, MX = I/2+1
@@ -57,7 +63,7 @@ struct Geo {
 struct PartGeo {
   int np, nl, nq, nb_copies, rotation;
   double radius, radfp, offset, dVlagr, dVeul, lx, ly, lz, dxi, dyi, dzi, dx, dy, dz;
-  double gacc[3], rkab[3], volp, ratiorho, mominert;
+  double gacc[3], rkab[3], volp, ratiorho, mominert, rthr;
   double kn_ss, etan_ss, kt_ss, etat_ss, muc_ss, kn_sw, etan_sw, kt_sw, etat_sw, muc_sw;
   double coeff_f, a11a_ini_pp, a11b_ini_pp, a11a_sat_pp, a11b_sat_pp, a11_ini_pw, a11_sat_pw;
   int I, J, K;
@@ -83,6 +89,35 @@ __device__ __forceinline__ float delta3f(float r) {
   if (ar > 0.5f) return (1.f / 6.f) * (5.f - 3.f * ar - sqrtf(-3.f * ((1.f - ar) * (1.f - ar)) + 1.f));
   return (1.f / 3.f) * (1.f + sqrtf(-3.f * (r * r) + 1.f));
 }
+// Error-free FP32 transformations (Knuth two-sum, FMA two-product) for
+// double-float arithmetic: a value is carried as hi + lo (about 48 bits) on the
+// FP32 pipes, which GB300 runs 64x faster than FP64.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+  p = __fmul_rn(a, b);
+  e = fmaf(a, b, -p);
+}
+// (ah + al) * (bh + bl) -> (ph + pl)
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float &ph, float &pl) {
+  float p, e;
+  two_prod(ah, bh, p, e);
+  e = fmaf(ah, bl, fmaf(al, bh, e));
+  ph = __fadd_rn(p, e);
+  pl = __fsub_rn(e, __fsub_rn(ph, p));
+}
+// (ah + al) + (bh + bl) -> (sh + sl)
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float &sh, float &sl) {
+  float s, e;
+  two_sum(ah, bh, s, e);
+  e = __fadd_rn(e, __fadd_rn(al, bl));
+  sh = __fadd_rn(s, e);
+  sl = __fsub_rn(e, __fsub_rn(sh, s));
+}
+
 // Fortran NINT (half away from zero)
 __device__ __forceinline__ int fnint(double x) { return (int)round(x); }
 

@@ -1,5 +1,7 @@
 // kernels.cuh -- launcher declarations shared by the C ABI and the kernels.
 #pragma once
+#include <cuda_bf16.h>
+
 #include "ibm_common.cuh"
 
 struct FftPlan {
@@ -10,27 +12,36 @@ struct FftPlan {
 namespace ibmk {
 
 // fluid_kernels.cu
-template <typename T>
-void launch_predict(cudaStream_t s, const Geo &g, int stage, const T *u, const T *v, const T *w, const T *p, T *ru,
-                    T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3);
-template <typename T, typename TP>
-void launch_correc(cudaStream_t s, const Geo &g, const T *fu, const T *fv, const T *fw, const T *phi, T *u, T *v,
-                   T *w, TP *pn, double fi, double fj, double fk);
+template <typename TU, typename T>
+void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
+                    T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3);
+template <typename TF, typename TPh, typename TU>
+void launch_correc(cudaStream_t s, const Geo &g, const TF *fu, const TF *fv, const TF *fw, const TPh *phi, TU *u,
+                   TU *v, TU *w, double *pn, float *pn32, double fi, double fj, double fk);
+void launch_correc_mixed(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
+                         const float *phi, float *u, float *v, float *w, float *ph, float *pl, double fi, double fj,
+                         double fk);
+void launch_df_to_d(cudaStream_t s, long n, const float *h, const float *l, double *d);
+void launch_d_to_df(cudaStream_t s, long n, const double *d, float *h, float *l);
 template <typename T> void launch_ref_to_dev(cudaStream_t s, const Geo &g, const double *ref, T *dev);
 template <typename T> void launch_dev_to_ref(cudaStream_t s, const Geo &g, const T *dev, double *ref);
-void launch_chkdiv(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w,
-                   double *scratch, double *out);
-void launch_chkdt(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w,
-                  double *scratch, double *out);
-void launch_wallshear(cudaStream_t s, const Geo &g, const double *v, double *out);
+template <typename T>
+void launch_chkdiv(cudaStream_t s, const Geo &g, const T *u, const T *v, const T *w, double *scratch, double *out);
+template <typename T>
+void launch_chkdt(cudaStream_t s, const Geo &g, const T *u, const T *v, const T *w, double *scratch, double *out);
+template <typename T>
+void launch_wallshear(cudaStream_t s, const Geo &g, const T *v, double *scratch, double *out);
 void launch_d2f(cudaStream_t s, long n, const double *a, float *b);
 void launch_f2d(cudaStream_t s, long n, const float *a, double *b);
 
 // fft_kernels.cu
-template <typename T>
-void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const T *fu, const T *fv,
-                    T *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
-                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches);
+// TIn: type of the velocity read by fillps (the forced predictor, or the
+// corrected state for the defect-correction residual); T: FFT type;
+// res64: evaluate the divergence in FP64 arithmetic.
+template <typename TIn, typename T>
+void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
+                    const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
+                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64 = false);
 template <typename T> int poisson_set_smem_limits();
 
 // ibm_kernels.cu
@@ -38,6 +49,7 @@ struct IbmBuffers {
   // per-point arrays [np*nl]
   double *xfp, *yfp, *zfp, *ul, *vl, *wl, *dudtl, *dvdtl, *dwdtl, *fxl, *fyl, *fzl;
   PointStencil *st;
+  PointStencilF *st32;
   int *nla;          // [np]
   double *pf;        // particle scalar fields [PF_N*np]
   double *diag;      // [8] force totals etc.
@@ -54,6 +66,51 @@ void launch_ibm_spread(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffe
 template <typename T>
 void launch_zero_plane(cudaStream_t s, const Geo &g, T *f, int k);
 void launch_slip_residual(cudaStream_t s, const PartGeo &pg, IbmBuffers b, double *out);
+// mixed form: FP32 fields, FP32 weights and interpolation sums, FP64 point
+// forces and per-particle sums
+void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b);
+void launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                               const float *fv, const float *fw, double dt, int first, const int *gate = nullptr);
+void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
+                         float *fw, double dt, const float *dfin = nullptr, const int *gate = nullptr);
+struct HarvestArgs {
+  float *feat;   // [cap][96] raw features
+  int *pidx;     // [cap] point index
+  float *targ;   // [cap][3] (F_final - F0) * dt
+  int *count;    // [2]: reserved slots, slots with targets
+  int cap, stride, phase;
+};
+void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                           const float *fv, const float *fw, double dt, const float *mu, const float *isig,
+                           __nv_bfloat16 *X, const HarvestArgs &H);
+void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs &H, double dt);
+void launch_ibm_learned_apply(cudaStream_t s, const PartGeo &pg, IbmBuffers b, const float *Y, const float *tmu,
+                              const float *tsig, double dt, float *dF);
+void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, double *scratch, long npts,
+                              double *ls, int *gate, int plain);
+
+// mlp_kernels.cu (learned forcing model)
+struct MlpTrainBuffers {
+  float *params, *m, *v, *grad, *loss;       // FP32 masters, Adam moments, gradient, loss accumulator
+  __nv_bfloat16 *w1b, *w2b, *w2tb;           // BF16 copies of W1, W2 and W2 transposed
+  __nv_bfloat16 *x;                           // [nb][96] batch features
+  float *t, *y, *z1, *z2;                     // targets [nb][3], outputs, pre-activations [nb][128]
+  __nv_bfloat16 *h1, *h2, *dz1, *dz2;         // [nb][128]
+};
+int mlp_nparam();
+int mlp_set_smem_limits();
+void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
+                        const __nv_bfloat16 *w2b, const float *params, float *y, float *z1, float *z2,
+                        __nv_bfloat16 *h1, __nv_bfloat16 *h2, int train);
+void launch_mlp_refresh(cudaStream_t s, const float *params, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b,
+                        __nv_bfloat16 *w2tb);
+void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr);
+void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb);
+void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,
+                      const float *tmu, const float *tsig, __nv_bfloat16 *X, float *T);
+void launch_mlp_gather(cudaStream_t s, int n, const __nv_bfloat16 *X, const float *T, int nb, unsigned seed, int step,
+                       __nv_bfloat16 *bx, float *bt);
+void launch_f2bf(cudaStream_t s, long n, const float *a, __nv_bfloat16 *b);
 
 // particle_kernels.cu
 struct PartBuffers {

@@ -1,0 +1,493 @@
+// mlp_kernels.cu -- learned multidirect-forcing correction.
+//
+// A per-Lagrangian-point MLP 96 -> 128 -> 128 -> 3 (tanh-form GELU) predicts
+// the rest of the multidirect forcing after the first pass: from the slip
+// left by pass 0 and the local velocity field it returns dF*dt, the
+// velocity-unit correction that the plain passes 1 and 2 would add
+// (interp_spread.f90 / forcing.f90, Nl = 3).
+//
+// Layers 1 and 2 run on the tensor cores: mma.sync m16n8k16 with BF16
+// operands (features, weights, hidden activations) and FP32 accumulators;
+// layer 3 (128 -> 3) and GELU run on the FP32 pipes.  Training (forward,
+// backward, weight gradients, Adam) uses the same fragments; the FP32 master
+// weights live on the device and BF16 copies are refreshed after each step.
+//
+// Parameter vector (FP32): W1[128][96], b1[128], W2[128][128], b2[128],
+// W3[3][128], b3[3].
+#include <cuda_bf16.h>
+
+#include "kernels.cuh"
+
+namespace ibmk {
+
+typedef __nv_bfloat16 bf16;
+
+// ---- tensor-core fragment helpers (PTX ISA, mma.m16n8k16 .bf16) -----------
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+// A tile row-major in shared memory (row stride lda, bf16 elements):
+// fragment of rows m0..m0+15, columns k0..k0+15
+__device__ __forceinline__ void load_a(uint32_t a[4], const bf16 *As, int lda, int m0, int k0, int lane) {
+  const int g = lane >> 2, t = lane & 3;
+  a[0] = *reinterpret_cast<const uint32_t *>(&As[(m0 + g) * lda + k0 + 2 * t]);
+  a[1] = *reinterpret_cast<const uint32_t *>(&As[(m0 + g + 8) * lda + k0 + 2 * t]);
+  a[2] = *reinterpret_cast<const uint32_t *>(&As[(m0 + g) * lda + k0 + 2 * t + 8]);
+  a[3] = *reinterpret_cast<const uint32_t *>(&As[(m0 + g + 8) * lda + k0 + 2 * t + 8]);
+}
+// B operand stored n-major (Bs[n][k], k contiguous, stride ldb)
+__device__ __forceinline__ void load_b(uint32_t b[2], const bf16 *Bs, int ldb, int n0, int k0, int lane) {
+  const int g = lane >> 2, t = lane & 3;
+  b[0] = *reinterpret_cast<const uint32_t *>(&Bs[(n0 + g) * ldb + k0 + 2 * t]);
+  b[1] = *reinterpret_cast<const uint32_t *>(&Bs[(n0 + g) * ldb + k0 + 2 * t + 8]);
+}
+
+__device__ __forceinline__ float gelu_f(float z) {
+  const float c = 0.7978845608028654f, a = 0.044715f;
+  return 0.5f * z * (1.f + tanhf(c * (z + a * z * z * z)));
+}
+__device__ __forceinline__ float gelu_grad_f(float z) {
+  const float c = 0.7978845608028654f, a = 0.044715f;
+  const float t = tanhf(c * (z + a * z * z * z));
+  return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * c * (1.f + 3.f * a * z * z);
+}
+
+constexpr int NIN = 96, NH = 128, NOUT = 3;
+constexpr int LDX = NIN + 8, LDH = NH + 8;  // padded shared-memory rows
+constexpr int TILE = 64;                    // rows per CTA tile (4 warps x 16)
+constexpr int OFF_B1 = NH * NIN, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
+              OFF_B3 = OFF_W3 + NOUT * NH, NPARAM = OFF_B3 + NOUT;
+
+// ---------------------------------------------------------------------------
+// Forward: X (N x 96, bf16) -> Y (N x 3, fp32).  Persistent CTAs keep W1, W2
+// in shared memory.  TRAIN additionally stores Z1, Z2 (fp32) and H1, H2
+// (bf16) for the backward pass.
+// ---------------------------------------------------------------------------
+struct MlpFwdArgs {
+  const bf16 *x;
+  int n;
+  const bf16 *w1b, *w2b;
+  const float *params;
+  float *y;
+  float *z1, *z2;
+  bf16 *h1, *h2;
+};
+
+template <bool TRAIN>
+__global__ void __launch_bounds__(128) k_mlp_forward(MlpFwdArgs A) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  bf16 *W1s = reinterpret_cast<bf16 *>(sm);   // [128][LDX]
+  bf16 *W2s = W1s + NH * LDX;                 // [128][LDH]
+  bf16 *Xs = W2s + NH * LDH;                  // [64][LDX]
+  bf16 *H1s = Xs + TILE * LDX;                // [64][LDH]
+  bf16 *H2s = H1s + TILE * LDH;               // [64][LDH]
+  float *bias = reinterpret_cast<float *>(H2s + TILE * LDH);  // b1, b2, W3, b3
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int t = tid; t < NH * NIN; t += blockDim.x) W1s[(t / NIN) * LDX + t % NIN] = A.w1b[t];
+  for (int t = tid; t < NH * NH; t += blockDim.x) W2s[(t / NH) * LDH + t % NH] = A.w2b[t];
+  for (int t = tid; t < NH; t += blockDim.x) { bias[t] = A.params[OFF_B1 + t]; bias[NH + t] = A.params[OFF_B2 + t]; }
+  for (int t = tid; t < NOUT * NH + NOUT; t += blockDim.x) bias[2 * NH + t] = A.params[OFF_W3 + t];
+  __syncthreads();
+  const float *b1 = bias, *b2 = bias + NH, *w3 = bias + 2 * NH, *b3 = w3 + NOUT * NH;
+  const int ntiles = (A.n + TILE - 1) / TILE;
+  const int g = lane >> 2, tq = lane & 3;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int row0 = tile * TILE;
+    // stage the feature tile (rows beyond n are zero)
+    for (int t = tid; t < TILE * NIN / 8; t += blockDim.x) {
+      const int r = t / (NIN / 8), c8 = (t % (NIN / 8)) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (row0 + r < A.n) v = *reinterpret_cast<const uint4 *>(&A.x[(long)(row0 + r) * NIN + c8]);
+      *reinterpret_cast<uint4 *>(&Xs[r * LDX + c8]) = v;
+    }
+    __syncthreads();
+    const int m0 = warp * 16;
+    // layer 1: 16 rows x 128 columns per warp
+    float acc[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+    for (int k0 = 0; k0 < NIN; k0 += 16) {
+      uint32_t a[4];
+      load_a(a, Xs, LDX, m0, k0, lane);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        uint32_t b[2];
+        load_b(b, W1s, LDX, j * 8, k0, lane);
+        mma16816(acc[j], a, b);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int col = j * 8 + 2 * tq;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = m0 + g + 8 * h;
+        const float z0 = acc[j][2 * h] + b1[col], z1 = acc[j][2 * h + 1] + b1[col + 1];
+        const bf16 h0 = __float2bfloat16(gelu_f(z0)), h1v = __float2bfloat16(gelu_f(z1));
+        H1s[r * LDH + col] = h0;
+        H1s[r * LDH + col + 1] = h1v;
+        if (TRAIN && row0 + r < A.n) {
+          const long o = (long)(row0 + r) * NH + col;
+          A.z1[o] = z0; A.z1[o + 1] = z1;
+          A.h1[o] = h0; A.h1[o + 1] = h1v;
+        }
+      }
+    }
+    __syncwarp();
+    // layer 2 (each warp reads only its own 16 rows of H1)
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+    for (int k0 = 0; k0 < NH; k0 += 16) {
+      uint32_t a[4];
+      load_a(a, H1s, LDH, m0, k0, lane);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        uint32_t b[2];
+        load_b(b, W2s, LDH, j * 8, k0, lane);
+        mma16816(acc[j], a, b);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int col = j * 8 + 2 * tq;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = m0 + g + 8 * h;
+        const float z0 = acc[j][2 * h] + b2[col], z1 = acc[j][2 * h + 1] + b2[col + 1];
+        const bf16 h0 = __float2bfloat16(gelu_f(z0)), h1v = __float2bfloat16(gelu_f(z1));
+        H2s[r * LDH + col] = h0;
+        H2s[r * LDH + col + 1] = h1v;
+        if (TRAIN && row0 + r < A.n) {
+          const long o = (long)(row0 + r) * NH + col;
+          A.z2[o] = z0; A.z2[o + 1] = z1;
+          A.h2[o] = h0; A.h2[o + 1] = h1v;
+        }
+      }
+    }
+    __syncwarp();
+    // layer 3 on the FP32 pipes: 16 rows x 3 outputs per warp
+    for (int q = lane; q < 16 * NOUT; q += 32) {
+      const int r = m0 + q / NOUT, o = q % NOUT;
+      float s = b3[o];
+      for (int c = 0; c < NH; ++c) s += __bfloat162float(H2s[r * LDH + c]) * w3[o * NH + c];
+      if (row0 + r < A.n) A.y[(long)(row0 + r) * NOUT + o] = s;
+    }
+    __syncthreads();
+  }
+}
+
+size_t mlp_forward_smem() {
+  return (size_t)(NH * LDX + NH * LDH + TILE * LDX + 2 * TILE * LDH) * sizeof(bf16) +
+         (size_t)(2 * NH + NOUT * NH + NOUT) * sizeof(float);
+}
+
+void launch_mlp_forward(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, const bf16 *w2b, const float *params,
+                        float *y, float *z1, float *z2, bf16 *h1, bf16 *h2, int train) {
+  if (n <= 0) return;
+  MlpFwdArgs A{x, n, w1b, w2b, params, y, z1, z2, h1, h2};
+  const int ntiles = (n + TILE - 1) / TILE;
+  const int grid = ntiles < 2 * 152 ? ntiles : 2 * 152;
+  if (train) k_mlp_forward<true><<<grid, 128, mlp_forward_smem(), s>>>(A);
+  else k_mlp_forward<false><<<grid, 128, mlp_forward_smem(), s>>>(A);
+}
+
+// ---------------------------------------------------------------------------
+// Backward through layer 3, GELU and layer 2 for a batch: dY = 2(Y-T)/B;
+// dH2 = dY W3; dZ2 = dH2 * gelu'(Z2) (bf16); dH1 = dZ2 W2 (tensor cores);
+// dZ1 = dH1 * gelu'(Z1) (bf16).  Bias and W3 gradients accumulate into grad.
+// ---------------------------------------------------------------------------
+struct MlpBwdArgs {
+  int nb;
+  const float *y, *t, *z1, *z2;
+  const bf16 *h2;
+  const bf16 *w2tb;  // W2 transposed: [in][out]
+  const float *params;
+  bf16 *dz1, *dz2;
+  float *grad;
+  float *loss;
+};
+
+__global__ void __launch_bounds__(128) k_mlp_backward(MlpBwdArgs A) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  bf16 *W2t = reinterpret_cast<bf16 *>(sm);  // [128][LDH]: W2t[i][o]
+  bf16 *D2 = W2t + NH * LDH;                 // [64][LDH] dZ2 tile
+  float *w3 = reinterpret_cast<float *>(D2 + TILE * LDH);  // [3][128]
+  float *dy = w3 + NOUT * NH;                              // [64][3]
+  float *red = dy + TILE * NOUT;                           // [128] bias-gradient partials
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int t = tid; t < NH * NH; t += blockDim.x) W2t[(t / NH) * LDH + t % NH] = A.w2tb[t];
+  for (int t = tid; t < NOUT * NH; t += blockDim.x) w3[t] = A.params[OFF_W3 + t];
+  const int row0 = blockIdx.x * TILE;
+  const float inv = 2.f / (float)A.nb;
+  float lsum = 0.f;
+  for (int q = tid; q < TILE * NOUT; q += blockDim.x) {
+    const int r = q / NOUT, o = q % NOUT;
+    float d = 0.f;
+    if (row0 + r < A.nb) {
+      const float e = A.y[(long)(row0 + r) * NOUT + o] - A.t[(long)(row0 + r) * NOUT + o];
+      d = inv * e;
+      lsum += e * e;
+    }
+    dy[q] = d;
+  }
+  __syncthreads();
+  // loss, W3 and b3 gradients
+  for (int q = tid; q < NOUT * NH + NOUT; q += blockDim.x) {
+    float s = 0.f;
+    if (q < NOUT * NH) {
+      const int o = q / NH, c = q % NH;
+      for (int r = 0; r < TILE && row0 + r < A.nb; ++r)
+        s += dy[r * NOUT + o] * __bfloat162float(A.h2[(long)(row0 + r) * NH + c]);
+      atomicAdd(&A.grad[OFF_W3 + q], s);
+    } else {
+      const int o = q - NOUT * NH;
+      for (int r = 0; r < TILE; ++r) s += dy[r * NOUT + o];
+      atomicAdd(&A.grad[OFF_B3 + o], s);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if (lane == 0) atomicAdd(A.loss, lsum / (float)A.nb);
+  // dZ2 = (dY W3) * gelu'(Z2)
+  for (int q = tid; q < TILE * NH; q += blockDim.x) {
+    const int r = q / NH, c = q % NH;
+    float v = 0.f;
+    if (row0 + r < A.nb) {
+      const float dh = dy[r * NOUT] * w3[c] + dy[r * NOUT + 1] * w3[NH + c] + dy[r * NOUT + 2] * w3[2 * NH + c];
+      v = dh * gelu_grad_f(A.z2[(long)(row0 + r) * NH + c]);
+    }
+    const bf16 vb = __float2bfloat16(v);
+    D2[r * LDH + c] = vb;
+    if (row0 + r < A.nb) A.dz2[(long)(row0 + r) * NH + c] = vb;
+  }
+  __syncthreads();
+  // b2 gradient (sum of the rounded dZ2 over the tile rows)
+  for (int c = tid; c < NH; c += blockDim.x) {
+    float s = 0.f;
+    for (int r = 0; r < TILE; ++r) s += __bfloat162float(D2[r * LDH + c]);
+    atomicAdd(&A.grad[OFF_B2 + c], s);
+  }
+  // dH1 = dZ2 W2 (K = 128 outputs of layer 2), then dZ1
+  const int m0 = warp * 16, g = lane >> 2, tq = lane & 3;
+  float acc[16][4];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+  for (int k0 = 0; k0 < NH; k0 += 16) {
+    uint32_t a[4];
+    load_a(a, D2, LDH, m0, k0, lane);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      uint32_t b[2];
+      load_b(b, W2t, LDH, j * 8, k0, lane);
+      mma16816(acc[j], a, b);
+    }
+  }
+  __syncthreads();
+  float *colsum = red;
+  for (int c = tid; c < NH; c += blockDim.x) colsum[c] = 0.f;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int col = j * 8 + 2 * tq;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = m0 + g + 8 * h;
+      if (row0 + r < A.nb) {
+        const long o = (long)(row0 + r) * NH + col;
+        const bf16 d0 = __float2bfloat16(acc[j][2 * h] * gelu_grad_f(A.z1[o]));
+        const bf16 d1 = __float2bfloat16(acc[j][2 * h + 1] * gelu_grad_f(A.z1[o + 1]));
+        A.dz1[o] = d0;
+        A.dz1[o + 1] = d1;
+        atomicAdd(&colsum[col], __bfloat162float(d0));
+        atomicAdd(&colsum[col + 1], __bfloat162float(d1));
+      }
+    }
+  }
+  __syncthreads();
+  for (int c = tid; c < NH; c += blockDim.x) atomicAdd(&A.grad[OFF_B1 + c], colsum[c]);
+}
+
+size_t mlp_backward_smem() {
+  return (size_t)(NH * LDH + TILE * LDH) * sizeof(bf16) + (size_t)(NOUT * NH + TILE * NOUT + NH) * sizeof(float);
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient G[o][i] += sum_r D[r][o] * H[r][i] over a chunk of batch
+// rows (tensor cores, K = batch): 8 warps, warp w owns outputs 16w..16w+15.
+// ---------------------------------------------------------------------------
+template <int NI>
+__global__ void __launch_bounds__(256) k_mlp_wgrad(int nb, const bf16 *__restrict__ D, const bf16 *__restrict__ H,
+                                                    float *__restrict__ G, int chunk) {
+  constexpr int KT = 32;            // batch rows per shared-memory stage
+  constexpr int LDK = KT + 8;
+  __shared__ __align__(16) bf16 Ds[NH * LDK];   // Ds[o][r]
+  __shared__ __align__(16) bf16 Hs[NI * LDK];   // Hs[i][r]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, tq = lane & 3;
+  constexpr int NJ = NI / 8;
+  float acc[NJ][4];
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  const int r0 = blockIdx.x * chunk, r1 = min(nb, r0 + chunk);
+  for (int rb = r0; rb < r1; rb += KT) {
+    __syncthreads();
+    for (int t = tid; t < KT * NH; t += blockDim.x) {
+      const int r = t / NH, o = t % NH;
+      Ds[o * LDK + r] = (rb + r < r1) ? D[(long)(rb + r) * NH + o] : __float2bfloat16(0.f);
+    }
+    for (int t = tid; t < KT * NI; t += blockDim.x) {
+      const int r = t / NI, i = t % NI;
+      Hs[i * LDK + r] = (rb + r < r1) ? H[(long)(rb + r) * NI + i] : __float2bfloat16(0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k0 = 0; k0 < KT; k0 += 16) {
+      uint32_t a[4];
+      load_a(a, Ds, LDK, warp * 16, k0, lane);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        uint32_t b[2];
+        load_b(b, Hs, LDK, j * 8, k0, lane);
+        mma16816(acc[j], a, b);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int col = j * 8 + 2 * tq;
+    const int o0 = warp * 16 + g;
+    atomicAdd(&G[o0 * NI + col], acc[j][0]);
+    atomicAdd(&G[o0 * NI + col + 1], acc[j][1]);
+    atomicAdd(&G[(o0 + 8) * NI + col], acc[j][2]);
+    atomicAdd(&G[(o0 + 8) * NI + col + 1], acc[j][3]);
+  }
+}
+
+// Adam (FP32 masters) followed by the BF16 weight copies
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m,
+                       float *__restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const float g = gr[t];
+    const float mm = b1 * m[t] + (1.f - b1) * g;
+    const float vv = b2 * v[t] + (1.f - b2) * g * g;
+    m[t] = mm;
+    v[t] = vv;
+    p[t] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+  }
+}
+__global__ void k_refresh_bf16(const float *__restrict__ p, bf16 *__restrict__ w1b, bf16 *__restrict__ w2b,
+                               bf16 *__restrict__ w2tb) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < NH * NIN + NH * NH; t += gridDim.x * blockDim.x) {
+    if (t < NH * NIN) {
+      w1b[t] = __float2bfloat16(p[t]);
+    } else {
+      const int q = t - NH * NIN, o = q / NH, i = q % NH;
+      const bf16 v = __float2bfloat16(p[OFF_W2 + q]);
+      w2b[q] = v;
+      w2tb[i * NH + o] = v;
+    }
+  }
+}
+
+int mlp_nparam() { return NPARAM; }
+
+void launch_mlp_refresh(cudaStream_t s, const float *params, bf16 *w1b, bf16 *w2b, bf16 *w2tb) {
+  k_refresh_bf16<<<64, 256, 0, s>>>(params, w1b, w2b, w2tb);
+}
+
+// one optimisation step on a batch already staged in x (bf16) and t (fp32)
+void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr) {
+  cudaMemsetAsync(B.grad, 0, NPARAM * sizeof(float), s);
+  cudaMemsetAsync(B.loss, 0, sizeof(float), s);
+  launch_mlp_forward(s, B.x, nb, B.w1b, B.w2b, B.params, B.y, B.z1, B.z2, B.h1, B.h2, 1);
+  MlpBwdArgs A{nb, B.y, B.t, B.z1, B.z2, B.h2, B.w2tb, B.params, B.dz1, B.dz2, B.grad, B.loss};
+  k_mlp_backward<<<(nb + TILE - 1) / TILE, 128, mlp_backward_smem(), s>>>(A);
+  const int chunk = 512;
+  const int nchunk = (nb + chunk - 1) / chunk;
+  k_mlp_wgrad<NH><<<nchunk, 256, 0, s>>>(nb, B.dz2, B.h1, B.grad + OFF_W2, chunk);
+  k_mlp_wgrad<NIN><<<nchunk, 256, 0, s>>>(nb, B.dz1, B.x, B.grad, chunk);
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  k_adam<<<64, 256, 0, s>>>(B.params, B.grad, B.m, B.v, NPARAM, lr, b1, b2, 1e-8f, c1, c2);
+  k_refresh_bf16<<<64, 256, 0, s>>>(B.params, B.w1b, B.w2b, B.w2tb);
+}
+
+// gradient only (for the check against the CPU reference)
+void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb) {
+  cudaMemsetAsync(B.grad, 0, NPARAM * sizeof(float), s);
+  cudaMemsetAsync(B.loss, 0, sizeof(float), s);
+  launch_mlp_forward(s, B.x, nb, B.w1b, B.w2b, B.params, B.y, B.z1, B.z2, B.h1, B.h2, 1);
+  MlpBwdArgs A{nb, B.y, B.t, B.z1, B.z2, B.h2, B.w2tb, B.params, B.dz1, B.dz2, B.grad, B.loss};
+  k_mlp_backward<<<(nb + TILE - 1) / TILE, 128, mlp_backward_smem(), s>>>(A);
+  const int chunk = 512;
+  const int nchunk = (nb + chunk - 1) / chunk;
+  k_mlp_wgrad<NH><<<nchunk, 256, 0, s>>>(nb, B.dz2, B.h1, B.grad + OFF_W2, chunk);
+  k_mlp_wgrad<NIN><<<nchunk, 256, 0, s>>>(nb, B.dz1, B.x, B.grad, chunk);
+}
+
+// harvested samples -> standardised training set: X (bf16), T (fp32)
+__global__ void k_mlp_stage(int n, const float *__restrict__ feat, const float *__restrict__ targ,
+                            const float *__restrict__ mu, const float *__restrict__ isig,
+                            const float *__restrict__ tmu, const float *__restrict__ tsig, bf16 *__restrict__ X,
+                            float *__restrict__ T) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < (long)n * NIN; q += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(q % NIN);
+    X[q] = __float2bfloat16((feat[q] - mu[c]) * isig[c]);
+  }
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < (long)n * NOUT; q += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(q % NOUT);
+    T[q] = (targ[q] - tmu[c]) / tsig[c];
+  }
+}
+void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,
+                      const float *tmu, const float *tsig, bf16 *X, float *T) {
+  k_mlp_stage<<<1216, 256, 0, s>>>(n, feat, targ, mu, isig, tmu, tsig, X, T);
+}
+
+// batch of nb rows drawn with replacement by a counter-based hash of
+// (seed, step, row) -- no host round trip between optimisation steps
+__device__ __forceinline__ unsigned mix32(unsigned x) {
+  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+  return x;
+}
+__global__ void k_mlp_gather(int n, const bf16 *__restrict__ X, const float *__restrict__ T, int nb, unsigned seed,
+                             int step, bf16 *__restrict__ bx, float *__restrict__ bt) {
+  for (int r = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < nb; r += gridDim.x * (blockDim.x / 32)) {
+    const unsigned h = mix32(seed ^ mix32((unsigned)step * 0x9E3779B9U + (unsigned)r));
+    const int src = (int)(h % (unsigned)n);
+    const int lane = threadIdx.x & 31;
+    // 96 bf16 = 48 words per row
+    const uint32_t *xs = reinterpret_cast<const uint32_t *>(X + (long)src * NIN);
+    uint32_t *xd = reinterpret_cast<uint32_t *>(bx + (long)r * NIN);
+    for (int w = lane; w < NIN / 2; w += 32) xd[w] = xs[w];
+    if (lane < NOUT) bt[(long)r * NOUT + lane] = T[(long)src * NOUT + lane];
+  }
+}
+void launch_mlp_gather(cudaStream_t s, int n, const bf16 *X, const float *T, int nb, unsigned seed, int step, bf16 *bx,
+                       float *bt) {
+  k_mlp_gather<<<(nb + 7) / 8 < 1216 ? (nb + 7) / 8 : 1216, 256, 0, s>>>(n, X, T, nb, seed, step, bx, bt);
+}
+
+__global__ void k_f2bf(long n, const float *__restrict__ a, bf16 *__restrict__ b) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+    b[q] = __float2bfloat16(a[q]);
+}
+void launch_f2bf(cudaStream_t s, long n, const float *a, bf16 *b) { k_f2bf<<<608, 256, 0, s>>>(n, a, b); }
+
+int mlp_set_smem_limits() {
+  cudaError_t e1 = cudaFuncSetAttribute(k_mlp_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)mlp_forward_smem());
+  cudaError_t e2 = cudaFuncSetAttribute(k_mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)mlp_forward_smem());
+  cudaError_t e3 = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)mlp_backward_smem());
+  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
+}
+
+}  // namespace ibmk

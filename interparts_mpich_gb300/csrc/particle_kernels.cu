@@ -52,6 +52,28 @@ __device__ __forceinline__ void copy_shift_sphere(int nbrecv, double lx, double 
   }
 }
 
+// corner signed-distance fraction of a cell cut by the sphere surface
+// (intgr_over_sphere.f90:357-374): sum of the positive signed distances over
+// the sum of their magnitudes, corners in the reference's order
+__device__ __forceinline__ double corner_fraction(double radius, double dxm2, double dxp2, double dym2, double dyp2,
+                                                  double dzm2, double dzp2) {
+  double sg[8];
+  sg[0] = radius - sqrt(dxm2 + dym2 + dzm2);
+  sg[1] = radius - sqrt(dxm2 + dyp2 + dzm2);
+  sg[2] = radius - sqrt(dxp2 + dyp2 + dzm2);
+  sg[3] = radius - sqrt(dxp2 + dym2 + dzm2);
+  sg[4] = radius - sqrt(dxm2 + dym2 + dzp2);
+  sg[5] = radius - sqrt(dxm2 + dyp2 + dzp2);
+  sg[6] = radius - sqrt(dxp2 + dyp2 + dzp2);
+  sg[7] = radius - sqrt(dxp2 + dym2 + dzp2);
+  double sum1 = 0., sum2 = 0.;
+  for (int cp = 0; cp < 8; ++cp) {
+    if (sg[cp] > 0.) sum1 = sum1 + sg[cp];
+    sum2 = sum2 + fabs(sg[cp]);
+  }
+  return sum1 / sum2;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffers b, const T *__restrict__ u,
                                                     const T *__restrict__ v, const T *__restrict__ w, int type) {
@@ -62,6 +84,10 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
   const double dx = 1. / g.dxi, dy = 1. / g.dyi, dz = 1. / g.dzi;
   const double radin = radius - 2. * dx;
   const double radin2 = radin * radin;
+  // sqrt(d2) >= radius  <=>  d2 >= rthr (rthr: smallest double whose
+  // correctly rounded square root is >= radius), so the two corner tests of
+  // the reference below need no square root.
+  const double rthr = pg.rthr;
   double ax[9], ay[9], az[9];
   ax[0] = PF(PF_X); ay[0] = PF(PF_Y); az[0] = PF(PF_Z);
   for (int n = 1; n < 9; ++n) { ax[n] = 0; ay[n] = 0; az[n] = 0; }
@@ -73,8 +99,12 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
       copy_shift_sphere(nbrecv, g.lx, g.ly, ax[nbrecv], ay[nbrecv]);
     }
   }
+  constexpr int AX = 128;
   __shared__ double red[6][256];
-  double tot[6] = {0, 0, 0, 0, 0, 0};  // thread 0: per-copy sums added in nb order
+  __shared__ double sxm[AX], sxp[AX], srx[AX], sym[AX], syp[AX], sry[AX], szm[AX], szp[AX], srz[AX];
+  __shared__ float fxm[AX], fxp[AX], fym[AX], fyp[AX], fzm[AX], fzp[AX];
+  const float radin2_lo = (float)(radin2 * (1. - 1e-5)), radin2_hi = (float)(radin2 * (1. + 1e-5));
+  const float rthr_lo = (float)(rthr * (1. - 1e-5)), rthr_hi = (float)(rthr * (1. + 1e-5));
   double cps[9][6];
   for (int n = 0; n < 9; ++n) for (int q = 0; q < 6; ++q) cps[n][q] = 0.;
   for (int nb = 0; nb <= 8; ++nb) {
@@ -92,65 +122,95 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
     if (ihigh > g.I) ihigh = g.I;
     if (jhigh > g.J) jhigh = g.J;
     if (khigh > g.K) khigh = g.K;
-    const int ni = ihigh - ilow + 1, nj = jhigh - jlow + 1, nk = khigh - klow + 1;
+    int ni = ihigh - ilow + 1, nj = jhigh - jlow + 1, nk = khigh - klow + 1;
+    if (ni > AX || nj > AX || nk > AX) {  // sphere wider than the axis tables: flag, skip
+      if (threadIdx.x == 0) atomicExch(&b.err[3], 1);
+      ni = nj = nk = 0;
+    }
     double acc[6] = {0, 0, 0, 0, 0, 0};
     if (ni > 0 && nj > 0 && nk > 0) {
-      const long ncell = (long)ni * nj * nk;
       for (int comp = 0; comp < 3; ++comp) {
         const T *F = comp == 0 ? u : (comp == 1 ? v : w);
-        for (long t = threadIdx.x; t < ncell; t += blockDim.x) {
-          const int i = ilow + (int)(t % ni);
-          const int j = jlow + (int)((t / ni) % nj);
-          const int k = klow + (int)(t / ((long)ni * nj));
-          double coorzmin, coorzplus, coorymin, cooryplus, coorxmin, coorxplus;
-          if (comp < 2) { coorzmin = (k - 1) * dz; coorzplus = k * dz; }
-          else { coorzmin = (k - 0.5) * dz; coorzplus = (k + 0.5) * dz; }
-          if (comp == 1) { coorymin = 0. + (j - 0.5) * dy; cooryplus = 0. + (j + 0.5) * dy; }
-          else { coorymin = 0. + (j - 1) * dy; cooryplus = 0. + j * dy; }
-          if (comp == 0) { coorxmin = 0. + (i - 0.5) * dx; coorxplus = 0. + (i + 0.5) * dx; }
-          else { coorxmin = 0. + (i - 1) * dx; coorxplus = 0. + i * dx; }
-          const double dzp2 = (coorzplus - cz) * (coorzplus - cz);
-          const double dyp2 = (cooryplus - cy) * (cooryplus - cy);
-          const double dxp2 = (coorxplus - cx) * (coorxplus - cx);
-          const double dist2 = dxp2 + dyp2 + dzp2;
+        // per-axis corner distances and cell-centre offsets, in the
+        // reference's expressions (intgr_over_sphere.f90:335-508)
+        __syncthreads();
+        for (int t = threadIdx.x; t < AX; t += blockDim.x) {
+          if (t < ni) {
+            const int i = ilow + t;
+            double mn, pl;
+            if (comp == 0) { mn = 0. + (i - 0.5) * dx; pl = 0. + (i + 0.5) * dx; }
+            else { mn = 0. + (i - 1) * dx; pl = 0. + i * dx; }
+            sxm[t] = (mn - cx) * (mn - cx); sxp[t] = (pl - cx) * (pl - cx);
+            fxm[t] = (float)sxm[t]; fxp[t] = (float)sxp[t];
+            srx[t] = 0. + (i - 0.5) * dx - cx;
+          }
+          if (t < nj) {
+            const int j = jlow + t;
+            double mn, pl;
+            if (comp == 1) { mn = 0. + (j - 0.5) * dy; pl = 0. + (j + 0.5) * dy; }
+            else { mn = 0. + (j - 1) * dy; pl = 0. + j * dy; }
+            sym[t] = (mn - cy) * (mn - cy); syp[t] = (pl - cy) * (pl - cy);
+            fym[t] = (float)sym[t]; fyp[t] = (float)syp[t];
+            sry[t] = 0. + (j - 0.5) * dy - cy;
+          }
+          if (t < nk) {
+            const int k = klow + t;
+            double mn, pl;
+            if (comp < 2) { mn = (k - 1) * dz; pl = k * dz; }
+            else { mn = (k - 0.5) * dz; pl = (k + 0.5) * dz; }
+            szm[t] = (mn - cz) * (mn - cz); szp[t] = (pl - cz) * (pl - cz);
+            fzm[t] = (float)szm[t]; fzp[t] = (float)szp[t];
+            srz[t] = (k - 0.5) * dz - cz;
+          }
+        }
+        __syncthreads();
+        const int ncell = ni * nj * nk;
+        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
+          const int ti = q % ni;
+          const int tj = (q / ni) % nj;
+          const int tk = q / (ni * nj);
+          // FP32 screening with a relative margin far above its rounding
+          // (~2e-7): it only takes decisions that the FP64 test below would
+          // take as well; every other cell runs the reference's FP64 test.
+          const float dxp2f = fxp[ti], dyp2f = fyp[tj], dzp2f = fzp[tk];
+          const float dist2f = dxp2f + dyp2f + dzp2f;
           double frac = 1.;
-          bool full = dist2 < radin2;
-          if (!full) {
-            const double dxm2 = (coorxmin - cx) * (coorxmin - cx);
-            const double dym2 = (coorymin - cy) * (coorymin - cy);
-            const double dzm2 = (coorzmin - cz) * (coorzmin - cz);
-            // exact shortcuts: every corner outside -> sum1 = 0 (no
-            // contribution); every corner inside -> sum1 == sum2 (frac = 1)
-            const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
-            if (sqrt(mind2) >= radius) continue;
-            const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
-            if (!(sqrt(maxd2) < radius)) {
-              double sg[8];
-              sg[0] = radius - sqrt(dxm2 + dym2 + dzm2);
-              sg[1] = radius - sqrt(dxm2 + dyp2 + dzm2);
-              sg[2] = radius - sqrt(dxp2 + dyp2 + dzm2);
-              sg[3] = radius - sqrt(dxp2 + dym2 + dzm2);
-              sg[4] = radius - sqrt(dxm2 + dym2 + dzp2);
-              sg[5] = radius - sqrt(dxm2 + dyp2 + dzp2);
-              sg[6] = radius - sqrt(dxp2 + dyp2 + dzp2);
-              sg[7] = radius - sqrt(dxp2 + dym2 + dzp2);
-              double sum1 = 0., sum2 = 0.;
-              for (int cp = 0; cp < 8; ++cp) {
-                if (sg[cp] > 0.) sum1 = sum1 + sg[cp];
-                sum2 = sum2 + fabs(sg[cp]);
-              }
-              frac = sum1 / sum2;
+          bool full;
+          if (dist2f < radin2_lo) {
+            full = true;
+          } else if (dist2f > radin2_hi) {
+            full = false;
+            const float mind2f = fminf(fxm[ti], dxp2f) + fminf(fym[tj], dyp2f) + fminf(fzm[tk], dzp2f);
+            if (mind2f > rthr_hi) continue;          // every corner outside: no contribution
+            const float maxd2f = fmaxf(fxm[ti], dxp2f) + fmaxf(fym[tj], dyp2f) + fmaxf(fzm[tk], dzp2f);
+            if (!(maxd2f < rthr_lo)) {                // not surely all inside: exact path
+              const double dxp2 = sxp[ti], dyp2 = syp[tj], dzp2 = szp[tk];
+              const double dxm2 = sxm[ti], dym2 = sym[tj], dzm2 = szm[tk];
+              const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
+              if (mind2 >= rthr) continue;
+              const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
+              if (!(maxd2 < rthr)) frac = corner_fraction(radius, dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
+            }
+          } else {
+            // ambiguous band around radin: the reference's FP64 tests
+            const double dxp2 = sxp[ti], dyp2 = syp[tj], dzp2 = szp[tk];
+            const double dist2 = dxp2 + dyp2 + dzp2;
+            full = dist2 < radin2;
+            if (!full) {
+              const double dxm2 = sxm[ti], dym2 = sym[tj], dzm2 = szm[tk];
+              const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
+              if (mind2 >= rthr) continue;
+              const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
+              if (!(maxd2 < rthr)) frac = corner_fraction(radius, dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
             }
           }
-          const double f = (double)F[fidx(g, i - 1, j - 1, k)];
+          const double f = (double)F[fidx(g, ilow + ti - 1, jlow + tj - 1, klow + tk)];
           if (type == 1) {
             acc[comp] += full ? dVeul : frac * dVeul;
           } else {
             if (type == 2 || type == 23) acc[comp] += full ? f * dVeul : f * frac * dVeul;
             if (type == 3 || type == 23) {
-              const double rx = 0. + (i - 0.5) * dx - cx;
-              const double ry = 0. + (j - 0.5) * dy - cy;
-              const double rz = (k - 0.5) * dz - cz;
+              const double rx = srx[ti], ry = sry[tj], rz = srz[tk];
               const int o = (type == 23) ? 3 : 0;
               if (comp == 0) {
                 if (full) { acc[o + 1] = acc[o + 1] + rz * f * dVeul; acc[o + 2] = acc[o + 2] - ry * f * dVeul; }
@@ -167,6 +227,7 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
         }
       }
     }
+    __syncthreads();
     for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = acc[q];
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -179,6 +240,7 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
     __syncthreads();
   }
   if (threadIdx.x == 0) {
+    double tot[6] = {0, 0, 0, 0, 0, 0};
     for (int n = 0; n <= 8; ++n)
       for (int q = 0; q < 6; ++q) tot[q] = tot[q] + cps[n][q];
     if (type == 1) {

@@ -98,10 +98,19 @@ class IBMSolver:
                 raise ValueError(f"field shape {a.shape} != {self.case.shape}")
         self._chk(self.fn["set_fields"](self.ctx, *[dptr(a) for a in arrs]))
 
-    def get_fields(self) -> dict[str, np.ndarray]:
-        arrs = self._field_arrays()
+    def get_fields(self, out: dict | None = None) -> dict[str, np.ndarray]:
+        """Fields in the reference layout; `out` may supply (pinned) arrays for
+        any of u, v, w, p, durk, dvrk, dwrk (the others are then skipped)."""
+        names = ["u", "v", "w", "p", "durk", "dvrk", "dwrk"]
+        if out is not None:
+            arrs = [out.get(n) for n in names]
+            for a in arrs:
+                if a is not None and (a.shape != self.case.shape or not a.flags.f_contiguous):
+                    raise ValueError("output arrays must be Fortran-ordered with the reference shape")
+        else:
+            arrs = self._field_arrays()
         self._chk(self.fn["get_fields"](self.ctx, *[dptr(a) for a in arrs]))
-        return dict(zip(["u", "v", "w", "p", "durk", "dvrk", "dwrk"], arrs))
+        return {n: a for n, a in zip(names, arrs) if a is not None}
 
     def get_intermediate(self) -> dict[str, np.ndarray]:
         arrs = self._field_arrays()[:3]
