@@ -153,7 +153,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     events on the library's stream, plus the per-phase times of one step."""
     import torch
 
-    from interparts_mpich_gb300 import IBMSolver
+    from interparts_mpich_gb300 import IBM_MODE_MIXED_LEARNED, IBMSolver
     from interparts_mpich_gb300.cases import channel_case
 
     case = channel_case(args.n, args.np, seed=1234)
@@ -162,7 +162,23 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver.set_stream(stream.cuda_stream)
     solver.setup(case.initial_fields())
     dt = 0.5 * solver.chkdt()  # frozen dt (0.5 dtmax at t=0, main.f90:151-154)
-    for _ in range(args.warmup):
+    learn = None
+    nwarm = args.warmup
+    if mode == IBM_MODE_MIXED_LEARNED:
+        # first warm-up step: plain passes with harvesting; then GPU training
+        solver.harvest(capacity=args.harvest, stride=1, passes=args.harvest_passes)
+        solver.rk3_step(dt)
+        solver.harvest(0)
+        solver.sync()
+        t0 = time.perf_counter()
+        loss = solver.train_forcing_model(args.train_steps, batch=args.batch, lr=1e-3, seed=1)
+        train_s = time.perf_counter() - t0
+        st = solver.learned_stats()
+        learn = {"harvested_samples": int(st["harvested"]), "train_steps": args.train_steps, "batch": args.batch,
+                 "adam_lr": 1e-3, "train_s": round(train_s, 3), "final_loss_std_units": round(loss, 5),
+                 "plain_rms_residual": st["plain_rms_ref"]}
+        nwarm -= 1
+    for _ in range(nwarm):
         solver.rk3_step(dt)
     solver.sync()
     phases = solver.timed_step(dt)
@@ -185,6 +201,10 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
     _, divmax, _ = solver.chkdiv()
+    if learn is not None:
+        st = solver.learned_stats()
+        learn.update({"learned_rms_residual_last": st["last_rms"], "fallbacks": int(st["fallbacks"]),
+                      "learned_loops": int(st["learned_loops"])})
     e2e = None
     if with_e2e and args.e2e_steps > 0:
         # end to end through the C ABI with host buffers: u,v,w,p and the
@@ -210,7 +230,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
     solver.close()
     return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
-            "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax}
+            "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn}
 
 
 def cpu_baseline(args, case_fn):
@@ -241,7 +261,11 @@ def main():
     ap.add_argument("--np", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"])
+    ap.add_argument("--form", default="all", choices=["all", "both", "plain", "mixed", "learned"])
+    ap.add_argument("--harvest", type=int, default=2_000_000, help="harvest capacity (samples)")
+    ap.add_argument("--harvest-passes", type=int, default=6)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=8192)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -280,15 +304,15 @@ def main():
 
     import torch
 
-    from interparts_mpich_gb300 import IBM_MODE_MIXED, IBM_MODE_PLAIN_FP64
+    from interparts_mpich_gb300 import IBM_MODE_MIXED, IBM_MODE_MIXED_LEARNED, IBM_MODE_PLAIN_FP64
     from interparts_mpich_gb300 import build as b
 
     torch.cuda.set_device(local)
     b.build()
     barrier(ws)
-    forms = {"plain": IBM_MODE_PLAIN_FP64, "mixed": IBM_MODE_MIXED}
-    wanted = ["plain", "mixed"] if args.form == "both" else [args.form]
-    head = "mixed" if "mixed" in wanted else "plain"
+    forms = {"plain": IBM_MODE_PLAIN_FP64, "mixed": IBM_MODE_MIXED, "learned": IBM_MODE_MIXED_LEARNED}
+    wanted = {"all": ["plain", "mixed", "learned"], "both": ["plain", "learned"]}.get(args.form, [args.form])
+    head = next(f for f in ("learned", "mixed", "plain") if f in wanted)
     res = {f: run_form(args, ws, rank, local, forms[f], with_e2e=(f == head)) for f in wanted}
     if rank != 0:
         return
@@ -307,13 +331,15 @@ def main():
     line = {
         "metric": METRIC, "value": round(r["ms"], 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(r["ms"], 4), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if head == "plain" else "f32+f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": {"plain": "f64", "mixed": "f32+f64", "learned": "f32+f64 (bf16 MLP)"}[head], "data": "synthetic",
         "config": config,
-        "form": {"plain": "plain FP64 (drop-in)", "mixed": "mixed FP32/FP64"}[head],
+        "form": {"plain": "plain FP64 (drop-in)", "mixed": "mixed FP32/FP64",
+                 "learned": "mixed FP32/FP64 + learned forcing"}[head],
         "forms": {f: {"ms_per_step": round(x["ms"], 4),
                       "mcell_steps_per_s": round(args.gpus * x["ncell"] / (x["ms"] * 1e-3) / 1e6, 1),
                       "phases_ms": {n: round(t, 4) for n, t in zip(names, x["phases"])},
-                      "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"])} for f, x in res.items()},
+                      "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"]),
+                      **({"learned_forcing": x["learn"]} if x["learn"] else {})} for f, x in res.items()},
         "mcell_steps_per_s": round(args.gpus * r["ncell"] / (r["ms"] * 1e-3) / 1e6, 1),
         "hbm_roofline_frac_step": round(ab["total"] / (r["ms"] * 1e-3) / 1e9 / hbm, 4),
         "roofline": {"bound": "hbm", "kernel": names[dom] + " phase", "achieved": round(achieved * w / 8, 1),
@@ -323,8 +349,9 @@ def main():
         "clocks": r["clocks"],
         "dt": r["dt"],
     }
-    if "plain" in res and "mixed" in res:
-        line["speedup_mixed_vs_plain"] = round(res["plain"]["ms"] / res["mixed"]["ms"], 3)
+    for f in ("mixed", "learned"):
+        if "plain" in res and f in res:
+            line[f"speedup_{f}_vs_plain"] = round(res["plain"]["ms"] / res[f]["ms"], 3)
     if r["e2e"]:
         line["e2e"] = r["e2e"]
     if not args.no_cpu_baseline:

@@ -198,6 +198,58 @@ long long ibm_launch_count(const ibm_ctx *ctx);
 /* Device synchronisation of the context stream. */
 int ibm_sync(ibm_ctx *ctx);
 
+/* --- learned forcing (IBM_MODE_MIXED_LEARNED; no counterpart in the reference) -
+ *
+ * A per-Lagrangian-point network 96 -> 128 -> 128 -> 3 (GELU) replaces the
+ * multidirect passes 2..nl_iter of ibm_forcing_loop: one plain pass, the
+ * network's prediction of the remaining correction, one spreading of it, and
+ * the plain passes as fallback whenever the rms no-slip residual exceeds
+ * fallback_ratio x the plain method's.  Features per point (after pass 1):
+ * slip, rigid-body velocity, outward normal, u/v/w at the 27 stencil taps
+ * relative to the body velocity, the pass-1 correction, centre delta
+ * weights.  Target: (F_final - F_pass1) * dt of the plain passes. */
+#define IBM_NN_IN     96
+#define IBM_NN_HIDDEN 128
+#define IBM_NN_OUT    3
+#define IBM_NN_NPARAM 29315   /* W1[128][96] b1[128] W2[128][128] b2[128] W3[3][128] b3[3] */
+#define IBM_NN_NNORM  198     /* feature mean[96], 1/sigma[96]; target mean[3], sigma[3] */
+
+/* Start harvesting (features, target) pairs from the plain passes of the
+ * following forcing loops: every stride-th point, up to capacity samples kept
+ * on the device (previous samples are discarded).  While harvesting, each
+ * loop runs max(nl_iter, passes) plain passes (passes > nl_iter harvests a
+ * more converged correction) and records the plain residual after nl_iter
+ * passes as the reference for the fallback test.  capacity = 0 stops
+ * harvesting and keeps the samples. */
+int ibm_harvest(ibm_ctx *ctx, int capacity, int stride, int passes);
+/* nsteps Adam steps (lr, betas 0.9/0.999) on batches of `batch` samples drawn
+ * with replacement from the harvest, on the GPU (BF16 tensor-core forward and
+ * backward, FP32 master weights).  On the first call, or with reinit, the
+ * standardisation is computed from the samples and the weights start afresh
+ * from `seed`.  *loss = mean squared error of the last batch (standardised
+ * units).  Enables the learned correction. */
+int ibm_train_forcing_model(ibm_ctx *ctx, int nsteps, int batch, double lr, unsigned seed, int reinit,
+                            double *loss);
+/* Model transfer: params[IBM_NN_NPARAM], norm[IBM_NN_NNORM].  set enables it. */
+int ibm_set_forcing_model(ibm_ctx *ctx, const float *params, const float *norm);
+int ibm_get_forcing_model(ibm_ctx *ctx, float *params, float *norm);
+/* enable (needs a model), fallback_ratio (default 1.5), plain_rms_ref > 0
+ * fixes the plain residual reference (else the mean over harvested loops). */
+int ibm_learned_config(ibm_ctx *ctx, int enable, double fallback_ratio, double plain_rms_ref);
+/* stats[6]: rms residual of the last learned loop, plain reference, ratio,
+ * fallbacks taken, learned loops run, harvested samples. */
+int ibm_learned_stats(ibm_ctx *ctx, double stats[6]);
+/* The training kernels on a caller batch (features x[nb][96] already
+ * standardised, targets t[nb][3]) with a scratch copy of params: loss,
+ * gradient[IBM_NN_NPARAM] and outputs y[nb][3] (any may be NULL).  Loss =
+ * mean over rows of the squared error summed over the 3 outputs. */
+int ibm_mlp_gradient(ibm_ctx *ctx, const float *params, const float *x, const float *t, int nb, float *grad,
+                     float *loss, float *y);
+/* nsteps full-batch Adam steps from params_in with fresh moments:
+ * params_out[IBM_NN_NPARAM], losses[nsteps] (loss before each update). */
+int ibm_mlp_fit(ibm_ctx *ctx, const float *params_in, const float *x, const float *t, int nb, int nsteps,
+                double lr, float *params_out, float *losses);
+
 /* --- allocation-free variant ------------------------------------------------ */
 
 /* chkdiv for callers that cannot allocate device memory (no counterpart in the

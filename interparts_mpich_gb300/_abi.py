@@ -9,6 +9,7 @@ import ctypes as C
 
 import numpy as np
 
+c_float_p = C.POINTER(C.c_float)
 c_double_p = C.POINTER(C.c_double)
 c_int_p = C.POINTER(C.c_int)
 
@@ -150,6 +151,15 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "sync": (C.c_int, [ctx]),
         "chkdiv_noalloc": (C.c_int, [c_double_p, c_double_p, c_double_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_double, C.c_double, c_double_p, C.c_void_p]),
+        "harvest": (C.c_int, [ctx, C.c_int, C.c_int, C.c_int]),
+        "train_forcing_model": (C.c_int, [ctx, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_int, c_double_p]),
+        "set_forcing_model": (C.c_int, [ctx, c_float_p, c_float_p]),
+        "get_forcing_model": (C.c_int, [ctx, c_float_p, c_float_p]),
+        "learned_config": (C.c_int, [ctx, C.c_int, C.c_double, C.c_double]),
+        "learned_stats": (C.c_int, [ctx, c_double_p]),
+        "mlp_gradient": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p]),
+        "mlp_fit": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, C.c_int, C.c_double, c_float_p,
+                              c_float_p]),
     }
     table = {}
     for name, (res, args) in list(sig.items()) + list(optional.items()):

@@ -354,7 +354,7 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, &c->pb.rkp, (size_t)RK_N * np))) return st;
     if ((st = dalloc(c, &c->pb.sincos, (size_t)4 * nl))) return st;
     if ((st = dalloc(c, &c->pb.err, 4))) return st;
-    if ((st = dalloc(c, &c->pb.red, (size_t)4 * np))) return st;
+    if ((st = dalloc(c, &c->pb.red, (size_t)10 * np))) return st;
     if ((st = dalloc(c, &c->ib.diag, 8))) return st;
     c->ib.pf = c->pb.pf;
     c->ib.err = c->pb.err;
@@ -624,7 +624,7 @@ ibm_ctx *ibm_create(const ibm_params *P) {
   int st = alloc_all(c);
   if (st == IBM_OK) st = build_solver_tables(c);
   if (st == IBM_OK && (poisson_set_smem_limits<double>() != 0 || poisson_set_smem_limits<float>() != 0 ||
-                       mlp_set_smem_limits() != 0))
+                       mlp_set_smem_limits() != 0 || ibm_set_smem_limits() != 0))
     st = set_err(c, IBM_E_CUDA, "cudaFuncSetAttribute failed");
   if (st == IBM_OK) st = cuda_err(c, cudaStreamSynchronize(c->stream), "create");
   if (st != IBM_OK) {

@@ -167,54 +167,7 @@ template void launch_ibm_interp_force<double>(cudaStream_t, const Geo &, const P
 template void launch_ibm_interp_force<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, const float *,
                                              const float *, const float *, double, int);
 
-// lagr2eulr increment: spread dF = (U_l - u~_l)/dt with the terms of
-// interp_spread.f90:329-355, F*coeff0*phix*phiy*phiz, the (j,k) factor
-// formed once per row of three taps
-template <typename T>
-__global__ void __launch_bounds__(256) k_ibm_spread(Geo g, PartGeo pg, IbmBuffers b, T *__restrict__ fu,
-                                                    T *__restrict__ fv, T *__restrict__ fw, double dti,
-                                                    double coeff0) {
-  const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int p = t / pg.nl, l = t - p * pg.nl;
-    if (l >= b.nla[p]) continue;
-    const PointStencil s = b.st[t];
-    const double dfx = (b.ul[t] - b.dudtl[t]) * dti;
-    const double dfy = (b.vl[t] - b.dvdtl[t]) * dti;
-    const double dfz = (b.wl[t] - b.dwdtl[t]) * dti;
-    int ix[3], ixh[3], jy[3], jyh[3];
-    for (int m = 0; m < 3; ++m) {
-      ix[m] = wrapm(s.ilows + m - 1, g.I);
-      ixh[m] = wrapm(s.ilow + m - 1, g.I);
-      jy[m] = wrapm(s.jlows + m - 1, g.J);
-      jyh[m] = wrapm(s.jlow + m - 1, g.J);
-    }
-    for (int k = 0; k < 3; ++k)
-      for (int j = 0; j < 3; ++j) {
-        const double a = dfx * coeff0 * s.phiyh[j] * s.phizh[k];
-        const double bb = dfy * coeff0 * s.phiy[j] * s.phizh[k];
-        const double cc = dfz * coeff0 * s.phiyh[j] * s.phiz[k];
-        for (int i = 0; i < 3; ++i) {
-          atomicAdd(&fu[fidx(g, ix[i], jyh[j], s.klow + k)], (T)(a * s.phix[i]));
-          atomicAdd(&fv[fidx(g, ixh[i], jy[j], s.klow + k)], (T)(bb * s.phixh[i]));
-          atomicAdd(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)], (T)(cc * s.phixh[i]));
-        }
-      }
-  }
-}
-
-template <typename T>
-void launch_ibm_spread(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, T *fu, T *fv, T *fw, double dt,
-                       int first) {
-  (void)first;
-  if (pg.np == 0) return;
-  const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread<T><<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0);
-}
-template void launch_ibm_spread<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, double *, double *,
-                                        double *, double, int);
-template void launch_ibm_spread<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, float *, float *,
-                                       float *, double, int);
+// lagr2eulr spreading: see k_ibm_spread_box below
 
 template <typename T>
 __global__ void k_zero_plane(Geo g, T *f, int k) {
@@ -382,51 +335,159 @@ void launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, 
   k_ibm_interp_force_f<<<pg.np, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, first, gate);
 }
 
-__global__ void __launch_bounds__(256) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
-                                                      float *__restrict__ fv, float *__restrict__ fw, double dti,
-                                                      double coeff0, const float *__restrict__ dfin,
-                                                      const int *__restrict__ gate) {
-  if (gate && *gate == 0) return;
-  const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int p = t / pg.nl, l = t - p * pg.nl;
-    if (l >= b.nla[p]) continue;
-    const PointStencilF s = b.st32[t];
-    float dfx, dfy, dfz;
-    if (dfin) {  // force increment given per point (learned correction)
-      dfx = (float)(dfin[3 * t] * coeff0);
-      dfy = (float)(dfin[3 * t + 1] * coeff0);
-      dfz = (float)(dfin[3 * t + 2] * coeff0);
-    } else {
-      dfx = (float)((b.ul[t] - b.dudtl[t]) * dti * coeff0);
-      dfy = (float)((b.vl[t] - b.dvdtl[t]) * dti * coeff0);
-      dfz = (float)((b.wl[t] - b.dwdtl[t]) * dti * coeff0);
-    }
-    int ix[3], ixh[3], jy[3], jyh[3];
-    for (int m = 0; m < 3; ++m) {
-      ix[m] = wrapm(s.ilows + m - 1, g.I);
-      ixh[m] = wrapm(s.ilow + m - 1, g.I);
-      jy[m] = wrapm(s.jlows + m - 1, g.J);
-      jyh[m] = wrapm(s.jlow + m - 1, g.J);
-    }
-    for (int k = 0; k < 3; ++k)
-      for (int j = 0; j < 3; ++j) {
-        const float a = dfx * s.phiyh[j] * s.phizh[k];
-        const float bb = dfy * s.phiy[j] * s.phizh[k];
-        const float c = dfz * s.phiyh[j] * s.phiz[k];
-        for (int i = 0; i < 3; ++i) {
-          atomicAdd(&fu[fidx(g, ix[i], jyh[j], s.klow + k)], a * s.phix[i]);
-          atomicAdd(&fv[fidx(g, ixh[i], jy[j], s.klow + k)], bb * s.phixh[i]);
-          atomicAdd(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)], c * s.phixh[i]);
-        }
-      }
+// ---------------------------------------------------------------------------
+// lagr2eulr spreading of dF = (U_l - u~_l)/dt (or a given increment) with
+// the terms of interp_spread.f90:329-355, F*coeff0*phix*phiy*phiz.  Block
+// (particle, component): the particle's contributions are accumulated in a
+// shared-memory box over the cells its stencils touch, then every touched
+// cell is flushed to HBM with one atomic add (instead of one per tap).  In
+// FP32 the box accumulation is compensated: the rounding error of each
+// shared atomic add is recovered exactly by TwoSum from the value the atomic
+// returned and accumulated in a second box, so the flushed hi+lo carries the
+// particle's sum to about FP64 accuracy.  A box larger than SPREAD_BOX cells
+// (spheres beyond ~D = 16 dx) falls back to direct atomics per tap.
+// ---------------------------------------------------------------------------
+constexpr int SPREAD_BOX = 8192;
+
+template <typename T>
+__device__ __forceinline__ void box_add(T *hi, T *lo, int c, T v) {
+  if constexpr (sizeof(T) == 8) {
+    atomicAdd(&hi[c], v);
+    (void)lo;
+  } else {
+    const float old = atomicAdd(&hi[c], v);
+    const float s = __fadd_rn(old, v);
+    const float bb = __fsub_rn(s, old);
+    const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+    if (e != 0.f) atomicAdd(&lo[c], e);
   }
 }
+
+template <typename T, typename ST, typename W>
+__global__ void __launch_bounds__(256) k_ibm_spread_box(Geo g, PartGeo pg, IbmBuffers b, const ST *__restrict__ st,
+                                                        T *__restrict__ fu, T *__restrict__ fv, T *__restrict__ fw,
+                                                        double dti, double coeff0, const float *__restrict__ dfin,
+                                                        const int *__restrict__ gate) {
+  if (gate && *gate == 0) return;  // learned form: plain pass not needed
+  const int p = blockIdx.x, comp = blockIdx.y;
+  const int nla = b.nla[p];
+  if (nla <= 0) return;
+  T *F = comp == 0 ? fu : (comp == 1 ? fv : fw);
+  extern __shared__ __align__(16) unsigned char spread_sm[];
+  T *hi = reinterpret_cast<T *>(spread_sm);
+  T *lo = hi + SPREAD_BOX;  // FP32 only
+  __shared__ int bmin[3], bmax[3];
+  const long t0 = (long)p * pg.nl;
+  const int refx = comp == 0 ? st[t0].ilows : st[t0].ilow;
+  const int refy = comp == 1 ? st[t0].jlows : st[t0].jlow;
+  const int hI = g.I / 2, hJ = g.J / 2;
+  if (threadIdx.x < 3) { bmin[threadIdx.x] = 0x7fffffff; bmax[threadIdx.x] = -0x7fffffff; }
+  __syncthreads();
+  // box of the stencil origins, x/y relative to the first point (periodic)
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const ST &s = st[t0 + l];
+    int rx = (comp == 0 ? s.ilows : s.ilow) - refx;
+    int ry = (comp == 1 ? s.jlows : s.jlow) - refy;
+    const int rz = comp == 2 ? s.klows : s.klow;
+    rx = rx >= hI ? rx - g.I : (rx < -hI ? rx + g.I : rx);
+    ry = ry >= hJ ? ry - g.J : (ry < -hJ ? ry + g.J : ry);
+    atomicMin(&bmin[0], rx); atomicMax(&bmax[0], rx);
+    atomicMin(&bmin[1], ry); atomicMax(&bmax[1], ry);
+    atomicMin(&bmin[2], rz); atomicMax(&bmax[2], rz);
+  }
+  __syncthreads();
+  const int nbx = bmax[0] - bmin[0] + 3, nby = bmax[1] - bmin[1] + 3, nbz = bmax[2] - bmin[2] + 3;
+  const long nbox = (long)nbx * nby * nbz;
+  const bool boxed = nbox <= SPREAD_BOX && nbx < hI && nby < hJ;
+  if (boxed) {
+    for (int c = threadIdx.x; c < nbox; c += blockDim.x) {
+      hi[c] = (T)0;
+      if constexpr (sizeof(T) == 4) lo[c] = 0.f;
+    }
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const long t = t0 + l;
+    const ST s = st[t];
+    int bx, by, bz;
+    W wx[3], wy[3], wz[3];
+    double ucomp, icomp;
+    if (comp == 0) {
+      bx = s.ilows; by = s.jlow; bz = s.klow;
+      for (int m = 0; m < 3; ++m) { wx[m] = s.phix[m]; wy[m] = s.phiyh[m]; wz[m] = s.phizh[m]; }
+      ucomp = b.ul[t]; icomp = b.dudtl[t];
+    } else if (comp == 1) {
+      bx = s.ilow; by = s.jlows; bz = s.klow;
+      for (int m = 0; m < 3; ++m) { wx[m] = s.phixh[m]; wy[m] = s.phiy[m]; wz[m] = s.phizh[m]; }
+      ucomp = b.vl[t]; icomp = b.dvdtl[t];
+    } else {
+      bx = s.ilow; by = s.jlow; bz = s.klows;
+      for (int m = 0; m < 3; ++m) { wx[m] = s.phixh[m]; wy[m] = s.phiyh[m]; wz[m] = s.phiz[m]; }
+      ucomp = b.wl[t]; icomp = b.dwdtl[t];
+    }
+    // the (j,k) factor first, then the x weight (the reference's product order)
+    T pre;
+    if constexpr (sizeof(T) == 8) pre = (ucomp - icomp) * dti * coeff0;
+    else pre = dfin ? (float)(dfin[3 * t + comp] * coeff0) : (float)((ucomp - icomp) * dti * coeff0);
+    if (boxed) {
+      int rx = bx - refx, ry = by - refy;
+      rx = rx >= hI ? rx - g.I : (rx < -hI ? rx + g.I : rx);
+      ry = ry >= hJ ? ry - g.J : (ry < -hJ ? ry + g.J : ry);
+      const int cx = rx - bmin[0], cy = ry - bmin[1], cz = bz - bmin[2];
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) {
+          const T a = pre * wy[j] * wz[k];
+          const int row = ((cz + k) * nby + (cy + j)) * nbx + cx;
+          for (int i = 0; i < 3; ++i) box_add<T>(hi, lo, row + i, (T)(a * wx[i]));
+        }
+    } else {
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) {
+          const T a = pre * wy[j] * wz[k];
+          const int y = wrapm(by + j - 1, g.J);
+          for (int i = 0; i < 3; ++i) atomicAdd(&F[fidx(g, wrapm(bx + i - 1, g.I), y, bz + k)], (T)(a * wx[i]));
+        }
+    }
+  }
+  if (!boxed) return;
+  __syncthreads();
+  for (int c = threadIdx.x; c < nbox; c += blockDim.x) {
+    T v = hi[c];
+    if constexpr (sizeof(T) == 4) v += lo[c];
+    if (v != (T)0) {
+      const int cx = c % nbx, cy = (c / nbx) % nby, cz = c / (nbx * nby);
+      const int x = wrapm(refx + bmin[0] - 1 + cx, g.I), y = wrapm(refy + bmin[1] - 1 + cy, g.J);
+      atomicAdd(&F[fidx(g, x, y, bmin[2] + cz)], v);
+    }
+  }
+}
+
+template <typename T>
+void launch_ibm_spread(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, T *fu, T *fv, T *fw, double dt,
+                       int first) {
+  (void)first;
+  if (pg.np == 0) return;
+  const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
+  k_ibm_spread_box<double, PointStencil, double><<<dim3(pg.np, 3), 256, SPREAD_BOX * sizeof(double), s>>>(
+      g, pg, b, b.st, fu, fv, fw, 1. / dt, coeff0, nullptr, nullptr);
+}
+template void launch_ibm_spread<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, double *, double *,
+                                        double *, double, int);
+
 void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
                          float *fw, double dt, const float *dfin, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0, dfin, gate);
+  k_ibm_spread_box<float, PointStencilF, float><<<dim3(pg.np, 3), 256, 2 * SPREAD_BOX * sizeof(float), s>>>(
+      g, pg, b, b.st32, fu, fv, fw, 1. / dt, coeff0, dfin, gate);
+}
+
+int ibm_set_smem_limits() {
+  cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_box<double, PointStencil, double>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SPREAD_BOX * (int)sizeof(double));
+  cudaError_t e2 = cudaFuncSetAttribute(k_ibm_spread_box<float, PointStencilF, float>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * SPREAD_BOX * (int)sizeof(float));
+  return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
 }
 
 // ---------------------------------------------------------------------------

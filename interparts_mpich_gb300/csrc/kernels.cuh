@@ -98,6 +98,7 @@ struct MlpTrainBuffers {
   __nv_bfloat16 *h1, *h2, *dz1, *dz2;         // [nb][128]
 };
 int mlp_nparam();
+int ibm_set_smem_limits();
 int mlp_set_smem_limits();
 void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
                         const __nv_bfloat16 *w2b, const float *params, float *y, float *z1, float *z2,
@@ -124,7 +125,7 @@ struct PartBuffers {
   double *rkp;    // [RK_N*np]
   double *sincos; // [4*nl]: sin(theta), cos(theta), sin(phi), cos(phi)
   int *err;       // [4] error flags
-  double *red;    // [np*9*6] sphere-integral partials
+  double *red;    // [10*np]: volume [np], sphere-integral partials [np][3][3]
 };
 template <typename T>
 void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,

@@ -74,45 +74,76 @@ __device__ __forceinline__ double corner_fraction(double radius, double dxm2, do
   return sum1 / sum2;
 }
 
-template <typename T>
+// FP32 corner fraction (mixed form): the same expression in single
+// precision; its decisions at the surface are continuous in the distances
+__device__ __forceinline__ float corner_fraction_f(float radius, float dxm2, float dxp2, float dym2, float dyp2,
+                                                  float dzm2, float dzp2) {
+  float sg[8];
+  sg[0] = radius - sqrtf(dxm2 + dym2 + dzm2);
+  sg[1] = radius - sqrtf(dxm2 + dyp2 + dzm2);
+  sg[2] = radius - sqrtf(dxp2 + dyp2 + dzm2);
+  sg[3] = radius - sqrtf(dxp2 + dym2 + dzm2);
+  sg[4] = radius - sqrtf(dxm2 + dym2 + dzp2);
+  sg[5] = radius - sqrtf(dxm2 + dyp2 + dzp2);
+  sg[6] = radius - sqrtf(dxp2 + dyp2 + dzp2);
+  sg[7] = radius - sqrtf(dxp2 + dym2 + dzp2);
+  float sum1 = 0.f, sum2 = 0.f;
+#pragma unroll
+  for (int cp = 0; cp < 8; ++cp) {
+    sum1 += fmaxf(sg[cp], 0.f);
+    sum2 += fabsf(sg[cp]);
+  }
+  return sum1 / sum2;
+}
+
+// Sums of one velocity component over the cells of the sphere's box.  Block
+// (p, comp); a thread owns whole i-lines (fixed j, k), so the lever arms ry,
+// rz of the torque are constant along its line and only
+//   S0 = sum f*w,  Sx = sum rx*f*w
+// accumulate per cell (FP64).  w = 1 for cells inside radin or with all
+// corners inside, 0 with all corners outside, else the corner fraction.
+// Classification: FP32 screening of the squared corner distances with a
+// relative margin (1e-5) far above its rounding; in the plain form every
+// cell the screen cannot decide goes to a shared-memory queue that all
+// threads then run through the reference's FP64 tests (full warps for the
+// FP64 work).  The mixed form (GEO32) evaluates the cut cells in FP32.
+// Output: b.red[np + (p*3 + comp)*3 + {0,1,2}] = {S0, torque_a, torque_b}
+// without the dVeul factor (k_sphere_final).
+template <typename T, bool GEO32>
 __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffers b, const T *__restrict__ u,
-                                                    const T *__restrict__ v, const T *__restrict__ w, int type) {
+                                                    const T *__restrict__ v, const T *__restrict__ w) {
+  constexpr int AX = 128, QCAP = 2048;
   const int np = pg.np;
-  const int p = blockIdx.x;
-  if (b.mslv[p] == 0) return;
-  const double radius = pg.radius, dVeul = pg.dVeul;
+  const int p = blockIdx.x, comp = blockIdx.y;
+  const int ms = b.mslv[p];
+  if (ms <= 0) return;
+  const double radius = pg.radius;
   const double dx = 1. / g.dxi, dy = 1. / g.dyi, dz = 1. / g.dzi;
   const double radin = radius - 2. * dx;
   const double radin2 = radin * radin;
   // sqrt(d2) >= radius  <=>  d2 >= rthr (rthr: smallest double whose
-  // correctly rounded square root is >= radius), so the two corner tests of
-  // the reference below need no square root.
+  // correctly rounded square root is >= radius)
   const double rthr = pg.rthr;
-  double ax[9], ay[9], az[9];
-  ax[0] = PF(PF_X); ay[0] = PF(PF_Y); az[0] = PF(PF_Z);
-  for (int n = 1; n < 9; ++n) { ax[n] = 0; ay[n] = 0; az[n] = 0; }
-  const int *nbf = b.nb + (long)p * 9;
-  for (int nb = 1; nb <= 8; ++nb) {
-    int nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8;
-    if (b.mslv[p] > 0 && nbf[nb] == 1) {
-      ax[nbrecv] = ax[0]; ay[nbrecv] = ay[0]; az[nbrecv] = az[0];
-      copy_shift_sphere(nbrecv, g.lx, g.ly, ax[nbrecv], ay[nbrecv]);
-    }
-  }
-  constexpr int AX = 128;
-  __shared__ double red[6][256];
-  __shared__ double sxm[AX], sxp[AX], srx[AX], sym[AX], syp[AX], sry[AX], szm[AX], szp[AX], srz[AX];
-  __shared__ float fxm[AX], fxp[AX], fym[AX], fyp[AX], fzm[AX], fzp[AX];
   const float radin2_lo = (float)(radin2 * (1. - 1e-5)), radin2_hi = (float)(radin2 * (1. + 1e-5));
   const float rthr_lo = (float)(rthr * (1. - 1e-5)), rthr_hi = (float)(rthr * (1. + 1e-5));
-  double cps[9][6];
-  for (int n = 0; n < 9; ++n) for (int q = 0; q < 6; ++q) cps[n][q] = 0.;
+  const float radin2f = (float)radin2, rthrf = (float)rthr, radiusf = (float)radius;
+  __shared__ double sxm[AX], sxp[AX], srx[AX], sym[AX], syp[AX], sry[AX], szm[AX], szp[AX], srz[AX];
+  __shared__ float fxm[AX], fxp[AX], fym[AX], fyp[AX], fzm[AX], fzp[AX];
+  __shared__ int queue[GEO32 ? 1 : QCAP];
+  __shared__ int qn;
+  __shared__ double red[3][256];
+  const T *F = comp == 0 ? u : (comp == 1 ? v : w);
+  const int *nbf = b.nb + (long)p * 9;
+  double a0 = 0., ta = 0., tb = 0.;
+  // lever arms per component: ta += la * f*w, tb += lb * f*w with
+  // comp 0: (rz, -ry), comp 1: (-rz, rx), comp 2: (ry, -rx)
   for (int nb = 0; nb <= 8; ++nb) {
-    const bool go = (nb == 0 && b.mslv[p] > 0) || (nb > 0 && b.mslv[p] > 0 && nbf[nb] == 1);
-    if (!go) continue;
+    if (nb > 0 && nbf[nb] != 1) continue;
     int nbrecv = nb;
     if (nb > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
-    const double cx = ax[nbrecv], cy = ay[nbrecv], cz = az[nbrecv];
+    double cx = PF(PF_X), cy = PF(PF_Y);
+    const double cz = PF(PF_Z);
+    if (nb > 0) copy_shift_sphere(nbrecv, g.lx, g.ly, cx, cy);
     int ilow = fnint((cx - radius) * g.dxi - 2.), ihigh = fnint((cx + radius) * g.dxi + 2.);
     int jlow = fnint((cy - radius) * g.dyi - 2.), jhigh = fnint((cy + radius) * g.dyi + 2.);
     int klow = fnint((cz - radius) * g.dzi - 2.), khigh = fnint((cz + radius) * g.dzi + 2.);
@@ -122,146 +153,185 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
     if (ihigh > g.I) ihigh = g.I;
     if (jhigh > g.J) jhigh = g.J;
     if (khigh > g.K) khigh = g.K;
-    int ni = ihigh - ilow + 1, nj = jhigh - jlow + 1, nk = khigh - klow + 1;
+    const int ni = ihigh - ilow + 1, nj = jhigh - jlow + 1, nk = khigh - klow + 1;
+    if (ni <= 0 || nj <= 0 || nk <= 0) continue;
     if (ni > AX || nj > AX || nk > AX) {  // sphere wider than the axis tables: flag, skip
       if (threadIdx.x == 0) atomicExch(&b.err[3], 1);
-      ni = nj = nk = 0;
+      continue;
     }
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    if (ni > 0 && nj > 0 && nk > 0) {
-      for (int comp = 0; comp < 3; ++comp) {
-        const T *F = comp == 0 ? u : (comp == 1 ? v : w);
-        // per-axis corner distances and cell-centre offsets, in the
-        // reference's expressions (intgr_over_sphere.f90:335-508)
-        __syncthreads();
-        for (int t = threadIdx.x; t < AX; t += blockDim.x) {
-          if (t < ni) {
-            const int i = ilow + t;
-            double mn, pl;
-            if (comp == 0) { mn = 0. + (i - 0.5) * dx; pl = 0. + (i + 0.5) * dx; }
-            else { mn = 0. + (i - 1) * dx; pl = 0. + i * dx; }
-            sxm[t] = (mn - cx) * (mn - cx); sxp[t] = (pl - cx) * (pl - cx);
-            fxm[t] = (float)sxm[t]; fxp[t] = (float)sxp[t];
-            srx[t] = 0. + (i - 0.5) * dx - cx;
-          }
-          if (t < nj) {
-            const int j = jlow + t;
-            double mn, pl;
-            if (comp == 1) { mn = 0. + (j - 0.5) * dy; pl = 0. + (j + 0.5) * dy; }
-            else { mn = 0. + (j - 1) * dy; pl = 0. + j * dy; }
-            sym[t] = (mn - cy) * (mn - cy); syp[t] = (pl - cy) * (pl - cy);
-            fym[t] = (float)sym[t]; fyp[t] = (float)syp[t];
-            sry[t] = 0. + (j - 0.5) * dy - cy;
-          }
-          if (t < nk) {
-            const int k = klow + t;
-            double mn, pl;
-            if (comp < 2) { mn = (k - 1) * dz; pl = k * dz; }
-            else { mn = (k - 0.5) * dz; pl = (k + 0.5) * dz; }
-            szm[t] = (mn - cz) * (mn - cz); szp[t] = (pl - cz) * (pl - cz);
-            fzm[t] = (float)szm[t]; fzp[t] = (float)szp[t];
-            srz[t] = (k - 0.5) * dz - cz;
-          }
-        }
-        __syncthreads();
-        const int ncell = ni * nj * nk;
-        for (int q = threadIdx.x; q < ncell; q += blockDim.x) {
-          const int ti = q % ni;
-          const int tj = (q / ni) % nj;
-          const int tk = q / (ni * nj);
-          // FP32 screening with a relative margin far above its rounding
-          // (~2e-7): it only takes decisions that the FP64 test below would
-          // take as well; every other cell runs the reference's FP64 test.
-          const float dxp2f = fxp[ti], dyp2f = fyp[tj], dzp2f = fzp[tk];
-          const float dist2f = dxp2f + dyp2f + dzp2f;
-          double frac = 1.;
-          bool full;
-          if (dist2f < radin2_lo) {
-            full = true;
-          } else if (dist2f > radin2_hi) {
-            full = false;
-            const float mind2f = fminf(fxm[ti], dxp2f) + fminf(fym[tj], dyp2f) + fminf(fzm[tk], dzp2f);
-            if (mind2f > rthr_hi) continue;          // every corner outside: no contribution
-            const float maxd2f = fmaxf(fxm[ti], dxp2f) + fmaxf(fym[tj], dyp2f) + fmaxf(fzm[tk], dzp2f);
-            if (!(maxd2f < rthr_lo)) {                // not surely all inside: exact path
-              const double dxp2 = sxp[ti], dyp2 = syp[tj], dzp2 = szp[tk];
-              const double dxm2 = sxm[ti], dym2 = sym[tj], dzm2 = szm[tk];
-              const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
-              if (mind2 >= rthr) continue;
-              const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
-              if (!(maxd2 < rthr)) frac = corner_fraction(radius, dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
-            }
-          } else {
-            // ambiguous band around radin: the reference's FP64 tests
-            const double dxp2 = sxp[ti], dyp2 = syp[tj], dzp2 = szp[tk];
-            const double dist2 = dxp2 + dyp2 + dzp2;
-            full = dist2 < radin2;
-            if (!full) {
-              const double dxm2 = sxm[ti], dym2 = sym[tj], dzm2 = szm[tk];
-              const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
-              if (mind2 >= rthr) continue;
-              const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
-              if (!(maxd2 < rthr)) frac = corner_fraction(radius, dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
-            }
-          }
-          const double f = (double)F[fidx(g, ilow + ti - 1, jlow + tj - 1, klow + tk)];
-          if (type == 1) {
-            acc[comp] += full ? dVeul : frac * dVeul;
-          } else {
-            if (type == 2 || type == 23) acc[comp] += full ? f * dVeul : f * frac * dVeul;
-            if (type == 3 || type == 23) {
-              const double rx = srx[ti], ry = sry[tj], rz = srz[tk];
-              const int o = (type == 23) ? 3 : 0;
-              if (comp == 0) {
-                if (full) { acc[o + 1] = acc[o + 1] + rz * f * dVeul; acc[o + 2] = acc[o + 2] - ry * f * dVeul; }
-                else { acc[o + 1] = acc[o + 1] + rz * f * frac * dVeul; acc[o + 2] = acc[o + 2] - ry * f * frac * dVeul; }
-              } else if (comp == 1) {
-                if (full) { acc[o + 0] = acc[o + 0] - rz * f * dVeul; acc[o + 2] = acc[o + 2] + rx * f * dVeul; }
-                else { acc[o + 0] = acc[o + 0] - rz * f * frac * dVeul; acc[o + 2] = acc[o + 2] + rx * f * frac * dVeul; }
-              } else {
-                if (full) { acc[o + 0] = acc[o + 0] + ry * f * dVeul; acc[o + 1] = acc[o + 1] - rx * f * dVeul; }
-                else { acc[o + 0] = acc[o + 0] + ry * f * frac * dVeul; acc[o + 1] = acc[o + 1] - rx * f * frac * dVeul; }
-              }
-            }
-          }
-        }
+    __syncthreads();  // previous copy done with the tables
+    // per-axis corner distances and cell-centre offsets, in the reference's
+    // expressions (intgr_over_sphere.f90:335-508)
+    for (int t = threadIdx.x; t < AX; t += blockDim.x) {
+      if (t < ni) {
+        const int i = ilow + t;
+        double mn, pl;
+        if (comp == 0) { mn = 0. + (i - 0.5) * dx; pl = 0. + (i + 0.5) * dx; }
+        else { mn = 0. + (i - 1) * dx; pl = 0. + i * dx; }
+        sxm[t] = (mn - cx) * (mn - cx); sxp[t] = (pl - cx) * (pl - cx);
+        fxm[t] = (float)sxm[t]; fxp[t] = (float)sxp[t];
+        srx[t] = 0. + (i - 0.5) * dx - cx;
+      }
+      if (t < nj) {
+        const int j = jlow + t;
+        double mn, pl;
+        if (comp == 1) { mn = 0. + (j - 0.5) * dy; pl = 0. + (j + 0.5) * dy; }
+        else { mn = 0. + (j - 1) * dy; pl = 0. + j * dy; }
+        sym[t] = (mn - cy) * (mn - cy); syp[t] = (pl - cy) * (pl - cy);
+        fym[t] = (float)sym[t]; fyp[t] = (float)syp[t];
+        sry[t] = 0. + (j - 0.5) * dy - cy;
+      }
+      if (t < nk) {
+        const int k = klow + t;
+        double mn, pl;
+        if (comp < 2) { mn = (k - 1) * dz; pl = k * dz; }
+        else { mn = (k - 0.5) * dz; pl = (k + 0.5) * dz; }
+        szm[t] = (mn - cz) * (mn - cz); szp[t] = (pl - cz) * (pl - cz);
+        fzm[t] = (float)szm[t]; fzp[t] = (float)szp[t];
+        srz[t] = (k - 0.5) * dz - cz;
       }
     }
+    if (threadIdx.x == 0) qn = 0;
     __syncthreads();
-    for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = acc[q];
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (threadIdx.x < o)
-        for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
-      __syncthreads();
+    const int nlines = nj * nk;
+    const long row0 = fidx(g, ilow - 1, 0, 0);
+    for (int base = 0; base < nlines; base += blockDim.x) {
+      const int L = base + threadIdx.x;
+      if (L < nlines) {
+        const int tj = L % nj, tk = L / nj;
+        const float yzp = fyp[tj] + fzp[tk];
+        const float ymin = fminf(fym[tj], fyp[tj]) + fminf(fzm[tk], fzp[tk]);
+        const float ymax = fmaxf(fym[tj], fyp[tj]) + fmaxf(fzm[tk], fzp[tk]);
+        const long lo = row0 + fidx(g, 0, jlow + tj - 1, klow + tk);
+        double s0 = 0., sx = 0.;
+        for (int ti = 0; ti < ni; ++ti) {
+          const float dxp2f = fxp[ti], dxm2f = fxm[ti];
+          const float dist2f = dxp2f + yzp;
+          const float mind2f = fminf(dxm2f, dxp2f) + ymin;
+          if (GEO32) {
+            if (!(dist2f < radin2f) && mind2f >= rthrf) continue;  // outside
+          } else {
+            if (!(dist2f < radin2_lo) && !(dist2f <= radin2_hi) && mind2f > rthr_hi) continue;
+          }
+          const double f = F ? (double)F[lo + ti] : 1.;
+          double fw;
+          if (GEO32) {
+            float wgt = 1.f;
+            if (!(dist2f < radin2f)) {
+              const float maxd2f = fmaxf(dxm2f, dxp2f) + ymax;
+              if (!(maxd2f < rthrf))
+                wgt = corner_fraction_f(radiusf, dxm2f, dxp2f, fym[tj], fyp[tj], fzm[tk], fzp[tk]);
+            }
+            fw = wgt == 1.f ? f : f * (double)wgt;
+          } else {
+            bool sure = dist2f < radin2_lo;  // surely inside radin
+            if (!sure && dist2f > radin2_hi) {
+              const float maxd2f = fmaxf(dxm2f, dxp2f) + ymax;
+              sure = maxd2f < rthr_lo;  // surely all corners inside
+            }
+            if (!sure) {  // the reference's FP64 test decides
+              const int q = atomicAdd(&qn, 1);
+              if (q < QCAP) {
+                queue[q] = ti | (tj << 8) | (tk << 16);
+                continue;
+              }
+              // queue full: decide here
+              const double dxp2 = sxp[ti], dyp2 = syp[tj], dzp2 = szp[tk];
+              double frac = 1.;
+              if (!(dxp2 + dyp2 + dzp2 < radin2)) {
+                const double dxm2 = sxm[ti], dym2 = sym[tj], dzm2 = szm[tk];
+                const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
+                if (mind2 >= rthr) continue;
+                const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
+                if (!(maxd2 < rthr)) frac = corner_fraction(radius, dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
+              }
+              fw = f * frac;
+            } else {
+              fw = f;
+            }
+          }
+          s0 += fw;
+          sx = fma(srx[ti], fw, sx);
+        }
+        const double ry = sry[tj], rz = srz[tk];
+        a0 += s0;
+        if (comp == 0) { ta = fma(rz, s0, ta); tb = fma(-ry, s0, tb); }
+        else if (comp == 1) { ta = fma(-rz, s0, ta); tb += sx; }
+        else { ta = fma(ry, s0, ta); tb -= sx; }
+      }
+      if (!GEO32) {
+        __syncthreads();
+        const int nq = min(qn, QCAP);
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+          const int e = queue[q];
+          const int ti = e & 0xff, tj = (e >> 8) & 0xff, tk = e >> 16;
+          const double dxp2 = sxp[ti], dyp2 = syp[tj], dzp2 = szp[tk];
+          double frac = 1.;
+          if (!(dxp2 + dyp2 + dzp2 < radin2)) {
+            const double dxm2 = sxm[ti], dym2 = sym[tj], dzm2 = szm[tk];
+            const double mind2 = fmin(dxm2, dxp2) + fmin(dym2, dyp2) + fmin(dzm2, dzp2);
+            if (mind2 >= rthr) continue;
+            const double maxd2 = fmax(dxm2, dxp2) + fmax(dym2, dyp2) + fmax(dzm2, dzp2);
+            if (!(maxd2 < rthr)) frac = corner_fraction(radius, dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
+          }
+          const double fw = (F ? (double)F[row0 + fidx(g, ti, jlow + tj - 1, klow + tk)] : 1.) * frac;
+          const double rx = srx[ti], ry = sry[tj], rz = srz[tk];
+          a0 += fw;
+          if (comp == 0) { ta = fma(rz, fw, ta); tb = fma(-ry, fw, tb); }
+          else if (comp == 1) { ta = fma(-rz, fw, ta); tb = fma(rx, fw, tb); }
+          else { ta = fma(ry, fw, ta); tb = fma(-rx, fw, tb); }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) qn = 0;
+        __syncthreads();
+      }
     }
-    if (threadIdx.x == 0)
-      for (int q = 0; q < 6; ++q) cps[nbrecv][q] = red[q][0];
+  }
+  red[0][threadIdx.x] = a0;
+  red[1][threadIdx.x] = ta;
+  red[2][threadIdx.x] = tb;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    double tot[6] = {0, 0, 0, 0, 0, 0};
-    for (int n = 0; n <= 8; ++n)
-      for (int q = 0; q < 6; ++q) tot[q] = tot[q] + cps[n][q];
-    if (type == 1) {
-      b.red[p] = tot[0];  // volume of the u-cells (intgr_over_sphere.f90:607-622)
-      PF(PF_INTU) = tot[0]; PF(PF_INTV) = tot[1]; PF(PF_INTW) = tot[2];
-    } else if (type == 2) {
-      PF(PF_INTU) = tot[0]; PF(PF_INTV) = tot[1]; PF(PF_INTW) = tot[2];
-    } else if (type == 3) {
-      PF(PF_INTOMX) = tot[0]; PF(PF_INTOMY) = tot[1]; PF(PF_INTOMZ) = tot[2];
-    } else {
-      PF(PF_INTU) = tot[0]; PF(PF_INTV) = tot[1]; PF(PF_INTW) = tot[2];
-      PF(PF_INTOMX) = tot[3]; PF(PF_INTOMY) = tot[4]; PF(PF_INTOMZ) = tot[5];
-    }
+  if (threadIdx.x < 3) b.red[np + ((long)p * 3 + comp) * 3 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// unit field for the volume sums (type 1)
+template <typename T>
+__global__ void k_sphere_final(PartGeo pg, PartBuffers b, int type) {
+  const int np = pg.np;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const int ms = b.mslv[p];
+  if (ms == 0) return;
+  const double dV = pg.dVeul;
+  double A[3] = {0, 0, 0}, tq[3] = {0, 0, 0};
+  if (ms > 0) {
+    const double *s = b.red + np + (long)p * 9;  // [comp][S0, ta, tb]
+    for (int c = 0; c < 3; ++c) A[c] = s[3 * c] * dV;
+    tq[0] = (s[3 * 1 + 1] + s[3 * 2 + 1]) * dV;
+    tq[1] = (s[3 * 0 + 1] + s[3 * 2 + 2]) * dV;
+    tq[2] = (s[3 * 0 + 2] + s[3 * 1 + 2]) * dV;
   }
+  if (type == 1) b.red[p] = A[0];  // volume of the u-cells (intgr_over_sphere.f90:607-622)
+  if (type == 1 || type == 2 || type == 23) { PF(PF_INTU) = A[0]; PF(PF_INTV) = A[1]; PF(PF_INTW) = A[2]; }
+  if (type == 3 || type == 23) { PF(PF_INTOMX) = tq[0]; PF(PF_INTOMY) = tq[1]; PF(PF_INTOMZ) = tq[2]; }
 }
 
 template <typename T>
 void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,
                              const T *w, int type) {
   if (pg.np == 0) return;
-  k_sphere_int<T><<<pg.np, 256, 0, s>>>(g, pg, b, u, v, w, type);
+  const dim3 grid(pg.np, 3);
+  const bool unit = type == 1;  // volume: integrate w = 1 (F == nullptr)
+  if constexpr (sizeof(T) == 4)
+    k_sphere_int<T, true><<<grid, 256, 0, s>>>(g, pg, b, unit ? nullptr : u, unit ? nullptr : v, unit ? nullptr : w);
+  else
+    k_sphere_int<T, false><<<grid, 256, 0, s>>>(g, pg, b, unit ? nullptr : u, unit ? nullptr : v, unit ? nullptr : w);
+  k_sphere_final<T><<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, type);
 }
 template void launch_sphere_integrals<double>(cudaStream_t, const Geo &, const PartGeo &, PartBuffers,
                                               const double *, const double *, const double *, int);

@@ -202,3 +202,67 @@ class IBMSolver:
     def sync(self):
         if "sync" in self.fn:
             self._chk(self.fn["sync"](self.ctx))
+
+    # --- learned forcing (IBM_MODE_MIXED_LEARNED) ------------------------------
+
+    NN_NPARAM = 29315
+    NN_NNORM = 198
+
+    def harvest(self, capacity: int, stride: int = 1, passes: int = 0):
+        """Collect (features, correction) pairs from the plain passes of the
+        following forcing loops; capacity=0 stops and keeps the samples."""
+        self._chk(self.fn["harvest"](self.ctx, int(capacity), int(stride), int(passes)))
+
+    def train_forcing_model(self, nsteps: int, batch: int = 8192, lr: float = 1e-3, seed: int = 0,
+                            reinit: bool = False) -> float:
+        loss = C.c_double()
+        self._chk(self.fn["train_forcing_model"](self.ctx, int(nsteps), int(batch), float(lr), int(seed) & 0xFFFFFFFF,
+                                                 int(reinit), C.byref(loss)))
+        return loss.value
+
+    def set_forcing_model(self, params: np.ndarray, norm: np.ndarray):
+        p = np.ascontiguousarray(params, np.float32)
+        n = np.ascontiguousarray(norm, np.float32)
+        assert p.size == self.NN_NPARAM and n.size == self.NN_NNORM
+        self._chk(self.fn["set_forcing_model"](self.ctx, _fp(p), _fp(n)))
+
+    def get_forcing_model(self) -> tuple[np.ndarray, np.ndarray]:
+        p = np.zeros(self.NN_NPARAM, np.float32)
+        n = np.zeros(self.NN_NNORM, np.float32)
+        self._chk(self.fn["get_forcing_model"](self.ctx, _fp(p), _fp(n)))
+        return p, n
+
+    def learned_config(self, enable: bool = True, fallback_ratio: float = 1.5, plain_rms_ref: float = 0.0):
+        self._chk(self.fn["learned_config"](self.ctx, int(enable), float(fallback_ratio), float(plain_rms_ref)))
+
+    def learned_stats(self) -> dict:
+        s = (C.c_double * 6)()
+        self._chk(self.fn["learned_stats"](self.ctx, s))
+        keys = ("last_rms", "plain_rms_ref", "fallback_ratio", "fallbacks", "learned_loops", "harvested")
+        return dict(zip(keys, list(s)))
+
+    def mlp_gradient(self, params, x, t):
+        """Loss, gradient and outputs of the library's training kernels on one batch."""
+        p = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        nb = x.shape[0]
+        g = np.zeros(self.NN_NPARAM, np.float32)
+        y = np.zeros((nb, 3), np.float32)
+        loss = C.c_float()
+        self._chk(self.fn["mlp_gradient"](self.ctx, _fp(p), _fp(x), _fp(t), nb, _fp(g), C.byref(loss), _fp(y)))
+        return float(loss.value), g, y
+
+    def mlp_fit(self, params, x, t, nsteps: int, lr: float = 1e-3):
+        p = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        out = np.zeros(self.NN_NPARAM, np.float32)
+        losses = np.zeros(max(nsteps, 1), np.float32)
+        self._chk(self.fn["mlp_fit"](self.ctx, _fp(p), _fp(x), _fp(t), x.shape[0], int(nsteps), float(lr),
+                                     _fp(out), _fp(losses)))
+        return out, losses[:nsteps]
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))

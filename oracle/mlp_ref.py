@@ -67,7 +67,14 @@ def init_params(seed: int) -> np.ndarray:
     return np.concatenate([np.ravel(x) for x in parts]).astype(np.float32)
 
 
-def forward(params: np.ndarray, x: np.ndarray) -> dict:
+def _ident(a):
+    return np.asarray(a, np.float64)
+
+
+def forward(params: np.ndarray, x: np.ndarray, exact: bool = False) -> dict:
+    """exact=True skips every BF16 rounding (float64 throughout), for the
+    finite-difference check of the backward formulas."""
+    bf16 = _ident if exact else globals()["bf16"]
     w1, b1, w2, b2, w3, b3 = split(params)
     xb = bf16(x)
     z1 = xb.astype(np.float64) @ bf16(w1).T.astype(np.float64) + b1
@@ -78,10 +85,11 @@ def forward(params: np.ndarray, x: np.ndarray) -> dict:
     return {"x": xb, "z1": z1, "h1": h1, "z2": z2, "h2": h2, "y": y}
 
 
-def loss_and_grads(params: np.ndarray, x: np.ndarray, t: np.ndarray):
+def loss_and_grads(params: np.ndarray, x: np.ndarray, t: np.ndarray, exact: bool = False):
     """MSE loss mean over the batch of the squared error summed over outputs."""
+    bf16 = _ident if exact else globals()["bf16"]
     w1, b1, w2, b2, w3, b3 = split(params)
-    f = forward(params, x)
+    f = forward(params, x, exact)
     nb = x.shape[0]
     diff = f["y"] - t
     loss = float(np.sum(diff * diff) / nb)

@@ -1,0 +1,196 @@
+"""Learned forcing (IBM_MODE_MIXED_LEARNED): the library's BF16 tensor-core
+training kernels against the CPU reference (oracle/mlp_ref.py), and what the
+trained network gains over the forcing loop without it."""
+import numpy as np
+import pytest
+
+from _util import field_errors, small_case
+from interparts_mpich_gb300 import IBM_MODE_MIXED_LEARNED, IBMSolver
+from oracle import mlp_ref
+from oracle.oracle import OracleSolver
+
+pytestmark = pytest.mark.gpu
+
+# GPU vs reference: the reference rounds to BF16 where the GPU does; what is
+# left is FP32 summation order inside the tensor-core tiles and tanhf, which
+# can move a value across a BF16 rounding boundary now and then.
+GRAD_REL_TOL = 5e-3
+OUT_REL_TOL = 2e-3
+
+
+def _blocks():
+    o = 0
+    for name, shape in (("W1", (128, 96)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)),
+                        ("W3", (3, 128)), ("b3", (3,))):
+        n = int(np.prod(shape))
+        yield name, slice(o, o + n)
+        o += n
+
+
+def _batch(nb, seed):
+    rng = np.random.default_rng(seed)
+    p = mlp_ref.init_params(seed)
+    p[12288:12416] = rng.standard_normal(128) * 0.1   # b1
+    p[28800:28928] = rng.standard_normal(128) * 0.1   # b2
+    p[28928:29312] *= 10.0                             # W3 of order 1
+    x = rng.standard_normal((nb, 96)).astype(np.float32)
+    t = rng.standard_normal((nb, 3)).astype(np.float32)
+    return p.astype(np.float32), x, t
+
+
+@pytest.mark.parametrize("nb", [64, 200, 1000])
+def test_mlp_gradient_matches_cpu_reference(gpu_lib, nb):
+    case = small_case(n=16, nsp=0)
+    g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    p, x, t = _batch(nb, seed=nb)
+    loss, grad, y = g.mlp_gradient(p, x, t)
+    f = mlp_ref.forward(p, x)
+    ref_loss, ref_grad = mlp_ref.loss_and_grads(p, x, t)
+    assert np.linalg.norm(y - f["y"]) <= OUT_REL_TOL * np.linalg.norm(f["y"])
+    assert abs(loss - ref_loss) <= OUT_REL_TOL * ref_loss
+    for name, sl in _blocks():
+        a, b = grad[sl].astype(np.float64), ref_grad[sl]
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err <= GRAD_REL_TOL, (name, err)
+
+
+def test_mlp_adam_steps_match_cpu_reference(gpu_lib):
+    case = small_case(n=16, nsp=0)
+    g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    p, x, t = _batch(256, seed=7)
+    lr = 1e-3
+    out, losses = g.mlp_fit(p, x, t, nsteps=3, lr=lr)
+    q = p.astype(np.float64)
+    m = np.zeros_like(q)
+    v = np.zeros_like(q)
+    ref_losses = []
+    for s in range(1, 4):
+        ls, gr = mlp_ref.loss_and_grads(q.astype(np.float32), x, t)
+        ref_losses.append(ls)
+        q, m, v = mlp_ref.adam_step(q, gr, m, v, s, lr=lr)
+    assert np.allclose(losses, ref_losses, rtol=OUT_REL_TOL)
+    # each Adam step moves a weight by about lr: compare the displacements
+    d_gpu = out.astype(np.float64) - p
+    d_ref = q - p
+    assert np.linalg.norm(d_gpu - d_ref) <= 2e-2 * np.linalg.norm(d_ref)
+
+
+def test_mlp_training_reduces_loss(gpu_lib):
+    """A learnable target (a fixed random network of the same shape): the
+    GPU training loop drives the loss down by orders of magnitude."""
+    case = small_case(n=16, nsp=0)
+    g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((2048, 96)).astype(np.float32)
+    teacher = mlp_ref.init_params(11)
+    t = mlp_ref.forward(teacher, x)["y"].astype(np.float32)
+    t /= t.std()
+    _, losses = g.mlp_fit(mlp_ref.init_params(12), x, t, nsteps=400, lr=2e-3)
+    assert losses[-1] < 0.05 * losses[0], (losses[0], losses[-1])
+
+
+def _flow_case():
+    return small_case(n=48, nsp=10, radius_cells=5.0, seed=11, visc=1.0 / 1000.0)
+
+
+@pytest.fixture(scope="module")
+def trained(gpu_lib):
+    """Harvest from the plain Nl=3 passes of 8 steps, train on the GPU."""
+    case = _flow_case()
+    s = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    s.setup()
+    dt = 0.5 * OracleSolver(case).chkdt()
+    s.harvest(capacity=400000, stride=1, passes=3)
+    s.run(dt, 8)
+    s.harvest(0)
+    st = s.learned_stats()
+    loss = s.train_forcing_model(nsteps=6000, batch=4096, lr=1e-3, seed=1)
+    return s, dt, loss, st
+
+
+def _loop_residual(s, dt, nl):
+    s.rk(1, dt)
+    s.forcing_loop(dt, nl)
+    return s.slip_residual()[1]
+
+
+def test_learned_forcing_gain(trained):
+    """Same state, same substep: the network after one plain sweep against
+    the plain loop with one sweep (the method without it) and with Nl=3."""
+    s, dt, loss, st = trained
+    assert st["harvested"] > 10000 and st["plain_rms_ref"] > 0
+    assert loss < 0.2, loss
+    s.learned_config(enable=False)
+    res_plain3 = _loop_residual(s, dt, 3)
+    res_one = _loop_residual(s, dt, 1)
+    s.learned_config(enable=True, fallback_ratio=1e9)
+    res_learned = _loop_residual(s, dt, 3)
+    stats = s.learned_stats()
+    assert stats["fallbacks"] == 0
+    print(f"rms no-slip residual: one sweep {res_one:.3e}, plain Nl=3 {res_plain3:.3e}, "
+          f"one sweep + network {res_learned:.3e}")
+    assert res_learned < 0.5 * res_one
+    # the fallback criterion: within 1.5x of the plain loop's residual
+    assert res_learned <= 1.5 * res_plain3
+
+
+def test_learned_fallback_runs_plain_passes(trained):
+    s, dt, _, _ = trained
+    s.learned_config(enable=True, fallback_ratio=1e9)
+    res_learned = _loop_residual(s, dt, 3)
+    before = s.learned_stats()["fallbacks"]
+    s.learned_config(enable=True, fallback_ratio=1e-12)  # every loop fails the test
+    res_fb = _loop_residual(s, dt, 3)
+    assert s.learned_stats()["fallbacks"] == before + 1
+    assert res_fb < res_learned
+    s.learned_config(enable=True, fallback_ratio=1.5)
+
+
+def test_learned_model_roundtrip(trained):
+    s, dt, _, _ = trained
+    p, n = s.get_forcing_model()
+    assert p.shape == (29315,) and n.shape == (198,) and np.all(np.isfinite(p))
+    case = _flow_case()
+    t = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    t.set_forcing_model(p, n)
+    q, m = t.get_forcing_model()
+    assert np.array_equal(p, q) and np.array_equal(n, m)
+
+
+def _steps(s, dt, nl, nsteps):
+    for _ in range(nsteps):
+        for r in (1, 2, 3):
+            s.rk(r, dt)
+            s.forcing_loop(dt, nl)
+            s.project(r, dt)
+            s.intgr_nwtn_eulr(r, dt)
+
+
+def test_learned_20_steps_against_oracle(trained):
+    """A fresh run with the trained model against the FP64 oracle after 20
+    steps.  The learned correction is an approximation of the plain Nl=3
+    correction, so its flow departs from the Nl=3 oracle by more than the
+    mixed form's 1e-4 (the plain method itself moves by 1.6e-2 on this case
+    between Nl=3 and Nl=6): it must stay within that spread of the method's
+    own forcing convergence, and its loops within the fallback bound."""
+    s, dt, _, _ = trained
+    p, n = s.get_forcing_model()
+    case = _flow_case()
+    m = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    m.setup()
+    m.set_forcing_model(p, n)
+    m.learned_config(enable=True, fallback_ratio=1.5, plain_rms_ref=s.learned_stats()["plain_rms_ref"])
+    m.run(dt, 20)
+    o3 = OracleSolver(case)
+    o3.setup()
+    _steps(o3, dt, 3, 20)
+    o6 = OracleSolver(case)
+    o6.setup()
+    _steps(o6, dt, 6, 20)
+    f3 = o3.get_fields()
+    e_learned = max(field_errors(m.get_fields(), f3, names=("u", "v", "w")).values())
+    e_nl = max(field_errors(o6.get_fields(), f3, names=("u", "v", "w")).values())
+    print(f"velocity rel L2 after 20 steps vs oracle Nl=3: learned {e_learned:.3e}, oracle Nl=6 {e_nl:.3e}")
+    assert e_learned < e_nl
+    st = m.learned_stats()
+    assert st["learned_loops"] == 60
