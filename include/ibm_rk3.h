@@ -245,6 +245,8 @@ int ibm_learned_stats(ibm_ctx *ctx, double stats[6]);
  * mean over rows of the squared error summed over the 3 outputs. */
 int ibm_mlp_gradient(ibm_ctx *ctx, const float *params, const float *x, const float *t, int nb, float *grad,
                      float *loss, float *y);
+/* The inference kernel of the forcing loop on a caller batch: y[nb][3]. */
+int ibm_mlp_infer(ibm_ctx *ctx, const float *params, const float *x, int nb, float *y);
 /* nsteps full-batch Adam steps from params_in with fresh moments:
  * params_out[IBM_NN_NPARAM], losses[nsteps] (loss before each update). */
 int ibm_mlp_fit(ibm_ctx *ctx, const float *params_in, const float *x, const float *t, int nb, int nsteps,

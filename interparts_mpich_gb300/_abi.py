@@ -158,6 +158,7 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "learned_config": (C.c_int, [ctx, C.c_int, C.c_double, C.c_double]),
         "learned_stats": (C.c_int, [ctx, c_double_p]),
         "mlp_gradient": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p]),
+        "mlp_infer": (C.c_int, [ctx, c_float_p, c_float_p, C.c_int, c_float_p]),
         "mlp_fit": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, C.c_int, C.c_double, c_float_p,
                               c_float_p]),
     }

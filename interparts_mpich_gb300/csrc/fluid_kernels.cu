@@ -25,29 +25,32 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z + 1;
   if (i >= g.I || j >= g.J) return;
-  const int ip = i + 1 == g.I ? 0 : i + 1, im = i == 0 ? g.I - 1 : i - 1;
-  const int jp = j + 1 == g.J ? 0 : j + 1, jm = j == 0 ? g.J - 1 : j - 1;
-  const long PL = g.plane;
+  // neighbours as 32-bit offsets from one 64-bit cell address (periodic
+  // wrap in x and y folded into the offsets)
+  const int dip = i + 1 == g.I ? 1 - g.I : 1, dim = i == 0 ? g.I - 1 : -1;
+  const int djp = (j + 1 == g.J ? 1 - g.J : 1) * g.I, djm = (j == 0 ? g.J - 1 : -1) * g.I;
+  const int PL = g.I * g.J;
   const long c = fidx(g, i, j, k);
-  const long rj = (long)k * g.J;  // row base helpers
-  auto at = [&](int ii, int jj, int kk) -> long { return ((long)kk * g.J + jj) * g.I + ii; };
-  (void)rj;
+  const int ip = dip, im = dim, jp = djp, jm = djm;
+  auto at = [&](int di, int dj, int dk) -> long { return c + (di + dj + dk); };
+  const int j0 = 0, i0 = 0;
+  const int kp = PL, km = -PL;
   const T dxi = (T)g.dxi, dyi = (T)g.dyi, dzi = (T)g.dzi, visc = (T)g.visc;
   const T q = (T)0.25;
   // u-neighbourhood
-  const T U0 = (T)u[c], Uip = (T)u[at(ip, j, k)], Uim = (T)u[at(im, j, k)], Ujp = (T)u[at(i, jp, k)],
-          Ujm = (T)u[at(i, jm, k)];
+  const T U0 = (T)u[c], Uip = (T)u[at(ip, j0, 0)], Uim = (T)u[at(im, j0, 0)], Ujp = (T)u[at(i0, jp, 0)],
+          Ujm = (T)u[at(i0, jm, 0)];
   const T Ukp = (T)u[c + PL], Ukm = (T)u[c - PL];
-  const T V0 = (T)v[c], Vip = (T)v[at(ip, j, k)], Vim = (T)v[at(im, j, k)], Vjp = (T)v[at(i, jp, k)],
-          Vjm = (T)v[at(i, jm, k)];
+  const T V0 = (T)v[c], Vip = (T)v[at(ip, j0, 0)], Vim = (T)v[at(im, j0, 0)], Vjp = (T)v[at(i0, jp, 0)],
+          Vjm = (T)v[at(i0, jm, 0)];
   const T Vkp = (T)v[c + PL], Vkm = (T)v[c - PL];
-  const T W0 = (T)w[c], Wip = (T)w[at(ip, j, k)], Wim = (T)w[at(im, j, k)], Wjp = (T)w[at(i, jp, k)],
-          Wjm = (T)w[at(i, jm, k)];
+  const T W0 = (T)w[c], Wip = (T)w[at(ip, j0, 0)], Wim = (T)w[at(im, j0, 0)], Wjp = (T)w[at(i0, jp, 0)],
+          Wjm = (T)w[at(i0, jm, 0)];
   const T Wkp = (T)w[c + PL], Wkm = (T)w[c - PL];
   // diagonal neighbours
-  const T Vipjm = (T)v[at(ip, jm, k)], Wipkm = (T)w[at(ip, j, k - 1)];
-  const T Uimjp = (T)u[at(im, jp, k)], Wjpkm = (T)w[at(i, jp, k - 1)];
-  const T Uimkp = (T)u[at(im, j, k + 1)], Vjmkp = (T)v[at(i, jm, k + 1)];
+  const T Vipjm = (T)v[at(ip, jm, 0)], Wipkm = (T)w[at(ip, j0, km)];
+  const T Uimjp = (T)u[at(im, jp, 0)], Wjpkm = (T)w[at(i0, jp, km)];
+  const T Uimkp = (T)u[at(im, j0, kp)], Vjmkp = (T)v[at(i0, jm, kp)];
   // momxad (mom.f90:21-50)
   T ru_new;
   {
@@ -93,8 +96,8 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
   }
   // pressure gradient (momxp/momyp/momzp)
   const T P0 = (T)p[c];
-  const T gx = -dxi * ((T)p[at(ip, j, k)] - P0);
-  const T gy = -dyi * ((T)p[at(i, jp, k)] - P0);
+  const T gx = -dxi * ((T)p[at(ip, j0, 0)] - P0);
+  const T gy = -dyi * ((T)p[at(i0, jp, 0)] - P0);
   const T gz = -dzi * ((T)p[c + PL] - P0);
   T du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
   if (STAGE == 1) {

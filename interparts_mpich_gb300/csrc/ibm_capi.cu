@@ -434,8 +434,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   HarvestArgs none{};
   launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->norm, c->norm + 96, c->lx,
                         none);
-  launch_mlp_forward(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly, nullptr, nullptr,
-                     nullptr, nullptr, 0);
+  launch_mlp_infer(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly);
   launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
   launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf);
   launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
@@ -1285,6 +1284,26 @@ int ibm_mlp_gradient(ibm_ctx *c, const float *params, const float *x, const floa
       e = cudaMemcpyAsync(y, B.y, (size_t)nb * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     st = cuda_err(c, e, "ibm_mlp_gradient");
+  }
+  cudaStreamSynchronize(c->stream);
+  free_mlp_batch(B);
+  free_mlp_model(B);
+  return st;
+}
+
+int ibm_mlp_infer(ibm_ctx *c, const float *params, const float *x, int nb, float *y) {
+  if (!c || !params || !x || !y || nb < 1) return IBM_E_INVALID;
+  MlpTrainBuffers B{};
+  std::vector<float> t((size_t)nb * 3, 0.f);
+  int st = mlp_scratch(c, params, x, t.data(), nb, B);
+  if (st == IBM_OK) {
+    launch_mlp_infer(c->stream, B.x, nb, B.w1b, B.w2b, B.params, B.y);
+    c->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(y, B.y, (size_t)nb * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    st = cuda_err(c, e, "ibm_mlp_infer");
   }
   cudaStreamSynchronize(c->stream);
   free_mlp_batch(B);

@@ -62,29 +62,107 @@ void launch_ibm_stencil(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuff
 template void launch_ibm_stencil<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers);
 template void launch_ibm_stencil<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers);
 
-// interpolation of the three staggered components at point t
-template <typename T>
-__device__ __forceinline__ void interp_point(const Geo &g, const PointStencil &s, const T *__restrict__ fu,
-                                             const T *__restrict__ fv, const T *__restrict__ fw, double &ou,
-                                             double &ov, double &ow) {
-  double au = 0., av = 0., aw = 0.;
-  int ix[3], ixh[3], jy[3], jyh[3];
-  for (int m = 0; m < 3; ++m) {
-    ix[m] = wrapm(s.ilows + m - 1, g.I);
-    ixh[m] = wrapm(s.ilow + m - 1, g.I);
-    jy[m] = wrapm(s.jlows + m - 1, g.J);
-    jyh[m] = wrapm(s.jlow + m - 1, g.J);
+
+// ---------------------------------------------------------------------------
+// Shared-memory field boxes of one particle.  Per component the box covers
+// the cells of the 27-tap stencils of the particle's points, x/y indices
+// relative to the first point (periodic wrap), z absolute; box cell
+// (cx, cy, cz) <-> tap (bx - 1 + i, by - 1 + j, bz + k) of a point with
+// relative origin (rx, ry, bz) at cx = rx - b0 + i, cy = ry - b1 + j,
+// cz = bz - b2 + k.  bg[c] = {refx, refy, b0, b1, b2, nbx, nby, nbz}.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int relwrap(int d, int n) {
+  const int h = n / 2;
+  return d >= h ? d - n : (d < -h ? d + n : d);
+}
+template <typename ST>
+__device__ __forceinline__ void comp_origin(const ST &s, int c, int &bx, int &by, int &bz) {
+  bx = c == 0 ? s.ilows : s.ilow;
+  by = c == 1 ? s.jlows : s.jlow;
+  bz = c == 2 ? s.klows : s.klow;
+}
+// block-wide; returns the same value in every thread: true when all three
+// boxes fit `cap` cells (and are not wider than half the periodic domain)
+template <typename T, typename ST>
+__device__ bool build_boxes(const Geo &g, const ST *__restrict__ st, long t0, int nla, const T *__restrict__ fu,
+                            const T *__restrict__ fv, const T *__restrict__ fw, T *box, int cap, int (*bg)[8],
+                            int (*bmax)[3]) {
+  if (threadIdx.x < 3) {
+    const int c = threadIdx.x;
+    int bx, by, bz;
+    comp_origin(st[t0], c, bx, by, bz);
+    bg[c][0] = bx; bg[c][1] = by;
+    bg[c][2] = bg[c][3] = bg[c][4] = 0x7fffffff;
+    bmax[c][0] = bmax[c][1] = bmax[c][2] = -0x7fffffff;
   }
-  // separable form of the 27-tap sums of interp_spread.f90:132-154:
-  // sum_k phiz_k sum_j phiy_j sum_i phix_i f_ijk (same terms, fewer FP64 ops)
+  __syncthreads();
+  // per-thread extremes, then one shared atomic per warp and bound
+  int lo[3][3], hi[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int d = 0; d < 3; ++d) { lo[c][d] = 0x7fffffff; hi[c][d] = -0x7fffffff; }
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const ST &s = st[t0 + l];
+    for (int c = 0; c < 3; ++c) {
+      int bx, by, bz;
+      comp_origin(s, c, bx, by, bz);
+      const int r[3] = {relwrap(bx - bg[c][0], g.I), relwrap(by - bg[c][1], g.J), bz};
+      for (int d = 0; d < 3; ++d) { lo[c][d] = min(lo[c][d], r[d]); hi[c][d] = max(hi[c][d], r[d]); }
+    }
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int d = 0; d < 3; ++d) {
+      const int wl = __reduce_min_sync(0xffffffffu, lo[c][d]), wh = __reduce_max_sync(0xffffffffu, hi[c][d]);
+      if ((threadIdx.x & 31) == 0) { atomicMin(&bg[c][2 + d], wl); atomicMax(&bmax[c][d], wh); }
+    }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int c = threadIdx.x;
+    bg[c][5] = bmax[c][0] - bg[c][2] + 3;
+    bg[c][6] = bmax[c][1] - bg[c][3] + 3;
+    bg[c][7] = bmax[c][2] - bg[c][4] + 3;
+  }
+  __syncthreads();
+  bool ok = true;
+  for (int c = 0; c < 3; ++c)
+    ok = ok && (long)bg[c][5] * bg[c][6] * bg[c][7] <= cap && bg[c][5] < g.I / 2 && bg[c][6] < g.J / 2;
+  if (!ok) return false;
+  for (int c = 0; c < 3; ++c) {
+    const T *F = c == 0 ? fu : (c == 1 ? fv : fw);
+    const int nbx = bg[c][5], nby = bg[c][6], nxy = nbx * nby, nbox = nxy * bg[c][7];
+    const int x0 = bg[c][0] + bg[c][2] - 1, y0 = bg[c][1] + bg[c][3] - 1, z0 = bg[c][4];
+    for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
+      const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
+      box[c * cap + q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
+    }
+  }
+  __syncthreads();
+  return true;
+}
+// offset of tap (0,0,0) of component c for a point, and the box strides
+template <typename ST>
+__device__ __forceinline__ int box_origin(const Geo &g, const ST &s, int c, const int (*bg)[8]) {
+  int bx, by, bz;
+  comp_origin(s, c, bx, by, bz);
+  const int cx = relwrap(bx - bg[c][0], g.I) - bg[c][2], cy = relwrap(by - bg[c][1], g.J) - bg[c][3];
+  return ((bz - bg[c][4]) * bg[c][6] + cy) * bg[c][5] + cx;
+}
+constexpr int INTERP_BOX = 8192;  // cells per component box
+
+// interpolation of the three staggered components at point t
+// separable form of the 27-tap sums of interp_spread.f90:132-154:
+// sum_k phiz_k sum_j phiy_j sum_i phix_i f_ijk (same terms, fewer FP64 ops)
+template <typename FU, typename FV, typename FW>
+__device__ __forceinline__ void interp_sep(const PointStencil &s, FU U, FV V, FW W, double &ou, double &ov,
+                                           double &ow) {
+  double au = 0., av = 0., aw = 0.;
   for (int k = 0; k < 3; ++k) {
     double su = 0., sv = 0., sw = 0.;
     for (int j = 0; j < 3; ++j) {
       double ru = 0., rv = 0., rw = 0.;
       for (int i = 0; i < 3; ++i) {
-        ru += (double)fu[fidx(g, ix[i], jyh[j], s.klow + k)] * s.phix[i];
-        rv += (double)fv[fidx(g, ixh[i], jy[j], s.klow + k)] * s.phixh[i];
-        rw += (double)fw[fidx(g, ixh[i], jyh[j], s.klows + k)] * s.phixh[i];
+        ru += U(i, j, k) * s.phix[i];
+        rv += V(i, j, k) * s.phixh[i];
+        rw += W(i, j, k) * s.phixh[i];
       }
       su += ru * s.phiyh[j];
       sv += rv * s.phiy[j];
@@ -95,6 +173,22 @@ __device__ __forceinline__ void interp_point(const Geo &g, const PointStencil &s
     aw += sw * s.phiz[k];
   }
   ou = au; ov = av; ow = aw;
+}
+
+template <typename T>
+__device__ __forceinline__ void interp_point(const Geo &g, const PointStencil &s, const T *__restrict__ fu,
+                                             const T *__restrict__ fv, const T *__restrict__ fw, double &ou,
+                                             double &ov, double &ow) {
+  int ix[3], ixh[3], jy[3], jyh[3];
+  for (int m = 0; m < 3; ++m) {
+    ix[m] = wrapm(s.ilows + m - 1, g.I);
+    ixh[m] = wrapm(s.ilow + m - 1, g.I);
+    jy[m] = wrapm(s.jlows + m - 1, g.J);
+    jyh[m] = wrapm(s.jlow + m - 1, g.J);
+  }
+  interp_sep(s, [&](int i, int j, int k) { return (double)fu[fidx(g, ix[i], jyh[j], s.klow + k)]; },
+             [&](int i, int j, int k) { return (double)fv[fidx(g, ixh[i], jy[j], s.klow + k)]; },
+             [&](int i, int j, int k) { return (double)fw[fidx(g, ixh[i], jyh[j], s.klows + k)]; }, ou, ov, ow);
 }
 
 // eulr2lagr + complagrforces/updtlagrforces for one particle per block:
@@ -164,10 +258,43 @@ void launch_ibm_interp_force(cudaStream_t s, const Geo &g, const PartGeo &pg, Ib
 }
 template void launch_ibm_interp_force<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, const double *,
                                               const double *, const double *, double, int);
-template void launch_ibm_interp_force<float>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, const float *,
-                                             const float *, const float *, double, int);
 
-// lagr2eulr spreading: see k_ibm_spread_box below
+// lagr2eulr increment: spread dF = (U_l - u~_l)/dt with the terms of
+// interp_spread.f90:329-355, F*coeff0*phix*phiy*phiz, the (j,k) factor
+// formed once per row of three taps
+template <typename T>
+__global__ void __launch_bounds__(256) k_ibm_spread(Geo g, PartGeo pg, IbmBuffers b, T *__restrict__ fu,
+                                                    T *__restrict__ fv, T *__restrict__ fw, double dti,
+                                                    double coeff0) {
+  const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int p = t / pg.nl, l = t - p * pg.nl;
+    if (l >= b.nla[p]) continue;
+    const PointStencil s = b.st[t];
+    const double dfx = (b.ul[t] - b.dudtl[t]) * dti;
+    const double dfy = (b.vl[t] - b.dvdtl[t]) * dti;
+    const double dfz = (b.wl[t] - b.dwdtl[t]) * dti;
+    int ix[3], ixh[3], jy[3], jyh[3];
+    for (int m = 0; m < 3; ++m) {
+      ix[m] = wrapm(s.ilows + m - 1, g.I);
+      ixh[m] = wrapm(s.ilow + m - 1, g.I);
+      jy[m] = wrapm(s.jlows + m - 1, g.J);
+      jyh[m] = wrapm(s.jlow + m - 1, g.J);
+    }
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j) {
+        const double a = dfx * coeff0 * s.phiyh[j] * s.phizh[k];
+        const double bb = dfy * coeff0 * s.phiy[j] * s.phizh[k];
+        const double cc = dfz * coeff0 * s.phiyh[j] * s.phiz[k];
+        for (int i = 0; i < 3; ++i) {
+          atomicAdd(&fu[fidx(g, ix[i], jyh[j], s.klow + k)], (T)(a * s.phix[i]));
+          atomicAdd(&fv[fidx(g, ixh[i], jy[j], s.klow + k)], (T)(bb * s.phixh[i]));
+          atomicAdd(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)], (T)(cc * s.phixh[i]));
+        }
+      }
+  }
+}
+
 
 template <typename T>
 __global__ void k_zero_plane(Geo g, T *f, int k) {
@@ -221,8 +348,11 @@ __global__ void __launch_bounds__(256) k_ibm_stencil_f(Geo g, PartGeo pg, IbmBuf
     const int p = t / pg.nl, l = t - p * pg.nl;
     if (l >= b.nla[p]) continue;
     const double xfp = b.xfp[t], yfp = b.yfp[t], zfp = b.zfp[t];
-    double coorxfp = xfp * g.dxi - (double)((long)floor((xfp - 0.5 * g.dx) / g.lx) * g.I);
-    double cooryfp = yfp * g.dyi - (double)((long)floor((yfp - 0.5 * g.dy) / g.ly) * g.J);
+    // periodic image by a multiply: any image whose coordinate stays in
+    // [0, I+1] addresses the same (wrapped) cells with the same weights
+    const double inv_lx = 1. / g.lx, inv_ly = 1. / g.ly;
+    double coorxfp = xfp * g.dxi - (double)((long)floor((xfp - 0.5 * g.dx) * inv_lx) * g.I);
+    double cooryfp = yfp * g.dyi - (double)((long)floor((yfp - 0.5 * g.dy) * inv_ly) * g.J);
     double coorzfp = zfp * g.dzi;
     if (!(coorxfp >= 0. && coorxfp <= g.I + 1.) || !(cooryfp >= 0. && cooryfp <= g.J + 1.) ||
         !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
@@ -236,13 +366,17 @@ __global__ void __launch_bounds__(256) k_ibm_stencil_f(Geo g, PartGeo pg, IbmBuf
     s.ilow = (int)floor(coorxfp);
     s.jlow = (int)floor(cooryfp);
     s.klow = max(min((int)floor(coorzfp), g.K - 2), 1);
+    // offsets of the point from the stencil origins (FP64, exact integer
+    // parts), the 3-tap arguments then in FP32
+    const float ox = (float)(coorxfp - s.ilows), oy = (float)(cooryfp - s.jlows), oz = (float)(coorzfp - s.klows);
+    const float hx = (float)(coorxfp - s.ilow), hy = (float)(cooryfp - s.jlow), hz = (float)(coorzfp - s.klow);
     for (int m = 0; m < 3; ++m) {
-      s.phix[m] = delta3f((float)(1. * s.ilows + m - coorxfp));
-      s.phiy[m] = delta3f((float)(1. * s.jlows + m - cooryfp));
-      s.phiz[m] = delta3f((float)(1. * s.klows + m - coorzfp));
-      s.phixh[m] = delta3f((float)(1. * s.ilow + m - .5 - coorxfp));
-      s.phiyh[m] = delta3f((float)(1. * s.jlow + m - .5 - cooryfp));
-      s.phizh[m] = delta3f((float)(1. * s.klow + m - .5 - coorzfp));
+      s.phix[m] = delta3f((float)m - ox);
+      s.phiy[m] = delta3f((float)m - oy);
+      s.phiz[m] = delta3f((float)m - oz);
+      s.phixh[m] = delta3f(((float)m - 0.5f) - hx);
+      s.phiyh[m] = delta3f(((float)m - 0.5f) - hy);
+      s.phizh[m] = delta3f(((float)m - 0.5f) - hz);
     }
     b.st32[t] = s;
   }
@@ -276,6 +410,27 @@ __device__ __forceinline__ void interp_point_f(const Geo &g, const PointStencilF
   ou = au; ov = av; ow = aw;
 }
 
+// interp_point_f from the particle's shared-memory boxes (same terms, same order)
+__device__ __forceinline__ void interp_box_f(const PointStencilF &s, const float *box, const int (*bg)[8],
+                                             const Geo &g, float &ou, float &ov, float &ow) {
+  const float *B0 = box + box_origin(g, s, 0, bg), *B1 = box + INTERP_BOX + box_origin(g, s, 1, bg),
+              *B2 = box + 2 * INTERP_BOX + box_origin(g, s, 2, bg);
+  const int y0 = bg[0][5], z0 = y0 * bg[0][6], y1 = bg[1][5], z1 = y1 * bg[1][6], y2 = bg[2][5], z2 = y2 * bg[2][6];
+  float au = 0.f, av = 0.f, aw = 0.f;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j) {
+      const float wyz = s.phiyh[j] * s.phizh[k];
+      const float wyz2 = s.phiy[j] * s.phizh[k];
+      const float wyz3 = s.phiyh[j] * s.phiz[k];
+      for (int i = 0; i < 3; ++i) {
+        au += B0[i + j * y0 + k * z0] * (s.phix[i] * wyz);
+        av += B1[i + j * y1 + k * z1] * (s.phixh[i] * wyz2);
+        aw += B2[i + j * y2 + k * z2] * (s.phixh[i] * wyz3);
+      }
+    }
+  ou = au; ov = av; ow = aw;
+}
+
 __global__ void __launch_bounds__(256) k_ibm_interp_force_f(Geo g, PartGeo pg, IbmBuffers b,
                                                             const float *__restrict__ fu, const float *__restrict__ fv,
                                                             const float *__restrict__ fw, double dti, int first,
@@ -285,12 +440,18 @@ __global__ void __launch_bounds__(256) k_ibm_interp_force_f(Geo g, PartGeo pg, I
   const int nla = b.nla[p];
   const double *pf = b.pf;
   const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
+  extern __shared__ __align__(16) unsigned char ibox_sm[];
+  float *box = reinterpret_cast<float *>(ibox_sm);
+  __shared__ int bg[3][8], bmx[3][3];
+  const bool boxed = nla > 0 && build_boxes<float, PointStencilF>(g, b.st32, (long)p * pg.nl, nla, fu, fv, fw, box,
+                                                                  INTERP_BOX, bg, bmx);
   double sfx = 0, sfy = 0, sfz = 0, stx = 0, sty = 0, stz = 0;
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const long t = (long)p * pg.nl + l;
     const PointStencilF s = b.st32[t];
     float iu, iv, iw;
-    interp_point_f(g, s, fu, fv, fw, iu, iv, iw);
+    if (boxed) interp_box_f(s, box, bg, g, iu, iv, iw);
+    else interp_point_f(g, s, fu, fv, fw, iu, iv, iw);
     b.dudtl[t] = iu; b.dvdtl[t] = iv; b.dwdtl[t] = iw;
     if (first < 0) continue;
     double fx, fy, fz;
@@ -332,7 +493,8 @@ __global__ void __launch_bounds__(256) k_ibm_interp_force_f(Geo g, PartGeo pg, I
 void launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                                const float *fv, const float *fw, double dt, int first, const int *gate) {
   if (pg.np == 0) return;
-  k_ibm_interp_force_f<<<pg.np, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, first, gate);
+  k_ibm_interp_force_f<<<pg.np, 256, 3 * INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, first,
+                                                                           gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -384,6 +546,7 @@ __global__ void __launch_bounds__(256) k_ibm_spread_box(Geo g, PartGeo pg, IbmBu
   if (threadIdx.x < 3) { bmin[threadIdx.x] = 0x7fffffff; bmax[threadIdx.x] = -0x7fffffff; }
   __syncthreads();
   // box of the stencil origins, x/y relative to the first point (periodic)
+  int elo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, ehi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const ST &s = st[t0 + l];
     int rx = (comp == 0 ? s.ilows : s.ilow) - refx;
@@ -391,9 +554,13 @@ __global__ void __launch_bounds__(256) k_ibm_spread_box(Geo g, PartGeo pg, IbmBu
     const int rz = comp == 2 ? s.klows : s.klow;
     rx = rx >= hI ? rx - g.I : (rx < -hI ? rx + g.I : rx);
     ry = ry >= hJ ? ry - g.J : (ry < -hJ ? ry + g.J : ry);
-    atomicMin(&bmin[0], rx); atomicMax(&bmax[0], rx);
-    atomicMin(&bmin[1], ry); atomicMax(&bmax[1], ry);
-    atomicMin(&bmin[2], rz); atomicMax(&bmax[2], rz);
+    elo[0] = min(elo[0], rx); ehi[0] = max(ehi[0], rx);
+    elo[1] = min(elo[1], ry); ehi[1] = max(ehi[1], ry);
+    elo[2] = min(elo[2], rz); ehi[2] = max(ehi[2], rz);
+  }
+  for (int d = 0; d < 3; ++d) {
+    const int wl = __reduce_min_sync(0xffffffffu, elo[d]), wh = __reduce_max_sync(0xffffffffu, ehi[d]);
+    if ((threadIdx.x & 31) == 0) { atomicMin(&bmin[d], wl); atomicMax(&bmax[d], wh); }
   }
   __syncthreads();
   const int nbx = bmax[0] - bmin[0] + 3, nby = bmax[1] - bmin[1] + 3, nbz = bmax[2] - bmin[2] + 3;
@@ -468,8 +635,9 @@ void launch_ibm_spread(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffe
   (void)first;
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_box<double, PointStencil, double><<<dim3(pg.np, 3), 256, SPREAD_BOX * sizeof(double), s>>>(
-      g, pg, b, b.st, fu, fv, fw, 1. / dt, coeff0, nullptr, nullptr);
+  // FP64: per-tap atomics (a 64 KB FP64 box per block leaves too few
+  // blocks per SM for the FP64-bound arithmetic)
+  k_ibm_spread<T><<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0);
 }
 template void launch_ibm_spread<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, double *, double *,
                                         double *, double, int);
@@ -482,13 +650,6 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
       g, pg, b, b.st32, fu, fv, fw, 1. / dt, coeff0, dfin, gate);
 }
 
-int ibm_set_smem_limits() {
-  cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_box<double, PointStencil, double>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SPREAD_BOX * (int)sizeof(double));
-  cudaError_t e2 = cudaFuncSetAttribute(k_ibm_spread_box<float, PointStencilF, float>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * SPREAD_BOX * (int)sizeof(float));
-  return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
-}
 
 // ---------------------------------------------------------------------------
 // Learned forcing (mixed form).  Features of each point after the first
@@ -508,13 +669,22 @@ __global__ void __launch_bounds__(256) k_ibm_features_f(Geo g, PartGeo pg, IbmBu
                                                         double dt, const float *__restrict__ mu,
                                                         const float *__restrict__ isig,
                                                         __nv_bfloat16 *__restrict__ X, HarvestArgs H) {
-  const int n = pg.np * pg.nl;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int p = t / pg.nl, l = t - p * pg.nl;
-    if (l >= b.nla[p]) {
+  const int p = blockIdx.x;
+  const int nla = b.nla[p];
+  const long t0 = (long)p * pg.nl;
+  extern __shared__ __align__(16) unsigned char ibox_sm[];
+  float *box = reinterpret_cast<float *>(ibox_sm);
+  __shared__ int bg[3][8], bmx[3][3];
+  const bool boxed =
+      nla > 0 && build_boxes<float, PointStencilF>(g, b.st32, t0, nla, fu, fv, fw, box, INTERP_BOX, bg, bmx);
+  const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
+  const float inv_r = (float)(1. / pg.radfp);
+  for (int l = threadIdx.x; l < pg.nl; l += blockDim.x) {
+    const long t = t0 + l;
+    if (l >= nla) {
       if (X)
         for (int q = 0; q < 96; q += 2)
-          *reinterpret_cast<__nv_bfloat162 *>(&X[(long)t * 96 + q]) = __floats2bfloat162_rn(0.f, 0.f);
+          *reinterpret_cast<__nv_bfloat162 *>(&X[t * 96 + q]) = __floats2bfloat162_rn(0.f, 0.f);
       continue;
     }
     const PointStencilF s = b.st32[t];
@@ -525,29 +695,46 @@ __global__ void __launch_bounds__(256) k_ibm_features_f(Geo g, PartGeo pg, IbmBu
       jy[m] = wrapm(s.jlows + m - 1, g.J);
       jyh[m] = wrapm(s.jlow + m - 1, g.J);
     }
+    const float *B0 = box, *B1 = box, *B2 = box;
+    int y0 = 0, z0 = 0, y1 = 0, z1 = 0, y2 = 0, z2 = 0;
+    if (boxed) {
+      B0 = box + box_origin(g, s, 0, bg);
+      B1 = box + INTERP_BOX + box_origin(g, s, 1, bg);
+      B2 = box + 2 * INTERP_BOX + box_origin(g, s, 2, bg);
+      y0 = bg[0][5]; z0 = y0 * bg[0][6]; y1 = bg[1][5]; z1 = y1 * bg[1][6]; y2 = bg[2][5]; z2 = y2 * bg[2][6];
+    }
     const float Ux = (float)b.ul[t], Uy = (float)b.vl[t], Uz = (float)b.wl[t];
     float f[96];
     float au = 0.f, av = 0.f, aw = 0.f;
-    int q = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
+      for (int j = 0; j < 3; ++j) {
+        const float wyz = s.phiyh[j] * s.phizh[k];
+        const float wyz2 = s.phiy[j] * s.phizh[k];
+        const float wyz3 = s.phiyh[j] * s.phiz[k];
 #pragma unroll
-        for (int i = 0; i < 3; ++i, ++q) {
-          const float tu = __ldg(&fu[fidx(g, ix[i], jyh[j], s.klow + k)]);
-          const float tv = __ldg(&fv[fidx(g, ixh[i], jy[j], s.klow + k)]);
-          const float tw = __ldg(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)]);
-          au += tu * (s.phix[i] * (s.phiyh[j] * s.phizh[k]));
-          av += tv * (s.phixh[i] * (s.phiy[j] * s.phizh[k]));
-          aw += tw * (s.phixh[i] * (s.phiyh[j] * s.phiz[k]));
+        for (int i = 0; i < 3; ++i) {
+          const int q = (k * 3 + j) * 3 + i;
+          float tu, tv, tw;
+          if (boxed) {
+            tu = B0[i + j * y0 + k * z0];
+            tv = B1[i + j * y1 + k * z1];
+            tw = B2[i + j * y2 + k * z2];
+          } else {
+            tu = __ldg(&fu[fidx(g, ix[i], jyh[j], s.klow + k)]);
+            tv = __ldg(&fv[fidx(g, ixh[i], jy[j], s.klow + k)]);
+            tw = __ldg(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)]);
+          }
+          au += tu * (s.phix[i] * wyz);
+          av += tv * (s.phixh[i] * wyz2);
+          aw += tw * (s.phixh[i] * wyz3);
           f[9 + q] = tu - Ux;
           f[36 + q] = tv - Uy;
           f[63 + q] = tw - Uz;
         }
+      }
     b.dudtl[t] = au; b.dvdtl[t] = av; b.dwdtl[t] = aw;
-    const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
-    const float inv_r = (float)(1. / pg.radfp);
     f[0] = Ux - au; f[1] = Uy - av; f[2] = Uz - aw;
     f[3] = Ux; f[4] = Uy; f[5] = Uz;
     f[6] = (float)(b.xfp[t] - px) * inv_r; f[7] = (float)(b.yfp[t] - py) * inv_r; f[8] = (float)(b.zfp[t] - pz) * inv_r;
@@ -555,16 +742,21 @@ __global__ void __launch_bounds__(256) k_ibm_features_f(Geo g, PartGeo pg, IbmBu
     f[93] = s.phix[1]; f[94] = s.phiy[1]; f[95] = s.phiz[1];
     if (X) {
 #pragma unroll
-      for (int c = 0; c < 96; c += 2)
-        *reinterpret_cast<__nv_bfloat162 *>(&X[(long)t * 96 + c]) =
-            __floats2bfloat162_rn((f[c] - mu[c]) * isig[c], (f[c + 1] - mu[c + 1]) * isig[c + 1]);
+      for (int c = 0; c < 96; c += 8) {
+        __nv_bfloat162 v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          v[e] = __floats2bfloat162_rn((f[c + 2 * e] - mu[c + 2 * e]) * isig[c + 2 * e],
+                                       (f[c + 2 * e + 1] - mu[c + 2 * e + 1]) * isig[c + 2 * e + 1]);
+        *reinterpret_cast<uint4 *>(&X[t * 96 + c]) = *reinterpret_cast<const uint4 *>(v);
+      }
     }
     if (H.feat && (t + H.phase) % H.stride == 0) {
       const int h = atomicAdd(&H.count[0], 1);
       if (h < H.cap) {
 #pragma unroll
         for (int c = 0; c < 96; ++c) H.feat[(long)h * 96 + c] = f[c];
-        H.pidx[h] = t;
+        H.pidx[h] = (int)t;
       }
     }
   }
@@ -573,7 +765,7 @@ void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmB
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                            __nv_bfloat16 *X, const HarvestArgs &H) {
   if (pg.np == 0) return;
-  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H);
+  k_ibm_features_f<<<pg.np, 256, 3 * INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H);
 }
 
 // targets of the slots reserved since the last call: (F_final - F0) * dt, the
@@ -695,5 +887,19 @@ void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, d
   k_ibm_res_gate<<<1, 32, 0, s>>>(nb, scratch, npts, ls, gate, plain);
 }
 
+
+int ibm_set_smem_limits() {
+  const cudaError_t e1 = cudaSuccess;
+  cudaError_t e2 = cudaFuncSetAttribute(k_ibm_spread_box<float, PointStencilF, float>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * SPREAD_BOX * (int)sizeof(float));
+  const cudaError_t e3 = cudaSuccess;
+  cudaError_t e4 = cudaFuncSetAttribute(k_ibm_interp_force_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        3 * INTERP_BOX * (int)sizeof(float));
+  cudaError_t e5 = cudaFuncSetAttribute(k_ibm_features_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        3 * INTERP_BOX * (int)sizeof(float));
+  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && e5 == cudaSuccess)
+             ? 0
+             : -1;
+}
 
 }  // namespace ibmk

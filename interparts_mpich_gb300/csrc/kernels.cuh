@@ -105,6 +105,8 @@ void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16 *x, int n, const __n
                         __nv_bfloat16 *h1, __nv_bfloat16 *h2, int train);
 void launch_mlp_refresh(cudaStream_t s, const float *params, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b,
                         __nv_bfloat16 *w2tb);
+void launch_mlp_infer(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
+                      const __nv_bfloat16 *w2b, const float *params, float *y);
 void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr);
 void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb);
 void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,

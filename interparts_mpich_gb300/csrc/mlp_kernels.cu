@@ -198,6 +198,136 @@ void launch_mlp_forward(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, c
 }
 
 // ---------------------------------------------------------------------------
+// Inference: X (N x 96, bf16) -> Y (N x 3, fp32), one warp per 16-row tile.
+// The layer-1 accumulators become the A fragments of layer 2 in registers:
+// the m16n8k16 C fragment of the 8-column tiles 2m and 2m+1 holds exactly the
+// A fragment of the 16-column k-block m (rows g, g+8; columns 2t, 2t+1 and
+// 2t+8, 2t+9).  Layer 3 is a per-lane partial dot product over the 32
+// columns a lane holds, summed over the 4 lanes of a row pair by shuffles.
+// Same rounding points as the training forward: BF16 inputs, weights of
+// layers 1-2 and hidden activations; FP32 accumulation; FP32 W3.
+// ---------------------------------------------------------------------------
+constexpr int IW = 8;  // warps per CTA
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+__global__ void __launch_bounds__(IW * 32, 1) k_mlp_infer(const bf16 *__restrict__ x, int n,
+                                                          const bf16 *__restrict__ w1b, const bf16 *__restrict__ w2b,
+                                                          const float *__restrict__ params, float *__restrict__ y) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  bf16 *W1s = reinterpret_cast<bf16 *>(sm);  // [128][LDX]
+  bf16 *W2s = W1s + NH * LDX;                // [128][LDH]
+  bf16 *Xs = W2s + NH * LDH;                 // [IW][16][LDX]
+  float *cst = reinterpret_cast<float *>(Xs + IW * 16 * LDX);  // b1, b2, W3, b3
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int t = tid; t < NH * NIN / 8; t += blockDim.x) {
+    const int r = t / (NIN / 8), c8 = (t % (NIN / 8)) * 8;
+    *reinterpret_cast<uint4 *>(&W1s[r * LDX + c8]) = *reinterpret_cast<const uint4 *>(&w1b[r * NIN + c8]);
+  }
+  for (int t = tid; t < NH * NH / 8; t += blockDim.x) {
+    const int r = t / (NH / 8), c8 = (t % (NH / 8)) * 8;
+    *reinterpret_cast<uint4 *>(&W2s[r * LDH + c8]) = *reinterpret_cast<const uint4 *>(&w2b[r * NH + c8]);
+  }
+  for (int t = tid; t < NH; t += blockDim.x) { cst[t] = params[OFF_B1 + t]; cst[NH + t] = params[OFF_B2 + t]; }
+  for (int t = tid; t < NOUT * NH + NOUT; t += blockDim.x) cst[2 * NH + t] = params[OFF_W3 + t];
+  __syncthreads();
+  const float *b1 = cst, *b2 = cst + NH, *w3 = cst + 2 * NH, *b3 = w3 + NOUT * NH;
+  bf16 *Xw = Xs + warp * 16 * LDX;
+  const int g = lane >> 2, tq = lane & 3;
+  const int ntiles = (n + 15) / 16;
+  for (int tile = blockIdx.x * IW + warp; tile < ntiles; tile += gridDim.x * IW) {
+    const long row0 = (long)tile * 16;
+    // stage the warp's 16 feature rows (12 x 16 B per row)
+    for (int q = lane; q < 16 * (NIN / 8); q += 32) {
+      const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (row0 + r < n) v = __ldg(reinterpret_cast<const uint4 *>(&x[(row0 + r) * NIN + c8]));
+      *reinterpret_cast<uint4 *>(&Xw[r * LDX + c8]) = v;
+    }
+    __syncwarp();
+    float acc[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+    for (int k0 = 0; k0 < NIN; k0 += 16) {
+      uint32_t a[4];
+      load_a(a, Xw, LDX, 0, k0, lane);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        uint32_t bb[2];
+        load_b(bb, W1s, LDX, j * 8, k0, lane);
+        mma16816(acc[j], a, bb);
+      }
+    }
+    // bias + GELU, rounded to BF16 straight into the layer-2 A fragments
+    uint32_t af[8][4];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int c0 = 16 * m + 2 * tq, c1 = c0 + 8;
+      af[m][0] = pack_bf2(gelu_f(acc[2 * m][0] + b1[c0]), gelu_f(acc[2 * m][1] + b1[c0 + 1]));
+      af[m][1] = pack_bf2(gelu_f(acc[2 * m][2] + b1[c0]), gelu_f(acc[2 * m][3] + b1[c0 + 1]));
+      af[m][2] = pack_bf2(gelu_f(acc[2 * m + 1][0] + b1[c1]), gelu_f(acc[2 * m + 1][1] + b1[c1 + 1]));
+      af[m][3] = pack_bf2(gelu_f(acc[2 * m + 1][2] + b1[c1]), gelu_f(acc[2 * m + 1][3] + b1[c1 + 1]));
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        uint32_t bb[2];
+        load_b(bb, W2s, LDH, j * 8, 16 * m, lane);
+        mma16816(acc[j], af[m], bb);
+      }
+    }
+    // bias + GELU (BF16-rounded), layer 3 partial sums for rows g and g+8
+    float part[2][NOUT];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int o = 0; o < NOUT; ++o) part[h][o] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int col = j * 8 + 2 * tq;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float h0 = __bfloat162float(__float2bfloat16(gelu_f(acc[j][2 * h] + b2[col])));
+        const float h1 = __bfloat162float(__float2bfloat16(gelu_f(acc[j][2 * h + 1] + b2[col + 1])));
+#pragma unroll
+        for (int o = 0; o < NOUT; ++o) part[h][o] += h0 * w3[o * NH + col] + h1 * w3[o * NH + col + 1];
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int o = 0; o < NOUT; ++o) {
+        part[h][o] += __shfl_xor_sync(0xffffffffu, part[h][o], 1);
+        part[h][o] += __shfl_xor_sync(0xffffffffu, part[h][o], 2);
+      }
+    if (tq == 0) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const long r = row0 + g + 8 * h;
+        if (r < n)
+          for (int o = 0; o < NOUT; ++o) y[r * NOUT + o] = part[h][o] + b3[o];
+      }
+    }
+    __syncwarp();
+  }
+}
+size_t mlp_infer_smem() {
+  return (size_t)(NH * LDX + NH * LDH + IW * 16 * LDX) * sizeof(bf16) + (size_t)(2 * NH + NOUT * NH + NOUT) * sizeof(float);
+}
+void launch_mlp_infer(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, const bf16 *w2b, const float *params,
+                      float *y) {
+  if (n <= 0) return;
+  const int ntiles = (n + 15) / 16;
+  const int grid = (ntiles + IW - 1) / IW < 152 ? (ntiles + IW - 1) / IW : 152;
+  k_mlp_infer<<<grid, IW * 32, mlp_infer_smem(), s>>>(x, n, w1b, w2b, params, y);
+}
+
+// ---------------------------------------------------------------------------
 // Backward through layer 3, GELU and layer 2 for a batch: dY = 2(Y-T)/B;
 // dH2 = dY W3; dZ2 = dH2 * gelu'(Z2) (bf16); dH1 = dZ2 W2 (tensor cores);
 // dZ1 = dH1 * gelu'(Z1) (bf16).  Bias and W3 gradients accumulate into grad.
@@ -487,7 +617,8 @@ int mlp_set_smem_limits() {
                                         (int)mlp_forward_smem());
   cudaError_t e3 = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)mlp_backward_smem());
-  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
+  cudaError_t e4 = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_infer_smem());
+  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess) ? 0 : -1;
 }
 
 }  // namespace ibmk

@@ -253,6 +253,14 @@ class IBMSolver:
         self._chk(self.fn["mlp_gradient"](self.ctx, _fp(p), _fp(x), _fp(t), nb, _fp(g), C.byref(loss), _fp(y)))
         return float(loss.value), g, y
 
+    def mlp_infer(self, params, x):
+        """Outputs of the library's inference kernel (the forcing loop's) on one batch."""
+        p = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((x.shape[0], 3), np.float32)
+        self._chk(self.fn["mlp_infer"](self.ctx, _fp(p), _fp(x), x.shape[0], _fp(y)))
+        return y
+
     def mlp_fit(self, params, x, t, nsteps: int, lr: float = 1e-3):
         p = np.ascontiguousarray(params, np.float32)
         x = np.ascontiguousarray(x, np.float32)

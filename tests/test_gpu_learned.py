@@ -54,6 +54,20 @@ def test_mlp_gradient_matches_cpu_reference(gpu_lib, nb):
         assert err <= GRAD_REL_TOL, (name, err)
 
 
+@pytest.mark.parametrize("nb", [16, 1000, 20011])
+def test_mlp_inference_matches_cpu_reference(gpu_lib, nb):
+    """The fused inference kernel (register-resident hidden layer) against
+    the CPU reference and against the training forward."""
+    case = small_case(n=16, nsp=0)
+    g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    p, x, t = _batch(nb, seed=nb + 1)
+    y = g.mlp_infer(p, x)
+    ref = mlp_ref.forward(p, x)["y"]
+    assert np.linalg.norm(y - ref) <= OUT_REL_TOL * np.linalg.norm(ref)
+    _, _, y_train = g.mlp_gradient(p, x, t)
+    assert np.linalg.norm(y - y_train) <= OUT_REL_TOL * np.linalg.norm(ref)
+
+
 def test_mlp_adam_steps_match_cpu_reference(gpu_lib):
     case = small_case(n=16, nsp=0)
     g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
@@ -99,7 +113,7 @@ def trained(gpu_lib):
     case = _flow_case()
     s = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
     s.setup()
-    dt = 0.5 * OracleSolver(case).chkdt()
+    dt = 0.5 * s.chkdt()
     s.harvest(capacity=400000, stride=1, passes=3)
     s.run(dt, 8)
     s.harvest(0)
