@@ -151,6 +151,288 @@ __device__ C *fft_smem1(C *a, C *b, int M, int nseq, int ss, const FftPlan &pl, 
 }
 
 // ---------------------------------------------------------------------------
+// Register four-step FFT (FP32 path).  N = N1*N2 with N1 = N2 or 2*N2 and
+// N1 <= 16: a group of N2 threads holds a sequence, thread t the elements
+// x[t + N2*n1]; an N1-point DFT in registers, the twiddle W_N^(t*k1), one
+// exchange through a padded shared buffer (group-private, __syncwarp only),
+// then N2-point DFTs in registers (N1/N2 per thread), written back in
+// natural order.  Same DFT as the Stockham stages, other summation order.
+// ---------------------------------------------------------------------------
+// multiply by exp(-+2 pi i m/den) given cos, sin of 2 pi m/den
+template <typename C>
+__device__ __forceinline__ C cmulcs(C x, float c, float s, int inv) {
+  return inv ? cmk<C>(x.x * c - x.y * s, x.y * c + x.x * s) : cmk<C>(x.x * c + x.y * s, x.y * c - x.x * s);
+}
+// cos, sin of 2 pi m / 16, m = 0..9
+__device__ __forceinline__ void w16(int m, float &c, float &s) {
+  const float C1 = 0.92387953251128675613f, S1 = 0.38268343236508977173f, R2 = 0.70710678118654752440f;
+  const float cs[10] = {1.f, C1, R2, S1, 0.f, -S1, -R2, -C1, -1.f, -C1};
+  const float sn[10] = {0.f, S1, R2, C1, 1.f, C1, R2, S1, 0.f, -S1};
+  c = cs[m]; s = sn[m];
+}
+template <int N, typename C> __device__ __forceinline__ void dft_reg(C *v, int inv);
+template <> __device__ __forceinline__ void dft_reg<2, float2>(float2 *v, int) { dft2(v); }
+template <> __device__ __forceinline__ void dft_reg<4, float2>(float2 *v, int inv) { dft4(v, inv); }
+template <> __device__ __forceinline__ void dft_reg<8, float2>(float2 *v, int inv) {
+  // n = n2 + 2 n1, k = k1 + 4 k2
+  float2 a0[4] = {v[0], v[2], v[4], v[6]}, a1[4] = {v[1], v[3], v[5], v[7]};
+  dft4(a0, inv);
+  dft4(a1, inv);
+  float c, s;
+  w16(2, c, s); a1[1] = cmulcs(a1[1], c, s, inv);
+  a1[2] = cmi(a1[2], inv);
+  w16(6, c, s); a1[3] = cmulcs(a1[3], c, s, inv);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) { v[k1] = cadd(a0[k1], a1[k1]); v[k1 + 4] = csub(a0[k1], a1[k1]); }
+}
+template <> __device__ __forceinline__ void dft_reg<16, float2>(float2 *v, int inv) {
+  // n = n2 + 4 n1, k = k1 + 4 k2
+  float2 a[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) a[n2][n1] = v[n2 + 4 * n1];
+    dft4(a[n2], inv);
+  }
+#pragma unroll
+  for (int n2 = 1; n2 < 4; ++n2)
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1) {
+      float c, s;
+      w16(n2 * k1, c, s);
+      a[n2][k1] = cmulcs(a[n2][k1], c, s, inv);
+    }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 b[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+    dft4(b, inv);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
+  }
+}
+// one sequence in shared memory (unit stride) per group of N2 threads;
+// ex: group-private exchange buffer of N1*(N2+1) elements.  Every thread of
+// the warp must call it (it synchronises the warp).
+template <int N1, int N2>
+__device__ __forceinline__ void fft_group(float2 *row, float2 *ex, int t, const float2 *__restrict__ tw, int inv,
+                                          bool active) {
+  constexpr int N = N1 * N2;
+  float2 v[N1];
+  if (active) {
+#pragma unroll
+    for (int r = 0; r < N1; ++r) v[r] = row[t + N2 * r];
+    dft_reg<N1, float2>(v, inv);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) {
+      if (t > 0) {
+        float2 w = __ldg(&tw[(t * k1) % N]);
+        if (inv) w.y = -w.y;
+        v[k1] = cmul(v[k1], w);
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) ex[k1 * (N2 + 1) + t] = v[k1];
+  }
+  __syncwarp();
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < N1 / N2; ++q) {
+      const int k1 = t + q * N2;
+      float2 w[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) w[n2] = ex[k1 * (N2 + 1) + n2];
+      dft_reg<N2, float2>(w, inv);
+#pragma unroll
+      for (int k2 = 0; k2 < N2; ++k2) row[k1 + N1 * k2] = w[k2];
+    }
+  }
+  __syncwarp();
+}
+// (N1, N2) of the supported lengths; 0 = use the Stockham stages
+__host__ __device__ inline int reg_n2(int N) {
+  return N == 16 ? 4 : N == 32 ? 4 : N == 64 ? 8 : N == 128 ? 8 : N == 256 ? 16 : 0;
+}
+
+template <int N1, int N2, bool DF>
+__global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__restrict__ fu,
+                                                       const float *__restrict__ fv, float *__restrict__ fw,
+                                                       float2 *__restrict__ S, const float2 *__restrict__ twM,
+                                                       const float2 *__restrict__ twN, double dtidxi, double dtidyi,
+                                                       double dtidzi) {
+  constexpr int M = N1 * N2, ROWS = 128 / N2;
+  __shared__ float2 A[ROWS * M];
+  __shared__ float2 EX[ROWS * N1 * (N2 + 1)];
+  const int row0 = blockIdx.x * ROWS;
+  const int nrow = g.J * g.K;
+  const float fx_hi = (float)dtidxi, fx_lo = (float)(dtidxi - (double)fx_hi);
+  const float fy_hi = (float)dtidyi, fy_lo = (float)(dtidyi - (double)fy_hi);
+  const float fz_hi = (float)dtidzi, fz_lo = (float)(dtidzi - (double)fz_hi);
+  const float fxs = (float)dtidxi, fys = (float)dtidyi, fzs = (float)dtidzi;
+  const int PL = g.I * g.J;
+  // 1. right-hand side, packed z_m = x_{2m} + i x_{2m+1}
+  for (int q = threadIdx.x; q < ROWS * 2 * M; q += blockDim.x) {
+    const int r = q / (2 * M), i = q - r * (2 * M);
+    const int row = row0 + r;
+    float val = 0.f;
+    if (row < nrow) {
+      const int j = row % g.J, k = row / g.J + 1;
+      const long c = fidx(g, i, j, k);
+      const float wk = (k == g.K) ? 0.f : fw[c];
+      const float wkm = fw[c - PL];  // plane 0 holds w(0)=0
+      if (k == g.K) fw[c] = 0.f;
+      const float vjm = fv[c + (j == 0 ? (g.J - 1) * g.I : -g.I)];
+      const float uim = fu[c + (i == 0 ? g.I - 1 : -1)];
+      if constexpr (DF) {
+        // divergence residual in double-float arithmetic: exact differences
+        // of the FP32 velocities, products with the split FP64 factors
+        float dh, dl, th, tl, sh, sl;
+        two_sum(wk, -wkm, dh, dl);
+        df_mul(dh, dl, fz_hi, fz_lo, sh, sl);
+        two_sum(fv[c], -vjm, dh, dl);
+        df_mul(dh, dl, fy_hi, fy_lo, th, tl);
+        df_add(sh, sl, th, tl, sh, sl);
+        two_sum(fu[c], -uim, dh, dl);
+        df_mul(dh, dl, fx_hi, fx_lo, th, tl);
+        df_add(sh, sl, th, tl, sh, sl);
+        val = sh + sl;
+      } else {
+        val = (wk - wkm) * fzs + (fv[c] - vjm) * fys + (fu[c] - uim) * fxs;
+      }
+    }
+    reinterpret_cast<float *>(A + r * M)[i] = val;
+  }
+  __syncthreads();
+  const int grp = threadIdx.x / N2, t = threadIdx.x - grp * N2;
+  fft_group<N1, N2>(A + grp * M, EX + grp * N1 * (N2 + 1), t, twM, 0, true);
+  __syncthreads();
+  // 2. unpack to X_k, k = 0..M  (X_k = E_k + W_N^k O_k)
+  for (int q = threadIdx.x; q < ROWS * (M + 1); q += blockDim.x) {
+    const int r = q / (M + 1), kx = q - r * (M + 1);
+    const int row = row0 + r;
+    if (row >= nrow) continue;
+    const float2 Zk = A[r * M + (kx == M ? 0 : kx)];
+    const float2 Zc = cconj(A[r * M + (kx == 0 ? 0 : M - kx)]);
+    const float2 E = cscale(cadd(Zk, Zc), 0.5f);
+    const float2 D = csub(Zk, Zc);
+    const float2 O = cmk<float2>(D.y * 0.5f, -D.x * 0.5f);  // D/(2i)
+    S[(long)row * g.MX + kx] = cadd(E, cmul(__ldg(&twN[kx]), O));
+  }
+}
+
+// complex FFT along y; a group of N2 threads per kx-column, 256 threads
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) k_ffty_r(Geo g, float2 *__restrict__ S, const float2 *__restrict__ twJ, int inv) {
+  constexpr int J = N1 * N2, COLS = 256 / N2, LD = J + 1;
+  extern __shared__ __align__(16) unsigned char smr[];
+  float2 *A = reinterpret_cast<float2 *>(smr);  // [COLS][LD]
+  float2 *EX = A + COLS * LD;                   // [COLS][N1*(N2+1)]
+  const int kx0 = blockIdx.x * COLS;
+  float2 *plane = S + (long)blockIdx.y * J * g.MX;
+  for (int q = threadIdx.x; q < J * COLS; q += blockDim.x) {
+    const int jy = q / COLS, cx = q - jy * COLS;
+    const int kx = kx0 + cx;
+    A[cx * LD + jy] = (kx < g.MX) ? plane[(long)jy * g.MX + kx] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int grp = threadIdx.x / N2, t = threadIdx.x - grp * N2;
+  fft_group<N1, N2>(A + grp * LD, EX + grp * N1 * (N2 + 1), t, twJ, inv, kx0 + grp < g.MX);
+  __syncthreads();
+  for (int q = threadIdx.x; q < J * COLS; q += blockDim.x) {
+    const int jy = q / COLS, cx = q - jy * COLS;
+    const int kx = kx0 + cx;
+    if (kx < g.MX) plane[(long)jy * g.MX + kx] = A[cx * LD + jy];
+  }
+}
+
+// inverse real FFT along x: spectrum row -> phi(i,j,k), k = 1..K
+template <int N1, int N2>
+__global__ void __launch_bounds__(128) k_ifftx_r(Geo g, const float2 *__restrict__ S, float *__restrict__ phi,
+                                                 const float2 *__restrict__ twM, const float2 *__restrict__ twN) {
+  constexpr int M = N1 * N2, ROWS = 128 / N2;
+  __shared__ float2 A[ROWS * M];
+  __shared__ float2 EX[ROWS * N1 * (N2 + 1)];
+  const int row0 = blockIdx.x * ROWS;
+  const int nrow = g.J * g.K;
+  // pack X_k and conj(X_{M-k}) straight from the (L2-resident) spectrum
+  for (int q = threadIdx.x; q < ROWS * M; q += blockDim.x) {
+    const int r = q / M, kx = q - r * M;
+    const int row = row0 + r;
+    float2 Xk = make_float2(0.f, 0.f), Xc = Xk;
+    if (row < nrow) {
+      Xk = S[(long)row * g.MX + kx];
+      Xc = cconj(S[(long)row * g.MX + (M - kx)]);
+    }
+    const float2 E = cscale(cadd(Xk, Xc), 0.5f);
+    const float2 O = cmul(cscale(csub(Xk, Xc), 0.5f), cconj(__ldg(&twN[kx])));
+    A[r * M + kx] = cadd(E, cmk<float2>(-O.y, O.x));  // E + i O
+  }
+  __syncthreads();
+  const int grp = threadIdx.x / N2, t = threadIdx.x - grp * N2;
+  fft_group<N1, N2>(A + grp * M, EX + grp * N1 * (N2 + 1), t, twM, 1, true);
+  __syncthreads();
+  for (int q = threadIdx.x; q < ROWS * 2 * M; q += blockDim.x) {
+    const int r = q / (2 * M), i = q - r * (2 * M);
+    const int row = row0 + r;
+    if (row >= nrow) continue;
+    const int j = row % g.J, k = row / g.J + 1;
+    phi[fidx(g, i, j, k)] = reinterpret_cast<const float *>(A + r * M)[i];
+  }
+}
+
+// dispatch of the register FFT kernels for one length pair (M = I/2, J)
+template <int M1, int M2>
+bool launch_fftx_r(cudaStream_t s, const Geo &g, const float *fu, const float *fv, float *fw, float2 *S,
+                   const float2 *twM, const float2 *twN, double a, double b, double c, bool df, bool inv, float *phi) {
+  const int nrow = g.J * g.K;
+  constexpr int ROWS = 128 / M2;
+  const int grid = (nrow + ROWS - 1) / ROWS;
+  if (inv) k_ifftx_r<M1, M2><<<grid, 128, 0, s>>>(g, S, phi, twM, twN);
+  else if (df) k_fillps_fftx_r<M1, M2, true><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c);
+  else k_fillps_fftx_r<M1, M2, false><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c);
+  return true;
+}
+bool fftx_r(cudaStream_t s, const Geo &g, const float *fu, const float *fv, float *fw, float2 *S, const float2 *twM,
+            const float2 *twN, double a, double b, double c, bool df, bool inv, float *phi) {
+  switch (g.I / 2) {
+    case 16: return launch_fftx_r<4, 4>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
+    case 32: return launch_fftx_r<8, 4>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
+    case 64: return launch_fftx_r<8, 8>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
+    case 128: return launch_fftx_r<16, 8>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
+    case 256: return launch_fftx_r<16, 16>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
+    default: return false;
+  }
+}
+template <int N1, int N2>
+size_t ffty_r_smem() { return (size_t)(256 / N2) * ((N1 * N2 + 1) + N1 * (N2 + 1)) * sizeof(float2); }
+template <int N1, int N2>
+void launch_ffty_r1(cudaStream_t s, const Geo &g, float2 *S, const float2 *twJ, int inv) {
+  constexpr int COLS = 256 / N2;
+  dim3 grid((g.MX + COLS - 1) / COLS, g.K);
+  k_ffty_r<N1, N2><<<grid, 256, ffty_r_smem<N1, N2>(), s>>>(g, S, twJ, inv);
+}
+bool ffty_r(cudaStream_t s, const Geo &g, float2 *S, const float2 *twJ, int inv) {
+  switch (g.J) {
+    case 16: launch_ffty_r1<4, 4>(s, g, S, twJ, inv); return true;
+    case 32: launch_ffty_r1<8, 4>(s, g, S, twJ, inv); return true;
+    case 64: launch_ffty_r1<8, 8>(s, g, S, twJ, inv); return true;
+    case 128: launch_ffty_r1<16, 8>(s, g, S, twJ, inv); return true;
+    case 256: launch_ffty_r1<16, 16>(s, g, S, twJ, inv); return true;
+    default: return false;
+  }
+}
+int ffty_r_set_smem_limits() {
+  cudaError_t e[5] = {
+      cudaFuncSetAttribute(k_ffty_r<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ffty_r_smem<4, 4>()),
+      cudaFuncSetAttribute(k_ffty_r<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ffty_r_smem<8, 4>()),
+      cudaFuncSetAttribute(k_ffty_r<8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ffty_r_smem<8, 8>()),
+      cudaFuncSetAttribute(k_ffty_r<16, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ffty_r_smem<16, 8>()),
+      cudaFuncSetAttribute(k_ffty_r<16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ffty_r_smem<16, 16>())};
+  for (cudaError_t x : e)
+    if (x != cudaSuccess) return -1;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // fillps + forward real FFT along x.  One CTA handles ROWS rows (j,k).
 // Reads the forced predictor (fu,fv,fw) with the bounduvw(dudt) wall values
 // w(0)=w(kmax)=0 applied (and stored back into fw plane K).
@@ -258,10 +540,15 @@ __global__ void __launch_bounds__(256) k_ffty(Geo g, FftPlan ply, typename cpx<T
 
 // Thomas sweep along z for every (kx,ky) (solver.f90:94-134), with the
 // precomputed pivots zt (pivot reciprocal for k<K, denominator for k=K).
+// The recurrence always runs in FP64.  For an FP32 spectrum the forward
+// intermediate goes to an FP64 scratch column (tmp) instead of back into
+// the FP32 spectrum, and the 1/(M*J) FFT scale is applied once in FP32 at
+// the final store (the recurrence is linear), so each element costs two
+// FP32<->FP64 conversions instead of four and no FP64 scale multiply.
 template <typename T>
 __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__restrict__ S,
-                                                const double *__restrict__ zt, double a2, double scale) {
-  // the recurrence always runs in FP64 (also for an FP32 spectrum)
+                                                const double *__restrict__ zt, double a2, double scale,
+                                                double2 *__restrict__ tmp) {
   typedef typename cpx<T>::t C;
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long ncol = (long)g.MX * g.J;
@@ -272,11 +559,33 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
   const double *z = zt + (long)kyy * g.MX + kx;
   const long sstride = (long)g.J * g.MX;
   C *s = S + t;
+  constexpr bool F32 = sizeof(T) == 4;
+  const double lscale = F32 ? 1. : scale;  // FP32: scale applied at the store
+  const float fscale = (float)scale;
   // The recurrence is a dependent chain over k; loads of the next planes
   // are issued in groups of PF so that several are in flight at once.
   constexpr int PF = 8;
-  auto ld = [&](int k) -> double2 { const C v = s[k * sstride]; return make_double2((double)v.x * scale, (double)v.y * scale); };
-  auto st = [&](int k, double2 v) { C o; o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; s[k * sstride] = o; };
+  auto ld = [&](int k) -> double2 {
+    const C v = s[k * sstride];
+    return F32 ? make_double2((double)v.x, (double)v.y) : make_double2((double)v.x * lscale, (double)v.y * lscale);
+  };
+  auto st_mid = [&](int k, double2 v) {  // forward intermediate
+    if constexpr (F32) {
+      tmp[k * ncol + t] = v;
+    } else {
+      C o; o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; s[k * sstride] = o;
+    }
+  };
+  auto ld_mid = [&](int k) -> double2 {
+    if constexpr (F32) return tmp[k * ncol + t];
+    else { const C v = s[k * sstride]; return make_double2((double)v.x, (double)v.y); }
+  };
+  auto st_fin = [&](int k, double2 v) {
+    C o;
+    if constexpr (F32) { o.x = (float)v.x * fscale; o.y = (float)v.y * fscale; }
+    else { o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; }
+    s[k * sstride] = o;
+  };
   const int K = g.K;
   double2 prev = make_double2(0., 0.);
   for (int k0 = 0; k0 < K; k0 += PF) {
@@ -305,8 +614,11 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
       prev = cur;
     }
 #pragma unroll
-    for (int q = 0; q < PF; ++q)
-      if (k0 + q < K) st(k0 + q, buf[q]);
+    for (int q = 0; q < PF; ++q) {
+      const int k = k0 + q;
+      if (k < K - 1) st_mid(k, buf[q]);
+      else if (k == K - 1) st_fin(k, buf[q]);
+    }
   }
   // back substitution, d(k) = c(k)*z(k) with c(k) = dzi^2 for k < kmax
   for (int k1 = K - 2; k1 >= 0; k1 -= PF) {
@@ -316,8 +628,7 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
     for (int q = 0; q < PF; ++q) {
       const int k = k1 - q;
       if (k >= 0) {
-        const C v = s[k * sstride];
-        buf[q] = make_double2((double)v.x, (double)v.y);
+        buf[q] = ld_mid(k);
         zb[q] = z[(long)k * zstride];
       }
     }
@@ -332,7 +643,7 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
     }
 #pragma unroll
     for (int q = 0; q < PF; ++q)
-      if (k1 - q >= 0) st(k1 - q, buf[q]);
+      if (k1 - q >= 0) st_fin(k1 - q, buf[q]);
   }
 }
 
@@ -378,13 +689,31 @@ __global__ void __launch_bounds__(128) k_ifftx(Geo g, FftPlan plx, const typenam
 template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
-                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64) {
+                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64,
+                    double2 *thomas_tmp) {
   typedef typename cpx<T>::t C;
   C *S = reinterpret_cast<C *>(spec);
   const int M = g.I / 2;
   const int rows = g.I <= 256 ? 4 : 2;
   const int nrow = g.J * g.K;
   size_t smx = (size_t)2 * rows * M * sizeof(C);
+  if constexpr (sizeof(T) == 4 && sizeof(TIn) == 4) {
+    // register four-step FFTs for the supported lengths
+    if (reg_n2(M) && reg_n2(g.J)) {
+      float2 *Sf = reinterpret_cast<float2 *>(spec);
+      const float2 *tM = (const float2 *)twM, *tN = (const float2 *)twN, *tJ = (const float2 *)twJ;
+      fftx_r(s, g, (const float *)fu, (const float *)fv, (float *)fw, Sf, tM, tN, dtidxi, dtidyi, dtidzi, res64, false,
+             nullptr);
+      ffty_r(s, g, Sf, tJ, 0);
+      const long ncol = (long)g.MX * g.J;
+      const double scale = 1.0 / ((double)M * g.J);
+      k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale, thomas_tmp);
+      ffty_r(s, g, Sf, tJ, 1);
+      fftx_r(s, g, nullptr, nullptr, nullptr, Sf, tM, tN, 0., 0., 0., false, true, (float *)phi);
+      if (launches) *launches += 5;
+      return;
+    }
+  }
   if (res64 && sizeof(TIn) == 4)
     k_fillps_fftx<TIn, T, float, true><<<(nrow + rows - 1) / rows, 128, smx, s>>>(
         g, plx, fu, fv, fw, S, (const C *)twM, (const C *)twN, dtidxi, dtidyi, dtidzi, rows);
@@ -402,7 +731,7 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
   k_ffty<T><<<gy, 256, smy, s>>>(g, ply, S, (const C *)twJ, cols, 0);
   const long ncol = (long)g.MX * g.J;
   const double scale = 1.0 / ((double)M * g.J);
-  k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale);
+  k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale, thomas_tmp);
   k_ffty<T><<<gy, 256, smy, s>>>(g, ply, S, (const C *)twJ, cols, 1);
   size_t smi = (size_t)(2 * rows * M + rows * (M + 1)) * sizeof(C);
   k_ifftx<T><<<(nrow + rows - 1) / rows, 128, smi, s>>>(g, plx, S, phi, (const C *)twM, (const C *)twN, rows);
@@ -411,6 +740,7 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
 
 template <typename T>
 int poisson_set_smem_limits() {
+  if (sizeof(T) == 4 && ffty_r_set_smem_limits() != 0) return -1;
   cudaError_t e[4];
   e[0] = cudaFuncSetAttribute(k_fillps_fftx<T, T, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (sizeof(T) == 4)
@@ -428,11 +758,11 @@ int poisson_set_smem_limits() {
 template void launch_poisson<double, double>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                              const double *, const double *, double *, void *, double *,
                                              const void *, const void *, const void *, const double *, double, double,
-                                             double, int *, bool);
+                                             double, int *, bool, double2 *);
 template void launch_poisson<float, float>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                            const float *, const float *, float *, void *, float *, const void *,
                                            const void *, const void *, const double *, double, double, double, int *,
-                                           bool);
+                                           bool, double2 *);
 template int poisson_set_smem_limits<double>();
 template int poisson_set_smem_limits<float>();
 

@@ -50,6 +50,7 @@ struct ibm_ctx {
   float *ru32 = nullptr, *rv32 = nullptr, *rw32 = nullptr;
   float *fu32 = nullptr, *fv32 = nullptr, *fw32 = nullptr, *phi32 = nullptr;
   void *spec32 = nullptr, *twM32 = nullptr, *twN32 = nullptr, *twJ32 = nullptr;
+  double2 *thomas_tmp = nullptr;  // FP64 forward intermediate of the Thomas sweep (FP32 spectrum)
   double *zt = nullptr;
   void *twM = nullptr, *twN = nullptr, *twJ = nullptr;
   FftPlan plx{}, ply{};
@@ -328,6 +329,7 @@ int alloc_all(ibm_ctx *c) {
                       &c->fw32, &c->phi32})
       if ((st = dalloc(c, f, nf))) return st;
     if ((st = dalloc(c, (float2 **)&c->spec32, (size_t)g.K * g.J * g.MX))) return st;
+    if ((st = dalloc(c, &c->thomas_tmp, (size_t)g.K * g.J * g.MX))) return st;
   }
   if ((st = dalloc(c, &c->scratch, 4096))) return st;
   if ((st = dalloc(c, &c->dout, 64))) return st;
@@ -508,7 +510,8 @@ int project(ibm_ctx *c, int rkiter, double dt) {
   if (c->mixed) {
     // FP32 solve of fillps(u*), FP64 Thomas; correction into the FP64 state
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
-                                 c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl);
+                                 c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl,
+                                 false, c->thomas_tmp);
     LAUNCHED(nl);
     launch_correc_mixed(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
                         factor * g.dxi, factor * g.dyi, factor * g.dzi);
@@ -518,7 +521,8 @@ int project(ibm_ctx *c, int rkiter, double dt) {
     // into the FP64 pnew
     nl = 0;
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->u32, c->v32, c->w32, c->spec32, c->phi32, c->twM32,
-                                 c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl, true);
+                                 c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl, true,
+                                 c->thomas_tmp);
     LAUNCHED(nl);
     launch_correc_mixed(c->stream, g, c->u32, c->v32, c->w32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
                         factor * g.dxi, factor * g.dyi, factor * g.dzi);
@@ -643,7 +647,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.st32, c->u32, c->v32,
-                  c->w32, c->p32, c->plo32};
+                  c->w32, c->p32, c->plo32, c->thomas_tmp};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,

@@ -653,38 +653,77 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
 
 // ---------------------------------------------------------------------------
 // Learned forcing (mixed form).  Features of each point after the first
-// forcing pass:
-//   [0:3]   slip U - u~ after pass 0      [3:6]  rigid-body velocity U
-//   [6:9]   outward unit normal           [9:90] u, v, w at the 3x27 stencil
-//                                                taps minus U (k,j,i order)
-//   [90:93] pass-0 correction F0*dt       [93:96] centre delta weights
+// forcing pass, in the order they are produced:
+//   [3q + c], q = (k*3 + j)*3 + i = 0..26, c = u, v, w : the velocity
+//            component c at stencil tap q minus the body velocity U_c
+//   [81:84] slip U - u~ after pass 1     [84:87] rigid-body velocity U
+//   [87:90] outward unit normal          [90:93] pass-1 correction F0*dt
+//   [93:96] centre delta weights (x, y, z)
 // X receives them standardised with (mu, isig) and rounded to BF16 for the
-// network; a harvest selects every stride-th point and stores the raw FP32
-// features with the point index, for the target written after the plain
-// passes.  The interpolated velocity is stored in dudtl as eulr2lagr would.
+// network, written in 16-byte groups as they are produced (no 96-float
+// register array); a harvest stores every stride-th point's raw FP32
+// features and index, for the target written after the plain passes.  The
+// interpolated velocity goes to dudtl as eulr2lagr would.
 // ---------------------------------------------------------------------------
+struct FeatSink {
+  __nv_bfloat16 *x;  // row of the standardised features (or null)
+  float *raw;        // row of the raw features (or null)
+  const float *mu, *isig;
+  float buf[8];
+  int n;  // features produced so far
+  __device__ __forceinline__ void put(float v) {
+    buf[n & 7] = v;
+    ++n;
+    if ((n & 7) == 0) flush(n - 8);
+  }
+  __device__ __forceinline__ void flush(int c0) {
+    if (x) {
+      __nv_bfloat162 h[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        h[e] = __floats2bfloat162_rn((buf[2 * e] - mu[c0 + 2 * e]) * isig[c0 + 2 * e],
+                                     (buf[2 * e + 1] - mu[c0 + 2 * e + 1]) * isig[c0 + 2 * e + 1]);
+      *reinterpret_cast<uint4 *>(x + c0) = *reinterpret_cast<const uint4 *>(h);
+    }
+    if (raw) {
+      *reinterpret_cast<float4 *>(raw + c0) = make_float4(buf[0], buf[1], buf[2], buf[3]);
+      *reinterpret_cast<float4 *>(raw + c0 + 4) = make_float4(buf[4], buf[5], buf[6], buf[7]);
+    }
+  }
+};
 
 __global__ void __launch_bounds__(256) k_ibm_features_f(Geo g, PartGeo pg, IbmBuffers b, const float *__restrict__ fu,
                                                         const float *__restrict__ fv, const float *__restrict__ fw,
                                                         double dt, const float *__restrict__ mu,
                                                         const float *__restrict__ isig,
                                                         __nv_bfloat16 *__restrict__ X, HarvestArgs H) {
-  const int p = blockIdx.x;
-  const int nla = b.nla[p];
-  const long t0 = (long)p * pg.nl;
-  extern __shared__ __align__(16) unsigned char ibox_sm[];
-  float *box = reinterpret_cast<float *>(ibox_sm);
-  __shared__ int bg[3][8], bmx[3][3];
-  const bool boxed =
-      nla > 0 && build_boxes<float, PointStencilF>(g, b.st32, t0, nla, fu, fv, fw, box, INTERP_BOX, bg, bmx);
-  const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
-  const float inv_r = (float)(1. / pg.radfp);
-  for (int l = threadIdx.x; l < pg.nl; l += blockDim.x) {
-    const long t = t0 + l;
-    if (l >= nla) {
+  const int n = pg.np * pg.nl;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int p = t / pg.nl, l = t - p * pg.nl;
+    if (l >= b.nla[p]) {
       if (X)
-        for (int q = 0; q < 96; q += 2)
-          *reinterpret_cast<__nv_bfloat162 *>(&X[t * 96 + q]) = __floats2bfloat162_rn(0.f, 0.f);
+        for (int q = 0; q < 96; q += 8) *reinterpret_cast<uint4 *>(&X[(long)t * 96 + q]) = make_uint4(0, 0, 0, 0);
+      continue;
+    }
+    FeatSink snk;
+    snk.x = X ? X + (long)t * 96 : nullptr;
+    snk.raw = nullptr;
+    snk.mu = mu;
+    snk.isig = isig;
+    snk.n = 0;
+    int h = -1;
+    if (H.feat && (t + H.phase) % H.stride == 0) {
+      h = atomicAdd(&H.count[0], 1);
+      if (h < H.cap) {
+        snk.raw = H.feat + (long)h * 96;
+        H.pidx[h] = t;
+      }
+    }
+    if (!snk.x && !snk.raw) {
+      // nothing to write for this point: interpolation only
+      float iu, iv, iw;
+      interp_point_f(g, b.st32[t], fu, fv, fw, iu, iv, iw);
+      b.dudtl[t] = iu; b.dvdtl[t] = iv; b.dwdtl[t] = iw;
       continue;
     }
     const PointStencilF s = b.st32[t];
@@ -695,16 +734,7 @@ __global__ void __launch_bounds__(256) k_ibm_features_f(Geo g, PartGeo pg, IbmBu
       jy[m] = wrapm(s.jlows + m - 1, g.J);
       jyh[m] = wrapm(s.jlow + m - 1, g.J);
     }
-    const float *B0 = box, *B1 = box, *B2 = box;
-    int y0 = 0, z0 = 0, y1 = 0, z1 = 0, y2 = 0, z2 = 0;
-    if (boxed) {
-      B0 = box + box_origin(g, s, 0, bg);
-      B1 = box + INTERP_BOX + box_origin(g, s, 1, bg);
-      B2 = box + 2 * INTERP_BOX + box_origin(g, s, 2, bg);
-      y0 = bg[0][5]; z0 = y0 * bg[0][6]; y1 = bg[1][5]; z1 = y1 * bg[1][6]; y2 = bg[2][5]; z2 = y2 * bg[2][6];
-    }
     const float Ux = (float)b.ul[t], Uy = (float)b.vl[t], Uz = (float)b.wl[t];
-    float f[96];
     float au = 0.f, av = 0.f, aw = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -715,57 +745,34 @@ __global__ void __launch_bounds__(256) k_ibm_features_f(Geo g, PartGeo pg, IbmBu
         const float wyz3 = s.phiyh[j] * s.phiz[k];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const int q = (k * 3 + j) * 3 + i;
-          float tu, tv, tw;
-          if (boxed) {
-            tu = B0[i + j * y0 + k * z0];
-            tv = B1[i + j * y1 + k * z1];
-            tw = B2[i + j * y2 + k * z2];
-          } else {
-            tu = __ldg(&fu[fidx(g, ix[i], jyh[j], s.klow + k)]);
-            tv = __ldg(&fv[fidx(g, ixh[i], jy[j], s.klow + k)]);
-            tw = __ldg(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)]);
-          }
+          const float tu = __ldg(&fu[fidx(g, ix[i], jyh[j], s.klow + k)]);
+          const float tv = __ldg(&fv[fidx(g, ixh[i], jy[j], s.klow + k)]);
+          const float tw = __ldg(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)]);
           au += tu * (s.phix[i] * wyz);
           av += tv * (s.phixh[i] * wyz2);
           aw += tw * (s.phixh[i] * wyz3);
-          f[9 + q] = tu - Ux;
-          f[36 + q] = tv - Uy;
-          f[63 + q] = tw - Uz;
+          snk.put(tu - Ux);
+          snk.put(tv - Uy);
+          snk.put(tw - Uz);
         }
       }
     b.dudtl[t] = au; b.dvdtl[t] = av; b.dwdtl[t] = aw;
-    f[0] = Ux - au; f[1] = Uy - av; f[2] = Uz - aw;
-    f[3] = Ux; f[4] = Uy; f[5] = Uz;
-    f[6] = (float)(b.xfp[t] - px) * inv_r; f[7] = (float)(b.yfp[t] - py) * inv_r; f[8] = (float)(b.zfp[t] - pz) * inv_r;
-    f[90] = (float)(b.fxl[t] * dt); f[91] = (float)(b.fyl[t] * dt); f[92] = (float)(b.fzl[t] * dt);
-    f[93] = s.phix[1]; f[94] = s.phiy[1]; f[95] = s.phiz[1];
-    if (X) {
-#pragma unroll
-      for (int c = 0; c < 96; c += 8) {
-        __nv_bfloat162 v[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          v[e] = __floats2bfloat162_rn((f[c + 2 * e] - mu[c + 2 * e]) * isig[c + 2 * e],
-                                       (f[c + 2 * e + 1] - mu[c + 2 * e + 1]) * isig[c + 2 * e + 1]);
-        *reinterpret_cast<uint4 *>(&X[t * 96 + c]) = *reinterpret_cast<const uint4 *>(v);
-      }
-    }
-    if (H.feat && (t + H.phase) % H.stride == 0) {
-      const int h = atomicAdd(&H.count[0], 1);
-      if (h < H.cap) {
-#pragma unroll
-        for (int c = 0; c < 96; ++c) H.feat[(long)h * 96 + c] = f[c];
-        H.pidx[h] = (int)t;
-      }
-    }
+    const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
+    const float inv_r = (float)(1. / pg.radfp);
+    snk.put(Ux - au); snk.put(Uy - av); snk.put(Uz - aw);
+    snk.put(Ux); snk.put(Uy); snk.put(Uz);
+    snk.put((float)(b.xfp[t] - px) * inv_r);
+    snk.put((float)(b.yfp[t] - py) * inv_r);
+    snk.put((float)(b.zfp[t] - pz) * inv_r);
+    snk.put((float)(b.fxl[t] * dt)); snk.put((float)(b.fyl[t] * dt)); snk.put((float)(b.fzl[t] * dt));
+    snk.put(s.phix[1]); snk.put(s.phiy[1]); snk.put(s.phiz[1]);
   }
 }
 void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                            __nv_bfloat16 *X, const HarvestArgs &H) {
   if (pg.np == 0) return;
-  k_ibm_features_f<<<pg.np, 256, 3 * INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H);
+  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H);
 }
 
 // targets of the slots reserved since the last call: (F_final - F0) * dt, the
@@ -895,8 +902,7 @@ int ibm_set_smem_limits() {
   const cudaError_t e3 = cudaSuccess;
   cudaError_t e4 = cudaFuncSetAttribute(k_ibm_interp_force_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         3 * INTERP_BOX * (int)sizeof(float));
-  cudaError_t e5 = cudaFuncSetAttribute(k_ibm_features_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        3 * INTERP_BOX * (int)sizeof(float));
+  const cudaError_t e5 = cudaSuccess;
   return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && e5 == cudaSuccess)
              ? 0
              : -1;

@@ -41,7 +41,8 @@ void launch_f2d(cudaStream_t s, long n, const float *a, double *b);
 template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
-                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64 = false);
+                    const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64 = false,
+                    double2 *thomas_tmp = nullptr);  // FP32 spectrum: FP64 scratch of (I/2+1)*J*K
 template <typename T> int poisson_set_smem_limits();
 
 // ibm_kernels.cu
