@@ -260,8 +260,11 @@ __global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__res
                                                        const float2 *__restrict__ twN, double dtidxi, double dtidyi,
                                                        double dtidzi) {
   constexpr int M = N1 * N2, ROWS = 128 / N2;
-  __shared__ float2 A[ROWS * M];
-  __shared__ float2 EX[ROWS * N1 * (N2 + 1)];
+  // group strides padded by 8 elements (64 B): groups sharing a warp start
+  // half a bank row apart
+  constexpr int RS = M + 8, ES = N1 * (N2 + 1) + 8;
+  __shared__ __align__(16) float2 A[ROWS * RS];
+  __shared__ float2 EX[ROWS * ES];
   const int row0 = blockIdx.x * ROWS;
   const int nrow = g.J * g.K;
   const float fx_hi = (float)dtidxi, fx_lo = (float)(dtidxi - (double)fx_hi);
@@ -269,49 +272,60 @@ __global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__res
   const float fz_hi = (float)dtidzi, fz_lo = (float)(dtidzi - (double)fz_hi);
   const float fxs = (float)dtidxi, fys = (float)dtidyi, fzs = (float)dtidzi;
   const int PL = g.I * g.J;
-  // 1. right-hand side, packed z_m = x_{2m} + i x_{2m+1}
-  for (int q = threadIdx.x; q < ROWS * 2 * M; q += blockDim.x) {
-    const int r = q / (2 * M), i = q - r * (2 * M);
+  // 1. right-hand side, packed z_m = x_{2m} + i x_{2m+1}; four consecutive
+  // i per thread with 128-bit loads (I % 4 == 0 on this path)
+  constexpr int Q = 2 * M / 4;  // float4 per row
+#pragma unroll 4
+  for (int q = threadIdx.x; q < ROWS * Q; q += blockDim.x) {
+    const int r = q / Q, i0 = (q - r * Q) * 4;
     const int row = row0 + r;
-    float val = 0.f;
+    float val[4] = {0.f, 0.f, 0.f, 0.f};
     if (row < nrow) {
       const int j = row % g.J, k = row / g.J + 1;
-      const long c = fidx(g, i, j, k);
-      const float wk = (k == g.K) ? 0.f : fw[c];
-      const float wkm = fw[c - PL];  // plane 0 holds w(0)=0
-      if (k == g.K) fw[c] = 0.f;
-      const float vjm = fv[c + (j == 0 ? (g.J - 1) * g.I : -g.I)];
-      const float uim = fu[c + (i == 0 ? g.I - 1 : -1)];
-      if constexpr (DF) {
-        // divergence residual in double-float arithmetic: exact differences
-        // of the FP32 velocities, products with the split FP64 factors
-        float dh, dl, th, tl, sh, sl;
-        two_sum(wk, -wkm, dh, dl);
-        df_mul(dh, dl, fz_hi, fz_lo, sh, sl);
-        two_sum(fv[c], -vjm, dh, dl);
-        df_mul(dh, dl, fy_hi, fy_lo, th, tl);
-        df_add(sh, sl, th, tl, sh, sl);
-        two_sum(fu[c], -uim, dh, dl);
-        df_mul(dh, dl, fx_hi, fx_lo, th, tl);
-        df_add(sh, sl, th, tl, sh, sl);
-        val = sh + sl;
-      } else {
-        val = (wk - wkm) * fzs + (fv[c] - vjm) * fys + (fu[c] - uim) * fxs;
+      const long c = fidx(g, i0, j, k);
+      const float4 w4 = (k == g.K) ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(fw + c);
+      const float4 wm4 = *reinterpret_cast<const float4 *>(fw + c - PL);  // plane 0 holds w(0)=0
+      if (k == g.K) *reinterpret_cast<float4 *>(fw + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 v4 = *reinterpret_cast<const float4 *>(fv + c);
+      const float4 vm4 = *reinterpret_cast<const float4 *>(fv + c + (j == 0 ? (g.J - 1) * g.I : -g.I));
+      const float4 u4 = *reinterpret_cast<const float4 *>(fu + c);
+      const float um1 = fu[c + (i0 == 0 ? g.I - 1 : -1)];
+      const float wk[4] = {w4.x, w4.y, w4.z, w4.w}, wkm[4] = {wm4.x, wm4.y, wm4.z, wm4.w};
+      const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, vjm[4] = {vm4.x, vm4.y, vm4.z, vm4.w};
+      const float uu[4] = {u4.x, u4.y, u4.z, u4.w}, uim[4] = {um1, u4.x, u4.y, u4.z};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if constexpr (DF) {
+          // divergence residual in double-float arithmetic: exact differences
+          // of the FP32 velocities, products with the split FP64 factors
+          float dh, dl, th, tl, sh, sl;
+          two_sum(wk[e], -wkm[e], dh, dl);
+          df_mul(dh, dl, fz_hi, fz_lo, sh, sl);
+          two_sum(vv[e], -vjm[e], dh, dl);
+          df_mul(dh, dl, fy_hi, fy_lo, th, tl);
+          df_add(sh, sl, th, tl, sh, sl);
+          two_sum(uu[e], -uim[e], dh, dl);
+          df_mul(dh, dl, fx_hi, fx_lo, th, tl);
+          df_add(sh, sl, th, tl, sh, sl);
+          val[e] = sh + sl;
+        } else {
+          val[e] = (wk[e] - wkm[e]) * fzs + (vv[e] - vjm[e]) * fys + (uu[e] - uim[e]) * fxs;
+        }
       }
     }
-    reinterpret_cast<float *>(A + r * M)[i] = val;
+    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(A + r * RS) + i0) = make_float4(val[0], val[1], val[2], val[3]);
   }
   __syncthreads();
   const int grp = threadIdx.x / N2, t = threadIdx.x - grp * N2;
-  fft_group<N1, N2>(A + grp * M, EX + grp * N1 * (N2 + 1), t, twM, 0, true);
+  fft_group<N1, N2>(A + grp * RS, EX + grp * ES, t, twM, 0, true);
   __syncthreads();
   // 2. unpack to X_k, k = 0..M  (X_k = E_k + W_N^k O_k)
   for (int q = threadIdx.x; q < ROWS * (M + 1); q += blockDim.x) {
     const int r = q / (M + 1), kx = q - r * (M + 1);
     const int row = row0 + r;
     if (row >= nrow) continue;
-    const float2 Zk = A[r * M + (kx == M ? 0 : kx)];
-    const float2 Zc = cconj(A[r * M + (kx == 0 ? 0 : M - kx)]);
+    const float2 Zk = A[r * RS + (kx == M ? 0 : kx)];
+    const float2 Zc = cconj(A[r * RS + (kx == 0 ? 0 : M - kx)]);
     const float2 E = cscale(cadd(Zk, Zc), 0.5f);
     const float2 D = csub(Zk, Zc);
     const float2 O = cmk<float2>(D.y * 0.5f, -D.x * 0.5f);  // D/(2i)
@@ -349,8 +363,9 @@ template <int N1, int N2>
 __global__ void __launch_bounds__(128) k_ifftx_r(Geo g, const float2 *__restrict__ S, float *__restrict__ phi,
                                                  const float2 *__restrict__ twM, const float2 *__restrict__ twN) {
   constexpr int M = N1 * N2, ROWS = 128 / N2;
-  __shared__ float2 A[ROWS * M];
-  __shared__ float2 EX[ROWS * N1 * (N2 + 1)];
+  constexpr int RS = M + 8, ES = N1 * (N2 + 1) + 8;  // padded group strides
+  __shared__ __align__(16) float2 A[ROWS * RS];
+  __shared__ float2 EX[ROWS * ES];
   const int row0 = blockIdx.x * ROWS;
   const int nrow = g.J * g.K;
   // pack X_k and conj(X_{M-k}) straight from the (L2-resident) spectrum
@@ -364,18 +379,20 @@ __global__ void __launch_bounds__(128) k_ifftx_r(Geo g, const float2 *__restrict
     }
     const float2 E = cscale(cadd(Xk, Xc), 0.5f);
     const float2 O = cmul(cscale(csub(Xk, Xc), 0.5f), cconj(__ldg(&twN[kx])));
-    A[r * M + kx] = cadd(E, cmk<float2>(-O.y, O.x));  // E + i O
+    A[r * RS + kx] = cadd(E, cmk<float2>(-O.y, O.x));  // E + i O
   }
   __syncthreads();
   const int grp = threadIdx.x / N2, t = threadIdx.x - grp * N2;
-  fft_group<N1, N2>(A + grp * M, EX + grp * N1 * (N2 + 1), t, twM, 1, true);
+  fft_group<N1, N2>(A + grp * RS, EX + grp * ES, t, twM, 1, true);
   __syncthreads();
-  for (int q = threadIdx.x; q < ROWS * 2 * M; q += blockDim.x) {
-    const int r = q / (2 * M), i = q - r * (2 * M);
+  constexpr int Q = 2 * M / 4;
+  for (int q = threadIdx.x; q < ROWS * Q; q += blockDim.x) {
+    const int r = q / Q, i0 = (q - r * Q) * 4;
     const int row = row0 + r;
     if (row >= nrow) continue;
     const int j = row % g.J, k = row / g.J + 1;
-    phi[fidx(g, i, j, k)] = reinterpret_cast<const float *>(A + r * M)[i];
+    *reinterpret_cast<float4 *>(phi + fidx(g, i0, j, k)) =
+        *reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(A + r * RS) + i0);
   }
 }
 

@@ -342,6 +342,7 @@ int alloc_all(ibm_ctx *c) {
       if ((st = dalloc(c, f, npl))) return st;
     if (c->mixed) {
       if ((st = dalloc(c, &c->ib.st32, npl))) return st;
+      if ((st = dalloc(c, &c->ib.psum, (size_t)9 * np))) return st;
     } else {
       if ((st = dalloc(c, &c->ib.st, npl))) return st;
     }
@@ -429,7 +430,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   const Geo &g = c->g;
   const long npts = (long)c->pg.np * c->pg.nl;
   launch_ibm_stencil_f(c->stream, g, c->pg, c->ib);
-  launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 1);
+  c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 1);
   launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
   launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt);
   LAUNCHED(4);
@@ -439,11 +440,11 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   launch_mlp_infer(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly);
   launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
   launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf);
-  launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
+  c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
   launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 0);
   LAUNCHED(7);
   for (int it = 1; it < nl_iter; ++it) {
-    launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 0, c->gate);
+    c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 0, c->gate);
     launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate);
     LAUNCHED(2);
   }
@@ -460,7 +461,7 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     launch_ibm_stencil_f(c->stream, g, c->pg, c->ib);
     LAUNCHED(1);
     for (int it = 0; it < npass; ++it) {
-      launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, it == 0 ? 1 : 0);
+      c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, it == 0 ? 1 : 0);
       LAUNCHED(1);
       if (it == 0) {
         launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
@@ -476,7 +477,7 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
       }
       if (c->harvesting && it == nl_iter - 1) {
         // the plain method's residual at its own number of passes
-        launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
+        c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
         launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 1);
         LAUNCHED(3);
       }
@@ -647,7 +648,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.st32, c->u32, c->v32,
-                  c->w32, c->p32, c->plo32, c->thomas_tmp};
+                  c->w32, c->p32, c->plo32, c->thomas_tmp, c->ib.psum};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
@@ -1029,7 +1030,8 @@ int ibm_slip_residual(ibm_ctx *c, double *maxres, double *rmsres) {
   if (!c) return IBM_E_INVALID;
   if (c->pg.np == 0) { if (maxres) *maxres = 0; if (rmsres) *rmsres = 0; return IBM_OK; }
   // re-interpolate the forced field (valid between ibm_forcing_loop and ibm_project)
-  if (c->mixed) launch_ibm_interp_force_f(c->stream, c->g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, 1., -1);
+  if (c->mixed) c->launches += -1 + launch_ibm_interp_force_f(c->stream, c->g, c->pg, c->ib, c->fu32, c->fv32, c->fw32,
+                                                             1., -1);
   else launch_ibm_interp_force<double>(c->stream, c->g, c->pg, c->ib, c->fu, c->fv, c->fw, 1., -1);
   LAUNCHED(1);
   launch_slip_residual(c->stream, c->pg, c->ib, c->dout + 16);

@@ -410,91 +410,152 @@ __device__ __forceinline__ void interp_point_f(const Geo &g, const PointStencilF
   ou = au; ov = av; ow = aw;
 }
 
-// interp_point_f from the particle's shared-memory boxes (same terms, same order)
-__device__ __forceinline__ void interp_box_f(const PointStencilF &s, const float *box, const int (*bg)[8],
-                                             const Geo &g, float &ou, float &ov, float &ow) {
-  const float *B0 = box + box_origin(g, s, 0, bg), *B1 = box + INTERP_BOX + box_origin(g, s, 1, bg),
-              *B2 = box + 2 * INTERP_BOX + box_origin(g, s, 2, bg);
-  const int y0 = bg[0][5], z0 = y0 * bg[0][6], y1 = bg[1][5], z1 = y1 * bg[1][6], y2 = bg[2][5], z2 = y2 * bg[2][6];
-  float au = 0.f, av = 0.f, aw = 0.f;
-  for (int k = 0; k < 3; ++k)
-    for (int j = 0; j < 3; ++j) {
-      const float wyz = s.phiyh[j] * s.phizh[k];
-      const float wyz2 = s.phiy[j] * s.phizh[k];
-      const float wyz3 = s.phiyh[j] * s.phiz[k];
-      for (int i = 0; i < 3; ++i) {
-        au += B0[i + j * y0 + k * z0] * (s.phix[i] * wyz);
-        av += B1[i + j * y1 + k * z1] * (s.phixh[i] * wyz2);
-        aw += B2[i + j * y2 + k * z2] * (s.phixh[i] * wyz3);
-      }
-    }
-  ou = au; ov = av; ow = aw;
+// eulr2lagr + complagrforces/updtlagrforces, mixed form.  Block (particle,
+// component): the component's field box in shared memory (32 KB), the 27-tap
+// interpolation of that component for every point (FP32, the same terms in
+// the same order as interp_point_f), the FP64 point-force update of that
+// component and its partial sums: sum F_c and the two lever-arm moments of
+// F_c that enter the torque.  k_ibm_force_sums combines the three components.
+__device__ bool build_box1(const Geo &g, const PointStencilF *__restrict__ st, long t0, int nla, int c,
+                           const float *__restrict__ F, float *box, int cap, int *bg, int *bmx) {
+  if (threadIdx.x == 0) {
+    int bx, by, bz;
+    comp_origin(st[t0], c, bx, by, bz);
+    bg[0] = bx; bg[1] = by;
+    bg[2] = bg[3] = bg[4] = 0x7fffffff;
+    bmx[0] = bmx[1] = bmx[2] = -0x7fffffff;
+  }
+  __syncthreads();
+  int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    int bx, by, bz;
+    comp_origin(st[t0 + l], c, bx, by, bz);
+    const int r[3] = {relwrap(bx - bg[0], g.I), relwrap(by - bg[1], g.J), bz};
+    for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], r[d]); hi[d] = max(hi[d], r[d]); }
+  }
+  for (int d = 0; d < 3; ++d) {
+    const int wl = __reduce_min_sync(0xffffffffu, lo[d]), wh = __reduce_max_sync(0xffffffffu, hi[d]);
+    if ((threadIdx.x & 31) == 0) { atomicMin(&bg[2 + d], wl); atomicMax(&bmx[d], wh); }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bg[5] = bmx[0] - bg[2] + 3;
+    bg[6] = bmx[1] - bg[3] + 3;
+    bg[7] = bmx[2] - bg[4] + 3;
+  }
+  __syncthreads();
+  const bool ok = (long)bg[5] * bg[6] * bg[7] <= cap && bg[5] < g.I / 2 && bg[6] < g.J / 2;
+  if (!ok) return false;
+  const int nbx = bg[5], nby = bg[6], nxy = nbx * nby, nbox = nxy * bg[7];
+  const int x0 = bg[0] + bg[2] - 1, y0 = bg[1] + bg[3] - 1, z0 = bg[4];
+  for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
+    const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
+    box[q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
+  }
+  __syncthreads();
+  return true;
 }
 
-__global__ void __launch_bounds__(256) k_ibm_interp_force_f(Geo g, PartGeo pg, IbmBuffers b,
-                                                            const float *__restrict__ fu, const float *__restrict__ fv,
-                                                            const float *__restrict__ fw, double dti, int first,
-                                                            const int *__restrict__ gate) {
+__global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
+                                                           const float *__restrict__ fu, const float *__restrict__ fv,
+                                                           const float *__restrict__ fw, double dti, int first,
+                                                           const int *__restrict__ gate) {
   if (gate && *gate == 0) return;  // learned form: plain pass not needed
-  const int p = blockIdx.x;
+  const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
-  const double *pf = b.pf;
-  const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
+  const long t0 = (long)p * pg.nl;
+  const float *F = c == 0 ? fu : (c == 1 ? fv : fw);
   extern __shared__ __align__(16) unsigned char ibox_sm[];
   float *box = reinterpret_cast<float *>(ibox_sm);
-  __shared__ int bg[3][8], bmx[3][3];
-  const bool boxed = nla > 0 && build_boxes<float, PointStencilF>(g, b.st32, (long)p * pg.nl, nla, fu, fv, fw, box,
-                                                                  INTERP_BOX, bg, bmx);
-  double sfx = 0, sfy = 0, sfz = 0, stx = 0, sty = 0, stz = 0;
+  __shared__ int bg[8], bmx[3];
+  const bool boxed = nla > 0 && build_box1(g, b.st32, t0, nla, c, F, box, INTERP_BOX, bg, bmx);
+  double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
+  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
+  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
+  const double *pf = b.pf;
+  const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
+  double sF = 0., sa = 0., sb = 0.;
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
-    const long t = (long)p * pg.nl + l;
+    const long t = t0 + l;
     const PointStencilF s = b.st32[t];
-    float iu, iv, iw;
-    if (boxed) interp_box_f(s, box, bg, g, iu, iv, iw);
-    else interp_point_f(g, s, fu, fv, fw, iu, iv, iw);
-    b.dudtl[t] = iu; b.dvdtl[t] = iv; b.dwdtl[t] = iw;
-    if (first < 0) continue;
-    double fx, fy, fz;
-    if (first) {
-      fx = (b.ul[t] - iu) * dti; fy = (b.vl[t] - iv) * dti; fz = (b.wl[t] - iw) * dti;
+    float wx[3], wy[3], wz[3];
+    if (c == 0) { for (int m = 0; m < 3; ++m) { wx[m] = s.phix[m]; wy[m] = s.phiyh[m]; wz[m] = s.phizh[m]; } }
+    else if (c == 1) { for (int m = 0; m < 3; ++m) { wx[m] = s.phixh[m]; wy[m] = s.phiy[m]; wz[m] = s.phizh[m]; } }
+    else { for (int m = 0; m < 3; ++m) { wx[m] = s.phixh[m]; wy[m] = s.phiyh[m]; wz[m] = s.phiz[m]; } }
+    float acc = 0.f;
+    if (boxed) {
+      int bx, by, bz;
+      comp_origin(s, c, bx, by, bz);
+      const float *B = box + ((bz - bg[4]) * bg[6] + relwrap(by - bg[1], g.J) - bg[3]) * bg[5] +
+                       (relwrap(bx - bg[0], g.I) - bg[2]);
+      const int ys = bg[5], zs = bg[5] * bg[6];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float wyz = wy[j] * wz[k];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) acc += B[i + j * ys + k * zs] * (wx[i] * wyz);
+        }
     } else {
-      fx = b.fxl[t] + (b.ul[t] - iu) * dti; fy = b.fyl[t] + (b.vl[t] - iv) * dti; fz = b.fzl[t] + (b.wl[t] - iw) * dti;
+      int bx, by, bz;
+      comp_origin(s, c, bx, by, bz);
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) {
+          const float wyz = wy[j] * wz[k];
+          const int y = wrapm(by + j - 1, g.J);
+          for (int i = 0; i < 3; ++i) acc += __ldg(&F[fidx(g, wrapm(bx + i - 1, g.I), y, bz + k)]) * (wx[i] * wyz);
+        }
     }
-    b.fxl[t] = fx; b.fyl[t] = fy; b.fzl[t] = fz;
-    const double rx = b.xfp[t] - px, ry = b.yfp[t] - py, rz = b.zfp[t] - pz;
-    sfx += fx; sfy += fy; sfz += fz;
-    stx = stx + ry * fz - rz * fy;
-    sty = sty + rz * fx - rx * fz;
-    stz = stz + rx * fy - ry * fx;
+    dud[t] = acc;
+    if (first < 0) continue;  // interpolation only (slip residual)
+    const double f = first ? (U[t] - acc) * dti : Fl[t] + (U[t] - acc) * dti;
+    Fl[t] = f;
+    // lever arms of the torque terms of this component:
+    // c=0: (rz, ry), c=1: (rz, rx), c=2: (ry, rx)
+    const double la = c == 2 ? b.yfp[t] - py : b.zfp[t] - pz;
+    const double lb = c == 0 ? b.yfp[t] - py : b.xfp[t] - px;
+    sF += f;
+    sa += la * f;
+    sb += lb * f;
   }
-  __shared__ double red[6][256];
-  red[0][threadIdx.x] = sfx; red[1][threadIdx.x] = sfy; red[2][threadIdx.x] = sfz;
-  red[3][threadIdx.x] = stx; red[4][threadIdx.x] = sty; red[5][threadIdx.x] = stz;
+  if (first < 0) return;
+  __shared__ double red[3][256];
+  red[0][threadIdx.x] = sF; red[1][threadIdx.x] = sa; red[2][threadIdx.x] = sb;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o)
-      for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0 && first >= 0) {
-    double *pw = b.pf;
-    const double dV = pg.dVlagr;
-    const double tx = red[3][0] * dV, ty = red[4][0] * dV, tz = red[5][0] * dV;
-    pw[PF_FXLTOT * pg.np + p] = red[0][0] * dV;
-    pw[PF_FYLTOT * pg.np + p] = red[1][0] * dV;
-    pw[PF_FZLTOT * pg.np + p] = red[2][0] * dV;
-    pw[PF_TQX * pg.np + p] = tx;
-    pw[PF_TQY * pg.np + p] = ty;
-    pw[PF_TQZ * pg.np + p] = tz;
-    const double phi = pw[PF_PHI * pg.np + p];
-    pw[PF_TQTHETA * pg.np + p] = (ty * cos(phi)) - (tx * sin(phi));
-  }
+  if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = red[threadIdx.x][0];
 }
-void launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
-                               const float *fv, const float *fw, double dt, int first, const int *gate) {
-  if (pg.np == 0) return;
-  k_ibm_interp_force_f<<<pg.np, 256, 3 * INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, first,
-                                                                           gate);
+// per-particle force and torque of updtlagrforces from the component sums
+__global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict__ gate) {
+  if (gate && *gate == 0) return;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= pg.np) return;
+  const double *s = b.psum + (long)p * 9;
+  const double dV = pg.dVlagr;
+  double *pw = b.pf;
+  const double tx = (s[7] - s[4]) * dV, ty = (s[1] - s[8]) * dV, tz = (s[5] - s[2]) * dV;
+  pw[PF_FXLTOT * pg.np + p] = s[0] * dV;
+  pw[PF_FYLTOT * pg.np + p] = s[3] * dV;
+  pw[PF_FZLTOT * pg.np + p] = s[6] * dV;
+  pw[PF_TQX * pg.np + p] = tx;
+  pw[PF_TQY * pg.np + p] = ty;
+  pw[PF_TQZ * pg.np + p] = tz;
+  const double phi = pw[PF_PHI * pg.np + p];
+  pw[PF_TQTHETA * pg.np + p] = (ty * cos(phi)) - (tx * sin(phi));
+}
+int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                              const float *fv, const float *fw, double dt, int first, const int *gate) {
+  if (pg.np == 0) return 0;
+  k_ibm_interp_comp_f<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, first,
+                                                                              gate);
+  if (first < 0) return 1;
+  k_ibm_force_sums<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, gate);
+  return 2;
 }
 
 // ---------------------------------------------------------------------------
@@ -526,7 +587,7 @@ __device__ __forceinline__ void box_add(T *hi, T *lo, int c, T v) {
 }
 
 template <typename T, typename ST, typename W>
-__global__ void __launch_bounds__(256) k_ibm_spread_box(Geo g, PartGeo pg, IbmBuffers b, const ST *__restrict__ st,
+__global__ void __launch_bounds__(384) k_ibm_spread_box(Geo g, PartGeo pg, IbmBuffers b, const ST *__restrict__ st,
                                                         T *__restrict__ fu, T *__restrict__ fv, T *__restrict__ fw,
                                                         double dti, double coeff0, const float *__restrict__ dfin,
                                                         const int *__restrict__ gate) {
@@ -646,7 +707,7 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
                          float *fw, double dt, const float *dfin, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_box<float, PointStencilF, float><<<dim3(pg.np, 3), 256, 2 * SPREAD_BOX * sizeof(float), s>>>(
+  k_ibm_spread_box<float, PointStencilF, float><<<dim3(pg.np, 3), 384, 2 * SPREAD_BOX * sizeof(float), s>>>(
       g, pg, b, b.st32, fu, fv, fw, 1. / dt, coeff0, dfin, gate);
 }
 
@@ -900,8 +961,8 @@ int ibm_set_smem_limits() {
   cudaError_t e2 = cudaFuncSetAttribute(k_ibm_spread_box<float, PointStencilF, float>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * SPREAD_BOX * (int)sizeof(float));
   const cudaError_t e3 = cudaSuccess;
-  cudaError_t e4 = cudaFuncSetAttribute(k_ibm_interp_force_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        3 * INTERP_BOX * (int)sizeof(float));
+  cudaError_t e4 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        INTERP_BOX * (int)sizeof(float));
   const cudaError_t e5 = cudaSuccess;
   return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && e5 == cudaSuccess)
              ? 0

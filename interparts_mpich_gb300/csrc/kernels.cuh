@@ -55,6 +55,7 @@ struct IbmBuffers {
   double *pf;        // particle scalar fields [PF_N*np]
   double *diag;      // [8] force totals etc.
   int *err;          // shared with PartBuffers::err ([2]: point outside the grid)
+  double *psum;      // [np*9] mixed form: per-component force and lever-arm sums
 };
 template <typename T>
 void launch_ibm_stencil(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b);
@@ -70,8 +71,8 @@ void launch_slip_residual(cudaStream_t s, const PartGeo &pg, IbmBuffers b, doubl
 // mixed form: FP32 fields, FP32 weights and interpolation sums, FP64 point
 // forces and per-particle sums
 void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b);
-void launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
-                               const float *fv, const float *fw, double dt, int first, const int *gate = nullptr);
+int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                              const float *fv, const float *fw, double dt, int first, const int *gate = nullptr);
 void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
                          float *fw, double dt, const float *dfin = nullptr, const int *gate = nullptr);
 struct HarvestArgs {

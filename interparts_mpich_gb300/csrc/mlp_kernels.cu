@@ -46,14 +46,31 @@ __device__ __forceinline__ void load_b(uint32_t b[2], const bf16 *Bs, int ldb, i
   b[1] = *reinterpret_cast<const uint32_t *>(&Bs[(n0 + g) * ldb + k0 + 2 * t + 8]);
 }
 
-__device__ __forceinline__ float gelu_f(float z) {
-  const float c = 0.7978845608028654f, a = 0.044715f;
-  return 0.5f * z * (1.f + tanhf(c * (z + a * z * z * z)));
+// tanh-form GELU written with the logistic function: 0.5 z (1 + tanh u) =
+// z * sigma(2u), u = c (z + a z^3) (the same function; no cancellation for
+// negative z, two fast special-function operations instead of tanhf)
+// B fragments of two adjacent 8-column tiles (n0..n0+15, k0..k0+15) from
+// an n-major shared array by one ldmatrix.x4: b0 = tile n0, b1 = tile n0+8
+__device__ __forceinline__ void load_b2(uint32_t b0[2], uint32_t b1[2], const bf16 *Bs, int ldb, int n0, int k0,
+                                        int lane) {
+  const int m = lane >> 3, i = lane & 7;
+  const bf16 *row = Bs + (n0 + (m >> 1) * 8 + i) * ldb + k0 + (m & 1) * 8;
+  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(row);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(b0[0]), "=r"(b0[1]), "=r"(b1[0]), "=r"(b1[1])
+               : "r"(addr));
 }
+__device__ __forceinline__ float sig2u(float z) {
+  const float c = 0.7978845608028654f, a = 0.044715f;
+  const float u = c * (z + a * z * z * z);
+  return __fdividef(1.f, 1.f + __expf(-2.f * u));
+}
+__device__ __forceinline__ float gelu_f(float z) { return z * sig2u(z); }
+// d/dz: sigma + z * 2 sigma (1 - sigma) * c (1 + 3 a z^2)
 __device__ __forceinline__ float gelu_grad_f(float z) {
   const float c = 0.7978845608028654f, a = 0.044715f;
-  const float t = tanhf(c * (z + a * z * z * z));
-  return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * c * (1.f + 3.f * a * z * z);
+  const float sg = sig2u(z);
+  return sg + 2.f * z * sg * (1.f - sg) * c * (1.f + 3.f * a * z * z);
 }
 
 constexpr int NIN = 96, NH = 128, NOUT = 3;
@@ -207,7 +224,7 @@ void launch_mlp_forward(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, c
 // Same rounding points as the training forward: BF16 inputs, weights of
 // layers 1-2 and hidden activations; FP32 accumulation; FP32 W3.
 // ---------------------------------------------------------------------------
-constexpr int IW = 8;  // warps per CTA
+constexpr int IW = 12;  // warps per CTA (163 registers: one CTA per SM)
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t *>(&v);
@@ -254,10 +271,11 @@ __global__ void __launch_bounds__(IW * 32, 1) k_mlp_infer(const bf16 *__restrict
       uint32_t a[4];
       load_a(a, Xw, LDX, 0, k0, lane);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        uint32_t bb[2];
-        load_b(bb, W1s, LDX, j * 8, k0, lane);
-        mma16816(acc[j], a, bb);
+      for (int j = 0; j < 16; j += 2) {
+        uint32_t b0[2], b1[2];
+        load_b2(b0, b1, W1s, LDX, j * 8, k0, lane);
+        mma16816(acc[j], a, b0);
+        mma16816(acc[j + 1], a, b1);
       }
     }
     // bias + GELU, rounded to BF16 straight into the layer-2 A fragments
@@ -265,20 +283,22 @@ __global__ void __launch_bounds__(IW * 32, 1) k_mlp_infer(const bf16 *__restrict
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const int c0 = 16 * m + 2 * tq, c1 = c0 + 8;
-      af[m][0] = pack_bf2(gelu_f(acc[2 * m][0] + b1[c0]), gelu_f(acc[2 * m][1] + b1[c0 + 1]));
-      af[m][1] = pack_bf2(gelu_f(acc[2 * m][2] + b1[c0]), gelu_f(acc[2 * m][3] + b1[c0 + 1]));
-      af[m][2] = pack_bf2(gelu_f(acc[2 * m + 1][0] + b1[c1]), gelu_f(acc[2 * m + 1][1] + b1[c1 + 1]));
-      af[m][3] = pack_bf2(gelu_f(acc[2 * m + 1][2] + b1[c1]), gelu_f(acc[2 * m + 1][3] + b1[c1 + 1]));
+      const float2 p0 = *reinterpret_cast<const float2 *>(&b1[c0]), p1 = *reinterpret_cast<const float2 *>(&b1[c1]);
+      af[m][0] = pack_bf2(gelu_f(acc[2 * m][0] + p0.x), gelu_f(acc[2 * m][1] + p0.y));
+      af[m][1] = pack_bf2(gelu_f(acc[2 * m][2] + p0.x), gelu_f(acc[2 * m][3] + p0.y));
+      af[m][2] = pack_bf2(gelu_f(acc[2 * m + 1][0] + p1.x), gelu_f(acc[2 * m + 1][1] + p1.y));
+      af[m][3] = pack_bf2(gelu_f(acc[2 * m + 1][2] + p1.x), gelu_f(acc[2 * m + 1][3] + p1.y));
     }
 #pragma unroll
     for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        uint32_t bb[2];
-        load_b(bb, W2s, LDH, j * 8, 16 * m, lane);
-        mma16816(acc[j], af[m], bb);
+      for (int j = 0; j < 16; j += 2) {
+        uint32_t b0[2], b1[2];
+        load_b2(b0, b1, W2s, LDH, j * 8, 16 * m, lane);
+        mma16816(acc[j], af[m], b0);
+        mma16816(acc[j + 1], af[m], b1);
       }
     }
     // bias + GELU (BF16-rounded), layer 3 partial sums for rows g and g+8
@@ -290,12 +310,16 @@ __global__ void __launch_bounds__(IW * 32, 1) k_mlp_infer(const bf16 *__restrict
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const int col = j * 8 + 2 * tq;
+      const float2 bb = *reinterpret_cast<const float2 *>(&b2[col]);
+      float2 w[NOUT];
+#pragma unroll
+      for (int o = 0; o < NOUT; ++o) w[o] = *reinterpret_cast<const float2 *>(&w3[o * NH + col]);
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const float h0 = __bfloat162float(__float2bfloat16(gelu_f(acc[j][2 * h] + b2[col])));
-        const float h1 = __bfloat162float(__float2bfloat16(gelu_f(acc[j][2 * h + 1] + b2[col + 1])));
+        const float h0 = __bfloat162float(__float2bfloat16(gelu_f(acc[j][2 * h] + bb.x)));
+        const float h1 = __bfloat162float(__float2bfloat16(gelu_f(acc[j][2 * h + 1] + bb.y)));
 #pragma unroll
-        for (int o = 0; o < NOUT; ++o) part[h][o] += h0 * w3[o * NH + col] + h1 * w3[o * NH + col + 1];
+        for (int o = 0; o < NOUT; ++o) part[h][o] += h0 * w[o].x + h1 * w[o].y;
       }
     }
 #pragma unroll
