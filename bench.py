@@ -148,6 +148,33 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
             "predictor": (10 + 13 + 10) * n * w, "projection": 3 * 21 * n * w}
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant kernels from one ncu capture of the same command, for the roofline's
+# `traffic` key: {(form, kernel class): bytes}
+TRAFFIC = {}
+
+
+def kernel_model(case, w: int) -> dict:
+    """Algorithmic bytes (or flops) per launch of each probed kernel class, in
+    the reference dataflow model (words of distinct compulsory traffic):
+    predictor 11 words/cell (stage average), fillps+x FFT 3 reads + 1
+    spectrum word, each spectrum pass 2 words, correc 9 words (11 with the
+    double-float pressure), IBM interpolation 3 and spreading 6 words per
+    footprint cell S_fp, sphere integrals 3 box words per sphere; the MLP in
+    flops (2 x 29,184 per point)."""
+    n = case.itot * case.jtot * case.ktot
+    ibm = s_fp(case) * case.np
+    npts = case.np * case.nl
+    return {
+        "predict": ("hbm", 11 * n * w), "stencil": ("hbm", npts * (24 + (96 if w == 4 else 168))),
+        "interp": ("hbm", 3 * ibm * w), "spread": ("hbm", 6 * ibm * w),
+        "fillps_fftx": ("hbm", 4 * n * w), "ffty": ("hbm", 2 * n * w), "thomas": ("hbm", 2 * n * w),
+        "ifftx": ("hbm", 2 * n * w), "correc": ("hbm", (11 if w == 4 else 9) * n * w),
+        "sphere": ("hbm", 3 * sphere_box(case) * case.np * w),
+        "features": ("hbm", 3 * ibm * w + npts * 96 * 2), "mlp": ("tensor", 2 * 29184 * npts),
+    }
+
+
 def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     """Times one arithmetic form on the channel case: K steps between CUDA
     events on the library's stream, plus the per-phase times of one step."""
@@ -189,6 +216,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        solver.probe()  # CUDA events around every kernel launch of the timed steps
         with torch.cuda.stream(stream):
             torch.cuda.nvtx.range_push("timed")  # profilers select the timed steps by this range
             ev0.record(stream)
@@ -199,6 +227,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     torch.cuda.synchronize()
     barrier(ws)
     ms = ev0.elapsed_time(ev1) / args.steps
+    kernels = solver.probe_result()
     launches = solver.launch_count() - launches0
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
@@ -241,7 +270,8 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
     solver.close()
     return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
-            "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn}
+            "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn,
+            "kernels": kernels}
 
 
 def cpu_baseline(args, case_fn):
@@ -331,14 +361,29 @@ def main():
     case = r["case"]
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
+    tflops = peaks.get("bf16_tflops", 1900.0)
     w = 8 if head == "plain" else 4
-    ab = algorithmic_bytes(case)
+
+    def kernel_table(x, wb):
+        model = kernel_model(x["case"], wb)
+        out = {}
+        for name, (tot_ms, cnt) in x["kernels"].items():
+            if cnt == 0:
+                continue
+            bound, units = model[name]
+            per = tot_ms / cnt
+            ach = units / (per * 1e-3) / (1e9 if bound == "hbm" else 1e12)
+            peak = hbm if bound == "hbm" else tflops
+            out[name] = {"launches_per_step": round(cnt / args.steps, 2), "ms_per_launch": round(per, 4),
+                         "share_of_step": round(tot_ms / args.steps / x["ms"], 4), "bound": bound,
+                         "algorithmic_per_launch": int(units), "achieved": round(ach, 1),
+                         "unit": "GB/s" if bound == "hbm" else "TFLOP/s", "frac": round(ach / peak, 4)}
+        return out
+    ab = algorithmic_bytes(case, w)
     names = ["predictor", "ibm", "projection", "newton_euler"]
-    byts = {"predictor": ab["predictor"], "ibm": ab["ibm"], "projection": ab["projection"],
-            "newton_euler": ab["sphere"]}
-    phases = r["phases"]
-    dom = max(range(4), key=lambda q: phases[q])
-    achieved = byts[names[dom]] / (phases[dom] * 1e-3) / 1e9
+    ktab = kernel_table(r, w)
+    dom = max(ktab, key=lambda k: ktab[k]["share_of_step"])
+    dk = ktab[dom]
     line = {
         "metric": METRIC, "value": round(r["ms"], 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(r["ms"], 4), "higher_is_better": False, "scaling": "weak",
@@ -350,12 +395,17 @@ def main():
                       "mcell_steps_per_s": round(args.gpus * x["ncell"] / (x["ms"] * 1e-3) / 1e6, 1),
                       "phases_ms": {n: round(t, 4) for n, t in zip(names, x["phases"])},
                       "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"]),
+                      "kernels": kernel_table(x, 8 if f == "plain" else 4),
                       **({"learned_forcing": x["learn"]} if x["learn"] else {})} for f, x in res.items()},
         "mcell_steps_per_s": round(args.gpus * r["ncell"] / (r["ms"] * 1e-3) / 1e6, 1),
         "hbm_roofline_frac_step": round(ab["total"] / (r["ms"] * 1e-3) / 1e9 / hbm, 4),
-        "roofline": {"bound": "hbm", "kernel": names[dom] + " phase", "achieved": round(achieved * w / 8, 1),
-                     "peak": hbm, "unit": "GB/s", "frac": round(achieved * w / 8 / hbm, 4), "traffic": None,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800"},
+        "roofline": {"bound": dk["bound"], "kernel": dom, "achieved": dk["achieved"],
+                     "peak": hbm if dk["bound"] == "hbm" else tflops, "unit": dk["unit"], "frac": dk["frac"],
+                     "traffic": TRAFFIC.get((head, dom)),
+                     "algorithmic_per_launch": dk["algorithmic_per_launch"], "ms_per_launch": dk["ms_per_launch"],
+                     "peak_source": ("MEASURED_PEAKS.json " + ("hbm_gbs" if dk["bound"] == "hbm" else "bf16_tflops")
+                                     + " (of measured)") if peaks else "fallback (of fallback)"},
+        "kernels": ktab,
         "gpu_launches": int(r["launches"]),
         "clocks": r["clocks"],
         "dt": r["dt"],

@@ -247,10 +247,35 @@ int ibm_mlp_gradient(ibm_ctx *ctx, const float *params, const float *x, const fl
                      float *loss, float *y);
 /* The inference kernel of the forcing loop on a caller batch: y[nb][3]. */
 int ibm_mlp_infer(ibm_ctx *ctx, const float *params, const float *x, int nb, float *y);
+/* The same on the tcgen05 (TMEM-accumulator) inference kernel. */
+int ibm_mlp_infer_tc(ibm_ctx *ctx, const float *params, const float *x, int nb, float *y);
 /* nsteps full-batch Adam steps from params_in with fresh moments:
  * params_out[IBM_NN_NPARAM], losses[nsteps] (loss before each update). */
 int ibm_mlp_fit(ibm_ctx *ctx, const float *params_in, const float *x, const float *t, int nb, int nsteps,
                 double lr, float *params_out, float *losses);
+
+/* --- per-kernel timing ------------------------------------------------------- */
+
+/* Kernel classes of the step for ibm_probe (bit i of the mask = class i). */
+#define IBM_PROBE_PREDICT     0   /* k_predict                                   */
+#define IBM_PROBE_STENCIL     1   /* IBM stencil cache                           */
+#define IBM_PROBE_INTERP      2   /* interpolation + point forces (+ force sums) */
+#define IBM_PROBE_SPREAD      3   /* spreading                                   */
+#define IBM_PROBE_FILLPS_FFTX 4   /* fillps fused with the x FFT                 */
+#define IBM_PROBE_FFTY        5   /* y FFT (forward and inverse)                 */
+#define IBM_PROBE_THOMAS      6   /* Thomas sweep in z                           */
+#define IBM_PROBE_IFFTX       7   /* inverse x FFT                               */
+#define IBM_PROBE_CORREC      8   /* correc + pnew update                        */
+#define IBM_PROBE_SPHERE      9   /* sphere integrals                            */
+#define IBM_PROBE_FEATURES    10  /* learned forcing: features                   */
+#define IBM_PROBE_MLP         11  /* learned forcing: network inference         */
+#define IBM_PROBE_N           12
+/* Records CUDA events on the context stream around every launch of the
+ * selected classes from now on (a profiler-free per-kernel timer; the events
+ * add no GPU work).  ibm_probe_result synchronises, returns per class the
+ * summed milliseconds and the number of launches timed, and stops probing. */
+int ibm_probe(ibm_ctx *ctx, unsigned mask);
+int ibm_probe_result(ibm_ctx *ctx, double ms[IBM_PROBE_N], int launches[IBM_PROBE_N]);
 
 /* --- allocation-free variant ------------------------------------------------ */
 

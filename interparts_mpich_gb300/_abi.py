@@ -151,6 +151,8 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "sync": (C.c_int, [ctx]),
         "chkdiv_noalloc": (C.c_int, [c_double_p, c_double_p, c_double_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_double, C.c_double, c_double_p, C.c_void_p]),
+        "probe": (C.c_int, [ctx, C.c_uint]),
+        "probe_result": (C.c_int, [ctx, c_double_p, c_int_p]),
         "harvest": (C.c_int, [ctx, C.c_int, C.c_int, C.c_int]),
         "train_forcing_model": (C.c_int, [ctx, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_int, c_double_p]),
         "set_forcing_model": (C.c_int, [ctx, c_float_p, c_float_p]),
@@ -159,6 +161,7 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "learned_stats": (C.c_int, [ctx, c_double_p]),
         "mlp_gradient": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p]),
         "mlp_infer": (C.c_int, [ctx, c_float_p, c_float_p, C.c_int, c_float_p]),
+        "mlp_infer_tc": (C.c_int, [ctx, c_float_p, c_float_p, C.c_int, c_float_p]),
         "mlp_fit": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, C.c_int, C.c_double, c_float_p,
                               c_float_p]),
     }

@@ -584,7 +584,8 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
   constexpr int PF = 8;
   auto ld = [&](int k) -> double2 {
     const C v = s[k * sstride];
-    return F32 ? make_double2((double)v.x, (double)v.y) : make_double2((double)v.x * lscale, (double)v.y * lscale);
+    if constexpr (F32) return make_double2((double)v.x, (double)v.y);
+    else return make_double2((double)v.x * lscale, (double)v.y * lscale);
   };
   auto st_mid = [&](int k, double2 v) {  // forward intermediate
     if constexpr (F32) {
@@ -707,7 +708,7 @@ template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
                     const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64,
-                    double2 *thomas_tmp) {
+                    double2 *thomas_tmp, PoissonHook hook) {
   typedef typename cpx<T>::t C;
   C *S = reinterpret_cast<C *>(spec);
   const int M = g.I / 2;
@@ -719,18 +720,29 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
     if (reg_n2(M) && reg_n2(g.J)) {
       float2 *Sf = reinterpret_cast<float2 *>(spec);
       const float2 *tM = (const float2 *)twM, *tN = (const float2 *)twN, *tJ = (const float2 *)twJ;
+      hook(0, 1);
       fftx_r(s, g, (const float *)fu, (const float *)fv, (float *)fw, Sf, tM, tN, dtidxi, dtidyi, dtidzi, res64, false,
              nullptr);
+      hook(0, 0);
+      hook(1, 1);
       ffty_r(s, g, Sf, tJ, 0);
+      hook(1, 0);
       const long ncol = (long)g.MX * g.J;
       const double scale = 1.0 / ((double)M * g.J);
+      hook(2, 1);
       k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale, thomas_tmp);
+      hook(2, 0);
+      hook(3, 1);
       ffty_r(s, g, Sf, tJ, 1);
+      hook(3, 0);
+      hook(4, 1);
       fftx_r(s, g, nullptr, nullptr, nullptr, Sf, tM, tN, 0., 0., 0., false, true, (float *)phi);
+      hook(4, 0);
       if (launches) *launches += 5;
       return;
     }
   }
+  hook(0, 1);
   if (res64 && sizeof(TIn) == 4)
     k_fillps_fftx<TIn, T, float, true><<<(nrow + rows - 1) / rows, 128, smx, s>>>(
         g, plx, fu, fv, fw, S, (const C *)twM, (const C *)twN, dtidxi, dtidyi, dtidzi, rows);
@@ -742,16 +754,25 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
     k_fillps_fftx<TIn, T, TIn><<<(nrow + rows - 1) / rows, 128, smx, s>>>(g, plx, fu, fv, fw, S, (const C *)twM,
                                                                          (const C *)twN, dtidxi, dtidyi, dtidzi,
                                                                          rows);
+  hook(0, 0);
   const int cols = 8;
   size_t smy = (size_t)2 * (g.J + 1) * cols * sizeof(C);
   dim3 gy((g.MX + cols - 1) / cols, g.K);
+  hook(1, 1);
   k_ffty<T><<<gy, 256, smy, s>>>(g, ply, S, (const C *)twJ, cols, 0);
+  hook(1, 0);
   const long ncol = (long)g.MX * g.J;
   const double scale = 1.0 / ((double)M * g.J);
+  hook(2, 1);
   k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale, thomas_tmp);
+  hook(2, 0);
+  hook(3, 1);
   k_ffty<T><<<gy, 256, smy, s>>>(g, ply, S, (const C *)twJ, cols, 1);
+  hook(3, 0);
   size_t smi = (size_t)(2 * rows * M + rows * (M + 1)) * sizeof(C);
+  hook(4, 1);
   k_ifftx<T><<<(nrow + rows - 1) / rows, 128, smi, s>>>(g, plx, S, phi, (const C *)twM, (const C *)twN, rows);
+  hook(4, 0);
   if (launches) *launches += 5;
 }
 
@@ -775,11 +796,11 @@ int poisson_set_smem_limits() {
 template void launch_poisson<double, double>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                              const double *, const double *, double *, void *, double *,
                                              const void *, const void *, const void *, const double *, double, double,
-                                             double, int *, bool, double2 *);
+                                             double, int *, bool, double2 *, PoissonHook);
 template void launch_poisson<float, float>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                            const float *, const float *, float *, void *, float *, const void *,
                                            const void *, const void *, const double *, double, double, double, int *,
-                                           bool, double2 *);
+                                           bool, double2 *, PoissonHook);
 template int poisson_set_smem_limits<double>();
 template int poisson_set_smem_limits<float>();
 

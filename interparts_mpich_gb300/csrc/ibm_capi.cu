@@ -76,6 +76,11 @@ struct ibm_ctx {
   __nv_bfloat16 *tx = nullptr; // staged training set
   float *tt = nullptr;
   int tcap = 0, train_step = 0;
+  // per-kernel event probe (ibm_probe): events around every launch of the
+  // selected kernel classes, on the context stream
+  unsigned probe_mask = 0;
+  std::vector<cudaEvent_t> probe_ev[IBM_PROBE_N];
+  int probe_used[IBM_PROBE_N] = {};
   bool have_fields = false, have_particles = false, particles_ready = false;
   long long launches = 0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -105,6 +110,29 @@ int cuda_err(ibm_ctx *c, cudaError_t e, const char *where) {
     c->launches += (n);                                                 \
     cudaError_t e_ = cudaGetLastError();                                \
     if (e_ != cudaSuccess) return cuda_err(c, e_, "kernel launch");     \
+  } while (0)
+
+void probe_mark(ibm_ctx *c, int id) {
+  if (!(c->probe_mask & (1u << id))) return;
+  std::vector<cudaEvent_t> &ev = c->probe_ev[id];
+  if (c->probe_used[id] == (int)ev.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) { c->probe_mask &= ~(1u << id); return; }
+    ev.push_back(e);
+  }
+  cudaEventRecord(ev[c->probe_used[id]++], c->stream);
+}
+// Poisson stages -> probe ids
+void poisson_probe(void *arg, int stage, int begin) {
+  (void)begin;
+  static const int ids[5] = {IBM_PROBE_FILLPS_FFTX, IBM_PROBE_FFTY, IBM_PROBE_THOMAS, IBM_PROBE_FFTY, IBM_PROBE_IFFTX};
+  probe_mark(reinterpret_cast<ibm_ctx *>(arg), ids[stage]);
+}
+#define PROBED(id, ...) \
+  do {                  \
+    probe_mark(c, id);  \
+    __VA_ARGS__;        \
+    probe_mark(c, id);  \
   } while (0)
 
 template <typename T>
@@ -341,7 +369,8 @@ int alloc_all(ibm_ctx *c) {
                        &c->ib.dvdtl, &c->ib.dwdtl, &c->ib.fxl, &c->ib.fyl, &c->ib.fzl})
       if ((st = dalloc(c, f, npl))) return st;
     if (c->mixed) {
-      if ((st = dalloc(c, &c->ib.st32, npl))) return st;
+      if ((st = dalloc(c, &c->ib.cs, 3 * npl))) return st;
+      if ((st = dalloc(c, &c->ib.bgeo, (size_t)24 * np))) return st;
       if ((st = dalloc(c, &c->ib.psum, (size_t)9 * np))) return st;
     } else {
       if ((st = dalloc(c, &c->ib.st, npl))) return st;
@@ -415,11 +444,11 @@ int predict(ibm_ctx *c, int rkiter, double dt) {
   else if (rkiter == 2) { f1 = dt * (8. / 60.); f2 = dt * (25. / 60.); f3 = dt * (17. / 60.); }
   else { f1 = dt * (20. / 60.); f2 = dt * (45. / 60.); f3 = dt * (25. / 60.); }
   if (c->mixed)
-    launch_predict<float, float>(c->stream, g, rkiter, c->u32, c->v32, c->w32, c->p32, c->ru32, c->rv32, c->rw32,
-                                 c->fu32, c->fv32, c->fw32, f1, f2, f3);
+    PROBED(IBM_PROBE_PREDICT, launch_predict<float, float>(c->stream, g, rkiter, c->u32, c->v32, c->w32, c->p32, c->ru32, c->rv32, c->rw32,
+                                 c->fu32, c->fv32, c->fw32, f1, f2, f3));
   else
-    launch_predict<double, double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv,
-                                   c->fw, f1, f2, f3);
+    PROBED(IBM_PROBE_PREDICT, launch_predict<double, double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv,
+                                   c->fw, f1, f2, f3));
   LAUNCHED(1);
   return IBM_OK;
 }
@@ -429,23 +458,23 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   // no-slip residual exceeds fallback_ratio x the plain method's
   const Geo &g = c->g;
   const long npts = (long)c->pg.np * c->pg.nl;
-  launch_ibm_stencil_f(c->stream, g, c->pg, c->ib);
-  c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 1);
+  PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
+  PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 1));
   launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
-  launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt);
+  PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt));
   LAUNCHED(4);
   HarvestArgs none{};
-  launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->norm, c->norm + 96, c->lx,
-                        none);
-  launch_mlp_infer(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly);
+  PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->norm, c->norm + 96, c->lx,
+                        none));
+  PROBED(IBM_PROBE_MLP, launch_mlp_infer(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly));
   launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
-  launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf);
-  c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
+  PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf));
+  PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
   launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 0);
   LAUNCHED(7);
   for (int it = 1; it < nl_iter; ++it) {
-    c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 0, c->gate);
-    launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate);
+    PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 0, c->gate));
+    PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate));
     LAUNCHED(2);
   }
   return IBM_OK;
@@ -458,26 +487,26 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     if (c->learn_on && !c->harvesting && nl_iter >= 2) return forcing_learned(c, dt, nl_iter);
     const long npts = (long)c->pg.np * c->pg.nl;
     const int npass = c->harvesting ? std::max(nl_iter, c->hv_passes) : nl_iter;
-    launch_ibm_stencil_f(c->stream, g, c->pg, c->ib);
+    PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
     LAUNCHED(1);
     for (int it = 0; it < npass; ++it) {
-      c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, it == 0 ? 1 : 0);
+      PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, it == 0 ? 1 : 0));
       LAUNCHED(1);
       if (it == 0) {
         launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
         LAUNCHED(1);
       }
-      launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt);
+      PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt));
       LAUNCHED(1);
       if (c->harvesting && it == 0) {
         c->hv.phase = (c->hv.phase + 1) % c->hv.stride;
-        launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, nullptr, nullptr,
-                              c->hv);
+        PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, nullptr, nullptr,
+                              c->hv));
         LAUNCHED(1);
       }
       if (c->harvesting && it == nl_iter - 1) {
         // the plain method's residual at its own number of passes
-        c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1);
+        PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
         launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 1);
         LAUNCHED(3);
       }
@@ -488,16 +517,17 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     }
     return IBM_OK;
   }
-  launch_ibm_stencil<double>(c->stream, g, c->pg, c->ib);
+  PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil<double>(c->stream, g, c->pg, c->ib));
   LAUNCHED(1);
   for (int it = 0; it < nl_iter; ++it) {
-    launch_ibm_interp_force<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0 ? 1 : 0);
+    PROBED(IBM_PROBE_INTERP,
+           launch_ibm_interp_force<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0 ? 1 : 0));
     LAUNCHED(1);
     if (it == 0) {  // dwdtf(:,:,k1) carries only S(F) (interp_spread.f90:267-269)
       launch_zero_plane<double>(c->stream, g, c->fw, g.K + 1);
       LAUNCHED(1);
     }
-    launch_ibm_spread<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0);
+    PROBED(IBM_PROBE_SPREAD, launch_ibm_spread<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0));
     LAUNCHED(1);
   }
   return IBM_OK;
@@ -512,10 +542,10 @@ int project(ibm_ctx *c, int rkiter, double dt) {
     // FP32 solve of fillps(u*), FP64 Thomas; correction into the FP64 state
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
                                  c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl,
-                                 false, c->thomas_tmp);
+                                 false, c->thomas_tmp, PoissonHook{poisson_probe, c});
     LAUNCHED(nl);
-    launch_correc_mixed(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
-                        factor * g.dxi, factor * g.dyi, factor * g.dzi);
+    PROBED(IBM_PROBE_CORREC, launch_correc_mixed(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
+                        factor * g.dxi, factor * g.dyi, factor * g.dzi));
     LAUNCHED(1);
     // one defect correction: the divergence residual of the corrected state,
     // evaluated in FP64, drives a second solve; its pressure is accumulated
@@ -523,18 +553,18 @@ int project(ibm_ctx *c, int rkiter, double dt) {
     nl = 0;
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->u32, c->v32, c->w32, c->spec32, c->phi32, c->twM32,
                                  c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl, true,
-                                 c->thomas_tmp);
+                                 c->thomas_tmp, PoissonHook{poisson_probe, c});
     LAUNCHED(nl);
-    launch_correc_mixed(c->stream, g, c->u32, c->v32, c->w32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
-                        factor * g.dxi, factor * g.dyi, factor * g.dzi);
+    PROBED(IBM_PROBE_CORREC, launch_correc_mixed(c->stream, g, c->u32, c->v32, c->w32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
+                        factor * g.dxi, factor * g.dyi, factor * g.dzi));
     LAUNCHED(1);
     return IBM_OK;
   }
   launch_poisson<double, double>(c->stream, g, c->plx, c->ply, c->fu, c->fv, c->fw, c->spec, c->phi, c->twM, c->twN,
-                                 c->twJ, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl);
+                                 c->twJ, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl, false, nullptr, PoissonHook{poisson_probe, c});
   LAUNCHED(nl);
-  launch_correc<double, double, double>(c->stream, g, c->fu, c->fv, c->fw, c->phi, c->u, c->v, c->w, c->p, nullptr,
-                                        factor * g.dxi, factor * g.dyi, factor * g.dzi);
+  PROBED(IBM_PROBE_CORREC, launch_correc<double, double, double>(c->stream, g, c->fu, c->fv, c->fw, c->phi, c->u, c->v, c->w, c->p, nullptr,
+                                        factor * g.dxi, factor * g.dyi, factor * g.dzi));
   LAUNCHED(1);
   return IBM_OK;
 }
@@ -543,8 +573,10 @@ int newton_euler(ibm_ctx *c, int rkiter, double dt) {
   if (c->pg.np == 0) return IBM_OK;
   launch_save_old(c->stream, c->pg, c->pb);
   LAUNCHED(1);
+  probe_mark(c, IBM_PROBE_SPHERE);
   if (c->mixed) launch_sphere_integrals<float>(c->stream, c->g, c->pg, c->pb, c->u32, c->v32, c->w32, 23);
   else launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
+  probe_mark(c, IBM_PROBE_SPHERE);
   LAUNCHED(1);
   for (int iter = 0; iter <= 1; ++iter) {
     launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt);
@@ -647,7 +679,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
-                  c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.st32, c->u32, c->v32,
+                  c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_tmp, c->ib.psum};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -657,6 +689,8 @@ int ibm_destroy(ibm_ctx *c) {
   for (void *q : lptrs)
     if (q) cudaFree(q);
   free_mlp_batch(c->mt);
+  for (auto &v : c->probe_ev)
+    for (cudaEvent_t e : v) cudaEventDestroy(e);
   if (c->hpin) cudaFreeHost(c->hpin);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -1317,6 +1351,31 @@ int ibm_mlp_infer(ibm_ctx *c, const float *params, const float *x, int nb, float
   return st;
 }
 
+int ibm_mlp_infer_tc(ibm_ctx *c, const float *params, const float *x, int nb, float *y) {
+  if (!c || !params || !x || !y || nb < 1) return IBM_E_INVALID;
+  MlpTrainBuffers B{};
+  std::vector<float> t((size_t)nb * 3, 0.f);
+  int st = mlp_scratch(c, params, x, t.data(), nb, B);
+  int *derr = nullptr;
+  if (st == IBM_OK) st = dalloc(c, &derr, 1);
+  if (st == IBM_OK) {
+    c->launches += launch_mlp_infer_tc(c->stream, B.x, nb, B.w1b, B.w2b, B.params, B.y, derr);
+    int herr = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(y, B.y, (size_t)nb * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    st = cuda_err(c, e, "ibm_mlp_infer_tc");
+    if (st == IBM_OK && herr) st = set_err(c, IBM_E_NOT_CONVERGED, "tensor-core MMA wait timed out");
+  }
+  cudaStreamSynchronize(c->stream);
+  if (derr) cudaFree(derr);
+  free_mlp_batch(B);
+  free_mlp_model(B);
+  return st;
+}
+
 int ibm_mlp_fit(ibm_ctx *c, const float *params_in, const float *x, const float *t, int nb, int nsteps, double lr,
                 float *params_out, float *losses) {
   if (!c || !params_in || !x || !t || nb < 1 || nsteps < 0 || !(lr > 0)) return IBM_E_INVALID;
@@ -1338,5 +1397,35 @@ int ibm_mlp_fit(ibm_ctx *c, const float *params_in, const float *x, const float 
   free_mlp_model(B);
   return st;
 }
+
+/* --- per-kernel event probe --------------------------------------------------- */
+
+int ibm_probe(ibm_ctx *c, unsigned mask) {
+  if (!c) return IBM_E_INVALID;
+  CK(cudaStreamSynchronize(c->stream));
+  c->probe_mask = mask & ((1u << IBM_PROBE_N) - 1);
+  for (int q = 0; q < IBM_PROBE_N; ++q) c->probe_used[q] = 0;
+  return IBM_OK;
+}
+
+int ibm_probe_result(ibm_ctx *c, double ms[IBM_PROBE_N], int launches[IBM_PROBE_N]) {
+  if (!c) return IBM_E_INVALID;
+  CK(cudaStreamSynchronize(c->stream));
+  for (int q = 0; q < IBM_PROBE_N; ++q) {
+    double tot = 0.;
+    const int n = c->probe_used[q] / 2;
+    for (int k = 0; k < n; ++k) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, c->probe_ev[q][2 * k], c->probe_ev[q][2 * k + 1]));
+      tot += t;
+    }
+    if (ms) ms[q] = tot;
+    if (launches) launches[q] = n;
+    c->probe_used[q] = 0;
+  }
+  c->probe_mask = 0;
+  return IBM_OK;
+}
+
 
 }  // extern "C"

@@ -46,10 +46,12 @@ struct PointStencil {
   double phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
 };
 
-// FP32 weights of the same stencil for the mixed form
-struct PointStencilF {
-  int ilow, jlow, klow, ilows, jlows, klows;
-  float phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
+// Mixed form: one velocity component of one Lagrangian point: index of tap
+// (0,0,0) of the 3x3x3 block (x, y unwrapped) and the component's FP32 delta
+// weights wx[3], wy[3], wz[3] (48 bytes, read as three float4)
+struct __align__(16) CompStencil {
+  int b[3];
+  float w[9];
 };
 
 // Constants of one context, passed by value to the kernels.

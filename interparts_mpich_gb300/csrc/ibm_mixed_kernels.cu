@@ -1,0 +1,477 @@
+// ibm_mixed_kernels.cu -- the multidirect IBM loop of the mixed form
+// (interp_spread.f90, forcing.f90 restated for FP32 fields).
+//
+// Per Lagrangian point and velocity component a 48-byte stencil record
+// (origin of the 3x3x3 tap block and the component's 9 delta weights) is
+// built once per substep; the per-particle, per-component box of cells the
+// stencils touch is computed once as well.  Interpolation and spreading then
+// run one block per (particle, component) on a shared-memory copy of that
+// box: interpolation reads it with coalesced rows, spreading accumulates into
+// it and flushes each touched cell to HBM once.
+//
+// Origins come from the FP64 point coordinates exactly as the FP64 form
+// computes them; delta weights, interpolation sums and spreading are FP32,
+// spreading compensated (TwoSum of every shared-memory add); point forces
+// F_l and the per-particle force/torque sums stay FP64.
+#include <cuda_bf16.h>
+
+#include "kernels.cuh"
+
+namespace ibmk {
+
+__device__ __forceinline__ int relwrap(int d, int n) {
+  const int h = n / 2;
+  return d >= h ? d - n : (d < -h ? d + n : d);
+}
+
+// ---------------------------------------------------------------------------
+// Stencil records.  Component c of point t at cs[c*npl + t]:
+//   u: taps (ilows-1+i, jlow-1+j, klow+k),  weights phix,  phiyh, phizh
+//   v: taps (ilow-1+i,  jlows-1+j, klow+k), weights phixh, phiy,  phizh
+//   w: taps (ilow-1+i,  jlow-1+j, klows+k), weights phixh, phiyh, phiz
+// with the stencil origins and delta arguments of eulr2lagr
+// (interp_spread.f90:60-131): x, y indices unwrapped (periodic wrap at use).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_ibm_stencil_c(Geo g, PartGeo pg, IbmBuffers b) {
+  const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int p = t / pg.nl, l = t - p * pg.nl;
+    if (l >= b.nla[p]) continue;
+    const double xfp = b.xfp[t], yfp = b.yfp[t], zfp = b.zfp[t];
+    // periodic image by a multiply: any image whose coordinate stays in
+    // [0, I+1] addresses the same (wrapped) cells with the same weights
+    const double inv_lx = 1. / g.lx, inv_ly = 1. / g.ly;
+    double coorxfp = xfp * g.dxi - (double)((long)floor((xfp - 0.5 * g.dx) * inv_lx) * g.I);
+    double cooryfp = yfp * g.dyi - (double)((long)floor((yfp - 0.5 * g.dy) * inv_ly) * g.J);
+    double coorzfp = zfp * g.dzi;
+    if (!(coorxfp >= 0. && coorxfp <= g.I + 1.) || !(cooryfp >= 0. && cooryfp <= g.J + 1.) ||
+        !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
+      atomicExch(&b.err[2], 1);
+      coorxfp = 1.; cooryfp = 1.; coorzfp = 1.5;
+    }
+    const int ilows = fnint(coorxfp) - 1, jlows = fnint(cooryfp) - 1, klows = max(fnint(coorzfp) - 1, 1);
+    const int ilow = (int)floor(coorxfp), jlow = (int)floor(cooryfp);
+    const int klow = max(min((int)floor(coorzfp), g.K - 2), 1);
+    // offsets of the point from the stencil origins (FP64, exact integer
+    // parts), the 3-tap arguments then in FP32
+    const float ox = (float)(coorxfp - ilows), oy = (float)(cooryfp - jlows), oz = (float)(coorzfp - klows);
+    const float hx = (float)(coorxfp - ilow), hy = (float)(cooryfp - jlow), hz = (float)(coorzfp - klow);
+    float phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
+    for (int m = 0; m < 3; ++m) {
+      phix[m] = delta3f((float)m - ox);
+      phiy[m] = delta3f((float)m - oy);
+      phiz[m] = delta3f((float)m - oz);
+      phixh[m] = delta3f(((float)m - 0.5f) - hx);
+      phiyh[m] = delta3f(((float)m - 0.5f) - hy);
+      phizh[m] = delta3f(((float)m - 0.5f) - hz);
+    }
+    const long npl = (long)n;
+    CompStencil s;
+    s.b[0] = ilows - 1; s.b[1] = jlow - 1; s.b[2] = klow;
+    for (int m = 0; m < 3; ++m) { s.w[m] = phix[m]; s.w[3 + m] = phiyh[m]; s.w[6 + m] = phizh[m]; }
+    b.cs[t] = s;
+    s.b[0] = ilow - 1; s.b[1] = jlows - 1; s.b[2] = klow;
+    for (int m = 0; m < 3; ++m) { s.w[m] = phixh[m]; s.w[3 + m] = phiy[m]; s.w[6 + m] = phizh[m]; }
+    b.cs[npl + t] = s;
+    s.b[0] = ilow - 1; s.b[1] = jlow - 1; s.b[2] = klows;
+    for (int m = 0; m < 3; ++m) { s.w[m] = phixh[m]; s.w[3 + m] = phiyh[m]; s.w[6 + m] = phiz[m]; }
+    b.cs[2 * npl + t] = s;
+  }
+}
+
+// Box of the cells the stencils of particle p, component c touch:
+// bgeo[(p*3 + c)*8 + ] = {refx, refy, bmin_x, bmin_y, bmin_z, nbx, nby, nbz};
+// x, y relative to the first point's origin (periodic), box cell (cx,cy,cz)
+// = tap (refx + bmin_x + cx, refy + bmin_y + cy, bmin_z + cz).
+__global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, int I, int J) {
+  const int p = blockIdx.x, c = blockIdx.y;
+  const int nla = b.nla[p];
+  const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
+  const CompStencil *cs = b.cs + c * npl + t0;
+  __shared__ int mn[3], mx[3];
+  if (threadIdx.x < 3) { mn[threadIdx.x] = 0x7fffffff; mx[threadIdx.x] = -0x7fffffff; }
+  __syncthreads();
+  const int refx = nla > 0 ? cs[0].b[0] : 0, refy = nla > 0 ? cs[0].b[1] : 0;
+  int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const int4 o = *reinterpret_cast<const int4 *>(&cs[l]);  // b[0..2] (+ w[0])
+    const int r[3] = {relwrap(o.x - refx, I), relwrap(o.y - refy, J), o.z};
+    for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], r[d]); hi[d] = max(hi[d], r[d]); }
+  }
+  for (int d = 0; d < 3; ++d) {
+    const int wl = __reduce_min_sync(0xffffffffu, lo[d]), wh = __reduce_max_sync(0xffffffffu, hi[d]);
+    if ((threadIdx.x & 31) == 0) { atomicMin(&mn[d], wl); atomicMax(&mx[d], wh); }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int *o = b.bgeo + ((long)p * 3 + c) * 8;
+    o[0] = refx; o[1] = refy;
+    if (nla > 0) {
+      o[2] = mn[0]; o[3] = mn[1]; o[4] = mn[2];
+      o[5] = mx[0] - mn[0] + 3; o[6] = mx[1] - mn[1] + 3; o[7] = mx[2] - mn[2] + 3;
+    } else {
+      o[2] = o[3] = o[4] = o[5] = o[6] = o[7] = 0;
+    }
+  }
+}
+
+void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b) {
+  if (pg.np == 0) return;
+  k_ibm_stencil_c<<<1216, 256, 0, s>>>(g, pg, b);
+  k_ibm_box_geom<<<dim3(pg.np, 3), 256, 0, s>>>(pg, b, g.I, g.J);
+}
+
+// box usable in shared memory: fits cap and narrower than half the periodic
+// domain (so relative indices are unambiguous)
+__device__ __forceinline__ bool box_ok(const int *bg, int cap, int I, int J) {
+  return bg[5] > 0 && (long)bg[5] * bg[6] * bg[7] <= cap && bg[5] < I / 2 && bg[6] < J / 2;
+}
+// offset of tap (0,0,0) of a point in its particle's box
+__device__ __forceinline__ int box_off(const CompStencil &s, const int *bg, int I, int J) {
+  const int cx = relwrap(s.b[0] - bg[0], I) - bg[2], cy = relwrap(s.b[1] - bg[1], J) - bg[3];
+  return ((s.b[2] - bg[4]) * bg[6] + cy) * bg[5] + cx;
+}
+__device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__ F, const int *bg, float *box) {
+  const int nbx = bg[5], nby = bg[6], nxy = nbx * nby, nbox = nxy * bg[7];
+  const int x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
+  for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
+    const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
+    box[q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
+  }
+}
+__device__ __forceinline__ CompStencil load_cs(const CompStencil *p) {
+  const float4 *q = reinterpret_cast<const float4 *>(p);
+  const float4 a = q[0], bb = q[1], c = q[2];
+  CompStencil s;
+  s.b[0] = __float_as_int(a.x); s.b[1] = __float_as_int(a.y); s.b[2] = __float_as_int(a.z);
+  s.w[0] = a.w; s.w[1] = bb.x; s.w[2] = bb.y; s.w[3] = bb.z; s.w[4] = bb.w;
+  s.w[5] = c.x; s.w[6] = c.y; s.w[7] = c.z; s.w[8] = c.w;
+  return s;
+}
+// 27-tap interpolation of one component, k outer, j, i inner, each term
+// f * (wx_i * (wy_j * wz_k))
+template <typename TAP>
+__device__ __forceinline__ float interp27(const CompStencil &s, TAP tap) {
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float wyz = s.w[3 + j] * s.w[6 + k];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) acc += tap(i, j, k) * (s.w[i] * wyz);
+    }
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// eulr2lagr + complagrforces/updtlagrforces: block (particle, component).
+// Interpolated component to dudtl/dvdtl/dwdtl; with first >= 0 the FP64
+// point-force update of the component and its partial sums (sum F_c and the
+// two lever-arm moments of F_c in the torque) to psum; k_ibm_force_sums
+// combines the components.  first < 0: interpolation only.
+// ---------------------------------------------------------------------------
+constexpr int INTERP_BOX = 8192;  // cells (32 KB)
+
+__global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
+                                                           const float *__restrict__ fu, const float *__restrict__ fv,
+                                                           const float *__restrict__ fw, double dti, int first,
+                                                           const int *__restrict__ gate) {
+  if (gate && *gate == 0) return;  // learned form: plain pass not needed
+  const int p = blockIdx.x, c = blockIdx.y;
+  const int nla = b.nla[p];
+  const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
+  const float *F = c == 0 ? fu : (c == 1 ? fv : fw);
+  extern __shared__ __align__(16) unsigned char ibox_sm[];
+  float *box = reinterpret_cast<float *>(ibox_sm);
+  __shared__ int bg[8];
+  if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
+  __syncthreads();
+  const bool boxed = box_ok(bg, INTERP_BOX, g.I, g.J);
+  if (boxed) {
+    load_box(g, F, bg, box);
+    __syncthreads();
+  }
+  double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
+  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
+  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
+  const double *pf = b.pf;
+  const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
+  const CompStencil *csp = b.cs + c * npl + t0;
+  const int ys = bg[5], zs = bg[5] * bg[6];
+  double sF = 0., sa = 0., sb = 0.;
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const long t = t0 + l;
+    const CompStencil s = load_cs(csp + l);
+    float acc;
+    if (boxed) {
+      const float *B = box + box_off(s, bg, g.I, g.J);
+      acc = interp27(s, [&](int i, int j, int k) { return B[i + j * ys + k * zs]; });
+    } else {
+      acc = interp27(s, [&](int i, int j, int k) {
+        return __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
+      });
+    }
+    dud[t] = acc;
+    if (first < 0) continue;
+    const double f = first ? (U[t] - acc) * dti : Fl[t] + (U[t] - acc) * dti;
+    Fl[t] = f;
+    // lever arms of the torque terms of this component:
+    // c=0: (rz, ry), c=1: (rz, rx), c=2: (ry, rx)
+    const double la = c == 2 ? b.yfp[t] - py : b.zfp[t] - pz;
+    const double lb = c == 0 ? b.yfp[t] - py : b.xfp[t] - px;
+    sF += f;
+    sa += la * f;
+    sb += lb * f;
+  }
+  if (first < 0) return;
+  __shared__ double red[3][256];
+  red[0][threadIdx.x] = sF; red[1][threadIdx.x] = sa; red[2][threadIdx.x] = sb;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = red[threadIdx.x][0];
+}
+// per-particle force and torque of updtlagrforces from the component sums
+__global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict__ gate) {
+  if (gate && *gate == 0) return;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= pg.np) return;
+  const double *s = b.psum + (long)p * 9;
+  const double dV = pg.dVlagr;
+  double *pw = b.pf;
+  const double tx = (s[7] - s[4]) * dV, ty = (s[1] - s[8]) * dV, tz = (s[5] - s[2]) * dV;
+  pw[PF_FXLTOT * pg.np + p] = s[0] * dV;
+  pw[PF_FYLTOT * pg.np + p] = s[3] * dV;
+  pw[PF_FZLTOT * pg.np + p] = s[6] * dV;
+  pw[PF_TQX * pg.np + p] = tx;
+  pw[PF_TQY * pg.np + p] = ty;
+  pw[PF_TQZ * pg.np + p] = tz;
+  const double phi = pw[PF_PHI * pg.np + p];
+  pw[PF_TQTHETA * pg.np + p] = (ty * cos(phi)) - (tx * sin(phi));
+}
+int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                              const float *fv, const float *fw, double dt, int first, const int *gate) {
+  if (pg.np == 0) return 0;
+  k_ibm_interp_comp_f<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, first,
+                                                                              gate);
+  if (first < 0) return 1;
+  k_ibm_force_sums<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, gate);
+  return 2;
+}
+
+// ---------------------------------------------------------------------------
+// lagr2eulr spreading of dF = (U_l - u~_l)/dt (or a given increment) with
+// the terms of interp_spread.f90:329-355, F*coeff0*phix*phiy*phiz.  Block
+// (particle, component): contributions accumulate in the particle's box in
+// shared memory, compensated: the rounding error of every shared atomic add
+// is recovered exactly by TwoSum from the value the atomic returned and
+// accumulated in a second box; each touched cell is flushed to HBM with one
+// atomic add of hi+lo.  Boxes beyond SPREAD_BOX cells add per tap instead.
+// ---------------------------------------------------------------------------
+constexpr int SPREAD_BOX = 8192;
+
+__device__ __forceinline__ void box_add(float *hi, float *lo, int c, float v) {
+  const float old = atomicAdd(&hi[c], v);
+  const float s = __fadd_rn(old, v);
+  const float bb = __fsub_rn(s, old);
+  const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+  if (e != 0.f) atomicAdd(&lo[c], e);
+}
+
+__global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
+                                                      float *__restrict__ fv, float *__restrict__ fw, double dti,
+                                                      double coeff0, const float *__restrict__ dfin,
+                                                      const int *__restrict__ gate) {
+  if (gate && *gate == 0) return;  // learned form: plain pass not needed
+  const int p = blockIdx.x, c = blockIdx.y;
+  const int nla = b.nla[p];
+  if (nla <= 0) return;
+  const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
+  float *F = c == 0 ? fu : (c == 1 ? fv : fw);
+  extern __shared__ __align__(16) unsigned char spread_sm[];
+  float *hi = reinterpret_cast<float *>(spread_sm);
+  float *lo = hi + SPREAD_BOX;
+  __shared__ int bg[8];
+  if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
+  __syncthreads();
+  const bool boxed = box_ok(bg, SPREAD_BOX, g.I, g.J);
+  const int nbx = bg[5], nby = bg[6], nbox = nbx * nby * bg[7];
+  if (boxed) {
+    for (int q = threadIdx.x; q < nbox; q += blockDim.x) { hi[q] = 0.f; lo[q] = 0.f; }
+    __syncthreads();
+  }
+  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
+  const double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
+  const CompStencil *csp = b.cs + c * npl + t0;
+  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+    const long t = t0 + l;
+    const CompStencil s = load_cs(csp + l);
+    const float pre = dfin ? (float)(dfin[3 * t + c] * coeff0) : (float)((U[t] - dud[t]) * dti * coeff0);
+    if (boxed) {
+      const int o = box_off(s, bg, g.I, g.J);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float a = pre * s.w[3 + j] * s.w[6 + k];  // the (j,k) factor, then the x weight
+          const int row = o + (k * nby + j) * nbx;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) box_add(hi, lo, row + i, a * s.w[i]);
+        }
+    } else {
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) {
+          const float a = pre * s.w[3 + j] * s.w[6 + k];
+          const int y = wrapm(s.b[1] + j, g.J);
+          for (int i = 0; i < 3; ++i) atomicAdd(&F[fidx(g, wrapm(s.b[0] + i, g.I), y, s.b[2] + k)], a * s.w[i]);
+        }
+    }
+  }
+  if (!boxed) return;
+  __syncthreads();
+  const int nxy = nbx * nby, x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
+  for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
+    const float v = hi[q] + lo[q];
+    if (v != 0.f) {
+      const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
+      atomicAdd(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)], v);
+    }
+  }
+}
+void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
+                         float *fw, double dt, const float *dfin, const int *gate) {
+  if (pg.np == 0) return;
+  const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
+  k_ibm_spread_f<<<dim3(pg.np, 3), 384, 2 * SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0,
+                                                                           dfin, gate);
+}
+
+// ---------------------------------------------------------------------------
+// Learned forcing.  Features of each point after the first forcing pass, in
+// the order they are produced:
+//   [3q + c], q = (k*3 + j)*3 + i = 0..26, c = u, v, w : the velocity
+//            component c at stencil tap q minus the body velocity U_c
+//   [81:84] slip U - u~ after pass 1     [84:87] rigid-body velocity U
+//   [87:90] outward unit normal          [90:93] pass-1 correction F0*dt
+//   [93:96] centre delta weights (x of u, y of v, z of w)
+// X receives them standardised with (mu, isig) and rounded to BF16 for the
+// network, written in 16-byte groups as they are produced; a harvest stores
+// every stride-th point's raw FP32 features and index, for the target written
+// after the plain passes.  The interpolated velocity goes to dudtl as
+// eulr2lagr would.
+// ---------------------------------------------------------------------------
+struct FeatSink {
+  __nv_bfloat16 *x;  // row of the standardised features (or null)
+  float *raw;        // row of the raw features (or null)
+  const float *mu, *isig;
+  float buf[8];
+  int n;  // features produced so far
+  __device__ __forceinline__ void put(float v) {
+    buf[n & 7] = v;
+    ++n;
+    if ((n & 7) == 0) flush(n - 8);
+  }
+  __device__ __forceinline__ void flush(int c0) {
+    if (x) {
+      __nv_bfloat162 h[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        h[e] = __floats2bfloat162_rn((buf[2 * e] - mu[c0 + 2 * e]) * isig[c0 + 2 * e],
+                                     (buf[2 * e + 1] - mu[c0 + 2 * e + 1]) * isig[c0 + 2 * e + 1]);
+      *reinterpret_cast<uint4 *>(x + c0) = *reinterpret_cast<const uint4 *>(h);
+    }
+    if (raw) {
+      *reinterpret_cast<float4 *>(raw + c0) = make_float4(buf[0], buf[1], buf[2], buf[3]);
+      *reinterpret_cast<float4 *>(raw + c0 + 4) = make_float4(buf[4], buf[5], buf[6], buf[7]);
+    }
+  }
+};
+
+__global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, IbmBuffers b, const float *__restrict__ fu,
+                                                        const float *__restrict__ fv, const float *__restrict__ fw,
+                                                        double dt, const float *__restrict__ mu,
+                                                        const float *__restrict__ isig,
+                                                        __nv_bfloat16 *__restrict__ X, HarvestArgs H) {
+  const int n = pg.np * pg.nl;
+  const long npl = n;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int p = t / pg.nl, l = t - p * pg.nl;
+    if (l >= b.nla[p]) {
+      if (X)
+        for (int q = 0; q < 96; q += 8) *reinterpret_cast<uint4 *>(&X[(long)t * 96 + q]) = make_uint4(0, 0, 0, 0);
+      continue;
+    }
+    FeatSink snk;
+    snk.x = X ? X + (long)t * 96 : nullptr;
+    snk.raw = nullptr;
+    snk.mu = mu;
+    snk.isig = isig;
+    snk.n = 0;
+    if (H.feat && (t + H.phase) % H.stride == 0) {
+      const int h = atomicAdd(&H.count[0], 1);
+      if (h < H.cap) {
+        snk.raw = H.feat + (long)h * 96;
+        H.pidx[h] = t;
+      }
+    }
+    const CompStencil su = load_cs(b.cs + t), sv = load_cs(b.cs + npl + t), sw = load_cs(b.cs + 2 * npl + t);
+    auto tap = [&](const float *F, const CompStencil &s, int i, int j, int k) {
+      return __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
+    };
+    if (!snk.x && !snk.raw) {  // interpolation only
+      b.dudtl[t] = interp27(su, [&](int i, int j, int k) { return tap(fu, su, i, j, k); });
+      b.dvdtl[t] = interp27(sv, [&](int i, int j, int k) { return tap(fv, sv, i, j, k); });
+      b.dwdtl[t] = interp27(sw, [&](int i, int j, int k) { return tap(fw, sw, i, j, k); });
+      continue;
+    }
+    const float Ux = (float)b.ul[t], Uy = (float)b.vl[t], Uz = (float)b.wl[t];
+    float au = 0.f, av = 0.f, aw = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float wyzu = su.w[3 + j] * su.w[6 + k], wyzv = sv.w[3 + j] * sv.w[6 + k],
+                    wyzw = sw.w[3 + j] * sw.w[6 + k];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float tu = tap(fu, su, i, j, k), tv = tap(fv, sv, i, j, k), tw = tap(fw, sw, i, j, k);
+          au += tu * (su.w[i] * wyzu);
+          av += tv * (sv.w[i] * wyzv);
+          aw += tw * (sw.w[i] * wyzw);
+          snk.put(tu - Ux);
+          snk.put(tv - Uy);
+          snk.put(tw - Uz);
+        }
+      }
+    b.dudtl[t] = au; b.dvdtl[t] = av; b.dwdtl[t] = aw;
+    const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
+    const float inv_r = (float)(1. / pg.radfp);
+    snk.put(Ux - au); snk.put(Uy - av); snk.put(Uz - aw);
+    snk.put(Ux); snk.put(Uy); snk.put(Uz);
+    snk.put((float)(b.xfp[t] - px) * inv_r);
+    snk.put((float)(b.yfp[t] - py) * inv_r);
+    snk.put((float)(b.zfp[t] - pz) * inv_r);
+    snk.put((float)(b.fxl[t] * dt)); snk.put((float)(b.fyl[t] * dt)); snk.put((float)(b.fzl[t] * dt));
+    snk.put(su.w[1]); snk.put(sv.w[4]); snk.put(sw.w[7]);
+  }
+}
+void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                           const float *fv, const float *fw, double dt, const float *mu, const float *isig,
+                           __nv_bfloat16 *X, const HarvestArgs &H) {
+  if (pg.np == 0) return;
+  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H);
+}
+
+int ibm_set_smem_limits() {
+  cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        2 * SPREAD_BOX * (int)sizeof(float));
+  cudaError_t e2 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        INTERP_BOX * (int)sizeof(float));
+  return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
+}
+
+}  // namespace ibmk

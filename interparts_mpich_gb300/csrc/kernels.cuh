@@ -37,12 +37,23 @@ void launch_f2d(cudaStream_t s, long n, const float *a, double *b);
 // fft_kernels.cu
 // TIn: type of the velocity read by fillps (the forced predictor, or the
 // corrected state for the defect-correction residual); T: FFT type;
+// Optional callback around each of the five kernels of a solve (stage 0
+// fillps + x FFT, 1 y FFT, 2 Thomas, 3 inverse y FFT, 4 inverse x FFT;
+// begin = 1 before the launch, 0 after), for per-kernel event timing.
+struct PoissonHook {
+  void (*fn)(void *arg, int stage, int begin);
+  void *arg;
+  void operator()(int stage, int begin) const {
+    if (fn) fn(arg, stage, begin);
+  }
+};
 // res64: evaluate the divergence in FP64 arithmetic.
 template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
                     const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64 = false,
-                    double2 *thomas_tmp = nullptr);  // FP32 spectrum: FP64 scratch of (I/2+1)*J*K
+                    double2 *thomas_tmp = nullptr,  // FP32 spectrum: FP64 scratch of (I/2+1)*J*K
+                    PoissonHook hook = PoissonHook{nullptr, nullptr});
 template <typename T> int poisson_set_smem_limits();
 
 // ibm_kernels.cu
@@ -50,7 +61,8 @@ struct IbmBuffers {
   // per-point arrays [np*nl]
   double *xfp, *yfp, *zfp, *ul, *vl, *wl, *dudtl, *dvdtl, *dwdtl, *fxl, *fyl, *fzl;
   PointStencil *st;
-  PointStencilF *st32;
+  CompStencil *cs;   // mixed form: [3][np*nl] per-component stencils
+  int *bgeo;         // mixed form: [np][3][8] per-particle stencil boxes
   int *nla;          // [np]
   double *pf;        // particle scalar fields [PF_N*np]
   double *diag;      // [8] force totals etc.
@@ -109,6 +121,8 @@ void launch_mlp_refresh(cudaStream_t s, const float *params, __nv_bfloat16 *w1b,
                         __nv_bfloat16 *w2tb);
 void launch_mlp_infer(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
                       const __nv_bfloat16 *w2b, const float *params, float *y);
+int launch_mlp_infer_tc(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
+                        const __nv_bfloat16 *w2b, const float *params, float *y, int *err);
 void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr);
 void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb);
 void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,

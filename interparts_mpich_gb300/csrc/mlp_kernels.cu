@@ -352,6 +352,214 @@ void launch_mlp_infer(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, con
 }
 
 // ---------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05): one CTA per SM
+// keeps W1 and W2 in shared memory; per tile of 128 rows one elected thread
+// issues layer 1 (M=128, N=128, K=96 as 6 MMAs of K=16) into TMEM columns
+// 0..127, the 4 warps read their 32 TMEM lanes (one row each), add b1,
+// apply GELU, round to BF16 and store the row as layer 2's A operand; layer 2
+// (K=128) goes to TMEM columns 128..255; the epilogue applies b2, GELU, BF16
+// rounding and the FP32 layer 3.  Operands use the no-swizzle K-major
+// layout: 8x8 core matrices (8 rows of 16 bytes) contiguous, LBO = 128 bytes
+// between core matrices along K, SBO = (K/8)*128 bytes between 8-row groups.
+// Every wait is bounded: on a timeout the CTA records err[0] and stops
+// issuing, waits (bounded) for its MMAs in flight and frees its TMEM.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // version 1, no swizzle
+}
+// kind::f16, BF16 A and B (K-major), FP32 D, M = 128, N = 128
+constexpr uint32_t UMMA_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+__device__ __forceinline__ void umma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(UMMA_IDESC), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase, long limit) {
+  for (long it = 0; it < limit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// 32 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+}
+// byte offset of element (row, k) in the no-swizzle K-major layout with K columns
+__host__ __device__ constexpr uint32_t kmaj_off(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+constexpr int TC_M = 128;
+constexpr size_t TC_SMEM = (size_t)(NH * NIN + NH * NH + TC_M * NIN + TC_M * NH) * sizeof(bf16) +
+                           (size_t)(2 * NH + NOUT * NH + 4) * sizeof(float) + 64;
+
+__global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict__ x, int n,
+                                                         const bf16 *__restrict__ w1b, const bf16 *__restrict__ w2b,
+                                                         const float *__restrict__ params, float *__restrict__ y,
+                                                         int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char *W1c = sm;                            // [128 x 96]  K-major
+  unsigned char *W2c = W1c + NH * NIN * 2;            // [128 x 128]
+  unsigned char *Xc = W2c + NH * NH * 2;              // [128 x 96]
+  unsigned char *Hc = Xc + TC_M * NIN * 2;            // [128 x 128]
+  float *cst = reinterpret_cast<float *>(Hc + TC_M * NH * 2);  // b1, b2, W3, b3
+  uint64_t *bar = reinterpret_cast<uint64_t *>(cst + 2 * NH + NOUT * NH + 4);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  int *bad = reinterpret_cast<int *>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // weights into the K-major layouts (16-byte chunks), constants
+  for (int q = tid; q < NH * NIN / 8; q += blockDim.x) {
+    const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+    *reinterpret_cast<uint4 *>(W1c + kmaj_off(r, c8, NIN)) = *reinterpret_cast<const uint4 *>(&w1b[r * NIN + c8]);
+  }
+  for (int q = tid; q < NH * NH / 8; q += blockDim.x) {
+    const int r = q / (NH / 8), c8 = (q % (NH / 8)) * 8;
+    *reinterpret_cast<uint4 *>(W2c + kmaj_off(r, c8, NH)) = *reinterpret_cast<const uint4 *>(&w2b[r * NH + c8]);
+  }
+  for (int t = tid; t < NH; t += blockDim.x) { cst[t] = params[OFF_B1 + t]; cst[NH + t] = params[OFF_B2 + t]; }
+  for (int t = tid; t < NOUT * NH + NOUT; t += blockDim.x) cst[2 * NH + t] = params[OFF_W3 + t];
+  if (warp == 0) {  // 256 TMEM columns: layer-1 and layer-2 accumulators
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tslot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *bad = 0;
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t D1 = tbase, D2 = tbase + 128;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const float *b1 = cst, *b2 = cst + NH, *w3 = cst + 2 * NH, *b3 = w3 + NOUT * NH;
+  const long LIMIT = 1L << 22;
+  uint32_t phase = 0;
+  const int ntiles = (n + TC_M - 1) / TC_M;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long row0 = (long)tile * TC_M;
+    for (int q = tid; q < TC_M * NIN / 8; q += blockDim.x) {
+      const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (row0 + r < n) v = __ldg(reinterpret_cast<const uint4 *>(&x[(row0 + r) * NIN + c8]));
+      *reinterpret_cast<uint4 *>(Xc + kmaj_off(r, c8, NIN)) = v;
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (*bad) break;
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t xa = smem_u32(Xc), wa = smem_u32(W1c);
+#pragma unroll
+      for (int kk = 0; kk < NIN / 16; ++kk)
+        umma_bf16(D1, umma_desc(xa + kk * 256, 128, (NIN / 8) * 128), umma_desc(wa + kk * 256, 128, (NIN / 8) * 128),
+                  kk > 0);
+      umma_commit(bar);
+    }
+    if (!mbar_wait(bar, phase, LIMIT)) { if (err) atomicExch(err, 1); *bad = 1; }
+    phase ^= 1u;
+    tc_fence_after();
+    __syncthreads();
+    if (*bad) break;
+    // epilogue 1: row r = tid, H1 = bf16(gelu(D1 + b1)) into layer 2's A layout
+    const int r = tid;
+#pragma unroll 1
+    for (int cc = 0; cc < NH / 32; ++cc) {
+      float v[32];
+      tmem_ld32(D1 + lane_base + cc * 32, v);
+#pragma unroll
+      for (int c8 = 0; c8 < 32; c8 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int col = cc * 32 + c8 + 2 * e;
+          __nv_bfloat162 h2 = __floats2bfloat162_rn(gelu_f(v[c8 + 2 * e] + b1[col]), gelu_f(v[c8 + 2 * e + 1] + b1[col + 1]));
+          pk[e] = *reinterpret_cast<uint32_t *>(&h2);
+        }
+        *reinterpret_cast<uint4 *>(Hc + kmaj_off(r, cc * 32 + c8, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    tc_fence_before();
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t ha = smem_u32(Hc), wa = smem_u32(W2c);
+#pragma unroll
+      for (int kk = 0; kk < NH / 16; ++kk)
+        umma_bf16(D2, umma_desc(ha + kk * 256, 128, (NH / 8) * 128), umma_desc(wa + kk * 256, 128, (NH / 8) * 128),
+                  kk > 0);
+      umma_commit(bar);
+    }
+    if (!mbar_wait(bar, phase, LIMIT)) { if (err) atomicExch(err, 1); *bad = 1; }
+    phase ^= 1u;
+    tc_fence_after();
+    __syncthreads();
+    if (*bad) break;
+    // epilogue 2: H2 = bf16(gelu(D2 + b2)), y = H2 W3^T + b3 (FP32)
+    float acc[NOUT] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+    for (int cc = 0; cc < NH / 32; ++cc) {
+      float v[32];
+      tmem_ld32(D2 + lane_base + cc * 32, v);
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int col = cc * 32 + q;
+        const float h = __bfloat162float(__float2bfloat16(gelu_f(v[q] + b2[col])));
+#pragma unroll
+        for (int o = 0; o < NOUT; ++o) acc[o] += h * w3[o * NH + col];
+      }
+    }
+    if (row0 + r < n)
+      for (int o = 0; o < NOUT; ++o) y[(row0 + r) * NOUT + o] = acc[o] + b3[o];
+    tc_fence_before();
+    __syncthreads();
+  }
+  // a timed-out MMA may still be running: give it a bounded time to land
+  if (*bad && tid == 0) mbar_wait(bar, phase, LIMIT);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tbase));
+}
+int launch_mlp_infer_tc(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, const bf16 *w2b, const float *params,
+                        float *y, int *err) {
+  if (n <= 0) return 0;
+  const int ntiles = (n + TC_M - 1) / TC_M;
+  const int grid = ntiles < 152 ? ntiles : 152;
+  k_mlp_infer_tc<<<grid, 128, TC_SMEM, s>>>(x, n, w1b, w2b, params, y, err);
+  return 1;
+}
+
+// ---------------------------------------------------------------------------
 // Backward through layer 3, GELU and layer 2 for a batch: dY = 2(Y-T)/B;
 // dH2 = dY W3; dZ2 = dH2 * gelu'(Z2) (bf16); dH1 = dZ2 W2 (tensor cores);
 // dZ1 = dH1 * gelu'(Z1) (bf16).  Bias and W3 gradients accumulate into grad.
@@ -642,7 +850,10 @@ int mlp_set_smem_limits() {
   cudaError_t e3 = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)mlp_backward_smem());
   cudaError_t e4 = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_infer_smem());
-  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess) ? 0 : -1;
+  cudaError_t e5 = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && e5 == cudaSuccess)
+             ? 0
+             : -1;
 }
 
 }  // namespace ibmk

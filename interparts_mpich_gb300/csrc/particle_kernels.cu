@@ -129,6 +129,7 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
   const float radin2f = (float)radin2, rthrf = (float)rthr, radiusf = (float)radius;
   __shared__ double sxm[AX], sxp[AX], srx[AX], sym[AX], syp[AX], sry[AX], szm[AX], szp[AX], srz[AX];
   __shared__ float fxm[AX], fxp[AX], fym[AX], fyp[AX], fzm[AX], fzp[AX];
+  __shared__ float frxh[GEO32 ? AX : 1], frxl[GEO32 ? AX : 1];  // rx as a double-float pair
   __shared__ int queue[GEO32 ? 1 : QCAP];
   __shared__ int qn;
   __shared__ double red[3][256];
@@ -171,6 +172,10 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
         sxm[t] = (mn - cx) * (mn - cx); sxp[t] = (pl - cx) * (pl - cx);
         fxm[t] = (float)sxm[t]; fxp[t] = (float)sxp[t];
         srx[t] = 0. + (i - 0.5) * dx - cx;
+        if constexpr (GEO32) {
+          frxh[t] = (float)srx[t];
+          frxl[t] = (float)(srx[t] - (double)frxh[t]);
+        }
       }
       if (t < nj) {
         const int j = jlow + t;
@@ -204,6 +209,7 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
         const float ymax = fmaxf(fym[tj], fyp[tj]) + fmaxf(fzm[tk], fzp[tk]);
         const long lo = row0 + fidx(g, 0, jlow + tj - 1, klow + tk);
         double s0 = 0., sx = 0.;
+        float s0h = 0.f, s0l = 0.f, sxh = 0.f, sxl = 0.f;  // mixed form: double-float line sums
         for (int ti = 0; ti < ni; ++ti) {
           const float dxp2f = fxp[ti], dxm2f = fxm[ti];
           const float dist2f = dxp2f + yzp;
@@ -213,17 +219,29 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
           } else {
             if (!(dist2f < radin2_lo) && !(dist2f <= radin2_hi) && mind2f > rthr_hi) continue;
           }
-          const double f = F ? (double)F[lo + ti] : 1.;
-          double fw;
-          if (GEO32) {
+          if constexpr (GEO32) {
+            // FP32 velocity times FP32 weight, summed along the line in
+            // double-float (error-free products and sums on the FP32 pipes)
+            const float ff = F ? (float)F[lo + ti] : 1.f;
             float wgt = 1.f;
             if (!(dist2f < radin2f)) {
               const float maxd2f = fmaxf(dxm2f, dxp2f) + ymax;
               if (!(maxd2f < rthrf))
                 wgt = corner_fraction_f(radiusf, dxm2f, dxp2f, fym[tj], fyp[tj], fzm[tk], fzp[tk]);
             }
-            fw = wgt == 1.f ? f : f * (double)wgt;
-          } else {
+            float ph = ff, pe = 0.f;
+            if (wgt != 1.f) two_prod(ff, wgt, ph, pe);
+            df_add(s0h, s0l, ph, pe, s0h, s0l);
+            if (comp != 0) {
+              float qh, ql;
+              df_mul(ph, pe, frxh[ti], frxl[ti], qh, ql);
+              df_add(sxh, sxl, qh, ql, sxh, sxl);
+            }
+            continue;
+          }
+          const double f = F ? (double)F[lo + ti] : 1.;
+          double fw;
+          {
             bool sure = dist2f < radin2_lo;  // surely inside radin
             if (!sure && dist2f > radin2_hi) {
               const float maxd2f = fmaxf(dxm2f, dxp2f) + ymax;
@@ -252,6 +270,10 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
           }
           s0 += fw;
           sx = fma(srx[ti], fw, sx);
+        }
+        if constexpr (GEO32) {
+          s0 = (double)s0h + (double)s0l;
+          sx = (double)sxh + (double)sxl;
         }
         const double ry = sry[tj], rz = srz[tk];
         a0 += s0;

@@ -203,6 +203,23 @@ class IBMSolver:
         if "sync" in self.fn:
             self._chk(self.fn["sync"](self.ctx))
 
+    # --- per-kernel event timing --------------------------------------------------
+
+    PROBE_NAMES = ("predict", "stencil", "interp", "spread", "fillps_fftx", "ffty", "thomas", "ifftx", "correc",
+                   "sphere", "features", "mlp")
+
+    def probe(self, mask: int = (1 << 12) - 1):
+        """Time every launch of the selected kernel classes with CUDA events."""
+        self._chk(self.fn["probe"](self.ctx, int(mask)))
+
+    def probe_result(self) -> dict:
+        """{class: (total ms, launches)} since probe(); stops probing."""
+        n = len(self.PROBE_NAMES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_int * n)()
+        self._chk(self.fn["probe_result"](self.ctx, ms, cnt))
+        return {name: (ms[q], cnt[q]) for q, name in enumerate(self.PROBE_NAMES)}
+
     # --- learned forcing (IBM_MODE_MIXED_LEARNED) ------------------------------
 
     NN_NPARAM = 29315
@@ -259,6 +276,14 @@ class IBMSolver:
         x = np.ascontiguousarray(x, np.float32)
         y = np.zeros((x.shape[0], 3), np.float32)
         self._chk(self.fn["mlp_infer"](self.ctx, _fp(p), _fp(x), x.shape[0], _fp(y)))
+        return y
+
+    def mlp_infer_tc(self, params, x):
+        """Outputs of the tcgen05 inference kernel on one batch."""
+        p = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((x.shape[0], 3), np.float32)
+        self._chk(self.fn["mlp_infer_tc"](self.ctx, _fp(p), _fp(x), x.shape[0], _fp(y)))
         return y
 
     def mlp_fit(self, params, x, t, nsteps: int, lr: float = 1e-3):

@@ -68,6 +68,19 @@ def test_mlp_inference_matches_cpu_reference(gpu_lib, nb):
     assert np.linalg.norm(y - y_train) <= OUT_REL_TOL * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("nb", [16, 128, 1000, 20011])
+def test_mlp_inference_tcgen05_matches_cpu_reference(gpu_lib, nb):
+    """The tcgen05 inference kernel (TMEM accumulators) against the CPU
+    reference and the mma.sync inference kernel."""
+    case = small_case(n=16, nsp=0)
+    g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    p, x, _ = _batch(nb, seed=nb + 7)
+    y = g.mlp_infer_tc(p, x)
+    ref = mlp_ref.forward(p, x)["y"]
+    assert np.linalg.norm(y - ref) <= OUT_REL_TOL * np.linalg.norm(ref)
+    assert np.linalg.norm(y - g.mlp_infer(p, x)) <= OUT_REL_TOL * np.linalg.norm(ref)
+
+
 def test_mlp_adam_steps_match_cpu_reference(gpu_lib):
     case = small_case(n=16, nsp=0)
     g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)

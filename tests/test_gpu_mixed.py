@@ -71,3 +71,4 @@ def test_mixed_collisions_same_contacts(gpu_lib):
         m.rk3_step(2e-3)
         o.rk3_step(2e-3)
     assert m.get_particles().contact_lists() == o.get_particles().contact_lists()
+
