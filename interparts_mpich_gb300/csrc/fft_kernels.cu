@@ -555,17 +555,11 @@ __global__ void __launch_bounds__(256) k_ffty(Geo g, FftPlan ply, typename cpx<T
   }
 }
 
-// Thomas sweep along z for every (kx,ky) (solver.f90:94-134), with the
-// precomputed pivots zt (pivot reciprocal for k<K, denominator for k=K).
-// The recurrence always runs in FP64.  For an FP32 spectrum the forward
-// intermediate goes to an FP64 scratch column (tmp) instead of back into
-// the FP32 spectrum, and the 1/(M*J) FFT scale is applied once in FP32 at
-// the final store (the recurrence is linear), so each element costs two
-// FP32<->FP64 conversions instead of four and no FP64 scale multiply.
+// Thomas sweep along z for every (kx,ky) (solver.f90:94-134), FP64, with
+// the precomputed pivots zt (pivot reciprocal for k<K, denominator for k=K).
 template <typename T>
 __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__restrict__ S,
-                                                const double *__restrict__ zt, double a2, double scale,
-                                                double2 *__restrict__ tmp) {
+                                                const double *__restrict__ zt, double a2, double scale) {
   typedef typename cpx<T>::t C;
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long ncol = (long)g.MX * g.J;
@@ -576,34 +570,14 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
   const double *z = zt + (long)kyy * g.MX + kx;
   const long sstride = (long)g.J * g.MX;
   C *s = S + t;
-  constexpr bool F32 = sizeof(T) == 4;
-  const double lscale = F32 ? 1. : scale;  // FP32: scale applied at the store
-  const float fscale = (float)scale;
   // The recurrence is a dependent chain over k; loads of the next planes
   // are issued in groups of PF so that several are in flight at once.
   constexpr int PF = 8;
   auto ld = [&](int k) -> double2 {
     const C v = s[k * sstride];
-    if constexpr (F32) return make_double2((double)v.x, (double)v.y);
-    else return make_double2((double)v.x * lscale, (double)v.y * lscale);
+    return make_double2((double)v.x * scale, (double)v.y * scale);
   };
-  auto st_mid = [&](int k, double2 v) {  // forward intermediate
-    if constexpr (F32) {
-      tmp[k * ncol + t] = v;
-    } else {
-      C o; o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; s[k * sstride] = o;
-    }
-  };
-  auto ld_mid = [&](int k) -> double2 {
-    if constexpr (F32) return tmp[k * ncol + t];
-    else { const C v = s[k * sstride]; return make_double2((double)v.x, (double)v.y); }
-  };
-  auto st_fin = [&](int k, double2 v) {
-    C o;
-    if constexpr (F32) { o.x = (float)v.x * fscale; o.y = (float)v.y * fscale; }
-    else { o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; }
-    s[k * sstride] = o;
-  };
+  auto st = [&](int k, double2 v) { C o; o.x = (decltype(o.x))v.x; o.y = (decltype(o.y))v.y; s[k * sstride] = o; };
   const int K = g.K;
   double2 prev = make_double2(0., 0.);
   for (int k0 = 0; k0 < K; k0 += PF) {
@@ -632,11 +606,8 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
       prev = cur;
     }
 #pragma unroll
-    for (int q = 0; q < PF; ++q) {
-      const int k = k0 + q;
-      if (k < K - 1) st_mid(k, buf[q]);
-      else if (k == K - 1) st_fin(k, buf[q]);
-    }
+    for (int q = 0; q < PF; ++q)
+      if (k0 + q < K) st(k0 + q, buf[q]);
   }
   // back substitution, d(k) = c(k)*z(k) with c(k) = dzi^2 for k < kmax
   for (int k1 = K - 2; k1 >= 0; k1 -= PF) {
@@ -646,7 +617,8 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
     for (int q = 0; q < PF; ++q) {
       const int k = k1 - q;
       if (k >= 0) {
-        buf[q] = ld_mid(k);
+        const C v = s[k * sstride];
+        buf[q] = make_double2((double)v.x, (double)v.y);
         zb[q] = z[(long)k * zstride];
       }
     }
@@ -661,7 +633,88 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
     }
 #pragma unroll
     for (int q = 0; q < PF; ++q)
-      if (k1 - q >= 0) st_fin(k1 - q, buf[q]);
+      if (k1 - q >= 0) st(k1 - q, buf[q]);
+  }
+}
+
+// Thomas sweep of the mixed form in double-float arithmetic (pairs of FP32
+// with error-free products and sums, ~48 significant bits) on the FP32
+// pipes; GB300 issues FP64 at 1/64 of the FP32 rate.  Tables (built on the
+// host in FP64, split hi + lo): zt[k] for k < K-1 and 1/den for k = K-1 (0
+// for the zero mode), azt[k] = dzi^2 * zt[k] for the back substitution.  The
+// recurrence carries its value in double-float from plane to plane; the
+// forward intermediate between the sweeps is kept in the FP32 spectrum, and
+// the 1/(M*J) FFT scale is applied at the final FP32 store.
+__global__ void __launch_bounds__(128) k_thomas_df(Geo g, float2 *__restrict__ S, const float2 *__restrict__ zt,
+                                                   const float2 *__restrict__ azt, float a2h, float a2l,
+                                                   float fscale) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long ncol = (long)g.MX * g.J;
+  if (t >= ncol) return;
+  const int kx = (int)(t % g.MX), ky = (int)(t / g.MX);
+  const int kyy = ky <= g.J / 2 ? ky : g.J - ky;
+  const long zstride = (long)(g.J / 2 + 1) * g.MX;
+  const float2 *z = zt + (long)kyy * g.MX + kx;
+  const float2 *az = azt + (long)kyy * g.MX + kx;
+  const long sstride = (long)g.J * g.MX;
+  float2 *s = S + t;
+  const int K = g.K;
+  constexpr int PF = 8;
+  // previous plane's value, real and imaginary parts, double-float
+  float prh = 0.f, prl = 0.f, pih = 0.f, pil = 0.f;
+  for (int k0 = 0; k0 < K; k0 += PF) {
+    float2 buf[PF], zb[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k0 + q;
+      if (k < K) { buf[q] = s[k * sstride]; zb[q] = z[(long)k * zstride]; }
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k0 + q;
+      if (k >= K) break;
+      float rh = buf[q].x, rl = 0.f, ih = buf[q].y, il = 0.f;
+      if (k > 0) {  // d - dzi^2 * prev
+        float qh, ql;
+        df_mul(a2h, a2l, prh, prl, qh, ql);
+        df_add(rh, rl, -qh, -ql, rh, rl);
+        df_mul(a2h, a2l, pih, pil, qh, ql);
+        df_add(ih, il, -qh, -ql, ih, il);
+      }
+      // times the pivot reciprocal (k < K-1) or 1/den (k = K-1)
+      df_mul(rh, rl, zb[q].x, zb[q].y, prh, prl);
+      df_mul(ih, il, zb[q].x, zb[q].y, pih, pil);
+      buf[q] = make_float2(__fadd_rn(prh, prl), __fadd_rn(pih, pil));
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k0 + q;
+      if (k < K - 1) s[k * sstride] = buf[q];
+      else if (k == K - 1) s[k * sstride] = make_float2(buf[q].x * fscale, buf[q].y * fscale);
+    }
+  }
+  // back substitution x_k = x'_k - dzi^2 z_k x_{k+1}
+  for (int k1 = K - 2; k1 >= 0; k1 -= PF) {
+    float2 buf[PF], ab[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k1 - q;
+      if (k >= 0) { buf[q] = s[k * sstride]; ab[q] = az[(long)k * zstride]; }
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+      const int k = k1 - q;
+      if (k < 0) break;
+      float qh, ql;
+      df_mul(ab[q].x, ab[q].y, prh, prl, qh, ql);
+      df_add(buf[q].x, 0.f, -qh, -ql, prh, prl);
+      df_mul(ab[q].x, ab[q].y, pih, pil, qh, ql);
+      df_add(buf[q].y, 0.f, -qh, -ql, pih, pil);
+      buf[q] = make_float2(__fadd_rn(prh, prl) * fscale, __fadd_rn(pih, pil) * fscale);
+    }
+#pragma unroll
+    for (int q = 0; q < PF; ++q)
+      if (k1 - q >= 0) s[(k1 - q) * sstride] = buf[q];
   }
 }
 
@@ -708,7 +761,7 @@ template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
                     const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64,
-                    double2 *thomas_tmp, PoissonHook hook) {
+                    const float2 *thomas_df, PoissonHook hook) {
   typedef typename cpx<T>::t C;
   C *S = reinterpret_cast<C *>(spec);
   const int M = g.I / 2;
@@ -730,7 +783,10 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
       const long ncol = (long)g.MX * g.J;
       const double scale = 1.0 / ((double)M * g.J);
       hook(2, 1);
-      k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale, thomas_tmp);
+      const double a2 = g.dzi * g.dzi;
+      const float a2h = (float)a2, a2l = (float)(a2 - (double)a2h);
+      k_thomas_df<<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(
+          g, Sf, thomas_df, thomas_df + (long)g.K * (g.J / 2 + 1) * g.MX, a2h, a2l, (float)scale);
       hook(2, 0);
       hook(3, 1);
       ffty_r(s, g, Sf, tJ, 1);
@@ -764,7 +820,15 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
   const long ncol = (long)g.MX * g.J;
   const double scale = 1.0 / ((double)M * g.J);
   hook(2, 1);
-  k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale, thomas_tmp);
+  if constexpr (sizeof(T) == 4) {
+    const double a2 = g.dzi * g.dzi;
+    const float a2h = (float)a2, a2l = (float)(a2 - (double)a2h);
+    k_thomas_df<<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(
+        g, reinterpret_cast<float2 *>(S), thomas_df, thomas_df + (long)g.K * (g.J / 2 + 1) * g.MX, a2h, a2l,
+        (float)scale);
+  } else {
+    k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale);
+  }
   hook(2, 0);
   hook(3, 1);
   k_ffty<T><<<gy, 256, smy, s>>>(g, ply, S, (const C *)twJ, cols, 1);
@@ -796,11 +860,11 @@ int poisson_set_smem_limits() {
 template void launch_poisson<double, double>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                              const double *, const double *, double *, void *, double *,
                                              const void *, const void *, const void *, const double *, double, double,
-                                             double, int *, bool, double2 *, PoissonHook);
+                                             double, int *, bool, const float2 *, PoissonHook);
 template void launch_poisson<float, float>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                            const float *, const float *, float *, void *, float *, const void *,
                                            const void *, const void *, const double *, double, double, double, int *,
-                                           bool, double2 *, PoissonHook);
+                                           bool, const float2 *, PoissonHook);
 template int poisson_set_smem_limits<double>();
 template int poisson_set_smem_limits<float>();
 

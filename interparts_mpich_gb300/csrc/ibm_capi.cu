@@ -50,7 +50,7 @@ struct ibm_ctx {
   float *ru32 = nullptr, *rv32 = nullptr, *rw32 = nullptr;
   float *fu32 = nullptr, *fv32 = nullptr, *fw32 = nullptr, *phi32 = nullptr;
   void *spec32 = nullptr, *twM32 = nullptr, *twN32 = nullptr, *twJ32 = nullptr;
-  double2 *thomas_tmp = nullptr;  // FP64 forward intermediate of the Thomas sweep (FP32 spectrum)
+  float2 *thomas_df = nullptr;  // mixed form: double-float pivot tables of the Thomas sweep
   double *zt = nullptr;
   void *twM = nullptr, *twN = nullptr, *twJ = nullptr;
   FftPlan plx{}, ply{};
@@ -337,6 +337,23 @@ int build_solver_tables(ibm_ctx *c) {
     }
   if ((st = dalloc(c, &c->zt, z.size()))) return st;
   CK(cudaMemcpyAsync(c->zt, z.data(), z.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->mixed) {
+    // double-float tables of the mixed form: pivots with 1/den in the last
+    // plane (0 for the zero mode, den == 0), and dzi^2 * pivot
+    std::vector<float2> t(2 * z.size());
+    const double a2 = g.dzi * g.dzi;
+    auto split = [](double v) {
+      const float h = (float)v;
+      return make_float2(h, (float)(v - (double)h));
+    };
+    for (size_t q = 0; q < z.size(); ++q) {
+      const bool last = q >= (size_t)(K - 1) * zst;
+      t[q] = split(last ? (z[q] != 0. ? 1. / z[q] : 0.) : z[q]);
+      t[z.size() + q] = split(a2 * z[q]);
+    }
+    if ((st = dalloc(c, &c->thomas_df, t.size()))) return st;
+    CK(cudaMemcpyAsync(c->thomas_df, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+  }
   CK(cudaStreamSynchronize(c->stream));
   return IBM_OK;
 }
@@ -357,7 +374,6 @@ int alloc_all(ibm_ctx *c) {
                       &c->fw32, &c->phi32})
       if ((st = dalloc(c, f, nf))) return st;
     if ((st = dalloc(c, (float2 **)&c->spec32, (size_t)g.K * g.J * g.MX))) return st;
-    if ((st = dalloc(c, &c->thomas_tmp, (size_t)g.K * g.J * g.MX))) return st;
   }
   if ((st = dalloc(c, &c->scratch, 4096))) return st;
   if ((st = dalloc(c, &c->dout, 64))) return st;
@@ -385,7 +401,7 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, &c->pb.mslv, np))) return st;
     if ((st = dalloc(c, &c->pb.rkp, (size_t)RK_N * np))) return st;
     if ((st = dalloc(c, &c->pb.sincos, (size_t)4 * nl))) return st;
-    if ((st = dalloc(c, &c->pb.err, 4))) return st;
+    if ((st = dalloc(c, &c->pb.err, 8))) return st;
     if ((st = dalloc(c, &c->pb.red, (size_t)10 * np))) return st;
     if ((st = dalloc(c, &c->ib.diag, 8))) return st;
     c->ib.pf = c->pb.pf;
@@ -424,9 +440,10 @@ int alloc_all(ibm_ctx *c) {
 
 int check_flags(ibm_ctx *c) {
   if (c->pg.np == 0) return IBM_OK;
-  int h[4];
-  CK(cudaMemcpyAsync(h, c->pb.err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  int h[5];
+  CK(cudaMemcpyAsync(h, c->pb.err, 5 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (h[4]) return set_err(c, IBM_E_NOT_CONVERGED, "a tensor-core MMA wait of the learned forcing timed out");
   if (h[2]) return set_err(c, IBM_E_INVALID, "a Lagrangian point left the grid (non-finite or beyond the walls)");
   if (h[3]) return set_err(c, IBM_E_INVALID, "sphere integration box wider than 128 cells");
   if (h[1]) return set_err(c, IBM_E_CONTACT_OVERFLOW, "a particle exceeded nqmax contacts (param.f90:100)");
@@ -466,7 +483,8 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   HarvestArgs none{};
   PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->norm, c->norm + 96, c->lx,
                         none));
-  PROBED(IBM_PROBE_MLP, launch_mlp_infer(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly));
+  PROBED(IBM_PROBE_MLP, launch_mlp_infer_tc(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly,
+                                            c->pb.err + 4));
   launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
   PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf));
   PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
@@ -542,7 +560,7 @@ int project(ibm_ctx *c, int rkiter, double dt) {
     // FP32 solve of fillps(u*), FP64 Thomas; correction into the FP64 state
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
                                  c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl,
-                                 false, c->thomas_tmp, PoissonHook{poisson_probe, c});
+                                 false, c->thomas_df, PoissonHook{poisson_probe, c});
     LAUNCHED(nl);
     PROBED(IBM_PROBE_CORREC, launch_correc_mixed(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
                         factor * g.dxi, factor * g.dyi, factor * g.dzi));
@@ -553,7 +571,7 @@ int project(ibm_ctx *c, int rkiter, double dt) {
     nl = 0;
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->u32, c->v32, c->w32, c->spec32, c->phi32, c->twM32,
                                  c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl, true,
-                                 c->thomas_tmp, PoissonHook{poisson_probe, c});
+                                 c->thomas_df, PoissonHook{poisson_probe, c});
     LAUNCHED(nl);
     PROBED(IBM_PROBE_CORREC, launch_correc_mixed(c->stream, g, c->u32, c->v32, c->w32, c->phi32, c->u32, c->v32, c->w32, c->p32, c->plo32,
                         factor * g.dxi, factor * g.dyi, factor * g.dzi));
@@ -680,7 +698,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
-                  c->w32, c->p32, c->plo32, c->thomas_tmp, c->ib.psum};
+                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
@@ -874,7 +892,7 @@ int ibm_set_particles(ibm_ctx *c, const ibm_particles *s) {
   for (int p = 0; p < np; ++p)
     for (int t = 0; t < RK_N; ++t) rk[(size_t)p * RK_N + t] = s->rkp[(size_t)p * RK_N + t];
   CK(cudaMemcpyAsync(c->pb.rkp, rk.data(), rk.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemsetAsync(c->pb.err, 0, 4 * sizeof(int), c->stream));
+  CK(cudaMemsetAsync(c->pb.err, 0, 8 * sizeof(int), c->stream));
   if (s->xfp && s->yfp && s->zfp && s->ul && s->vl && s->wl) {
     const size_t npl = (size_t)np * nl;
     const double *la[6] = {s->xfp, s->yfp, s->zfp, s->ul, s->vl, s->wl};

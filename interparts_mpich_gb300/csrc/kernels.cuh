@@ -52,7 +52,7 @@ template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
                     const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64 = false,
-                    double2 *thomas_tmp = nullptr,  // FP32 spectrum: FP64 scratch of (I/2+1)*J*K
+                    const float2 *thomas_df = nullptr,  // FP32 spectrum: double-float pivot tables
                     PoissonHook hook = PoissonHook{nullptr, nullptr});
 template <typename T> int poisson_set_smem_limits();
 
@@ -142,7 +142,7 @@ struct PartBuffers {
   int *mslv;      // [np]
   double *rkp;    // [RK_N*np]
   double *sincos; // [4*nl]: sin(theta), cos(theta), sin(phi), cos(phi)
-  int *err;       // [4] error flags
+  int *err;       // [8] error flags ([4]: learned-forcing MMA wait timeout)
   double *red;    // [10*np]: volume [np], sphere-integral partials [np][3][3]
 };
 template <typename T>

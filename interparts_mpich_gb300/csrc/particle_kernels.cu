@@ -19,16 +19,27 @@ namespace ibmk {
 // new -> old (intgr_nwtn_eulr.f90:77-118)
 // ---------------------------------------------------------------------------
 __global__ void k_save_old(PartGeo pg, PartBuffers b) {
+  // one element per thread: the scalar fields x..coltz and the contact
+  // fields dx..dwt of every master particle into their "old" copies
   const int np = pg.np, nq = pg.nq;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np || b.mslv[p] <= 0) return;
-  for (int f = PF_X; f <= PF_COLTZ; ++f) PF(f + (PF_OX - PF_X)) = PF(f);
-  for (int q = 0; q < nq; ++q)
-    for (int f = CF_DX; f <= CF_DWT; ++f) CFA(f + (CF_ODX - CF_DX), q) = CFA(f, q);
+  const long nps = (long)(PF_COLTZ - PF_X + 1) * np;
+  const long ncf = (long)(CF_DWT - CF_DX + 1) * np * nq;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < nps + ncf; e += (long)gridDim.x * blockDim.x) {
+    if (e < nps) {
+      const int f = PF_X + (int)(e / np), p = (int)(e % np);
+      if (b.mslv[p] > 0) b.pf[(long)(f + (PF_OX - PF_X)) * np + p] = b.pf[(long)f * np + p];
+    } else {
+      const long r = e - nps;
+      const int f = CF_DX + (int)(r / ((long)np * nq));
+      const long pq = r % ((long)np * nq);
+      const int p = (int)(pq / nq);
+      if (b.mslv[p] > 0) b.cf[(long)(f + (CF_ODX - CF_DX)) * np * nq + pq] = b.cf[(long)f * np * nq + pq];
+    }
+  }
 }
 void launch_save_old(cudaStream_t s, const PartGeo &pg, PartBuffers b) {
   if (pg.np == 0) return;
-  k_save_old<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b);
+  k_save_old<<<304, 256, 0, s>>>(pg, b);
 }
 
 // ---------------------------------------------------------------------------
