@@ -200,14 +200,16 @@ int ibm_sync(ibm_ctx *ctx);
 
 /* --- learned forcing (IBM_MODE_MIXED_LEARNED; no counterpart in the reference) -
  *
- * A per-Lagrangian-point network 96 -> 128 -> 128 -> 3 (GELU) replaces the
- * multidirect passes 2..nl_iter of ibm_forcing_loop: one plain pass, the
- * network's prediction of the remaining correction, one spreading of it, and
- * the plain passes as fallback whenever the rms no-slip residual exceeds
- * fallback_ratio x the plain method's.  Features per point (after pass 1):
- * slip, rigid-body velocity, outward normal, u/v/w at the 27 stencil taps
- * relative to the body velocity, the pass-1 correction, centre delta
- * weights.  Target: (F_final - F_pass1) * dt of the plain passes. */
+ * A per-Lagrangian-point network 96 -> 128 -> 128 -> 3 (GELU) collapses the
+ * multidirect passes of ibm_forcing_loop to one sweep plus one inference: the
+ * first pass's interpolation and point forces F0, the network's prediction
+ * of the correction the remaining passes would add, one spreading of
+ * F0 + correction; the plain passes 2..nl_iter run as fallback whenever the
+ * rms no-slip residual exceeds fallback_ratio x the plain method's.
+ * Features per point, from the field the first pass interpolates: u/v/w at
+ * the 27 stencil taps relative to the body velocity, slip, rigid-body
+ * velocity, outward normal, F0*dt, centre delta weights.  Target:
+ * (F_final - F0) * dt of the plain passes. */
 #define IBM_NN_IN     96
 #define IBM_NN_HIDDEN 128
 #define IBM_NN_OUT    3

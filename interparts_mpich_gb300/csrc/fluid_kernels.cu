@@ -119,9 +119,146 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
   }
 }
 
+// FP32 predictor with 2.5D blocking: a 32 x 8 column tile marches along z
+// through a chunk of planes, keeping the planes k-1, k, k+1 of u, v, w and
+// k, k+1 of p (with a one-cell x/y halo, periodic) in shared memory, so each
+// field is read from HBM about once.  Same expressions as k_predict.
+constexpr int PTX = 32, PTY = 8, PHX = PTX + 2, PHY = PTY + 2, PKC = 32;
+template <int STAGE>
+__global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *__restrict__ u,
+                                                            const float *__restrict__ v,
+                                                            const float *__restrict__ w,
+                                                            const float *__restrict__ p, float *__restrict__ ru,
+                                                            float *__restrict__ rv, float *__restrict__ rw,
+                                                            float *__restrict__ fu, float *__restrict__ fv,
+                                                            float *__restrict__ fw, float f1, float f2, float f3) {
+  __shared__ float su[3][PHY][PHX], sv[3][PHY][PHX], sw[3][PHY][PHX], sp[2][PHY][PHX];
+  const int tx = threadIdx.x % PTX, ty = threadIdx.x / PTX;
+  const int i0 = blockIdx.x * PTX, j0 = blockIdx.y * PTY;
+  const int k0 = 1 + blockIdx.z * PKC, k1 = min(g.K, k0 + PKC - 1);
+  const int i = i0 + tx, j = j0 + ty;
+  const bool in = i < g.I && j < g.J;
+  const long PL = (long)g.I * g.J;
+  // halo element e of plane kk into slot
+  auto load_plane = [&](float (*dst)[PHX], const float *__restrict__ F, int kk) {
+    for (int e = threadIdx.x; e < PHY * PHX; e += PTX * PTY) {
+      const int hy = e / PHX, hx = e - hy * PHX;
+      // full periodic wrap: tiles wider than the grid (I or J < 32) reach
+      // beyond one period
+      int gi = (i0 - 1 + hx) % g.I, gj = (j0 - 1 + hy) % g.J;
+      if (gi < 0) gi += g.I;
+      if (gj < 0) gj += g.J;
+      dst[hy][hx] = F[(long)kk * PL + (long)gj * g.I + gi];
+    }
+  };
+  // slots: plane kk lives in slot kk % 3 (u, v, w) and kk % 2 (p)
+  load_plane(su[(k0 - 1) % 3], u, k0 - 1);
+  load_plane(sv[(k0 - 1) % 3], v, k0 - 1);
+  load_plane(sw[(k0 - 1) % 3], w, k0 - 1);
+  load_plane(su[k0 % 3], u, k0);
+  load_plane(sv[k0 % 3], v, k0);
+  load_plane(sw[k0 % 3], w, k0);
+  load_plane(sp[k0 % 2], p, k0);
+  const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi, visc = (float)g.visc;
+  const float q = 0.25f;
+  for (int k = k0; k <= k1; ++k) {
+    load_plane(su[(k + 1) % 3], u, k + 1);
+    load_plane(sv[(k + 1) % 3], v, k + 1);
+    load_plane(sw[(k + 1) % 3], w, k + 1);
+    load_plane(sp[(k + 1) % 2], p, k + 1);
+    __syncthreads();
+    if (in) {
+      const int cm = (k - 1) % 3, c0 = k % 3, cp = (k + 1) % 3;
+      const int x = tx + 1, y = ty + 1;
+      const float U0 = su[c0][y][x], Uip = su[c0][y][x + 1], Uim = su[c0][y][x - 1], Ujp = su[c0][y + 1][x],
+                  Ujm = su[c0][y - 1][x], Ukp = su[cp][y][x], Ukm = su[cm][y][x];
+      const float V0 = sv[c0][y][x], Vip = sv[c0][y][x + 1], Vim = sv[c0][y][x - 1], Vjp = sv[c0][y + 1][x],
+                  Vjm = sv[c0][y - 1][x], Vkp = sv[cp][y][x], Vkm = sv[cm][y][x];
+      const float W0 = sw[c0][y][x], Wip = sw[c0][y][x + 1], Wim = sw[c0][y][x - 1], Wjp = sw[c0][y + 1][x],
+                  Wjm = sw[c0][y - 1][x], Wkp = sw[cp][y][x], Wkm = sw[cm][y][x];
+      const float Vipjm = sv[c0][y - 1][x + 1], Wipkm = sw[cm][y][x + 1];
+      const float Uimjp = su[c0][y + 1][x - 1], Wjpkm = sw[cm][y + 1][x];
+      const float Uimkp = su[cp][y][x - 1], Vjmkp = sv[cp][y - 1][x];
+      float ru_new, rv_new, rw_new;
+      {  // momxad (mom.f90:21-50)
+        const float uuip = q * (Uip + U0) * (Uip + U0);
+        const float uuim = q * (Uim + U0) * (Uim + U0);
+        const float uvjp = q * (Ujp + U0) * (Vip + V0);
+        const float uvjm = q * (Ujm + U0) * (Vipjm + Vjm);
+        const float uwkp = q * (Ukp + U0) * (Wip + W0);
+        const float uwkm = q * (Ukm + U0) * (Wipkm + Wkm);
+        const float dudxp = (Uip - U0) * dxi, dudxm = (U0 - Uim) * dxi;
+        const float dudyp = (Ujp - U0) * dyi, dudym = (U0 - Ujm) * dyi;
+        const float dudzp = (Ukp - U0) * dzi, dudzm = (U0 - Ukm) * dzi;
+        ru_new = dxi * (-uuip + uuim) + visc * (dudxp - dudxm) * dxi + dyi * (-uvjp + uvjm) +
+                 visc * (dudyp - dudym) * dyi + dzi * (-uwkp + uwkm) + visc * (dudzp - dudzm) * dzi;
+      }
+      {  // momyad (mom.f90:94-123)
+        const float uvip = q * (U0 + Ujp) * (V0 + Vip);
+        const float uvim = q * (Uim + Uimjp) * (V0 + Vim);
+        const float vvjp = q * (V0 + Vjp) * (V0 + Vjp);
+        const float vvjm = q * (V0 + Vjm) * (V0 + Vjm);
+        const float wvkp = q * (W0 + Wjp) * (Vkp + V0);
+        const float wvkm = q * (Wkm + Wjpkm) * (Vkm + V0);
+        const float dvdxp = (Vip - V0) * dxi, dvdxm = (V0 - Vim) * dxi;
+        const float dvdyp = (Vjp - V0) * dyi, dvdym = (V0 - Vjm) * dyi;
+        const float dvdzp = (Vkp - V0) * dzi, dvdzm = (V0 - Vkm) * dzi;
+        rv_new = dxi * (-uvip + uvim) + visc * (dvdxp - dvdxm) * dxi + dyi * (-vvjp + vvjm) +
+                 visc * (dvdyp - dvdym) * dyi + dzi * (-wvkp + wvkm) + visc * (dvdzp - dvdzm) * dzi;
+      }
+      {  // momzad (mom.f90:170-199)
+        const float uwip = q * (W0 + Wip) * (U0 + Ukp);
+        const float uwim = q * (W0 + Wim) * (Uim + Uimkp);
+        const float vwjp = q * (W0 + Wjp) * (V0 + Vkp);
+        const float vwjm = q * (W0 + Wjm) * (Vjm + Vjmkp);
+        const float wwkp = q * (W0 + Wkp) * (W0 + Wkp);
+        const float wwkm = q * (W0 + Wkm) * (W0 + Wkm);
+        const float dwdxp = (Wip - W0) * dxi, dwdxm = (W0 - Wim) * dxi;
+        const float dwdyp = (Wjp - W0) * dyi, dwdym = (W0 - Wjm) * dyi;
+        const float dwdzp = (Wkp - W0) * dzi, dwdzm = (W0 - Wkm) * dzi;
+        rw_new = dxi * (-uwip + uwim) + visc * (dwdxp - dwdxm) * dxi + dyi * (-vwjp + vwjm) +
+                 visc * (dwdyp - dwdym) * dyi + dzi * (-wwkp + wwkm) + visc * (dwdzp - dwdzm) * dzi;
+      }
+      // pressure gradient (momxp/momyp/momzp)
+      const float P0 = sp[k % 2][y][x];
+      const float gx = -dxi * (sp[k % 2][y][x + 1] - P0);
+      const float gy = -dyi * (sp[k % 2][y + 1][x] - P0);
+      const float gz = -dzi * (sp[(k + 1) % 2][y][x] - P0);
+      const long c = (long)k * PL + (long)j * g.I + i;
+      float du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
+      if (STAGE == 1) {
+        du = du + f1 * ru_new;
+        dv = dv + f1 * rv_new;
+        dw = dw + f1 * rw_new;
+      } else {
+        du = du + (f2 * ru_new - f3 * ru[c]);
+        dv = dv + (f2 * rv_new - f3 * rv[c]);
+        dw = dw + (f2 * rw_new - f3 * rw[c]);
+      }
+      fu[c] = du;
+      fv[c] = dv;
+      fw[c] = dw;
+      if (STAGE != 3) {
+        ru[c] = ru_new;
+        rv[c] = rv_new;
+        rw[c] = rw_new;
+      }
+    }
+    __syncthreads();  // slot (k-1) % 3 is reloaded next
+  }
+}
+
 template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
                     T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3) {
+  if constexpr (sizeof(T) == 4 && sizeof(TU) == 4) {
+    dim3 grd((g.I + PTX - 1) / PTX, (g.J + PTY - 1) / PTY, (g.K + PKC - 1) / PKC);
+    const float a = (float)f1, b = (float)f2, c = (float)f3;
+    if (stage == 1) k_predict_tiled<1><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
+    else if (stage == 2) k_predict_tiled<2><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
+    else k_predict_tiled<3><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
+    return;
+  }
   dim3 blk(64, 4, 1);
   dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
   if (stage == 1)

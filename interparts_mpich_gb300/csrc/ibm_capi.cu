@@ -471,28 +471,32 @@ int predict(ibm_ctx *c, int rkiter, double dt) {
 }
 
 int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
-  // one plain sweep, one inference, then the plain passes only where the
-  // no-slip residual exceeds fallback_ratio x the plain method's
+  // one sweep plus one inference: the first pass's interpolation and point
+  // forces F0 together with the network features (one kernel), the
+  // network's correction, one spreading of F0 + correction; then the plain
+  // passes 2..Nl only where the no-slip residual exceeds fallback_ratio x
+  // the plain method's
   const Geo &g = c->g;
   const long npts = (long)c->pg.np * c->pg.nl;
   PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
-  PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 1));
-  launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
-  PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt));
-  LAUNCHED(4);
   HarvestArgs none{};
-  PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->norm, c->norm + 96, c->lx,
-                        none));
+  PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt,
+                                                   c->norm, c->norm + 96, c->lx, none, 1));
+  launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
+  LAUNCHED(4);
   PROBED(IBM_PROBE_MLP, launch_mlp_infer_tc(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly,
                                             c->pb.err + 4));
   launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
   PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf));
-  PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
+  PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
+                                                                         c->fv32, c->fw32, dt, -1));
   launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 0);
-  LAUNCHED(7);
+  LAUNCHED(6);
   for (int it = 1; it < nl_iter; ++it) {
-    PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, 0, c->gate));
-    PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate));
+    PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
+                                                                           c->fv32, c->fw32, dt, 0, c->gate));
+    PROBED(IBM_PROBE_SPREAD,
+           launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate));
     LAUNCHED(2);
   }
   return IBM_OK;
@@ -508,20 +512,23 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
     LAUNCHED(1);
     for (int it = 0; it < npass; ++it) {
-      PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, it == 0 ? 1 : 0));
+      PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
+                                                                             c->fv32, c->fw32, dt, it == 0 ? 1 : 0));
       LAUNCHED(1);
+      if (c->harvesting && it == 0) {
+        // features from the field the first pass interpolated (before any
+        // spreading), as the learned loop computes them
+        c->hv.phase = (c->hv.phase + 1) % c->hv.stride;
+        PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt,
+                                                         nullptr, nullptr, nullptr, c->hv, 0));
+        LAUNCHED(1);
+      }
       if (it == 0) {
         launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
         LAUNCHED(1);
       }
       PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt));
       LAUNCHED(1);
-      if (c->harvesting && it == 0) {
-        c->hv.phase = (c->hv.phase + 1) % c->hv.stride;
-        PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, nullptr, nullptr,
-                              c->hv));
-        LAUNCHED(1);
-      }
       if (c->harvesting && it == nl_iter - 1) {
         // the plain method's residual at its own number of passes
         PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));

@@ -283,8 +283,9 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
   k_ibm_harvest_close<<<1, 32, 0, s>>>(H);
 }
 
-// learned update: dF = Y/dt per point, F += dF, and the per-particle force and
-// torque sums of the updated F (as updtlagrforces computes them)
+// learned update: F = F0 + Y/dt per point (Y de-standardised), the total F
+// to dF for the one spreading of the loop, and the per-particle force and
+// torque sums of F (as updtlagrforces computes them)
 __global__ void __launch_bounds__(256) k_ibm_learned_apply(PartGeo pg, IbmBuffers b, const float *__restrict__ Y,
                                                            const float *__restrict__ tmu,
                                                            const float *__restrict__ tsig, double dti,
@@ -298,9 +299,9 @@ __global__ void __launch_bounds__(256) k_ibm_learned_apply(PartGeo pg, IbmBuffer
     const double dx = (double)(Y[3 * t] * tsig[0] + tmu[0]) * dti;
     const double dy = (double)(Y[3 * t + 1] * tsig[1] + tmu[1]) * dti;
     const double dz = (double)(Y[3 * t + 2] * tsig[2] + tmu[2]) * dti;
-    dF[3 * t] = (float)dx; dF[3 * t + 1] = (float)dy; dF[3 * t + 2] = (float)dz;
     const double fx = b.fxl[t] + dx, fy = b.fyl[t] + dy, fz = b.fzl[t] + dz;
     b.fxl[t] = fx; b.fyl[t] = fy; b.fzl[t] = fz;
+    dF[3 * t] = (float)fx; dF[3 * t + 1] = (float)fy; dF[3 * t + 2] = (float)fz;  // total force, spread once
     const double rx = b.xfp[t] - px, ry = b.yfp[t] - py, rz = b.zfp[t] - pz;
     sfx += fx; sfy += fy; sfz += fz;
     stx = stx + ry * fz - rz * fy;

@@ -351,18 +351,21 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
 }
 
 // ---------------------------------------------------------------------------
-// Learned forcing.  Features of each point after the first forcing pass, in
-// the order they are produced:
+// Learned forcing.  Features of each point from the field before the
+// forcing of the substep (the state the first pass interpolates), in the
+// order they are produced:
 //   [3q + c], q = (k*3 + j)*3 + i = 0..26, c = u, v, w : the velocity
 //            component c at stencil tap q minus the body velocity U_c
-//   [81:84] slip U - u~ after pass 1     [84:87] rigid-body velocity U
-//   [87:90] outward unit normal          [90:93] pass-1 correction F0*dt
+//   [81:84] slip U - u~                  [84:87] rigid-body velocity U
+//   [87:90] outward unit normal          [90:93] first-pass force F0*dt
 //   [93:96] centre delta weights (x of u, y of v, z of w)
 // X receives them standardised with (mu, isig) and rounded to BF16 for the
 // network, written in 16-byte groups as they are produced; a harvest stores
 // every stride-th point's raw FP32 features and index, for the target written
 // after the plain passes.  The interpolated velocity goes to dudtl as
-// eulr2lagr would.
+// eulr2lagr would; with first_force the first pass's point force F0 =
+// (U - u~)/dt as well (complagrforces), so one kernel is that pass's
+// interpolation.
 // ---------------------------------------------------------------------------
 struct FeatSink {
   __nv_bfloat16 *x;  // row of the standardised features (or null)
@@ -395,9 +398,11 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
                                                         const float *__restrict__ fv, const float *__restrict__ fw,
                                                         double dt, const float *__restrict__ mu,
                                                         const float *__restrict__ isig,
-                                                        __nv_bfloat16 *__restrict__ X, HarvestArgs H) {
+                                                        __nv_bfloat16 *__restrict__ X, HarvestArgs H,
+                                                        int first_force) {
   const int n = pg.np * pg.nl;
   const long npl = n;
+  const double dti = 1. / dt;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
     if (l >= b.nla[p]) {
@@ -422,10 +427,14 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
     auto tap = [&](const float *F, const CompStencil &s, int i, int j, int k) {
       return __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
     };
-    if (!snk.x && !snk.raw) {  // interpolation only
-      b.dudtl[t] = interp27(su, [&](int i, int j, int k) { return tap(fu, su, i, j, k); });
-      b.dvdtl[t] = interp27(sv, [&](int i, int j, int k) { return tap(fv, sv, i, j, k); });
-      b.dwdtl[t] = interp27(sw, [&](int i, int j, int k) { return tap(fw, sw, i, j, k); });
+    if (!snk.x && !snk.raw) {  // interpolation (and the first-pass force) only
+      const float iu = interp27(su, [&](int i, int j, int k) { return tap(fu, su, i, j, k); });
+      const float iv = interp27(sv, [&](int i, int j, int k) { return tap(fv, sv, i, j, k); });
+      const float iw = interp27(sw, [&](int i, int j, int k) { return tap(fw, sw, i, j, k); });
+      b.dudtl[t] = iu; b.dvdtl[t] = iv; b.dwdtl[t] = iw;
+      if (first_force) {
+        b.fxl[t] = (b.ul[t] - iu) * dti; b.fyl[t] = (b.vl[t] - iv) * dti; b.fzl[t] = (b.wl[t] - iw) * dti;
+      }
       continue;
     }
     const float Ux = (float)b.ul[t], Uy = (float)b.vl[t], Uz = (float)b.wl[t];
@@ -448,6 +457,9 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
         }
       }
     b.dudtl[t] = au; b.dvdtl[t] = av; b.dwdtl[t] = aw;
+    if (first_force) {  // complagrforces of the first pass: F0 = (U - u~)/dt
+      b.fxl[t] = (b.ul[t] - au) * dti; b.fyl[t] = (b.vl[t] - av) * dti; b.fzl[t] = (b.wl[t] - aw) * dti;
+    }
     const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
     const float inv_r = (float)(1. / pg.radfp);
     snk.put(Ux - au); snk.put(Uy - av); snk.put(Uz - aw);
@@ -461,9 +473,9 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
 }
 void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
-                           __nv_bfloat16 *X, const HarvestArgs &H) {
+                           __nv_bfloat16 *X, const HarvestArgs &H, int first_force) {
   if (pg.np == 0) return;
-  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H);
+  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H, first_force);
 }
 
 int ibm_set_smem_limits() {

@@ -96,7 +96,7 @@ struct HarvestArgs {
 };
 void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
-                           __nv_bfloat16 *X, const HarvestArgs &H);
+                           __nv_bfloat16 *X, const HarvestArgs &H, int first_force = 0);
 void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs &H, double dt);
 void launch_ibm_learned_apply(cudaStream_t s, const PartGeo &pg, IbmBuffers b, const float *Y, const float *tmu,
                               const float *tsig, double dt, float *dF);

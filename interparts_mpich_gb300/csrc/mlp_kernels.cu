@@ -416,10 +416,14 @@ __host__ __device__ constexpr uint32_t kmaj_off(int row, int k, int K) {
   return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 constexpr int TC_M = 128;
-constexpr size_t TC_SMEM = (size_t)(NH * NIN + NH * NH + TC_M * NIN + TC_M * NH) * sizeof(bf16) +
-                           (size_t)(2 * NH + NOUT * NH + 4) * sizeof(float) + 64;
+// the layer-2 A operand (H1, 128 x 128) reuses the X tile's space: X is dead
+// once layer 1 has completed, and the next X tile is loaded only after
+// layer 2 has completed; ~91 KB lets two CTAs share an SM
+constexpr int TC_XH = TC_M * NH * 2;  // bytes of the X / H1 region (H1 is the larger)
+constexpr size_t TC_SMEM = (size_t)(NH * NIN + NH * NH) * sizeof(bf16) + TC_XH +
+                           (size_t)(2 * NH + NOUT * NH + 4 + TC_M * 4) * sizeof(float) + 64;
 
-__global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict__ x, int n,
+__global__ void __launch_bounds__(256, 2) k_mlp_infer_tc(const bf16 *__restrict__ x, int n,
                                                          const bf16 *__restrict__ w1b, const bf16 *__restrict__ w2b,
                                                          const float *__restrict__ params, float *__restrict__ y,
                                                          int *__restrict__ err) {
@@ -427,9 +431,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict_
   unsigned char *W1c = sm;                            // [128 x 96]  K-major
   unsigned char *W2c = W1c + NH * NIN * 2;            // [128 x 128]
   unsigned char *Xc = W2c + NH * NH * 2;              // [128 x 96]
-  unsigned char *Hc = Xc + TC_M * NIN * 2;            // [128 x 128]
-  float *cst = reinterpret_cast<float *>(Hc + TC_M * NH * 2);  // b1, b2, W3, b3
-  uint64_t *bar = reinterpret_cast<uint64_t *>(cst + 2 * NH + NOUT * NH + 4);
+  unsigned char *Hc = Xc;                             // [128 x 128], same space
+  float *cst = reinterpret_cast<float *>(Xc + TC_XH);  // b1, b2, W3, b3
+  float *ypart = cst + 2 * NH + NOUT * NH + 4;           // [128][4] layer-3 partials of the upper column half
+  uint64_t *bar = reinterpret_cast<uint64_t *>(ypart + TC_M * 4);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
   int *bad = reinterpret_cast<int *>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -459,7 +464,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict_
   tc_fence_after();
   const uint32_t tbase = *tslot;
   const uint32_t D1 = tbase, D2 = tbase + 128;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  // 8 warps: warp w reads TMEM lanes 32*(w%4).. (rows), columns of half w/4
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+  const int half = warp >> 2;
   const float *b1 = cst, *b2 = cst + NH, *w3 = cst + 2 * NH, *b3 = w3 + NOUT * NH;
   const long LIMIT = 1L << 22;
   uint32_t phase = 0;
@@ -489,10 +496,11 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict_
     tc_fence_after();
     __syncthreads();
     if (*bad) break;
-    // epilogue 1: row r = tid, H1 = bf16(gelu(D1 + b1)) into layer 2's A layout
-    const int r = tid;
+    // epilogue 1: row r, column half `half`: H1 = bf16(gelu(D1 + b1)) into
+    // layer 2's A layout
+    const int r = tid & 127;
 #pragma unroll 1
-    for (int cc = 0; cc < NH / 32; ++cc) {
+    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
       float v[32];
       tmem_ld32(D1 + lane_base + cc * 32, v);
 #pragma unroll
@@ -527,7 +535,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict_
     // epilogue 2: H2 = bf16(gelu(D2 + b2)), y = H2 W3^T + b3 (FP32)
     float acc[NOUT] = {0.f, 0.f, 0.f};
 #pragma unroll 1
-    for (int cc = 0; cc < NH / 32; ++cc) {
+    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
       float v[32];
       tmem_ld32(D2 + lane_base + cc * 32, v);
 #pragma unroll
@@ -538,10 +546,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict_
         for (int o = 0; o < NOUT; ++o) acc[o] += h * w3[o * NH + col];
       }
     }
-    if (row0 + r < n)
-      for (int o = 0; o < NOUT; ++o) y[(row0 + r) * NOUT + o] = acc[o] + b3[o];
+    if (half == 1)
+      for (int o = 0; o < NOUT; ++o) ypart[r * 4 + o] = acc[o];
     tc_fence_before();
     __syncthreads();
+    if (half == 0 && row0 + r < n)
+      for (int o = 0; o < NOUT; ++o) y[(row0 + r) * NOUT + o] = (acc[o] + ypart[r * 4 + o]) + b3[o];
   }
   // a timed-out MMA may still be running: give it a bounded time to land
   if (*bad && tid == 0) mbar_wait(bar, phase, LIMIT);
@@ -554,8 +564,8 @@ int launch_mlp_infer_tc(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, c
                         float *y, int *err) {
   if (n <= 0) return 0;
   const int ntiles = (n + TC_M - 1) / TC_M;
-  const int grid = ntiles < 152 ? ntiles : 152;
-  k_mlp_infer_tc<<<grid, 128, TC_SMEM, s>>>(x, n, w1b, w2b, params, y, err);
+  const int grid = ntiles < 2 * 152 ? ntiles : 2 * 152;
+  k_mlp_infer_tc<<<grid, 256, TC_SMEM, s>>>(x, n, w1b, w2b, params, y, err);
   return 1;
 }
 
