@@ -151,7 +151,13 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # dominant kernels from one ncu capture of the same command, for the roofline's
 # `traffic` key: {(form, kernel class): bytes}
-TRAFFIC = {}
+TRAFFIC = {
+    ("learned", "correc"): 402452992 + 288781568,  # k_correc_mixed
+    ("mixed", "correc"): 402452992 + 288781568,
+    ("learned", "spread"): 238345472 + 39752192,   # k_ibm_spread_f (cold cache)
+    ("mixed", "spread"): 238345472 + 39752192,
+    ("learned", "mlp"): 143344640 + 7269376,       # k_mlp_infer_tc
+}
 
 
 def kernel_model(case, w: int) -> dict:

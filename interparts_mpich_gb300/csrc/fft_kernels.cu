@@ -253,12 +253,16 @@ __host__ __device__ inline int reg_n2(int N) {
   return N == 16 ? 4 : N == 32 ? 4 : N == 64 ? 8 : N == 128 ? 8 : N == 256 ? 16 : 0;
 }
 
+// With phi1 (defect correction, DF): the right-hand side is the divergence
+// residual of the corrected velocity u* - f grad(phi1) (correc's FP32
+// expressions), formed on the fly instead of read from a stored state.
 template <int N1, int N2, bool DF>
 __global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__restrict__ fu,
                                                        const float *__restrict__ fv, float *__restrict__ fw,
                                                        float2 *__restrict__ S, const float2 *__restrict__ twM,
                                                        const float2 *__restrict__ twN, double dtidxi, double dtidyi,
-                                                       double dtidzi) {
+                                                       double dtidzi, const float *__restrict__ phi1, float cfi,
+                                                       float cfj, float cfk) {
   constexpr int M = N1 * N2, ROWS = 128 / N2;
   // group strides padded by 8 elements (64 B): groups sharing a warp start
   // half a bank row apart
@@ -286,13 +290,39 @@ __global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__res
       const float4 w4 = (k == g.K) ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(fw + c);
       const float4 wm4 = *reinterpret_cast<const float4 *>(fw + c - PL);  // plane 0 holds w(0)=0
       if (k == g.K) *reinterpret_cast<float4 *>(fw + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+      const long cjm = c + (j == 0 ? (g.J - 1) * g.I : -g.I);
       const float4 v4 = *reinterpret_cast<const float4 *>(fv + c);
-      const float4 vm4 = *reinterpret_cast<const float4 *>(fv + c + (j == 0 ? (g.J - 1) * g.I : -g.I));
+      const float4 vm4 = *reinterpret_cast<const float4 *>(fv + cjm);
       const float4 u4 = *reinterpret_cast<const float4 *>(fu + c);
-      const float um1 = fu[c + (i0 == 0 ? g.I - 1 : -1)];
-      const float wk[4] = {w4.x, w4.y, w4.z, w4.w}, wkm[4] = {wm4.x, wm4.y, wm4.z, wm4.w};
-      const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, vjm[4] = {vm4.x, vm4.y, vm4.z, vm4.w};
-      const float uu[4] = {u4.x, u4.y, u4.z, u4.w}, uim[4] = {um1, u4.x, u4.y, u4.z};
+      const long cim = c + (i0 == 0 ? g.I - 1 : -1);
+      const float um1 = fu[cim];
+      float wk[4] = {w4.x, w4.y, w4.z, w4.w}, wkm[4] = {wm4.x, wm4.y, wm4.z, wm4.w};
+      float vv[4] = {v4.x, v4.y, v4.z, v4.w}, vjm[4] = {vm4.x, vm4.y, vm4.z, vm4.w};
+      float uu[4] = {u4.x, u4.y, u4.z, u4.w}, uim[4] = {um1, u4.x, u4.y, u4.z};
+      if (DF && phi1) {
+        // u - fi (phi(i+1) - phi(i)) etc. as correc stores them (w = 0 on
+        // the walls k = K and 0)
+        const float4 p4 = *reinterpret_cast<const float4 *>(phi1 + c);
+        const float pim = phi1[cim];
+        const float pip = phi1[c + (i0 + 4 == g.I ? 4 - g.I : 4)];
+        const float4 pjp4 = *reinterpret_cast<const float4 *>(phi1 + c + (j + 1 == g.J ? (1 - g.J) * g.I : g.I));
+        const float4 pjm4 = *reinterpret_cast<const float4 *>(phi1 + cjm);
+        const float4 pkp4 = (k == g.K) ? p4 : *reinterpret_cast<const float4 *>(phi1 + c + PL);
+        const float4 pkm4 = *reinterpret_cast<const float4 *>(phi1 + c - PL);
+        const float P[6] = {pim, p4.x, p4.y, p4.z, p4.w, pip};
+        const float Pjp[4] = {pjp4.x, pjp4.y, pjp4.z, pjp4.w}, Pjm[4] = {pjm4.x, pjm4.y, pjm4.z, pjm4.w};
+        const float Pkp[4] = {pkp4.x, pkp4.y, pkp4.z, pkp4.w}, Pkm[4] = {pkm4.x, pkm4.y, pkm4.z, pkm4.w};
+        for (int e = 0; e < 4; ++e) {
+          const float P0 = P[e + 1];
+          const float un = uu[e] - cfi * (P[e + 2] - P0);
+          const float unm = uim[e] - cfi * (P0 - P[e]);
+          const float vn = vv[e] - cfj * (Pjp[e] - P0);
+          const float vnm = vjm[e] - cfj * (P0 - Pjm[e]);
+          const float wn = (k == g.K) ? 0.f : wk[e] - cfk * (Pkp[e] - P0);
+          const float wnm = (k == 1) ? 0.f : wkm[e] - cfk * (P0 - Pkm[e]);
+          uu[e] = un; uim[e] = unm; vv[e] = vn; vjm[e] = vnm; wk[e] = wn; wkm[e] = wnm;
+        }
+      }
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         if constexpr (DF) {
@@ -399,26 +429,31 @@ __global__ void __launch_bounds__(128) k_ifftx_r(Geo g, const float2 *__restrict
 // dispatch of the register FFT kernels for one length pair (M = I/2, J)
 template <int M1, int M2>
 bool launch_fftx_r(cudaStream_t s, const Geo &g, const float *fu, const float *fv, float *fw, float2 *S,
-                   const float2 *twM, const float2 *twN, double a, double b, double c, bool df, bool inv, float *phi) {
+                   const float2 *twM, const float2 *twN, double a, double b, double c, bool df, bool inv, float *phi,
+                   const PoissonResid &rs) {
   const int nrow = g.J * g.K;
   constexpr int ROWS = 128 / M2;
   const int grid = (nrow + ROWS - 1) / ROWS;
   if (inv) k_ifftx_r<M1, M2><<<grid, 128, 0, s>>>(g, S, phi, twM, twN);
-  else if (df) k_fillps_fftx_r<M1, M2, true><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c);
-  else k_fillps_fftx_r<M1, M2, false><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c);
+  else if (df)
+    k_fillps_fftx_r<M1, M2, true><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c, rs.phi1, rs.fi, rs.fj,
+                                                        rs.fk);
+  else
+    k_fillps_fftx_r<M1, M2, false><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c, nullptr, 0.f, 0.f, 0.f);
   return true;
 }
 bool fftx_r(cudaStream_t s, const Geo &g, const float *fu, const float *fv, float *fw, float2 *S, const float2 *twM,
-            const float2 *twN, double a, double b, double c, bool df, bool inv, float *phi) {
+            const float2 *twN, double a, double b, double c, bool df, bool inv, float *phi, const PoissonResid &rs) {
   switch (g.I / 2) {
-    case 16: return launch_fftx_r<4, 4>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
-    case 32: return launch_fftx_r<8, 4>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
-    case 64: return launch_fftx_r<8, 8>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
-    case 128: return launch_fftx_r<16, 8>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
-    case 256: return launch_fftx_r<16, 16>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi);
+    case 16: return launch_fftx_r<4, 4>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi, rs);
+    case 32: return launch_fftx_r<8, 4>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi, rs);
+    case 64: return launch_fftx_r<8, 8>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi, rs);
+    case 128: return launch_fftx_r<16, 8>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi, rs);
+    case 256: return launch_fftx_r<16, 16>(s, g, fu, fv, fw, S, twM, twN, a, b, c, df, inv, phi, rs);
     default: return false;
   }
 }
+bool poisson_fused_residual_ok(const Geo &g) { return reg_n2(g.I / 2) && reg_n2(g.J) && g.I % 4 == 0; }
 template <int N1, int N2>
 size_t ffty_r_smem() { return (size_t)(256 / N2) * ((N1 * N2 + 1) + N1 * (N2 + 1)) * sizeof(float2); }
 template <int N1, int N2>
@@ -761,7 +796,7 @@ template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
                     const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64,
-                    const float2 *thomas_df, PoissonHook hook) {
+                    const float2 *thomas_df, PoissonHook hook, PoissonResid resid) {
   typedef typename cpx<T>::t C;
   C *S = reinterpret_cast<C *>(spec);
   const int M = g.I / 2;
@@ -775,7 +810,7 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
       const float2 *tM = (const float2 *)twM, *tN = (const float2 *)twN, *tJ = (const float2 *)twJ;
       hook(0, 1);
       fftx_r(s, g, (const float *)fu, (const float *)fv, (float *)fw, Sf, tM, tN, dtidxi, dtidyi, dtidzi, res64, false,
-             nullptr);
+             nullptr, resid);
       hook(0, 0);
       hook(1, 1);
       ffty_r(s, g, Sf, tJ, 0);
@@ -792,7 +827,7 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
       ffty_r(s, g, Sf, tJ, 1);
       hook(3, 0);
       hook(4, 1);
-      fftx_r(s, g, nullptr, nullptr, nullptr, Sf, tM, tN, 0., 0., 0., false, true, (float *)phi);
+      fftx_r(s, g, nullptr, nullptr, nullptr, Sf, tM, tN, 0., 0., 0., false, true, (float *)phi, PoissonResid{});
       hook(4, 0);
       if (launches) *launches += 5;
       return;
@@ -860,11 +895,11 @@ int poisson_set_smem_limits() {
 template void launch_poisson<double, double>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                              const double *, const double *, double *, void *, double *,
                                              const void *, const void *, const void *, const double *, double, double,
-                                             double, int *, bool, const float2 *, PoissonHook);
+                                             double, int *, bool, const float2 *, PoissonHook, PoissonResid);
 template void launch_poisson<float, float>(cudaStream_t, const Geo &, const FftPlan &, const FftPlan &,
                                            const float *, const float *, float *, void *, float *, const void *,
                                            const void *, const void *, const double *, double, double, double, int *,
-                                           bool, const float2 *, PoissonHook);
+                                           bool, const float2 *, PoissonHook, PoissonResid);
 template int poisson_set_smem_limits<double>();
 template int poisson_set_smem_limits<float>();
 

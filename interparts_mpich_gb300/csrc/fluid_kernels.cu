@@ -138,35 +138,52 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
   const int k0 = 1 + blockIdx.z * PKC, k1 = min(g.K, k0 + PKC - 1);
   const int i = i0 + tx, j = j0 + ty;
   const bool in = i < g.I && j < g.J;
-  const long PL = (long)g.I * g.J;
-  // halo element e of plane kk into slot
-  auto load_plane = [&](float (*dst)[PHX], const float *__restrict__ F, int kk) {
-    for (int e = threadIdx.x; e < PHY * PHX; e += PTX * PTY) {
-      const int hy = e / PHX, hx = e - hy * PHX;
-      // full periodic wrap: tiles wider than the grid (I or J < 32) reach
-      // beyond one period
-      int gi = (i0 - 1 + hx) % g.I, gj = (j0 - 1 + hy) % g.J;
-      if (gi < 0) gi += g.I;
-      if (gj < 0) gj += g.J;
-      dst[hy][hx] = F[(long)kk * PL + (long)gj * g.I + gi];
-    }
+  const int PL = g.I * g.J;  // 32-bit offsets: launched only for fields < 2^31 cells
+  // this thread's halo elements (at most two of the PHY*PHX) and their
+  // in-plane offsets, periodic in x and y (full wrap: tiles wider than the
+  // grid reach beyond one period)
+  constexpr int NH = PHY * PHX, NT = PTX * PTY;
+  int hoff[2], hyx[2];
+  bool has[2];
+  for (int q = 0; q < 2; ++q) {
+    const int e = threadIdx.x + q * NT;
+    has[q] = e < NH;
+    const int hy = has[q] ? e / PHX : 0, hx = has[q] ? e - hy * PHX : 0;
+    int gi = (i0 - 1 + hx) % g.I, gj = (j0 - 1 + hy) % g.J;
+    if (gi < 0) gi += g.I;
+    if (gj < 0) gj += g.J;
+    hoff[q] = gj * g.I + gi;
+    hyx[q] = hy * PHX + hx;
+  }
+  // next plane in registers (u, v, w, p for each halo element)
+  float nu[2], nv[2], nw[2], np_[2];
+  auto fetch = [&](int kk) {
+    for (int q = 0; q < 2; ++q)
+      if (has[q]) {
+        const int o = kk * PL + hoff[q];
+        nu[q] = u[o]; nv[q] = v[o]; nw[q] = w[o]; np_[q] = p[o];
+      }
   };
-  // slots: plane kk lives in slot kk % 3 (u, v, w) and kk % 2 (p)
-  load_plane(su[(k0 - 1) % 3], u, k0 - 1);
-  load_plane(sv[(k0 - 1) % 3], v, k0 - 1);
-  load_plane(sw[(k0 - 1) % 3], w, k0 - 1);
-  load_plane(su[k0 % 3], u, k0);
-  load_plane(sv[k0 % 3], v, k0);
-  load_plane(sw[k0 % 3], w, k0);
-  load_plane(sp[k0 % 2], p, k0);
+  auto commit = [&](int kk) {
+    for (int q = 0; q < 2; ++q)
+      if (has[q]) {
+        (&su[kk % 3][0][0])[hyx[q]] = nu[q];
+        (&sv[kk % 3][0][0])[hyx[q]] = nv[q];
+        (&sw[kk % 3][0][0])[hyx[q]] = nw[q];
+        (&sp[kk % 2][0][0])[hyx[q]] = np_[q];
+      }
+  };
+  fetch(k0 - 1);
+  commit(k0 - 1);
+  fetch(k0);
+  commit(k0);
+  fetch(k0 + 1);
   const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi, visc = (float)g.visc;
   const float q = 0.25f;
   for (int k = k0; k <= k1; ++k) {
-    load_plane(su[(k + 1) % 3], u, k + 1);
-    load_plane(sv[(k + 1) % 3], v, k + 1);
-    load_plane(sw[(k + 1) % 3], w, k + 1);
-    load_plane(sp[(k + 1) % 2], p, k + 1);
+    commit(k + 1);  // slots of k-2 (u, v, w) and k-1 (p) are free
     __syncthreads();
+    if (k + 1 <= k1) fetch(k + 2);  // in flight while plane k is computed
     if (in) {
       const int cm = (k - 1) % 3, c0 = k % 3, cp = (k + 1) % 3;
       const int x = tx + 1, y = ty + 1;
@@ -224,7 +241,7 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
       const float gx = -dxi * (sp[k % 2][y][x + 1] - P0);
       const float gy = -dyi * (sp[k % 2][y + 1][x] - P0);
       const float gz = -dzi * (sp[(k + 1) % 2][y][x] - P0);
-      const long c = (long)k * PL + (long)j * g.I + i;
+      const int c = k * PL + j * g.I + i;
       float du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
       if (STAGE == 1) {
         du = du + f1 * ru_new;
@@ -252,12 +269,14 @@ template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
                     T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3) {
   if constexpr (sizeof(T) == 4 && sizeof(TU) == 4) {
+    if (g.nfield < (1L << 31)) {
     dim3 grd((g.I + PTX - 1) / PTX, (g.J + PTY - 1) / PTY, (g.K + PKC - 1) / PKC);
     const float a = (float)f1, b = (float)f2, c = (float)f3;
     if (stage == 1) k_predict_tiled<1><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
     else if (stage == 2) k_predict_tiled<2><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
     else k_predict_tiled<3><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
     return;
+    }
   }
   dim3 blk(64, 4, 1);
   dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
@@ -386,6 +405,63 @@ __global__ void __launch_bounds__(256) k_correc_mixed(Geo g, const float *fu, co
     pl[c - PL] = sl;
   }
 }
+// correc with the defect correction folded in: u = u* - f grad(phi1 + phi2)
+// and pnew += phi1 + phi2 (double-float), one pass over the fields
+__global__ void __launch_bounds__(256) k_correc_mixed2(Geo g, const float *__restrict__ fu,
+                                                       const float *__restrict__ fv, const float *__restrict__ fw,
+                                                       const float *__restrict__ phi1,
+                                                       const float *__restrict__ phi2, float *__restrict__ u,
+                                                       float *__restrict__ v, float *__restrict__ w,
+                                                       float *__restrict__ ph, float *__restrict__ pl, float fi,
+                                                       float fj, float fk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;
+  if (i >= g.I || j >= g.J) return;
+  const int dip = i + 1 == g.I ? 1 - g.I : 1;
+  const int djp = (j + 1 == g.J ? 1 - g.J : 1) * g.I;
+  const long PL = g.plane;
+  const long c = fidx(g, i, j, k);
+  const float a0 = phi1[c], b0 = phi2[c];
+  const float P0 = a0 + b0;
+  const float Pip = phi1[c + dip] + phi2[c + dip];
+  const float Pjp = phi1[c + djp] + phi2[c + djp];
+  const float Pkp = (k == g.K) ? P0 : phi1[c + PL] + phi2[c + PL];
+  const float un = fu[c] - fi * (Pip - P0);
+  const float vn = fv[c] - fj * (Pjp - P0);
+  const float wn = (k == g.K) ? 0.f : fw[c] - fk * (Pkp - P0);
+  u[c] = un;
+  v[c] = vn;
+  w[c] = wn;
+  float sh, sl;
+  df_add(ph[c], pl[c], a0, 0.f, sh, sl);
+  df_add(sh, sl, b0, 0.f, sh, sl);
+  ph[c] = sh;
+  pl[c] = sl;
+  if (k == g.K) {
+    const float sg = g.bc_top == IBM_BC_NOSLIP ? -1.f : 1.f;
+    u[c + PL] = sg * un;
+    v[c + PL] = sg * vn;
+    ph[c + PL] = sh;
+    pl[c + PL] = sl;
+  }
+  if (k == 1) {
+    const float sg = g.bc_bot == IBM_BC_NOSLIP ? -1.f : 1.f;
+    u[c - PL] = sg * un;
+    v[c - PL] = sg * vn;
+    w[c - PL] = 0.f;
+    ph[c - PL] = sh;
+    pl[c - PL] = sl;
+  }
+}
+void launch_correc_mixed2(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
+                          const float *phi1, const float *phi2, float *u, float *v, float *w, float *ph, float *pl,
+                          double fi, double fj, double fk) {
+  dim3 blk(64, 4, 1);
+  dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
+  k_correc_mixed2<<<grd, blk, 0, s>>>(g, fu, fv, fw, phi1, phi2, u, v, w, ph, pl, (float)fi, (float)fj, (float)fk);
+}
+
 void launch_correc_mixed(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
                          const float *phi, float *u, float *v, float *w, float *ph, float *pl, double fi, double fj,
                          double fk) {

@@ -49,6 +49,7 @@ struct ibm_ctx {
   float *plo32 = nullptr;  // pnew = p32 + plo32 (double-float); p is the FP64 staging copy
   float *ru32 = nullptr, *rv32 = nullptr, *rw32 = nullptr;
   float *fu32 = nullptr, *fv32 = nullptr, *fw32 = nullptr, *phi32 = nullptr;
+  float *phi32b = nullptr;  // second (defect-correction) Poisson solution
   void *spec32 = nullptr, *twM32 = nullptr, *twN32 = nullptr, *twJ32 = nullptr;
   float2 *thomas_df = nullptr;  // mixed form: double-float pivot tables of the Thomas sweep
   double *zt = nullptr;
@@ -371,7 +372,7 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, (double2 **)&c->spec, (size_t)g.K * g.J * g.MX))) return st;
   } else {
     for (float **f : {&c->u32, &c->v32, &c->w32, &c->p32, &c->plo32, &c->ru32, &c->rv32, &c->rw32, &c->fu32, &c->fv32,
-                      &c->fw32, &c->phi32})
+                      &c->fw32, &c->phi32, &c->phi32b})
       if ((st = dalloc(c, f, nf))) return st;
     if ((st = dalloc(c, (float2 **)&c->spec32, (size_t)g.K * g.J * g.MX))) return st;
   }
@@ -563,6 +564,29 @@ int project(ibm_ctx *c, int rkiter, double dt) {
   const double dti = 1. / (c->rkab[rkiter - 1] * dt);
   int nl = 0;
   const double factor = c->rkab[rkiter - 1] * dt;
+  if (c->mixed && poisson_fused_residual_ok(g)) {
+    // FP32 solve of fillps(u*) -> phi1; one defect correction: the divergence
+    // residual of u* - f grad(phi1), evaluated in double-float, drives a
+    // second solve -> phi2; then one correction u = u* - f grad(phi1 + phi2),
+    // pnew += phi1 + phi2
+    launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
+                                 c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl,
+                                 false, c->thomas_df, PoissonHook{poisson_probe, c});
+    LAUNCHED(nl);
+    nl = 0;
+    PoissonResid rs;
+    rs.phi1 = c->phi32;
+    rs.fi = (float)(factor * g.dxi); rs.fj = (float)(factor * g.dyi); rs.fk = (float)(factor * g.dzi);
+    launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32b,
+                                 c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl,
+                                 true, c->thomas_df, PoissonHook{poisson_probe, c}, rs);
+    LAUNCHED(nl);
+    PROBED(IBM_PROBE_CORREC, launch_correc_mixed2(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->phi32b,
+                                                  c->u32, c->v32, c->w32, c->p32, c->plo32, factor * g.dxi,
+                                                  factor * g.dyi, factor * g.dzi));
+    LAUNCHED(1);
+    return IBM_OK;
+  }
   if (c->mixed) {
     // FP32 solve of fillps(u*), FP64 Thomas; correction into the FP64 state
     launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
@@ -704,7 +728,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
-                  c->fv32, c->fw32, c->phi32, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
+                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum};
   for (void *q : ptrs)
     if (q) cudaFree(q);

@@ -18,6 +18,9 @@ void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const 
 template <typename TF, typename TPh, typename TU>
 void launch_correc(cudaStream_t s, const Geo &g, const TF *fu, const TF *fv, const TF *fw, const TPh *phi, TU *u,
                    TU *v, TU *w, double *pn, float *pn32, double fi, double fj, double fk);
+void launch_correc_mixed2(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
+                          const float *phi1, const float *phi2, float *u, float *v, float *w, float *ph, float *pl,
+                          double fi, double fj, double fk);
 void launch_correc_mixed(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
                          const float *phi, float *u, float *v, float *w, float *ph, float *pl, double fi, double fj,
                          double fk);
@@ -47,13 +50,21 @@ struct PoissonHook {
     if (fn) fn(arg, stage, begin);
   }
 };
+// Defect-correction right-hand side without a stored corrected state: with
+// phi1 the FP32 register-FFT path forms the divergence residual of
+// u - (fi, fj, fk) grad(phi1) on the fly (poisson_fused_residual_ok).
+struct PoissonResid {
+  const float *phi1 = nullptr;
+  float fi = 0.f, fj = 0.f, fk = 0.f;
+};
+bool poisson_fused_residual_ok(const Geo &g);
 // res64: evaluate the divergence in FP64 arithmetic.
 template <typename TIn, typename T>
 void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftPlan &ply, const TIn *fu,
                     const TIn *fv, TIn *fw, void *spec, T *phi, const void *twM, const void *twN, const void *twJ,
                     const double *zt, double dtidxi, double dtidyi, double dtidzi, int *launches, bool res64 = false,
                     const float2 *thomas_df = nullptr,  // FP32 spectrum: double-float pivot tables
-                    PoissonHook hook = PoissonHook{nullptr, nullptr});
+                    PoissonHook hook = PoissonHook{nullptr, nullptr}, PoissonResid resid = PoissonResid{});
 template <typename T> int poisson_set_smem_limits();
 
 // ibm_kernels.cu
