@@ -404,6 +404,7 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, &c->pb.sincos, (size_t)4 * nl))) return st;
     if ((st = dalloc(c, &c->pb.err, 8))) return st;
     if ((st = dalloc(c, &c->pb.red, (size_t)10 * np))) return st;
+    if ((st = dalloc(c, &c->pb.pos4, (size_t)np))) return st;
     if ((st = dalloc(c, &c->ib.diag, 8))) return st;
     c->ib.pf = c->pb.pf;
     c->ib.err = c->pb.err;
@@ -481,8 +482,9 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   const long npts = (long)c->pg.np * c->pg.nl;
   PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
   HarvestArgs none{};
-  PROBED(IBM_PROBE_FEATURES, launch_ibm_features_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt,
-                                                   c->norm, c->norm + 96, c->lx, none, 1));
+  (void)none;
+  PROBED(IBM_PROBE_FEATURES, launch_ibm_features_comp(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt,
+                                                      c->norm, c->norm + 96, c->lx));
   launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
   LAUNCHED(4);
   PROBED(IBM_PROBE_MLP, launch_mlp_infer_tc(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly,
@@ -727,7 +729,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->twN, c->twJ, c->scratch, c->dout, c->href, c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl,
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
-                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->ru32, c->rv32, c->rw32, c->fu32,
+                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum};
   for (void *q : ptrs)

@@ -352,20 +352,21 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
 
 // ---------------------------------------------------------------------------
 // Learned forcing.  Features of each point from the field before the
-// forcing of the substep (the state the first pass interpolates), in the
-// order they are produced:
-//   [3q + c], q = (k*3 + j)*3 + i = 0..26, c = u, v, w : the velocity
-//            component c at stencil tap q minus the body velocity U_c
-//   [81:84] slip U - u~                  [84:87] rigid-body velocity U
-//   [87:90] outward unit normal          [90:93] first-pass force F0*dt
-//   [93:96] centre delta weights (x of u, y of v, z of w)
+// forcing of the substep (the state the first pass interpolates), 32 per
+// velocity component c = u, v, w at [32c + k]:
+//   k = 0..26   the component at stencil tap q = (kz*3 + jy)*3 + ix minus U_c
+//   k = 27      slip U_c - u~_c            k = 28  rigid-body velocity U_c
+//   k = 29      outward unit normal (c)    k = 30  first-pass force F0_c*dt
+//   k = 31      centre delta weight of the component's own axis
 // X receives them standardised with (mu, isig) and rounded to BF16 for the
-// network, written in 16-byte groups as they are produced; a harvest stores
-// every stride-th point's raw FP32 features and index, for the target written
-// after the plain passes.  The interpolated velocity goes to dudtl as
-// eulr2lagr would; with first_force the first pass's point force F0 =
-// (U - u~)/dt as well (complagrforces), so one kernel is that pass's
-// interpolation.
+// network.  The interpolated velocity goes to dudtl as eulr2lagr would;
+// with first_force the first pass's point force F0 = (U - u~)/dt as well
+// (complagrforces), so the feature kernel is that pass's interpolation.
+// k_ibm_features_comp (one block per particle and component, on the
+// particle's shared-memory box) serves the learned loop; k_ibm_features_f
+// (one thread per point, all components) serves the harvest, which also
+// stores every stride-th point's raw FP32 features and index for the target
+// written after the plain passes.
 // ---------------------------------------------------------------------------
 struct FeatSink {
   __nv_bfloat16 *x;  // row of the standardised features (or null)
@@ -437,38 +438,40 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
       }
       continue;
     }
-    const float Ux = (float)b.ul[t], Uy = (float)b.vl[t], Uz = (float)b.wl[t];
-    float au = 0.f, av = 0.f, aw = 0.f;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const float wyzu = su.w[3 + j] * su.w[6 + k], wyzv = sv.w[3 + j] * sv.w[6 + k],
-                    wyzw = sw.w[3 + j] * sw.w[6 + k];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float tu = tap(fu, su, i, j, k), tv = tap(fv, sv, i, j, k), tw = tap(fw, sw, i, j, k);
-          au += tu * (su.w[i] * wyzu);
-          av += tv * (sv.w[i] * wyzv);
-          aw += tw * (sw.w[i] * wyzw);
-          snk.put(tu - Ux);
-          snk.put(tv - Uy);
-          snk.put(tw - Uz);
-        }
-      }
-    b.dudtl[t] = au; b.dvdtl[t] = av; b.dwdtl[t] = aw;
-    if (first_force) {  // complagrforces of the first pass: F0 = (U - u~)/dt
-      b.fxl[t] = (b.ul[t] - au) * dti; b.fyl[t] = (b.vl[t] - av) * dti; b.fzl[t] = (b.wl[t] - aw) * dti;
-    }
     const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
     const float inv_r = (float)(1. / pg.radfp);
-    snk.put(Ux - au); snk.put(Uy - av); snk.put(Uz - aw);
-    snk.put(Ux); snk.put(Uy); snk.put(Uz);
-    snk.put((float)(b.xfp[t] - px) * inv_r);
-    snk.put((float)(b.yfp[t] - py) * inv_r);
-    snk.put((float)(b.zfp[t] - pz) * inv_r);
-    snk.put((float)(b.fxl[t] * dt)); snk.put((float)(b.fyl[t] * dt)); snk.put((float)(b.fzl[t] * dt));
-    snk.put(su.w[1]); snk.put(sv.w[4]); snk.put(sw.w[7]);
+    const float nrm[3] = {(float)(b.xfp[t] - px) * inv_r, (float)(b.yfp[t] - py) * inv_r,
+                          (float)(b.zfp[t] - pz) * inv_r};
+    const CompStencil *cs3[3] = {&su, &sv, &sw};
+    const float *F3[3] = {fu, fv, fw};
+    const double *U3[3] = {b.ul, b.vl, b.wl};
+    double *D3[3] = {b.dudtl, b.dvdtl, b.dwdtl};
+    double *Fl3[3] = {b.fxl, b.fyl, b.fzl};
+#pragma unroll 1
+    for (int c = 0; c < 3; ++c) {
+      const CompStencil &s = *cs3[c];
+      const float Uc = (float)U3[c][t];
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float wyz = s.w[3 + j] * s.w[6 + k];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const float tv = tap(F3[c], s, i, j, k);
+            acc += tv * (s.w[i] * wyz);
+            snk.put(tv - Uc);
+          }
+        }
+      D3[c][t] = acc;
+      if (first_force) Fl3[c][t] = (U3[c][t] - acc) * dti;
+      snk.put(Uc - acc);
+      snk.put(Uc);
+      snk.put(nrm[c]);
+      snk.put((float)(Fl3[c][t] * dt));
+      snk.put(s.w[3 * c + 1]);
+    }
   }
 }
 void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
@@ -478,12 +481,100 @@ void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmB
   k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H, first_force);
 }
 
+// Features of the learned loop, one block per (particle, component) on the
+// particle's box (same values and order as k_ibm_features_f); also the first
+// pass's interpolation and point forces F0.
+__global__ void __launch_bounds__(256) k_ibm_features_comp(Geo g, PartGeo pg, IbmBuffers b,
+                                                           const float *__restrict__ fu,
+                                                           const float *__restrict__ fv,
+                                                           const float *__restrict__ fw, double dt,
+                                                           const float *__restrict__ mu,
+                                                           const float *__restrict__ isig,
+                                                           __nv_bfloat16 *__restrict__ X) {
+  const int p = blockIdx.x, c = blockIdx.y;
+  const int nla = b.nla[p];
+  const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
+  const float *F = c == 0 ? fu : (c == 1 ? fv : fw);
+  extern __shared__ __align__(16) unsigned char ibox_sm[];
+  float *box = reinterpret_cast<float *>(ibox_sm);
+  __shared__ int bg[8];
+  __shared__ float smu[32], sis[32];
+  if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
+  if (threadIdx.x < 32) { smu[threadIdx.x] = mu[32 * c + threadIdx.x]; sis[threadIdx.x] = isig[32 * c + threadIdx.x]; }
+  __syncthreads();
+  const bool boxed = box_ok(bg, INTERP_BOX, g.I, g.J);
+  if (boxed) {
+    load_box(g, F, bg, box);
+    __syncthreads();
+  }
+  double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
+  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
+  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
+  const double *xc = c == 0 ? b.xfp : (c == 1 ? b.yfp : b.zfp);
+  const double pc = b.pf[(c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z)) * pg.np + p];
+  const float inv_r = (float)(1. / pg.radfp);
+  const double dti = 1. / dt;
+  const CompStencil *csp = b.cs + c * npl + t0;
+  const int ys = bg[5], zs = bg[5] * bg[6];
+  for (int l = threadIdx.x; l < pg.nl; l += blockDim.x) {
+    const long t = t0 + l;
+    __nv_bfloat16 *xr = X + t * 96 + 32 * c;
+    if (l >= nla) {
+      for (int q = 0; q < 32; q += 8) *reinterpret_cast<uint4 *>(xr + q) = make_uint4(0, 0, 0, 0);
+      continue;
+    }
+    const CompStencil s = load_cs(csp + l);
+    const float Uc = (float)U[t];
+    const float *B = boxed ? box + box_off(s, bg, g.I, g.J) : nullptr;
+    float f[32];
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float wyz = s.w[3 + j] * s.w[6 + k];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float tv = boxed ? B[i + j * ys + k * zs]
+                                 : __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
+          acc += tv * (s.w[i] * wyz);
+          f[(k * 3 + j) * 3 + i] = tv - Uc;
+        }
+      }
+    dud[t] = acc;
+    const double F0 = (U[t] - acc) * dti;
+    Fl[t] = F0;
+    f[27] = Uc - acc;
+    f[28] = Uc;
+    f[29] = (float)(xc[t] - pc) * inv_r;
+    f[30] = (float)(F0 * dt);
+    f[31] = s.w[3 * c + 1];
+#pragma unroll
+    for (int q = 0; q < 32; q += 8) {
+      __nv_bfloat162 h[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        h[e] = __floats2bfloat162_rn((f[q + 2 * e] - smu[q + 2 * e]) * sis[q + 2 * e],
+                                     (f[q + 2 * e + 1] - smu[q + 2 * e + 1]) * sis[q + 2 * e + 1]);
+      *reinterpret_cast<uint4 *>(xr + q) = *reinterpret_cast<const uint4 *>(h);
+    }
+  }
+}
+void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                              const float *fv, const float *fw, double dt, const float *mu, const float *isig,
+                              __nv_bfloat16 *X) {
+  if (pg.np == 0) return;
+  k_ibm_features_comp<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X);
+}
+
 int ibm_set_smem_limits() {
   cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         2 * SPREAD_BOX * (int)sizeof(float));
   cudaError_t e2 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         INTERP_BOX * (int)sizeof(float));
-  return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
+  cudaError_t e3 = cudaFuncSetAttribute(k_ibm_features_comp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        INTERP_BOX * (int)sizeof(float));
+  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
 }
 
 }  // namespace ibmk

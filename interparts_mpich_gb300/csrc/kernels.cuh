@@ -108,6 +108,9 @@ struct HarvestArgs {
 void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                            __nv_bfloat16 *X, const HarvestArgs &H, int first_force = 0);
+void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
+                              const float *fv, const float *fw, double dt, const float *mu, const float *isig,
+                              __nv_bfloat16 *X);
 void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs &H, double dt);
 void launch_ibm_learned_apply(cudaStream_t s, const PartGeo &pg, IbmBuffers b, const float *Y, const float *tmu,
                               const float *tsig, double dt, float *dF);
@@ -155,6 +158,7 @@ struct PartBuffers {
   double *sincos; // [4*nl]: sin(theta), cos(theta), sin(phi), cos(phi)
   int *err;       // [8] error flags ([4]: learned-forcing MMA wait timeout)
   double *red;    // [10*np]: volume [np], sphere-integral partials [np][3][3]
+  float4 *pos4;   // [np] FP32 snapshot positions (w: master flag) for the collision filter
 };
 template <typename T>
 void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,

@@ -537,6 +537,8 @@ __global__ void k_snapshot(PartGeo pg, PartBuffers b) {
   PF(PF_SX) = m ? PF(PF_X) : 0.; PF(PF_SY) = m ? PF(PF_Y) : 0.; PF(PF_SZ) = m ? PF(PF_Z) : 0.;
   PF(PF_SU) = m ? PF(PF_U) : 0.; PF(PF_SV) = m ? PF(PF_V) : 0.; PF(PF_SW) = m ? PF(PF_W) : 0.;
   PF(PF_SOMX) = m ? PF(PF_OMX) : 0.; PF(PF_SOMY) = m ? PF(PF_OMY) : 0.; PF(PF_SOMZ) = m ? PF(PF_OMZ) : 0.;
+  // FP32 copy of the snapshot positions for the candidate filter (w: master flag)
+  b.pos4[p] = make_float4((float)PF(PF_SX), (float)PF(PF_SY), (float)PF(PF_SZ), m ? 1.f : 0.f);
 }
 
 // One warp per particle: a coarse FP32 periodic-distance filter selects the
@@ -559,18 +561,22 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   const float thr = 2.1f * (float)radius;
   const float thr2 = thr * thr;
   const float lxf = (float)pg.lx, lyf = (float)pg.ly;
-  const float pxf = (float)PF(PF_SX), pyf = (float)PF(PF_SY), pzf = (float)PF(PF_SZ);
+  const float4 pp = b.pos4[p];
+  const float pxf = pp.x, pyf = pp.y, pzf = pp.z;
   for (int base = 0; base < np; base += 32) {
     const int q = base + lane;
     bool c = false;
-    if (q < np && q != p && b.mslv[q] > 0) {
-      float dxf = fabsf((float)b.pf[(long)PF_SX * np + q] - pxf);
-      float dyf = fabsf((float)b.pf[(long)PF_SY * np + q] - pyf);
-      const float dzf = (float)b.pf[(long)PF_SZ * np + q] - pzf;
-      dxf = fminf(dxf, fabsf(lxf - dxf));
-      dyf = fminf(dyf, fabsf(lyf - dyf));
-      c = dxf * dxf + dyf * dyf + dzf * dzf < thr2;
-      for (int i = 0; i < qmax0 && !c; ++i) c = (fc[i] == b.mslv[q]);
+    if (q < np && q != p) {
+      const float4 qp = b.pos4[q];  // snapshot position, w = 1 for masters
+      if (qp.w != 0.f) {
+        float dxf = fabsf(qp.x - pxf);
+        float dyf = fabsf(qp.y - pyf);
+        const float dzf = qp.z - pzf;
+        dxf = fminf(dxf, fabsf(lxf - dxf));
+        dyf = fminf(dyf, fabsf(lyf - dyf));
+        c = dxf * dxf + dyf * dyf + dzf * dzf < thr2;
+        for (int i = 0; i < qmax0 && !c; ++i) c = (fc[i] == b.mslv[q]);
+      }
     }
     const unsigned m = __ballot_sync(0xffffffffu, c);
     if (c) {
