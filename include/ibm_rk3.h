@@ -162,6 +162,12 @@ int ibm_rk3_step(ibm_ctx *ctx, double dt);
 /* nsteps consecutive RK3 steps with a fixed dt. */
 int ibm_run(ibm_ctx *ctx, double dt, int nsteps);
 
+/* nsteps RK3 steps with the reference's time-step control (main.f90:425-441):
+ * every ioutchk steps chkdiv (IBM_E_DIVERGENCE above a total of 1e-3, as the
+ * reference aborts) and chkdt, then dt = 0.75*dtmax.  dt (in: first step's,
+ * out: current) and time (may be NULL) are updated in place. */
+int ibm_run_adaptive(ibm_ctx *ctx, int nsteps, int ioutchk, double *dt, double *time);
+
 /* --- diagnostics ----------------------------------------------------------- */
 
 /* chkdiv (chkdiv.f90:7-61): total and max |div| of (unew,vnew,wnew) and the

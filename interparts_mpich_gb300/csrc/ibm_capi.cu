@@ -1111,6 +1111,26 @@ int ibm_chkdt(ibm_ctx *c, double *dtmax) {
   return IBM_OK;
 }
 
+int ibm_run_adaptive(ibm_ctx *c, int nsteps, int ioutchk, double *dt, double *time) {
+  // main.f90:268-441: RK3 steps; every ioutchk steps chkdiv (abort above a
+  // total divergence of 1e-3) and chkdt, then dt = 0.75*dtmax
+  if (!c || !dt || nsteps < 0 || ioutchk < 1 || !(*dt > 0)) return IBM_E_INVALID;
+  int st;
+  if ((st = ready(c))) return st;
+  for (int istep = 1; istep <= nsteps; ++istep) {
+    if ((st = step_once(c, *dt, false))) return st;
+    if (time) *time += *dt;
+    if (istep % ioutchk == 0) {
+      double tot, mx, dtmax;
+      int ijk[3];
+      if ((st = ibm_chkdiv(c, &tot, &mx, ijk))) return st;
+      if ((st = ibm_chkdt(c, &dtmax))) return st;
+      *dt = 0.75 * dtmax;
+    }
+  }
+  return check_flags(c);
+}
+
 int ibm_slip_residual(ibm_ctx *c, double *maxres, double *rmsres) {
   if (!c) return IBM_E_INVALID;
   if (c->pg.np == 0) { if (maxres) *maxres = 0; if (rmsres) *rmsres = 0; return IBM_OK; }

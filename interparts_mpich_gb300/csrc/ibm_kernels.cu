@@ -270,9 +270,10 @@ __global__ void k_ibm_harvest_targets(IbmBuffers b, HarvestArgs H, double dt) {
   const int lo = H.count[1], hi = min(H.count[0], H.cap);
   for (int h = lo + blockIdx.x * blockDim.x + threadIdx.x; h < hi; h += gridDim.x * blockDim.x) {
     const int t = H.pidx[h];
-    H.targ[3 * (long)h] = (float)(b.fxl[t] * dt) - H.feat[(long)h * 96 + 90];
-    H.targ[3 * (long)h + 1] = (float)(b.fyl[t] * dt) - H.feat[(long)h * 96 + 91];
-    H.targ[3 * (long)h + 2] = (float)(b.fzl[t] * dt) - H.feat[(long)h * 96 + 92];
+    const float *f = H.feat + (long)h * 96 + FEAT_F0;
+    H.targ[3 * (long)h] = (float)(b.fxl[t] * dt) - f[0];
+    H.targ[3 * (long)h + 1] = (float)(b.fyl[t] * dt) - f[FEAT_PER_COMP];
+    H.targ[3 * (long)h + 2] = (float)(b.fzl[t] * dt) - f[2 * FEAT_PER_COMP];
   }
 }
 __global__ void k_ibm_harvest_close(HarvestArgs H) {

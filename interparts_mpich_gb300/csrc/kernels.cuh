@@ -98,6 +98,9 @@ int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, I
                               const float *fv, const float *fw, double dt, int first, const int *gate = nullptr);
 void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
                          float *fw, double dt, const float *dfin = nullptr, const int *gate = nullptr);
+// feature row of a Lagrangian point: 32 per velocity component c at
+// [FEAT_PER_COMP*c + k]; k = FEAT_F0 holds the first-pass force F0_c*dt
+constexpr int FEAT_PER_COMP = 32, FEAT_F0 = 30;
 struct HarvestArgs {
   float *feat;   // [cap][96] raw features
   int *pidx;     // [cap] point index

@@ -163,6 +163,24 @@ class IBMSolver:
     def run(self, dt: float, nsteps: int):
         self._chk(self.fn["run"](self.ctx, dt, nsteps))
 
+    def run_adaptive(self, nsteps: int, ioutchk: int, dt: float, time: float = 0.0) -> tuple[float, float]:
+        """RK3 steps with the reference's time-step control (main.f90:425-441):
+        every ioutchk steps chkdiv and chkdt, dt = 0.75*dtmax.  Returns (dt, time)."""
+        if "run_adaptive" in self.fn:
+            d, t = C.c_double(dt), C.c_double(time)
+            self._chk(self.fn["run_adaptive"](self.ctx, int(nsteps), int(ioutchk), C.byref(d), C.byref(t)))
+            return d.value, t.value
+        # backends without the entry point (the oracle): the same loop on the host
+        for istep in range(1, nsteps + 1):
+            self.rk3_step(dt)
+            time += dt
+            if istep % ioutchk == 0:
+                tot, _, _ = self.chkdiv()
+                if tot > 1e-3:
+                    raise IBMError(-6, "total divergence > 1e-3 (chkdiv.f90:51-58)")
+                dt = 0.75 * self.chkdt()
+        return dt, time
+
     def timed_step(self, dt: float) -> list[float]:
         self._chk(self.fn["timed_step"](self.ctx, dt))
         ms = (C.c_double * 4)()

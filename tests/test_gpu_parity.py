@@ -163,3 +163,20 @@ def test_settling_sphere(gpu_lib):
     assert pg.w[0] < 0  # it falls
     e = field_errors(g.get_fields(), o.get_fields())
     assert max(e.values()) < 1e-10, e
+
+
+def test_adaptive_time_step_control_matches_oracle(gpu_lib):
+    """main.f90:425-441 on the device: every ioutchk steps chkdt sets
+    dt = 0.75 dtmax; same dt sequence and fields as the oracle's loop."""
+    case = small_case(n=32, nsp=4, seed=21)
+    g = IBMSolver(case)
+    o = OracleSolver(case)
+    g.setup()
+    o.setup()
+    dt0 = 0.5 * o.chkdt()
+    dg, tg = g.run_adaptive(6, 2, dt0)
+    do, to = o.run_adaptive(6, 2, dt0)
+    assert abs(dg - do) <= 1e-12 * do and abs(tg - to) <= 1e-12 * to
+    assert dg != dt0
+    e = field_errors(g.get_fields(), o.get_fields())
+    assert max(e.values()) <= PLAIN_TOL_10STEP, e
