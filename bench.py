@@ -181,6 +181,32 @@ def kernel_model(case, w: int) -> dict:
     }
 
 
+def statistics_timing(solver, case, calls: int) -> dict:
+    """post1d on the final state: the phase indicator and the plane sums on
+    the device, the O(ktot) epilogue on the host.  Kernel times from the
+    event probe; the plane-sum kernel's roofline from its compulsory reads
+    per cell (u, v, w, p, the four phase keys, the three winner codes)."""
+    solver.post1d()  # first call allocates the phase buffers
+    solver.sync()
+    solver.probe((1 << 12) | (1 << 13))
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        solver.post1d()
+    call_ms = (time.perf_counter() - t0) * 1e3 / calls
+    k = solver.probe_result()
+    phase_ms = k["phase"][0] / max(k["phase"][1], 1)
+    sums_ms = k["stats"][0] / max(k["stats"][1], 1)
+    w = 8 if solver.mode == 0 else 4
+    ncell = case.itot * case.jtot * case.ktot
+    bytes_per_cell = 3 * w + 8 + 4 * 8 + 3 * 4
+    ach = ncell * bytes_per_cell / (sums_ms * 1e-3) / 1e9
+    hbm = measured_peaks().get("hbm_gbs", 6800.0)
+    return {"calls": calls, "ms_per_call": round(call_ms, 4), "phase_indicator_ms": round(phase_ms, 4),
+            "plane_sums_ms": round(sums_ms, 4),
+            "plane_sums_roofline": {"bound": "hbm", "algorithmic_per_launch": ncell * bytes_per_cell,
+                                    "achieved": round(ach, 1), "unit": "GB/s", "frac": round(ach / hbm, 4)}}
+
+
 def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     """Times one arithmetic form on the channel case: K steps between CUDA
     events on the library's stream, plus the per-phase times of one step."""
@@ -238,6 +264,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
     _, divmax, _ = solver.chkdiv()
+    stats = statistics_timing(solver, case, args.stats_calls) if args.stats_calls > 0 else None
     if learn is not None:
         st = solver.learned_stats()
         learn.update({"learned_rms_residual_last": st["last_rms"], "fallbacks": int(st["fallbacks"]),
@@ -277,7 +304,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver.close()
     return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
             "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn,
-            "kernels": kernels}
+            "kernels": kernels, "stats": stats}
 
 
 def cpu_baseline(args, case_fn):
@@ -293,9 +320,13 @@ def cpu_baseline(args, case_fn):
     t0 = time.perf_counter()
     o.rk3_step(dt)
     t = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    o.post1d()
+    t_stats = (time.perf_counter() - t0) * 1e3
     o.close()
     return {"value": round(t, 1), "unit": "ms/step", "cores": int(cores), "kind": "port",
-            "sample": f"1 RK3 step of the same {case.itot}^3 / {case.np}-sphere case (oracle restatement, OpenMP)"}
+            "sample": f"1 RK3 step of the same {case.itot}^3 / {case.np}-sphere case (oracle restatement, OpenMP)",
+            "post1d_ms": round(t_stats, 1)}
 
 
 def main():
@@ -313,6 +344,7 @@ def main():
     ap.add_argument("--harvest-passes", type=int, default=6)
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=8192)
+    ap.add_argument("--stats-calls", type=int, default=3, help="post1d calls timed after the steps (0: none)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -402,6 +434,7 @@ def main():
                       "phases_ms": {n: round(t, 4) for n, t in zip(names, x["phases"])},
                       "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"]),
                       "kernels": kernel_table(x, 8 if f == "plain" else 4),
+                      **({"post1d": x["stats"]} if x["stats"] else {}),
                       **({"learned_forcing": x["learn"]} if x["learn"] else {})} for f, x in res.items()},
         "mcell_steps_per_s": round(args.gpus * r["ncell"] / (r["ms"] * 1e-3) / 1e6, 1),
         "hbm_roofline_frac_step": round(ab["total"] / (r["ms"] * 1e-3) / 1e9 / hbm, 4),

@@ -184,6 +184,90 @@ int ibm_slip_residual(ibm_ctx *ctx, double *maxres, double *rmsres);
 int ibm_diagnostics(ibm_ctx *ctx, double *wallshearnew, double *wallshearold,
                     double forcetot[3]);
 
+/* --- scalar field (runmodes 1001-1003) --------------------------------------- */
+
+#define IBM_BC_C_DIRICHLET 0        /* 'BC_DIRICHLET' (bound.f90:113-122)           */
+#define IBM_BC_C_NEUMANN   1        /* 'BC_NEUMANN'   (bound.f90:124-132)           */
+
+typedef struct ibm_scalar_params {
+  double pran;                      /* Prandtl number: kappa = visc/Pran (init.f90:94) */
+  double beta;                      /* expansion coefficient (param.f90:47)        */
+  double bc_c_top_val, bc_c_bot_val;/* wall values (param.f90:41-42)               */
+  int    bc_c_top_type, bc_c_bot_type; /* IBM_BC_C_* (param.f90:39-40)             */
+} ibm_scalar_params;
+
+/* Scalar field cnew and its stored right-hand side dcrkold (main.f90:49),
+ * reference layout (0:i1,0:j1,0:k1), and the scalar parameters.  The set
+ * applies boundscal (bound.f90:109-171) as the driver does after loading
+ * (main.f90:198); dcrk may be NULL (zero).  Once set, every RK substep
+ * transports the scalar (scalad, scal.f90:11-58, in rk1..rk3, rk3.f90:13-329;
+ * cnew = dcdt and boundscal after the projection, main.f90:374-376) and adds
+ * the buoyancy momzbuoy (mom.f90:233-259) to the w right-hand side.  Without
+ * a call the scalar is zero and stays zero, as it does in the reference with
+ * zero wall values. */
+int ibm_set_scalar(ibm_ctx *ctx, const ibm_scalar_params *sp, const double *c, const double *dcrk);
+int ibm_get_scalar(ibm_ctx *ctx, double *c, double *dcrk);
+
+/* --- plane statistics (post1d, output.f90:13-917) ------------------------------ */
+
+/* phase_indicator (phase_indicator.f90:11-559) on one rank: fluid fractions
+ * gamu..gamp of the u, v, w and pressure cells (1 = fluid) and the rigid-body
+ * velocity of the particle occupying each cell, reference layout
+ * (0:i1,0:j1,0:k1) with the reference's halos and wall ghost planes.
+ * itype 1: translation + rotation on the velocity cells; itype 0: angular
+ * velocity on the pressure cells.  Any output pointer may be NULL.  The
+ * fractions are bit-identical to the reference's arithmetic. */
+int ibm_phase_indicator(ibm_ctx *ctx, int itype, double *gamu, double *gamv, double *gamw,
+                        double *gamp, double *upart, double *vpart, double *wpart);
+
+/* Profiles of post1d, each ktot+2 values k = 0..k1, quantity-major:
+ * profiles[IBM_STAT_x*(ktot+2) + k].  Entries the reference leaves unset
+ * (gwm(0), gpm/cm/c2/wc/cdflx ghost planes, ss/ssp(k1)) are 0. */
+#define IBM_STAT_UM    0   /* phase-averaged mean velocity and pressure       */
+#define IBM_STAT_VM    1
+#define IBM_STAT_WM    2
+#define IBM_STAT_PM    3
+#define IBM_STAT_U2    4   /* rms                                              */
+#define IBM_STAT_V2    5
+#define IBM_STAT_W2    6
+#define IBM_STAT_P2    7
+#define IBM_STAT_UV    8   /* plane sums of the fluid-weighted products        */
+#define IBM_STAT_UW    9
+#define IBM_STAT_VW    10  /* Reynolds stress v'w'                             */
+#define IBM_STAT_UPM   11  /* solid-phase rigid-body velocity                  */
+#define IBM_STAT_VPM   12
+#define IBM_STAT_WPM   13
+#define IBM_STAT_UP2   14
+#define IBM_STAT_VP2   15
+#define IBM_STAT_WP2   16
+#define IBM_STAT_UPVP  17
+#define IBM_STAT_UPWP  18
+#define IBM_STAT_VPWP  19
+#define IBM_STAT_GUM   20  /* plane sums of the fluid fractions                */
+#define IBM_STAT_GVM   21
+#define IBM_STAT_GWM   22
+#define IBM_STAT_GPM   23
+#define IBM_STAT_GP2   24
+#define IBM_STAT_GUV   25
+#define IBM_STAT_GUW   26
+#define IBM_STAT_GVW   27
+#define IBM_STAT_SS    28  /* viscous shear stress, fluid and particle phase   */
+#define IBM_STAT_SSP   29
+#define IBM_STAT_CM    30  /* scalar mean, rms, convective and diffusive flux  */
+#define IBM_STAT_C2    31
+#define IBM_STAT_WC    32
+#define IBM_STAT_CDFLX 33
+#define IBM_NSTAT      34
+/* scalars[]: Re_tau, u_tau, Nu, Re_RBC, grad_k_wall (output.f90:465-477) */
+#define IBM_NSTAT_SCALAR 5
+
+/* post1d (output.f90:13-917) without its file output: phase_indicator(itype
+ * 1) when np > 0, the plane sums of output.f90:88-364 as device reductions,
+ * then the reference's ghost values, normalisations and derived scalars.
+ * profiles: IBM_NSTAT*(ktot+2) doubles; scalars: IBM_NSTAT_SCALAR doubles
+ * (either may be NULL). */
+int ibm_post1d(ibm_ctx *ctx, double *profiles, double *scalars);
+
 /* --- streams and timing ------------------------------------------------------ */
 
 /* Runs all further work of the context on the given cudaStream_t (NULL:
@@ -277,7 +361,9 @@ int ibm_mlp_fit(ibm_ctx *ctx, const float *params_in, const float *x, const floa
 #define IBM_PROBE_SPHERE      9   /* sphere integrals                            */
 #define IBM_PROBE_FEATURES    10  /* learned forcing: features                   */
 #define IBM_PROBE_MLP         11  /* learned forcing: network inference         */
-#define IBM_PROBE_N           12
+#define IBM_PROBE_PHASE       12  /* statistics: phase indicator (both passes)   */
+#define IBM_PROBE_STATS       13  /* statistics: plane sums of post1d            */
+#define IBM_PROBE_N           14
 /* Records CUDA events on the context stream around every launch of the
  * selected classes from now on (a profiler-free per-kernel timer; the events
  * add no GPU work).  ibm_probe_result synchronises, returns per class the

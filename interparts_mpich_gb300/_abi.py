@@ -29,6 +29,15 @@ IBM_MODE_PLAIN_FP64 = 0
 IBM_MODE_MIXED = 1
 IBM_MODE_MIXED_LEARNED = 2
 
+IBM_BC_C_DIRICHLET = 0
+IBM_BC_C_NEUMANN = 1
+
+# post1d profiles (include/ibm_rk3.h IBM_STAT_*), in order
+STAT_NAMES = ("um", "vm", "wm", "pm", "u2", "v2", "w2", "p2", "uv", "uw", "vw", "upm", "vpm", "wpm",
+              "up2", "vp2", "wp2", "upvp", "upwp", "vpwp", "gum", "gvm", "gwm", "gpm", "gp2", "guv",
+              "guw", "gvw", "ss", "ssp", "cm", "c2", "wc", "cdflx")
+STAT_SCALAR_NAMES = ("re_tau", "u_tau", "nu", "re_rbc", "grad_k_wall")
+
 
 class IbmParams(C.Structure):
     _fields_ = [
@@ -54,6 +63,11 @@ LAGRANGIAN_ARRAYS = ["xfp", "yfp", "zfp", "ul", "vl", "wl", "fxl", "fyl", "fzl"]
 RKP_FIELDS = ["fxltot", "fyltot", "fzltot", "torqxltot", "torqyltot", "torqzltot", "torqtheta",
               "colfx", "colfy", "colfz", "coltx", "colty", "coltz", "dudt", "dvdt", "dwdt",
               "domxdt", "domydt", "domzdt"]
+
+
+class IbmScalarParams(C.Structure):
+    _fields_ = [("pran", C.c_double), ("beta", C.c_double), ("bc_c_top_val", C.c_double),
+                ("bc_c_bot_val", C.c_double), ("bc_c_top_type", C.c_int), ("bc_c_bot_type", C.c_int)]
 
 
 class IbmParticles(C.Structure):
@@ -141,6 +155,10 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "chkdt": (C.c_int, [ctx, c_double_p]),
         "slip_residual": (C.c_int, [ctx, c_double_p, c_double_p]),
         "diagnostics": (C.c_int, [ctx, c_double_p, c_double_p, c_double_p]),
+        "set_scalar": (C.c_int, [ctx, P(IbmScalarParams), c_double_p, c_double_p]),
+        "get_scalar": (C.c_int, [ctx, c_double_p, c_double_p]),
+        "phase_indicator": (C.c_int, [ctx, C.c_int] + [c_double_p] * 7),
+        "post1d": (C.c_int, [ctx, c_double_p, c_double_p]),
     }
     optional = {
         "abi_version": (C.c_int, []),

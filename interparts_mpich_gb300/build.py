@@ -23,7 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
           "-Xptxas", "-warn-spills"]
 # Sources whose FP64 arithmetic must keep the reference's separate
 # multiply/add roundings (stencil indices, contact decisions).
-NO_FMA = {"ibm_kernels.cu", "particle_kernels.cu"}
+NO_FMA = {"ibm_kernels.cu", "particle_kernels.cu", "stats_kernels.cu"}
 
 
 def nvcc() -> str:

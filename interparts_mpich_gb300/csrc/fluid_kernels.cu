@@ -4,6 +4,8 @@
 // One thread per interior cell; x/y neighbours by periodic wrap, z ghosts
 // stored.  All arithmetic follows the reference expression order; FP64
 // fused multiply-add contraction is allowed (differences at 1 ulp level).
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace ibmk {
@@ -20,7 +22,7 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
                                                  const TU *__restrict__ w, const TU *__restrict__ p,
                                                  T *__restrict__ ru, T *__restrict__ rv, T *__restrict__ rw,
                                                  T *__restrict__ fu, T *__restrict__ fv, T *__restrict__ fw,
-                                                 T f1, T f2, T f3) {
+                                                 T f1, T f2, T f3, const double *__restrict__ cb, double bcoef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z + 1;
@@ -94,6 +96,8 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
     rw_new = dxi * (-uwip + uwim) + visc * (dwdxp - dwdxm) * dxi + dyi * (-vwjp + vwjm) +
              visc * (dwdyp - dwdym) * dyi + dzi * (-wwkp + wwkm) + visc * (dwdzp - dwdzm) * dzi;
   }
+  // momzbuoy (mom.f90:251), added as rk1..rk3 do (rk3.f90:56-58)
+  if (cb) rw_new = (T)(bcoef * (cb[c] + cb[c + PL])) + rw_new;
   // pressure gradient (momxp/momyp/momzp)
   const T P0 = (T)p[c];
   const T gx = -dxi * ((T)p[at(ip, j0, 0)] - P0);
@@ -131,7 +135,8 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
                                                             const float *__restrict__ p, float *__restrict__ ru,
                                                             float *__restrict__ rv, float *__restrict__ rw,
                                                             float *__restrict__ fu, float *__restrict__ fv,
-                                                            float *__restrict__ fw, float f1, float f2, float f3) {
+                                                            float *__restrict__ fw, float f1, float f2, float f3,
+                                                            const double *__restrict__ cb, double bcoef) {
   __shared__ float su[3][PHY][PHX], sv[3][PHY][PHX], sw[3][PHY][PHX], sp[2][PHY][PHX];
   const int tx = threadIdx.x % PTX, ty = threadIdx.x / PTX;
   const int i0 = blockIdx.x * PTX, j0 = blockIdx.y * PTY;
@@ -242,6 +247,7 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
       const float gy = -dyi * (sp[k % 2][y + 1][x] - P0);
       const float gz = -dzi * (sp[(k + 1) % 2][y][x] - P0);
       const int c = k * PL + j * g.I + i;
+      if (cb) rw_new = (float)(bcoef * (cb[c] + cb[c + PL])) + rw_new;  // momzbuoy
       float du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
       if (STAGE == 1) {
         du = du + f1 * ru_new;
@@ -267,32 +273,103 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
 
 template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
-                    T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3) {
+                    T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3, const double *cb,
+                    double bcoef) {
   if constexpr (sizeof(T) == 4 && sizeof(TU) == 4) {
     if (g.nfield < (1L << 31)) {
     dim3 grd((g.I + PTX - 1) / PTX, (g.J + PTY - 1) / PTY, (g.K + PKC - 1) / PKC);
     const float a = (float)f1, b = (float)f2, c = (float)f3;
-    if (stage == 1) k_predict_tiled<1><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
-    else if (stage == 2) k_predict_tiled<2><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
-    else k_predict_tiled<3><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c);
+    if (stage == 1)
+      k_predict_tiled<1><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
+    else if (stage == 2)
+      k_predict_tiled<2><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
+    else
+      k_predict_tiled<3><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
     return;
     }
   }
   dim3 blk(64, 4, 1);
   dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
   if (stage == 1)
-    k_predict<TU, T, 1><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+    k_predict<TU, T, 1><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3, cb, bcoef);
   else if (stage == 2)
-    k_predict<TU, T, 2><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+    k_predict<TU, T, 2><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3, cb, bcoef);
   else
-    k_predict<TU, T, 3><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3);
+    k_predict<TU, T, 3><<<grd, blk, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, (T)f1, (T)f2, (T)f3, cb, bcoef);
 }
 template void launch_predict<double, double>(cudaStream_t, const Geo &, int, const double *, const double *,
                                              const double *, const double *, double *, double *, double *,
-                                             double *, double *, double *, double, double, double);
+                                             double *, double *, double *, double, double, double, const double *,
+                                             double);
 template void launch_predict<float, float>(cudaStream_t, const Geo &, int, const float *, const float *,
                                            const float *, const float *, float *, float *, float *, float *,
-                                           float *, float *, double, double, double);
+                                           float *, float *, double, double, double, const double *, double);
+
+// ---------------------------------------------------------------------------
+// Scalar: scalad (scal.f90:11-58) fused with the dcdt update of rk1..rk3
+// (rk3.f90:48,78 / 151,188 / 266,300).  STAGE 1: cnext = c + f1*RHS,
+// rhs_old = RHS; STAGE 2/3: cnext = c + (f2*RHS - f3*rhs_old), stage 2 stores
+// rhs_old = RHS.  cnext becomes cnew after the projection (main.f90:374-376).
+// ---------------------------------------------------------------------------
+template <typename TU, int STAGE>
+__global__ void __launch_bounds__(256) k_scalar_stage(Geo g, const TU *__restrict__ u, const TU *__restrict__ v,
+                                                      const TU *__restrict__ w, const double *__restrict__ cf,
+                                                      double *__restrict__ rc, double *__restrict__ cnext,
+                                                      double kappa, double f1, double f2, double f3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;
+  if (i >= g.I || j >= g.J) return;
+  const long c = fidx(g, i, j, k);
+  const long cip = fidx(g, i + 1 == g.I ? 0 : i + 1, j, k), cim = fidx(g, i == 0 ? g.I - 1 : i - 1, j, k);
+  const long cjp = fidx(g, i, j + 1 == g.J ? 0 : j + 1, k), cjm = fidx(g, i, j == 0 ? g.J - 1 : j - 1, k);
+  const long ckp = c + g.plane, ckm = c - g.plane;
+  const double dxi = g.dxi, dyi = g.dyi, dzi = g.dzi;
+  const double C0 = cf[c], Cip = cf[cip], Cim = cf[cim], Cjp = cf[cjp], Cjm = cf[cjm], Ckp = cf[ckp], Ckm = cf[ckm];
+  const double ucip = 0.5 * (double)u[c] * (Cip + C0);
+  const double ucim = 0.5 * (double)u[cim] * (C0 + Cim);
+  const double vcjp = 0.5 * (double)v[c] * (Cjp + C0);
+  const double vcjm = 0.5 * (double)v[cjm] * (C0 + Cjm);
+  const double wckp = 0.5 * (double)w[c] * (Ckp + C0);
+  const double wckm = 0.5 * (double)w[ckm] * (C0 + Ckm);
+  const double dcdxp = (Cip - C0) * dxi, dcdxm = (C0 - Cim) * dxi;
+  const double dcdyp = (Cjp - C0) * dyi, dcdym = (C0 - Cjm) * dyi;
+  const double dcdzp = (Ckp - C0) * dzi, dcdzm = (C0 - Ckm) * dzi;
+  const double rhs = dxi * (-ucip + ucim) + kappa * (dcdxp - dcdxm) * dxi + dyi * (-vcjp + vcjm) +
+                     kappa * (dcdyp - dcdym) * dyi + dzi * (-wckp + wckm) + kappa * (dcdzp - dcdzm) * dzi;
+  if (STAGE == 1) cnext[c] = C0 + f1 * rhs;
+  else cnext[c] = C0 + (f2 * rhs - f3 * rc[c]);
+  if (STAGE != 3) rc[c] = rhs;
+}
+template <typename TU>
+void launch_scalar_stage(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w,
+                         const double *cf, double *rc, double *cnext, double kappa, double f1, double f2, double f3) {
+  dim3 blk(64, 4, 1);
+  dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
+  if (stage == 1) k_scalar_stage<TU, 1><<<grd, blk, 0, s>>>(g, u, v, w, cf, rc, cnext, kappa, f1, f2, f3);
+  else if (stage == 2) k_scalar_stage<TU, 2><<<grd, blk, 0, s>>>(g, u, v, w, cf, rc, cnext, kappa, f1, f2, f3);
+  else k_scalar_stage<TU, 3><<<grd, blk, 0, s>>>(g, u, v, w, cf, rc, cnext, kappa, f1, f2, f3);
+}
+template void launch_scalar_stage<double>(cudaStream_t, const Geo &, int, const double *, const double *,
+                                          const double *, const double *, double *, double *, double, double,
+                                          double, double);
+template void launch_scalar_stage<float>(cudaStream_t, const Geo &, int, const float *, const float *, const float *,
+                                         const double *, double *, double *, double, double, double, double);
+
+// boundscal (bound.f90:109-171): wall ghost planes of the scalar
+__global__ void k_boundscal(Geo g, double *__restrict__ cf, int top_dirichlet, double top, int bot_dirichlet,
+                            double bot) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < g.plane; e += (long)gridDim.x * blockDim.x) {
+    const long t = (long)(g.K + 1) * g.plane + e, n = (long)g.K * g.plane + e;
+    cf[t] = top_dirichlet ? 2 * top - cf[n] : cf[n];
+    cf[e] = bot_dirichlet ? 2 * bot - cf[g.plane + e] : cf[g.plane + e];
+  }
+}
+void launch_boundscal(cudaStream_t s, const Geo &g, double *cf, int top_dirichlet, double top, int bot_dirichlet,
+                      double bot) {
+  k_boundscal<<<(int)std::min<long>(1216, (g.plane + 255) / 256), 256, 0, s>>>(g, cf, top_dirichlet, top,
+                                                                               bot_dirichlet, bot);
+}
 
 // ---------------------------------------------------------------------------
 // correc (correc.f90:11-42) + pnew += p (main.f90:369-371) + bounduvw(unew)

@@ -1,11 +1,13 @@
 // ibm_capi.cu -- the C ABI of include/ibm_rk3.h: context set-up (derived
 // parameters, solver tables), state transfer and the per-subroutine entry
 // points that sequence the kernels on the context stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "kernels.cuh"
@@ -88,6 +90,16 @@ struct ibm_ctx {
   double phase_ms[4] = {0, 0, 0, 0};
   double wall_raw[3] = {0, 0, 0};
   double dt_last = 0;
+  // plane statistics and the scalar field
+  PhaseBuffers ph{};
+  double *stat_part = nullptr;  // [ktot][slices][POST1D_NSUM] plane partial sums
+  size_t stat_cap = 0;
+  double *cfield = nullptr;     // scalar cnew, device layout; null until ibm_set_scalar
+  double *cnext = nullptr;      // dcdt of the substep: cnew after the projection
+  double *crk = nullptr;        // dcrkold, the scalar's stored right-hand side
+  bool c_pending = false;       // cnext holds this substep's scalar
+  ibm_scalar_params sp{};
+  double kappa = 0.;
 };
 
 namespace {
@@ -462,13 +474,26 @@ int predict(ibm_ctx *c, int rkiter, double dt) {
   if (rkiter == 1) f1 = dt * (32. / 60.);
   else if (rkiter == 2) { f1 = dt * (8. / 60.); f2 = dt * (25. / 60.); f3 = dt * (17. / 60.); }
   else { f1 = dt * (20. / 60.); f2 = dt * (45. / 60.); f3 = dt * (25. / 60.); }
+  // buoyancy 0.5*beta*9.81*(c + c(k+1)) of momzbuoy (mom.f90:251) once a scalar is set
+  const double *cb = c->cfield;
+  const double bcoef = 0.5 * c->sp.beta * 9.81;
   if (c->mixed)
     PROBED(IBM_PROBE_PREDICT, launch_predict<float, float>(c->stream, g, rkiter, c->u32, c->v32, c->w32, c->p32, c->ru32, c->rv32, c->rw32,
-                                 c->fu32, c->fv32, c->fw32, f1, f2, f3));
+                                 c->fu32, c->fv32, c->fw32, f1, f2, f3, cb, bcoef));
   else
     PROBED(IBM_PROBE_PREDICT, launch_predict<double, double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv,
-                                   c->fw, f1, f2, f3));
+                                   c->fw, f1, f2, f3, cb, bcoef));
   LAUNCHED(1);
+  if (c->cfield) {  // scalad and dcdt of rk1..rk3
+    if (c->mixed)
+      launch_scalar_stage<float>(c->stream, g, rkiter, c->u32, c->v32, c->w32, c->cfield, c->crk, c->cnext, c->kappa,
+                                 f1, f2, f3);
+    else
+      launch_scalar_stage<double>(c->stream, g, rkiter, c->u, c->v, c->w, c->cfield, c->crk, c->cnext, c->kappa, f1,
+                                  f2, f3);
+    LAUNCHED(1);
+    c->c_pending = true;
+  }
   return IBM_OK;
 }
 
@@ -561,7 +586,7 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
   return IBM_OK;
 }
 
-int project(ibm_ctx *c, int rkiter, double dt) {
+int project_fluid(ibm_ctx *c, int rkiter, double dt) {
   const Geo &g = c->g;
   const double dti = 1. / (c->rkab[rkiter - 1] * dt);
   int nl = 0;
@@ -617,6 +642,19 @@ int project(ibm_ctx *c, int rkiter, double dt) {
   PROBED(IBM_PROBE_CORREC, launch_correc<double, double, double>(c->stream, g, c->fu, c->fv, c->fw, c->phi, c->u, c->v, c->w, c->p, nullptr,
                                         factor * g.dxi, factor * g.dyi, factor * g.dzi));
   LAUNCHED(1);
+  return IBM_OK;
+}
+
+int project(ibm_ctx *c, int rkiter, double dt) {
+  int st;
+  if ((st = project_fluid(c, rkiter, dt))) return st;
+  if (c->c_pending) {  // cnew = dcdt; boundscal (main.f90:374-376)
+    std::swap(c->cfield, c->cnext);
+    launch_boundscal(c->stream, c->g, c->cfield, c->sp.bc_c_top_type == IBM_BC_C_DIRICHLET, c->sp.bc_c_top_val,
+                     c->sp.bc_c_bot_type == IBM_BC_C_DIRICHLET, c->sp.bc_c_bot_val);
+    LAUNCHED(1);
+    c->c_pending = false;
+  }
   return IBM_OK;
 }
 
@@ -731,7 +769,8 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
-                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum};
+                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ph.G, c->ph.W, c->stat_part,
+                  c->cfield, c->cnext, c->crk};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
@@ -1129,6 +1168,254 @@ int ibm_run_adaptive(ibm_ctx *c, int nsteps, int ioutchk, double *dt, double *ti
     }
   }
   return check_flags(c);
+}
+
+
+// ---------------------------------------------------------------------------
+// scalar field and plane statistics (post1d, output.f90:13-917)
+// ---------------------------------------------------------------------------
+int ibm_set_scalar(ibm_ctx *c, const ibm_scalar_params *sp, const double *cf, const double *dcrk) {
+  if (!c) return IBM_E_INVALID;
+  if (!sp || !(sp->pran > 0.)) return set_err(c, IBM_E_INVALID, "scalar parameters need pran > 0");
+  if ((sp->bc_c_top_type != IBM_BC_C_DIRICHLET && sp->bc_c_top_type != IBM_BC_C_NEUMANN) ||
+      (sp->bc_c_bot_type != IBM_BC_C_DIRICHLET && sp->bc_c_bot_type != IBM_BC_C_NEUMANN))
+    return set_err(c, IBM_E_INVALID, "scalar boundary types must be IBM_BC_C_DIRICHLET or IBM_BC_C_NEUMANN");
+  int st;
+  if ((st = ensure_href(c))) return st;
+  for (double **f : {&c->cfield, &c->cnext, &c->crk})
+    if (!*f) CK(cudaMalloc((void **)f, (size_t)c->g.nfield * sizeof(double)));
+  c->sp = *sp;
+  c->kappa = c->prm.visc / sp->pran;  // init.f90:94
+  c->c_pending = false;
+  if ((st = upload_field(c, cf, c->cfield))) return st;
+  if ((st = upload_field(c, dcrk, c->crk))) return st;
+  // boundscal as the driver applies it after loading (main.f90:198)
+  launch_boundscal(c->stream, c->g, c->cfield, sp->bc_c_top_type == IBM_BC_C_DIRICHLET, sp->bc_c_top_val,
+                   sp->bc_c_bot_type == IBM_BC_C_DIRICHLET, sp->bc_c_bot_val);
+  LAUNCHED(1);
+  // cells of cnext that the stage kernel does not write (ghost planes) start
+  // from cnew
+  CK(cudaMemcpyAsync(c->cnext, c->cfield, (size_t)c->g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
+int ibm_get_scalar(ibm_ctx *c, double *cf, double *dcrk) {
+  if (!c) return IBM_E_INVALID;
+  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  if (!c->cfield) {
+    if (cf) std::memset(cf, 0, n * sizeof(double));
+    if (dcrk) std::memset(dcrk, 0, n * sizeof(double));
+    return IBM_OK;
+  }
+  int st;
+  if ((st = ensure_href(c))) return st;
+  if ((st = download_field(c, c->cfield, cf))) return st;
+  return download_field(c, c->crk, dcrk);
+}
+
+static int run_phase_indicator(ibm_ctx *c, int itype) {
+  if (!c->ph.G) {
+    const size_t nc = (size_t)c->g.I * c->g.J * c->g.K;
+    CK(cudaMalloc((void **)&c->ph.G, 4 * nc * sizeof(unsigned long long)));
+    CK(cudaMalloc((void **)&c->ph.W, 4 * nc * sizeof(int)));
+  }
+  PROBED(IBM_PROBE_PHASE, launch_phase_indicator(c->stream, c->g, c->pg, c->pb, c->ph, itype));
+  LAUNCHED(c->pg.np > 0 ? 2 : 0);
+  return IBM_OK;
+}
+
+static PhaseView phase_view(const ibm_ctx *c, int itype, bool parts) {
+  PhaseView v;
+  v.G = c->ph.G;
+  v.W = c->ph.W;
+  v.pf = c->pb.pf;
+  v.np = c->pg.np;
+  v.I = c->g.I; v.J = c->g.J; v.K = c->g.K;
+  v.itype = itype;
+  v.parts = parts;
+  v.dx = 1. / c->g.dxi; v.dy = 1. / c->g.dyi; v.dz = 1. / c->g.dzi;
+  return v;
+}
+
+int ibm_phase_indicator(ibm_ctx *c, int itype, double *gamu, double *gamv, double *gamw, double *gamp,
+                        double *upart, double *vpart, double *wpart) {
+  if (!c) return IBM_E_INVALID;
+  if (itype != 0 && itype != 1) return set_err(c, IBM_E_INVALID, "itype must be 0 or 1");
+  if (c->pg.np > 0 && !c->have_particles) return set_err(c, IBM_E_STATE, "no particles set");
+  int st;
+  if ((st = ensure_href(c))) return st;
+  if ((st = run_phase_indicator(c, itype))) return st;
+  const PhaseView v = phase_view(c, itype, true);
+  double *out[7] = {gamu, gamv, gamw, gamp, upart, vpart, wpart};
+  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
+  for (int f = 0; f < 7; ++f) {
+    if (!out[f]) continue;
+    launch_phase_export(c->stream, v, f, c->href);
+    LAUNCHED(1);
+    CK(cudaMemcpyAsync(out[f], c->href, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
+// Ghost values, normalisations and derived scalars of post1d
+// (output.f90:178-200, 276-294, 401-477, 549-566) from the plane sums
+// S[k-1][POST1D_NSUM], k = 1..ktot.  Whole-array Fortran assignments read
+// their right-hand sides before writing, hence the two-loop forms.
+static void post1d_finish(const ibm_ctx *c, const std::vector<double> &S, bool parts, double *prof, double *scal) {
+  const int K = c->g.K, k1 = K + 1, nk = K + 2;
+  std::vector<std::vector<double>> q(IBM_NSTAT, std::vector<double>(nk, 0.));
+  // plane sum index -> profile
+  static const int src[POST1D_NSUM] = {
+      IBM_STAT_UM,  IBM_STAT_VM,  IBM_STAT_WM,  IBM_STAT_PM,   IBM_STAT_CM,   IBM_STAT_UPM,  IBM_STAT_VPM, IBM_STAT_WPM,
+      IBM_STAT_GUM, IBM_STAT_GVM, IBM_STAT_GWM, IBM_STAT_GPM,  IBM_STAT_U2,   IBM_STAT_V2,   IBM_STAT_W2,  IBM_STAT_P2,
+      IBM_STAT_C2,  IBM_STAT_UP2, IBM_STAT_VP2, IBM_STAT_WP2,  IBM_STAT_GP2,  IBM_STAT_UV,   IBM_STAT_UW,  IBM_STAT_VW,
+      IBM_STAT_WC,  IBM_STAT_CDFLX, IBM_STAT_UPVP, IBM_STAT_UPWP, IBM_STAT_VPWP, IBM_STAT_GUV, IBM_STAT_GUW, IBM_STAT_GVW};
+  for (int k = 1; k <= K; ++k)
+    for (int n = 0; n < POST1D_NSUM; ++n) q[src[n]][k] = S[(size_t)(k - 1) * POST1D_NSUM + n];
+  auto &um = q[IBM_STAT_UM], &vm = q[IBM_STAT_VM], &wm = q[IBM_STAT_WM], &pm = q[IBM_STAT_PM];
+  auto &u2 = q[IBM_STAT_U2], &v2 = q[IBM_STAT_V2], &w2 = q[IBM_STAT_W2], &p2 = q[IBM_STAT_P2];
+  auto &uv = q[IBM_STAT_UV], &uw = q[IBM_STAT_UW], &vw = q[IBM_STAT_VW];
+  auto &upm = q[IBM_STAT_UPM], &vpm = q[IBM_STAT_VPM], &wpm = q[IBM_STAT_WPM];
+  auto &up2 = q[IBM_STAT_UP2], &vp2 = q[IBM_STAT_VP2], &wp2 = q[IBM_STAT_WP2];
+  auto &upvp = q[IBM_STAT_UPVP], &upwp = q[IBM_STAT_UPWP], &vpwp = q[IBM_STAT_VPWP];
+  auto &gum = q[IBM_STAT_GUM], &gvm = q[IBM_STAT_GVM], &gwm = q[IBM_STAT_GWM], &gpm = q[IBM_STAT_GPM];
+  auto &gp2 = q[IBM_STAT_GP2], &guv = q[IBM_STAT_GUV], &guw = q[IBM_STAT_GUW], &gvw = q[IBM_STAT_GVW];
+  auto &ss = q[IBM_STAT_SS], &ssp = q[IBM_STAT_SSP];
+  auto &cm = q[IBM_STAT_CM], &c2 = q[IBM_STAT_C2], &wc = q[IBM_STAT_WC], &cdflx = q[IBM_STAT_CDFLX];
+  // ghost planes of the raw sums; w-type quantities are zero on the top wall
+  um[0] = -um[1]; um[k1] = -um[K];
+  vm[0] = -vm[1]; vm[k1] = -vm[K];
+  wm[0] = 0.; wm[K] = 0.; wm[k1] = wm[K - 1];
+  pm[0] = pm[1]; pm[k1] = pm[K];
+  upm[0] = -upm[1]; upm[k1] = -upm[K];
+  vpm[0] = -vpm[1]; vpm[k1] = -vpm[K];
+  wpm[0] = 0.; wpm[K] = 0.; wpm[k1] = wm[K - 1];  // wm, as the reference writes it
+  gum[0] = gum[1]; gum[k1] = gum[K];
+  gvm[0] = gvm[1]; gvm[k1] = gvm[K];
+  gwm[k1] = gwm[K - 1];
+  u2[0] = -u2[1]; u2[k1] = -u2[K];
+  v2[0] = -v2[1]; v2[k1] = -v2[K];
+  w2[0] = 0.; w2[K] = 0.; w2[k1] = w2[K - 1];
+  p2[0] = p2[1]; p2[k1] = p2[K];
+  up2[0] = -up2[1]; up2[k1] = -up2[K];
+  vp2[0] = -vp2[1]; vp2[k1] = -vp2[K];
+  wp2[0] = 0.; wp2[K] = 0.; wp2[k1] = w2[K - 1];  // w2, as the reference writes it
+  gp2[0] = gp2[1]; gp2[k1] = gp2[K];
+  uv[0] = -uv[1]; uv[k1] = -uv[K];
+  uw[0] = 0.; uw[K] = 0.; uw[k1] = uw[K - 1];
+  vw[0] = 0.; vw[k1] = vw[K - 1]; vw[K] = 0.;
+  upvp[0] = -upvp[1]; upvp[k1] = -upvp[K];
+  upwp[0] = 0.; upwp[K] = 0.; upwp[k1] = upwp[K - 1];
+  vpwp[0] = 0.; vpwp[k1] = vpwp[K - 1]; vpwp[K] = 0.;
+  guv[0] = guv[1]; guv[k1] = guv[K];
+  guw[0] = guw[1]; guw[k1] = guw[K];
+  gvw[0] = gvw[1]; gvw[k1] = gvw[K];
+  // means and rms of the fluid (np > 0: weighted by the fluid fraction)
+  const double N = 1. * c->prm.itot * c->prm.jtot;
+  auto den = [&](const std::vector<double> &g, int k) { return parts ? g[k] : N - g[k]; };
+  for (int k = 1; k <= K; ++k) {
+    um[k] = um[k] / den(gum, k); vm[k] = vm[k] / den(gvm, k); wm[k] = wm[k] / den(gwm, k);
+    cm[k] = cm[k] / den(gpm, k); pm[k] = pm[k] / den(gpm, k);
+  }
+  for (int k = 1; k <= K; ++k) {
+    u2[k] = std::sqrt(u2[k] / den(gum, k) - um[k] * um[k]);
+    v2[k] = std::sqrt(v2[k] / den(gvm, k) - vm[k] * vm[k]);
+    w2[k] = std::sqrt(w2[k] / den(gwm, k) - wm[k] * wm[k]);
+    p2[k] = std::sqrt(p2[k] / den(gpm, k) - pm[k] * pm[k]);
+    c2[k] = std::sqrt(c2[k] / den(gpm, k) - cm[k] * cm[k]);
+  }
+  std::vector<double> t(nk);
+  for (int k = 1; k <= K; ++k) t[k] = vw[k] / den(gvw, k) - 0.5 * (vm[k] + vm[k + 1]) * wm[k];
+  for (int k = 1; k <= K; ++k) vw[k] = t[k];
+  vw[0] = 0.;
+  double umax = u2[0];
+  for (int k = 1; k <= k1; ++k) umax = std::max(umax, u2[k]);
+  const double visc = c->prm.visc, lz = c->prm.lz, dzi = c->g.dzi;
+  const double re_rbc = umax * lz / visc;
+  for (int k = 1; k <= K; ++k) {
+    wc[k] = wc[k] / (N - gwm[k]);
+    cdflx[k] = cdflx[k] / (N - gwm[k]);
+  }
+  // wall shear stress and friction velocity
+  vm[0] = -vm[1]; vm[k1] = -vm[K];
+  for (int k = 1; k <= K; ++k) ss[k] = (vm[k + 1] - vm[k]) * dzi * visc;
+  ss[0] = (vm[1] - vm[0]) * dzi * visc;
+  um[0] = -um[1]; um[k1] = -um[K];
+  for (int k = 1; k <= K; ++k) {
+    const double d = (um[k + 1] - um[k]) * dzi * visc;
+    ss[k] = std::sqrt(ss[k] * ss[k] + d * d);
+  }
+  const double d0 = (um[1] - um[0]) * dzi * visc;
+  ss[0] = std::sqrt(ss[0] * ss[0] + d0 * d0);
+  const double grad_k_wall = dzi * (std::sqrt(0.5 * (u2[1] * u2[1] + v2[1] * v2[1] + w2[1] * w2[1])) -
+                                    std::sqrt(0.5 * (u2[0] * u2[0] + v2[0] * v2[0] + w2[0] * w2[0])));
+  const double u_tau = std::sqrt(visc * grad_k_wall);
+  const double re_tau = u_tau * lz / visc;
+  // Nusselt number
+  double swc = 0., scd = 0.;
+  for (int k = 1; k <= K; ++k) swc = swc + wc[k];
+  for (int k = 1; k <= K; ++k) scd = scd + cdflx[k];
+  const double nu = lz / (c->kappa * (c->sp.bc_c_bot_val - c->sp.bc_c_top_val)) * (swc / K + scd / K);
+  // particle phase
+  for (int k = 1; k <= K; ++k) {
+    upm[k] = upm[k] / (N - gum[k]);
+    vpm[k] = vpm[k] / (N - gvm[k]);
+    wpm[k] = wpm[k] / (N - gwm[k]);
+  }
+  for (int k = 1; k <= K; ++k) {
+    up2[k] = std::sqrt(up2[k] / (N - gum[k]) - upm[k] * upm[k]);
+    vp2[k] = std::sqrt(vp2[k] / (N - gvm[k]) - vpm[k] * vpm[k]);
+    wp2[k] = std::sqrt(wp2[k] / (N - gwm[k]) - wpm[k] * wpm[k]);
+  }
+  for (int k = 1; k <= K; ++k) t[k] = vpwp[k] / (N - gvw[k]) - 0.5 * (vpm[k] + vpm[k + 1]) * wpm[k];
+  for (int k = 1; k <= K; ++k) vpwp[k] = t[k];
+  vpwp[0] = 0.;
+  vpm[0] = -vpm[1]; vpm[k1] = -vpm[K];
+  for (int k = 1; k <= K; ++k) ssp[k] = (vpm[k + 1] - vpm[k]) * dzi * visc;
+  ssp[0] = (vpm[1] - vpm[0]) * dzi * visc;
+  if (prof)
+    for (int n = 0; n < IBM_NSTAT; ++n) std::memcpy(prof + (size_t)n * nk, q[n].data(), nk * sizeof(double));
+  if (scal) { scal[0] = re_tau; scal[1] = u_tau; scal[2] = nu; scal[3] = re_rbc; scal[4] = grad_k_wall; }
+}
+
+int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
+  if (!c) return IBM_E_INVALID;
+  if (!c->have_fields) return set_err(c, IBM_E_STATE, "no fields set");
+  const bool parts = c->pg.np > 0;
+  if (parts && !c->have_particles) return set_err(c, IBM_E_STATE, "no particles set");
+  int st;
+  if (parts && (st = run_phase_indicator(c, 1))) return st;
+  const int K = c->g.K;
+  // slices per plane: about four blocks per SM in all
+  const int slices = std::max(1, std::min(64, (608 + K - 1) / K));
+  const size_t np = (size_t)K * slices * POST1D_NSUM;
+  if (c->stat_cap < np) {
+    if (c->stat_part) cudaFree(c->stat_part);
+    c->stat_part = nullptr;
+    c->stat_cap = 0;
+    CK(cudaMalloc((void **)&c->stat_part, np * sizeof(double)));
+    c->stat_cap = np;
+  }
+  const PhaseView v = phase_view(c, 1, parts);
+  if (c->mixed)
+    PROBED(IBM_PROBE_STATS, launch_post1d_sums<float>(c->stream, c->g, v, c->u32, c->v32, c->w32, nullptr, c->p32,
+                                                      c->plo32, c->cfield, c->kappa, c->stat_part, slices));
+  else
+    PROBED(IBM_PROBE_STATS, launch_post1d_sums<double>(c->stream, c->g, v, c->u, c->v, c->w, c->p, nullptr, nullptr,
+                                                       c->cfield, c->kappa, c->stat_part, slices));
+  LAUNCHED(1);
+  std::vector<double> part(np), S((size_t)K * POST1D_NSUM, 0.);
+  CK(cudaMemcpyAsync(part.data(), c->stat_part, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < K; ++k)
+    for (int s = 0; s < slices; ++s)
+      for (int n = 0; n < POST1D_NSUM; ++n)
+        S[(size_t)k * POST1D_NSUM + n] += part[((size_t)k * slices + s) * POST1D_NSUM + n];
+  post1d_finish(c, S, parts, prof, scal);
+  return IBM_OK;
 }
 
 int ibm_slip_residual(ibm_ctx *c, double *maxres, double *rmsres) {

@@ -14,7 +14,13 @@ namespace ibmk {
 // fluid_kernels.cu
 template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
-                    T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3);
+                    T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3,
+                    const double *cb = nullptr, double bcoef = 0.);
+template <typename TU>
+void launch_scalar_stage(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w,
+                         const double *cf, double *rc, double *cnext, double kappa, double f1, double f2, double f3);
+void launch_boundscal(cudaStream_t s, const Geo &g, double *cf, int top_dirichlet, double top, int bot_dirichlet,
+                      double bot);
 template <typename TF, typename TPh, typename TU>
 void launch_correc(cudaStream_t s, const Geo &g, const TF *fu, const TF *fv, const TF *fw, const TPh *phi, TU *u,
                    TU *v, TU *w, double *pn, float *pn32, double fi, double fj, double fk);
@@ -169,5 +175,77 @@ void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, Pa
 void launch_save_old(cudaStream_t s, const PartGeo &pg, PartBuffers b);
 void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt);
 void launch_ne_finalize(cudaStream_t s, const PartGeo &pg, PartBuffers b, IbmBuffers ib, int init_flags);
+
+
+// ---------------------------------------------------------------------------
+// plane statistics (stats_kernels.cu)
+// ---------------------------------------------------------------------------
+constexpr unsigned long long PH_INNER = 0x7FF0000000000000ull;  // +inf bits: above every fraction
+constexpr int POST1D_NSUM = 32;  // plane sums of output.f90:88-355
+struct PhaseBuffers {
+  unsigned long long *G;  // [4][K*I*J] largest candidate key per cell (grids u, v, w, p)
+  int *W;                 // [4][K*I*J] winner code per cell
+};
+void launch_phase_indicator(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, PhaseBuffers ph,
+                            int itype);
+// Reads of the phase fields at reference indices i, j in 1..I/J (periodic
+// halos wrapped by the caller) and k in 0..K+1 with the wall ghost rules of
+// phase_indicator.f90:497-530.
+struct PhaseView {
+  const unsigned long long *G;
+  const int *W;
+  const double *pf;
+  int np, I, J, K, itype;
+  bool parts;  // false: np = 0, post1d's zero fields (output.f90:41-49)
+  double dx, dy, dz;
+
+  __device__ __forceinline__ long cell(int i, int j, int k) const {
+    return (long)(k - 1) * I * J + (long)(j - 1) * I + (i - 1);
+  }
+  // fluid fraction of grid c (0..3)
+  __device__ __forceinline__ double gam(int c, int i, int j, int k) const {
+    if (!parts) return 0.;
+    if (k < 1) k = 1;
+    if (k > K) k = K;
+    const unsigned long long key = G[(long)c * I * J * K + cell(i, j, k)];
+    const double s = key == 0ull ? 0. : (key == PH_INNER ? 1. : __longlong_as_double((long long)key));
+    return 1. - s;
+  }
+  // rigid-body velocity component c (0..2) at an interior cell
+  __device__ double part_in(int c, int i, int j, int k) const {
+    const int grid = itype == 1 ? c : 3;
+    const long off = (long)grid * I * J * K + cell(i, j, k);
+    const unsigned long long key = G[off];
+    if (key == 0ull) return 0.;
+    const int w = W[off];
+    if (w <= 0) return 0.;  // no winner recorded (not reached: pass 1 repeats pass 0's keys)
+    const int q = key == PH_INNER ? w - 1 : 9 * np + 1 - w;
+    const int p = q / 9, nb = q - 9 * p;
+    if (nb > 0) return 0.;  // the copies carry no velocity (phase_indicator.f90:68-78, 83-87)
+    if (itype == 0) return pf[(long)(PF_OMX + c) * np + p];
+    const double x = pf[(long)PF_X * np + p], y = pf[(long)PF_Y * np + p], z = pf[(long)PF_Z * np + p];
+    const double omx = pf[(long)PF_OMX * np + p], omy = pf[(long)PF_OMY * np + p], omz = pf[(long)PF_OMZ * np + p];
+    if (c == 0) return pf[(long)PF_U * np + p] + omy * ((k - 0.5) * dz - z) - omz * ((j - 0.5) * dy - y);
+    if (c == 1) return pf[(long)PF_V * np + p] + omz * ((i - 0.5) * dx - x) - omx * ((k - 0.5) * dz - z);
+    return pf[(long)PF_W * np + p] + omx * ((j - 0.5) * dy - y) - omy * ((i - 0.5) * dx - x);
+  }
+  __device__ double part(int c, int i, int j, int k) const {
+    if (!parts) return 0.;
+    if (c < 2) {
+      if (k == 0) return -part_in(c, i, j, 1);
+      if (k == K + 1) return -part_in(c, i, j, K);
+      return part_in(c, i, j, k);
+    }
+    if (k == 0 || k == K) return 0.;
+    if (k == K + 1) return K - 1 >= 1 ? part_in(2, i, j, K - 1) : 0.;
+    return part_in(2, i, j, k);
+  }
+};
+
+void launch_phase_export(cudaStream_t s, const PhaseView &v, int f, double *out);
+template <typename T>
+void launch_post1d_sums(cudaStream_t s, const Geo &g, const PhaseView &ph, const T *u, const T *v, const T *w,
+                        const double *p, const float *phi, const float *plo, const double *c, double kappa,
+                        double *part, int slices);
 
 }  // namespace ibmk

@@ -51,6 +51,7 @@ class IBMSolver:
 
     def __init__(self, case: Case, mode: int = _abi.IBM_MODE_PLAIN_FP64, backend=None):
         self.case = case
+        self.mode = mode
         if backend is None:
             _, self.fn = load_library()
         else:
@@ -211,6 +212,52 @@ class IBMSolver:
         self._chk(self.fn["diagnostics"](self.ctx, C.byref(wn), C.byref(wo), ft))
         return {"wallshearnew": wn.value, "wallshearold": wo.value, "forcetot": list(ft)}
 
+    # ---- scalar field and plane statistics (post1d) --------------------------------
+    def set_scalar(self, c=None, pran: float = 1.0, beta: float = 0.0, bc_c_top_val: float = 0.0,
+                   bc_c_bot_val: float = 0.0, bc_c_top_type: int = _abi.IBM_BC_C_DIRICHLET,
+                   bc_c_bot_type: int = _abi.IBM_BC_C_DIRICHLET, dcrk=None):
+        """Scalar field cnew and its stored RHS dcrkold in the reference layout
+        (None: zero) and the scalar parameters (param.f90:39-47; kappa =
+        visc/Pran, init.f90:94).  From then on every substep transports it."""
+        arrs = []
+        for f in (c, dcrk):
+            a = None
+            if f is not None:
+                a = np.asfortranarray(f, np.float64)
+                if a.shape != self.case.shape:
+                    raise ValueError(f"field shape {a.shape} != {self.case.shape}")
+            arrs.append(a)
+        sp = _abi.IbmScalarParams(float(pran), float(beta), float(bc_c_top_val), float(bc_c_bot_val),
+                                  int(bc_c_top_type), int(bc_c_bot_type))
+        self._chk(self.fn["set_scalar"](self.ctx, C.byref(sp), dptr(arrs[0]), dptr(arrs[1])))
+
+    def get_scalar(self) -> tuple[np.ndarray, np.ndarray]:
+        """(cnew, dcrkold) in the reference layout."""
+        a = np.zeros(self.case.shape, order="F")
+        b = np.zeros(self.case.shape, order="F")
+        self._chk(self.fn["get_scalar"](self.ctx, dptr(a), dptr(b)))
+        return a, b
+
+    PHASE_NAMES = ("gamu", "gamv", "gamw", "gamp", "upart", "vpart", "wpart")
+
+    def phase_indicator(self, itype: int = 1) -> dict[str, np.ndarray]:
+        """phase_indicator (phase_indicator.f90:11-559): fluid fractions and
+        rigid-body velocities in the reference layout."""
+        arrs = self._field_arrays()
+        self._chk(self.fn["phase_indicator"](self.ctx, int(itype), *[dptr(a) for a in arrs]))
+        return dict(zip(self.PHASE_NAMES, arrs))
+
+    def post1d(self) -> tuple[dict[str, np.ndarray], dict[str, float]]:
+        """post1d (output.f90:13-917) without its files: the plane profiles
+        (k = 0..k1) and the derived scalars."""
+        nk = self.case.shape[2]
+        prof = np.zeros(len(_abi.STAT_NAMES) * nk)
+        scal = np.zeros(len(_abi.STAT_SCALAR_NAMES))
+        self._chk(self.fn["post1d"](self.ctx, dptr(prof), dptr(scal)))
+        prof = prof.reshape(len(_abi.STAT_NAMES), nk)
+        return ({n: prof[q] for q, n in enumerate(_abi.STAT_NAMES)},
+                {n: float(scal[q]) for q, n in enumerate(_abi.STAT_SCALAR_NAMES)})
+
     def set_stream(self, stream_handle: int | None):
         self._chk(self.fn["set_stream"](self.ctx, C.c_void_p(stream_handle or 0)))
 
@@ -224,9 +271,9 @@ class IBMSolver:
     # --- per-kernel event timing --------------------------------------------------
 
     PROBE_NAMES = ("predict", "stencil", "interp", "spread", "fillps_fftx", "ffty", "thomas", "ifftx", "correc",
-                   "sphere", "features", "mlp")
+                   "sphere", "features", "mlp", "phase", "stats")
 
-    def probe(self, mask: int = (1 << 12) - 1):
+    def probe(self, mask: int = (1 << 14) - 1):
         """Time every launch of the selected kernel classes with CUDA events."""
         self._chk(self.fn["probe"](self.ctx, int(mask)))
 

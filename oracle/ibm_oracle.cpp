@@ -181,6 +181,12 @@ struct orc_ctx {
   // fields (common.f90:4-8)
   Arr3 unew, vnew, wnew, pnew, dudt, dvdt, dwdt, dudtold, dvdtold, dwdtold, p;
   Arr3 durk, dvrk, dwrk;
+  // scalar (param.f90:39-47, init.f90:94); zero and not transported unless
+  // set (cnew = 0 with zero wall values stays 0 exactly in the reference)
+  Arr3 cnew, dcdt, dcrk;
+  bool have_scalar = false;
+  double kappa = 0., beta = 0., bc_c_top_val = 0., bc_c_bot_val = 0.;
+  int bc_c_top_type = IBM_BC_C_DIRICHLET, bc_c_bot_type = IBM_BC_C_DIRICHLET;
   Arr3 dudtf, dvdtf, dwdtf;
   // solver (initsolver.f90)
   std::vector<double> a, b, c, xyrt;
@@ -455,8 +461,58 @@ double wallshear_sum(orc_ctx *c) {
   return s;
 }
 
-// rk1/rk2/rk3 (rk3.f90:13-329).  The scalar (scalad, momzbuoy) is inert:
-// beta=0 and c=0 add exactly +0 (rk3.f90:56-59).
+// scalad (scal.f90:11-58): advection-diffusion of the scalar
+void scalad(orc_ctx *c, Arr3 &dcdt, const Arr3 &U, const Arr3 &V, const Arr3 &W, const Arr3 &C) {
+  const double dxi = c->dxi, dyi = c->dyi, dzi = c->dzi, kappa = c->kappa;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= c->kmax; ++k)
+    for (int j = 1; j <= c->jmax; ++j)
+      for (int i = 1; i <= c->imax; ++i) {
+        const int ip = i + 1, jp = j + 1, kp = k + 1, im = i - 1, jm = j - 1, km = k - 1;
+        const double ucip = 0.5 * U(i, j, k) * (C(ip, j, k) + C(i, j, k));
+        const double ucim = 0.5 * U(im, j, k) * (C(i, j, k) + C(im, j, k));
+        const double vcjp = 0.5 * V(i, j, k) * (C(i, jp, k) + C(i, j, k));
+        const double vcjm = 0.5 * V(i, jm, k) * (C(i, j, k) + C(i, jm, k));
+        const double wckp = 0.5 * W(i, j, k) * (C(i, j, kp) + C(i, j, k));
+        const double wckm = 0.5 * W(i, j, km) * (C(i, j, k) + C(i, j, km));
+        const double dcdxp = (C(ip, j, k) - C(i, j, k)) * dxi, dcdxm = (C(i, j, k) - C(im, j, k)) * dxi;
+        const double dcdyp = (C(i, jp, k) - C(i, j, k)) * dyi, dcdym = (C(i, j, k) - C(i, jm, k)) * dyi;
+        const double dcdzp = (C(i, j, kp) - C(i, j, k)) * dzi, dcdzm = (C(i, j, k) - C(i, j, km)) * dzi;
+        dcdt(i, j, k) = dxi * (-ucip + ucim) + kappa * (dcdxp - dcdxm) * dxi + dyi * (-vcjp + vcjm) +
+                        kappa * (dcdyp - dcdym) * dyi + dzi * (-wckp + wckm) + kappa * (dcdzp - dcdzm) * dzi;
+      }
+}
+
+// momzbuoy (mom.f90:233-259) added to the advective w right-hand side the
+// way rk1..rk3 combine them (rk3.f90:56-58): dw = B + dw
+void add_buoyancy(orc_ctx *c, Arr3 &dw, const Arr3 &C) {
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= c->kmax; ++k)
+    for (int j = 1; j <= c->jmax; ++j)
+      for (int i = 1; i <= c->imax; ++i)
+        dw(i, j, k) = 0.5 * c->beta * 9.81 * (C(i, j, k) + C(i, j, k + 1)) + dw(i, j, k);
+}
+
+// boundscal (bound.f90:109-171)
+void boundscal(orc_ctx *c, Arr3 &C) {
+  const int k1 = c->k1, kmax = c->kmax;
+  for (int j = 0; j <= c->j1; ++j)
+    for (int i = 0; i <= c->i1; ++i) {
+      if (c->bc_c_top_type == IBM_BC_C_DIRICHLET) C(i, j, k1) = 2 * c->bc_c_top_val - C(i, j, kmax);
+      else C(i, j, k1) = C(i, j, kmax);
+    }
+  for (int j = 0; j <= c->j1; ++j)
+    for (int i = 0; i <= c->i1; ++i) {
+      if (c->bc_c_bot_type == IBM_BC_C_DIRICHLET) C(i, j, 0) = 2 * c->bc_c_bot_val - C(i, j, 1);
+      else C(i, j, 0) = C(i, j, 1);
+    }
+  updthalos(c, C, 1);
+  updthalos(c, C, 2);
+}
+
+// rk1/rk2/rk3 (rk3.f90:13-329), with the scalar (dcdt, scalad) and the
+// buoyancy term (momzbuoy) once a scalar is set; without one they add
+// exactly +0 to the momentum (c = 0).
 void rk_stage(orc_ctx *c, int rkiter, double dt) {
   Arr3 &du = c->durk, &dv = c->dvrk, &dw = c->dwrk;
   const double dVeul = (1. / c->dxi) * (1. / c->dyi) * (1. / c->dzi);
@@ -475,6 +531,10 @@ void rk_stage(orc_ctx *c, int rkiter, double dt) {
     momxad(c, du, c->unew, c->vnew, c->wnew);
     momyad(c, dv, c->unew, c->vnew, c->wnew);
     momzad(c, dw, c->unew, c->vnew, c->wnew);
+    if (c->have_scalar) {
+      add_buoyancy(c, dw, c->cnew);
+      scalad(c, c->dcrk, c->unew, c->vnew, c->wnew, c->cnew);
+    }
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= c->kmax; ++k)
       for (int j = 1; j <= c->jmax; ++j)
@@ -482,6 +542,7 @@ void rk_stage(orc_ctx *c, int rkiter, double dt) {
           c->dudt(i, j, k) = c->dudt(i, j, k) + factor * du(i, j, k);
           c->dvdt(i, j, k) = c->dvdt(i, j, k) + factor * dv(i, j, k);
           c->dwdt(i, j, k) = c->dwdt(i, j, k) + factor * dw(i, j, k);
+          if (c->have_scalar) c->dcdt(i, j, k) = c->cnew(i, j, k) + factor * c->dcrk(i, j, k);
         }
     double all = wallshear_sum(c);
     c->wallshearnew = (factor / dt) * all / (dVeul * ntot);
@@ -503,6 +564,12 @@ void rk_stage(orc_ctx *c, int rkiter, double dt) {
     momxad(c, dnu, c->unew, c->vnew, c->wnew);
     momyad(c, dnv, c->unew, c->vnew, c->wnew);
     momzad(c, dnw, c->unew, c->vnew, c->wnew);
+    Arr3 dnc;
+    if (c->have_scalar) {
+      dnc = c->cnew;  // dummy array (shape only)
+      add_buoyancy(c, dnw, c->cnew);
+      scalad(c, dnc, c->unew, c->vnew, c->wnew, c->cnew);
+    }
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= c->kmax; ++k)
       for (int j = 1; j <= c->jmax; ++j)
@@ -510,10 +577,13 @@ void rk_stage(orc_ctx *c, int rkiter, double dt) {
           c->dudt(i, j, k) = c->dudt(i, j, k) + (factor2 * dnu(i, j, k) - factor3 * du(i, j, k));
           c->dvdt(i, j, k) = c->dvdt(i, j, k) + (factor2 * dnv(i, j, k) - factor3 * dv(i, j, k));
           c->dwdt(i, j, k) = c->dwdt(i, j, k) + (factor2 * dnw(i, j, k) - factor3 * dw(i, j, k));
+          if (c->have_scalar)
+            c->dcdt(i, j, k) = c->cnew(i, j, k) + (factor2 * dnc(i, j, k) - factor3 * c->dcrk(i, j, k));
           if (rkiter == 2) {
             du(i, j, k) = dnu(i, j, k);
             dv(i, j, k) = dnv(i, j, k);
             dw(i, j, k) = dnw(i, j, k);
+            if (c->have_scalar) c->dcrk(i, j, k) = dnc(i, j, k);
           }
         }
     double all = wallshear_sum(c);
@@ -1331,7 +1401,8 @@ int intgr_nwtn_eulr(orc_ctx *c, int rkiter, double dt) {
 void alloc(orc_ctx *c) {
   const int ni = c->i1 + 1, nj = c->j1 + 1, nk = c->k1 + 1;
   for (Arr3 *a : {&c->unew, &c->vnew, &c->wnew, &c->pnew, &c->dudt, &c->dvdt, &c->dwdt,
-                  &c->dudtold, &c->dvdtold, &c->dwdtold, &c->p, &c->durk, &c->dvrk, &c->dwrk})
+                  &c->dudtold, &c->dvdtold, &c->dwdtold, &c->p, &c->durk, &c->dvrk, &c->dwrk, &c->cnew,
+                  &c->dcdt, &c->dcrk})
     a->init(0, ni, nj, nk);
   for (Arr3 *a : {&c->dudtf, &c->dvdtf, &c->dwdtf}) a->init(-1, c->i1 + 3, c->j1 + 3, c->k1 + 3);
   c->ap.assign(c->npmax, Part());      // value-initialised: scalars zero
@@ -1396,6 +1467,407 @@ void project(orc_ctx *c, int rkiter, double dt) {
   bounduvw(c, c->unew, c->vnew, c->wnew);
   for (size_t n = 0; n < c->pnew.d.size(); ++n) c->pnew.d[n] = c->pnew.d[n] + c->p.d[n];
   boundp(c, c->pnew);
+  if (c->have_scalar) {  // main.f90:374-376
+    c->cnew.d = c->dcdt.d;
+    boundscal(c, c->cnew);
+  }
+}
+
+// phase_indicator (phase_indicator.f90:11-559) on one rank.  Every particle
+// is its own master; its self-neighbour copies nbrecv = nb+4 (mod 8) for the
+// flagged nb carry the shifted position only: the reference copies x, y, z
+// into anb(nbrecv) (:83-119) and leaves u..omz at their zero initialisation
+// (:68-78), so cells won by a copy get a zero rigid-body velocity.
+void phase_indicator(orc_ctx *c, int itype, Arr3 &gamu, Arr3 &gamv, Arr3 &gamw, Arr3 &gamp, Arr3 &upart,
+                     Arr3 &vpart, Arr3 &wpart) {
+  struct Anb { double x, y, z, u, v, w, omx, omy, omz; };
+  const double dx = 1. / c->dxi, dy = 1. / c->dyi, dz = 1. / c->dzi;
+  const double radius = c->radius;
+  const double radin = radius - 2. * dx;
+  const double radin2 = radin * radin;
+  const double bl = 0., bf = 0.;  // boundleftmyid, boundfrontmyid
+  for (Arr3 *a : {&gamu, &gamv, &gamw, &gamp, &upart, &vpart, &wpart}) std::fill(a->d.begin(), a->d.end(), 0.);
+  for (int p = 0; p < c->pmax; ++p) {
+    const Part &P = c->ap[p];
+    if (P.mslv == 0) continue;
+    Anb anb[9];
+    for (auto &a : anb) a = Anb{0, 0, 0, 0, 0, 0, 0, 0, 0};
+    anb[0] = Anb{P.x, P.y, P.z, P.u, P.v, P.w, P.omx, P.omy, P.omz};
+    for (int nb = 1; nb <= 8; ++nb) {
+      int nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8;
+      if (P.mslv > 0 && P.nb[nb] == 1) {
+        anb[nbrecv].x = anb[0].x; anb[nbrecv].y = anb[0].y; anb[nbrecv].z = anb[0].z;
+        copy_shift_sphere(c, nbrecv, anb[nbrecv].x, anb[nbrecv].y);
+      }
+    }
+    for (int nb = 0; nb <= 8; ++nb) {
+      if (!((nb == 0 && P.mslv > 0) || (nb > 0 && P.mslv > 0 && P.nb[nb] == 1))) continue;
+      int nbrecv = nb;
+      if (nb > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
+      const Anb &A = anb[nbrecv];
+      const double coorxc = A.x - bl, cooryc = A.y - bf, coorzc = A.z;
+      int ilow = nint((coorxc - radius) * c->dxi - 2.), ihigh = nint((coorxc + radius) * c->dxi + 2.);
+      int jlow = nint((cooryc - radius) * c->dyi - 2.), jhigh = nint((cooryc + radius) * c->dyi + 2.);
+      int klow = nint((coorzc - radius) * c->dzi - 2.), khigh = nint((coorzc + radius) * c->dzi + 2.);
+      if (ilow < 1) ilow = 1;
+      if (jlow < 1) jlow = 1;
+      if (klow < 1) klow = 1;
+      if (ihigh > c->imax) ihigh = c->imax;
+      if (jhigh > c->jmax) jhigh = c->jmax;
+      if (khigh > c->kmax) khigh = c->kmax;
+      // the eight corner distances in the reference's corner order
+      auto frac = [&](double dxm2, double dxp2, double dym2, double dyp2, double dzm2, double dzp2) {
+        double sg[8];
+        sg[0] = radius - std::sqrt(dxm2 + dym2 + dzm2);
+        sg[1] = radius - std::sqrt(dxm2 + dyp2 + dzm2);
+        sg[2] = radius - std::sqrt(dxp2 + dyp2 + dzm2);
+        sg[3] = radius - std::sqrt(dxp2 + dym2 + dzm2);
+        sg[4] = radius - std::sqrt(dxm2 + dym2 + dzp2);
+        sg[5] = radius - std::sqrt(dxm2 + dyp2 + dzp2);
+        sg[6] = radius - std::sqrt(dxp2 + dyp2 + dzp2);
+        sg[7] = radius - std::sqrt(dxp2 + dym2 + dzp2);
+        double sum1 = 0., sum2 = 0.;
+        for (int cp = 0; cp < 8; ++cp) {
+          if (sg[cp] > 0.) sum1 = sum1 + sg[cp];
+          sum2 = sum2 + std::fabs(sg[cp]);
+        }
+        return sum1 / sum2;
+      };
+      // u cells (:266-309)
+      for (int k = klow; k <= khigh; ++k) {
+        const double zmn = (k - 1) * dz, zpl = k * dz;
+        const double dzp2 = (zpl - A.z) * (zpl - A.z);
+        for (int j = jlow; j <= jhigh; ++j) {
+          const double ymn = bf + (j - 1) * dy, ypl = bf + j * dy;
+          const double dyp2 = (ypl - A.y) * (ypl - A.y);
+          for (int i = ilow; i <= ihigh; ++i) {
+            const double xmn = bl + (i - 0.5) * dx, xpl = bl + (i + 0.5) * dx;
+            const double dxp2 = (xpl - A.x) * (xpl - A.x);
+            const double dist2 = dxp2 + dyp2 + dzp2;
+            const double vel = A.u + A.omy * ((k - 0.5) * dz - A.z) - A.omz * ((j - 0.5) * dy - A.y + bf);
+            if (dist2 < radin2 && itype == 1) {
+              gamu(i, j, k) = 1.;
+              upart(i, j, k) = vel;
+            } else {
+              const double f = frac((xmn - A.x) * (xmn - A.x), dxp2, (ymn - A.y) * (ymn - A.y), dyp2,
+                                    (zmn - A.z) * (zmn - A.z), dzp2);
+              if (f > gamu(i, j, k) && itype == 1) { gamu(i, j, k) = f; upart(i, j, k) = vel; }
+            }
+          }
+        }
+      }
+      // v cells (:313-356)
+      for (int k = klow; k <= khigh; ++k) {
+        const double zmn = (k - 1) * dz, zpl = k * dz;
+        const double dzp2 = (zpl - A.z) * (zpl - A.z);
+        for (int j = jlow; j <= jhigh; ++j) {
+          const double ymn = bf + (j - 0.5) * dy, ypl = bf + (j + 0.5) * dy;
+          const double dyp2 = (ypl - A.y) * (ypl - A.y);
+          for (int i = ilow; i <= ihigh; ++i) {
+            const double xmn = bl + (i - 1) * dx, xpl = bl + i * dx;
+            const double dxp2 = (xpl - A.x) * (xpl - A.x);
+            const double dist2 = dxp2 + dyp2 + dzp2;
+            const double vel = A.v + A.omz * ((i - 0.5) * dx - A.x + bl) - A.omx * ((k - 0.5) * dz - A.z);
+            if (dist2 < radin2 && itype == 1) {
+              gamv(i, j, k) = 1.;
+              vpart(i, j, k) = vel;
+            } else {
+              const double f = frac((xmn - A.x) * (xmn - A.x), dxp2, (ymn - A.y) * (ymn - A.y), dyp2,
+                                    (zmn - A.z) * (zmn - A.z), dzp2);
+              if (f > gamv(i, j, k) && itype == 1) { gamv(i, j, k) = f; vpart(i, j, k) = vel; }
+            }
+          }
+        }
+      }
+      // w cells (:360-403)
+      for (int k = klow; k <= khigh; ++k) {
+        const double zmn = (k - 0.5) * dz, zpl = (k + 0.5) * dz;
+        const double dzp2 = (zpl - A.z) * (zpl - A.z);
+        for (int j = jlow; j <= jhigh; ++j) {
+          const double ymn = bf + (j - 1) * dy, ypl = bf + j * dy;
+          const double dyp2 = (ypl - A.y) * (ypl - A.y);
+          for (int i = ilow; i <= ihigh; ++i) {
+            const double xmn = bl + (i - 1) * dx, xpl = bl + i * dx;
+            const double dxp2 = (xpl - A.x) * (xpl - A.x);
+            const double dist2 = dxp2 + dyp2 + dzp2;
+            const double vel = A.w + A.omx * ((j - 0.5) * dy - A.y + bf) - A.omy * ((i - 0.5) * dx - A.x + bl);
+            if (dist2 < radin2 && itype == 1) {
+              gamw(i, j, k) = 1.;
+              wpart(i, j, k) = vel;
+            } else {
+              const double f = frac((xmn - A.x) * (xmn - A.x), dxp2, (ymn - A.y) * (ymn - A.y), dyp2,
+                                    (zmn - A.z) * (zmn - A.z), dzp2);
+              if (f > gamw(i, j, k) && itype == 1) { gamw(i, j, k) = f; wpart(i, j, k) = vel; }
+            }
+          }
+        }
+      }
+      // pressure cells (:407-476)
+      for (int k = klow; k <= khigh; ++k) {
+        const double zmn = (k - 1) * dz, zpl = k * dz;
+        const double dzp2 = (zpl - A.z) * (zpl - A.z);
+        for (int j = jlow; j <= jhigh; ++j) {
+          const double ymn = bf + (j - 1) * dy, ypl = bf + j * dy;
+          const double dyp2 = (ypl - A.y) * (ypl - A.y);
+          for (int i = ilow; i <= ihigh; ++i) {
+            const double xmn = bl + (i - 1) * dx, xpl = bl + i * dx;
+            const double dxp2 = (xpl - A.x) * (xpl - A.x);
+            const double dist2 = dxp2 + dyp2 + dzp2;
+            const double dxm2 = (xmn - A.x) * (xmn - A.x), dym2 = (ymn - A.y) * (ymn - A.y),
+                         dzm2 = (zmn - A.z) * (zmn - A.z);
+            if (dist2 < radin2 && itype == 1) {
+              gamp(i, j, k) = 1.;
+            } else {
+              const double f = frac(dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
+              if (itype == 1) gamp(i, j, k) = std::max(f, gamp(i, j, k));
+            }
+            if (dist2 < radin2 && itype == 0) {
+              gamp(i, j, k) = 1.;
+              upart(i, j, k) = A.omx; vpart(i, j, k) = A.omy; wpart(i, j, k) = A.omz;
+            } else {
+              const double f = frac(dxm2, dxp2, dym2, dyp2, dzm2, dzp2);
+              if (f > gamp(i, j, k) && itype == 0) {
+                gamp(i, j, k) = f;
+                upart(i, j, k) = A.omx; vpart(i, j, k) = A.omy; wpart(i, j, k) = A.omz;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  // (:480-530)
+  for (Arr3 *a : {&gamp, &gamu, &gamv, &gamw})
+    for (auto &x : a->d) x = 1. - x;
+  for (Arr3 *a : {&gamp, &gamu, &gamv, &gamw}) updthalos(c, *a, 1);
+  for (Arr3 *a : {&gamp, &gamu, &gamv, &gamw}) updthalos(c, *a, 2);
+  for (Arr3 *a : {&upart, &vpart, &wpart}) updthalos(c, *a, 1);
+  for (Arr3 *a : {&upart, &vpart, &wpart}) updthalos(c, *a, 2);
+  const int k1 = c->k1, kmax = c->kmax;
+  for (int j = 0; j <= c->j1; ++j)
+    for (int i = 0; i <= c->i1; ++i)
+      for (Arr3 *a : {&gamu, &gamv, &gamw, &gamp}) {
+        (*a)(i, j, 0) = (*a)(i, j, 1);
+        (*a)(i, j, k1) = (*a)(i, j, kmax);
+      }
+  for (int j = 0; j <= c->j1; ++j)
+    for (int i = 0; i <= c->i1; ++i) {
+      upart(i, j, 0) = -upart(i, j, 1);
+      vpart(i, j, 0) = -vpart(i, j, 1);
+      wpart(i, j, 0) = 0.;
+      upart(i, j, k1) = -upart(i, j, kmax);
+      vpart(i, j, k1) = -vpart(i, j, kmax);
+      wpart(i, j, kmax) = 0.;
+      wpart(i, j, k1) = wpart(i, j, kmax - 1);
+    }
+}
+
+// post1d (output.f90:13-917) without its file output: the plane sums
+// (:88-364), ghost values, normalisations and derived scalars (:178-566).
+// prof[q*(k1+1) + k] in the IBM_STAT_* order; entries the reference leaves
+// unset are 0.  The quadrant analysis after the routine's `return` (:585) is
+// dead code and not restated.
+void post1d(orc_ctx *c, double *prof, double *scal) {
+  const int kmax = c->kmax, k1 = c->k1, imax = c->imax, jmax = c->jmax;
+  const int nk = k1 + 1;
+  Arr3 gamu, gamv, gamw, gamp, upar, vpar, wpar;
+  for (Arr3 *a : {&gamu, &gamv, &gamw, &gamp, &upar, &vpar, &wpar}) a->init(0, c->i1 + 1, c->j1 + 1, k1 + 1);
+  if (c->np > 0) phase_indicator(c, 1, gamu, gamv, gamw, gamp, upar, vpar, wpar);
+  const Arr3 &U = c->unew, &V = c->vnew, &W = c->wnew, &P = c->pnew, &C = c->cnew;
+  std::vector<std::vector<double>> q(IBM_NSTAT, std::vector<double>(nk, 0.));
+  auto &um = q[IBM_STAT_UM], &vm = q[IBM_STAT_VM], &wm = q[IBM_STAT_WM], &pm = q[IBM_STAT_PM];
+  auto &u2 = q[IBM_STAT_U2], &v2 = q[IBM_STAT_V2], &w2 = q[IBM_STAT_W2], &p2 = q[IBM_STAT_P2];
+  auto &uv = q[IBM_STAT_UV], &uw = q[IBM_STAT_UW], &vw = q[IBM_STAT_VW];
+  auto &upm = q[IBM_STAT_UPM], &vpm = q[IBM_STAT_VPM], &wpm = q[IBM_STAT_WPM];
+  auto &up2 = q[IBM_STAT_UP2], &vp2 = q[IBM_STAT_VP2], &wp2 = q[IBM_STAT_WP2];
+  auto &upvp = q[IBM_STAT_UPVP], &upwp = q[IBM_STAT_UPWP], &vpwp = q[IBM_STAT_VPWP];
+  auto &gum = q[IBM_STAT_GUM], &gvm = q[IBM_STAT_GVM], &gwm = q[IBM_STAT_GWM], &gpm = q[IBM_STAT_GPM];
+  auto &gp2 = q[IBM_STAT_GP2], &guv = q[IBM_STAT_GUV], &guw = q[IBM_STAT_GUW], &gvw = q[IBM_STAT_GVW];
+  auto &ss = q[IBM_STAT_SS], &ssp = q[IBM_STAT_SSP];
+  auto &cm = q[IBM_STAT_CM], &c2 = q[IBM_STAT_C2], &wc = q[IBM_STAT_WC], &cdflx = q[IBM_STAT_CDFLX];
+  const bool parts = c->np > 0;
+  // first moments (:88-127); one thread per plane, as the reference's omp do
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j)
+      for (int i = 1; i <= imax; ++i) {
+        if (parts) {
+          um[k] = um[k] + U(i, j, k) * gamu(i, j, k);
+          vm[k] = vm[k] + V(i, j, k) * gamv(i, j, k);
+          wm[k] = wm[k] + W(i, j, k) * gamw(i, j, k);
+          pm[k] = pm[k] + P(i, j, k) * gamp(i, j, k);
+          cm[k] = cm[k] + C(i, j, k) * gamp(i, j, k);
+        } else {
+          um[k] = um[k] + U(i, j, k) * (1. - gamu(i, j, k));
+          vm[k] = vm[k] + V(i, j, k) * (1. - gamv(i, j, k));
+          wm[k] = wm[k] + W(i, j, k) * (1. - gamw(i, j, k));
+          pm[k] = pm[k] + P(i, j, k) * (1. - gamp(i, j, k));
+          cm[k] = cm[k] + C(i, j, k) * (1. - gamp(i, j, k));
+        }
+        upm[k] = upm[k] + upar(i, j, k) * (1. - gamu(i, j, k));
+        vpm[k] = vpm[k] + vpar(i, j, k) * (1. - gamv(i, j, k));
+        wpm[k] = wpm[k] + wpar(i, j, k) * (1. - gamw(i, j, k));
+        gum[k] = gum[k] + gamu(i, j, k);
+        gvm[k] = gvm[k] + gamv(i, j, k);
+        gwm[k] = gwm[k] + gamw(i, j, k);
+        gpm[k] = gpm[k] + gamp(i, j, k);
+      }
+  // (:178-200)
+  um[0] = -um[1]; um[k1] = -um[kmax];
+  vm[0] = -vm[1]; vm[k1] = -vm[kmax];
+  wm[0] = 0.; wm[kmax] = 0.; wm[k1] = wm[kmax - 1];
+  pm[0] = pm[1]; pm[k1] = pm[kmax];
+  upm[0] = -upm[1]; upm[k1] = -upm[kmax];
+  vpm[0] = -vpm[1]; vpm[k1] = -vpm[kmax];
+  wpm[0] = 0.; wpm[kmax] = 0.; wpm[k1] = wm[kmax - 1];
+  gum[0] = gum[1]; gum[k1] = gum[kmax];
+  gvm[0] = gvm[1]; gvm[k1] = gvm[kmax];
+  gwm[k1] = gwm[kmax - 1];
+  // second moments (:207-238); x**2. is x*x
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j)
+      for (int i = 1; i <= imax; ++i) {
+        const double uu = U(i, j, k), vv = V(i, j, k), ww = W(i, j, k), pp = P(i, j, k), cc = C(i, j, k);
+        if (parts) {
+          u2[k] = u2[k] + uu * uu * gamu(i, j, k);
+          v2[k] = v2[k] + vv * vv * gamv(i, j, k);
+          w2[k] = w2[k] + ww * ww * gamw(i, j, k);
+          p2[k] = p2[k] + pp * pp * gamp(i, j, k);
+          c2[k] = c2[k] + cc * cc * gamp(i, j, k);
+        } else {
+          u2[k] = u2[k] + uu * uu * (1. - gamu(i, j, k));
+          v2[k] = v2[k] + vv * vv * (1. - gamv(i, j, k));
+          w2[k] = w2[k] + ww * ww * (1. - gamw(i, j, k));
+          p2[k] = p2[k] + pp * pp * (1. - gamp(i, j, k));
+          c2[k] = c2[k] + cc * cc * (1. - gamp(i, j, k));
+        }
+        up2[k] = up2[k] + upar(i, j, k) * upar(i, j, k) * (1. - gamu(i, j, k));
+        vp2[k] = vp2[k] + vpar(i, j, k) * vpar(i, j, k) * (1. - gamv(i, j, k));
+        wp2[k] = wp2[k] + wpar(i, j, k) * wpar(i, j, k) * (1. - gamw(i, j, k));
+        gp2[k] = gp2[k] + gamp(i, j, k) * gamp(i, j, k);
+      }
+  // (:276-294)
+  u2[0] = -u2[1]; u2[k1] = -u2[kmax];
+  v2[0] = -v2[1]; v2[k1] = -v2[kmax];
+  w2[0] = 0.; w2[kmax] = 0.; w2[k1] = w2[kmax - 1];
+  p2[0] = p2[1]; p2[k1] = p2[kmax];
+  up2[0] = -up2[1]; up2[k1] = -up2[kmax];
+  vp2[0] = -vp2[1]; vp2[k1] = -vp2[kmax];
+  wp2[0] = 0.; wp2[kmax] = 0.; wp2[k1] = w2[kmax - 1];
+  gp2[0] = gp2[1]; gp2[k1] = gp2[kmax];
+  // products and fluxes (:301-355)
+  const double kappa = c->kappa, dzi = c->dzi;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j)
+      for (int i = 1; i <= imax; ++i) {
+        uv[k] = uv[k] + 0.25 * (U(i, j + 1, k) + U(i, j, k)) * (V(i + 1, j, k) + V(i, j, k)) *
+                            (0.25 * (gamu(i, j + 1, k) + gamu(i, j, k) + gamv(i + 1, j, k) + gamv(i, j, k)));
+        uw[k] = uw[k] + 0.25 * (U(i, j, k + 1) + U(i, j, k)) * (W(i + 1, j, k) + W(i, j, k)) *
+                            (0.25 * (gamu(i, j, k + 1) + gamu(i, j, k) + gamw(i + 1, j, k) + gamw(i, j, k)));
+        vw[k] = vw[k] + 0.25 * (V(i, j, k + 1) + V(i, j, k)) * (W(i, j + 1, k) + W(i, j, k)) *
+                            (0.25 * (gamv(i, j, k + 1) + gamv(i, j, k) + gamw(i, j + 1, k) + gamw(i, j, k)));
+        wc[k] = wc[k] + 0.5 * (C(i, j, k + 1) + C(i, j, k)) * W(i, j, k) * (1 - gamw(i, j, k));
+        cdflx[k] = cdflx[k] - kappa * (C(i, j, k + 1) - C(i, j, k)) * dzi;
+        upvp[k] = upvp[k] + 0.25 * (upar(i, j + 1, k) + upar(i, j, k)) * (vpar(i + 1, j, k) + vpar(i, j, k)) *
+                                (0.25 * (2. - gamu(i, j + 1, k) - gamu(i, j, k) + 2. - gamv(i + 1, j, k) -
+                                         gamv(i, j, k)));
+        upwp[k] = upwp[k] + 0.25 * (upar(i, j, k + 1) + upar(i, j, k)) * (wpar(i + 1, j, k) + wpar(i, j, k)) *
+                                (0.25 * (2. - gamu(i, j, k + 1) - gamu(i, j, k) + 2. - gamw(i + 1, j, k) -
+                                         gamw(i, j, k)));
+        vpwp[k] = vpwp[k] + 0.25 * (vpar(i, j, k + 1) + vpar(i, j, k)) * (wpar(i, j + 1, k) + wpar(i, j, k)) *
+                                (0.25 * (2. - gamv(i, j, k + 1) - gamv(i, j, k) + 2. - gamw(i, j + 1, k) -
+                                         gamw(i, j, k)));
+        guv[k] = guv[k] + 0.25 * (gamu(i, j + 1, k) + gamu(i, j, k) + (gamv(i + 1, j, k) + gamv(i, j, k)));
+        guw[k] = guw[k] + 0.25 * (gamu(i, j, k + 1) + gamu(i, j, k) + (gamw(i + 1, j, k) + gamw(i, j, k)));
+        gvw[k] = gvw[k] + 0.25 * (gamv(i, j, k + 1) + gamv(i, j, k) + (gamw(i, j + 1, k) + gamw(i, j, k)));
+      }
+  // (:401-422)
+  uv[0] = -uv[1]; uv[k1] = -uv[kmax];
+  uw[0] = 0.; uw[kmax] = 0.; uw[k1] = uw[kmax - 1];
+  vw[0] = 0.; vw[k1] = vw[kmax - 1]; vw[kmax] = 0.;
+  upvp[0] = -upvp[1]; upvp[k1] = -upvp[kmax];
+  upwp[0] = 0.; upwp[kmax] = 0.; upwp[k1] = upwp[kmax - 1];
+  vpwp[0] = 0.; vpwp[k1] = vpwp[kmax - 1]; vpwp[kmax] = 0.;
+  guv[0] = guv[1]; guv[k1] = guv[kmax];
+  guw[0] = guw[1]; guw[k1] = guw[kmax];
+  gvw[0] = gvw[1]; gvw[k1] = gvw[kmax];
+  // normalisation (:426-455); whole-array assignments read the old right-hand side
+  const double N = 1. * c->itot * c->jtot;
+  std::vector<double> vw_new(nk);
+  for (int k = 1; k <= kmax; ++k) {
+    const double du = parts ? gum[k] : N - gum[k], dv = parts ? gvm[k] : N - gvm[k];
+    const double dw = parts ? gwm[k] : N - gwm[k], dp = parts ? gpm[k] : N - gpm[k];
+    um[k] = um[k] / du; vm[k] = vm[k] / dv; wm[k] = wm[k] / dw;
+    cm[k] = cm[k] / dp; pm[k] = pm[k] / dp;
+  }
+  for (int k = 1; k <= kmax; ++k) {
+    const double du = parts ? gum[k] : N - gum[k], dv = parts ? gvm[k] : N - gvm[k];
+    const double dw = parts ? gwm[k] : N - gwm[k], dp = parts ? gpm[k] : N - gpm[k];
+    u2[k] = std::sqrt(u2[k] / du - um[k] * um[k]);
+    v2[k] = std::sqrt(v2[k] / dv - vm[k] * vm[k]);
+    w2[k] = std::sqrt(w2[k] / dw - wm[k] * wm[k]);
+    p2[k] = std::sqrt(p2[k] / dp - pm[k] * pm[k]);
+    c2[k] = std::sqrt(c2[k] / dp - cm[k] * cm[k]);
+  }
+  for (int k = 1; k <= kmax; ++k) {
+    const double dvw = parts ? gvw[k] : N - gvw[k];
+    vw_new[k] = vw[k] / dvw - 0.5 * (vm[k] + vm[k + 1]) * wm[k];
+  }
+  for (int k = 1; k <= kmax; ++k) vw[k] = vw_new[k];
+  vw[0] = 0.;
+  // (:457-477)
+  double umax = u2[0];
+  for (int k = 1; k <= k1; ++k) umax = std::max(umax, u2[k]);
+  const double re_rbc = umax * c->lz / c->visc;
+  for (int k = 1; k <= kmax; ++k) {
+    wc[k] = wc[k] / (N - gwm[k]);
+    cdflx[k] = cdflx[k] / (N - gwm[k]);
+  }
+  const double visc = c->visc;
+  vm[0] = -vm[1]; vm[k1] = -vm[kmax];
+  for (int k = 1; k <= kmax; ++k) ss[k] = (vm[k + 1] - vm[k]) * dzi * visc;
+  ss[0] = (vm[1] - vm[0]) * dzi * visc;
+  um[0] = -um[1]; um[k1] = -um[kmax];
+  for (int k = 1; k <= kmax; ++k) {
+    const double t = (um[k + 1] - um[k]) * dzi * visc;
+    ss[k] = std::sqrt(ss[k] * ss[k] + t * t);
+  }
+  {
+    const double t = (um[1] - um[0]) * dzi * visc;
+    ss[0] = std::sqrt(ss[0] * ss[0] + t * t);
+  }
+  const double grad_k_wall = dzi * (std::sqrt(0.5 * (u2[1] * u2[1] + v2[1] * v2[1] + w2[1] * w2[1])) -
+                                    std::sqrt(0.5 * (u2[0] * u2[0] + v2[0] * v2[0] + w2[0] * w2[0])));
+  const double u_tau = std::sqrt(visc * grad_k_wall);
+  const double re_tau = u_tau * c->lz / visc;
+  double wcs = 0., cds = 0.;
+  for (int k = 1; k <= kmax; ++k) wcs = wcs + wc[k];
+  for (int k = 1; k <= kmax; ++k) cds = cds + cdflx[k];
+  const double wc_avg = wcs / kmax, cdflx_avg = cds / kmax;
+  const double nu = c->lz / (kappa * (c->bc_c_bot_val - c->bc_c_top_val)) * (wc_avg + cdflx_avg);
+  // particle phase (:549-566)
+  std::vector<double> vpwp_new(nk);
+  for (int k = 1; k <= kmax; ++k) {
+    upm[k] = upm[k] / (N - gum[k]);
+    vpm[k] = vpm[k] / (N - gvm[k]);
+    wpm[k] = wpm[k] / (N - gwm[k]);
+  }
+  for (int k = 1; k <= kmax; ++k) {
+    up2[k] = std::sqrt(up2[k] / (N - gum[k]) - upm[k] * upm[k]);
+    vp2[k] = std::sqrt(vp2[k] / (N - gvm[k]) - vpm[k] * vpm[k]);
+    wp2[k] = std::sqrt(wp2[k] / (N - gwm[k]) - wpm[k] * wpm[k]);
+  }
+  for (int k = 1; k <= kmax; ++k) vpwp_new[k] = vpwp[k] / (N - gvw[k]) - 0.5 * (vpm[k] + vpm[k + 1]) * wpm[k];
+  for (int k = 1; k <= kmax; ++k) vpwp[k] = vpwp_new[k];
+  vpwp[0] = 0.;
+  vpm[0] = -vpm[1]; vpm[k1] = -vpm[kmax];
+  for (int k = 1; k <= kmax; ++k) ssp[k] = (vpm[k + 1] - vpm[k]) * dzi * visc;
+  ssp[0] = (vpm[1] - vpm[0]) * dzi * visc;
+  if (prof)
+    for (int n = 0; n < IBM_NSTAT; ++n) std::memcpy(prof + (size_t)n * nk, q[n].data(), nk * sizeof(double));
+  if (scal) { scal[0] = re_tau; scal[1] = u_tau; scal[2] = nu; scal[3] = re_rbc; scal[4] = grad_k_wall; }
 }
 
 void copy_in(orc_ctx *c, Arr3 &a, const double *src) {
@@ -1686,6 +2158,39 @@ int orc_diagnostics(orc_ctx *c, double *wsn, double *wso, double ft[3]) {
   if (wsn) *wsn = c->wallshearnew;
   if (wso) *wso = c->wallshearold;
   if (ft) { ft[0] = c->forcetot[0]; ft[1] = c->forcetot[1]; ft[2] = c->forcetot[2]; }
+  return IBM_OK;
+}
+
+int orc_set_scalar(orc_ctx *c, const ibm_scalar_params *sp, const double *cf, const double *dcrk) {
+  if (!sp || !(sp->pran > 0.)) return fail(c, IBM_E_INVALID, "scalar parameters need pran > 0");
+  c->kappa = c->visc / sp->pran;  // init.f90:94
+  c->beta = sp->beta;
+  c->bc_c_top_val = sp->bc_c_top_val; c->bc_c_bot_val = sp->bc_c_bot_val;
+  c->bc_c_top_type = sp->bc_c_top_type; c->bc_c_bot_type = sp->bc_c_bot_type;
+  copy_in(c, c->cnew, cf);
+  copy_in(c, c->dcrk, dcrk);
+  boundscal(c, c->cnew);  // as the driver does after loading (main.f90:198)
+  c->have_scalar = true;
+  return IBM_OK;
+}
+int orc_get_scalar(orc_ctx *c, double *cf, double *dcrk) {
+  copy_out(c->cnew, cf);
+  copy_out(c->dcrk, dcrk);
+  return IBM_OK;
+}
+int orc_phase_indicator(orc_ctx *c, int itype, double *gamu, double *gamv, double *gamw, double *gamp,
+                        double *upart, double *vpart, double *wpart) {
+  if (itype != 0 && itype != 1) return fail(c, IBM_E_INVALID, "itype must be 0 or 1");
+  Arr3 a[7];
+  for (auto &x : a) x.init(0, c->i1 + 1, c->j1 + 1, c->k1 + 1);
+  phase_indicator(c, itype, a[0], a[1], a[2], a[3], a[4], a[5], a[6]);
+  double *out[7] = {gamu, gamv, gamw, gamp, upart, vpart, wpart};
+  for (int n = 0; n < 7; ++n) copy_out(a[n], out[n]);
+  return IBM_OK;
+}
+int orc_post1d(orc_ctx *c, double *profiles, double *scalars) {
+  if (!c->have_fields) return fail(c, IBM_E_STATE, "no fields set");
+  post1d(c, profiles, scalars);
   return IBM_OK;
 }
 

@@ -46,6 +46,11 @@ int orc_chkdiv(orc_ctx *c, double *divtot, double *divmax, int ijk[3]);
 int orc_chkdt(orc_ctx *c, double *dtmax);
 int orc_slip_residual(orc_ctx *c, double *maxres, double *rmsres);
 int orc_diagnostics(orc_ctx *c, double *wallshearnew, double *wallshearold, double forcetot[3]);
+int orc_set_scalar(orc_ctx *c, const ibm_scalar_params *sp, const double *cf, const double *dcrk);
+int orc_get_scalar(orc_ctx *c, double *cf, double *dcrk);
+int orc_phase_indicator(orc_ctx *c, int itype, double *gamu, double *gamv, double *gamw, double *gamp,
+                        double *upart, double *vpart, double *wpart);
+int orc_post1d(orc_ctx *c, double *profiles, double *scalars);
 /* pins */
 double orc_kernel(double r);
 double orc_kerneltest(void);
