@@ -769,7 +769,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
-                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ph.G, c->ph.W, c->stat_part,
+                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
                   c->cfield, c->cnext, c->crk};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -1215,20 +1215,38 @@ int ibm_get_scalar(ibm_ctx *c, double *cf, double *dcrk) {
 }
 
 static int run_phase_indicator(ibm_ctx *c, int itype) {
+  if (c->pg.np >= (1 << 20)) return set_err(c, IBM_E_INVALID, "phase indicator: more than 2^20 particles");
+  // widest box (phase_indicator.f90:255-273): 2 r/dx + 4 cells plus rounding
+  const int nx = (int)std::ceil(2. * c->prm.radius * c->g.dxi) + 6, ny = (int)std::ceil(2. * c->prm.radius * c->g.dyi) + 6;
+  const size_t smem = phase_smem_bytes(nx, ny);
+  if (smem > 227 * 1024) return set_err(c, IBM_E_INVALID, "phase indicator: sphere too wide for the plane tables");
   if (!c->ph.G) {
     const size_t nc = (size_t)c->g.I * c->g.J * c->g.K;
     CK(cudaMalloc((void **)&c->ph.G, 4 * nc * sizeof(unsigned long long)));
-    CK(cudaMalloc((void **)&c->ph.W, 4 * nc * sizeof(int)));
+    CK(cudaMalloc((void **)&c->ph.W0, 4 * nc * sizeof(unsigned long long)));
+    CK(cudaMalloc((void **)&c->ph.W1, 4 * nc * sizeof(int)));
+    if (smem > 48 * 1024 && phase_set_smem(smem)) return set_err(c, IBM_E_CUDA, "phase indicator: shared memory");
   }
-  PROBED(IBM_PROBE_PHASE, launch_phase_indicator(c->stream, c->g, c->pg, c->pb, c->ph, itype));
+  c->ph.err = c->pb.err + 5;
+  PROBED(IBM_PROBE_PHASE, launch_phase_indicator(c->stream, c->g, c->pg, c->pb, c->ph, itype, nx, ny));
   LAUNCHED(c->pg.np > 0 ? 2 : 0);
+  return IBM_OK;
+}
+
+static int phase_check(ibm_ctx *c) {
+  if (c->pg.np == 0) return IBM_OK;
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, c->pb.err + 5, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (h) return set_err(c, IBM_E_INVALID, "phase indicator: a box exceeded its tables");
   return IBM_OK;
 }
 
 static PhaseView phase_view(const ibm_ctx *c, int itype, bool parts) {
   PhaseView v;
   v.G = c->ph.G;
-  v.W = c->ph.W;
+  v.W0 = c->ph.W0;
+  v.W1 = c->ph.W1;
   v.pf = c->pb.pf;
   v.np = c->pg.np;
   v.I = c->g.I; v.J = c->g.J; v.K = c->g.K;
@@ -1256,8 +1274,7 @@ int ibm_phase_indicator(ibm_ctx *c, int itype, double *gamu, double *gamv, doubl
     CK(cudaMemcpyAsync(out[f], c->href, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
-  CK(cudaStreamSynchronize(c->stream));
-  return IBM_OK;
+  return phase_check(c);
 }
 
 // Ghost values, normalisations and derived scalars of post1d
@@ -1389,8 +1406,8 @@ int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
   int st;
   if (parts && (st = run_phase_indicator(c, 1))) return st;
   const int K = c->g.K;
-  // slices per plane: about four blocks per SM in all
-  const int slices = std::max(1, std::min(64, (608 + K - 1) / K));
+  // slices per plane: about four waves of three 128-thread blocks per SM
+  const int slices = std::max(1, std::min(64, (1824 + K - 1) / K));
   const size_t np = (size_t)K * slices * POST1D_NSUM;
   if (c->stat_cap < np) {
     if (c->stat_part) cudaFree(c->stat_part);
@@ -1410,6 +1427,7 @@ int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
   std::vector<double> part(np), S((size_t)K * POST1D_NSUM, 0.);
   CK(cudaMemcpyAsync(part.data(), c->stat_part, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (parts && (st = phase_check(c))) return st;
   for (int k = 0; k < K; ++k)
     for (int s = 0; s < slices; ++s)
       for (int n = 0; n < POST1D_NSUM; ++n)

@@ -134,6 +134,26 @@ __device__ __forceinline__ int box_off(const CompStencil &s, const int *bg, int 
 __device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__ F, const int *bg, float *box) {
   const int nbx = bg[5], nby = bg[6], nxy = nbx * nby, nbox = nxy * bg[7];
   const int x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
+  if ((g.I & 3) == 0) {
+    // rows read as 16-byte quads of x-cells (aligned: I is a multiple of 4,
+    // so a quad never straddles the periodic wrap); cells outside the row
+    // are dropped
+    const int a0 = x0 - (((x0 % 4) + 4) % 4);
+    const int nq = (x0 + nbx - a0 + 3) >> 2, nrow = nby * bg[7];
+    for (int e = threadIdx.x; e < nrow * nq; e += blockDim.x) {
+      const int row = e / nq, t = e - row * nq;
+      const int cz = row / nby, cy = row - cz * nby, gx = a0 + 4 * t;
+      const float4 v =
+          __ldg(reinterpret_cast<const float4 *>(&F[fidx(g, wrapm(gx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]));
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int d = 0; d < 4; ++d) {
+        const int cx = gx + d - x0;
+        if (cx >= 0 && cx < nbx) box[row * nbx + cx] = vv[d];
+      }
+    }
+    return;
+  }
   for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
     const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
     box[q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
@@ -334,6 +354,27 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
   if (!boxed) return;
   __syncthreads();
   const int nxy = nbx * nby, x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
+  if ((g.I & 3) == 0) {
+    // flush by 16-byte quads of x-cells (rows padded with zeros to the
+    // aligned quads that cover them; with I a multiple of 4 a quad never
+    // straddles the periodic wrap): one vector atomic per nonzero quad
+    const int a0 = x0 - (((x0 % 4) + 4) % 4);
+    const int nq = (x0 + nbx - a0 + 3) >> 2, nrow = nby * bg[7];
+    for (int e = threadIdx.x; e < nrow * nq; e += blockDim.x) {
+      const int row = e / nq, t = e - row * nq;
+      const int cz = row / nby, cy = row - cz * nby, gx = a0 + 4 * t;
+      float v[4];
+#pragma unroll
+      for (int d = 0; d < 4; ++d) {
+        const int cx = gx + d - x0;
+        v[d] = (cx >= 0 && cx < nbx) ? hi[row * nbx + cx] + lo[row * nbx + cx] : 0.f;
+      }
+      if (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f && v[3] == 0.f) continue;
+      float4 *dst = reinterpret_cast<float4 *>(&F[fidx(g, wrapm(gx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
+      atomicAdd(dst, make_float4(v[0], v[1], v[2], v[3]));
+    }
+    return;
+  }
   for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
     const float v = hi[q] + lo[q];
     if (v != 0.f) {

@@ -184,16 +184,22 @@ constexpr unsigned long long PH_INNER = 0x7FF0000000000000ull;  // +inf bits: ab
 constexpr int POST1D_NSUM = 32;  // plane sums of output.f90:88-355
 struct PhaseBuffers {
   unsigned long long *G;  // [4][K*I*J] largest candidate key per cell (grids u, v, w, p)
-  int *W;                 // [4][K*I*J] winner code per cell
+  unsigned long long *W0; // [4][K*I*J] sum over candidates of (1 << 32) + code: count and, if one, its code
+  int *W1;                // [4][K*I*J] winner code of cells with several candidates
+  int *err;               // error flag (a box wider than the plane tables)
 };
+// shared memory of the marking pass for boxes of up to nx x ny cells
+size_t phase_smem_bytes(int nx, int ny);
+int phase_set_smem(size_t bytes);
 void launch_phase_indicator(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, PhaseBuffers ph,
-                            int itype);
+                            int itype, int nxmax, int nymax);
 // Reads of the phase fields at reference indices i, j in 1..I/J (periodic
 // halos wrapped by the caller) and k in 0..K+1 with the wall ghost rules of
 // phase_indicator.f90:497-530.
 struct PhaseView {
   const unsigned long long *G;
-  const int *W;
+  const unsigned long long *W0;
+  const int *W1;
   const double *pf;
   int np, I, J, K, itype;
   bool parts;  // false: np = 0, post1d's zero fields (output.f90:41-49)
@@ -202,23 +208,25 @@ struct PhaseView {
   __device__ __forceinline__ long cell(int i, int j, int k) const {
     return (long)(k - 1) * I * J + (long)(j - 1) * I + (i - 1);
   }
+  __device__ __forceinline__ long grid_off(int c) const { return (long)c * I * J * K; }
+  // solid fraction encoded by a key
+  __device__ __forceinline__ static double solid(unsigned long long key) {
+    return key == 0ull ? 0. : (key == PH_INNER ? 1. : __longlong_as_double((long long)key));
+  }
   // fluid fraction of grid c (0..3)
   __device__ __forceinline__ double gam(int c, int i, int j, int k) const {
     if (!parts) return 0.;
     if (k < 1) k = 1;
     if (k > K) k = K;
-    const unsigned long long key = G[(long)c * I * J * K + cell(i, j, k)];
-    const double s = key == 0ull ? 0. : (key == PH_INNER ? 1. : __longlong_as_double((long long)key));
-    return 1. - s;
+    return 1. - solid(G[grid_off(c) + cell(i, j, k)]);
   }
-  // rigid-body velocity component c (0..2) at an interior cell
-  __device__ double part_in(int c, int i, int j, int k) const {
-    const int grid = itype == 1 ? c : 3;
-    const long off = (long)grid * I * J * K + cell(i, j, k);
-    const unsigned long long key = G[off];
+  // rigid-body velocity component c (0..2) at an interior cell whose key on
+  // the velocity's grid is `key` (element `off` of that grid's arrays)
+  __device__ double part_key(int c, unsigned long long key, long off, int i, int j, int k) const {
     if (key == 0ull) return 0.;
-    const int w = W[off];
-    if (w <= 0) return 0.;  // no winner recorded (not reached: pass 1 repeats pass 0's keys)
+    const unsigned long long w0 = W0[off];
+    const int w = (w0 >> 32) == 1 ? (int)(w0 & 0xFFFFFFFFull) : W1[off];
+    if (w <= 0) return 0.;  // no winner recorded (not reached: the resolving pass repeats the keys)
     const int q = key == PH_INNER ? w - 1 : 9 * np + 1 - w;
     const int p = q / 9, nb = q - 9 * p;
     if (nb > 0) return 0.;  // the copies carry no velocity (phase_indicator.f90:68-78, 83-87)
@@ -228,6 +236,10 @@ struct PhaseView {
     if (c == 0) return pf[(long)PF_U * np + p] + omy * ((k - 0.5) * dz - z) - omz * ((j - 0.5) * dy - y);
     if (c == 1) return pf[(long)PF_V * np + p] + omz * ((i - 0.5) * dx - x) - omx * ((k - 0.5) * dz - z);
     return pf[(long)PF_W * np + p] + omx * ((j - 0.5) * dy - y) - omy * ((i - 0.5) * dx - x);
+  }
+  __device__ double part_in(int c, int i, int j, int k) const {
+    const long off = grid_off(itype == 1 ? c : 3) + cell(i, j, k);
+    return part_key(c, G[off], off, i, j, k);
   }
   __device__ double part(int c, int i, int j, int k) const {
     if (!parts) return 0.;
