@@ -128,6 +128,20 @@ def measured_peaks() -> dict:
     return {}
 
 
+def fp64_peak() -> float | None:
+    """Measured FP64 FMA rate of this GPU (TFLOP/s) through the library's
+    calibration kernel; None when the library lacks it."""
+    import ctypes as C
+
+    from interparts_mpich_gb300.solver import load_library
+
+    _, fn = load_library()
+    if "fp64_peak" not in fn:
+        return None
+    t = C.c_double()
+    return t.value if fn["fp64_peak"](C.byref(t)) == 0 else None
+
+
 def sphere_box(case) -> int:
     return int(round(2 * case.radius * case.dxi + 5)) ** 3
 
@@ -160,6 +174,12 @@ TRAFFIC = {
 }
 
 
+# FP64 flops per cell of the FP64 predictor (momxad/momyad/momzad 3 x 54,
+# pressure gradient 6, RK combination 12-18): the plain form's predictor is
+# bound by the FP64 pipe, not by HBM
+PREDICT_FP64_FLOPS = 183
+
+
 def kernel_model(case, w: int) -> dict:
     """Algorithmic bytes (or flops) per launch of each probed kernel class, in
     the reference dataflow model (words of distinct compulsory traffic):
@@ -167,12 +187,13 @@ def kernel_model(case, w: int) -> dict:
     spectrum word, each spectrum pass 2 words, correc 9 words (11 with the
     double-float pressure), IBM interpolation 3 and spreading 6 words per
     footprint cell S_fp, sphere integrals 3 box words per sphere; the MLP in
-    flops (2 x 29,184 per point)."""
+    flops (2 x 29,184 per point); the FP64 predictor in FP64 flops."""
     n = case.itot * case.jtot * case.ktot
     ibm = s_fp(case) * case.np
     npts = case.np * case.nl
     return {
-        "predict": ("hbm", 11 * n * w), "stencil": ("hbm", npts * (24 + (96 if w == 4 else 168))),
+        "predict": ("fp64", PREDICT_FP64_FLOPS * n) if w == 8 else ("hbm", 11 * n * w),
+        "stencil": ("hbm", npts * (24 + (96 if w == 4 else 168))),
         "interp": ("hbm", 3 * ibm * w), "spread": ("hbm", 6 * ibm * w),
         "fillps_fftx": ("hbm", 4 * n * w), "ffty": ("hbm", 2 * n * w), "thomas": ("hbm", 2 * n * w),
         "ifftx": ("hbm", 2 * n * w), "correc": ("hbm", (11 if w == 4 else 9) * n * w),
@@ -217,6 +238,8 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
 
     case = channel_case(args.n, args.np, seed=1234)
     solver = IBMSolver(case, mode=mode)
+    if args.proj_solves and mode != 0:
+        solver.set_projection_solves(args.proj_solves)
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
     solver.setup(case.initial_fields())
@@ -342,9 +365,11 @@ def main():
     ap.add_argument("--form", default="all", choices=["all", "both", "plain", "mixed", "learned"])
     ap.add_argument("--harvest", type=int, default=2_000_000, help="harvest capacity (samples)")
     ap.add_argument("--harvest-passes", type=int, default=6)
-    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--stats-calls", type=int, default=3, help="post1d calls timed after the steps (0: none)")
+    ap.add_argument("--proj-solves", type=int, default=0,
+                    help="FP32 Poisson solves per projection in the mixed forms (0: the library default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -400,6 +425,9 @@ def main():
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
     tflops = peaks.get("bf16_tflops", 1900.0)
+    fp64 = fp64_peak()
+    peak_of = {"hbm": hbm, "tensor": tflops, "fp64": fp64 or float("nan")}
+    unit_of = {"hbm": "GB/s", "tensor": "TFLOP/s", "fp64": "TFLOP/s"}
     w = 8 if head == "plain" else 4
 
     def kernel_table(x, wb):
@@ -411,11 +439,11 @@ def main():
             bound, units = model[name]
             per = tot_ms / cnt
             ach = units / (per * 1e-3) / (1e9 if bound == "hbm" else 1e12)
-            peak = hbm if bound == "hbm" else tflops
+            peak = peak_of[bound]
             out[name] = {"launches_per_step": round(cnt / args.steps, 2), "ms_per_launch": round(per, 4),
                          "share_of_step": round(tot_ms / args.steps / x["ms"], 4), "bound": bound,
-                         "algorithmic_per_launch": int(units), "achieved": round(ach, 1),
-                         "unit": "GB/s" if bound == "hbm" else "TFLOP/s", "frac": round(ach / peak, 4)}
+                         "algorithmic_per_launch": int(units), "achieved": round(ach, 3 if bound == "fp64" else 1),
+                         "unit": unit_of[bound], "frac": round(ach / peak, 4)}
         return out
     ab = algorithmic_bytes(case, w)
     names = ["predictor", "ibm", "projection", "newton_euler"]
@@ -439,11 +467,13 @@ def main():
         "mcell_steps_per_s": round(args.gpus * r["ncell"] / (r["ms"] * 1e-3) / 1e6, 1),
         "hbm_roofline_frac_step": round(ab["total"] / (r["ms"] * 1e-3) / 1e9 / hbm, 4),
         "roofline": {"bound": dk["bound"], "kernel": dom, "achieved": dk["achieved"],
-                     "peak": hbm if dk["bound"] == "hbm" else tflops, "unit": dk["unit"], "frac": dk["frac"],
+                     "peak": peak_of[dk["bound"]], "unit": dk["unit"], "frac": dk["frac"],
                      "traffic": TRAFFIC.get((head, dom)),
                      "algorithmic_per_launch": dk["algorithmic_per_launch"], "ms_per_launch": dk["ms_per_launch"],
-                     "peak_source": ("MEASURED_PEAKS.json " + ("hbm_gbs" if dk["bound"] == "hbm" else "bf16_tflops")
-                                     + " (of measured)") if peaks else "fallback (of fallback)"},
+                     "peak_source": ("ibm_fp64_peak, FMA chains on all SMs (of measured)" if dk["bound"] == "fp64"
+                                     else ("MEASURED_PEAKS.json " + ("hbm_gbs" if dk["bound"] == "hbm" else "bf16_tflops")
+                                           + " (of measured)") if peaks else "fallback (of fallback)")},
+        "fp64_peak_tflops": round(fp64, 4) if fp64 else None,
         "kernels": ktab,
         "gpu_launches": int(r["launches"]),
         "clocks": r["clocks"],

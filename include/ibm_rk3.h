@@ -168,6 +168,15 @@ int ibm_run(ibm_ctx *ctx, double dt, int nsteps);
  * out: current) and time (may be NULL) are updated in place. */
 int ibm_run_adaptive(ibm_ctx *ctx, int nsteps, int ioutchk, double *dt, double *time);
 
+/* Mixed forms: FP32 Poisson solves per projection.  1 (default): one solve
+ * of fillps(u*) (double-float Thomas sweep), one correction into the FP32
+ * velocity and the double-float pnew; 2: that solve plus one defect-
+ * correction solve driven by the double-float divergence residual of the
+ * corrected state.  Both end with the divergence at the FP32 rounding level
+ * of the velocity state.  The FP64 form always solves once in FP64 (only 1
+ * is accepted there). */
+int ibm_set_projection_solves(ibm_ctx *ctx, int solves);
+
 /* --- diagnostics ----------------------------------------------------------- */
 
 /* chkdiv (chkdiv.f90:7-61): total and max |div| of (unew,vnew,wnew) and the
@@ -370,6 +379,13 @@ int ibm_mlp_fit(ibm_ctx *ctx, const float *params_in, const float *x, const floa
  * summed milliseconds and the number of launches timed, and stops probing. */
 int ibm_probe(ibm_ctx *ctx, unsigned mask);
 int ibm_probe_result(ibm_ctx *ctx, double ms[IBM_PROBE_N], int launches[IBM_PROBE_N]);
+
+/* --- calibration (no counterpart in the reference) --------------------------- */
+
+/* FP64 fused multiply-add rate of the current device in TFLOP/s, measured with
+ * independent FMA chains on all SMs: the roofline denominator of the kernels
+ * whose bound is the FP64 pipe (GB300 issues FP64 at 1/64 of the FP32 rate). */
+int ibm_fp64_peak(double *tflops);
 
 /* --- allocation-free variant ------------------------------------------------ */
 

@@ -170,6 +170,8 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "chkdiv_noalloc": (C.c_int, [c_double_p, c_double_p, c_double_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_double, C.c_double, c_double_p, C.c_void_p]),
         "run_adaptive": (C.c_int, [ctx, C.c_int, C.c_int, c_double_p, c_double_p]),
+        "fp64_peak": (C.c_int, [c_double_p]),
+        "set_projection_solves": (C.c_int, [ctx, C.c_int]),
         "probe": (C.c_int, [ctx, C.c_uint]),
         "probe_result": (C.c_int, [ctx, c_double_p, c_int_p]),
         "harvest": (C.c_int, [ctx, C.c_int, C.c_int, C.c_int]),

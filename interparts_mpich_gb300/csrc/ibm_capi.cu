@@ -70,7 +70,7 @@ struct ibm_ctx {
   int mt_cap = 0;              // batch capacity of mt
   float *norm = nullptr;       // [198]: feature mean, 1/sigma; target mean, sigma
   __nv_bfloat16 *lx = nullptr; // [np*nl][96] standardised features
-  float *ly = nullptr, *ldf = nullptr;  // [np*nl][3] network output, force increment
+  float *ly = nullptr;         // [np*nl][3] network output
   double *ls = nullptr;        // learn state, see k_ibm_res_gate
   int *gate = nullptr;
   HarvestArgs hv{};
@@ -98,6 +98,7 @@ struct ibm_ctx {
   double *cnext = nullptr;      // dcdt of the substep: cnew after the projection
   double *crk = nullptr;        // dcrkold, the scalar's stored right-hand side
   bool c_pending = false;       // cnext holds this substep's scalar
+  int proj_solves = 1;          // mixed forms: FP32 Poisson solves per projection (2: defect correction)
   ibm_scalar_params sp{};
   double kappa = 0.;
 };
@@ -446,7 +447,6 @@ int alloc_all(ibm_ctx *c) {
       const size_t npl = (size_t)np * nl;
       if ((st = dalloc(c, &c->lx, npl * 96))) return st;
       if ((st = dalloc(c, &c->ly, npl * 3))) return st;
-      if ((st = dalloc(c, &c->ldf, npl * 3))) return st;
     }
   }
   return IBM_OK;
@@ -506,25 +506,26 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   const Geo &g = c->g;
   const long npts = (long)c->pg.np * c->pg.nl;
   PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
-  HarvestArgs none{};
-  (void)none;
   PROBED(IBM_PROBE_FEATURES, launch_ibm_features_comp(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt,
                                                       c->norm, c->norm + 96, c->lx));
   launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
   LAUNCHED(4);
   PROBED(IBM_PROBE_MLP, launch_mlp_infer_tc(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly,
                                             c->pb.err + 4));
-  launch_ibm_learned_apply(c->stream, c->pg, c->ib, c->ly, c->norm + 192, c->norm + 195, dt, c->ldf);
-  PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, c->ldf));
+  // F = F0 + the network's correction per point, its force and torque sums,
+  // one spreading
+  const LearnedForce lf{c->ly, c->norm + 192, c->norm + 195, 1. / dt};
+  PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, lf));
+  launch_ibm_force_sums(c->stream, c->pg, c->ib);
   PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
                                                                          c->fv32, c->fw32, dt, -1));
-  launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 0);
-  LAUNCHED(6);
+  launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 0);
+  LAUNCHED(5);
   for (int it = 1; it < nl_iter; ++it) {
     PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
                                                                            c->fv32, c->fw32, dt, 0, c->gate));
     PROBED(IBM_PROBE_SPREAD,
-           launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, nullptr, c->gate));
+           launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, LearnedForce{}, c->gate));
     LAUNCHED(2);
   }
   return IBM_OK;
@@ -560,8 +561,8 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
       if (c->harvesting && it == nl_iter - 1) {
         // the plain method's residual at its own number of passes
         PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
-        launch_ibm_residual_gate(c->stream, c->pg, c->ib, c->scratch, npts, c->ls, c->gate, 1);
-        LAUNCHED(3);
+        launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 1);
+        LAUNCHED(2);
       }
     }
     if (c->harvesting) {
@@ -591,6 +592,19 @@ int project_fluid(ibm_ctx *c, int rkiter, double dt) {
   const double dti = 1. / (c->rkab[rkiter - 1] * dt);
   int nl = 0;
   const double factor = c->rkab[rkiter - 1] * dt;
+  if (c->mixed && c->proj_solves == 1) {
+    // one FP32 solve of fillps(u*) and one correction into the FP32 state
+    // and the double-float pnew
+    launch_poisson<float, float>(c->stream, g, c->plx, c->ply, c->fu32, c->fv32, c->fw32, c->spec32, c->phi32,
+                                 c->twM32, c->twN32, c->twJ32, c->zt, dti * g.dxi, dti * g.dyi, dti * g.dzi, &nl,
+                                 false, c->thomas_df, PoissonHook{poisson_probe, c});
+    LAUNCHED(nl);
+    PROBED(IBM_PROBE_CORREC, launch_correc_mixed(c->stream, g, c->fu32, c->fv32, c->fw32, c->phi32, c->u32, c->v32,
+                                                 c->w32, c->p32, c->plo32, factor * g.dxi, factor * g.dyi,
+                                                 factor * g.dzi));
+    LAUNCHED(1);
+    return IBM_OK;
+  }
   if (c->mixed && poisson_fused_residual_ok(g)) {
     // FP32 solve of fillps(u*) -> phi1; one defect correction: the divergence
     // residual of u* - f grad(phi1), evaluated in double-float, drives a
@@ -774,7 +788,7 @@ int ibm_destroy(ibm_ctx *c) {
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
-                   c->norm, c->ls, c->gate, c->lx, c->ly, c->ldf, c->hv.feat, c->hv.pidx, c->hv.targ,
+                   c->norm, c->ls, c->gate, c->lx, c->ly, c->hv.feat, c->hv.pidx, c->hv.targ,
                    c->hv.count, c->tx, c->tt};
   for (void *q : lptrs)
     if (q) cudaFree(q);
@@ -1433,6 +1447,14 @@ int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
       for (int n = 0; n < POST1D_NSUM; ++n)
         S[(size_t)k * POST1D_NSUM + n] += part[((size_t)k * slices + s) * POST1D_NSUM + n];
   post1d_finish(c, S, parts, prof, scal);
+  return IBM_OK;
+}
+
+int ibm_set_projection_solves(ibm_ctx *c, int solves) {
+  if (!c) return IBM_E_INVALID;
+  if (solves != 1 && solves != 2) return set_err(c, IBM_E_INVALID, "projection solves must be 1 or 2");
+  if (!c->mixed) return solves == 1 ? IBM_OK : set_err(c, IBM_E_STATE, "the FP64 form solves once");
+  c->proj_solves = solves;
   return IBM_OK;
 }
 

@@ -283,89 +283,25 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
   k_ibm_harvest_targets<<<152, 256, 0, s>>>(b, H, dt);
   k_ibm_harvest_close<<<1, 32, 0, s>>>(H);
 }
-
-// learned update: F = F0 + Y/dt per point (Y de-standardised), the total F
-// to dF for the one spreading of the loop, and the per-particle force and
-// torque sums of F (as updtlagrforces computes them)
-__global__ void __launch_bounds__(256) k_ibm_learned_apply(PartGeo pg, IbmBuffers b, const float *__restrict__ Y,
-                                                           const float *__restrict__ tmu,
-                                                           const float *__restrict__ tsig, double dti,
-                                                           float *__restrict__ dF) {
-  const int p = blockIdx.x;
-  const int nla = b.nla[p];
-  const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
-  double sfx = 0, sfy = 0, sfz = 0, stx = 0, sty = 0, stz = 0;
-  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
-    const long t = (long)p * pg.nl + l;
-    const double dx = (double)(Y[3 * t] * tsig[0] + tmu[0]) * dti;
-    const double dy = (double)(Y[3 * t + 1] * tsig[1] + tmu[1]) * dti;
-    const double dz = (double)(Y[3 * t + 2] * tsig[2] + tmu[2]) * dti;
-    const double fx = b.fxl[t] + dx, fy = b.fyl[t] + dy, fz = b.fzl[t] + dz;
-    b.fxl[t] = fx; b.fyl[t] = fy; b.fzl[t] = fz;
-    dF[3 * t] = (float)fx; dF[3 * t + 1] = (float)fy; dF[3 * t + 2] = (float)fz;  // total force, spread once
-    const double rx = b.xfp[t] - px, ry = b.yfp[t] - py, rz = b.zfp[t] - pz;
-    sfx += fx; sfy += fy; sfz += fz;
-    stx = stx + ry * fz - rz * fy;
-    sty = sty + rz * fx - rx * fz;
-    stz = stz + rx * fy - ry * fx;
-  }
-  __shared__ double red[6][256];
-  red[0][threadIdx.x] = sfx; red[1][threadIdx.x] = sfy; red[2][threadIdx.x] = sfz;
-  red[3][threadIdx.x] = stx; red[4][threadIdx.x] = sty; red[5][threadIdx.x] = stz;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o)
-      for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double *pw = b.pf;
-    const double dV = pg.dVlagr;
-    const double tx = red[3][0] * dV, ty = red[4][0] * dV, tz = red[5][0] * dV;
-    pw[PF_FXLTOT * pg.np + p] = red[0][0] * dV;
-    pw[PF_FYLTOT * pg.np + p] = red[1][0] * dV;
-    pw[PF_FZLTOT * pg.np + p] = red[2][0] * dV;
-    pw[PF_TQX * pg.np + p] = tx;
-    pw[PF_TQY * pg.np + p] = ty;
-    pw[PF_TQZ * pg.np + p] = tz;
-    const double phi = pw[PF_PHI * pg.np + p];
-    pw[PF_TQTHETA * pg.np + p] = (ty * cos(phi)) - (tx * sin(phi));
-  }
-}
-void launch_ibm_learned_apply(cudaStream_t s, const PartGeo &pg, IbmBuffers b, const float *Y, const float *tmu,
-                              const float *tsig, double dt, float *dF) {
-  if (pg.np == 0) return;
-  k_ibm_learned_apply<<<pg.np, 256, 0, s>>>(pg, b, Y, tmu, tsig, 1. / dt, dF);
-}
-
-// residual gate: sum of |U - u~|^2 over the points (block partials), then
-// gate = (rms > threshold); counts fallbacks
-__global__ void k_ibm_res_partial(PartGeo pg, IbmBuffers b, double *__restrict__ part) {
+// Residual gate: the rms of |U - u~| over all points from the per-(particle,
+// component) sums psum[p][c][0]; gate = (rms > fallback ratio x the plain
+// method's).  LearnState (device): [0] rms of the last learned substep,
+// [1] sum and [2] count of the plain passes' rms, [3] fallback ratio,
+// [4] fallbacks, [5] learned substeps; gate = 1 runs the plain passes after
+// the inference.
+__global__ void __launch_bounds__(256) k_ibm_res_gate(int n, const double *__restrict__ psum, long npts, double *ls,
+                                                      int *gate, int plain) {
   __shared__ double sm[256];
   double acc = 0.;
-  const int n = pg.np * pg.nl;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int p = t / pg.nl, l = t - p * pg.nl;
-    if (l >= b.nla[p]) continue;
-    const double ex = b.ul[t] - b.dudtl[t], ey = b.vl[t] - b.dvdtl[t], ez = b.wl[t] - b.dwdtl[t];
-    acc += ex * ex + ey * ey + ez * ez;
-  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) acc += psum[3 * (long)q];
   sm[threadIdx.x] = acc;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
     if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
-}
-// LearnState (device): [0] rms of the last learned substep, [1] sum and
-// [2] count of the plain passes' rms, [3] fallback ratio, [4] fallbacks,
-// [5] learned substeps; gate = 1 runs the plain passes after the inference
-__global__ void k_ibm_res_gate(int nb, const double *__restrict__ part, long npts, double *ls, int *gate, int plain) {
   if (threadIdx.x != 0) return;
-  double s = 0.;
-  for (int q = 0; q < nb; ++q) s += part[q];
-  const double rms = npts ? sqrt(s / (double)npts) : 0.;
+  const double rms = npts ? sqrt(sm[0] / (double)npts) : 0.;
   if (plain) {  // residual of the plain passes: the reference the learned one is held to
     ls[1] += rms;
     ls[2] += 1.;
@@ -378,13 +314,9 @@ __global__ void k_ibm_res_gate(int nb, const double *__restrict__ part, long npt
   *gate = g;
   if (g) ls[4] += 1.;
 }
-void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, double *scratch, long npts,
-                              double *ls, int *gate, int plain) {
-  const int nb = 152;
-  k_ibm_res_partial<<<nb, 256, 0, s>>>(pg, b, scratch);
-  k_ibm_res_gate<<<1, 32, 0, s>>>(nb, scratch, npts, ls, gate, plain);
+void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
+                              int plain) {
+  k_ibm_res_gate<<<1, 256, 0, s>>>(3 * pg.np, b.psum, npts, ls, gate, plain);
 }
-
-
 
 }  // namespace ibmk

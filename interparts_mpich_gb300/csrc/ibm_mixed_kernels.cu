@@ -193,6 +193,28 @@ __device__ __forceinline__ float interp27(const CompStencil &s, TAP tap) {
 // ---------------------------------------------------------------------------
 constexpr int INTERP_BOX = 8192;  // cells (32 KB)
 
+// sum of three per-thread values over the block (blockDim a multiple of 32,
+// at most 1024); the result in thread 0 (and in threads 1, 2 for b, c)
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &c) {
+  __shared__ double red3[32][3];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, d);
+    b += __shfl_down_sync(0xffffffffu, b, d);
+    c += __shfl_down_sync(0xffffffffu, c, d);
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { red3[w][0] = a; red3[w][1] = b; red3[w][2] = c; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double x = 0.;
+    for (int q = 0; q < nw; ++q) x += red3[q][threadIdx.x];
+    if (threadIdx.x == 0) a = x;
+    else if (threadIdx.x == 1) b = x;
+    else c = x;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
                                                            const float *__restrict__ fu, const float *__restrict__ fv,
                                                            const float *__restrict__ fw, double dti, int first,
@@ -233,7 +255,11 @@ __global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, Ib
       });
     }
     dud[t] = acc;
-    if (first < 0) continue;
+    if (first < 0) {  // residual only: sum of (U - u~)^2 of the component
+      const double e = U[t] - acc;
+      sF += e * e;
+      continue;
+    }
     const double f = first ? (U[t] - acc) * dti : Fl[t] + (U[t] - acc) * dti;
     Fl[t] = f;
     // lever arms of the torque terms of this component:
@@ -244,16 +270,11 @@ __global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, Ib
     sa += la * f;
     sb += lb * f;
   }
-  if (first < 0) return;
-  __shared__ double red[3][256];
-  red[0][threadIdx.x] = sF; red[1][threadIdx.x] = sa; red[2][threadIdx.x] = sb;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o)
-      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = red[threadIdx.x][0];
+  block_sum3(sF, sa, sb);
+  // psum[p][c]: force and lever-arm sums, or (first < 0) the residual sum in
+  // slot 0 for k_ibm_res_gate
+  if (threadIdx.x < (first < 0 ? 1 : 3))
+    b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = threadIdx.x == 0 ? sF : (threadIdx.x == 1 ? sa : sb);
 }
 // per-particle force and torque of updtlagrforces from the component sums
 __global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict__ gate) {
@@ -304,12 +325,15 @@ __device__ __forceinline__ void box_add(float *hi, float *lo, int c, float v) {
 
 __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
                                                       float *__restrict__ fv, float *__restrict__ fw, double dti,
-                                                      double coeff0, const float *__restrict__ dfin,
+                                                      double coeff0, LearnedForce lf,
                                                       const int *__restrict__ gate) {
   if (gate && *gate == 0) return;  // learned form: plain pass not needed
   const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
-  if (nla <= 0) return;
+  if (nla <= 0) {
+    if (lf.Y && threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = 0.;
+    return;
+  }
   const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
   float *F = c == 0 ? fu : (c == 1 ? fv : fw);
   extern __shared__ __align__(16) unsigned char spread_sm[];
@@ -326,11 +350,33 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
   }
   const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
   const double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
+  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
   const CompStencil *csp = b.cs + c * npl + t0;
+  double sF = 0., sa = 0., sb = 0.;
+  double px = 0., py = 0., pz = 0.;
+  float ysig = 0.f, ymu = 0.f;
+  if (lf.Y) {
+    px = b.pf[PF_X * pg.np + p]; py = b.pf[PF_Y * pg.np + p]; pz = b.pf[PF_Z * pg.np + p];
+    ysig = lf.tsig[c]; ymu = lf.tmu[c];
+  }
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const long t = t0 + l;
     const CompStencil s = load_cs(csp + l);
-    const float pre = dfin ? (float)(dfin[3 * t + c] * coeff0) : (float)((U[t] - dud[t]) * dti * coeff0);
+    float pre;
+    if (lf.Y) {
+      // total point force F0 + the network's correction, its sums
+      // (updtlagrforces), spread once
+      const double f = Fl[t] + (double)(lf.Y[3 * t + c] * ysig + ymu) * lf.dti;
+      Fl[t] = f;
+      const double la = c == 2 ? b.yfp[t] - py : b.zfp[t] - pz;
+      const double lb = c == 0 ? b.yfp[t] - py : b.xfp[t] - px;
+      sF += f;
+      sa += la * f;
+      sb += lb * f;
+      pre = (float)(f * coeff0);
+    } else {
+      pre = (float)((U[t] - dud[t]) * dti * coeff0);
+    }
     if (boxed) {
       const int o = box_off(s, bg, g.I, g.J);
 #pragma unroll
@@ -350,6 +396,11 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
           for (int i = 0; i < 3; ++i) atomicAdd(&F[fidx(g, wrapm(s.b[0] + i, g.I), y, s.b[2] + k)], a * s.w[i]);
         }
     }
+  }
+  if (lf.Y) {  // psum[p][c] for k_ibm_force_sums
+    block_sum3(sF, sa, sb);
+    if (threadIdx.x < 3)
+      b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = threadIdx.x == 0 ? sF : (threadIdx.x == 1 ? sa : sb);
   }
   if (!boxed) return;
   __syncthreads();
@@ -384,11 +435,15 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
   }
 }
 void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
-                         float *fw, double dt, const float *dfin, const int *gate) {
+                         float *fw, double dt, const LearnedForce &lf, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
   k_ibm_spread_f<<<dim3(pg.np, 3), 384, 2 * SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0,
-                                                                           dfin, gate);
+                                                                           lf, gate);
+}
+void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b) {
+  if (pg.np == 0) return;
+  k_ibm_force_sums<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, nullptr);
 }
 
 // ---------------------------------------------------------------------------

@@ -102,8 +102,15 @@ void launch_slip_residual(cudaStream_t s, const PartGeo &pg, IbmBuffers b, doubl
 void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b);
 int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                               const float *fv, const float *fw, double dt, int first, const int *gate = nullptr);
+// learned form: the network's output Y, its target de-standardisation
+// (mean, sigma) and 1/dt; Y == nullptr: the plain pass
+struct LearnedForce {
+  const float *Y, *tmu, *tsig;
+  double dti;
+};
 void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
-                         float *fw, double dt, const float *dfin = nullptr, const int *gate = nullptr);
+                         float *fw, double dt, const LearnedForce &lf = LearnedForce{}, const int *gate = nullptr);
+void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b);
 // feature row of a Lagrangian point: 32 per velocity component c at
 // [FEAT_PER_COMP*c + k]; k = FEAT_F0 holds the first-pass force F0_c*dt
 constexpr int FEAT_PER_COMP = 32, FEAT_F0 = 30;
@@ -121,10 +128,10 @@ void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, I
                               const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                               __nv_bfloat16 *X);
 void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs &H, double dt);
-void launch_ibm_learned_apply(cudaStream_t s, const PartGeo &pg, IbmBuffers b, const float *Y, const float *tmu,
-                              const float *tsig, double dt, float *dF);
-void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, double *scratch, long npts,
-                              double *ls, int *gate, int plain);
+// residual gate from the per-(particle, component) sums of (U - u~)^2 that
+// the interpolation with first < 0 leaves in psum[p][c][0]
+void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
+                              int plain);
 
 // mlp_kernels.cu (learned forcing model)
 struct MlpTrainBuffers {

@@ -258,6 +258,11 @@ class IBMSolver:
         return ({n: prof[q] for q, n in enumerate(_abi.STAT_NAMES)},
                 {n: float(scal[q]) for q, n in enumerate(_abi.STAT_SCALAR_NAMES)})
 
+    def set_projection_solves(self, solves: int):
+        """Mixed forms: 1 FP32 Poisson solve per projection (the default) or
+        2 (the solve plus a defect-correction solve)."""
+        self._chk(self.fn["set_projection_solves"](self.ctx, int(solves)))
+
     def set_stream(self, stream_handle: int | None):
         self._chk(self.fn["set_stream"](self.ctx, C.c_void_p(stream_handle or 0)))
 

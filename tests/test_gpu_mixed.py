@@ -1,9 +1,10 @@
 """The mixed-precision form (IBM_MODE_MIXED) against the FP64 oracle.
 
-FP32 velocity state, stencil, IBM interpolation/spreading and FFTs; FP64
-Thomas sweep, FP64 divergence residual driving one defect-correction solve,
-FP64 pressure accumulation, FP64 sphere integrals and Newton-Euler.
-Target: velocity relative L2 <= 1e-4 after 20 RK3 steps."""
+FP32 velocity state, stencil, IBM interpolation/spreading and FFTs;
+double-float Thomas sweep and pressure accumulation; one FP32 projection
+solve (default) or the solve plus a defect-correction solve driven by the
+double-float divergence residual; FP64 sphere integral totals and
+Newton-Euler.  Target: velocity relative L2 <= 1e-4 after 20 RK3 steps."""
 import numpy as np
 import pytest
 
@@ -16,9 +17,11 @@ pytestmark = pytest.mark.gpu
 MIXED_VEL_TOL_20 = 1e-4
 
 
-def test_mixed_20_steps(gpu_lib):
+@pytest.mark.parametrize("solves", [1, 2])
+def test_mixed_20_steps(gpu_lib, solves):
     case = small_case(n=48, nsp=10, radius_cells=5.0, seed=11, visc=1.0 / 1000.0)
     m = IBMSolver(case, mode=IBM_MODE_MIXED)
+    m.set_projection_solves(solves)
     o = OracleSolver(case)
     m.setup()
     o.setup()
@@ -36,12 +39,14 @@ def test_mixed_20_steps(gpu_lib):
     assert mx / (umax * case.dxi) < 1e-6, mx
 
 
-def test_mixed_defect_correction_divergence(gpu_lib):
-    """FP32 solve plus one defect-correction solve driven by the FP64
-    divergence residual: the divergence ends at the rounding level of the
-    FP32 velocity state."""
+@pytest.mark.parametrize("solves", [1, 2])
+def test_mixed_projection_divergence(gpu_lib, solves):
+    """One FP32 solve, or the solve plus one defect-correction solve driven
+    by the double-float divergence residual: the divergence ends at the
+    rounding level of the FP32 velocity state."""
     case = small_case(n=64, nsp=0)
     g = IBMSolver(case, mode=IBM_MODE_MIXED)
+    g.set_projection_solves(solves)
     f = case.initial_fields()
     rng = np.random.default_rng(5)
     for n in ("u", "v", "w"):
@@ -54,6 +59,7 @@ def test_mixed_defect_correction_divergence(gpu_lib):
     g.project(1, dt)
     tot, mx, _ = g.chkdiv()
     umax = max(np.abs(g.get_fields()[n]).max() for n in "uvw")
+    print(f"projection solves {solves}: max|div| / (|u|max/dx) = {mx / (umax * case.dxi):.2e}")
     assert mx / (umax * case.dxi) < 1e-6, (tot, mx)
 
 
