@@ -429,28 +429,79 @@ __host__ __device__ constexpr uint32_t kmaj_off(int row, int k, int K) {
   return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 constexpr int TC_M = 128;
-// the layer-2 A operand (H1, 128 x 128) reuses the X tile's space: X is dead
-// once layer 1 has completed, and the next X tile is loaded only after
-// layer 2 has completed; ~91 KB lets two CTAs share an SM
-constexpr int TC_XH = TC_M * NH * 2;  // bytes of the X / H1 region (H1 is the larger)
-constexpr size_t TC_SMEM = (size_t)(NH * NIN + NH * NH) * sizeof(bf16) + TC_XH +
-                           (size_t)(2 * NH + NOUT * NH + 4 + TC_M * 4) * sizeof(float) + 64;
+// One CTA per SM holds W1, W2 and the split layer-3 weights once; its four
+// warpgroups each run their own tile pipeline (X tile -> layer 1 -> GELU ->
+// layer 2 -> GELU -> layer 3) in a private 32 KB operand region and 128 TMEM
+// columns, so that one group's MMAs run while the others are in their
+// epilogues.  The TMEM columns are reused layer after layer (each epilogue
+// has read them completely before the next MMA is issued) and the operand
+// region likewise (X, then H1, then H2: each is dead once the MMA that reads
+// it has completed).  Layer 3 (3 outputs) runs on the tensor cores as well,
+// N = 16: B rows 0..2 hold bf16(W3) and rows 3..5 bf16(W3 - bf16(W3)), so
+// y = D[:, o] + D[:, 3 + o] carries W3 to about 16 significant bits with FP32
+// accumulation, like the FP32 layer 3 it replaces.
+constexpr int TC_GROUPS = 4, TC_THREADS = 128 * TC_GROUPS;
+constexpr int TC_REGION = TC_M * NH * 2;   // bytes of one group's X / H1 / H2 region
+constexpr int TC_W3ROWS = 16;
+constexpr size_t TC_SMEM = (size_t)(NH * NIN + NH * NH + TC_W3ROWS * NH) * sizeof(bf16) +
+                           (size_t)TC_GROUPS * TC_REGION + (size_t)(2 * NH + 4) * sizeof(float) + 128;
+// kind::f16, BF16 A and B (K-major), FP32 D, M = 128, N = 16
+constexpr uint32_t UMMA_IDESC_N16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+__device__ __forceinline__ void umma_bf16_n16(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(UMMA_IDESC_N16), "r"(acc));
+}
+// 8 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[q] = __uint_as_float(r[q]);
+}
+__device__ __forceinline__ void group_sync(int g) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(128) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+  const uint32_t d = smem_u32(dst);
+  const int n = valid ? 16 : 0;  // zero-fill rows beyond n
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
+}
+// GELU of 32 accumulator columns plus bias, rounded to BF16 into the next
+// layer's K-major A operand (row r, columns col0..col0+31)
+__device__ __forceinline__ void gelu_store32(const float v[32], const float *bias, int col0, unsigned char *A, int r) {
+#pragma unroll
+  for (int c8 = 0; c8 < 32; c8 += 8) {
+    uint32_t pk[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int col = col0 + c8 + 2 * e;
+      __nv_bfloat162 h2 = __floats2bfloat162_rn(gelu_hw(v[c8 + 2 * e] + bias[col]), gelu_hw(v[c8 + 2 * e + 1] + bias[col + 1]));
+      pk[e] = *reinterpret_cast<uint32_t *>(&h2);
+    }
+    *reinterpret_cast<uint4 *>(A + kmaj_off(r, col0 + c8, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+  }
+}
 
-__global__ void __launch_bounds__(256, 2) k_mlp_infer_tc(const bf16 *__restrict__ x, int n,
-                                                         const bf16 *__restrict__ w1b, const bf16 *__restrict__ w2b,
-                                                         const float *__restrict__ params, float *__restrict__ y,
-                                                         int *__restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char *W1c = sm;                            // [128 x 96]  K-major
-  unsigned char *W2c = W1c + NH * NIN * 2;            // [128 x 128]
-  unsigned char *Xc = W2c + NH * NH * 2;              // [128 x 96]
-  unsigned char *Hc = Xc;                             // [128 x 128], same space
-  float *cst = reinterpret_cast<float *>(Xc + TC_XH);  // b1, b2, W3, b3
-  float *ypart = cst + 2 * NH + NOUT * NH + 4;           // [128][4] layer-3 partials of the upper column half
-  uint64_t *bar = reinterpret_cast<uint64_t *>(ypart + TC_M * 4);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
-  int *bad = reinterpret_cast<int *>(tslot + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__restrict__ x, int n,
+                                                                const bf16 *__restrict__ w1b,
+                                                                const bf16 *__restrict__ w2b,
+                                                                const float *__restrict__ params,
+                                                                float *__restrict__ y, int *__restrict__ err) {
+  extern __shared__ __align__(16) unsigned char tc_sm[];
+  unsigned char *W1c = tc_sm;                                 // [128 x 96]  K-major
+  unsigned char *W2c = W1c + NH * NIN * 2;                    // [128 x 128]
+  unsigned char *W3c = W2c + NH * NH * 2;                     // [16 x 128]
+  unsigned char *R0 = W3c + TC_W3ROWS * NH * 2;               // group regions
+  float *cst = reinterpret_cast<float *>(R0 + TC_GROUPS * TC_REGION);  // b1, b2, b3
+  uint64_t *bars = reinterpret_cast<uint64_t *>(cst + 2 * NH + 4);     // one per group
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + TC_GROUPS);
+  int *gbad = reinterpret_cast<int *>(tslot + 1);  // per group: an MMA wait timed out
+  const int tid = threadIdx.x, warp = tid >> 5, g = warp >> 2, gt = tid & 127;
   // weights into the K-major layouts (16-byte chunks), constants
   for (int q = tid; q < NH * NIN / 8; q += blockDim.x) {
     const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
@@ -460,125 +511,136 @@ __global__ void __launch_bounds__(256, 2) k_mlp_infer_tc(const bf16 *__restrict_
     const int r = q / (NH / 8), c8 = (q % (NH / 8)) * 8;
     *reinterpret_cast<uint4 *>(W2c + kmaj_off(r, c8, NH)) = *reinterpret_cast<const uint4 *>(&w2b[r * NH + c8]);
   }
+  for (int q = tid; q < TC_W3ROWS * NH; q += blockDim.x) {  // split W3 (FP32) into hi and lo BF16 rows
+    const int r = q / NH, k = q % NH;
+    bf16 v = __float2bfloat16(0.f);
+    if (r < 2 * NOUT) {
+      const float w = params[OFF_W3 + (r % NOUT) * NH + k];
+      const bf16 hi = __float2bfloat16(w);
+      v = r < NOUT ? hi : __float2bfloat16(w - __bfloat162float(hi));
+    }
+    *reinterpret_cast<bf16 *>(W3c + kmaj_off(r, k, NH)) = v;
+  }
   for (int t = tid; t < NH; t += blockDim.x) { cst[t] = params[OFF_B1 + t]; cst[NH + t] = params[OFF_B2 + t]; }
-  for (int t = tid; t < NOUT * NH + NOUT; t += blockDim.x) cst[2 * NH + t] = params[OFF_W3 + t];
-  if (warp == 0) {  // 256 TMEM columns: layer-1 and layer-2 accumulators
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tslot)));
+  if (tid < NOUT) cst[2 * NH + tid] = params[OFF_B3 + tid];
+  if (warp == 0) {  // 512 TMEM columns: 128 per group
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    *bad = 0;
+  if (tid < TC_GROUPS) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[tid])));
+    gbad[tid] = 0;
   }
+  if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tbase = *tslot;
-  const uint32_t D1 = tbase, D2 = tbase + 128;
-  // 8 warps: warp w reads TMEM lanes 32*(w%4).. (rows), columns of half w/4
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  const int half = warp >> 2;
-  const float *b1 = cst, *b2 = cst + NH, *w3 = cst + 2 * NH, *b3 = w3 + NOUT * NH;
+  const uint32_t D = *tslot + (uint32_t)(g * 128);
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;  // warp w of the group reads lanes 32w..
+  unsigned char *A = R0 + g * TC_REGION;
+  uint64_t *bar = &bars[g];
+  const float *b1 = cst, *b2 = cst + NH, *b3 = cst + 2 * NH;
   const long LIMIT = 1L << 22;
   uint32_t phase = 0;
   const int ntiles = (n + TC_M - 1) / TC_M;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long row0 = (long)tile * TC_M;
-    for (int q = tid; q < TC_M * NIN / 8; q += blockDim.x) {
-      const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (row0 + r < n) v = __ldg(reinterpret_cast<const uint4 *>(&x[(row0 + r) * NIN + c8]));
-      *reinterpret_cast<uint4 *>(Xc + kmaj_off(r, c8, NIN)) = v;
+  const int r = gt;  // this thread's row of the tile (its TMEM lane)
+  const uint32_t aa = smem_u32(A);
+  // every thread of the group waits (bounded) for the group's MMAs; the
+  // group then decides together whether to go on
+  auto wait_mma = [&]() -> bool {
+    if (!mbar_wait(bar, phase, LIMIT)) {
+      if (err) atomicExch(err, 1);
+      gbad[g] = 1;
     }
+    phase ^= 1u;
+    tc_fence_after();
+    group_sync(g);
+    return gbad[g] == 0;
+  };
+  for (int tile = blockIdx.x * TC_GROUPS + g; tile < ntiles; tile += gridDim.x * TC_GROUPS) {
+    const long row0 = (long)tile * TC_M;
+    // X tile (zero rows beyond n) by asynchronous 16-byte copies
+    for (int q = gt; q < TC_M * NIN / 8; q += 128) {
+      const int rr = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+      const bool valid = row0 + rr < n;
+      cp_async16(A + kmaj_off(rr, c8, NIN), valid ? &x[(row0 + rr) * NIN + c8] : x, valid);
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
     fence_async_smem();
-    __syncthreads();
-    if (*bad) break;
-    if (tid == 0) {
+    group_sync(g);
+    if (gt == 0) {  // layer 1
       tc_fence_after();
-      const uint32_t xa = smem_u32(Xc), wa = smem_u32(W1c);
+      const uint32_t wa = smem_u32(W1c);
 #pragma unroll
       for (int kk = 0; kk < NIN / 16; ++kk)
-        umma_bf16(D1, umma_desc(xa + kk * 256, 128, (NIN / 8) * 128), umma_desc(wa + kk * 256, 128, (NIN / 8) * 128),
+        umma_bf16(D, umma_desc(aa + kk * 256, 128, (NIN / 8) * 128), umma_desc(wa + kk * 256, 128, (NIN / 8) * 128),
                   kk > 0);
       umma_commit(bar);
     }
-    if (!mbar_wait(bar, phase, LIMIT)) { if (err) atomicExch(err, 1); *bad = 1; }
-    phase ^= 1u;
-    tc_fence_after();
-    __syncthreads();
-    if (*bad) break;
-    // epilogue 1: row r, column half `half`: H1 = bf16(gelu(D1 + b1)) into
-    // layer 2's A layout
-    const int r = tid & 127;
+    if (!wait_mma()) break;
+    // epilogue 1: H1 = bf16(gelu(D + b1)) over X (dead once layer 1 completed)
 #pragma unroll 1
-    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
+    for (int cc = 0; cc < 4; ++cc) {
       float v[32];
-      tmem_ld32(D1 + lane_base + cc * 32, v);
-#pragma unroll
-      for (int c8 = 0; c8 < 32; c8 += 8) {
-        uint32_t pk[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int col = cc * 32 + c8 + 2 * e;
-          __nv_bfloat162 h2 = __floats2bfloat162_rn(gelu_hw(v[c8 + 2 * e] + b1[col]), gelu_hw(v[c8 + 2 * e + 1] + b1[col + 1]));
-          pk[e] = *reinterpret_cast<uint32_t *>(&h2);
-        }
-        *reinterpret_cast<uint4 *>(Hc + kmaj_off(r, cc * 32 + c8, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-      }
+      tmem_ld32(D + lane_base + cc * 32, v);
+      gelu_store32(v, b1, cc * 32, A, r);
     }
     tc_fence_before();
     fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
+    group_sync(g);
+    if (gt == 0) {  // layer 2 into the same columns (read completely above)
       tc_fence_after();
-      const uint32_t ha = smem_u32(Hc), wa = smem_u32(W2c);
+      const uint32_t wa = smem_u32(W2c);
 #pragma unroll
       for (int kk = 0; kk < NH / 16; ++kk)
-        umma_bf16(D2, umma_desc(ha + kk * 256, 128, (NH / 8) * 128), umma_desc(wa + kk * 256, 128, (NH / 8) * 128),
+        umma_bf16(D, umma_desc(aa + kk * 256, 128, (NH / 8) * 128), umma_desc(wa + kk * 256, 128, (NH / 8) * 128),
                   kk > 0);
       umma_commit(bar);
     }
-    if (!mbar_wait(bar, phase, LIMIT)) { if (err) atomicExch(err, 1); *bad = 1; }
-    phase ^= 1u;
-    tc_fence_after();
-    __syncthreads();
-    if (*bad) break;
-    // epilogue 2: H2 = bf16(gelu(D2 + b2)), y = H2 W3^T + b3 (FP32)
-    float acc[NOUT] = {0.f, 0.f, 0.f};
+    if (!wait_mma()) break;
+    // epilogue 2: H2 = bf16(gelu(D + b2)) over H1
 #pragma unroll 1
-    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
+    for (int cc = 0; cc < 4; ++cc) {
       float v[32];
-      tmem_ld32(D2 + lane_base + cc * 32, v);
-#pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int col = cc * 32 + q;
-        const float h = __bfloat162float(__float2bfloat16(gelu_hw(v[q] + b2[col])));
-#pragma unroll
-        for (int o = 0; o < NOUT; ++o) acc[o] += h * w3[o * NH + col];
-      }
+      tmem_ld32(D + lane_base + cc * 32, v);
+      gelu_store32(v, b2, cc * 32, A, r);
     }
-    if (half == 1)
-      for (int o = 0; o < NOUT; ++o) ypart[r * 4 + o] = acc[o];
     tc_fence_before();
-    __syncthreads();
-    if (half == 0 && row0 + r < n)
-      for (int o = 0; o < NOUT; ++o) y[(row0 + r) * NOUT + o] = (acc[o] + ypart[r * 4 + o]) + b3[o];
+    fence_async_smem();
+    group_sync(g);
+    if (gt == 0) {  // layer 3: N = 16 (W3 hi and lo rows)
+      tc_fence_after();
+      const uint32_t wa = smem_u32(W3c);
+#pragma unroll
+      for (int kk = 0; kk < NH / 16; ++kk)
+        umma_bf16_n16(D, umma_desc(aa + kk * 256, 128, (NH / 8) * 128),
+                      umma_desc(wa + kk * 256, 128, (NH / 8) * 128), kk > 0);
+      umma_commit(bar);
+    }
+    if (!wait_mma()) break;
+    float v[8];
+    tmem_ld8(D + lane_base, v);
+    if (row0 + r < n)
+      for (int o = 0; o < NOUT; ++o) y[(row0 + r) * NOUT + o] = (v[o] + v[NOUT + o]) + b3[o];
+    tc_fence_before();
+    group_sync(g);  // D and A are reused by the next tile
   }
   // a timed-out MMA may still be running: give it a bounded time to land
-  if (*bad && tid == 0) mbar_wait(bar, phase, LIMIT);
+  // (the parity that timed out; wait_mma has already flipped `phase`)
+  if (gbad[g] && gt == 0) mbar_wait(bar, phase ^ 1u, LIMIT);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tbase));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(*tslot));
 }
 int launch_mlp_infer_tc(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, const bf16 *w2b, const float *params,
                         float *y, int *err) {
   if (n <= 0) return 0;
   const int ntiles = (n + TC_M - 1) / TC_M;
-  const int grid = ntiles < 2 * 152 ? ntiles : 2 * 152;
-  k_mlp_infer_tc<<<grid, 256, TC_SMEM, s>>>(x, n, w1b, w2b, params, y, err);
+  const int nblk = (ntiles + TC_GROUPS - 1) / TC_GROUPS;
+  const int grid = nblk < 152 ? nblk : 152;
+  k_mlp_infer_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(x, n, w1b, w2b, params, y, err);
   return 1;
 }
 
