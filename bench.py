@@ -234,6 +234,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     import torch
 
     from interparts_mpich_gb300 import IBM_MODE_MIXED_LEARNED, IBMSolver
+    from interparts_mpich_gb300._abi import ParticleState
     from interparts_mpich_gb300.cases import channel_case
 
     case = channel_case(args.n, args.np, seed=1234)
@@ -309,9 +310,15 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
         cur = solver.get_fields()
         for k in "uvwp":
             pin[k][...] = cur[k]
-        ps = solver.get_particles(lagrangian=True)
-        h2d = 4 * pin["u"].nbytes
-        d2h = 4 * pin["u"].nbytes
+        tdt = {np.float64: torch.float64, np.int32: torch.int32}
+
+        def pinned(n, dt):
+            return torch.zeros(n, dtype=tdt[dt], pin_memory=True).numpy()
+
+        ps = ParticleState(case.np, solver.nq, solver.nl, lagrangian=True, alloc=pinned)
+        solver.get_particles(out=ps)
+        h2d = 4 * pin["u"].nbytes + ps.nbytes()
+        d2h = 4 * pin["u"].nbytes + ps.nbytes()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
@@ -319,7 +326,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
             solver.set_particles(ps)
             solver.rk3_step(dt)
             solver.get_fields(out=pin)
-            ps = solver.get_particles(lagrangian=True)
+            solver.get_particles(out=ps)
         torch.cuda.synchronize()
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
         e2e = {"value": round(max_over_ranks(e2e_ms, ws), 4), "unit": "ms/step",

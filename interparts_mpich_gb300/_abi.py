@@ -95,19 +95,24 @@ def iptr(a: np.ndarray | None):
 class ParticleState:
     """Host copy of the particle state (SoA numpy arrays) in the header's layout."""
 
-    def __init__(self, np_: int, nq: int, nl: int, lagrangian: bool = True):
+    def __init__(self, np_: int, nq: int, nl: int, lagrangian: bool = True, alloc=None):
+        """alloc(n, dtype) -> zeroed 1-D array (default numpy.zeros); a caller
+        that moves the state every step passes one returning page-locked
+        memory and reuses the object (get_particles(out=...))."""
+        z = alloc or (lambda n, dt: np.zeros(n, dt))
         self.np, self.nq, self.nl = np_, nq, nl
         for n in PARTICLE_SCALARS:
-            setattr(self, n, np.zeros(np_, np.float64))
-        self.qmax = np.zeros(np_, np.int32)
-        self.firstc = np.zeros(np_ * nq, np.int32)
+            setattr(self, n, z(np_, np.float64))
+        self.qmax = z(np_, np.int32)
+        self.firstc = z(np_ * nq, np.int32)
         for n in CONTACT_ARRAYS:
-            setattr(self, n, np.zeros(np_ * nq, np.float64))
-        self.nb = np.zeros(np_ * 9, np.int32)
-        self.mslv = np.arange(1, np_ + 1, dtype=np.int32)
-        self.rkp = np.zeros(np_ * 19, np.float64)
+            setattr(self, n, z(np_ * nq, np.float64))
+        self.nb = z(np_ * 9, np.int32)
+        self.mslv = z(np_, np.int32)
+        self.mslv[:] = np.arange(1, np_ + 1, dtype=np.int32)
+        self.rkp = z(np_ * 19, np.float64)
         for n in LAGRANGIAN_ARRAYS:
-            setattr(self, n, np.zeros(np_ * nl, np.float64) if lagrangian else None)
+            setattr(self, n, z(np_ * nl, np.float64) if lagrangian else None)
 
     def struct(self) -> IbmParticles:
         s = IbmParticles()
@@ -116,6 +121,10 @@ class ParticleState:
         for n in ("qmax", "firstc", "nb", "mslv"):
             setattr(s, n, iptr(getattr(self, n)))
         return s
+
+    def nbytes(self) -> int:
+        """Bytes of all arrays (what one set or get moves)."""
+        return int(sum(a.nbytes for a in vars(self).values() if isinstance(a, np.ndarray)))
 
     def copy(self) -> "ParticleState":
         o = ParticleState(self.np, self.nq, self.nl, lagrangian=self.xfp is not None)

@@ -122,8 +122,10 @@ class IBMSolver:
         s = ps.struct()
         self._chk(self.fn["set_particles"](self.ctx, C.byref(s)))
 
-    def get_particles(self, lagrangian: bool = True) -> ParticleState:
-        ps = ParticleState(self.case.np, self.nq, self.nl, lagrangian=lagrangian)
+    def get_particles(self, lagrangian: bool = True, out: ParticleState | None = None) -> ParticleState:
+        """The particle state; `out` (e.g. page-locked, reused every step)
+        receives it instead of a new object."""
+        ps = out if out is not None else ParticleState(self.case.np, self.nq, self.nl, lagrangian=lagrangian)
         s = ps.struct()
         self._chk(self.fn["get_particles"](self.ctx, C.byref(s)))
         return ps
