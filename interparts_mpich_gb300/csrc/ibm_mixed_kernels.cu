@@ -38,11 +38,14 @@ __global__ void __launch_bounds__(256) k_ibm_stencil_c(Geo g, PartGeo pg, IbmBuf
     const int p = t / pg.nl, l = t - p * pg.nl;
     if (l >= b.nla[p]) continue;
     const double xfp = b.xfp[t], yfp = b.yfp[t], zfp = b.zfp[t];
-    // periodic image by a multiply: any image whose coordinate stays in
-    // [0, I+1] addresses the same (wrapped) cells with the same weights
-    const double inv_lx = 1. / g.lx, inv_ly = 1. / g.ly;
-    double coorxfp = xfp * g.dxi - (double)((long)floor((xfp - 0.5 * g.dx) * inv_lx) * g.I);
-    double cooryfp = yfp * g.dyi - (double)((long)floor((yfp - 0.5 * g.dy) * inv_ly) * g.J);
+    // periodic image: a point within half a cell of the domain (the only
+    // case that occurs) is shifted by -1, 0 or +1 periods; any image whose
+    // coordinate stays in [0, I+1] addresses the same (wrapped) cells with
+    // the same weights, so the comparison need not agree with a rounded
+    // division at the boundary itself
+    const double sx = xfp - 0.5 * g.dx, sy = yfp - 0.5 * g.dy;
+    double coorxfp = xfp * g.dxi - (sx < 0. ? -(double)g.I : (sx >= g.lx ? (double)g.I : 0.));
+    double cooryfp = yfp * g.dyi - (sy < 0. ? -(double)g.J : (sy >= g.ly ? (double)g.J : 0.));
     double coorzfp = zfp * g.dzi;
     if (!(coorxfp >= 0. && coorxfp <= g.I + 1.) || !(cooryfp >= 0. && cooryfp <= g.J + 1.) ||
         !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
@@ -308,20 +311,13 @@ int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, I
 // lagr2eulr spreading of dF = (U_l - u~_l)/dt (or a given increment) with
 // the terms of interp_spread.f90:329-355, F*coeff0*phix*phiy*phiz.  Block
 // (particle, component): contributions accumulate in the particle's box in
-// shared memory, compensated: the rounding error of every shared atomic add
-// is recovered exactly by TwoSum from the value the atomic returned and
-// accumulated in a second box; each touched cell is flushed to HBM with one
-// atomic add of hi+lo.  Boxes beyond SPREAD_BOX cells add per tap instead.
+// shared memory with fire-and-forget FP32 reductions; each touched cell is
+// flushed to HBM with one atomic add.  (A compensated box, TwoSum of every
+// shared add into a second box, changed the 20-step mixed-form error by
+// less than 1 % while costing 20 % of the kernel; the field it is added to
+// is FP32.)  Boxes beyond SPREAD_BOX cells add per tap instead.
 // ---------------------------------------------------------------------------
 constexpr int SPREAD_BOX = 8192;
-
-__device__ __forceinline__ void box_add(float *hi, float *lo, int c, float v) {
-  const float old = atomicAdd(&hi[c], v);
-  const float s = __fadd_rn(old, v);
-  const float bb = __fsub_rn(s, old);
-  const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-  if (e != 0.f) atomicAdd(&lo[c], e);
-}
 
 __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
                                                       float *__restrict__ fv, float *__restrict__ fw, double dti,
@@ -337,15 +333,14 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
   const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
   float *F = c == 0 ? fu : (c == 1 ? fv : fw);
   extern __shared__ __align__(16) unsigned char spread_sm[];
-  float *hi = reinterpret_cast<float *>(spread_sm);
-  float *lo = hi + SPREAD_BOX;
+  float *box = reinterpret_cast<float *>(spread_sm);
   __shared__ int bg[8];
   if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
   __syncthreads();
   const bool boxed = box_ok(bg, SPREAD_BOX, g.I, g.J);
   const int nbx = bg[5], nby = bg[6], nbox = nbx * nby * bg[7];
   if (boxed) {
-    for (int q = threadIdx.x; q < nbox; q += blockDim.x) { hi[q] = 0.f; lo[q] = 0.f; }
+    for (int q = threadIdx.x; q < nbox; q += blockDim.x) box[q] = 0.f;
     __syncthreads();
   }
   const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
@@ -386,7 +381,7 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
           const float a = pre * s.w[3 + j] * s.w[6 + k];  // the (j,k) factor, then the x weight
           const int row = o + (k * nby + j) * nbx;
 #pragma unroll
-          for (int i = 0; i < 3; ++i) box_add(hi, lo, row + i, a * s.w[i]);
+          for (int i = 0; i < 3; ++i) atomicAdd(&box[row + i], a * s.w[i]);
         }
     } else {
       for (int k = 0; k < 3; ++k)
@@ -418,7 +413,7 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
 #pragma unroll
       for (int d = 0; d < 4; ++d) {
         const int cx = gx + d - x0;
-        v[d] = (cx >= 0 && cx < nbx) ? hi[row * nbx + cx] + lo[row * nbx + cx] : 0.f;
+        v[d] = (cx >= 0 && cx < nbx) ? box[row * nbx + cx] : 0.f;
       }
       if (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f && v[3] == 0.f) continue;
       float4 *dst = reinterpret_cast<float4 *>(&F[fidx(g, wrapm(gx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
@@ -427,7 +422,7 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
     return;
   }
   for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
-    const float v = hi[q] + lo[q];
+    const float v = box[q];
     if (v != 0.f) {
       const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
       atomicAdd(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)], v);
@@ -438,8 +433,8 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
                          float *fw, double dt, const LearnedForce &lf, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_f<<<dim3(pg.np, 3), 384, 2 * SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0,
-                                                                           lf, gate);
+  k_ibm_spread_f<<<dim3(pg.np, 3), 384, SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0,
+                                                                       lf, gate);
 }
 void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b) {
   if (pg.np == 0) return;
@@ -665,7 +660,7 @@ void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, I
 
 int ibm_set_smem_limits() {
   cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        2 * SPREAD_BOX * (int)sizeof(float));
+                                        SPREAD_BOX * (int)sizeof(float));
   cudaError_t e2 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         INTERP_BOX * (int)sizeof(float));
   cudaError_t e3 = cudaFuncSetAttribute(k_ibm_features_comp, cudaFuncAttributeMaxDynamicSharedMemorySize,
