@@ -1463,7 +1463,7 @@ int ibm_slip_residual(ibm_ctx *c, double *maxres, double *rmsres) {
   if (c->pg.np == 0) { if (maxres) *maxres = 0; if (rmsres) *rmsres = 0; return IBM_OK; }
   // re-interpolate the forced field (valid between ibm_forcing_loop and ibm_project)
   if (c->mixed) c->launches += -1 + launch_ibm_interp_force_f(c->stream, c->g, c->pg, c->ib, c->fu32, c->fv32, c->fw32,
-                                                             1., -1);
+                                                             1., -2);
   else launch_ibm_interp_force<double>(c->stream, c->g, c->pg, c->ib, c->fu, c->fv, c->fw, 1., -1);
   LAUNCHED(1);
   launch_slip_residual(c->stream, c->pg, c->ib, c->dout + 16);

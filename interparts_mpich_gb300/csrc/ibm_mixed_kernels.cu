@@ -10,9 +10,8 @@
 // it and flushes each touched cell to HBM once.
 //
 // Origins come from the FP64 point coordinates exactly as the FP64 form
-// computes them; delta weights, interpolation sums and spreading are FP32,
-// spreading compensated (TwoSum of every shared-memory add); point forces
-// F_l and the per-particle force/torque sums stay FP64.
+// computes them; delta weights, interpolation sums and spreading are FP32;
+// point forces F_l and the per-particle force/torque sums stay FP64.
 #include <cuda_bf16.h>
 
 #include "kernels.cuh"
@@ -32,6 +31,15 @@ __device__ __forceinline__ int relwrap(int d, int n) {
 // with the stencil origins and delta arguments of eulr2lagr
 // (interp_spread.f90:60-131): x, y indices unwrapped (periodic wrap at use).
 // ---------------------------------------------------------------------------
+// one 48-byte record as three 16-byte stores (the layout load_cs reads)
+__device__ __forceinline__ void store_cs(CompStencil *dst, int b0, int b1, int b2, const float *wx, const float *wy,
+                                         const float *wz) {
+  float4 *q = reinterpret_cast<float4 *>(dst);
+  q[0] = make_float4(__int_as_float(b0), __int_as_float(b1), __int_as_float(b2), wx[0]);
+  q[1] = make_float4(wx[1], wx[2], wy[0], wy[1]);
+  q[2] = make_float4(wy[2], wz[0], wz[1], wz[2]);
+}
+
 __global__ void __launch_bounds__(256) k_ibm_stencil_c(Geo g, PartGeo pg, IbmBuffers b) {
   const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -69,16 +77,9 @@ __global__ void __launch_bounds__(256) k_ibm_stencil_c(Geo g, PartGeo pg, IbmBuf
       phizh[m] = delta3f(((float)m - 0.5f) - hz);
     }
     const long npl = (long)n;
-    CompStencil s;
-    s.b[0] = ilows - 1; s.b[1] = jlow - 1; s.b[2] = klow;
-    for (int m = 0; m < 3; ++m) { s.w[m] = phix[m]; s.w[3 + m] = phiyh[m]; s.w[6 + m] = phizh[m]; }
-    b.cs[t] = s;
-    s.b[0] = ilow - 1; s.b[1] = jlows - 1; s.b[2] = klow;
-    for (int m = 0; m < 3; ++m) { s.w[m] = phixh[m]; s.w[3 + m] = phiy[m]; s.w[6 + m] = phizh[m]; }
-    b.cs[npl + t] = s;
-    s.b[0] = ilow - 1; s.b[1] = jlow - 1; s.b[2] = klows;
-    for (int m = 0; m < 3; ++m) { s.w[m] = phixh[m]; s.w[3 + m] = phiyh[m]; s.w[6 + m] = phiz[m]; }
-    b.cs[2 * npl + t] = s;
+    store_cs(b.cs + t, ilows - 1, jlow - 1, klow, phix, phiyh, phizh);
+    store_cs(b.cs + npl + t, ilow - 1, jlows - 1, klow, phixh, phiy, phizh);
+    store_cs(b.cs + 2 * npl + t, ilow - 1, jlow - 1, klows, phixh, phiyh, phiz);
   }
 }
 
@@ -192,33 +193,50 @@ __device__ __forceinline__ float interp27(const CompStencil &s, TAP tap) {
 // Interpolated component to dudtl/dvdtl/dwdtl; with first >= 0 the FP64
 // point-force update of the component and its partial sums (sum F_c and the
 // two lever-arm moments of F_c in the torque) to psum; k_ibm_force_sums
-// combines the components.  first < 0: interpolation only.
+// combines the components.  first == -1: the residual sum of (U - u~)^2 only
+// (FP32: it feeds the learned loop's gate), dudtl left as it was; first ==
+// -2: the interpolation to dudtl only (the slip-residual diagnostic).
 // ---------------------------------------------------------------------------
 constexpr int INTERP_BOX = 8192;  // cells (32 KB)
+constexpr int INTERP_THREADS = 256;
 
-// sum of three per-thread values over the block (blockDim a multiple of 32,
-// at most 1024); the result in thread 0 (and in threads 1, 2 for b, c)
-__device__ __forceinline__ void block_sum3(double &a, double &b, double &c) {
-  __shared__ double red3[32][3];
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, d);
-    b += __shfl_down_sync(0xffffffffu, b, d);
-    c += __shfl_down_sync(0xffffffffu, c, d);
-  }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (lane == 0) { red3[w][0] = a; red3[w][1] = b; red3[w][2] = c; }
+// Sums of three per-thread FP64 values over a block of NT threads (NT a
+// multiple of 32, at least 96) through the [3][NT] shared buffer st: each of
+// three warps sums one value (NT/32 per lane, then across the lanes), so the
+// block spends 3 (NT/32 + 5) FP64 warp instructions instead of a shuffle tree
+// in every warp (FP64 issues at 1/64 of the FP32 rate).  The sums land in
+// res[0..2]; st and res are valid for every thread after the call.
+template <int NT>
+__device__ __forceinline__ void block_sum3(double a, double b, double c, double *st, double *res) {
+  st[threadIdx.x] = a;
+  st[NT + threadIdx.x] = b;
+  st[2 * NT + threadIdx.x] = c;
   __syncthreads();
-  if (threadIdx.x < 3) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w < 3) {
     double x = 0.;
-    for (int q = 0; q < nw; ++q) x += red3[q][threadIdx.x];
-    if (threadIdx.x == 0) a = x;
-    else if (threadIdx.x == 1) b = x;
-    else c = x;
+#pragma unroll
+    for (int q = lane; q < NT; q += 32) x += st[w * NT + q];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
+    if (lane == 0) res[w] = x;
   }
+  __syncthreads();
+}
+// FP32 sum over the block (blockDim a multiple of 32, at most 1024), to every thread
+__device__ __forceinline__ float block_sum_all(float a) {
+  __shared__ float part[32];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) a += __shfl_xor_sync(0xffffffffu, a, d);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) part[w] = a;
+  __syncthreads();
+  float t = 0.f;
+  for (int q = 0; q < nw; ++q) t += part[q];
+  return t;
 }
 
-__global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
+__global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
                                                            const float *__restrict__ fu, const float *__restrict__ fv,
                                                            const float *__restrict__ fw, double dti, int first,
                                                            const int *__restrict__ gate) {
@@ -245,6 +263,7 @@ __global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, Ib
   const CompStencil *csp = b.cs + c * npl + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
   double sF = 0., sa = 0., sb = 0.;
+  float r2 = 0.f;
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const long t = t0 + l;
     const CompStencil s = load_cs(csp + l);
@@ -257,12 +276,13 @@ __global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, Ib
         return __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
       });
     }
-    dud[t] = acc;
-    if (first < 0) {  // residual only: sum of (U - u~)^2 of the component
-      const double e = U[t] - acc;
-      sF += e * e;
+    if (first == -1) {  // residual only: sum of (U - u~)^2 of the component
+      const float e = (float)U[t] - acc;
+      r2 = fmaf(e, e, r2);
       continue;
     }
+    dud[t] = acc;
+    if (first < 0) continue;
     const double f = first ? (U[t] - acc) * dti : Fl[t] + (U[t] - acc) * dti;
     Fl[t] = f;
     // lever arms of the torque terms of this component:
@@ -273,11 +293,19 @@ __global__ void __launch_bounds__(256) k_ibm_interp_comp_f(Geo g, PartGeo pg, Ib
     sa += la * f;
     sb += lb * f;
   }
-  block_sum3(sF, sa, sb);
   // psum[p][c]: force and lever-arm sums, or (first < 0) the residual sum in
   // slot 0 for k_ibm_res_gate
-  if (threadIdx.x < (first < 0 ? 1 : 3))
-    b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = threadIdx.x == 0 ? sF : (threadIdx.x == 1 ? sa : sb);
+  if (first == -1) {
+    const float tot = block_sum_all(r2);
+    if (threadIdx.x == 0) b.psum[((long)p * 3 + c) * 3] = tot;
+    return;
+  }
+  if (first < 0) return;
+  __syncthreads();  // the box is dead: its first words hold the partial sums
+  double *st = reinterpret_cast<double *>(ibox_sm);
+  __shared__ double res[3];
+  block_sum3<INTERP_THREADS>(sF, sa, sb, st, res);
+  if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
 }
 // per-particle force and torque of updtlagrforces from the component sums
 __global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict__ gate) {
@@ -300,8 +328,8 @@ __global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict
 int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                               const float *fv, const float *fw, double dt, int first, const int *gate) {
   if (pg.np == 0) return 0;
-  k_ibm_interp_comp_f<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, first,
-                                                                              gate);
+  k_ibm_interp_comp_f<<<dim3(pg.np, 3), INTERP_THREADS, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw,
+                                                                                         1. / dt, first, gate);
   if (first < 0) return 1;
   k_ibm_force_sums<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, gate);
   return 2;
@@ -311,15 +339,42 @@ int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, I
 // lagr2eulr spreading of dF = (U_l - u~_l)/dt (or a given increment) with
 // the terms of interp_spread.f90:329-355, F*coeff0*phix*phiy*phiz.  Block
 // (particle, component): contributions accumulate in the particle's box in
-// shared memory with fire-and-forget FP32 reductions; each touched cell is
-// flushed to HBM with one atomic add.  (A compensated box, TwoSum of every
-// shared add into a second box, changed the 20-step mixed-form error by
-// less than 1 % while costing 20 % of the kernel; the field it is added to
-// is FP32.)  Boxes beyond SPREAD_BOX cells add per tap instead.
+// shared memory, and each touched cell is flushed to HBM with one atomic add.
+// The box holds 32-bit fixed-point sums: a first pass computes every point's
+// prefactor F*coeff0 into shared memory and their absolute sum B, which
+// bounds every cell's sum (the 27 delta weights of a point are non-negative
+// and sum to one); with the scale 2^s, B * 2^s < 2^30, each tap adds
+// rint(2^s * prefactor * weight) with a native integer shared-memory add
+// (no compare-and-swap loop, no wait on its result), and the sums are exact
+// and independent of the order of the adds.  The resolution is B / 2^30 per
+// tap, below the FP32 rounding of the sums it replaces.  Particles with
+// more than SPREAD_PRE points, or a bound that is zero or not finite, add
+// FP32 values into the box instead; boxes beyond SPREAD_BOX cells add per
+// tap to the field.
 // ---------------------------------------------------------------------------
 constexpr int SPREAD_BOX = 8192;
+constexpr int SPREAD_PRE = 2048;
+constexpr int SPREAD_THREADS = 384;
 
-__global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
+// the 27 taps of one point into the box: FP32 adds, or fixed-point adds of
+// rint(pre * w) (pre already scaled)
+template <bool FIXED>
+__device__ __forceinline__ void spread27_box(float *box, const CompStencil &s, int o, int nbx, int nby, float pre) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float a = pre * s.w[3 + j] * s.w[6 + k];  // the (j,k) factor, then the x weight
+      const int row = o + (k * nby + j) * nbx;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        if constexpr (FIXED) atomicAdd(reinterpret_cast<int *>(box) + row + i, __float2int_rn(a * s.w[i]));
+        else atomicAdd(&box[row + i], a * s.w[i]);
+      }
+    }
+}
+
+__global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
                                                       float *__restrict__ fv, float *__restrict__ fw, double dti,
                                                       double coeff0, LearnedForce lf,
                                                       const int *__restrict__ gate) {
@@ -334,10 +389,13 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
   float *F = c == 0 ? fu : (c == 1 ? fv : fw);
   extern __shared__ __align__(16) unsigned char spread_sm[];
   float *box = reinterpret_cast<float *>(spread_sm);
+  int *ibox = reinterpret_cast<int *>(spread_sm);
   __shared__ int bg[8];
+  __shared__ float spre[SPREAD_PRE];  // prefactors of the staged points
   if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
   __syncthreads();
   const bool boxed = box_ok(bg, SPREAD_BOX, g.I, g.J);
+  const bool staged = boxed && nla <= SPREAD_PRE;
   const int nbx = bg[5], nby = bg[6], nbox = nbx * nby * bg[7];
   if (boxed) {
     for (int q = threadIdx.x; q < nbox; q += blockDim.x) box[q] = 0.f;
@@ -354,9 +412,16 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
     px = b.pf[PF_X * pg.np + p]; py = b.pf[PF_Y * pg.np + p]; pz = b.pf[PF_Z * pg.np + p];
     ysig = lf.tsig[c]; ymu = lf.tmu[c];
   }
-  for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+  // prefactors F coeff0 (F given) or (U - u~) dti coeff0, as FP32 products
+  const float pcoef = (float)coeff0, ucoef = (float)(dti * coeff0);
+  // points in transposed order: the 32 lanes of a warp take points nq apart
+  // in the particle's list (neighbouring points have overlapping stencils)
+  const int nq = (nla + 31) >> 5;
+  float asum = 0.f;
+  for (int m = threadIdx.x; m < 32 * nq; m += blockDim.x) {
+    const int l = (m & 31) * nq + (m >> 5);
+    if (l >= nla) continue;
     const long t = t0 + l;
-    const CompStencil s = load_cs(csp + l);
     float pre;
     if (lf.Y) {
       // total point force F0 + the network's correction, its sums
@@ -368,21 +433,18 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
       sF += f;
       sa += la * f;
       sb += lb * f;
-      pre = (float)(f * coeff0);
+      pre = (float)f * pcoef;
     } else {
-      pre = (float)((U[t] - dud[t]) * dti * coeff0);
+      pre = (float)(U[t] - dud[t]) * ucoef;
     }
+    if (staged) {
+      spre[l] = pre;
+      asum += fabsf(pre);
+      continue;
+    }
+    const CompStencil s = load_cs(csp + l);
     if (boxed) {
-      const int o = box_off(s, bg, g.I, g.J);
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const float a = pre * s.w[3 + j] * s.w[6 + k];  // the (j,k) factor, then the x weight
-          const int row = o + (k * nby + j) * nbx;
-#pragma unroll
-          for (int i = 0; i < 3; ++i) atomicAdd(&box[row + i], a * s.w[i]);
-        }
+      spread27_box<false>(box, s, box_off(s, bg, g.I, g.J), nbx, nby, pre);
     } else {
       for (int k = 0; k < 3; ++k)
         for (int j = 0; j < 3; ++j) {
@@ -393,27 +455,48 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
     }
   }
   if (lf.Y) {  // psum[p][c] for k_ibm_force_sums
-    block_sum3(sF, sa, sb);
-    if (threadIdx.x < 3)
-      b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = threadIdx.x == 0 ? sF : (threadIdx.x == 1 ? sa : sb);
+    __shared__ double sred[3 * SPREAD_THREADS], res[3];
+    block_sum3<SPREAD_THREADS>(sF, sa, sb, sred, res);
+    if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
   }
   if (!boxed) return;
+  // fixed point: scale 2^(29 - e) with bound < 2^e, so that bound * scale < 2^30
+  float scale = 0.f;
+  if (staged) {
+    const float bound = block_sum_all(asum);  // also orders spre before its reads
+    int e = 0;
+    if (bound > 0.f && bound <= 3.0e38f) {
+      frexpf(bound, &e);
+      scale = ldexpf(1.f, min(29 - e, 126));
+    }
+    for (int m = threadIdx.x; m < 32 * nq; m += blockDim.x) {
+      const int l = (m & 31) * nq + (m >> 5);
+      if (l >= nla) continue;
+      const CompStencil s = load_cs(csp + l);
+      const int o = box_off(s, bg, g.I, g.J);
+      if (scale > 0.f) spread27_box<true>(box, s, o, nbx, nby, spre[l] * scale);
+      else spread27_box<false>(box, s, o, nbx, nby, spre[l]);
+    }
+  }
   __syncthreads();
+  const bool fixed = scale > 0.f;
+  const float iscale = fixed ? 1.f / scale : 0.f;  // a power of two: exact
+  auto cell = [&](int q) { return fixed ? (float)ibox[q] * iscale : box[q]; };
   const int nxy = nbx * nby, x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
   if ((g.I & 3) == 0) {
     // flush by 16-byte quads of x-cells (rows padded with zeros to the
     // aligned quads that cover them; with I a multiple of 4 a quad never
     // straddles the periodic wrap): one vector atomic per nonzero quad
     const int a0 = x0 - (((x0 % 4) + 4) % 4);
-    const int nq = (x0 + nbx - a0 + 3) >> 2, nrow = nby * bg[7];
-    for (int e = threadIdx.x; e < nrow * nq; e += blockDim.x) {
-      const int row = e / nq, t = e - row * nq;
+    const int nqd = (x0 + nbx - a0 + 3) >> 2, nrow = nby * bg[7];
+    for (int e = threadIdx.x; e < nrow * nqd; e += blockDim.x) {
+      const int row = e / nqd, t = e - row * nqd;
       const int cz = row / nby, cy = row - cz * nby, gx = a0 + 4 * t;
       float v[4];
 #pragma unroll
       for (int d = 0; d < 4; ++d) {
         const int cx = gx + d - x0;
-        v[d] = (cx >= 0 && cx < nbx) ? box[row * nbx + cx] : 0.f;
+        v[d] = (cx >= 0 && cx < nbx) ? cell(row * nbx + cx) : 0.f;
       }
       if (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f && v[3] == 0.f) continue;
       float4 *dst = reinterpret_cast<float4 *>(&F[fidx(g, wrapm(gx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
@@ -422,7 +505,7 @@ __global__ void __launch_bounds__(384) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuff
     return;
   }
   for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
-    const float v = box[q];
+    const float v = cell(q);
     if (v != 0.f) {
       const int cz = q / nxy, r = q - cz * nxy, cy = r / nbx, cx = r - cy * nbx;
       atomicAdd(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)], v);
@@ -433,8 +516,8 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
                          float *fw, double dt, const LearnedForce &lf, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_f<<<dim3(pg.np, 3), 384, SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0,
-                                                                       lf, gate);
+  k_ibm_spread_f<<<dim3(pg.np, 3), SPREAD_THREADS, SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt,
+                                                                                  coeff0, lf, gate);
 }
 void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b) {
   if (pg.np == 0) return;
@@ -560,7 +643,7 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
       snk.put(Uc - acc);
       snk.put(Uc);
       snk.put(nrm[c]);
-      snk.put((float)(Fl3[c][t] * dt));
+      snk.put((float)Fl3[c][t] * (float)dt);
       snk.put(s.w[3 * c + 1]);
     }
   }
@@ -638,7 +721,7 @@ __global__ void __launch_bounds__(256) k_ibm_features_comp(Geo g, PartGeo pg, Ib
     f[27] = Uc - acc;
     f[28] = Uc;
     f[29] = (float)(xc[t] - pc) * inv_r;
-    f[30] = (float)(F0 * dt);
+    f[30] = (float)F0 * (float)dt;
     f[31] = s.w[3 * c + 1];
 #pragma unroll
     for (int q = 0; q < 32; q += 8) {

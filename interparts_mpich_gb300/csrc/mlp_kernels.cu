@@ -15,6 +15,7 @@
 // Parameter vector (FP32): W1[128][96], b1[128], W2[128][128], b2[128],
 // W3[3][128], b3[3].
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "kernels.cuh"
 
@@ -436,22 +437,27 @@ constexpr int TC_M = 128;
 // epilogues.  The TMEM columns are reused layer after layer (each epilogue
 // has read them completely before the next MMA is issued) and the operand
 // region likewise (X, then H1, then H2: each is dead once the MMA that reads
-// it has completed).  Layer 3 (3 outputs) runs on the tensor cores as well,
-// N = 16: B rows 0..2 hold bf16(W3) and rows 3..5 bf16(W3 - bf16(W3)), so
-// y = D[:, o] + D[:, 3 + o] carries W3 to about 16 significant bits with FP32
+// it has completed).  Layer 1 multiplies the BF16 features by BF16 W1; the
+// GELU epilogues run in packed half precision and store 2 gelu(z) as F16, so
+// layers 2 and 3 are F16 x F16 products with W2 / 2 and W3 / 2 (exact
+// halvings).  Layer 3 (3 outputs) runs on the tensor cores as well, N = 16:
+// B rows 0..2 hold f16(W3/2) and rows 3..5 the F16 remainder, so
+// y = D[:, o] + D[:, 3 + o] carries W3 to about 22 significant bits with FP32
 // accumulation, like the FP32 layer 3 it replaces.
 constexpr int TC_GROUPS = 4, TC_THREADS = 128 * TC_GROUPS;
 constexpr int TC_REGION = TC_M * NH * 2;   // bytes of one group's X / H1 / H2 region
 constexpr int TC_W3ROWS = 16;
 constexpr size_t TC_SMEM = (size_t)(NH * NIN + NH * NH + TC_W3ROWS * NH) * sizeof(bf16) +
                            (size_t)TC_GROUPS * TC_REGION + (size_t)(2 * NH + 4) * sizeof(float) + 128;
-// kind::f16, BF16 A and B (K-major), FP32 D, M = 128, N = 16
-constexpr uint32_t UMMA_IDESC_N16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
-__device__ __forceinline__ void umma_bf16_n16(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+// kind::f16 with F16 A and B (K-major), FP32 D, M = 128: N = 128 (layer 2)
+// and N = 16 (layer 3)
+constexpr uint32_t UMMA_IDESC_H = (1u << 4) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t UMMA_IDESC_H_N16 = (1u << 4) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+__device__ __forceinline__ void umma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-      "l"(a), "l"(b), "r"(UMMA_IDESC_N16), "r"(acc));
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 // 8 consecutive FP32 columns of this thread's TMEM lane
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
@@ -471,17 +477,31 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool vali
   const int n = valid ? 16 : 0;  // zero-fill rows beyond n
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
 }
-// GELU of 32 accumulator columns plus bias, rounded to BF16 into the next
-// layer's K-major A operand (row r, columns col0..col0+31)
-__device__ __forceinline__ void gelu_store32(const float v[32], const float *bias, int col0, unsigned char *A, int r) {
+__device__ __forceinline__ uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t *>(&h); }
+__device__ __forceinline__ __half2 bits_h2(uint32_t u) { return *reinterpret_cast<__half2 *>(&u); }
+__device__ __forceinline__ __half2 tanh_h2(__half2 x) {
+  uint32_t y;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(y) : "r"(h2_bits(x)));
+  return bits_h2(y);
+}
+// Twice the GELU of 32 accumulator columns plus bias, x (1 + tanh(c x (1 +
+// a x^2))) with x = z + b, in packed half precision (two columns per
+// instruction), into the next layer's K-major F16 A operand (row r, columns
+// col0..col0+31).  The factor 1/2 is carried by the next layer's weights.
+// bias2: the layer's biases as F16 pairs.
+__device__ __forceinline__ void gelu2_store32(const float v[32], const uint32_t *bias2, int col0, unsigned char *A,
+                                              int r) {
+  const __half2 c0 = __float2half2_rn(0.7978845608028654f), c1 = __float2half2_rn(0.7978845608028654f * 0.044715f);
 #pragma unroll
   for (int c8 = 0; c8 < 32; c8 += 8) {
+    const uint4 bq = *reinterpret_cast<const uint4 *>(bias2 + (col0 + c8) / 2);
+    const uint32_t bb[4] = {bq.x, bq.y, bq.z, bq.w};
     uint32_t pk[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int col = col0 + c8 + 2 * e;
-      __nv_bfloat162 h2 = __floats2bfloat162_rn(gelu_hw(v[c8 + 2 * e] + bias[col]), gelu_hw(v[c8 + 2 * e + 1] + bias[col + 1]));
-      pk[e] = *reinterpret_cast<uint32_t *>(&h2);
+      const __half2 x = __hadd2(__floats2half2_rn(v[c8 + 2 * e], v[c8 + 2 * e + 1]), bits_h2(bb[e]));
+      const __half2 in = __hmul2(x, __hfma2(c1, __hmul2(x, x), c0));
+      pk[e] = h2_bits(__hfma2(x, tanh_h2(in), x));
     }
     *reinterpret_cast<uint4 *>(A + kmaj_off(r, col0 + c8, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
   }
@@ -497,7 +517,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
   unsigned char *W2c = W1c + NH * NIN * 2;                    // [128 x 128]
   unsigned char *W3c = W2c + NH * NH * 2;                     // [16 x 128]
   unsigned char *R0 = W3c + TC_W3ROWS * NH * 2;               // group regions
-  float *cst = reinterpret_cast<float *>(R0 + TC_GROUPS * TC_REGION);  // b1, b2, b3
+  float *cst = reinterpret_cast<float *>(R0 + TC_GROUPS * TC_REGION);  // b1, b2 (F16 pairs), b3
+  uint32_t *hb = reinterpret_cast<uint32_t *>(cst);
   uint64_t *bars = reinterpret_cast<uint64_t *>(cst + 2 * NH + 4);     // one per group
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + TC_GROUPS);
   int *gbad = reinterpret_cast<int *>(tslot + 1);  // per group: an MMA wait timed out
@@ -507,22 +528,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
     const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
     *reinterpret_cast<uint4 *>(W1c + kmaj_off(r, c8, NIN)) = *reinterpret_cast<const uint4 *>(&w1b[r * NIN + c8]);
   }
-  for (int q = tid; q < NH * NH / 8; q += blockDim.x) {
-    const int r = q / (NH / 8), c8 = (q % (NH / 8)) * 8;
-    *reinterpret_cast<uint4 *>(W2c + kmaj_off(r, c8, NH)) = *reinterpret_cast<const uint4 *>(&w2b[r * NH + c8]);
+  for (int q = tid; q < NH * NH / 2; q += blockDim.x) {  // W2 / 2 in F16 (the epilogues store 2 gelu)
+    const int r = q / (NH / 2), k = (q % (NH / 2)) * 2;
+    const float2 w = *reinterpret_cast<const float2 *>(&params[OFF_W2 + r * NH + k]);
+    *reinterpret_cast<__half2 *>(W2c + kmaj_off(r, k, NH)) = __floats2half2_rn(0.5f * w.x, 0.5f * w.y);
   }
-  for (int q = tid; q < TC_W3ROWS * NH; q += blockDim.x) {  // split W3 (FP32) into hi and lo BF16 rows
+  for (int q = tid; q < TC_W3ROWS * NH; q += blockDim.x) {  // W3 / 2 split into hi and lo F16 rows
     const int r = q / NH, k = q % NH;
-    bf16 v = __float2bfloat16(0.f);
+    __half v = __float2half_rn(0.f);
     if (r < 2 * NOUT) {
-      const float w = params[OFF_W3 + (r % NOUT) * NH + k];
-      const bf16 hi = __float2bfloat16(w);
-      v = r < NOUT ? hi : __float2bfloat16(w - __bfloat162float(hi));
+      const float w = 0.5f * params[OFF_W3 + (r % NOUT) * NH + k];
+      const __half hi = __float2half_rn(w);
+      v = r < NOUT ? hi : __float2half_rn(w - __half2float(hi));
     }
-    *reinterpret_cast<bf16 *>(W3c + kmaj_off(r, k, NH)) = v;
+    *reinterpret_cast<__half *>(W3c + kmaj_off(r, k, NH)) = v;
   }
-  for (int t = tid; t < NH; t += blockDim.x) { cst[t] = params[OFF_B1 + t]; cst[NH + t] = params[OFF_B2 + t]; }
-  if (tid < NOUT) cst[2 * NH + tid] = params[OFF_B3 + tid];
+  for (int t = tid; t < NH / 2; t += blockDim.x) {
+    hb[t] = h2_bits(__floats2half2_rn(params[OFF_B1 + 2 * t], params[OFF_B1 + 2 * t + 1]));
+    hb[NH / 2 + t] = h2_bits(__floats2half2_rn(params[OFF_B2 + 2 * t], params[OFF_B2 + 2 * t + 1]));
+  }
+  if (tid < NOUT) cst[NH + tid] = params[OFF_B3 + tid];
   if (warp == 0) {  // 512 TMEM columns: 128 per group
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -540,7 +565,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;  // warp w of the group reads lanes 32w..
   unsigned char *A = R0 + g * TC_REGION;
   uint64_t *bar = &bars[g];
-  const float *b1 = cst, *b2 = cst + NH, *b3 = cst + 2 * NH;
+  const uint32_t *hb1 = hb, *hb2 = hb + NH / 2;
+  const float *b3 = cst + NH;
   const long LIMIT = 1L << 22;
   uint32_t phase = 0;
   const int ntiles = (n + TC_M - 1) / TC_M;
@@ -579,12 +605,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
       umma_commit(bar);
     }
     if (!wait_mma()) break;
-    // epilogue 1: H1 = bf16(gelu(D + b1)) over X (dead once layer 1 completed)
+    // epilogue 1: H1 = f16(2 gelu(D + b1)) over X (dead once layer 1 completed)
 #pragma unroll 1
     for (int cc = 0; cc < 4; ++cc) {
       float v[32];
       tmem_ld32(D + lane_base + cc * 32, v);
-      gelu_store32(v, b1, cc * 32, A, r);
+      gelu2_store32(v, hb1, cc * 32, A, r);
     }
     tc_fence_before();
     fence_async_smem();
@@ -594,17 +620,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
       const uint32_t wa = smem_u32(W2c);
 #pragma unroll
       for (int kk = 0; kk < NH / 16; ++kk)
-        umma_bf16(D, umma_desc(aa + kk * 256, 128, (NH / 8) * 128), umma_desc(wa + kk * 256, 128, (NH / 8) * 128),
-                  kk > 0);
+        umma_f16(D, umma_desc(aa + kk * 256, 128, (NH / 8) * 128), umma_desc(wa + kk * 256, 128, (NH / 8) * 128),
+                 UMMA_IDESC_H, kk > 0);
       umma_commit(bar);
     }
     if (!wait_mma()) break;
-    // epilogue 2: H2 = bf16(gelu(D + b2)) over H1
+    // epilogue 2: H2 = f16(2 gelu(D + b2)) over H1
 #pragma unroll 1
     for (int cc = 0; cc < 4; ++cc) {
       float v[32];
       tmem_ld32(D + lane_base + cc * 32, v);
-      gelu_store32(v, b2, cc * 32, A, r);
+      gelu2_store32(v, hb2, cc * 32, A, r);
     }
     tc_fence_before();
     fence_async_smem();
@@ -614,8 +640,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
       const uint32_t wa = smem_u32(W3c);
 #pragma unroll
       for (int kk = 0; kk < NH / 16; ++kk)
-        umma_bf16_n16(D, umma_desc(aa + kk * 256, 128, (NH / 8) * 128),
-                      umma_desc(wa + kk * 256, 128, (NH / 8) * 128), kk > 0);
+        umma_f16(D, umma_desc(aa + kk * 256, 128, (NH / 8) * 128), umma_desc(wa + kk * 256, 128, (NH / 8) * 128),
+                 UMMA_IDESC_H_N16, kk > 0);
       umma_commit(bar);
     }
     if (!wait_mma()) break;

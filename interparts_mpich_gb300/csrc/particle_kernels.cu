@@ -376,9 +376,9 @@ template void launch_sphere_integrals<float>(cudaStream_t, const Geo &, const Pa
 // and the normal lubrication force are applied (collisions.f90:199-205,
 // 430-432); the tangential history is still evolved and stored.
 // ---------------------------------------------------------------------------
-__device__ void d_lubrication(const PartGeo &pg, double pu, double pv, double pw, int idq, double nx, double ny,
-                              double nz, double eps, double u_nb, double v_nb, double w_nb, double &cfx, double &cfy,
-                              double &cfz) {
+// the scalar normal lubrication force f1 of lubrication (collisions.f90:222-438)
+__device__ double d_lub_f1(const PartGeo &pg, double pu, double pv, double pw, int idq, double nx, double ny,
+                           double nz, double eps, double u_nb, double v_nb, double w_nb) {
   const double u1a = pu * nx + pv * ny + pw * nz;
   const double u1b = u_nb * nx + v_nb * ny + w_nb * nz;
   double f1;
@@ -399,6 +399,12 @@ __device__ void d_lubrication(const PartGeo &pg, double pu, double pv, double pw
     f1 = (a11a * u1a + a11b * u1b);
     f1 = pg.coeff_f * (f1 - (pg.a11a_ini_pp * u1a + pg.a11b_ini_pp * u1b));
   }
+  return f1;
+}
+__device__ void d_lubrication(const PartGeo &pg, double pu, double pv, double pw, int idq, double nx, double ny,
+                              double nz, double eps, double u_nb, double v_nb, double w_nb, double &cfx, double &cfy,
+                              double &cfz) {
+  const double f1 = d_lub_f1(pg, pu, pv, pw, idq, nx, ny, nz, eps, u_nb, v_nb, w_nb);
   cfx = cfx + f1 * nx;
   cfy = cfy + f1 * ny;
   cfz = cfz + f1 * nz;
@@ -549,47 +555,59 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
                                                                    double dt) {
   __shared__ int cand[COLL_WARPS][COLL_CAP];
   __shared__ int ncand[COLL_WARPS];
+  __shared__ int fcs[COLL_WARPS][16];  // the particle's first contact partners (nq <= 15 here)
   const int np = pg.np, nq = pg.nq;
   const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int p = blockIdx.x * COLL_WARPS + wid;
   if (p >= np) return;
   if (lane == 0) ncand[wid] = 0;
-  __syncwarp();
   const double radius = pg.radius;
   const int qmax0 = b.qmax[p];
   const int *fc = b.firstc + (long)p * nq;
+  if (lane < qmax0 && lane < 16) fcs[wid][lane] = fc[lane];
+  __syncwarp();
   const float thr = 2.1f * (float)radius;
   const float thr2 = thr * thr;
   const float lxf = (float)pg.lx, lyf = (float)pg.ly;
   const float4 pp = b.pos4[p];
   const float pxf = pp.x, pyf = pp.y, pzf = pp.z;
-  for (int base = 0; base < np; base += 32) {
-    const int q = base + lane;
-    bool c = false;
-    if (q < np && q != p) {
-      const float4 qp = b.pos4[q];  // snapshot position, w = 1 for masters
-      if (qp.w != 0.f) {
-        float dxf = fabsf(qp.x - pxf);
-        float dyf = fabsf(qp.y - pyf);
-        const float dzf = qp.z - pzf;
+  // candidates in ascending q: within the collision distance or already in
+  // contact; four slices of 32 per round, loads issued together
+  constexpr int SL = 4;
+  for (int base = 0; base < np; base += 32 * SL) {
+    float4 qp[SL];
+    int qms[SL];
+#pragma unroll
+    for (int u = 0; u < SL; ++u) {
+      const int q = base + 32 * u + lane;
+      qp[u] = q < np ? b.pos4[q] : make_float4(0.f, 0.f, 0.f, 0.f);  // w: 1 for masters
+      qms[u] = q < np ? b.mslv[q] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < SL; ++u) {
+      const int q = base + 32 * u + lane;
+      bool c = false;
+      if (q < np && q != p && qp[u].w != 0.f) {
+        float dxf = fabsf(qp[u].x - pxf);
+        float dyf = fabsf(qp[u].y - pyf);
+        const float dzf = qp[u].z - pzf;
         dxf = fminf(dxf, fabsf(lxf - dxf));
         dyf = fminf(dyf, fabsf(lyf - dyf));
         c = dxf * dxf + dyf * dyf + dzf * dzf < thr2;
-        for (int i = 0; i < qmax0 && !c; ++i) c = (fc[i] == b.mslv[q]);
+        for (int i = 0; i < qmax0 && !c; ++i) c = ((i < 16 ? fcs[wid][i] : fc[i]) == qms[u]);
       }
+      const unsigned m = __ballot_sync(0xffffffffu, c);
+      if (c) {
+        const int pos = ncand[wid] + __popc(m & ((1u << lane) - 1u));
+        if (pos < COLL_CAP) cand[wid][pos] = q;
+      }
+      __syncwarp();
+      if (lane == 0) ncand[wid] += __popc(m);
+      __syncwarp();
     }
-    const unsigned m = __ballot_sync(0xffffffffu, c);
-    if (c) {
-      const int pos = ncand[wid] + __popc(m & ((1u << lane) - 1u));
-      if (pos < COLL_CAP) cand[wid][pos] = q;
-    }
-    __syncwarp();
-    if (lane == 0) ncand[wid] += __popc(m);
-    __syncwarp();
   }
-  if (lane != 0) return;
   int nc = ncand[wid];
-  if (nc > COLL_CAP) { atomicExch(&b.err[0], 1); nc = COLL_CAP; }
+  if (nc > COLL_CAP) { if (lane == 0) atomicExch(&b.err[0], 1); nc = COLL_CAP; }
   if (b.mslv[p] <= 0) return;
   const int idp = b.mslv[p];
   const double rkab = pg.rkab[rkiter - 1];
@@ -600,53 +618,92 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   const double px = PF(PF_X), py = PF(PF_Y), pz = PF(PF_Z);
   int qlast = b.qmax[p];
   int *fcw = b.firstc + (long)p * nq, *ofcw = b.ofirstc + (long)p * nq;
-  // (i) other particles, nb-outer / q-inner as in the reference
-  for (int nb = 0; nb < pg.nb_copies; ++nb) {
-    for (int ci = 0; ci < nc; ++ci) {
-      const int q = cand[wid][ci];
-      if (idp == b.mslv[q]) continue;
-      if (!(b.mslv[q] > 0)) continue;
-      const int idq = b.mslv[q];
-      double qx = b.pf[(long)PF_SX * np + q], qy = b.pf[(long)PF_SY * np + q];
-      const double qz = b.pf[(long)PF_SZ * np + q];
-      copy_shift_coll(nb, pg.lx, pg.ly, qx, qy);
-      const double deltaz = qz - pz;
-      const double deltax = minimg(qx - px, qx - pg.lx - px, qx + pg.lx - px);
-      const double deltay = minimg(qy - py, qy - pg.ly - py, qy + pg.ly - py);
-      const double dist = sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
-      const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
-      const double eps = (dist - 2. * radius) / radius;
-      const double qu = b.pf[(long)PF_SU * np + q], qv = b.pf[(long)PF_SV * np + q], qw = b.pf[(long)PF_SW * np + q];
-      if ((eps < 0.025) && (eps > 0.))
-        d_lubrication(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, qu, qv, qw, S.colfx, S.colfy, S.colfz);
+  // (i) other particles, nb-outer / q-inner as in the reference.  The 32
+  // lanes evaluate the geometry and the lubrication force f1 of 32 (copy,
+  // candidate) pairs at a time; lane 0 then takes them in the reference's
+  // order for the force sums, the contact bookkeeping and the collision
+  // forces, with the same arithmetic as a sequential pass.
+  const int npair = pg.nb_copies * nc;
+  for (int base = 0; base < npair; base += 32) {
+    const int k = base + lane;
+    int q = 0, idq = 0, use = 0, lub = 0;
+    double dist = 0., deltax = 0., deltay = 0., deltaz = 0., nx = 0., ny = 0., nz = 0., f1 = 0.;
+    double qu = 0., qv = 0., qw = 0.;
+    if (k < npair) {
+      const int nb = k / nc, ci = k - nb * nc;
+      q = cand[wid][ci];
+      use = idp != b.mslv[q] && b.mslv[q] > 0;
+      if (use) {
+        idq = b.mslv[q];
+        double qx = b.pf[(long)PF_SX * np + q], qy = b.pf[(long)PF_SY * np + q];
+        const double qz = b.pf[(long)PF_SZ * np + q];
+        copy_shift_coll(nb, pg.lx, pg.ly, qx, qy);
+        deltaz = qz - pz;
+        deltax = minimg(qx - px, qx - pg.lx - px, qx + pg.lx - px);
+        deltay = minimg(qy - py, qy - pg.ly - py, qy + pg.ly - py);
+        dist = sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
+        nx = deltax / dist; ny = deltay / dist; nz = deltaz / dist;
+        const double eps = (dist - 2. * radius) / radius;
+        qu = b.pf[(long)PF_SU * np + q]; qv = b.pf[(long)PF_SV * np + q]; qw = b.pf[(long)PF_SW * np + q];
+        if ((eps < 0.025) && (eps > 0.)) {
+          lub = 1;
+          f1 = d_lub_f1(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, qu, qv, qw);
+        }
+      }
+    }
+    const int cnt = min(32, npair - base);
+    for (int j = 0; j < cnt; ++j) {
+      const int juse = __shfl_sync(0xffffffffu, use, j);
+      if (!juse) continue;  // uniform across the warp
+      const int jq = __shfl_sync(0xffffffffu, q, j), jidq = __shfl_sync(0xffffffffu, idq, j);
+      const int jlub = __shfl_sync(0xffffffffu, lub, j);
+      const double jdist = __shfl_sync(0xffffffffu, dist, j);
+      const double jdx = __shfl_sync(0xffffffffu, deltax, j), jdy = __shfl_sync(0xffffffffu, deltay, j),
+                   jdz = __shfl_sync(0xffffffffu, deltaz, j);
+      const double jnx = __shfl_sync(0xffffffffu, nx, j), jny = __shfl_sync(0xffffffffu, ny, j),
+                   jnz = __shfl_sync(0xffffffffu, nz, j);
+      const double jf1 = __shfl_sync(0xffffffffu, f1, j);
+      const double jqu = __shfl_sync(0xffffffffu, qu, j), jqv = __shfl_sync(0xffffffffu, qv, j),
+                   jqw = __shfl_sync(0xffffffffu, qw, j);
+      if (lane != 0) continue;
+      if (jlub) {
+        S.colfx = S.colfx + jf1 * jnx;
+        S.colfy = S.colfy + jf1 * jny;
+        S.colfz = S.colfz + jf1 * jnz;
+      }
       int qq = 0;
       const int qm = b.qmax[p];
       for (int i = 1; i <= qm; ++i) {
-        if (idq == fcw[i - 1]) {
-          if (dist < (2. * radius)) {
+        if (jidq == fcw[i - 1]) {
+          if (jdist < (2. * radius)) {
             qq = i;
-            d_collisions(pg, b, p, S, qq, idq, dist, deltax, deltay, deltaz, qu, qv, qw,
-                         b.pf[(long)PF_SOMX * np + q], b.pf[(long)PF_SOMY * np + q], b.pf[(long)PF_SOMZ * np + q],
+            d_collisions(pg, b, p, S, qq, jidq, jdist, jdx, jdy, jdz, jqu, jqv, jqw,
+                         b.pf[(long)PF_SOMX * np + jq], b.pf[(long)PF_SOMY * np + jq], b.pf[(long)PF_SOMZ * np + jq],
                          dt, rkab);
           } else if (iter == itermax) {
             d_remove_contact(pg, b, p, i, qlast);
           }
         }
       }
-      if (qq == 0 && dist < (2. * radius)) {
+      if (qq == 0 && jdist < (2. * radius)) {
         qlast = qlast + 1;
-        if (qlast > nq) { atomicExch(&b.err[1], 1); qlast = nq; continue; }
+        if (qlast > nq) {  // overflow: flagged, the pair's update skipped
+          atomicExch(&b.err[1], 1);
+          qlast = nq;
+          continue;
+        }
         qq = qlast;
         d_new_contact(pg, b, p, qq);
-        d_collisions(pg, b, p, S, qq, idq, dist, deltax, deltay, deltaz, qu, qv, qw,
-                     b.pf[(long)PF_SOMX * np + q], b.pf[(long)PF_SOMY * np + q], b.pf[(long)PF_SOMZ * np + q],
+        d_collisions(pg, b, p, S, qq, jidq, jdist, jdx, jdy, jdz, jqu, jqv, jqw,
+                     b.pf[(long)PF_SOMX * np + jq], b.pf[(long)PF_SOMY * np + jq], b.pf[(long)PF_SOMZ * np + jq],
                      dt, rkab);
-        fcw[qlast - 1] = idq;
-        ofcw[qlast - 1] = idq;
+        fcw[qlast - 1] = jidq;
+        ofcw[qlast - 1] = jidq;
       }
       b.qmax[p] = qlast;
     }
   }
+  if (lane != 0) return;
   // (ii) walls (intgr_nwtn_eulr.f90:503-603)
   const int botw = np + 1, topw = np + 2;
   const int qm_w = b.qmax[p];
@@ -751,11 +808,11 @@ void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int
 // One block per particle; the compaction of points flagged `isout` keeps the
 // reference order.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_ne_finalize(PartGeo pg, PartBuffers b, IbmBuffers ib, int init) {
+__global__ void __launch_bounds__(256) k_ne_finalize(PartGeo pg, PartBuffers b, IbmBuffers ib, int init) {
   const int np = pg.np;
   const int p = blockIdx.x;
   __shared__ double sx, sy, sz, su, sv, sw, somx, somy, somz;
-  __shared__ int wcount[4];
+  __shared__ int wcount[32];
   __shared__ int base;
   // init: 0 = after Newton-Euler, 1 = initial set-up (initparticles +
   // coordsfp), 2 = Lagrangian points only (restart with given flags)
@@ -842,7 +899,7 @@ __global__ void __launch_bounds__(128) k_ne_finalize(PartGeo pg, PartBuffers b, 
 
 void launch_ne_finalize(cudaStream_t s, const PartGeo &pg, PartBuffers b, IbmBuffers ib, int init) {
   if (pg.np == 0) return;
-  k_ne_finalize<<<pg.np, 128, 0, s>>>(pg, b, ib, init);
+  k_ne_finalize<<<pg.np, 256, 0, s>>>(pg, b, ib, init);
 }
 
 }  // namespace ibmk

@@ -85,6 +85,27 @@ def forward(params: np.ndarray, x: np.ndarray, exact: bool = False) -> dict:
     return {"x": xb, "z1": z1, "h1": h1, "z2": z2, "h2": h2, "y": y}
 
 
+def f16(a: np.ndarray) -> np.ndarray:
+    """Round float32 values to IEEE half precision (round to nearest even), returned as float32."""
+    return np.asarray(a, np.float32).astype(np.float16).astype(np.float32)
+
+
+def forward_f16(params: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """The rounding points of the tensor-core inference kernel: BF16 features
+    and W1; pre-activations rounded to F16 before the F16 bias is added; the
+    epilogue stores f16(2 gelu(x)) and layers 2 and 3 use f16(W2 / 2) and
+    W3 / 2 split into an F16 value and its F16 remainder.  The GELU itself is
+    evaluated exactly here (the kernel evaluates it in packed half precision)."""
+    w1, b1, w2, b2, w3, b3 = split(params)
+    z1 = bf16(x).astype(np.float64) @ bf16(w1).T.astype(np.float64)
+    g1 = f16(2.0 * gelu(f16(f16(z1) + f16(b1))))
+    z2 = g1.astype(np.float64) @ f16(0.5 * w2).T.astype(np.float64)
+    g2 = f16(2.0 * gelu(f16(f16(z2) + f16(b2))))
+    hi = f16(0.5 * w3)
+    lo = f16(0.5 * w3 - hi)
+    return g2.astype(np.float64) @ (hi.astype(np.float64) + lo).T + b3
+
+
 def loss_and_grads(params: np.ndarray, x: np.ndarray, t: np.ndarray, exact: bool = False):
     """MSE loss mean over the batch of the squared error summed over outputs."""
     bf16 = _ident if exact else globals()["bf16"]

@@ -16,6 +16,10 @@ pytestmark = pytest.mark.gpu
 # can move a value across a BF16 rounding boundary now and then.
 GRAD_REL_TOL = 5e-3
 OUT_REL_TOL = 2e-3
+# the tensor-core inference kernel keeps its hidden activations in F16, the
+# training kernels and the mma.sync inference kernel in BF16: the two differ
+# by the BF16 rounding of the activations (3-4e-3 relative on these batches)
+F16_VS_BF16_TOL = 6e-3
 
 
 def _blocks():
@@ -70,15 +74,20 @@ def test_mlp_inference_matches_cpu_reference(gpu_lib, nb):
 
 @pytest.mark.parametrize("nb", [16, 128, 1000, 20011])
 def test_mlp_inference_tcgen05_matches_cpu_reference(gpu_lib, nb):
-    """The tcgen05 inference kernel (TMEM accumulators) against the CPU
-    reference and the mma.sync inference kernel."""
+    """The tcgen05 inference kernel (TMEM accumulators, F16 hidden
+    activations) against the CPU reference with its rounding points, the
+    mma.sync inference kernel, and the unrounded network: no less accurate
+    than the BF16 path."""
     case = small_case(n=16, nsp=0)
     g = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
     p, x, _ = _batch(nb, seed=nb + 7)
     y = g.mlp_infer_tc(p, x)
-    ref = mlp_ref.forward(p, x)["y"]
+    ref = mlp_ref.forward_f16(p, x)
     assert np.linalg.norm(y - ref) <= OUT_REL_TOL * np.linalg.norm(ref)
-    assert np.linalg.norm(y - g.mlp_infer(p, x)) <= OUT_REL_TOL * np.linalg.norm(ref)
+    assert np.linalg.norm(y - g.mlp_infer(p, x)) <= F16_VS_BF16_TOL * np.linalg.norm(ref)
+    exact = mlp_ref.forward(p, x, exact=True)["y"]
+    bf = mlp_ref.forward(p, x)["y"]
+    assert np.linalg.norm(y - exact) <= np.linalg.norm(bf - exact)
 
 
 def test_mlp_adam_steps_match_cpu_reference(gpu_lib):

@@ -55,3 +55,19 @@ def test_adam_first_step_is_signed_lr():
     g = np.array([1e-3, -2.0, 5.0], np.float64)
     p, m, v = mlp_ref.adam_step(np.zeros(3), g, np.zeros(3), np.zeros(3), 1, lr=1e-3)
     assert np.allclose(p, -1e-3 * np.sign(g), rtol=1e-4)
+
+
+def test_f16_forward_is_closer_to_exact_than_bf16():
+    """The F16 rounding model of the tensor-core inference kernel: within a
+    few 1e-3 of the unrounded network, and closer to it than the BF16 model
+    (the features and W1 are BF16 in both)."""
+    rng = np.random.default_rng(5)
+    p = mlp_ref.init_params(5)
+    p[12288:12416] = rng.standard_normal(128) * 0.1
+    p[28928:29312] *= 10.0
+    x = rng.standard_normal((500, 96)).astype(np.float32)
+    exact = mlp_ref.forward(p, x, exact=True)["y"]
+    e16 = np.linalg.norm(mlp_ref.forward_f16(p, x) - exact) / np.linalg.norm(exact)
+    eb = np.linalg.norm(mlp_ref.forward(p, x)["y"] - exact) / np.linalg.norm(exact)
+    assert e16 < 5e-3
+    assert e16 < eb
