@@ -253,6 +253,11 @@ __host__ __device__ inline int reg_n2(int N) {
   return N == 16 ? 4 : N == 32 ? 4 : N == 64 ? 8 : N == 128 ? 8 : N == 256 ? 16 : 0;
 }
 
+// divergence factors dt/dx, dt/dy, dt/dz as double-float pairs (hi, lo)
+struct DivScale {
+  float xh, xl, yh, yl, zh, zl;
+};
+
 // With phi1 (defect correction, DF): the right-hand side is the divergence
 // residual of the corrected velocity u* - f grad(phi1) (correc's FP32
 // expressions), formed on the fly instead of read from a stored state.
@@ -260,9 +265,9 @@ template <int N1, int N2, bool DF>
 __global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__restrict__ fu,
                                                        const float *__restrict__ fv, float *__restrict__ fw,
                                                        float2 *__restrict__ S, const float2 *__restrict__ twM,
-                                                       const float2 *__restrict__ twN, double dtidxi, double dtidyi,
-                                                       double dtidzi, const float *__restrict__ phi1, float cfi,
-                                                       float cfj, float cfk) {
+                                                       const float2 *__restrict__ twN, DivScale ds,
+                                                       const float *__restrict__ phi1, float cfi, float cfj,
+                                                       float cfk) {
   constexpr int M = N1 * N2, ROWS = 128 / N2;
   // group strides padded by 8 elements (64 B): groups sharing a warp start
   // half a bank row apart
@@ -271,10 +276,8 @@ __global__ void __launch_bounds__(128) k_fillps_fftx_r(Geo g, const float *__res
   __shared__ float2 EX[ROWS * ES];
   const int row0 = blockIdx.x * ROWS;
   const int nrow = g.J * g.K;
-  const float fx_hi = (float)dtidxi, fx_lo = (float)(dtidxi - (double)fx_hi);
-  const float fy_hi = (float)dtidyi, fy_lo = (float)(dtidyi - (double)fy_hi);
-  const float fz_hi = (float)dtidzi, fz_lo = (float)(dtidzi - (double)fz_hi);
-  const float fxs = (float)dtidxi, fys = (float)dtidyi, fzs = (float)dtidzi;
+  const float fx_hi = ds.xh, fx_lo = ds.xl, fy_hi = ds.yh, fy_lo = ds.yl, fz_hi = ds.zh, fz_lo = ds.zl;
+  const float fxs = ds.xh, fys = ds.yh, fzs = ds.zh;
   const int PL = g.I * g.J;
   // 1. right-hand side, packed z_m = x_{2m} + i x_{2m+1}; four consecutive
   // i per thread with 128-bit loads (I % 4 == 0 on this path)
@@ -434,12 +437,17 @@ bool launch_fftx_r(cudaStream_t s, const Geo &g, const float *fu, const float *f
   const int nrow = g.J * g.K;
   constexpr int ROWS = 128 / M2;
   const int grid = (nrow + ROWS - 1) / ROWS;
+  // the divergence factors as double-float pairs, split here once rather
+  // than in every thread (FP64 issues at a small fraction of the FP32 rate)
+  DivScale ds;
+  ds.xh = (float)a; ds.xl = (float)(a - (double)ds.xh);
+  ds.yh = (float)b; ds.yl = (float)(b - (double)ds.yh);
+  ds.zh = (float)c; ds.zl = (float)(c - (double)ds.zh);
   if (inv) k_ifftx_r<M1, M2><<<grid, 128, 0, s>>>(g, S, phi, twM, twN);
   else if (df)
-    k_fillps_fftx_r<M1, M2, true><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c, rs.phi1, rs.fi, rs.fj,
-                                                        rs.fk);
+    k_fillps_fftx_r<M1, M2, true><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, ds, rs.phi1, rs.fi, rs.fj, rs.fk);
   else
-    k_fillps_fftx_r<M1, M2, false><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, a, b, c, nullptr, 0.f, 0.f, 0.f);
+    k_fillps_fftx_r<M1, M2, false><<<grid, 128, 0, s>>>(g, fu, fv, fw, S, twM, twN, ds, nullptr, 0.f, 0.f, 0.f);
   return true;
 }
 bool fftx_r(cudaStream_t s, const Geo &g, const float *fu, const float *fv, float *fw, float2 *S, const float2 *twM,

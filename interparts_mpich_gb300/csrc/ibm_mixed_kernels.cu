@@ -55,18 +55,27 @@ __global__ void __launch_bounds__(256) k_ibm_stencil_c(Geo g, PartGeo pg, IbmBuf
     double coorxfp = xfp * g.dxi - (sx < 0. ? -(double)g.I : (sx >= g.lx ? (double)g.I : 0.));
     double cooryfp = yfp * g.dyi - (sy < 0. ? -(double)g.J : (sy >= g.ly ? (double)g.J : 0.));
     double coorzfp = zfp * g.dzi;
-    if (!(coorxfp >= 0. && coorxfp <= g.I + 1.) || !(cooryfp >= 0. && cooryfp <= g.J + 1.) ||
-        !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
+    // floor n and exact fraction f = c - n of each coordinate (FP64 issues
+    // at a small fraction of the FP32 rate: the origins and range checks
+    // follow from n and f with integer and FP32 work); NINT rounds half
+    // away from zero
+    int nx = __double2int_rd(coorxfp), ny = __double2int_rd(cooryfp), nz = __double2int_rd(coorzfp);
+    double frx = coorxfp - (double)nx, fry = cooryfp - (double)ny, frz = coorzfp - (double)nz;
+    if (!(nx >= 0 && (nx <= g.I || (nx == g.I + 1 && frx == 0.))) ||
+        !(ny >= 0 && (ny <= g.J || (ny == g.J + 1 && fry == 0.))) || !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
       atomicExch(&b.err[2], 1);
-      coorxfp = 1.; cooryfp = 1.; coorzfp = 1.5;
+      nx = 1; ny = 1; nz = 1; frx = 0.; fry = 0.; frz = 0.5;
     }
-    const int ilows = fnint(coorxfp) - 1, jlows = fnint(cooryfp) - 1, klows = max(fnint(coorzfp) - 1, 1);
-    const int ilow = (int)floor(coorxfp), jlow = (int)floor(cooryfp);
-    const int klow = max(min((int)floor(coorzfp), g.K - 2), 1);
-    // offsets of the point from the stencil origins (FP64, exact integer
-    // parts), the 3-tap arguments then in FP32
-    const float ox = (float)(coorxfp - ilows), oy = (float)(cooryfp - jlows), oz = (float)(coorzfp - klows);
-    const float hx = (float)(coorxfp - ilow), hy = (float)(cooryfp - jlow), hz = (float)(coorzfp - klow);
+    const int ux = frx > 0.5 || (frx == 0.5 && nx >= 0), uy = fry > 0.5 || (fry == 0.5 && ny >= 0),
+              uz = frz > 0.5 || (frz == 0.5 && nz >= 0);
+    const int ilows = nx + ux - 1, jlows = ny + uy - 1, klows = max(nz + uz - 1, 1);
+    const int ilow = nx, jlow = ny;
+    const int klow = max(min(nz, g.K - 2), 1);
+    // offsets of the point from the stencil origins: the FP32 fraction plus
+    // the small integer between floor and origin (0, 1 or 2)
+    const float fx = (float)frx, fy = (float)fry, fz = (float)frz;
+    const float ox = fx + (float)(nx - ilows), oy = fy + (float)(ny - jlows), oz = fz + (float)(nz - klows);
+    const float hx = fx, hy = fy, hz = fz + (float)(nz - klow);
     float phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
     for (int m = 0; m < 3; ++m) {
       phix[m] = delta3f((float)m - ox);
@@ -571,13 +580,13 @@ struct FeatSink {
 
 __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, IbmBuffers b, const float *__restrict__ fu,
                                                         const float *__restrict__ fv, const float *__restrict__ fw,
-                                                        double dt, const float *__restrict__ mu,
+                                                        double dt, double dti, float inv_r,
+                                                        const float *__restrict__ mu,
                                                         const float *__restrict__ isig,
                                                         __nv_bfloat16 *__restrict__ X, HarvestArgs H,
                                                         int first_force) {
   const int n = pg.np * pg.nl;
   const long npl = n;
-  const double dti = 1. / dt;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
     if (l >= b.nla[p]) {
@@ -613,7 +622,6 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
       continue;
     }
     const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
-    const float inv_r = (float)(1. / pg.radfp);
     const float nrm[3] = {(float)(b.xfp[t] - px) * inv_r, (float)(b.yfp[t] - py) * inv_r,
                           (float)(b.zfp[t] - pz) * inv_r};
     const CompStencil *cs3[3] = {&su, &sv, &sw};
@@ -652,16 +660,19 @@ void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmB
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                            __nv_bfloat16 *X, const HarvestArgs &H, int first_force) {
   if (pg.np == 0) return;
-  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X, H, first_force);
+  // reciprocals on the host: an FP64 division in every thread costs more
+  // than the kernel's per-point FP64 work
+  k_ibm_features_f<<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, dt, 1. / dt, (float)(1. / pg.radfp), mu, isig, X, H,
+                                        first_force);
 }
 
 // Features of the learned loop, one block per (particle, component) on the
 // particle's box (same values and order as k_ibm_features_f); also the first
 // pass's interpolation and point forces F0.
-__global__ void __launch_bounds__(256) k_ibm_features_comp(Geo g, PartGeo pg, IbmBuffers b,
+__global__ void __launch_bounds__(256, 4) k_ibm_features_comp(Geo g, PartGeo pg, IbmBuffers b,
                                                            const float *__restrict__ fu,
                                                            const float *__restrict__ fv,
-                                                           const float *__restrict__ fw, double dt,
+                                                           const float *__restrict__ fw, double dt, double dti, float inv_r,
                                                            const float *__restrict__ mu,
                                                            const float *__restrict__ isig,
                                                            __nv_bfloat16 *__restrict__ X) {
@@ -686,8 +697,6 @@ __global__ void __launch_bounds__(256) k_ibm_features_comp(Geo g, PartGeo pg, Ib
   double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
   const double *xc = c == 0 ? b.xfp : (c == 1 ? b.yfp : b.zfp);
   const double pc = b.pf[(c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z)) * pg.np + p];
-  const float inv_r = (float)(1. / pg.radfp);
-  const double dti = 1. / dt;
   const CompStencil *csp = b.cs + c * npl + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
   for (int l = threadIdx.x; l < pg.nl; l += blockDim.x) {
@@ -738,7 +747,8 @@ void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, I
                               const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                               __nv_bfloat16 *X) {
   if (pg.np == 0) return;
-  k_ibm_features_comp<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, dt, mu, isig, X);
+  k_ibm_features_comp<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, dt, 1. / dt,
+                                                                              (float)(1. / pg.radfp), mu, isig, X);
 }
 
 int ibm_set_smem_limits() {

@@ -86,25 +86,33 @@ __device__ __forceinline__ double corner_fraction(double radius, double dxm2, do
 }
 
 // FP32 corner fraction (mixed form): the same expression in single
-// precision; its decisions at the surface are continuous in the distances
+// precision, with the hardware's approximate square root and reciprocal
+// (relative errors of a few 1e-7, below the FP32 rounding of the squared
+// distances they act on); its decisions at the surface are continuous in
+// the distances
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ float corner_fraction_f(float radius, float dxm2, float dxp2, float dym2, float dyp2,
                                                   float dzm2, float dzp2) {
   float sg[8];
-  sg[0] = radius - sqrtf(dxm2 + dym2 + dzm2);
-  sg[1] = radius - sqrtf(dxm2 + dyp2 + dzm2);
-  sg[2] = radius - sqrtf(dxp2 + dyp2 + dzm2);
-  sg[3] = radius - sqrtf(dxp2 + dym2 + dzm2);
-  sg[4] = radius - sqrtf(dxm2 + dym2 + dzp2);
-  sg[5] = radius - sqrtf(dxm2 + dyp2 + dzp2);
-  sg[6] = radius - sqrtf(dxp2 + dyp2 + dzp2);
-  sg[7] = radius - sqrtf(dxp2 + dym2 + dzp2);
+  sg[0] = radius - sqrt_approx(dxm2 + dym2 + dzm2);
+  sg[1] = radius - sqrt_approx(dxm2 + dyp2 + dzm2);
+  sg[2] = radius - sqrt_approx(dxp2 + dyp2 + dzm2);
+  sg[3] = radius - sqrt_approx(dxp2 + dym2 + dzm2);
+  sg[4] = radius - sqrt_approx(dxm2 + dym2 + dzp2);
+  sg[5] = radius - sqrt_approx(dxm2 + dyp2 + dzp2);
+  sg[6] = radius - sqrt_approx(dxp2 + dyp2 + dzp2);
+  sg[7] = radius - sqrt_approx(dxp2 + dym2 + dzp2);
   float sum1 = 0.f, sum2 = 0.f;
 #pragma unroll
   for (int cp = 0; cp < 8; ++cp) {
     sum1 += fmaxf(sg[cp], 0.f);
     sum2 += fabsf(sg[cp]);
   }
-  return sum1 / sum2;
+  return __fdividef(sum1, sum2);
 }
 
 // Sums of one velocity component over the cells of the sphere's box.  Block
@@ -128,50 +136,78 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
   const int p = blockIdx.x, comp = blockIdx.y;
   const int ms = b.mslv[p];
   if (ms <= 0) return;
-  const double radius = pg.radius;
-  const double dx = 1. / g.dxi, dy = 1. / g.dyi, dz = 1. / g.dzi;
-  const double radin = radius - 2. * dx;
-  const double radin2 = radin * radin;
-  // sqrt(d2) >= radius  <=>  d2 >= rthr (rthr: smallest double whose
-  // correctly rounded square root is >= radius)
-  const double rthr = pg.rthr;
-  const float radin2_lo = (float)(radin2 * (1. - 1e-5)), radin2_hi = (float)(radin2 * (1. + 1e-5));
-  const float rthr_lo = (float)(rthr * (1. - 1e-5)), rthr_hi = (float)(rthr * (1. + 1e-5));
-  const float radin2f = (float)radin2, rthrf = (float)rthr, radiusf = (float)radius;
+  // Block-uniform FP64 set-up (thresholds, the box of each periodic copy)
+  // is computed by one thread and read from shared memory: FP64 issues at a
+  // small fraction of the FP32 rate, and every thread repeating it cost more
+  // than the line sums themselves.
+  __shared__ double s_radin2, s_cx, s_cy, s_cz;
+  __shared__ float s_thr[7];
+  __shared__ int s_box[6];  // ilow, ni, jlow, nj, klow, nk
+  if (threadIdx.x == 0) {
+    const double radin = pg.radius - 2. * g.dx;
+    const double radin2 = radin * radin;
+    s_radin2 = radin2;
+    // sqrt(d2) >= radius  <=>  d2 >= rthr (rthr: smallest double whose
+    // correctly rounded square root is >= radius)
+    s_thr[0] = (float)(radin2 * (1. - 1e-5));
+    s_thr[1] = (float)(radin2 * (1. + 1e-5));
+    s_thr[2] = (float)(pg.rthr * (1. - 1e-5));
+    s_thr[3] = (float)(pg.rthr * (1. + 1e-5));
+    s_thr[4] = (float)radin2;
+    s_thr[5] = (float)pg.rthr;
+    s_thr[6] = (float)pg.radius;
+  }
+  __syncthreads();
+  const double radius = pg.radius, dx = g.dx, dy = g.dy, dz = g.dz;
+  const double radin2 = s_radin2, rthr = pg.rthr;
+  const float radin2_lo = s_thr[0], radin2_hi = s_thr[1], rthr_lo = s_thr[2], rthr_hi = s_thr[3];
+  const float radin2f = s_thr[4], rthrf = s_thr[5], radiusf = s_thr[6];
   __shared__ double sxm[AX], sxp[AX], srx[AX], sym[AX], syp[AX], sry[AX], szm[AX], szp[AX], srz[AX];
   __shared__ float fxm[AX], fxp[AX], fym[AX], fyp[AX], fzm[AX], fzp[AX];
-  __shared__ float frxh[GEO32 ? AX : 1], frxl[GEO32 ? AX : 1];  // rx as a double-float pair
+  // rx, ry, rz as double-float pairs (mixed form)
+  __shared__ float frxh[GEO32 ? AX : 1], frxl[GEO32 ? AX : 1], fryh[GEO32 ? AX : 1], fryl[GEO32 ? AX : 1];
+  __shared__ float frzh[GEO32 ? AX : 1], frzl[GEO32 ? AX : 1];
   __shared__ int queue[GEO32 ? 1 : QCAP];
   __shared__ int qn;
   __shared__ double red[3][256];
   const T *F = comp == 0 ? u : (comp == 1 ? v : w);
   const int *nbf = b.nb + (long)p * 9;
   double a0 = 0., ta = 0., tb = 0.;
+  // mixed form: the same three sums in double-float across the lines
+  float A0h = 0.f, A0l = 0.f, TAh = 0.f, TAl = 0.f, TBh = 0.f, TBl = 0.f;
   // lever arms per component: ta += la * f*w, tb += lb * f*w with
   // comp 0: (rz, -ry), comp 1: (-rz, rx), comp 2: (ry, -rx)
   for (int nb = 0; nb <= 8; ++nb) {
     if (nb > 0 && nbf[nb] != 1) continue;
-    int nbrecv = nb;
-    if (nb > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
-    double cx = PF(PF_X), cy = PF(PF_Y);
-    const double cz = PF(PF_Z);
-    if (nb > 0) copy_shift_sphere(nbrecv, g.lx, g.ly, cx, cy);
-    int ilow = fnint((cx - radius) * g.dxi - 2.), ihigh = fnint((cx + radius) * g.dxi + 2.);
-    int jlow = fnint((cy - radius) * g.dyi - 2.), jhigh = fnint((cy + radius) * g.dyi + 2.);
-    int klow = fnint((cz - radius) * g.dzi - 2.), khigh = fnint((cz + radius) * g.dzi + 2.);
-    if (ilow < 1) ilow = 1;
-    if (jlow < 1) jlow = 1;
-    if (klow < 1) klow = 1;
-    if (ihigh > g.I) ihigh = g.I;
-    if (jhigh > g.J) jhigh = g.J;
-    if (khigh > g.K) khigh = g.K;
-    const int ni = ihigh - ilow + 1, nj = jhigh - jlow + 1, nk = khigh - klow + 1;
+    __syncthreads();  // previous copy done with the tables and the box
+    if (threadIdx.x == 0) {
+      int nbrecv = nb;
+      if (nb > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
+      double cx = PF(PF_X), cy = PF(PF_Y);
+      const double cz = PF(PF_Z);
+      if (nb > 0) copy_shift_sphere(nbrecv, g.lx, g.ly, cx, cy);
+      int ilow = fnint((cx - radius) * g.dxi - 2.), ihigh = fnint((cx + radius) * g.dxi + 2.);
+      int jlow = fnint((cy - radius) * g.dyi - 2.), jhigh = fnint((cy + radius) * g.dyi + 2.);
+      int klow = fnint((cz - radius) * g.dzi - 2.), khigh = fnint((cz + radius) * g.dzi + 2.);
+      if (ilow < 1) ilow = 1;
+      if (jlow < 1) jlow = 1;
+      if (klow < 1) klow = 1;
+      if (ihigh > g.I) ihigh = g.I;
+      if (jhigh > g.J) jhigh = g.J;
+      if (khigh > g.K) khigh = g.K;
+      s_cx = cx; s_cy = cy; s_cz = cz;
+      s_box[0] = ilow; s_box[1] = ihigh - ilow + 1;
+      s_box[2] = jlow; s_box[3] = jhigh - jlow + 1;
+      s_box[4] = klow; s_box[5] = khigh - klow + 1;
+    }
+    __syncthreads();
+    const double cx = s_cx, cy = s_cy, cz = s_cz;
+    const int ilow = s_box[0], ni = s_box[1], jlow = s_box[2], nj = s_box[3], klow = s_box[4], nk = s_box[5];
     if (ni <= 0 || nj <= 0 || nk <= 0) continue;
     if (ni > AX || nj > AX || nk > AX) {  // sphere wider than the axis tables: flag, skip
       if (threadIdx.x == 0) atomicExch(&b.err[3], 1);
       continue;
     }
-    __syncthreads();  // previous copy done with the tables
     // per-axis corner distances and cell-centre offsets, in the reference's
     // expressions (intgr_over_sphere.f90:335-508)
     for (int t = threadIdx.x; t < AX; t += blockDim.x) {
@@ -196,6 +232,10 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
         sym[t] = (mn - cy) * (mn - cy); syp[t] = (pl - cy) * (pl - cy);
         fym[t] = (float)sym[t]; fyp[t] = (float)syp[t];
         sry[t] = 0. + (j - 0.5) * dy - cy;
+        if constexpr (GEO32) {
+          fryh[t] = (float)sry[t];
+          fryl[t] = (float)(sry[t] - (double)fryh[t]);
+        }
       }
       if (t < nk) {
         const int k = klow + t;
@@ -205,6 +245,10 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
         szm[t] = (mn - cz) * (mn - cz); szp[t] = (pl - cz) * (pl - cz);
         fzm[t] = (float)szm[t]; fzp[t] = (float)szp[t];
         srz[t] = (k - 0.5) * dz - cz;
+        if constexpr (GEO32) {
+          frzh[t] = (float)srz[t];
+          frzl[t] = (float)(srz[t] - (double)frzh[t]);
+        }
       }
     }
     if (threadIdx.x == 0) qn = 0;
@@ -283,14 +327,31 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
           sx = fma(srx[ti], fw, sx);
         }
         if constexpr (GEO32) {
-          s0 = (double)s0h + (double)s0l;
-          sx = (double)sxh + (double)sxl;
+          // the line sums into the thread's double-float totals (no FP64
+          // per line)
+          float qh, ql;
+          df_add(A0h, A0l, s0h, s0l, A0h, A0l);
+          if (comp == 0) {
+            df_mul(s0h, s0l, frzh[tk], frzl[tk], qh, ql);
+            df_add(TAh, TAl, qh, ql, TAh, TAl);
+            df_mul(s0h, s0l, fryh[tj], fryl[tj], qh, ql);
+            df_add(TBh, TBl, -qh, -ql, TBh, TBl);
+          } else if (comp == 1) {
+            df_mul(s0h, s0l, frzh[tk], frzl[tk], qh, ql);
+            df_add(TAh, TAl, -qh, -ql, TAh, TAl);
+            df_add(TBh, TBl, sxh, sxl, TBh, TBl);
+          } else {
+            df_mul(s0h, s0l, fryh[tj], fryl[tj], qh, ql);
+            df_add(TAh, TAl, qh, ql, TAh, TAl);
+            df_add(TBh, TBl, -sxh, -sxl, TBh, TBl);
+          }
+        } else {
+          const double ry = sry[tj], rz = srz[tk];
+          a0 += s0;
+          if (comp == 0) { ta = fma(rz, s0, ta); tb = fma(-ry, s0, tb); }
+          else if (comp == 1) { ta = fma(-rz, s0, ta); tb += sx; }
+          else { ta = fma(ry, s0, ta); tb -= sx; }
         }
-        const double ry = sry[tj], rz = srz[tk];
-        a0 += s0;
-        if (comp == 0) { ta = fma(rz, s0, ta); tb = fma(-ry, s0, tb); }
-        else if (comp == 1) { ta = fma(-rz, s0, ta); tb += sx; }
-        else { ta = fma(ry, s0, ta); tb -= sx; }
       }
       if (!GEO32) {
         __syncthreads();
@@ -320,16 +381,24 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
       }
     }
   }
+  if constexpr (GEO32) {
+    a0 += (double)A0h + (double)A0l;
+    ta += (double)TAh + (double)TAl;
+    tb += (double)TBh + (double)TBl;
+  }
+  // block sums: three warps, each over one of the staged partials
   red[0][threadIdx.x] = a0;
   red[1][threadIdx.x] = ta;
   red[2][threadIdx.x] = tb;
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o)
-      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
-    __syncthreads();
+  const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (wq < 3) {
+    double x = 0.;
+    for (int q = lane; q < (int)blockDim.x; q += 32) x += red[wq][q];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
+    if (lane == 0) b.red[np + ((long)p * 3 + comp) * 3 + wq] = x;
   }
-  if (threadIdx.x < 3) b.red[np + ((long)p * 3 + comp) * 3 + threadIdx.x] = red[threadIdx.x][0];
 }
 
 // unit field for the volume sums (type 1)
@@ -856,25 +925,38 @@ __global__ void __launch_bounds__(256) k_ne_finalize(PartGeo pg, PartBuffers b, 
   __syncthreads();
   const int nl = pg.nl;
   const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const float lxf = (float)pg.lx, lyf = (float)pg.ly;
   for (int l0 = 0; l0 < nl; l0 += blockDim.x) {
     const int l = l0 + threadIdx.x;
     bool keep = false;
-    double xfploc = 0, yfploc = 0, zfploc = 0;
+    double xfploc = 0, yfploc = 0, zfploc = 0, rx = 0, ry = 0, rz = 0;
     if (l < nl && b.mslv[p] != 0) {
       const double st = b.sincos[l], ct = b.sincos[nl + l], sp = b.sincos[2 * nl + l], cp = b.sincos[3 * nl + l];
-      xfploc = sx + pg.radfp * st * cp;
-      yfploc = sy + pg.radfp * st * sp;
-      zfploc = sz + pg.radfp * ct;
-      double isperiodx = 0., isperiody = 0.;
-      if (xfploc < 0. + 0.5 * pg.dx) isperiodx = 1.;
-      if (xfploc >= pg.lx + 0.5 * pg.dx) isperiodx = -1.;
-      if (yfploc < 0. + 0.5 * pg.dy) isperiody = 1.;
-      if (yfploc >= pg.ly + 0.5 * pg.dy) isperiody = -1.;
+      // offsets from the centre, radfp*st*cp etc. with the reference's
+      // rounding; they also serve as (xfp - xc) in the point velocities
+      const double rst = pg.radfp * st;
+      rx = rst * cp;
+      ry = rst * sp;
+      rz = pg.radfp * ct;
+      xfploc = sx + rx;
+      yfploc = sy + ry;
+      zfploc = sz + rz;
+      // isout (periodic image outside 1..I, 1..J) is impossible for points
+      // within half a domain of it: an FP32 screen decides those, the
+      // reference's FP64 test the rest
+      const float xf = (float)xfploc, yf = (float)yfploc;
       bool isout = false;
-      const double coorxfp = (xfploc + isperiodx * pg.lx - 0.) * pg.dxi;
-      if (fnint(coorxfp) < 1 || fnint(coorxfp) > pg.I) isout = true;
-      const double cooryfp = (yfploc + isperiody * pg.ly - 0.) * pg.dyi;
-      if (fnint(cooryfp) < 1 || fnint(cooryfp) > pg.J) isout = true;
+      if (!(xf > -0.4f * lxf && xf < 1.4f * lxf && yf > -0.4f * lyf && yf < 1.4f * lyf)) {
+        double isperiodx = 0., isperiody = 0.;
+        if (xfploc < 0. + 0.5 * pg.dx) isperiodx = 1.;
+        if (xfploc >= pg.lx + 0.5 * pg.dx) isperiodx = -1.;
+        if (yfploc < 0. + 0.5 * pg.dy) isperiody = 1.;
+        if (yfploc >= pg.ly + 0.5 * pg.dy) isperiody = -1.;
+        const double coorxfp = (xfploc + isperiodx * pg.lx - 0.) * pg.dxi;
+        if (fnint(coorxfp) < 1 || fnint(coorxfp) > pg.I) isout = true;
+        const double cooryfp = (yfploc + isperiody * pg.ly - 0.) * pg.dyi;
+        if (fnint(cooryfp) < 1 || fnint(cooryfp) > pg.J) isout = true;
+      }
       keep = !isout;
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -886,9 +968,9 @@ __global__ void __launch_bounds__(256) k_ne_finalize(PartGeo pg, PartBuffers b, 
     if (keep) {
       const long t = (long)p * nl + off;
       ib.xfp[t] = xfploc; ib.yfp[t] = yfploc; ib.zfp[t] = zfploc;
-      ib.ul[t] = su + somy * (zfploc - sz) - somz * (yfploc - sy);
-      ib.vl[t] = sv + somz * (xfploc - sx) - somx * (zfploc - sz);
-      ib.wl[t] = sw + somx * (yfploc - sy) - somy * (xfploc - sx);
+      ib.ul[t] = su + somy * rz - somz * ry;
+      ib.vl[t] = sv + somz * rx - somx * rz;
+      ib.wl[t] = sw + somx * ry - somy * rx;
     }
     __syncthreads();
     if (threadIdx.x == 0) for (int q = 0; q < (int)(blockDim.x / 32); ++q) base += wcount[q];
