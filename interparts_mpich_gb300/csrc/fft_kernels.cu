@@ -705,18 +705,24 @@ __global__ void __launch_bounds__(128) k_thomas_df(Geo g, float2 *__restrict__ S
   constexpr int PF = 8;
   // previous plane's value, real and imaginary parts, double-float
   float prh = 0.f, prl = 0.f, pih = 0.f, pil = 0.f;
-  for (int k0 = 0; k0 < K; k0 += PF) {
-    float2 buf[PF], zb[PF];
+  // Both sweeps run over chunks of PF planes with the next chunk's loads
+  // issued before the current chunk is computed (two buffers), so that the
+  // HBM latency of a chunk overlaps the dependent double-float chain of the
+  // previous one.
+  float2 buf[2][PF], cb[2][PF];
+  auto load_fwd = [&](int slot, int k0) {
 #pragma unroll
     for (int q = 0; q < PF; ++q) {
       const int k = k0 + q;
-      if (k < K) { buf[q] = s[k * sstride]; zb[q] = z[(long)k * zstride]; }
+      if (k < K) { buf[slot][q] = s[k * sstride]; cb[slot][q] = z[(long)k * zstride]; }
     }
+  };
+  auto fwd = [&](int slot, int k0) {
 #pragma unroll
     for (int q = 0; q < PF; ++q) {
       const int k = k0 + q;
       if (k >= K) break;
-      float rh = buf[q].x, rl = 0.f, ih = buf[q].y, il = 0.f;
+      float rh = buf[slot][q].x, rl = 0.f, ih = buf[slot][q].y, il = 0.f;
       if (k > 0) {  // d - dzi^2 * prev
         float qh, ql;
         df_mul(a2h, a2l, prh, prl, qh, ql);
@@ -725,39 +731,49 @@ __global__ void __launch_bounds__(128) k_thomas_df(Geo g, float2 *__restrict__ S
         df_add(ih, il, -qh, -ql, ih, il);
       }
       // times the pivot reciprocal (k < K-1) or 1/den (k = K-1)
-      df_mul(rh, rl, zb[q].x, zb[q].y, prh, prl);
-      df_mul(ih, il, zb[q].x, zb[q].y, pih, pil);
-      buf[q] = make_float2(__fadd_rn(prh, prl), __fadd_rn(pih, pil));
+      df_mul(rh, rl, cb[slot][q].x, cb[slot][q].y, prh, prl);
+      df_mul(ih, il, cb[slot][q].x, cb[slot][q].y, pih, pil);
+      const float2 o = make_float2(__fadd_rn(prh, prl), __fadd_rn(pih, pil));
+      if (k < K - 1) s[k * sstride] = o;
+      else s[k * sstride] = make_float2(o.x * fscale, o.y * fscale);
     }
-#pragma unroll
-    for (int q = 0; q < PF; ++q) {
-      const int k = k0 + q;
-      if (k < K - 1) s[k * sstride] = buf[q];
-      else if (k == K - 1) s[k * sstride] = make_float2(buf[q].x * fscale, buf[q].y * fscale);
-    }
+  };
+  load_fwd(0, 0);
+  for (int k0 = 0; k0 < K; k0 += 2 * PF) {
+    if (k0 + PF < K) load_fwd(1, k0 + PF);
+    fwd(0, k0);
+    if (k0 + PF >= K) break;
+    if (k0 + 2 * PF < K) load_fwd(0, k0 + 2 * PF);
+    fwd(1, k0 + PF);
   }
   // back substitution x_k = x'_k - dzi^2 z_k x_{k+1}
-  for (int k1 = K - 2; k1 >= 0; k1 -= PF) {
-    float2 buf[PF], ab[PF];
+  auto load_bwd = [&](int slot, int k1) {
 #pragma unroll
     for (int q = 0; q < PF; ++q) {
       const int k = k1 - q;
-      if (k >= 0) { buf[q] = s[k * sstride]; ab[q] = az[(long)k * zstride]; }
+      if (k >= 0) { buf[slot][q] = s[k * sstride]; cb[slot][q] = az[(long)k * zstride]; }
     }
+  };
+  auto bwd = [&](int slot, int k1) {
 #pragma unroll
     for (int q = 0; q < PF; ++q) {
       const int k = k1 - q;
       if (k < 0) break;
       float qh, ql;
-      df_mul(ab[q].x, ab[q].y, prh, prl, qh, ql);
-      df_add(buf[q].x, 0.f, -qh, -ql, prh, prl);
-      df_mul(ab[q].x, ab[q].y, pih, pil, qh, ql);
-      df_add(buf[q].y, 0.f, -qh, -ql, pih, pil);
-      buf[q] = make_float2(__fadd_rn(prh, prl) * fscale, __fadd_rn(pih, pil) * fscale);
+      df_mul(cb[slot][q].x, cb[slot][q].y, prh, prl, qh, ql);
+      df_add(buf[slot][q].x, 0.f, -qh, -ql, prh, prl);
+      df_mul(cb[slot][q].x, cb[slot][q].y, pih, pil, qh, ql);
+      df_add(buf[slot][q].y, 0.f, -qh, -ql, pih, pil);
+      s[k * sstride] = make_float2(__fadd_rn(prh, prl) * fscale, __fadd_rn(pih, pil) * fscale);
     }
-#pragma unroll
-    for (int q = 0; q < PF; ++q)
-      if (k1 - q >= 0) s[(k1 - q) * sstride] = buf[q];
+  };
+  if (K >= 2) load_bwd(0, K - 2);
+  for (int k1 = K - 2; k1 >= 0; k1 -= 2 * PF) {
+    if (k1 - PF >= 0) load_bwd(1, k1 - PF);
+    bwd(0, k1);
+    if (k1 - PF < 0) break;
+    if (k1 - 2 * PF >= 0) load_bwd(0, k1 - 2 * PF);
+    bwd(1, k1 - PF);
   }
 }
 
