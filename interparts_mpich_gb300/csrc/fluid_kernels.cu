@@ -128,7 +128,11 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
 // k, k+1 of p (with a one-cell x/y halo, periodic) in shared memory, so each
 // field is read from HBM about once.  Same expressions as k_predict.
 constexpr int PTX = 32, PTY = 8, PHX = PTX + 2, PHY = PTY + 2, PKC = 32;
-template <int STAGE>
+// BUOY: momzbuoy from the scalar field cb (FP64).  A separate instantiation
+// keeps the FP64 buoyancy instructions out of the kernel without a scalar:
+// issued under a false predicate they still take FP64 issue slots, which on
+// this GPU run at 1/64 of the FP32 rate.
+template <int STAGE, bool BUOY>
 __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *__restrict__ u,
                                                             const float *__restrict__ v,
                                                             const float *__restrict__ w,
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
       const float gy = -dyi * (sp[k % 2][y + 1][x] - P0);
       const float gz = -dzi * (sp[(k + 1) % 2][y][x] - P0);
       const int c = k * PL + j * g.I + i;
-      if (cb) rw_new = (float)(bcoef * (cb[c] + cb[c + PL])) + rw_new;  // momzbuoy
+      if constexpr (BUOY) rw_new = (float)(bcoef * (cb[c] + cb[c + PL])) + rw_new;  // momzbuoy
       float du = U0 + f1 * gx, dv = V0 + f1 * gy, dw = W0 + f1 * gz;
       if (STAGE == 1) {
         du = du + f1 * ru_new;
@@ -279,12 +283,16 @@ void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const 
     if (g.nfield < (1L << 31)) {
     dim3 grd((g.I + PTX - 1) / PTX, (g.J + PTY - 1) / PTY, (g.K + PKC - 1) / PKC);
     const float a = (float)f1, b = (float)f2, c = (float)f3;
-    if (stage == 1)
-      k_predict_tiled<1><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
-    else if (stage == 2)
-      k_predict_tiled<2><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
-    else
-      k_predict_tiled<3><<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
+    auto go = [&](auto kern) { kern<<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef); };
+    if (cb) {
+      if (stage == 1) go(k_predict_tiled<1, true>);
+      else if (stage == 2) go(k_predict_tiled<2, true>);
+      else go(k_predict_tiled<3, true>);
+    } else {
+      if (stage == 1) go(k_predict_tiled<1, false>);
+      else if (stage == 2) go(k_predict_tiled<2, false>);
+      else go(k_predict_tiled<3, false>);
+    }
     return;
     }
   }
