@@ -166,6 +166,8 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
 # dominant kernels from one ncu capture of the same command, for the roofline's
 # `traffic` key: {(form, kernel class): bytes}
 TRAFFIC = {
+    ("learned", "predict"): 283552512 + 355950080,  # k_predict_tiled<1>
+    ("mixed", "predict"): 283552512 + 355950080,
     ("learned", "correc"): 402452992 + 288781568,  # k_correc_mixed
     ("mixed", "correc"): 402452992 + 288781568,
     ("learned", "spread"): 238345472 + 39752192,   # k_ibm_spread_f (cold cache)
@@ -265,6 +267,14 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
         solver.rk3_step(dt)
     solver.sync()
     phases = solver.timed_step(dt)
+    # one untimed step with CUDA events around every kernel class: the kernel
+    # table, and the dominant class, the only one timed inside the timed steps
+    # (events around every class cost about 0.2 ms per step)
+    solver.probe()
+    solver.run(dt, 1)
+    kernels_all = solver.probe_result()
+    dom_class = max(kernels_all, key=lambda k: kernels_all[k][0])
+    mask = args.probe_mask if args.probe_mask >= 0 else 1 << solver.PROBE_NAMES.index(dom_class)
     torch.cuda.synchronize()
     launches0 = solver.launch_count()
     barrier(ws)
@@ -272,7 +282,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        solver.probe()  # CUDA events around every kernel launch of the timed steps
+        solver.probe(mask)  # CUDA events around every launch of the selected kernel classes
         with torch.cuda.stream(stream):
             torch.cuda.nvtx.range_push("timed")  # profilers select the timed steps by this range
             ev0.record(stream)
@@ -283,7 +293,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     torch.cuda.synchronize()
     barrier(ws)
     ms = ev0.elapsed_time(ev1) / args.steps
-    kernels = solver.probe_result()
+    kernels_timed = solver.probe_result()
     launches = solver.launch_count() - launches0
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
@@ -334,7 +344,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver.close()
     return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
             "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn,
-            "kernels": kernels, "stats": stats}
+            "kernels": kernels_all, "kernels_timed": kernels_timed, "stats": stats}
 
 
 def cpu_baseline(args, case_fn):
@@ -375,6 +385,9 @@ def main():
     ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--stats-calls", type=int, default=3, help="post1d calls timed after the steps (0: none)")
+    ap.add_argument("--probe-mask", type=int, default=-1,
+                    help="kernel classes timed with CUDA events inside the timed steps (bit per class; "
+                         "default: the dominant class of an untimed probed step)")
     ap.add_argument("--proj-solves", type=int, default=0,
                     help="FP32 Poisson solves per projection in the mixed forms (0: the library default)")
     args = ap.parse_args()
@@ -437,30 +450,36 @@ def main():
     unit_of = {"hbm": "GB/s", "tensor": "TFLOP/s", "fp64": "TFLOP/s"}
     w = 8 if head == "plain" else 4
 
-    def kernel_table(x, wb):
+    def kernel_table(x, wb, key="kernels", steps=1):
+        """Per kernel class: launches and mean duration (CUDA events), the
+        algorithmic bytes or flops per launch and the fraction of the peak.
+        key "kernels": the untimed probed step (every class); "kernels_timed":
+        the classes probed inside the timed steps."""
         model = kernel_model(x["case"], wb)
         out = {}
-        for name, (tot_ms, cnt) in x["kernels"].items():
+        for name, (tot_ms, cnt) in x[key].items():
             if cnt == 0:
                 continue
             bound, units = model[name]
             per = tot_ms / cnt
             ach = units / (per * 1e-3) / (1e9 if bound == "hbm" else 1e12)
             peak = peak_of[bound]
-            out[name] = {"launches_per_step": round(cnt / args.steps, 2), "ms_per_launch": round(per, 4),
-                         "share_of_step": round(tot_ms / args.steps / x["ms"], 4), "bound": bound,
+            out[name] = {"launches_per_step": round(cnt / steps, 2), "ms_per_launch": round(per, 4),
+                         "share_of_step": round(tot_ms / steps / x["ms"], 4), "bound": bound,
                          "algorithmic_per_launch": int(units), "achieved": round(ach, 3 if bound == "fp64" else 1),
                          "unit": unit_of[bound], "frac": round(ach / peak, 4)}
         return out
     ab = algorithmic_bytes(case, w)
     names = ["predictor", "ibm", "projection", "newton_euler"]
     ktab = kernel_table(r, w)
-    dom = max(ktab, key=lambda k: ktab[k]["share_of_step"])
-    dk = ktab[dom]
+    # the roofline kernel: the dominant class, timed inside the timed steps
+    ttab = kernel_table(r, w, "kernels_timed", args.steps)
+    dom = max(ttab, key=lambda k: ttab[k]["share_of_step"])
+    dk = ttab[dom]
     line = {
         "metric": METRIC, "value": round(r["ms"], 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(r["ms"], 4), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"plain": "f64", "mixed": "f32+f64", "learned": "f32+f64 (bf16 MLP)"}[head], "data": "synthetic",
+        "vs_baseline": None, "dtype": {"plain": "f64", "mixed": "f32+f64", "learned": "f32+f64 (bf16/f16 MLP)"}[head], "data": "synthetic",
         "config": config,
         "form": {"plain": "plain FP64 (drop-in)", "mixed": "mixed FP32/FP64",
                  "learned": "mixed FP32/FP64 + learned forcing"}[head],

@@ -423,12 +423,15 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   }
   // prefactors F coeff0 (F given) or (U - u~) dti coeff0, as FP32 products
   const float pcoef = (float)coeff0, ucoef = (float)(dti * coeff0);
-  // points in transposed order: the 32 lanes of a warp take points nq apart
-  // in the particle's list (neighbouring points have overlapping stencils)
+  // Taps into the box: points in transposed order, the 32 lanes of a warp
+  // taking points nq apart in the particle's list (neighbouring points have
+  // overlapping stencils, and shared-memory adds to one address in one
+  // instruction serialise).  Prefactors of staged points: natural order
+  // (coalesced loads of the point arrays).
   const int nq = (nla + 31) >> 5;
   float asum = 0.f;
   for (int m = threadIdx.x; m < 32 * nq; m += blockDim.x) {
-    const int l = (m & 31) * nq + (m >> 5);
+    const int l = staged ? m : (m & 31) * nq + (m >> 5);
     if (l >= nla) continue;
     const long t = t0 + l;
     float pre;
