@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(256) k_predict(Geo g, const TU *__restrict__ u
 // FP32 predictor with 2.5D blocking: a 32 x 8 column tile marches along z
 // through a chunk of planes, keeping the planes k-1, k, k+1 of u, v, w and
 // k, k+1 of p (with a one-cell x/y halo, periodic) in shared memory, so each
-// field is read from HBM about once.  Same expressions as k_predict.
+// field is read from HBM about once.  The terms of k_predict, regrouped (below).
 constexpr int PTX = 32, PTY = 8, PHX = PTX + 2, PHY = PTY + 2, PKC = 32;
 // BUOY: momzbuoy from the scalar field cb (FP64).  A separate instantiation
 // keeps the FP64 buoyancy instructions out of the kernel without a scalar:
@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
   commit(k0);
   fetch(k0 + 1);
   const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi, visc = (float)g.visc;
-  const float q = 0.25f;
+  const float qdxi = 0.25f * dxi, qdyi = 0.25f * dyi, qdzi = 0.25f * dzi;
+  const float vdx2 = visc * dxi * dxi, vdy2 = visc * dyi * dyi, vdz2 = visc * dzi * dzi;
   for (int k = k0; k <= k1; ++k) {
     commit(k + 1);  // slots of k-2 (u, v, w) and k-1 (p) are free
     __syncthreads();
@@ -205,45 +206,32 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
       const float Vipjm = sv[c0][y - 1][x + 1], Wipkm = sw[cm][y][x + 1];
       const float Uimjp = su[c0][y + 1][x - 1], Wjpkm = sw[cm][y + 1][x];
       const float Uimkp = su[cp][y][x - 1], Vjmkp = sv[cp][y - 1][x];
+      // momxad, momyad, momzad (mom.f90:21-50, 94-123, 170-199), the same
+      // terms regrouped for the FP32 pipes: each of the three mixed products
+      // that two equations share is formed once; q (a + b)^2 - q (c + d)^2
+      // as one FMA; the diffusion from neighbour differences, which are
+      // exact for neighbouring values within a factor of two.
+      const float Puv = (Ujp + U0) * (Vip + V0);  // momx uvjp, momy uvip
+      const float Puw = (Ukp + U0) * (Wip + W0);  // momx uwkp, momz uwip
+      const float Pvw = (Wjp + W0) * (Vkp + V0);  // momy wvkp, momz vwjp
       float ru_new, rv_new, rw_new;
-      {  // momxad (mom.f90:21-50)
-        const float uuip = q * (Uip + U0) * (Uip + U0);
-        const float uuim = q * (Uim + U0) * (Uim + U0);
-        const float uvjp = q * (Ujp + U0) * (Vip + V0);
-        const float uvjm = q * (Ujm + U0) * (Vipjm + Vjm);
-        const float uwkp = q * (Ukp + U0) * (Wip + W0);
-        const float uwkm = q * (Ukm + U0) * (Wipkm + Wkm);
-        const float dudxp = (Uip - U0) * dxi, dudxm = (U0 - Uim) * dxi;
-        const float dudyp = (Ujp - U0) * dyi, dudym = (U0 - Ujm) * dyi;
-        const float dudzp = (Ukp - U0) * dzi, dudzm = (U0 - Ukm) * dzi;
-        ru_new = dxi * (-uuip + uuim) + visc * (dudxp - dudxm) * dxi + dyi * (-uvjp + uvjm) +
-                 visc * (dudyp - dudym) * dyi + dzi * (-uwkp + uwkm) + visc * (dudzp - dudzm) * dzi;
+      {
+        const float sp_ = Uip + U0, sm_ = Uim + U0;
+        ru_new = qdxi * fmaf(sm_, sm_, -(sp_ * sp_)) + qdyi * ((Ujm + U0) * (Vipjm + Vjm) - Puv) +
+                 qdzi * ((Ukm + U0) * (Wipkm + Wkm) - Puw) + vdx2 * ((Uip - U0) - (U0 - Uim)) +
+                 vdy2 * ((Ujp - U0) - (U0 - Ujm)) + vdz2 * ((Ukp - U0) - (U0 - Ukm));
       }
-      {  // momyad (mom.f90:94-123)
-        const float uvip = q * (U0 + Ujp) * (V0 + Vip);
-        const float uvim = q * (Uim + Uimjp) * (V0 + Vim);
-        const float vvjp = q * (V0 + Vjp) * (V0 + Vjp);
-        const float vvjm = q * (V0 + Vjm) * (V0 + Vjm);
-        const float wvkp = q * (W0 + Wjp) * (Vkp + V0);
-        const float wvkm = q * (Wkm + Wjpkm) * (Vkm + V0);
-        const float dvdxp = (Vip - V0) * dxi, dvdxm = (V0 - Vim) * dxi;
-        const float dvdyp = (Vjp - V0) * dyi, dvdym = (V0 - Vjm) * dyi;
-        const float dvdzp = (Vkp - V0) * dzi, dvdzm = (V0 - Vkm) * dzi;
-        rv_new = dxi * (-uvip + uvim) + visc * (dvdxp - dvdxm) * dxi + dyi * (-vvjp + vvjm) +
-                 visc * (dvdyp - dvdym) * dyi + dzi * (-wvkp + wvkm) + visc * (dvdzp - dvdzm) * dzi;
+      {
+        const float sp_ = V0 + Vjp, sm_ = V0 + Vjm;
+        rv_new = qdxi * ((Uim + Uimjp) * (V0 + Vim) - Puv) + qdyi * fmaf(sm_, sm_, -(sp_ * sp_)) +
+                 qdzi * ((Wkm + Wjpkm) * (Vkm + V0) - Pvw) + vdx2 * ((Vip - V0) - (V0 - Vim)) +
+                 vdy2 * ((Vjp - V0) - (V0 - Vjm)) + vdz2 * ((Vkp - V0) - (V0 - Vkm));
       }
-      {  // momzad (mom.f90:170-199)
-        const float uwip = q * (W0 + Wip) * (U0 + Ukp);
-        const float uwim = q * (W0 + Wim) * (Uim + Uimkp);
-        const float vwjp = q * (W0 + Wjp) * (V0 + Vkp);
-        const float vwjm = q * (W0 + Wjm) * (Vjm + Vjmkp);
-        const float wwkp = q * (W0 + Wkp) * (W0 + Wkp);
-        const float wwkm = q * (W0 + Wkm) * (W0 + Wkm);
-        const float dwdxp = (Wip - W0) * dxi, dwdxm = (W0 - Wim) * dxi;
-        const float dwdyp = (Wjp - W0) * dyi, dwdym = (W0 - Wjm) * dyi;
-        const float dwdzp = (Wkp - W0) * dzi, dwdzm = (W0 - Wkm) * dzi;
-        rw_new = dxi * (-uwip + uwim) + visc * (dwdxp - dwdxm) * dxi + dyi * (-vwjp + vwjm) +
-                 visc * (dwdyp - dwdym) * dyi + dzi * (-wwkp + wwkm) + visc * (dwdzp - dwdzm) * dzi;
+      {
+        const float sp_ = W0 + Wkp, sm_ = W0 + Wkm;
+        rw_new = qdxi * ((W0 + Wim) * (Uim + Uimkp) - Puw) + qdyi * ((W0 + Wjm) * (Vjm + Vjmkp) - Pvw) +
+                 qdzi * fmaf(sm_, sm_, -(sp_ * sp_)) + vdx2 * ((Wip - W0) - (W0 - Wim)) +
+                 vdy2 * ((Wjp - W0) - (W0 - Wjm)) + vdz2 * ((Wkp - W0) - (W0 - Wkm));
       }
       // pressure gradient (momxp/momyp/momzp)
       const float P0 = sp[k % 2][y][x];
