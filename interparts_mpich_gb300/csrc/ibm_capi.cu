@@ -498,20 +498,38 @@ int predict(ibm_ctx *c, int rkiter, double dt) {
 }
 
 int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
-  // one sweep plus one inference: the first pass's interpolation and point
-  // forces F0 together with the network features (one kernel), the
-  // network's correction, one spreading of F0 + correction; then the plain
-  // passes 2..Nl only where the no-slip residual exceeds fallback_ratio x
-  // the plain method's
+  // one sweep plus one inference: the first pass's interpolation, the point
+  // forces F0 and the network features formed in the inference kernel's
+  // operand tiles, the network's correction (one kernel); one spreading of
+  // F0 + correction; then the plain passes 2..Nl only where the no-slip
+  // residual exceeds fallback_ratio x the plain method's
   const Geo &g = c->g;
   const long npts = (long)c->pg.np * c->pg.nl;
   PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
-  PROBED(IBM_PROBE_FEATURES, launch_ibm_features_comp(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt,
-                                                      c->norm, c->norm + 96, c->lx));
+  LAUNCHED(2);
+  FeatIn fi;
+  fi.g = g;
+  fi.np = c->pg.np;
+  fi.nl = c->pg.nl;
+  fi.nla = c->ib.nla;
+  fi.cs = c->ib.cs;
+  fi.F[0] = c->fu32; fi.F[1] = c->fv32; fi.F[2] = c->fw32;
+  fi.U[0] = c->ib.ul; fi.U[1] = c->ib.vl; fi.U[2] = c->ib.wl;
+  fi.X[0] = c->ib.xfp; fi.X[1] = c->ib.yfp; fi.X[2] = c->ib.zfp;
+  fi.pf = c->pb.pf;
+  fi.dud[0] = c->ib.dudtl; fi.dud[1] = c->ib.dvdtl; fi.dud[2] = c->ib.dwdtl;
+  fi.Fl[0] = c->ib.fxl; fi.Fl[1] = c->ib.fyl; fi.Fl[2] = c->ib.fzl;
+  fi.dt = dt;
+  fi.dti = 1. / dt;
+  fi.inv_r = (float)(1. / c->pg.radfp);
+  fi.mu = c->norm;
+  fi.isig = c->norm + 96;
+  PROBED(IBM_PROBE_MLP, c->launches += launch_mlp_features_tc(c->stream, fi, c->mt.w1b, c->mt.params, c->ly,
+                                                              c->pb.err + 4));
+  // the top plane of fw carries only the spread force (read above by the
+  // w features, zeroed before the spreading)
   launch_zero_plane<float>(c->stream, g, c->fw32, g.K + 1);
-  LAUNCHED(4);
-  PROBED(IBM_PROBE_MLP, launch_mlp_infer_tc(c->stream, c->lx, (int)npts, c->mt.w1b, c->mt.w2b, c->mt.params, c->ly,
-                                            c->pb.err + 4));
+  LAUNCHED(1);
   // F = F0 + the network's correction per point, its force and torque sums,
   // one spreading
   const LearnedForce lf{c->ly, c->norm + 192, c->norm + 195, 1. / dt};
@@ -520,7 +538,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
                                                                          c->fv32, c->fw32, dt, -1));
   launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 0);
-  LAUNCHED(5);
+  LAUNCHED(4);  // spreading, force sums, residual interpolation, gate
   for (int it = 1; it < nl_iter; ++it) {
     PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
                                                                            c->fv32, c->fw32, dt, 0, c->gate));

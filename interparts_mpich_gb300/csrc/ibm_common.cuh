@@ -53,6 +53,16 @@ struct __align__(16) CompStencil {
   int b[3];
   float w[9];
 };
+// one 48-byte record as three 16-byte loads
+__device__ __forceinline__ CompStencil load_cs(const CompStencil *p) {
+  const float4 *q = reinterpret_cast<const float4 *>(p);
+  const float4 a = q[0], bb = q[1], c = q[2];
+  CompStencil s;
+  s.b[0] = __float_as_int(a.x); s.b[1] = __float_as_int(a.y); s.b[2] = __float_as_int(a.z);
+  s.w[0] = a.w; s.w[1] = bb.x; s.w[2] = bb.y; s.w[3] = bb.z; s.w[4] = bb.w;
+  s.w[5] = c.x; s.w[6] = c.y; s.w[7] = c.z; s.w[8] = c.w;
+  return s;
+}
 
 // Constants of one context, passed by value to the kernels.
 struct Geo {

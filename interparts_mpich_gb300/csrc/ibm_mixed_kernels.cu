@@ -172,15 +172,6 @@ __device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__
     box[q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
   }
 }
-__device__ __forceinline__ CompStencil load_cs(const CompStencil *p) {
-  const float4 *q = reinterpret_cast<const float4 *>(p);
-  const float4 a = q[0], bb = q[1], c = q[2];
-  CompStencil s;
-  s.b[0] = __float_as_int(a.x); s.b[1] = __float_as_int(a.y); s.b[2] = __float_as_int(a.z);
-  s.w[0] = a.w; s.w[1] = bb.x; s.w[2] = bb.y; s.w[3] = bb.z; s.w[4] = bb.w;
-  s.w[5] = c.x; s.w[6] = c.y; s.w[7] = c.z; s.w[8] = c.w;
-  return s;
-}
 // 27-tap interpolation of one component, k outer, j, i inner, each term
 // f * (wx_i * (wy_j * wz_k))
 template <typename TAP>

@@ -153,6 +153,26 @@ void launch_mlp_infer(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_
                       const __nv_bfloat16 *w2b, const float *params, float *y);
 int launch_mlp_infer_tc(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
                         const __nv_bfloat16 *w2b, const float *params, float *y, int *err);
+// Inputs of the fused feature + inference kernel of the learned loop: the
+// first pass's interpolation (to dudtl), point forces F0 (to fxl) and the 96
+// standardised features of every point are formed in the tile's operand
+// region, the same values the feature kernel writes to HBM.
+struct FeatIn {
+  Geo g;
+  int np, nl;
+  const int *nla;
+  const CompStencil *cs;
+  const float *F[3];   // u, v, w (FP32 fields)
+  const double *U[3];  // rigid-body velocity at the points
+  const double *X[3];  // point coordinates
+  const double *pf;    // particle scalar fields (centres)
+  double *dud[3], *Fl[3];
+  double dt, dti;
+  float inv_r;
+  const float *mu, *isig;  // feature standardisation
+};
+int launch_mlp_features_tc(cudaStream_t s, const FeatIn &fi, const __nv_bfloat16 *w1b, const float *params,
+                           float *y, int *err);
 void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr);
 void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb);
 void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,

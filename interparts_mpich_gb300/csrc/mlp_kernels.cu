@@ -507,11 +507,73 @@ __device__ __forceinline__ void gelu2_store32(const float v[32], const uint32_t 
   }
 }
 
+// The 96 features of point t (see k_ibm_features_comp: the 27 taps minus U,
+// U - u~, U, the normal component, F0 dt and the centre weight of each
+// velocity component, standardised and rounded to BF16) into row r of the
+// K-major operand tile, with the first pass's interpolation to dudtl and
+// F0 = (U - u~)/dt to fxl.  Taps are read from the fields directly (the
+// 3-float rows of a stencil share cache lines with the tile's neighbouring
+// points).  Rows beyond the points, or points not active (l >= nla), get
+// zero features.
+__device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned char *A, int r) {
+  const long npl = (long)fi.np * fi.nl;
+  const int p = t < npl ? (int)(t / fi.nl) : 0;
+  if (t >= npl || (int)(t - (long)p * fi.nl) >= fi.nla[p]) {
+#pragma unroll
+    for (int c8 = 0; c8 < NIN; c8 += 8) *reinterpret_cast<uint4 *>(A + kmaj_off(r, c8, NIN)) = make_uint4(0, 0, 0, 0);
+    return;
+  }
+  const Geo &g = fi.g;
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    const CompStencil s = load_cs(fi.cs + c * npl + t);
+    const float *F = fi.F[c];
+    const double Ud = fi.U[c][t];
+    const float Uc = (float)Ud;
+    float f[FEAT_PER_COMP];
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float wyz = s.w[3 + j] * s.w[6 + k];
+        const int y = wrapm(s.b[1] + j, g.J);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float tv = __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), y, s.b[2] + k)]);
+          acc += tv * (s.w[i] * wyz);
+          f[(k * 3 + j) * 3 + i] = tv - Uc;
+        }
+      }
+    fi.dud[c][t] = acc;
+    const double F0 = (Ud - acc) * fi.dti;
+    fi.Fl[c][t] = F0;
+    f[27] = Uc - acc;
+    f[28] = Uc;
+    f[29] = (float)(fi.X[c][t] - fi.pf[(c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z)) * fi.np + p]) * fi.inv_r;
+    f[30] = (float)F0 * (float)fi.dt;
+    f[31] = s.w[3 * c + 1];
+    const float *mu = fi.mu + FEAT_PER_COMP * c, *is = fi.isig + FEAT_PER_COMP * c;
+#pragma unroll
+    for (int q = 0; q < FEAT_PER_COMP; q += 8) {
+      uint32_t pk[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        __nv_bfloat162 h = __floats2bfloat162_rn((f[q + 2 * e] - __ldg(&mu[q + 2 * e])) * __ldg(&is[q + 2 * e]),
+                                                 (f[q + 2 * e + 1] - __ldg(&mu[q + 2 * e + 1])) * __ldg(&is[q + 2 * e + 1]));
+        pk[e] = *reinterpret_cast<uint32_t *>(&h);
+      }
+      *reinterpret_cast<uint4 *>(A + kmaj_off(r, FEAT_PER_COMP * c + q, NIN)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+
+template <bool FUSED>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__restrict__ x, int n,
                                                                 const bf16 *__restrict__ w1b,
-                                                                const bf16 *__restrict__ w2b,
                                                                 const float *__restrict__ params,
-                                                                float *__restrict__ y, int *__restrict__ err) {
+                                                                float *__restrict__ y, int *__restrict__ err,
+                                                                const FeatIn fi) {
   extern __shared__ __align__(16) unsigned char tc_sm[];
   unsigned char *W1c = tc_sm;                                 // [128 x 96]  K-major
   unsigned char *W2c = W1c + NH * NIN * 2;                    // [128 x 128]
@@ -586,13 +648,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
   };
   for (int tile = blockIdx.x * TC_GROUPS + g; tile < ntiles; tile += gridDim.x * TC_GROUPS) {
     const long row0 = (long)tile * TC_M;
-    // X tile (zero rows beyond n) by asynchronous 16-byte copies
-    for (int q = gt; q < TC_M * NIN / 8; q += 128) {
-      const int rr = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
-      const bool valid = row0 + rr < n;
-      cp_async16(A + kmaj_off(rr, c8, NIN), valid ? &x[(row0 + rr) * NIN + c8] : x, valid);
+    if constexpr (FUSED) {
+      feature_row(fi, row0 + gt, A, gt);  // this thread's row of the X tile
+    } else {
+      // X tile (zero rows beyond n) by asynchronous 16-byte copies
+      for (int q = gt; q < TC_M * NIN / 8; q += 128) {
+        const int rr = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+        const bool valid = row0 + rr < n;
+        cp_async16(A + kmaj_off(rr, c8, NIN), valid ? &x[(row0 + rr) * NIN + c8] : x, valid);
+      }
+      asm volatile("cp.async.wait_all;\n" ::: "memory");
     }
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
     fence_async_smem();
     group_sync(g);
     if (gt == 0) {  // layer 1
@@ -662,11 +728,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const bf16 *__re
 }
 int launch_mlp_infer_tc(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, const bf16 *w2b, const float *params,
                         float *y, int *err) {
+  (void)w2b;  // layers 2 and 3 take F16 copies of the FP32 weights in params
   if (n <= 0) return 0;
   const int ntiles = (n + TC_M - 1) / TC_M;
   const int nblk = (ntiles + TC_GROUPS - 1) / TC_GROUPS;
   const int grid = nblk < 152 ? nblk : 152;
-  k_mlp_infer_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(x, n, w1b, w2b, params, y, err);
+  k_mlp_infer_tc<false><<<grid, TC_THREADS, TC_SMEM, s>>>(x, n, w1b, params, y, err, FeatIn{});
+  return 1;
+}
+int launch_mlp_features_tc(cudaStream_t s, const FeatIn &fi, const bf16 *w1b, const float *params, float *y,
+                           int *err) {
+  const long n = (long)fi.np * fi.nl;
+  if (n <= 0) return 0;
+  const int ntiles = (int)((n + TC_M - 1) / TC_M);
+  const int nblk = (ntiles + TC_GROUPS - 1) / TC_GROUPS;
+  const int grid = nblk < 152 ? nblk : 152;
+  k_mlp_infer_tc<true><<<grid, TC_THREADS, TC_SMEM, s>>>(nullptr, (int)n, w1b, params, y, err, fi);
   return 1;
 }
 
@@ -961,7 +1038,9 @@ int mlp_set_smem_limits() {
   cudaError_t e3 = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)mlp_backward_smem());
   cudaError_t e4 = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_infer_smem());
-  cudaError_t e5 = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+  cudaError_t e5 = cudaFuncSetAttribute(k_mlp_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+  if (e5 == cudaSuccess)
+    e5 = cudaFuncSetAttribute(k_mlp_infer_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
   return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && e5 == cudaSuccess)
              ? 0
              : -1;
