@@ -172,7 +172,7 @@ TRAFFIC = {
     ("mixed", "correc"): 402452992 + 288781568,
     ("learned", "spread"): 238345472 + 39752192,   # k_ibm_spread_f (cold cache)
     ("mixed", "spread"): 238345472 + 39752192,
-    ("learned", "mlp"): 143344640 + 7269376,       # k_mlp_infer_tc
+    ("learned", "mlp"): 280366848 + 35936000,      # k_mlp_infer_tc<true> (features formed in the kernel)
 }
 
 
