@@ -343,11 +343,12 @@ int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, I
 // The box holds 32-bit fixed-point sums: a first pass computes every point's
 // prefactor F*coeff0 into shared memory and their absolute sum B, which
 // bounds every cell's sum (the 27 delta weights of a point are non-negative
-// and sum to one); with the scale 2^s, B * 2^s < 2^30, each tap adds
+// and sum to one); with the scale 2^s, B * 2^s < 2^29, each tap adds
 // rint(2^s * prefactor * weight) with a native integer shared-memory add
 // (no compare-and-swap loop, no wait on its result), and the sums are exact
-// and independent of the order of the adds.  The resolution is B / 2^30 per
-// tap, below the FP32 rounding of the sums it replaces.  Particles with
+// and independent of the order of the adds.  The resolution, at most
+// B / 2^28 per tap, is of the order of the FP32 rounding of the cell sums
+// it replaces (B is a few hundred times the largest prefactor).  Particles with
 // more than SPREAD_PRE points, or a bound that is zero or not finite, add
 // FP32 values into the box instead; boxes beyond SPREAD_BOX cells add per
 // tap to the field.
