@@ -69,7 +69,6 @@ struct ibm_ctx {
   MlpTrainBuffers mt{};        // model (params, Adam moments, BF16 copies) + training batch buffers
   int mt_cap = 0;              // batch capacity of mt
   float *norm = nullptr;       // [198]: feature mean, 1/sigma; target mean, sigma
-  __nv_bfloat16 *lx = nullptr; // [np*nl][96] standardised features
   float *ly = nullptr;         // [np*nl][3] network output
   double *ls = nullptr;        // learn state, see k_ibm_res_gate
   int *gate = nullptr;
@@ -445,7 +444,6 @@ int alloc_all(ibm_ctx *c) {
     CK(cudaStreamSynchronize(c->stream));
     if (np > 0) {
       const size_t npl = (size_t)np * nl;
-      if ((st = dalloc(c, &c->lx, npl * 96))) return st;
       if ((st = dalloc(c, &c->ly, npl * 3))) return st;
     }
   }
@@ -806,7 +804,7 @@ int ibm_destroy(ibm_ctx *c) {
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
-                   c->norm, c->ls, c->gate, c->lx, c->ly, c->hv.feat, c->hv.pidx, c->hv.targ,
+                   c->norm, c->ls, c->gate, c->ly, c->hv.feat, c->hv.pidx, c->hv.targ,
                    c->hv.count, c->tx, c->tt};
   for (void *q : lptrs)
     if (q) cudaFree(q);
