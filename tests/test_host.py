@@ -73,3 +73,22 @@ def test_oracle_error_codes():
     o = OracleSolver(c)
     with pytest.raises(IBMError):
         o.rk(4, 1e-3)
+
+
+def test_bench_kernel_model_covers_probe_classes():
+    """Every kernel class the library times inside a step has an algorithmic model in the bench
+    (bytes or flops per launch), and every recorded ncu traffic entry names a modelled class."""
+    import bench
+    from interparts_mpich_gb300.cases import channel_case
+    from interparts_mpich_gb300.solver import IBMSolver
+    case = channel_case()
+    for w in (4, 8):
+        model = bench.kernel_model(case, w)
+        for name in IBMSolver.PROBE_NAMES:
+            if name in ("phase", "stats"):  # post1d classes, timed by statistics_timing
+                continue
+            assert name in model, name
+            bound, units = model[name]
+            assert bound in ("hbm", "tensor", "fp64") and units > 0
+    for form, name in bench.TRAFFIC:
+        assert form in ("mixed", "learned", "plain") and name in bench.kernel_model(case, 4)
