@@ -289,19 +289,21 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
 // [1] sum and [2] count of the plain passes' rms, [3] fallback ratio,
 // [4] fallbacks, [5] learned substeps; gate = 1 runs the plain passes after
 // the inference.
-__global__ void __launch_bounds__(256) k_ibm_res_gate(int n, const double *__restrict__ psum, long npts, double *ls,
-                                                      int *gate, int plain) {
-  __shared__ double sm[256];
-  double acc = 0.;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) acc += psum[3 * (long)q];
-  sm[threadIdx.x] = acc;
+__global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__restrict__ psum, long npts, double *ls,
+                                                       int *gate, int plain) {
+  // the per-particle residual sums are FP32-accurate (formed in FP32); their
+  // total in FP32 with warp shuffles, FP64 only for the gate's arithmetic
+  __shared__ float sm[32];
+  float acc = 0.f;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) acc += (float)psum[3 * (long)q];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
   __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
-    __syncthreads();
-  }
   if (threadIdx.x != 0) return;
-  const double rms = npts ? sqrt(sm[0] / (double)npts) : 0.;
+  double tot = 0.;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += sm[w];
+  const double rms = npts ? sqrt(tot / (double)npts) : 0.;
   if (plain) {  // residual of the plain passes: the reference the learned one is held to
     ls[1] += rms;
     ls[2] += 1.;
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(256) k_ibm_res_gate(int n, const double *__res
 }
 void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
                               int plain) {
-  k_ibm_res_gate<<<1, 256, 0, s>>>(3 * pg.np, b.psum, npts, ls, gate, plain);
+  k_ibm_res_gate<<<1, 1024, 0, s>>>(3 * pg.np, b.psum, npts, ls, gate, plain);
 }
 
 }  // namespace ibmk
