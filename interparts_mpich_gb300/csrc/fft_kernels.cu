@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(128) k_thomas_df(Geo g, float2 *__restrict__ S
   const long sstride = (long)g.J * g.MX;
   float2 *s = S + t;
   const int K = g.K;
-  constexpr int PF = 8;
+  constexpr int PF = 16;
   // previous plane's value, real and imaginary parts, double-float
   float prh = 0.f, prl = 0.f, pih = 0.f, pil = 0.f;
   // Both sweeps run over chunks of PF planes with the next chunk's loads
