@@ -375,11 +375,17 @@ __global__ void __launch_bounds__(256) k_ffty_r(Geo g, float2 *__restrict__ S, c
   float2 *EX = A + COLS * LD;                   // [COLS][N1*(N2+1)]
   const int kx0 = blockIdx.x * COLS;
   float2 *plane = S + (long)blockIdx.y * J * g.MX;
+  // the block's columns straight into shared memory by asynchronous 8-byte
+  // copies (all of a thread's loads in flight together; zero fill beyond MX)
   for (int q = threadIdx.x; q < J * COLS; q += blockDim.x) {
     const int jy = q / COLS, cx = q - jy * COLS;
     const int kx = kx0 + cx;
-    A[cx * LD + jy] = (kx < g.MX) ? plane[(long)jy * g.MX + kx] : make_float2(0.f, 0.f);
+    const bool ok = kx < g.MX;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&A[cx * LD + jy]);
+    const float2 *src = ok ? &plane[(long)jy * g.MX + kx] : plane;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0));
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
   const int grp = threadIdx.x / N2, t = threadIdx.x - grp * N2;
   fft_group<N1, N2>(A + grp * LD, EX + grp * N1 * (N2 + 1), t, twJ, inv, kx0 + grp < g.MX);
