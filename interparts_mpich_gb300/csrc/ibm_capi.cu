@@ -693,13 +693,15 @@ int newton_euler(ibm_ctx *c, int rkiter, double dt) {
   launch_save_old(c->stream, c->pg, c->pb);
   LAUNCHED(1);
   probe_mark(c, IBM_PROBE_SPHERE);
-  if (c->mixed) launch_sphere_integrals<float>(c->stream, c->g, c->pg, c->pb, c->u32, c->v32, c->w32, 23);
-  else launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23);
+  // the sphere integrals' final kernel also takes the first collision
+  // iteration's snapshot
+  if (c->mixed) launch_sphere_integrals<float>(c->stream, c->g, c->pg, c->pb, c->u32, c->v32, c->w32, 23, true);
+  else launch_sphere_integrals<double>(c->stream, c->g, c->pg, c->pb, c->u, c->v, c->w, 23, true);
   probe_mark(c, IBM_PROBE_SPHERE);
   LAUNCHED(1);
   for (int iter = 0; iter <= 1; ++iter) {
-    launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt);
-    LAUNCHED(2);
+    launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt, iter > 0);
+    LAUNCHED(iter > 0 ? 2 : 1);
   }
   launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 0);
   LAUNCHED(1);

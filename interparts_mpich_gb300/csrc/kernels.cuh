@@ -198,9 +198,12 @@ struct PartBuffers {
 };
 template <typename T>
 void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,
-                             const T *w, int type);
+                             const T *w, int type, bool snapshot = false);
 void launch_save_old(cudaStream_t s, const PartGeo &pg, PartBuffers b);
-void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt);
+// snapshot: take the iteration's snapshot first (false when the sphere
+// integrals' final kernel took it)
+void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt,
+                           bool snapshot = true);
 void launch_ne_finalize(cudaStream_t s, const PartGeo &pg, PartBuffers b, IbmBuffers ib, int init_flags);
 
 

@@ -402,11 +402,15 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
 }
 
 // unit field for the volume sums (type 1)
+__device__ __forceinline__ void snapshot_particle(const PartGeo &pg, PartBuffers &b, int p);
+// snap: also take the collision iteration's snapshot of this particle (the
+// positions and velocities the integrals leave unchanged), saving its launch
 template <typename T>
-__global__ void k_sphere_final(PartGeo pg, PartBuffers b, int type) {
+__global__ void k_sphere_final(PartGeo pg, PartBuffers b, int type, int snap) {
   const int np = pg.np;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= np) return;
+  if (snap) snapshot_particle(pg, b, p);
   const int ms = b.mslv[p];
   if (ms == 0) return;
   const double dV = pg.dVeul;
@@ -425,7 +429,7 @@ __global__ void k_sphere_final(PartGeo pg, PartBuffers b, int type) {
 
 template <typename T>
 void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,
-                             const T *w, int type) {
+                             const T *w, int type, bool snapshot) {
   if (pg.np == 0) return;
   const dim3 grid(pg.np, 3);
   const bool unit = type == 1;  // volume: integrate w = 1 (F == nullptr)
@@ -433,12 +437,12 @@ void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, Pa
     k_sphere_int<T, true><<<grid, 256, 0, s>>>(g, pg, b, unit ? nullptr : u, unit ? nullptr : v, unit ? nullptr : w);
   else
     k_sphere_int<T, false><<<grid, 256, 0, s>>>(g, pg, b, unit ? nullptr : u, unit ? nullptr : v, unit ? nullptr : w);
-  k_sphere_final<T><<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, type);
+  k_sphere_final<T><<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, type, snapshot ? 1 : 0);
 }
 template void launch_sphere_integrals<double>(cudaStream_t, const Geo &, const PartGeo &, PartBuffers,
-                                              const double *, const double *, const double *, int);
+                                              const double *, const double *, const double *, int, bool);
 template void launch_sphere_integrals<float>(cudaStream_t, const Geo &, const PartGeo &, PartBuffers, const float *,
-                                             const float *, const float *, int);
+                                             const float *, const float *, int, bool);
 
 // ---------------------------------------------------------------------------
 // collisions / lubrication (collisions.f90).  Only the normal contact force
@@ -604,16 +608,18 @@ __device__ __forceinline__ double minimg(double a0, double a1, double a2) {
 #define COLL_CAP 64
 
 // snapshot of the collision iteration (anb(:,0), intgr_nwtn_eulr.f90:153-206)
-__global__ void k_snapshot(PartGeo pg, PartBuffers b) {
+__device__ __forceinline__ void snapshot_particle(const PartGeo &pg, PartBuffers &b, int p) {
   const int np = pg.np;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
   const bool m = b.mslv[p] > 0;
   PF(PF_SX) = m ? PF(PF_X) : 0.; PF(PF_SY) = m ? PF(PF_Y) : 0.; PF(PF_SZ) = m ? PF(PF_Z) : 0.;
   PF(PF_SU) = m ? PF(PF_U) : 0.; PF(PF_SV) = m ? PF(PF_V) : 0.; PF(PF_SW) = m ? PF(PF_W) : 0.;
   PF(PF_SOMX) = m ? PF(PF_OMX) : 0.; PF(PF_SOMY) = m ? PF(PF_OMY) : 0.; PF(PF_SOMZ) = m ? PF(PF_OMZ) : 0.;
   // FP32 copy of the snapshot positions for the candidate filter (w: master flag)
   b.pos4[p] = make_float4((float)PF(PF_SX), (float)PF(PF_SY), (float)PF(PF_SZ), m ? 1.f : 0.f);
+}
+__global__ void k_snapshot(PartGeo pg, PartBuffers b) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < pg.np) snapshot_particle(pg, b, p);
 }
 
 // One warp per particle: a coarse FP32 periodic-distance filter selects the
@@ -865,9 +871,10 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   r[RK_DWDT] = r[RK_DWDT] + (nw - ow) / dt;
 }
 
-void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt) {
+void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt,
+                           bool snapshot) {
   if (pg.np == 0) return;
-  k_snapshot<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b);
+  if (snapshot) k_snapshot<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b);
   k_collide_update<<<(pg.np + COLL_WARPS - 1) / COLL_WARPS, 32 * COLL_WARPS, 0, s>>>(pg, b, iter, rkiter, dt);
 }
 
