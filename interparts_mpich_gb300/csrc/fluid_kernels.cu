@@ -535,9 +535,75 @@ void launch_correc_mixed2(cudaStream_t s, const Geo &g, const float *fu, const f
   k_correc_mixed2<<<grd, blk, 0, s>>>(g, fu, fv, fw, phi1, phi2, u, v, w, ph, pl, (float)fi, (float)fj, (float)fk);
 }
 
+// The same update four x-cells per thread with 16-byte loads and stores
+// (I a multiple of 4): identical arithmetic per cell, a quarter of the
+// memory instructions.
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__global__ void __launch_bounds__(256) k_correc_mixed4(Geo g, const float *fu, const float *fv, const float *fw,
+                                                       const float *__restrict__ phi, float *u, float *v, float *w,
+                                                       float *__restrict__ ph, float *__restrict__ pl, float fi,
+                                                       float fj, float fk) {
+  const int i0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z + 1;
+  if (i0 >= g.I || j >= g.J) return;
+  const int jp = j + 1 == g.J ? 0 : j + 1;
+  const long PL = g.plane;
+  const long c = fidx(g, i0, j, k);
+  const float4 P0 = ld4(phi + c);
+  const float P4 = phi[fidx(g, i0 + 4 == g.I ? 0 : i0 + 4, j, k)];
+  const float4 Pjp = ld4(phi + fidx(g, i0, jp, k));
+  const float4 Pkp = (k == g.K) ? P0 : ld4(phi + c + PL);
+  const float4 FU = ld4(fu + c), FV = ld4(fv + c);
+  const float4 FW = (k == g.K) ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(fw + c);
+  const float p0[4] = {P0.x, P0.y, P0.z, P0.w}, pip[4] = {P0.y, P0.z, P0.w, P4};
+  const float pjp[4] = {Pjp.x, Pjp.y, Pjp.z, Pjp.w}, pkp[4] = {Pkp.x, Pkp.y, Pkp.z, Pkp.w};
+  const float fu4[4] = {FU.x, FU.y, FU.z, FU.w}, fv4[4] = {FV.x, FV.y, FV.z, FV.w}, fw4[4] = {FW.x, FW.y, FW.z, FW.w};
+  const float4 H = ld4(ph + c), Lo = ld4(pl + c);
+  const float h4[4] = {H.x, H.y, H.z, H.w}, l4[4] = {Lo.x, Lo.y, Lo.z, Lo.w};
+  float un[4], vn[4], wn[4], sh[4], sl[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    un[e] = fu4[e] - fi * (pip[e] - p0[e]);
+    vn[e] = fv4[e] - fj * (pjp[e] - p0[e]);
+    wn[e] = (k == g.K) ? 0.f : fw4[e] - fk * (pkp[e] - p0[e]);
+    df_add(h4[e], l4[e], p0[e], 0.f, sh[e], sl[e]);
+  }
+  const float4 U = make_float4(un[0], un[1], un[2], un[3]), V = make_float4(vn[0], vn[1], vn[2], vn[3]);
+  const float4 W = make_float4(wn[0], wn[1], wn[2], wn[3]);
+  const float4 SH = make_float4(sh[0], sh[1], sh[2], sh[3]), SL = make_float4(sl[0], sl[1], sl[2], sl[3]);
+  st4(u + c, U);
+  st4(v + c, V);
+  st4(w + c, W);
+  st4(ph + c, SH);
+  st4(pl + c, SL);
+  if (k == g.K) {
+    const float sg = g.bc_top == IBM_BC_NOSLIP ? -1.f : 1.f;
+    st4(u + c + PL, make_float4(sg * un[0], sg * un[1], sg * un[2], sg * un[3]));
+    st4(v + c + PL, make_float4(sg * vn[0], sg * vn[1], sg * vn[2], sg * vn[3]));
+    st4(ph + c + PL, SH);
+    st4(pl + c + PL, SL);
+  }
+  if (k == 1) {
+    const float sg = g.bc_bot == IBM_BC_NOSLIP ? -1.f : 1.f;
+    st4(u + c - PL, make_float4(sg * un[0], sg * un[1], sg * un[2], sg * un[3]));
+    st4(v + c - PL, make_float4(sg * vn[0], sg * vn[1], sg * vn[2], sg * vn[3]));
+    st4(w + c - PL, make_float4(0.f, 0.f, 0.f, 0.f));
+    st4(ph + c - PL, SH);
+    st4(pl + c - PL, SL);
+  }
+}
+
 void launch_correc_mixed(cudaStream_t s, const Geo &g, const float *fu, const float *fv, const float *fw,
                          const float *phi, float *u, float *v, float *w, float *ph, float *pl, double fi, double fj,
                          double fk) {
+  if ((g.I & 3) == 0) {
+    dim3 blk(64, 4, 1);
+    dim3 grd((g.I / 4 + 63) / 64, (g.J + 3) / 4, g.K);
+    k_correc_mixed4<<<grd, blk, 0, s>>>(g, fu, fv, fw, phi, u, v, w, ph, pl, (float)fi, (float)fj, (float)fk);
+    return;
+  }
   dim3 blk(64, 4, 1);
   dim3 grd((g.I + 63) / 64, (g.J + 3) / 4, g.K);
   k_correc_mixed<<<grd, blk, 0, s>>>(g, fu, fv, fw, phi, u, v, w, ph, pl, (float)fi, (float)fj, (float)fk);
