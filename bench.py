@@ -250,19 +250,24 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     learn = None
     nwarm = args.warmup
     if mode == IBM_MODE_MIXED_LEARNED:
-        # first warm-up step: plain passes with harvesting; then GPU training
-        solver.harvest(capacity=args.harvest, stride=1, passes=args.harvest_passes)
-        solver.rk3_step(dt)
+        # the first warm-up steps: plain passes with harvesting (every
+        # stride-th point, so that the samples span all of them); then GPU
+        # training
+        hs = max(1, args.harvest_steps)
+        stride = max(1, -(-hs * 3 * case.np * case.nl // args.harvest))
+        solver.harvest(capacity=args.harvest, stride=stride, passes=args.harvest_passes)
+        for _ in range(hs):
+            solver.rk3_step(dt)
         solver.harvest(0)
         solver.sync()
         t0 = time.perf_counter()
         loss = solver.train_forcing_model(args.train_steps, batch=args.batch, lr=1e-3, seed=1)
         train_s = time.perf_counter() - t0
         st = solver.learned_stats()
-        learn = {"harvested_samples": int(st["harvested"]), "train_steps": args.train_steps, "batch": args.batch,
-                 "adam_lr": 1e-3, "train_s": round(train_s, 3), "final_loss_std_units": round(loss, 5),
-                 "plain_rms_residual": st["plain_rms_ref"]}
-        nwarm -= 1
+        learn = {"harvested_samples": int(st["harvested"]), "harvest_steps": hs, "harvest_stride": stride,
+                 "harvest_passes": args.harvest_passes, "train_steps": args.train_steps, "batch": args.batch,
+                 "adam_lr": 1e-3, "train_s": round(train_s, 3), "final_loss_std_units": round(loss, 5)}
+        nwarm = max(1, nwarm - hs)
     for _ in range(nwarm):
         solver.rk3_step(dt)
     solver.sync()
@@ -301,9 +306,14 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     stats = statistics_timing(solver, case, args.stats_calls) if args.stats_calls > 0 else None
     if learn is not None:
         st = solver.learned_stats()
-        learn.update({"learned_rms_residual_last": st["last_rms"], "fallbacks": int(st["fallbacks"]),
-                      "learned_loops": int(st["learned_loops"])})
+        gs = solver.learned_gate_state()
+        learn.update({"learned_rms_residual_last": st["last_rms"],
+                      "plain_reference_last": st["plain_rms_ref"],
+                      "plain_reduction_factor": gs["plain_factor"],
+                      "plain_calibration_loops": int(gs["plain_loops"]),
+                      "fallbacks": int(st["fallbacks"]), "learned_loops": int(st["learned_loops"])})
         # the same substep from the same state, three ways: rms no-slip residual
+        solver.learned_calibration(0)
         res = {}
         for name, nl, on in (("one_sweep", 1, False), ("plain_nl3", 3, False), ("one_sweep_plus_network", 3, True)):
             solver.learned_config(enable=on, fallback_ratio=1e9 if on else 1.5)
@@ -381,7 +391,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="all", choices=["all", "both", "plain", "mixed", "learned"])
     ap.add_argument("--harvest", type=int, default=2_000_000, help="harvest capacity (samples)")
-    ap.add_argument("--harvest-passes", type=int, default=6)
+    ap.add_argument("--harvest-steps", type=int, default=3, help="plain warm-up steps harvested")
+    ap.add_argument("--harvest-passes", type=int, default=3,
+                    help="plain passes of the harvested loops (3: the Nl = 3 correction the network replaces)")
     ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--stats-calls", type=int, default=3, help="post1d calls timed after the steps (0: none)")
@@ -437,7 +449,7 @@ def main():
     forms = {"plain": IBM_MODE_PLAIN_FP64, "mixed": IBM_MODE_MIXED, "learned": IBM_MODE_MIXED_LEARNED}
     wanted = {"all": ["plain", "mixed", "learned"], "both": ["plain", "learned"]}.get(args.form, [args.form])
     head = next(f for f in ("learned", "mixed", "plain") if f in wanted)
-    res = {f: run_form(args, ws, rank, local, forms[f], with_e2e=(f == head)) for f in wanted}
+    res = {f: run_form(args, ws, rank, local, forms[f], with_e2e=True) for f in wanted}
     if rank != 0:
         return
     r = res[head]
@@ -488,6 +500,7 @@ def main():
                       "phases_ms": {n: round(t, 4) for n, t in zip(names, x["phases"])},
                       "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"]),
                       "kernels": kernel_table(x, 8 if f == "plain" else 4),
+                      **({"e2e": x["e2e"]} if x["e2e"] else {}),
                       **({"post1d": x["stats"]} if x["stats"] else {}),
                       **({"learned_forcing": x["learn"]} if x["learn"] else {})} for f, x in res.items()},
         "mcell_steps_per_s": round(args.gpus * r["ncell"] / (r["ms"] * 1e-3) / 1e6, 1),

@@ -83,7 +83,10 @@ typedef struct ibm_params {
  * ([p*9 + nb], the neighbour flags ap(p)%nb(0:8)); rkp has np*19 entries in
  * the field order of particle_sumrk.  nqmax = min(np+2, 15) (param.f90:100).
  * Lagrangian arrays (np*nl, [p*nl + l]) are optional on set (may be NULL:
- * they are then regenerated from the centres as coordsfp does).
+ * they are then regenerated from the centres as coordsfp does).  nb may be
+ * NULL on set: the flags are then derived from the centres as a warm start
+ * does (loadd.f90:362-397); rkp may be NULL (zero).  On get, any member may
+ * be NULL (not returned).
  */
 typedef struct ibm_particles {
   double *x, *y, *z, *theta, *phi;
@@ -335,11 +338,31 @@ int ibm_train_forcing_model(ibm_ctx *ctx, int nsteps, int batch, double lr, unsi
 int ibm_set_forcing_model(ibm_ctx *ctx, const float *params, const float *norm);
 int ibm_get_forcing_model(ibm_ctx *ctx, float *params, float *norm);
 /* enable (needs a model), fallback_ratio (default 1.5), plain_rms_ref > 0
- * fixes the plain residual reference (else the mean over harvested loops). */
+ * fixes the plain residual reference; 0 (the default) uses the live one:
+ * the learned loop's residual R is held to fallback_ratio x c x R0, R0 its
+ * own first-pass slip (rms |U - u~| before any forcing) and c the factor by
+ * which the plain passes reduced the first-pass slip on the latest plain
+ * loop measured (harvested loops and the calibration loops below). */
 int ibm_learned_config(ibm_ctx *ctx, int enable, double fallback_ratio, double plain_rms_ref);
-/* stats[6]: rms residual of the last learned loop, plain reference, ratio,
- * fallbacks taken, learned loops run, harvested samples. */
+/* With the network on, every period-th forcing loop runs the plain passes
+ * instead and measures c on the current state (default 9: once every three
+ * RK3 steps; 0: never, c then comes from the harvest); the first loop with
+ * the network on is one when no plain loop has been measured yet. */
+int ibm_learned_calibration(ibm_ctx *ctx, int period);
+/* stats[6]: rms residual of the last learned loop, the reference its gate
+ * used (before any learned loop: the last plain residual measured), fallback
+ * ratio, fallbacks taken, learned loops run, harvested samples. */
 int ibm_learned_stats(ibm_ctx *ctx, double stats[6]);
+/* g[6]: first-pass slip R0 of the last learned loop, the plain reduction
+ * factor c, plain loops measured, the last gate's reference, R0 and residual
+ * of the last plain loop measured. */
+int ibm_learned_gate_state(ibm_ctx *ctx, double g[6]);
+/* Error-budget experiment for the learned form (mixed forms, plain passes):
+ * after the plain passes of every following forcing loop, each point's
+ * F*dt gets independent normal noise of rms sigma[c] per component
+ * (velocity units; seeded), spread into the forced field as an increment
+ * and included in the force sums.  All zero switches it off. */
+int ibm_forcing_perturbation(ibm_ctx *ctx, const double sigma[3], unsigned seed);
 /* The training kernels on a caller batch (features x[nb][96] already
  * standardised, targets t[nb][3]) with a scratch copy of params: loss,
  * gradient[IBM_NN_NPARAM] and outputs y[nb][3] (any may be NULL).  Loss =

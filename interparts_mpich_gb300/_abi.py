@@ -189,6 +189,9 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "get_forcing_model": (C.c_int, [ctx, c_float_p, c_float_p]),
         "learned_config": (C.c_int, [ctx, C.c_int, C.c_double, C.c_double]),
         "learned_stats": (C.c_int, [ctx, c_double_p]),
+        "learned_calibration": (C.c_int, [ctx, C.c_int]),
+        "learned_gate_state": (C.c_int, [ctx, c_double_p]),
+        "forcing_perturbation": (C.c_int, [ctx, c_double_p, C.c_uint]),
         "mlp_gradient": (C.c_int, [ctx, c_float_p, c_float_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p]),
         "mlp_infer": (C.c_int, [ctx, c_float_p, c_float_p, C.c_int, c_float_p]),
         "mlp_infer_tc": (C.c_int, [ctx, c_float_p, c_float_p, C.c_int, c_float_p]),

@@ -54,6 +54,17 @@ def bounduvw(u, v, w, bc_top=IBM_BC_NOSLIP, bc_bot=IBM_BC_NOSLIP):
         f[:, 0, :] = f[:, -2, :]
 
 
+def boundp(p):
+    """Reference ghost values of the pressure (boundp, bound.f90:82-107):
+    Neumann at the walls, periodic in x and y, on a (0:i1,0:j1,0:k1) array."""
+    p[:, :, 0] = p[:, :, 1]
+    p[:, :, -1] = p[:, :, -2]
+    p[-1, :, :] = p[1, :, :]
+    p[0, :, :] = p[-2, :, :]
+    p[:, -1, :] = p[:, 1, :]
+    p[:, 0, :] = p[:, -2, :]
+
+
 @dataclass
 class Case:
     name: str

@@ -16,9 +16,14 @@ i.e. 31 + 11*nqmax doubles in memory, but the writer streams only
 skip*npmstr doubles with skip = 27 + 10*nqmax + 2 + nqmax = 29 + 11*nqmax
 (loadd.f90:143-144, 679-686).  The file therefore holds the first
 (29 + 11*nqmax)*np doubles of the record array: the last 2*np doubles of the
-records are not written.  Both functions below reproduce that byte stream;
-the reader returns the particles whose records are complete in the file
-and the truncated tail as NaN.  The writer fills flag1/flag2 with 0 and
+records are not written, and a reader that loads the stream back into the
+record array (as loadpart does, loadd.f90:195) keeps whatever that memory
+held.  Both functions below reproduce that byte stream; the reader returns
+the truncated tail as NaN, or with fill_tail as a zero-initialised record
+array on one rank leaves it (0, with the particle id idp = index + 1).  For
+np <= 4 the tail is only the last particle's qmax, idp and firstc, so a
+particle without contacts restarts exactly; larger np lose data of the last
+particles in the reference's own format.  The writer fills flag1/flag2 with 0 and
 dut..psi with the values given (the reference leaves them unset).
 """
 from __future__ import annotations
@@ -106,13 +111,17 @@ def write_allpartdata(path: str | Path, ps: ParticleState) -> Path:
     return p
 
 
-def read_allpartdata(path: str | Path, np_: int, nq: int, nl: int = 0) -> ParticleState:
+def read_allpartdata(path: str | Path, np_: int, nq: int, nl: int = 0, fill_tail: bool = False) -> ParticleState:
     raw = np.fromfile(path, dtype=np.float64)
     if raw.size != written_len(nq) * np_:
         raise ValueError(f"{path}: {raw.size} doubles, expected {written_len(nq) * np_}")
-    full = np.full(record_len(nq) * np_, np.nan)
+    full = np.full(record_len(nq) * np_, 0.0 if fill_tail else np.nan)
     full[: raw.size] = raw
     rec = full.reshape(np_, record_len(nq))
+    if fill_tail:  # the id slot of every record whose idp was not written
+        idp_col = len(PART_SCALARS) + 10 * nq + 1
+        lost = np.arange(np_) * record_len(nq) + idp_col >= raw.size
+        rec[lost, idp_col] = np.arange(1, np_ + 1)[lost]
     ps = ParticleState(np_, nq, nl, lagrangian=False)
     for q, name in enumerate(PART_SCALARS):
         if name in ("flag1", "flag2"):
@@ -129,3 +138,37 @@ def read_allpartdata(path: str | Path, np_: int, nq: int, nl: int = 0) -> Partic
     ps.mslv = np.where(np.isnan(idp), -1, idp).astype(np.int32)
     ps.firstc = np.where(np.isnan(fc), -1, fc).astype(np.int32).ravel()
     return ps
+
+
+def save_restart(solver, directory: str | Path, istep: int, time: float, dt: float) -> tuple[Path, Path]:
+    """loadd(1, istep) of the driver (main.f90:495-506): fld<istep> and
+    allpartdata<istep> of the solver's current state in `directory`."""
+    d = Path(directory)
+    f = solver.get_fields()
+    pf = write_fld(d / fld_name(istep), f, time, istep, dt)
+    pp = d / allpartdata_name(istep)
+    if solver.case.np > 0:
+        write_allpartdata(pp, solver.get_particles(lagrangian=False))
+    return pf, pp
+
+
+def load_restart(solver, directory: str | Path, istep: int) -> tuple[float, int, float]:
+    """Warm start of program interpt (main.f90:155-201) into a fresh solver:
+    loadpart and loadflds, the boundary conditions, then coordsfp (the
+    Lagrangian points from the centres) without intgr_over_sphere; the
+    neighbour flags come from the centres as loadpart sets them.  Returns
+    (time, istep, dt) of the file."""
+    from .cases import boundp, bounduvw
+
+    c = solver.case
+    d = Path(directory)
+    f, time, istep_f, dt = read_fld(d / fld_name(istep), c.itot, c.jtot, c.ktot)
+    bounduvw(f["u"], f["v"], f["w"], c.bc_top, c.bc_bot)
+    boundp(f["p"])
+    solver.set_fields(f["u"], f["v"], f["w"], f["p"])
+    ps = read_allpartdata(d / allpartdata_name(istep), c.np, solver.nq, fill_tail=True) if c.np else \
+        ParticleState(0, solver.nq, 0, lagrangian=False)
+    ps.nb = None
+    ps.rkp = None
+    solver.set_particles(ps)
+    return time, istep_f, dt

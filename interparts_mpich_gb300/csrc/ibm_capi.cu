@@ -75,6 +75,19 @@ struct ibm_ctx {
   HarvestArgs hv{};
   int hv_passes = 0;
   bool harvesting = false, learn_on = false, model_ready = false, stats_ready = false;
+  // live plain reference of the fallback gate: every calib_period-th loop
+  // with the network on runs the plain passes and measures their reduction
+  // of the first-pass slip (also the first such loop when no plain loop has
+  // been measured yet)
+  int calib_period = 9;
+  long long learn_calls = 0;
+  bool calibrated = false;
+  // forcing perturbation (a test of the learned form's error budget): point
+  // noise of rms noise_sigma (velocity units) after the plain passes
+  double noise_sigma[3] = {0, 0, 0};
+  unsigned noise_seed = 0, noise_counter = 0;
+  float *noise_y = nullptr;    // [np*nl*3] deviates
+  float *noise_par = nullptr;  // [6]: sigma (3), mean 0 (3)
   __nv_bfloat16 *tx = nullptr; // staged training set
   float *tt = nullptr;
   int tcap = 0, train_step = 0;
@@ -401,6 +414,7 @@ int alloc_all(ibm_ctx *c) {
       if ((st = dalloc(c, &c->ib.cs, 3 * npl))) return st;
       if ((st = dalloc(c, &c->ib.bgeo, (size_t)24 * np))) return st;
       if ((st = dalloc(c, &c->ib.psum, (size_t)9 * np))) return st;
+      if ((st = dalloc(c, &c->ib.rsum, (size_t)3 * np))) return st;
     } else {
       if ((st = dalloc(c, &c->ib.st, npl))) return st;
     }
@@ -437,9 +451,10 @@ int alloc_all(ibm_ctx *c) {
     for (__nv_bfloat16 **f : {&c->mt.w1b, &c->mt.w2b, &c->mt.w2tb})
       if ((st = dalloc(c, f, 128 * 128))) return st;
     if ((st = dalloc(c, &c->norm, 198))) return st;
-    if ((st = dalloc(c, &c->ls, 8))) return st;
+    if ((st = dalloc(c, &c->ls, IBM_LS_N))) return st;
     if ((st = dalloc(c, &c->gate, 4))) return st;
-    const double ls0[8] = {0, 0, 0, 1.5, 0, 0, 0, 0};
+    double ls0[IBM_LS_N] = {};
+    ls0[3] = 1.5;
     CK(cudaMemcpyAsync(c->ls, ls0, sizeof(ls0), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (np > 0) {
@@ -530,7 +545,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   LAUNCHED(1);
   // F = F0 + the network's correction per point, its force and torque sums,
   // one spreading
-  const LearnedForce lf{c->ly, c->norm + 192, c->norm + 195, 1. / dt};
+  const LearnedForce lf{c->ly, c->norm + 192, c->norm + 195, 1. / dt, 0};
   PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, lf));
   launch_ibm_force_sums(c->stream, c->pg, c->ib);
   PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
@@ -547,11 +562,38 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   return IBM_OK;
 }
 
+int perturb_forces(ibm_ctx *c, double dt) {
+  // point noise of rms noise_sigma (velocity units) added to F*dt of every
+  // point and spread as an increment; the force sums follow
+  const long npts = (long)c->pg.np * c->pg.nl;
+  int st;
+  if (!c->noise_y) {
+    if ((st = dalloc(c, &c->noise_y, (size_t)3 * npts))) return st;
+    if ((st = dalloc(c, &c->noise_par, 6))) return st;
+  }
+  const float par[6] = {(float)c->noise_sigma[0], (float)c->noise_sigma[1], (float)c->noise_sigma[2], 0.f, 0.f, 0.f};
+  CK(cudaMemcpyAsync(c->noise_par, par, sizeof(par), cudaMemcpyHostToDevice, c->stream));
+  launch_normal_fill(c->stream, c->noise_y, 3 * npts, c->noise_seed, c->noise_counter++);
+  const LearnedForce lf{c->noise_y, c->noise_par + 3, c->noise_par, 1. / dt, 1};
+  launch_ibm_spread_f(c->stream, c->g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, lf);
+  launch_ibm_force_sums(c->stream, c->pg, c->ib);
+  LAUNCHED(3);
+  CK(cudaStreamSynchronize(c->stream));  // par is a host array
+  return IBM_OK;
+}
+
 int forcing(ibm_ctx *c, double dt, int nl_iter) {
   if (c->pg.np == 0 || nl_iter <= 0) return IBM_OK;
   const Geo &g = c->g;
   if (c->mixed) {
-    if (c->learn_on && !c->harvesting && nl_iter >= 2) return forcing_learned(c, dt, nl_iter);
+    bool calibrate = false;
+    if (c->learn_on && !c->harvesting && nl_iter >= 2) {
+      const long long k = c->learn_calls++;
+      calibrate = !c->calibrated || (c->calib_period > 0 && k % c->calib_period == c->calib_period - 1);
+      if (!calibrate) return forcing_learned(c, dt, nl_iter);
+      c->calibrated = true;
+    }
+    const bool measure = c->harvesting || calibrate;
     const long npts = (long)c->pg.np * c->pg.nl;
     const int npass = c->harvesting ? std::max(nl_iter, c->hv_passes) : nl_iter;
     PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
@@ -574,16 +616,20 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
       }
       PROBED(IBM_PROBE_SPREAD, launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt));
       LAUNCHED(1);
-      if (c->harvesting && it == nl_iter - 1) {
-        // the plain method's residual at its own number of passes
+      if (measure && c->ls && it == nl_iter - 1) {
+        // the plain method's residual at its own number of passes, against
+        // its first-pass slip: the reference of the learned loop's gate
         PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
         launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 1);
         LAUNCHED(2);
+        c->calibrated = true;
       }
     }
     if (c->harvesting) {
       launch_ibm_harvest_targets(c->stream, c->ib, c->hv, dt);
       LAUNCHED(2);
+    } else if (c->noise_sigma[0] > 0 || c->noise_sigma[1] > 0 || c->noise_sigma[2] > 0) {
+      return perturb_forces(c, dt);
     }
     return IBM_OK;
   }
@@ -801,7 +847,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
-                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
+                  c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
                   c->cfield, c->cnext, c->crk};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -979,22 +1025,49 @@ int ibm_set_particles(ibm_ctx *c, const ibm_particles *s) {
   for (int f = 0; f < 10; ++f)
     if (carr[f]) std::memcpy(&cf[(size_t)f * np * nq], carr[f], (size_t)np * nq * sizeof(double));
   CK(cudaMemcpyAsync(c->pb.cf, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  if (!s->qmax || !s->firstc || !s->nb || !s->mslv || !s->rkp)
-    return set_err(c, IBM_E_INVALID, "qmax, firstc, nb, mslv and rkp are required");
+  if (!s->qmax || !s->firstc || !s->mslv)
+    return set_err(c, IBM_E_INVALID, "qmax, firstc and mslv are required");
   for (int p = 0; p < np; ++p) {
     if (s->qmax[p] < 0 || s->qmax[p] > nq) return set_err(c, IBM_E_INVALID, "qmax outside 0..nqmax");
     if (s->mslv[p] != p + 1) return set_err(c, IBM_E_INVALID, "mslv must be the particle id p+1 on one rank");
-    for (int n = 0; n < 9; ++n)
-      if (s->nb[(size_t)p * 9 + n] != 0 && s->nb[(size_t)p * 9 + n] != 1) return set_err(c, IBM_E_INVALID, "nb flags must be 0/1");
+    if (s->nb)
+      for (int n = 0; n < 9; ++n)
+        if (s->nb[(size_t)p * 9 + n] != 0 && s->nb[(size_t)p * 9 + n] != 1) return set_err(c, IBM_E_INVALID, "nb flags must be 0/1");
+  }
+  // without nb: the flags of the self-neighbour copies from the centres, as a
+  // warm start sets them (loadd.f90:362-397, one rank: bounds 0..lx, 0..ly)
+  std::vector<int> nbh((size_t)np * 9, 0);
+  if (s->nb) {
+    std::memcpy(nbh.data(), s->nb, nbh.size() * sizeof(int));
+  } else {
+    const double ro = c->prm.radius + c->offset, rightb = c->prm.lx, backb = c->prm.ly, leftb = 0., frontb = 0.;
+    for (int p = 0; p < np; ++p) {
+      const double x = s->x[p], y = s->y[p];
+      int *f = &nbh[(size_t)p * 9];
+      double dist;
+      if (x > (rightb - ro)) f[1] = 1;
+      dist = std::sqrt((rightb - x) * (rightb - x) + (frontb - y) * (frontb - y));
+      if (std::fabs(dist) < ro) f[2] = 1;
+      if (y < (frontb + ro)) f[3] = 1;
+      dist = std::sqrt((leftb - x) * (leftb - x) + (frontb - y) * (frontb - y));
+      if (std::fabs(dist) < ro) f[4] = 1;
+      if (x < (leftb + ro)) f[5] = 1;
+      dist = std::sqrt((leftb - x) * (leftb - x) + (backb - y) * (backb - y));
+      if (std::fabs(dist) < ro) f[6] = 1;
+      if (y > (backb - ro)) f[7] = 1;
+      dist = std::sqrt((rightb - x) * (rightb - x) + (backb - y) * (backb - y));
+      if (std::fabs(dist) < ro) f[8] = 1;
+    }
   }
   CK(cudaMemcpyAsync(c->pb.qmax, s->qmax, np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->pb.firstc, s->firstc, (size_t)np * nq * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->pb.ofirstc, s->firstc, (size_t)np * nq * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->pb.nb, s->nb, (size_t)np * 9 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->pb.nb, nbh.data(), (size_t)np * 9 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->pb.mslv, s->mslv, np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  std::vector<double> rk((size_t)RK_N * np);
-  for (int p = 0; p < np; ++p)
-    for (int t = 0; t < RK_N; ++t) rk[(size_t)p * RK_N + t] = s->rkp[(size_t)p * RK_N + t];
+  std::vector<double> rk((size_t)RK_N * np, 0.);  // rkp may be NULL (zero)
+  if (s->rkp)
+    for (int p = 0; p < np; ++p)
+      for (int t = 0; t < RK_N; ++t) rk[(size_t)p * RK_N + t] = s->rkp[(size_t)p * RK_N + t];
   CK(cudaMemcpyAsync(c->pb.rkp, rk.data(), rk.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->pb.err, 0, 8 * sizeof(int), c->stream));
   if (s->xfp && s->yfp && s->zfp && s->ul && s->vl && s->wl) {
@@ -1675,11 +1748,11 @@ int ibm_learned_config(ibm_ctx *c, int enable, double fallback_ratio, double pla
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "needs IBM_MODE_MIXED_LEARNED");
   if (enable && !c->model_ready) return set_err(c, IBM_E_STATE, "no model to enable");
   if (!(fallback_ratio > 0) || plain_rms_ref < 0) return set_err(c, IBM_E_INVALID, "bad learned-forcing settings");
-  double h[8];
+  double h[IBM_LS_N];
   CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   h[3] = fallback_ratio;
-  if (plain_rms_ref > 0) { h[1] = plain_rms_ref; h[2] = 1.; }
+  h[8] = plain_rms_ref;  // > 0: a fixed reference; 0: the live one
   CK(cudaMemcpyAsync(c->ls, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   c->learn_on = enable != 0;
@@ -1690,17 +1763,48 @@ int ibm_learned_stats(ibm_ctx *c, double stats[6]) {
   if (!c || !stats) return IBM_E_INVALID;
   for (int q = 0; q < 6; ++q) stats[q] = 0.;
   if (c->mode != IBM_MODE_MIXED_LEARNED) return IBM_OK;
-  double h[8];
+  double h[IBM_LS_N];
   int cnt[2] = {0, 0};
   CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   if (c->hv.count) CK(cudaMemcpyAsync(cnt, c->hv.count, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   stats[0] = h[0];
-  stats[1] = h[2] > 0 ? h[1] / h[2] : 0.;
+  stats[1] = h[5] > 0 ? h[7] : h[10];  // the last gate's reference (before any: the last plain residual)
   stats[2] = h[3];
   stats[3] = h[4];
   stats[4] = h[5];
   stats[5] = cnt[1];
+  return IBM_OK;
+}
+
+int ibm_learned_calibration(ibm_ctx *c, int period) {
+  if (!c) return IBM_E_INVALID;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "needs IBM_MODE_MIXED_LEARNED");
+  if (period < 0) return set_err(c, IBM_E_INVALID, "period must be >= 0");
+  c->calib_period = period;
+  c->learn_calls = 0;
+  return IBM_OK;
+}
+
+int ibm_learned_gate_state(ibm_ctx *c, double g[6]) {
+  if (!c || !g) return IBM_E_INVALID;
+  for (int q = 0; q < 6; ++q) g[q] = 0.;
+  if (c->mode != IBM_MODE_MIXED_LEARNED) return IBM_OK;
+  double h[IBM_LS_N];
+  CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  g[0] = h[6]; g[1] = h[1]; g[2] = h[2]; g[3] = h[7]; g[4] = h[9]; g[5] = h[10];
+  return IBM_OK;
+}
+
+int ibm_forcing_perturbation(ibm_ctx *c, const double sigma[3], unsigned seed) {
+  if (!c || !sigma) return IBM_E_INVALID;
+  if (!c->mixed) return set_err(c, IBM_E_STATE, "the forcing perturbation needs a mixed form");
+  for (int q = 0; q < 3; ++q)
+    if (!(sigma[q] >= 0.)) return set_err(c, IBM_E_INVALID, "sigma must be >= 0");
+  for (int q = 0; q < 3; ++q) c->noise_sigma[q] = sigma[q];
+  c->noise_seed = seed;
+  c->noise_counter = 0;
   return IBM_OK;
 }
 

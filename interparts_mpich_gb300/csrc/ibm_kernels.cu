@@ -283,42 +283,81 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
   k_ibm_harvest_targets<<<152, 256, 0, s>>>(b, H, dt);
   k_ibm_harvest_close<<<1, 32, 0, s>>>(H);
 }
-// Residual gate: the rms of |U - u~| over all points from the per-(particle,
-// component) sums psum[p][c][0]; gate = (rms > fallback ratio x the plain
-// method's).  LearnState (device): [0] rms of the last learned substep,
-// [1] sum and [2] count of the plain passes' rms, [3] fallback ratio,
-// [4] fallbacks, [5] learned substeps; gate = 1 runs the plain passes after
-// the inference.
-__global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__restrict__ psum, long npts, double *ls,
+// Residual gate.  R = rms |U - u~| over all points after the loop (from the
+// per-(particle, component) sums psum[p][c][0]) and R0 = rms of the first
+// pass's slip (from rsum).  The plain loop's R/R0 measures how far its Nl
+// passes reduce the slip on the current state; the learned loop is held to
+// fallback ratio x (that ratio x its own R0), i.e. to what the plain passes
+// would reach from the same first-pass slip.  Learn state ls (device):
+//   [0] R of the last learned loop      [1] plain R/R0 (running, weight 1/2)
+//   [2] plain loops measured            [3] fallback ratio
+//   [4] fallbacks taken                 [5] learned loops
+//   [6] R0 of the last learned loop     [7] reference of the last gate
+//   [8] fixed reference (> 0 replaces ratio x R0)
+//   [9] R0 and [10] R of the last plain loop measured
+// gate = 1 runs the plain passes 2..Nl after the learned correction.
+__global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__restrict__ psum,
+                                                       const float *__restrict__ rsum, long npts, double *ls,
                                                        int *gate, int plain) {
-  // the per-particle residual sums are FP32-accurate (formed in FP32); their
-  // total in FP32 with warp shuffles, FP64 only for the gate's arithmetic
-  __shared__ float sm[32];
-  float acc = 0.f;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) acc += (float)psum[3 * (long)q];
+  // per-(particle, component) sums are FP32 accurate (formed in FP32): their
+  // totals in FP32 with warp shuffles, FP64 only for the gate's arithmetic
+  __shared__ float sm[2][32];
+  float acc = 0.f, acc0 = 0.f;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    acc += (float)psum[3 * (long)q];
+    acc0 += rsum[q];
+  }
 #pragma unroll
-  for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  for (int d = 16; d > 0; d >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, d);
+    acc0 += __shfl_xor_sync(0xffffffffu, acc0, d);
+  }
+  if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = acc; sm[1][threadIdx.x >> 5] = acc0; }
   __syncthreads();
   if (threadIdx.x != 0) return;
-  double tot = 0.;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += sm[w];
-  const double rms = npts ? sqrt(tot / (double)npts) : 0.;
-  if (plain) {  // residual of the plain passes: the reference the learned one is held to
-    ls[1] += rms;
+  double tot = 0., tot0 = 0.;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tot += sm[0][w]; tot0 += sm[1][w]; }
+  const double R = npts ? sqrt(tot / (double)npts) : 0., R0 = npts ? sqrt(tot0 / (double)npts) : 0.;
+  if (plain) {  // the plain passes' reduction of the slip on the current state
+    const double ci = R0 > 0. ? R / R0 : 0.;
+    ls[1] = ls[2] > 0. ? 0.5 * ls[1] + 0.5 * ci : ci;
     ls[2] += 1.;
+    ls[9] = R0;
+    ls[10] = R;
     return;
   }
-  ls[0] = rms;
+  const double ref = ls[8] > 0. ? ls[8] : (ls[2] > 0. ? ls[1] * R0 : 0.);
+  ls[0] = R;
   ls[5] += 1.;
-  const double ref = ls[2] > 0. ? ls[1] / ls[2] : 0.;
-  const int g = (!(rms <= ls[3] * ref)) ? 1 : 0;  // NaN falls back too
+  ls[6] = R0;
+  ls[7] = ref;
+  const int g = (!(R <= ls[3] * ref)) ? 1 : 0;  // NaN falls back too
   *gate = g;
   if (g) ls[4] += 1.;
 }
 void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
                               int plain) {
-  k_ibm_res_gate<<<1, 1024, 0, s>>>(3 * pg.np, b.psum, npts, ls, gate, plain);
+  k_ibm_res_gate<<<1, 1024, 0, s>>>(3 * pg.np, b.psum, b.rsum, npts, ls, gate, plain);
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {  // splitmix64 finaliser
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__global__ void k_normal_fill(float *__restrict__ y, long n, unsigned seed, unsigned counter) {
+  const unsigned long long key = ((unsigned long long)seed << 32) ^ counter;
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+    const unsigned long long h = mix64(mix64(key * 0x9E3779B97F4A7C15ULL + (unsigned long long)q));
+    // two 24-bit uniforms in (0, 1), Box-Muller (one deviate kept)
+    const float u1 = ((float)(h & 0xFFFFFF) + 0.5f) * (1.f / 16777216.f);
+    const float u2 = ((float)((h >> 24) & 0xFFFFFF) + 0.5f) * (1.f / 16777216.f);
+    y[q] = sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+  }
+}
+void launch_normal_fill(cudaStream_t s, float *y, long n, unsigned seed, unsigned counter) {
+  if (n <= 0) return;
+  k_normal_fill<<<1216, 256, 0, s>>>(y, n, seed, counter);
 }
 
 }  // namespace ibmk

@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
   const CompStencil *csp = b.cs + c * npl + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
   double sF = 0., sa = 0., sb = 0.;
-  float r2 = 0.f;
+  float r2 = 0.f, r0 = 0.f;
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const long t = t0 + l;
     const CompStencil s = load_cs(csp + l);
@@ -283,6 +283,10 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
     }
     dud[t] = acc;
     if (first < 0) continue;
+    if (first) {  // first-pass slip, for the learned loop's gate reference
+      const float e = (float)U[t] - acc;
+      r0 = fmaf(e, e, r0);
+    }
     const double f = first ? (U[t] - acc) * dti : Fl[t] + (U[t] - acc) * dti;
     Fl[t] = f;
     // lever arms of the torque terms of this component:
@@ -301,6 +305,10 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
     return;
   }
   if (first < 0) return;
+  if (first) {
+    const float tot = block_sum_all(r0);
+    if (threadIdx.x == 0) b.rsum[(long)p * 3 + c] = tot;
+  }
   __syncthreads();  // the box is dead: its first words hold the partial sums
   double *st = reinterpret_cast<double *>(ibox_sm);
   __shared__ double res[3];
@@ -384,6 +392,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   const int nla = b.nla[p];
   if (nla <= 0) {
     if (lf.Y && threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = 0.;
+    if (lf.Y && !lf.incr && threadIdx.x == 0) b.rsum[(long)p * 3 + c] = 0.f;
     return;
   }
   const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
@@ -421,7 +430,8 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   // instruction serialise).  Prefactors of staged points: natural order
   // (coalesced loads of the point arrays).
   const int nq = (nla + 31) >> 5;
-  float asum = 0.f;
+  float asum = 0.f, r0 = 0.f;
+  const double dt_l = lf.Y ? 1. / lf.dti : 0.;
   for (int m = threadIdx.x; m < 32 * nq; m += blockDim.x) {
     const int l = staged ? m : (m & 31) * nq + (m >> 5);
     if (l >= nla) continue;
@@ -430,14 +440,18 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     if (lf.Y) {
       // total point force F0 + the network's correction, its sums
       // (updtlagrforces), spread once
-      const double f = Fl[t] + (double)(lf.Y[3 * t + c] * ysig + ymu) * lf.dti;
+      const double f0 = Fl[t];
+      const double d = (double)(lf.Y[3 * t + c] * ysig + ymu) * lf.dti;
+      const double f = f0 + d;
       Fl[t] = f;
+      const float e0 = (float)(f0 * dt_l);  // the first pass's slip U - u~
+      r0 = fmaf(e0, e0, r0);
       const double la = c == 2 ? b.yfp[t] - py : b.zfp[t] - pz;
       const double lb = c == 0 ? b.yfp[t] - py : b.xfp[t] - px;
       sF += f;
       sa += la * f;
       sb += lb * f;
-      pre = (float)f * pcoef;
+      pre = (float)(lf.incr ? d : f) * pcoef;
     } else {
       pre = (float)(U[t] - dud[t]) * ucoef;
     }
@@ -458,10 +472,15 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
         }
     }
   }
-  if (lf.Y) {  // psum[p][c] for k_ibm_force_sums
+  if (lf.Y) {  // psum[p][c] for k_ibm_force_sums; rsum for the gate
     __shared__ double sred[3 * SPREAD_THREADS], res[3];
     block_sum3<SPREAD_THREADS>(sF, sa, sb, sred, res);
     if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
+    if (!lf.incr) {
+      const float tot = block_sum_all(r0);
+      if (threadIdx.x == 0) b.rsum[(long)p * 3 + c] = tot;
+      __syncthreads();  // block_sum_all's partials are read again below
+    }
   }
   if (!boxed) return;
   // fixed point: scale 2^(29 - e) with bound < 2^e, so that bound * scale < 2^30

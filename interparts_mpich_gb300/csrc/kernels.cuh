@@ -85,6 +85,7 @@ struct IbmBuffers {
   double *diag;      // [8] force totals etc.
   int *err;          // shared with PartBuffers::err ([2]: point outside the grid)
   double *psum;      // [np*9] mixed form: per-component force and lever-arm sums
+  float *rsum;       // [np*3] mixed form: per-component sums of the first-pass slip (U - u~)^2
 };
 template <typename T>
 void launch_ibm_stencil(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b);
@@ -104,9 +105,14 @@ int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, I
                               const float *fv, const float *fw, double dt, int first, const int *gate = nullptr);
 // learned form: the network's output Y, its target de-standardisation
 // (mean, sigma) and 1/dt; Y == nullptr: the plain pass
+// Point-force increment spread by k_ibm_spread_f: per point and component
+// d = (Y*tsig + tmu)*dti is added to F; incr = 0 spreads the total F (the
+// learned loop: F0 + the network's correction, the field holding no part of
+// F yet), incr = 1 only d (a perturbation of an already spread F).
 struct LearnedForce {
   const float *Y, *tmu, *tsig;
   double dti;
+  int incr;
 };
 void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, float *fu, float *fv,
                          float *fw, double dt, const LearnedForce &lf = LearnedForce{}, const int *gate = nullptr);
@@ -128,10 +134,15 @@ void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, I
                               const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                               __nv_bfloat16 *X);
 void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs &H, double dt);
-// residual gate from the per-(particle, component) sums of (U - u~)^2 that
-// the interpolation with first < 0 leaves in psum[p][c][0]
+// Residual gate from the per-(particle, component) sums of (U - u~)^2 that
+// the interpolation with first < 0 leaves in psum[p][c][0] and the sums of
+// the first-pass slip in rsum.  Learn state ls[IBM_LS_N], see k_ibm_res_gate.
+constexpr int IBM_LS_N = 16;
 void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
                               int plain);
+// y[3*npts] standard normal deviates from (seed, counter, index): a
+// counter-based hash and the Box-Muller transform
+void launch_normal_fill(cudaStream_t s, float *y, long n, unsigned seed, unsigned counter);
 
 // mlp_kernels.cu (learned forcing model)
 struct MlpTrainBuffers {

@@ -20,7 +20,13 @@
 //     that overlap on the GPU (for example on two streams at once) race;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current) and caches it; make that
-//     first call before any stream capture.
+//     first call before any stream capture.  The cached address belongs to
+//     the device's primary context: after cudaDeviceReset a new context may
+//     load the array elsewhere, so a process that resets a device must not
+//     call this function on that device again;
+//   * each launch reports its own status (cudaLaunchKernel), so an error
+//     pending from the caller's earlier work is neither returned here nor
+//     cleared.
 #include <mutex>
 
 #include "kernels.cuh"
@@ -118,7 +124,13 @@ extern "C" int ibm_chkdiv_noalloc(const double *u, const double *v, const double
     rec = g_noalloc_ptr[dev];
   }
   cudaStream_t s = (cudaStream_t)cuda_stream;
-  k_div_planes_ref<<<ktot, 256, 0, s>>>(u, v, w, itot, jtot, dxi, dyi, dzi, rec, ktot);
-  k_div_planes_final<<<1, 32, 0, s>>>(rec, ktot, itot, jtot, out5);
-  return cudaGetLastError() == cudaSuccess ? IBM_OK : IBM_E_CUDA;
+  int I = itot, J = jtot, K = ktot;
+  void *a1[] = {(void *)&u, (void *)&v, (void *)&w, &I, &J, &dxi, &dyi, &dzi, &rec, &K};
+  if (cudaLaunchKernel((const void *)k_div_planes_ref, dim3(ktot), dim3(256), a1, 0, s) != cudaSuccess)
+    return IBM_E_CUDA;
+  const double *crec = rec;
+  void *a2[] = {(void *)&crec, &K, &I, &J, &out5};
+  if (cudaLaunchKernel((const void *)k_div_planes_final, dim3(1), dim3(32), a2, 0, s) != cudaSuccess)
+    return IBM_E_CUDA;
+  return IBM_OK;
 }

@@ -324,6 +324,23 @@ class IBMSolver:
     def learned_config(self, enable: bool = True, fallback_ratio: float = 1.5, plain_rms_ref: float = 0.0):
         self._chk(self.fn["learned_config"](self.ctx, int(enable), float(fallback_ratio), float(plain_rms_ref)))
 
+    def learned_calibration(self, period: int):
+        """Every period-th loop with the network on runs the plain passes and
+        refreshes the gate's reference (0: never)."""
+        self._chk(self.fn["learned_calibration"](self.ctx, int(period)))
+
+    def learned_gate_state(self) -> dict:
+        g = (C.c_double * 6)()
+        self._chk(self.fn["learned_gate_state"](self.ctx, g))
+        keys = ("r0_last", "plain_factor", "plain_loops", "reference_last", "plain_r0_last", "plain_rms_last")
+        return dict(zip(keys, list(g)))
+
+    def forcing_perturbation(self, sigma, seed: int = 0):
+        """Point noise of rms sigma[c] (velocity units) after the plain passes
+        of every following forcing loop (mixed forms); zeros switch it off."""
+        s = (C.c_double * 3)(*[float(x) for x in sigma])
+        self._chk(self.fn["forcing_perturbation"](self.ctx, s, int(seed) & 0xFFFFFFFF))
+
     def learned_stats(self) -> dict:
         s = (C.c_double * 6)()
         self._chk(self.fn["learned_stats"](self.ctx, s))

@@ -1956,9 +1956,12 @@ int orc_set_particles(orc_ctx *c, const ibm_particles *s) {
       P.dxt[q] = s->cdxt[o]; P.dyt[q] = s->cdyt[o]; P.dzt[q] = s->cdzt[o];
       P.dut[q] = s->cdut[o]; P.dvt[q] = s->cdvt[o]; P.dwt[q] = s->cdwt[o]; P.psi[q] = s->cpsi[o];
     }
-    for (int n = 0; n < 9; ++n) P.nb[n] = s->nb[(size_t)p * 9 + n];
     P.mslv = s->mslv[p];
-    for (int t = 0; t < RK_N; ++t) c->rkp[(size_t)p * RK_N + t] = s->rkp[(size_t)p * RK_N + t];
+    // nb NULL: the flags from the centre, as a warm start sets them
+    // (loadd.f90:362-397); rkp NULL: zero
+    if (s->nb) for (int n = 0; n < 9; ++n) P.nb[n] = s->nb[(size_t)p * 9 + n];
+    else nb_flags(c, P);
+    for (int t = 0; t < RK_N; ++t) c->rkp[(size_t)p * RK_N + t] = s->rkp ? s->rkp[(size_t)p * RK_N + t] : 0.;
     c->op[p].firstc = P.firstc;
   }
   c->pmax = c->np;
@@ -1976,44 +1979,55 @@ int orc_set_particles(orc_ctx *c, const ibm_particles *s) {
   } else {
     lagrangian_points(c);
   }
+  // dVlagr of the outer shell and dVeul (coordsfp.f90:84-90), and the
+  // per-particle constants of initparticles: a warm start (main.f90:166-201)
+  // runs coordsfp without intgr_over_sphere
+  c->dVlagr = ((4. / 3.) * PI * std::pow(c->radfp + 0.5 / c->dxi, 3.) -
+               (4. / 3.) * PI * std::pow(c->radfp - 0.5 / c->dxi, 3.)) / (1. * c->nl);
+  c->dVeul = 1. / (c->dxi * c->dyi * c->dzi);
+  for (auto &P : c->ap) { P.vol = c->volp; P.ratiorho = c->ratiorho; P.mominert = c->mominert; }
   c->have_particles = true;
   return IBM_OK;
 }
 
 int orc_get_particles(orc_ctx *c, ibm_particles *s) {
+  // any member pointer may be NULL (not returned), as in the library
   const int nq = c->nqmax;
+#define PUT(arr, idx, val) \
+  do {                     \
+    if (arr) (arr)[idx] = (val); \
+  } while (0)
   for (int p = 0; p < c->np; ++p) {
     const Part &P = c->ap[p];
-    s->x[p] = P.x; s->y[p] = P.y; s->z[p] = P.z; s->theta[p] = P.theta; s->phi[p] = P.phi;
-    s->u[p] = P.u; s->v[p] = P.v; s->w[p] = P.w; s->omx[p] = P.omx; s->omy[p] = P.omy; s->omz[p] = P.omz;
-    s->omtheta[p] = P.omtheta;
-    s->intu[p] = P.intu; s->intv[p] = P.intv; s->intw[p] = P.intw;
-    s->intomx[p] = P.intomx; s->intomy[p] = P.intomy; s->intomz[p] = P.intomz;
-    s->colfx[p] = P.colfx; s->colfy[p] = P.colfy; s->colfz[p] = P.colfz;
-    s->coltx[p] = P.coltx; s->colty[p] = P.colty; s->coltz[p] = P.coltz;
-    s->fxltot[p] = P.fxltot; s->fyltot[p] = P.fyltot; s->fzltot[p] = P.fzltot;
-    s->torqxltot[p] = P.torqxltot; s->torqyltot[p] = P.torqyltot; s->torqzltot[p] = P.torqzltot;
-    s->torqtheta[p] = P.torqtheta;
-    s->qmax[p] = P.qmax;
+    PUT(s->x, p, P.x); PUT(s->y, p, P.y); PUT(s->z, p, P.z); PUT(s->theta, p, P.theta); PUT(s->phi, p, P.phi);
+    PUT(s->u, p, P.u); PUT(s->v, p, P.v); PUT(s->w, p, P.w); PUT(s->omx, p, P.omx); PUT(s->omy, p, P.omy);
+    PUT(s->omz, p, P.omz); PUT(s->omtheta, p, P.omtheta);
+    PUT(s->intu, p, P.intu); PUT(s->intv, p, P.intv); PUT(s->intw, p, P.intw);
+    PUT(s->intomx, p, P.intomx); PUT(s->intomy, p, P.intomy); PUT(s->intomz, p, P.intomz);
+    PUT(s->colfx, p, P.colfx); PUT(s->colfy, p, P.colfy); PUT(s->colfz, p, P.colfz);
+    PUT(s->coltx, p, P.coltx); PUT(s->colty, p, P.colty); PUT(s->coltz, p, P.coltz);
+    PUT(s->fxltot, p, P.fxltot); PUT(s->fyltot, p, P.fyltot); PUT(s->fzltot, p, P.fzltot);
+    PUT(s->torqxltot, p, P.torqxltot); PUT(s->torqyltot, p, P.torqyltot); PUT(s->torqzltot, p, P.torqzltot);
+    PUT(s->torqtheta, p, P.torqtheta);
+    PUT(s->qmax, p, P.qmax);
     for (int q = 0; q < nq; ++q) {
       const size_t o = (size_t)p * nq + q;
-      s->firstc[o] = P.firstc[q];
-      s->cdx[o] = P.dx[q]; s->cdy[o] = P.dy[q]; s->cdz[o] = P.dz[q];
-      s->cdxt[o] = P.dxt[q]; s->cdyt[o] = P.dyt[q]; s->cdzt[o] = P.dzt[q];
-      s->cdut[o] = P.dut[q]; s->cdvt[o] = P.dvt[q]; s->cdwt[o] = P.dwt[q]; s->cpsi[o] = P.psi[q];
+      PUT(s->firstc, o, P.firstc[q]);
+      PUT(s->cdx, o, P.dx[q]); PUT(s->cdy, o, P.dy[q]); PUT(s->cdz, o, P.dz[q]);
+      PUT(s->cdxt, o, P.dxt[q]); PUT(s->cdyt, o, P.dyt[q]); PUT(s->cdzt, o, P.dzt[q]);
+      PUT(s->cdut, o, P.dut[q]); PUT(s->cdvt, o, P.dvt[q]); PUT(s->cdwt, o, P.dwt[q]); PUT(s->cpsi, o, P.psi[q]);
     }
-    for (int n = 0; n < 9; ++n) s->nb[(size_t)p * 9 + n] = P.nb[n];
-    s->mslv[p] = P.mslv;
-    for (int t = 0; t < RK_N; ++t) s->rkp[(size_t)p * RK_N + t] = c->rkp[(size_t)p * RK_N + t];
-    if (s->xfp) {
-      for (int l = 0; l < c->nl; ++l) {
-        const size_t o = (size_t)p * c->nl + l;
-        s->xfp[o] = P.xfp[l]; s->yfp[o] = P.yfp[l]; s->zfp[o] = P.zfp[l];
-        s->ul[o] = P.ul[l]; s->vl[o] = P.vl[l]; s->wl[o] = P.wl[l];
-        if (s->fxl) { s->fxl[o] = P.fxl[l]; s->fyl[o] = P.fyl[l]; s->fzl[o] = P.fzl[l]; }
-      }
+    for (int n = 0; n < 9; ++n) PUT(s->nb, (size_t)p * 9 + n, P.nb[n]);
+    PUT(s->mslv, p, P.mslv);
+    for (int t = 0; t < RK_N; ++t) PUT(s->rkp, (size_t)p * RK_N + t, c->rkp[(size_t)p * RK_N + t]);
+    for (int l = 0; l < c->nl; ++l) {
+      const size_t o = (size_t)p * c->nl + l;
+      PUT(s->xfp, o, P.xfp[l]); PUT(s->yfp, o, P.yfp[l]); PUT(s->zfp, o, P.zfp[l]);
+      PUT(s->ul, o, P.ul[l]); PUT(s->vl, o, P.vl[l]); PUT(s->wl, o, P.wl[l]);
+      PUT(s->fxl, o, P.fxl[l]); PUT(s->fyl, o, P.fyl[l]); PUT(s->fzl, o, P.fzl[l]);
     }
   }
+#undef PUT
   return IBM_OK;
 }
 

@@ -48,3 +48,32 @@ def test_allpartdata_stream(tmp_path):
     assert record_len(nq) - written_len(nq) == 2
     assert np.array_equal(back.x[:2], ps.x[:2]) and np.array_equal(back.mslv[:2], [1, 2])
     assert back.contact_lists()[0] == [2]
+
+
+def test_restart_roundtrip_oracle(tmp_path):
+    """2 steps, fld/allpartdata written and read back into a fresh context
+    (warm start), 2 more steps: identical to 4 uninterrupted steps.  Four
+    spheres: the format's lost tail is then only the last particle's qmax,
+    idp and firstc, which a particle without contacts does not use."""
+    from interparts_mpich_gb300.checkpoint import load_restart, save_restart
+
+    c = Case(name="rs", itot=32, jtot=32, ktot=32, radius=4.0 / 32, np=4, visc=1.0 / 500.0, seed=5)
+    a = OracleSolver(c)
+    a.setup()
+    dt = 0.5 * a.chkdt()
+    a.run(dt, 4)
+    b = OracleSolver(c)
+    b.setup()
+    b.run(dt, 2)
+    assert all(q == 0 for q in b.get_particles(lagrangian=False).qmax)
+    save_restart(b, tmp_path, 2, 2 * dt, dt)
+    r = OracleSolver(c)
+    time, istep, dt_f = load_restart(r, tmp_path, 2)
+    assert (istep, dt_f) == (2, dt)
+    r.run(dt, 2)
+    fa, fr = a.get_fields(), r.get_fields()
+    for n in "uvwp":
+        assert np.array_equal(fa[n][1:-1, 1:-1, 1:-1], fr[n][1:-1, 1:-1, 1:-1]), n
+    pa, pr = a.get_particles(), r.get_particles()
+    for n in ("x", "y", "z", "u", "v", "w", "omx", "intu", "intomz", "xfp", "ul"):
+        assert np.array_equal(getattr(pa, n), getattr(pr, n)), n

@@ -141,6 +141,7 @@ def trained(gpu_lib):
     s.harvest(0)
     st = s.learned_stats()
     loss = s.train_forcing_model(nsteps=6000, batch=4096, lr=1e-3, seed=1)
+    s.learned_calibration(0)  # the tests below call loops one at a time: no interleaved plain loops
     return s, dt, loss, st
 
 
@@ -202,20 +203,20 @@ def _steps(s, dt, nl, nsteps):
             s.intgr_nwtn_eulr(r, dt)
 
 
-def test_learned_20_steps_against_oracle(trained):
+def test_learned_20_steps_within_oracle_nl_spread(trained):
     """A fresh run with the trained model against the FP64 oracle after 20
-    steps.  The learned correction is an approximation of the plain Nl=3
-    correction, so its flow departs from the Nl=3 oracle by more than the
-    mixed form's 1e-4 (the plain method itself moves by 1.6e-2 on this case
-    between Nl=3 and Nl=6): it must stay within that spread of the method's
-    own forcing convergence, and its loops within the fallback bound."""
+    steps.  This is not the 1e-4 velocity target (the bench-size test
+    test_gpu_fullsize.py holds that target, marked as missed): the learned
+    correction approximates the plain Nl = 3 correction, and its flow departs
+    from the Nl = 3 oracle by less than the plain method itself moves
+    between Nl = 3 and Nl = 6 on this case."""
     s, dt, _, _ = trained
     p, n = s.get_forcing_model()
     case = _flow_case()
     m = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
     m.setup()
     m.set_forcing_model(p, n)
-    m.learned_config(enable=True, fallback_ratio=1.5, plain_rms_ref=s.learned_stats()["plain_rms_ref"])
+    m.learned_config(enable=True, fallback_ratio=1.5)
     m.run(dt, 20)
     o3 = OracleSolver(case)
     o3.setup()
@@ -226,7 +227,93 @@ def test_learned_20_steps_against_oracle(trained):
     f3 = o3.get_fields()
     e_learned = max(field_errors(m.get_fields(), f3, names=("u", "v", "w")).values())
     e_nl = max(field_errors(o6.get_fields(), f3, names=("u", "v", "w")).values())
-    print(f"velocity rel L2 after 20 steps vs oracle Nl=3: learned {e_learned:.3e}, oracle Nl=6 {e_nl:.3e}")
-    assert e_learned < e_nl
     st = m.learned_stats()
-    assert st["learned_loops"] == 60
+    gs = m.learned_gate_state()
+    print(f"velocity rel L2 after 20 steps vs oracle Nl=3: learned {e_learned:.3e}, oracle Nl=6 {e_nl:.3e}; "
+          f"learned loops {int(st['learned_loops'])}, plain calibration loops {int(gs['plain_loops'])}, "
+          f"fallbacks {int(st['fallbacks'])}")
+    assert e_learned < e_nl
+    assert st["learned_loops"] + gs["plain_loops"] == 60
+
+
+def test_fallback_gate_fires_on_degraded_network(trained):
+    """Mid-run on the 48^3 flow: with the trained network the live gate
+    (learned residual against 1.5 x the plain passes' reduction of the same
+    loop's first-pass slip) never falls back; with every weight and bias of
+    the network halved it falls back."""
+    s, dt, _, _ = trained
+    p, n = s.get_forcing_model()
+    case = _flow_case()
+    m = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    m.setup()
+    m.set_forcing_model(p, n)
+    m.learned_config(enable=True, fallback_ratio=1.5)
+    m.run(dt, 4)
+    good = m.learned_stats()
+    g_good = m.learned_gate_state()
+    m.set_forcing_model(0.5 * p, n)
+    m.learned_config(enable=True, fallback_ratio=1.5)
+    m.run(dt, 2)
+    bad = m.learned_stats()
+    g_bad = m.learned_gate_state()
+    print(f"good network: residual {good['last_rms']:.3e} vs reference {good['plain_rms_ref']:.3e} "
+          f"(plain factor {g_good['plain_factor']:.3f}), fallbacks {int(good['fallbacks'])}; degraded: residual "
+          f"{bad['last_rms']:.3e} vs reference {bad['plain_rms_ref']:.3e}, fallbacks "
+          f"{int(bad['fallbacks'] - good['fallbacks'])} of {int(bad['learned_loops'] - good['learned_loops'])}")
+    assert good["fallbacks"] == 0 and good["learned_loops"] > 0
+    assert bad["fallbacks"] - good["fallbacks"] >= 1
+    assert bad["last_rms"] > 1.5 * bad["plain_rms_ref"]
+
+
+def _point_force_error(s, dt):
+    """Same state, same substep: the learned loop's point forces against the
+    plain Nl = 3 loop's, rms of the difference of F*dt per component."""
+    s.learned_config(enable=False)
+    s.rk(1, dt)
+    s.forcing_loop(dt, 3)
+    f3 = s.get_particles()
+    s.learned_config(enable=True, fallback_ratio=1e9)
+    s.rk(1, dt)
+    s.forcing_loop(dt, 3)
+    fl = s.get_particles()
+    s.learned_config(enable=True, fallback_ratio=1.5)
+    return [float(np.sqrt(np.mean(((getattr(fl, n) - getattr(f3, n)) * dt) ** 2))) for n in ("fxl", "fyl", "fzl")]
+
+
+def test_learned_error_budget_noise_ablation(trained):
+    """What the learned form's 20-step deviation is made of.  sigma = the
+    network's per-point error of F*dt on the same state; the mixed form with
+    the exact Nl = 3 forcing plus independent point noise of that rms (and
+    of a tenth of it) runs 20 steps against the oracle, beside the learned
+    form.  A deviation that scales with the noise shows a linear response
+    (no chaotic growth over 20 steps); the printed numbers compare the
+    network's error with uncorrelated noise of the same size."""
+    s, dt, _, _ = trained
+    sigma = _point_force_error(s, dt)
+    case = _flow_case()
+    o = OracleSolver(case)
+    o.setup()
+    _steps(o, dt, 3, 20)
+    fo = o.get_fields()
+    errs = {}
+    for scale in (1.0, 0.1):
+        m = IBMSolver(case, mode=IBM_MODE_MIXED)
+        m.setup()
+        m.forcing_perturbation([scale * x for x in sigma], seed=7)
+        m.run(dt, 20)
+        errs[scale] = max(field_errors(m.get_fields(), fo, names=("u", "v", "w")).values())
+        m.close()
+    p, n = s.get_forcing_model()
+    lm = IBMSolver(case, mode=IBM_MODE_MIXED_LEARNED)
+    lm.setup()
+    lm.set_forcing_model(p, n)
+    lm.learned_config(enable=True, fallback_ratio=1.5)
+    lm.run(dt, 20)
+    e_learned = max(field_errors(lm.get_fields(), fo, names=("u", "v", "w")).values())
+    print(f"network per-point error of F*dt (u, v, w): {sigma[0]:.3e} {sigma[1]:.3e} {sigma[2]:.3e}; "
+          f"20-step velocity rel L2 vs oracle: exact Nl=3 + noise sigma {errs[1.0]:.3e}, + noise sigma/10 "
+          f"{errs[0.1]:.3e}, learned {e_learned:.3e}")
+    assert all(x > 0 for x in sigma)
+    assert errs[1.0] > errs[0.1] > 1e-6
+    # linear response: a tenth of the noise gives about a tenth of the deviation
+    assert 3.0 < errs[1.0] / errs[0.1] < 30.0
