@@ -230,6 +230,33 @@ def statistics_timing(solver, case, calls: int) -> dict:
                                     "achieved": round(ach, 1), "unit": "GB/s", "frac": round(ach / hbm, 4)}}
 
 
+def workload_case(args):
+    from interparts_mpich_gb300.cases import channel_case, wide_channel_case
+
+    if args.workload == "wide":
+        return wide_channel_case(2 * args.n, args.n, args.np if args.np != 1000 else 8000, seed=1234)
+    return channel_case(args.n, args.np, seed=1234)
+
+
+def harvest_and_train(solver, case, dt, args) -> dict:
+    """Plain warm-up steps with harvesting (every stride-th point, so that the
+    samples span all of them), then the GPU training of the network."""
+    hs = max(1, args.harvest_steps)
+    stride = max(1, -(-hs * 3 * case.np * case.nl // args.harvest))
+    solver.harvest(capacity=args.harvest, stride=stride, passes=args.harvest_passes)
+    for _ in range(hs):
+        solver.rk3_step(dt)
+    solver.harvest(0)
+    solver.sync()
+    t0 = time.perf_counter()
+    loss = solver.train_forcing_model(args.train_steps, batch=args.batch, lr=1e-3, seed=1)
+    train_s = time.perf_counter() - t0
+    st = solver.learned_stats()
+    return {"harvested_samples": int(st["harvested"]), "harvest_steps": hs, "harvest_stride": stride,
+            "harvest_passes": args.harvest_passes, "train_steps": args.train_steps, "batch": args.batch,
+            "adam_lr": 1e-3, "train_s": round(train_s, 3), "final_loss_std_units": round(loss, 5)}
+
+
 def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     """Times one arithmetic form on the channel case: K steps between CUDA
     events on the library's stream, plus the per-phase times of one step."""
@@ -239,7 +266,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     from interparts_mpich_gb300._abi import ParticleState
     from interparts_mpich_gb300.cases import channel_case
 
-    case = channel_case(args.n, args.np, seed=1234)
+    case = workload_case(args)
     solver = IBMSolver(case, mode=mode)
     if args.proj_solves and mode != 0:
         solver.set_projection_solves(args.proj_solves)
@@ -250,24 +277,22 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     learn = None
     nwarm = args.warmup
     if mode == IBM_MODE_MIXED_LEARNED:
-        # the first warm-up steps: plain passes with harvesting (every
-        # stride-th point, so that the samples span all of them); then GPU
-        # training
-        hs = max(1, args.harvest_steps)
-        stride = max(1, -(-hs * 3 * case.np * case.nl // args.harvest))
-        solver.harvest(capacity=args.harvest, stride=stride, passes=args.harvest_passes)
-        for _ in range(hs):
-            solver.rk3_step(dt)
-        solver.harvest(0)
-        solver.sync()
-        t0 = time.perf_counter()
-        loss = solver.train_forcing_model(args.train_steps, batch=args.batch, lr=1e-3, seed=1)
-        train_s = time.perf_counter() - t0
-        st = solver.learned_stats()
-        learn = {"harvested_samples": int(st["harvested"]), "harvest_steps": hs, "harvest_stride": stride,
-                 "harvest_passes": args.harvest_passes, "train_steps": args.train_steps, "batch": args.batch,
-                 "adam_lr": 1e-3, "train_s": round(train_s, 3), "final_loss_std_units": round(loss, 5)}
-        nwarm = max(1, nwarm - hs)
+        if args.workload == "channel":
+            # the first warm-up steps: plain passes with harvesting; then GPU training
+            learn = harvest_and_train(solver, case, dt, args)
+            nwarm = max(1, nwarm - learn["harvest_steps"])
+        else:
+            # the network is harvested and trained on the 256^3 channel, then
+            # runs on this case
+            ch = channel_case(256, 1000, seed=1234)
+            src = IBMSolver(ch, mode=mode)
+            src.setup(ch.initial_fields())
+            learn = harvest_and_train(src, ch, 0.5 * src.chkdt(), args)
+            learn["trained_on"] = "channel 256^3, 1000 spheres"
+            p, nrm = src.get_forcing_model()
+            src.close()
+            solver.set_forcing_model(p, nrm)
+            solver.learned_config(enable=True, fallback_ratio=1.5)
     for _ in range(nwarm):
         solver.rk3_step(dt)
     solver.sync()
@@ -385,13 +410,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "wide"],
+                    help="channel: n^3, np spheres (the headline case); wide: 2n x 2n x n on a (2, 2, 1) box, "
+                         "8000 spheres, the learned network trained on the 256^3 channel")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--np", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="all", choices=["all", "both", "plain", "mixed", "learned"])
     ap.add_argument("--harvest", type=int, default=2_000_000, help="harvest capacity (samples)")
-    ap.add_argument("--harvest-steps", type=int, default=3, help="plain warm-up steps harvested")
+    ap.add_argument("--harvest-steps", type=int, default=6,
+                    help="plain warm-up steps harvested (every stride-th point, so that the capacity spans them)")
     ap.add_argument("--harvest-passes", type=int, default=3,
                     help="plain passes of the harvested loops (3: the Nl = 3 correction the network replaces)")
     ap.add_argument("--train-steps", type=int, default=6000)
@@ -408,9 +437,12 @@ def main():
 
     from interparts_mpich_gb300.cases import channel_case
 
-    config = {"workload": f"channel {args.n}^3, {args.np} spheres D=16dx, perturbed Poiseuille Re_b=5600, "
-                          f"Nl=3, dt=0.5 dtmax frozen", "grid": [args.n] * 3, "spheres": args.np,
-              "l2_policy": "inputs larger than L2 (each field 137 MB > 129 MB L2)"}
+    wl = workload_case(args)
+    config = {"workload": f"{'channel' if args.workload == 'channel' else 'wide channel'} "
+                          f"{wl.itot}x{wl.jtot}x{wl.ktot} ({wl.lx:g} x {wl.ly:g} x {wl.lz:g}), {wl.np} spheres "
+                          f"D=16dx, perturbed Poiseuille Re_b=5600, Nl=3, dt=0.5 dtmax frozen",
+              "grid": [wl.itot, wl.jtot, wl.ktot], "spheres": wl.np,
+              "l2_policy": "inputs larger than L2 (each field >= 137 MB > 129 MB L2)"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -418,7 +450,7 @@ def main():
         from oracle.oracle import OracleSolver, load
         lib, _ = load()
         cores = lib.orc_set_threads(os.cpu_count() or 1)
-        case = channel_case(args.n, args.np, seed=1234)
+        case = workload_case(args)
         o = OracleSolver(case)
         o.setup()
         dt = 0.5 * o.chkdt()
@@ -525,7 +557,7 @@ def main():
         line["e2e"] = r["e2e"]
     if not args.no_cpu_baseline:
         try:
-            line["cpu_baseline"] = cpu_baseline(args, lambda: channel_case(args.n, args.np, seed=1234))
+            line["cpu_baseline"] = cpu_baseline(args, lambda: workload_case(args))
         except Exception as ex:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
     print(json.dumps(line))

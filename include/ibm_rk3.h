@@ -339,23 +339,25 @@ int ibm_set_forcing_model(ibm_ctx *ctx, const float *params, const float *norm);
 int ibm_get_forcing_model(ibm_ctx *ctx, float *params, float *norm);
 /* enable (needs a model), fallback_ratio (default 1.5), plain_rms_ref > 0
  * fixes the plain residual reference; 0 (the default) uses the live one:
- * the learned loop's residual R is held to fallback_ratio x c x R0, R0 its
- * own first-pass slip (rms |U - u~| before any forcing) and c the factor by
- * which the plain passes reduced the first-pass slip on the latest plain
- * loop measured (harvested loops and the calibration loops below). */
+ * the learned loop's residual R is held to fallback_ratio x c_s x R0, R0 its
+ * own first-pass slip (rms |U - u~| before any forcing) and c_s the factor
+ * by which the plain passes reduced the first-pass slip on the latest plain
+ * loops measured at the same RK stage s (harvested loops and the
+ * calibration loops below).  The stage is that of the last ibm_rk_predict. */
 int ibm_learned_config(ibm_ctx *ctx, int enable, double fallback_ratio, double plain_rms_ref);
 /* With the network on, every period-th forcing loop runs the plain passes
- * instead and measures c on the current state (default 9: once every three
- * RK3 steps; 0: never, c then comes from the harvest); the first loop with
- * the network on is one when no plain loop has been measured yet. */
+ * instead and measures c_s on the current state (default 10, which visits
+ * the three stages in turn, each once every ten RK3 steps; 0: never, c_s
+ * then comes from the harvest); a loop with the network on at a stage
+ * without any plain loop measured yet is one. */
 int ibm_learned_calibration(ibm_ctx *ctx, int period);
 /* stats[6]: rms residual of the last learned loop, the reference its gate
  * used (before any learned loop: the last plain residual measured), fallback
  * ratio, fallbacks taken, learned loops run, harvested samples. */
 int ibm_learned_stats(ibm_ctx *ctx, double stats[6]);
-/* g[6]: first-pass slip R0 of the last learned loop, the plain reduction
- * factor c, plain loops measured, the last gate's reference, R0 and residual
- * of the last plain loop measured. */
+/* g[6]: first-pass slip R0 of the last learned loop, the reduction factor
+ * c_s its gate used, plain loops measured, the last gate's reference
+ * c_s x R0, R0 and residual of the last plain loop measured. */
 int ibm_learned_gate_state(ibm_ctx *ctx, double g[6]);
 /* Error-budget experiment for the learned form (mixed forms, plain passes):
  * after the plain passes of every following forcing loop, each point's

@@ -148,12 +148,29 @@ class Case:
     def sphere_centres(self) -> np.ndarray:
         if self.centres is not None:
             return np.asarray(self.centres, np.float64).reshape(self.np, 3)
+        if getattr(self, "_placed", None) is None:
+            self._placed = self._place_spheres()
+        return self._placed.copy()
+
+    def _place_spheres(self) -> np.ndarray:
         R = self.radius
         D = 2 * R
         zmin, zmax = R + self.gap * D, self.lz - R - self.gap * D
         dmin = D + self.gap * D
         rng = np.random.default_rng(self.seed + 7919)
         out = np.zeros((self.np, 3))
+        # accepted centres binned in cells at least dmin wide (periodic in x
+        # and y): a candidate is tested against the spheres of its 27
+        # neighbouring cells only, which are all that can lie within dmin
+        nx = max(1, int(self.lx // dmin))
+        ny = max(1, int(self.ly // dmin))
+        nz = max(1, int(self.lz // dmin))
+        cells: dict[tuple[int, int, int], list[int]] = {}
+
+        def cell(c):
+            return (min(int(c[0] / self.lx * nx), nx - 1), min(int(c[1] / self.ly * ny), ny - 1),
+                    min(int(c[2] / self.lz * nz), nz - 1))
+
         n = 0
         tries = 0
         while n < self.np:
@@ -162,12 +179,20 @@ class Case:
                 raise RuntimeError("could not place the spheres without overlap")
             c = np.array([rng.uniform(0, self.lx), rng.uniform(0, self.ly), rng.uniform(zmin, zmax)])
             if n:
-                d = np.abs(out[:n] - c)
-                d[:, 0] = np.minimum(d[:, 0], self.lx - d[:, 0])
-                d[:, 1] = np.minimum(d[:, 1], self.ly - d[:, 1])
-                if np.min(np.einsum("ij,ij->i", d, d)) < dmin * dmin:
-                    continue
+                ix, iy, iz = cell(c)
+                near = []
+                for a in {(ix + q) % nx for q in (-1, 0, 1)}:
+                    for b in {(iy + q) % ny for q in (-1, 0, 1)}:
+                        for z in range(max(iz - 1, 0), min(iz + 2, nz)):
+                            near.extend(cells.get((a, b, z), ()))
+                if near:
+                    d = np.abs(out[near] - c)
+                    d[:, 0] = np.minimum(d[:, 0], self.lx - d[:, 0])
+                    d[:, 1] = np.minimum(d[:, 1], self.ly - d[:, 1])
+                    if np.min(np.sum(d * d, axis=1)) < dmin * dmin:
+                        continue
             out[n] = c
+            cells.setdefault(cell(c), []).append(n)
             n += 1
         return out
 
@@ -189,6 +214,18 @@ def channel_case(n: int = 256, nspheres: int = 1000, seed: int = 1234) -> Case:
     D = 16 dx with gaps >= 0.1 D."""
     return Case(name=f"channel{n}_np{nspheres}", itot=n, jtot=n, ktot=n, visc=1.0 / 5600.0,
                 radius=8.0 / n, ratiorho=1.0, np=nspheres, seed=seed, flow="poi", perturb=0.05)
+
+
+def wide_channel_case(nx: int = 512, nz: int = 256, nspheres: int = 8000, seed: int = 1234) -> Case:
+    """The wide channel of the learned-forcing runs: nx x nx x nz grid on a
+    (2, 2, 1) box (dx = 1/nz), walls at z = 0 and z = 1, perturbed Poiseuille
+    flow at bulk Re 5600 (streamwise y), neutrally buoyant spheres of
+    D = 16 dx placed at random without overlap (gaps >= 0.05 D to each other
+    and to the walls; at 8000 spheres the volume fraction is 25.6 %)."""
+    lx = nx / nz
+    return Case(name=f"wide{nx}x{nz}_np{nspheres}", itot=nx, jtot=nx, ktot=nz, lx=lx, ly=lx, lz=1.0,
+                visc=1.0 / 5600.0, radius=8.0 / nz, ratiorho=1.0, np=nspheres, seed=seed, flow="poi", perturb=0.05,
+                gap=0.05)
 
 
 def settling_case(n: int = 64, seed: int = 1) -> Case:

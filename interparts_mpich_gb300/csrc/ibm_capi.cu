@@ -77,11 +77,13 @@ struct ibm_ctx {
   bool harvesting = false, learn_on = false, model_ready = false, stats_ready = false;
   // live plain reference of the fallback gate: every calib_period-th loop
   // with the network on runs the plain passes and measures their reduction
-  // of the first-pass slip (also the first such loop when no plain loop has
-  // been measured yet)
-  int calib_period = 9;
+  // of the first-pass slip, per RK stage (also the first such loop of a
+  // stage when that stage has no plain loop measured yet); a period that is
+  // not a multiple of 3 visits the stages in turn
+  int calib_period = 10;
   long long learn_calls = 0;
-  bool calibrated = false;
+  bool calibrated[3] = {false, false, false};
+  int stage = 0;  // RK stage of the last predictor call (0..2)
   // forcing perturbation (a test of the learned form's error budget): point
   // noise of rms noise_sigma (velocity units) after the plain passes
   double noise_sigma[3] = {0, 0, 0};
@@ -287,6 +289,15 @@ void derived(ibm_ctx *c) {
   pg.a11_ini_pw = -(1. / eps_ini_pw) + 1. / 5. * std::log(eps_ini_pw) + 1. / 21. * eps_ini_pw * std::log(eps_ini_pw) - .9713;
   pg.a11_sat_pw = -(1. / eps_sat_pw) + 1. / 5. * std::log(eps_sat_pw) + 1. / 21. * eps_sat_pw * std::log(eps_sat_pw) - .9713;
   pg.I = g.I; pg.J = g.J; pg.K = g.K;
+  {  // collision cell list: cells >= 1.01 x 2.1 R wide
+    const double w = 1.01 * 2.1 * P.radius;
+    pg.ncx = std::max(1, (int)std::floor(P.lx / w));
+    pg.ncy = std::max(1, (int)std::floor(P.ly / w));
+    pg.ncz = std::max(1, (int)std::floor(P.lz / w));
+    pg.cix = (float)(pg.ncx / P.lx);
+    pg.ciy = (float)(pg.ncy / P.ly);
+    pg.ciz = (float)(pg.ncz / P.lz);
+  }
   // smallest double x with sqrt(x) >= radius (sqrt is correctly rounded and
   // monotone on host and device alike)
   double t = P.radius * P.radius;
@@ -431,6 +442,11 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, &c->pb.err, 8))) return st;
     if ((st = dalloc(c, &c->pb.red, (size_t)10 * np))) return st;
     if ((st = dalloc(c, &c->pb.pos4, (size_t)np))) return st;
+    const size_t ncell = (size_t)c->pg.ncx * c->pg.ncy * c->pg.ncz;
+    if ((st = dalloc(c, &c->pb.cstart, ncell + 1))) return st;
+    if ((st = dalloc(c, &c->pb.cfill, ncell))) return st;
+    if ((st = dalloc(c, &c->pb.citem, (size_t)np))) return st;
+    if ((st = dalloc(c, &c->pb.ccell, (size_t)np))) return st;
     if ((st = dalloc(c, &c->ib.diag, 8))) return st;
     c->ib.pf = c->pb.pf;
     c->ib.err = c->pb.err;
@@ -480,6 +496,7 @@ int check_flags(ibm_ctx *c) {
 
 int predict(ibm_ctx *c, int rkiter, double dt) {
   const Geo &g = c->g;
+  c->stage = rkiter - 1;
   if (c->mixed) launch_wallshear<float>(c->stream, g, c->v32, c->scratch, c->dout + 8 + (rkiter - 1));
   else launch_wallshear<double>(c->stream, g, c->v, c->scratch, c->dout + 8 + (rkiter - 1));
   LAUNCHED(2);
@@ -550,7 +567,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   launch_ibm_force_sums(c->stream, c->pg, c->ib);
   PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
                                                                          c->fv32, c->fw32, dt, -1));
-  launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 0);
+  launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 0, c->stage);
   LAUNCHED(4);  // spreading, force sums, residual interpolation, gate
   for (int it = 1; it < nl_iter; ++it) {
     PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
@@ -589,9 +606,8 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     bool calibrate = false;
     if (c->learn_on && !c->harvesting && nl_iter >= 2) {
       const long long k = c->learn_calls++;
-      calibrate = !c->calibrated || (c->calib_period > 0 && k % c->calib_period == c->calib_period - 1);
+      calibrate = !c->calibrated[c->stage] || (c->calib_period > 0 && k % c->calib_period == c->calib_period - 1);
       if (!calibrate) return forcing_learned(c, dt, nl_iter);
-      c->calibrated = true;
     }
     const bool measure = c->harvesting || calibrate;
     const long npts = (long)c->pg.np * c->pg.nl;
@@ -620,9 +636,9 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
         // the plain method's residual at its own number of passes, against
         // its first-pass slip: the reference of the learned loop's gate
         PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
-        launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 1);
+        launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 1, c->stage);
         LAUNCHED(2);
-        c->calibrated = true;
+        c->calibrated[c->stage] = true;
       }
     }
     if (c->harvesting) {
@@ -746,8 +762,8 @@ int newton_euler(ibm_ctx *c, int rkiter, double dt) {
   probe_mark(c, IBM_PROBE_SPHERE);
   LAUNCHED(1);
   for (int iter = 0; iter <= 1; ++iter) {
-    launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt, iter > 0);
-    LAUNCHED(iter > 0 ? 2 : 1);
+    c->launches += launch_collide_update(c->stream, c->pg, c->pb, iter, rkiter, dt, iter > 0);
+    LAUNCHED(0);
   }
   launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 0);
   LAUNCHED(1);
@@ -845,7 +861,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->twN, c->twJ, c->scratch, c->dout, c->href, c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl,
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
-                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->ru32, c->rv32, c->rw32, c->fu32,
+                  c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->pb.cstart, c->pb.cfill, c->pb.citem, c->pb.ccell, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.cs, c->ib.bgeo, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
                   c->cfield, c->cnext, c->crk};
@@ -1793,7 +1809,7 @@ int ibm_learned_gate_state(ibm_ctx *c, double g[6]) {
   double h[IBM_LS_N];
   CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  g[0] = h[6]; g[1] = h[1]; g[2] = h[2]; g[3] = h[7]; g[4] = h[9]; g[5] = h[10];
+  g[0] = h[6]; g[1] = h[6] > 0 ? h[7] / h[6] : 0.; g[2] = h[2]; g[3] = h[7]; g[4] = h[9]; g[5] = h[10];
   return IBM_OK;
 }
 

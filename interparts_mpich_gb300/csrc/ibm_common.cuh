@@ -79,6 +79,11 @@ struct PartGeo {
   double kn_ss, etan_ss, kt_ss, etat_ss, muc_ss, kn_sw, etan_sw, kt_sw, etat_sw, muc_sw;
   double coeff_f, a11a_ini_pp, a11b_ini_pp, a11a_sat_pp, a11b_sat_pp, a11_ini_pw, a11_sat_pw;
   int I, J, K;
+  // uniform cell list of the collision candidate search: cells at least
+  // 1.01 x the FP32 filter distance 2.1 R wide (ncx, ncy >= 3, else the
+  // search scans all particles)
+  int ncx, ncy, ncz;
+  float cix, ciy, ciz;  // cells per unit length
 };
 
 __host__ __device__ inline long fidx(const Geo &g, int i, int j, int k) {

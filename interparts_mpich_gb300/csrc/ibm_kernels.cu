@@ -285,20 +285,23 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
 }
 // Residual gate.  R = rms |U - u~| over all points after the loop (from the
 // per-(particle, component) sums psum[p][c][0]) and R0 = rms of the first
-// pass's slip (from rsum).  The plain loop's R/R0 measures how far its Nl
-// passes reduce the slip on the current state; the learned loop is held to
-// fallback ratio x (that ratio x its own R0), i.e. to what the plain passes
-// would reach from the same first-pass slip.  Learn state ls (device):
-//   [0] R of the last learned loop      [1] plain R/R0 (running, weight 1/2)
+// pass's slip (from rsum).  A plain loop's R/R0 measures how far its Nl
+// passes reduce the slip on the current state, per RK stage (the predicted
+// field, and with it the slip's pattern, differs between the stages); the
+// learned loop of stage s is held to fallback ratio x (that stage's ratio x
+// its own R0), i.e. to what the plain passes would reach from the same
+// first-pass slip.  Learn state ls (device):
+//   [0] R of the last learned loop      [1] plain R/R0 of stage 1 (running, weight 1/2)
 //   [2] plain loops measured            [3] fallback ratio
 //   [4] fallbacks taken                 [5] learned loops
 //   [6] R0 of the last learned loop     [7] reference of the last gate
 //   [8] fixed reference (> 0 replaces ratio x R0)
 //   [9] R0 and [10] R of the last plain loop measured
+//   [11], [12] plain R/R0 of stages 2 and 3; [13..15] plain loops measured per stage
 // gate = 1 runs the plain passes 2..Nl after the learned correction.
 __global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__restrict__ psum,
                                                        const float *__restrict__ rsum, long npts, double *ls,
-                                                       int *gate, int plain) {
+                                                       int *gate, int plain, int stage) {
   // per-(particle, component) sums are FP32 accurate (formed in FP32): their
   // totals in FP32 with warp shuffles, FP64 only for the gate's arithmetic
   __shared__ float sm[2][32];
@@ -318,15 +321,17 @@ __global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__re
   double tot = 0., tot0 = 0.;
   for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tot += sm[0][w]; tot0 += sm[1][w]; }
   const double R = npts ? sqrt(tot / (double)npts) : 0., R0 = npts ? sqrt(tot0 / (double)npts) : 0.;
+  const int cs = stage == 0 ? 1 : 10 + stage, ns = 13 + stage;
   if (plain) {  // the plain passes' reduction of the slip on the current state
     const double ci = R0 > 0. ? R / R0 : 0.;
-    ls[1] = ls[2] > 0. ? 0.5 * ls[1] + 0.5 * ci : ci;
+    ls[cs] = ls[ns] > 0. ? 0.5 * ls[cs] + 0.5 * ci : ci;
+    ls[ns] += 1.;
     ls[2] += 1.;
     ls[9] = R0;
     ls[10] = R;
     return;
   }
-  const double ref = ls[8] > 0. ? ls[8] : (ls[2] > 0. ? ls[1] * R0 : 0.);
+  const double ref = ls[8] > 0. ? ls[8] : (ls[ns] > 0. ? ls[cs] * R0 : 0.);
   ls[0] = R;
   ls[5] += 1.;
   ls[6] = R0;
@@ -336,8 +341,8 @@ __global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__re
   if (g) ls[4] += 1.;
 }
 void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
-                              int plain) {
-  k_ibm_res_gate<<<1, 1024, 0, s>>>(3 * pg.np, b.psum, b.rsum, npts, ls, gate, plain);
+                              int plain, int stage) {
+  k_ibm_res_gate<<<1, 1024, 0, s>>>(3 * pg.np, b.psum, b.rsum, npts, ls, gate, plain, stage);
 }
 
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {  // splitmix64 finaliser

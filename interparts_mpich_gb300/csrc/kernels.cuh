@@ -139,7 +139,7 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
 // the first-pass slip in rsum.  Learn state ls[IBM_LS_N], see k_ibm_res_gate.
 constexpr int IBM_LS_N = 16;
 void launch_ibm_residual_gate(cudaStream_t s, const PartGeo &pg, IbmBuffers b, long npts, double *ls, int *gate,
-                              int plain);
+                              int plain, int stage);
 // y[3*npts] standard normal deviates from (seed, counter, index): a
 // counter-based hash and the Box-Muller transform
 void launch_normal_fill(cudaStream_t s, float *y, long n, unsigned seed, unsigned counter);
@@ -206,6 +206,10 @@ struct PartBuffers {
   int *err;       // [8] error flags ([4]: learned-forcing MMA wait timeout)
   double *red;    // [10*np]: volume [np], sphere-integral partials [np][3][3]
   float4 *pos4;   // [np] FP32 snapshot positions (w: master flag) for the collision filter
+  int *cstart;    // [ncell+1] cell list of the snapshot positions: first item of each cell
+  int *cfill;     // [ncell] scatter cursors
+  int *citem;     // [np] particle indices by cell, ascending within a cell
+  int *ccell;     // [np] cell of each particle
 };
 template <typename T>
 void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, PartBuffers b, const T *u, const T *v,
@@ -213,8 +217,9 @@ void launch_sphere_integrals(cudaStream_t s, const Geo &g, const PartGeo &pg, Pa
 void launch_save_old(cudaStream_t s, const PartGeo &pg, PartBuffers b);
 // snapshot: take the iteration's snapshot first (false when the sphere
 // integrals' final kernel took it)
-void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt,
-                           bool snapshot = true);
+// returns the number of kernels launched
+int launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt,
+                          bool snapshot = true);
 void launch_ne_finalize(cudaStream_t s, const PartGeo &pg, PartBuffers b, IbmBuffers ib, int init_flags);
 
 

@@ -622,10 +622,78 @@ __global__ void k_snapshot(PartGeo pg, PartBuffers b) {
   if (p < pg.np) snapshot_particle(pg, b, p);
 }
 
+// Uniform cell list of the snapshot positions (one block): cell of every
+// particle, counts, exclusive scan, scatter, then every cell's items sorted
+// ascending.  Cells are at least 1.01 x the filter distance wide, so every
+// partner the FP32 filter accepts lies in the 27 cells around the particle's
+// own (periodic in x and y, clamped in z).
+__device__ __forceinline__ int coll_cell(const PartGeo &pg, float4 x) {
+  int cx = (int)floorf(x.x * pg.cix), cy = (int)floorf(x.y * pg.ciy), cz = (int)floorf(x.z * pg.ciz);
+  cx = ((cx % pg.ncx) + pg.ncx) % pg.ncx;
+  cy = ((cy % pg.ncy) + pg.ncy) % pg.ncy;
+  cz = min(max(cz, 0), pg.ncz - 1);
+  return (cz * pg.ncy + cy) * pg.ncx + cx;
+}
+__global__ void __launch_bounds__(1024) k_cell_build(PartGeo pg, PartBuffers b) {
+  const int np = pg.np, ncell = pg.ncx * pg.ncy * pg.ncz, tid = threadIdx.x;
+  __shared__ int part[1024];
+  for (int q = tid; q < ncell; q += 1024) b.cfill[q] = 0;
+  __syncthreads();
+  for (int p = tid; p < np; p += 1024) {
+    const int c = coll_cell(pg, b.pos4[p]);
+    b.ccell[p] = c;
+    atomicAdd(&b.cfill[c], 1);
+  }
+  __syncthreads();
+  const int per = (ncell + 1023) / 1024, lo = min(tid * per, ncell), hi = min(lo + per, ncell);
+  int sum = 0;
+  for (int q = lo; q < hi; ++q) sum += b.cfill[q];
+  part[tid] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int v = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int run = tid ? part[tid - 1] : 0;
+  for (int q = lo; q < hi; ++q) {
+    const int n = b.cfill[q];
+    b.cstart[q] = run;
+    b.cfill[q] = run;
+    run += n;
+  }
+  if (tid == 1023) b.cstart[ncell] = part[1023];
+  __syncthreads();
+  for (int p = tid; p < np; p += 1024) b.citem[atomicAdd(&b.cfill[b.ccell[p]], 1)] = p;
+  __syncthreads();
+  for (int q = tid; q < ncell; q += 1024) {  // ascending within the cell
+    const int e0 = b.cstart[q], e1 = b.cstart[q + 1];
+    for (int i = e0 + 1; i < e1; ++i) {
+      const int v = b.citem[i];
+      int j = i - 1;
+      while (j >= e0 && b.citem[j] > v) { b.citem[j + 1] = b.citem[j]; --j; }
+      b.citem[j + 1] = v;
+    }
+  }
+}
+
+// the FP32 periodic-distance filter of the candidate search
+__device__ __forceinline__ bool coll_near(float4 q, float pxf, float pyf, float pzf, float lxf, float lyf, float thr2) {
+  float dxf = fabsf(q.x - pxf);
+  float dyf = fabsf(q.y - pyf);
+  const float dzf = q.z - pzf;
+  dxf = fminf(dxf, fabsf(lxf - dxf));
+  dyf = fminf(dyf, fabsf(lyf - dyf));
+  return dxf * dxf + dyf * dyf + dzf * dzf < thr2;
+}
+
 // One warp per particle: a coarse FP32 periodic-distance filter selects the
 // partners that can interact (lubrication range, contact, or listed in
-// firstc); lane 0 then walks them in the reference (nb, q) order, handles
-// the walls, integrates Newton-Euler and accumulates sumrk3.
+// firstc), from the 27 cells of the cell list around the particle (or from
+// all particles when the grid is narrower than three cells), in ascending
+// particle order; lane 0 then walks them in the reference (nb, q) order,
+// handles the walls, integrates Newton-Euler and accumulates sumrk3.
 __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, PartBuffers b, int iter, int rkiter,
                                                                    double dt) {
   __shared__ int cand[COLL_WARPS][COLL_CAP];
@@ -646,6 +714,52 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   const float lxf = (float)pg.lx, lyf = (float)pg.ly;
   const float4 pp = b.pos4[p];
   const float pxf = pp.x, pyf = pp.y, pzf = pp.z;
+  if (pg.ncx >= 3 && pg.ncy >= 3) {
+    // cell list: lane t < 27 scans neighbouring cell t; partners in firstc
+    // beyond the filter distance are added by the lane of their slot; then
+    // the list is sorted ascending (as the full scan produces it)
+    if (lane < 27) {
+      const int c0 = b.ccell[p];
+      const int cx = c0 % pg.ncx, cy = (c0 / pg.ncx) % pg.ncy, cz = c0 / (pg.ncx * pg.ncy);
+      const int x = (cx + lane % 3 - 1 + pg.ncx) % pg.ncx, y = (cy + (lane / 3) % 3 - 1 + pg.ncy) % pg.ncy;
+      const int z = cz + lane / 9 - 1;
+      if (z >= 0 && z < pg.ncz) {
+        const int c = (z * pg.ncy + y) * pg.ncx + x;
+        for (int t = b.cstart[c]; t < b.cstart[c + 1]; ++t) {
+          const int q = b.citem[t];
+          const float4 qp = b.pos4[q];
+          if (q != p && qp.w != 0.f && coll_near(qp, pxf, pyf, pzf, lxf, lyf, thr2)) {
+            const int pos = atomicAdd(&ncand[wid], 1);
+            if (pos < COLL_CAP) cand[wid][pos] = q;
+          }
+        }
+      }
+    }
+    if (lane < qmax0) {
+      const int id = fc[lane];
+      if (id >= 1 && id <= np) {
+        const int q = id - 1;
+        const float4 qp = b.pos4[q];
+        if (q != p && qp.w != 0.f && b.mslv[q] == id && !coll_near(qp, pxf, pyf, pzf, lxf, lyf, thr2)) {
+          const int pos = atomicAdd(&ncand[wid], 1);
+          if (pos < COLL_CAP) cand[wid][pos] = q;
+        }
+      }
+    }
+    __syncwarp();
+    const int n = min(ncand[wid], COLL_CAP);
+    const int v0 = lane < n ? cand[wid][lane] : 0, v1 = lane + 32 < n ? cand[wid][lane + 32] : 0;
+    int r0 = 0, r1 = 0;
+    for (int i = 0; i < n; ++i) {
+      const int w = cand[wid][i];
+      r0 += w < v0;
+      r1 += w < v1;
+    }
+    __syncwarp();
+    if (lane < n) cand[wid][r0] = v0;
+    if (lane + 32 < n) cand[wid][r1] = v1;
+    __syncwarp();
+  } else {
   // candidates in ascending q: within the collision distance or already in
   // contact; four slices of 32 per round, loads issued together
   constexpr int SL = 4;
@@ -663,12 +777,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
       const int q = base + 32 * u + lane;
       bool c = false;
       if (q < np && q != p && qp[u].w != 0.f) {
-        float dxf = fabsf(qp[u].x - pxf);
-        float dyf = fabsf(qp[u].y - pyf);
-        const float dzf = qp[u].z - pzf;
-        dxf = fminf(dxf, fabsf(lxf - dxf));
-        dyf = fminf(dyf, fabsf(lyf - dyf));
-        c = dxf * dxf + dyf * dyf + dzf * dzf < thr2;
+        c = coll_near(qp[u], pxf, pyf, pzf, lxf, lyf, thr2);
         for (int i = 0; i < qmax0 && !c; ++i) c = ((i < 16 ? fcs[wid][i] : fc[i]) == qms[u]);
       }
       const unsigned m = __ballot_sync(0xffffffffu, c);
@@ -680,6 +789,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
       if (lane == 0) ncand[wid] += __popc(m);
       __syncwarp();
     }
+  }
   }
   int nc = ncand[wid];
   if (nc > COLL_CAP) { if (lane == 0) atomicExch(&b.err[0], 1); nc = COLL_CAP; }
@@ -871,11 +981,14 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   r[RK_DWDT] = r[RK_DWDT] + (nw - ow) / dt;
 }
 
-void launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt,
-                           bool snapshot) {
-  if (pg.np == 0) return;
-  if (snapshot) k_snapshot<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b);
+int launch_collide_update(cudaStream_t s, const PartGeo &pg, PartBuffers b, int iter, int rkiter, double dt,
+                          bool snapshot) {
+  if (pg.np == 0) return 0;
+  int n = 1;
+  if (snapshot) { k_snapshot<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b); ++n; }
+  if (pg.ncx >= 3 && pg.ncy >= 3) { k_cell_build<<<1, 1024, 0, s>>>(pg, b); ++n; }
   k_collide_update<<<(pg.np + COLL_WARPS - 1) / COLL_WARPS, 32 * COLL_WARPS, 0, s>>>(pg, b, iter, rkiter, dt);
+  return n;
 }
 
 // ---------------------------------------------------------------------------

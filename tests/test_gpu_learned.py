@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from _util import field_errors, small_case
-from interparts_mpich_gb300 import IBM_MODE_MIXED_LEARNED, IBMSolver
+from interparts_mpich_gb300 import IBM_MODE_MIXED, IBM_MODE_MIXED_LEARNED, IBMSolver
 from oracle import mlp_ref
 from oracle.oracle import OracleSolver
 
