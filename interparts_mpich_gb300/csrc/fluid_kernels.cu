@@ -6,6 +6,8 @@
 // fused multiply-add contraction is allowed (differences at 1 ulp level).
 #include <algorithm>
 
+#include <cstdlib>
+
 #include "kernels.cuh"
 
 namespace ibmk {
@@ -263,14 +265,206 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
   }
 }
 
+// The same stage with two x-neighbouring cells per thread in packed FP32x2
+// arithmetic (one instruction for both cells; the x neighbours of the pair
+// come from three aligned 8-byte shared loads instead of six): 64 x 8 cells
+// per block, rows padded to an even start so that every pair is aligned.
+constexpr int QTX = 64, QTY = 8, QHY = QTY + 2, QROW = QTX + 4, QKC = 32;
+// IBM_PREDICT_SCALAR=1 selects k_predict_tiled (one cell per thread) instead
+bool predict_pairs() {
+  static const bool on = [] {
+    const char *e = std::getenv("IBM_PREDICT_SCALAR");
+    return !(e && e[0] == '1');
+  }();
+  return on;
+}
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 ld2(const float *row, int idx) { return *reinterpret_cast<const float2 *>(row + idx); }
+__device__ __forceinline__ float2 mid(float2 a, float2 b) { return make_float2(a.y, b.x); }
+template <int STAGE, bool BUOY>
+__global__ void __launch_bounds__(QTX / 2 * QTY) k_predict_pair(Geo g, const float *__restrict__ u,
+                                                               const float *__restrict__ v,
+                                                               const float *__restrict__ w,
+                                                               const float *__restrict__ p, float *__restrict__ ru,
+                                                               float *__restrict__ rv, float *__restrict__ rw,
+                                                               float *__restrict__ fu, float *__restrict__ fv,
+                                                               float *__restrict__ fw, float f1, float f2_, float f3,
+                                                               const double *__restrict__ cb, double bcoef) {
+  // row layout: [pad, x = i0 - 1, x = i0 .. i0 + 63, x = i0 + 64, pad]
+  __shared__ __align__(16) float su[3][QHY][QROW], sv[3][QHY][QROW], sw[3][QHY][QROW], sp[2][QHY][QROW];
+  constexpr int NT = QTX / 2 * QTY, NH = QHY * (QTX + 2), HQ = (NH + NT - 1) / NT;
+  const int tx = threadIdx.x % (QTX / 2), ty = threadIdx.x / (QTX / 2);
+  const int i0 = blockIdx.x * QTX, j0 = blockIdx.y * QTY;
+  const int k0 = 1 + blockIdx.z * QKC, k1 = min(g.K, k0 + QKC - 1);
+  const int i = i0 + 2 * tx, j = j0 + ty;
+  const bool in = i < g.I && j < g.J;  // I even: i + 1 < I as well
+  const int PL = g.I * g.J;  // 32-bit offsets: launched only for fields < 2^31 cells
+  int hoff[HQ], hyx[HQ];
+  bool has[HQ];
+#pragma unroll
+  for (int q = 0; q < HQ; ++q) {
+    const int e = threadIdx.x + q * NT;
+    has[q] = e < NH;
+    const int hy = has[q] ? e / (QTX + 2) : 0, hx = has[q] ? e - hy * (QTX + 2) : 0;
+    int gi = (i0 - 1 + hx) % g.I, gj = (j0 - 1 + hy) % g.J;
+    if (gi < 0) gi += g.I;
+    if (gj < 0) gj += g.J;
+    hoff[q] = gj * g.I + gi;
+    hyx[q] = hy * QROW + hx + 1;
+  }
+  float nu[HQ], nv[HQ], nw[HQ], np_[HQ];
+  auto fetch = [&](int kk) {
+#pragma unroll
+    for (int q = 0; q < HQ; ++q)
+      if (has[q]) {
+        const int o = kk * PL + hoff[q];
+        nu[q] = u[o]; nv[q] = v[o]; nw[q] = w[o]; np_[q] = p[o];
+      }
+  };
+  auto commit = [&](int kk) {
+#pragma unroll
+    for (int q = 0; q < HQ; ++q)
+      if (has[q]) {
+        (&su[kk % 3][0][0])[hyx[q]] = nu[q];
+        (&sv[kk % 3][0][0])[hyx[q]] = nv[q];
+        (&sw[kk % 3][0][0])[hyx[q]] = nw[q];
+        (&sp[kk % 2][0][0])[hyx[q]] = np_[q];
+      }
+  };
+  fetch(k0 - 1);
+  commit(k0 - 1);
+  fetch(k0);
+  commit(k0);
+  fetch(k0 + 1);
+  const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi, visc = (float)g.visc;
+  const float2 qdxi = f2(0.25f * dxi), qdyi = f2(0.25f * dyi), qdzi = f2(0.25f * dzi);
+  const float2 vdx2 = f2(visc * dxi * dxi), vdy2 = f2(visc * dyi * dyi), vdz2 = f2(visc * dzi * dzi);
+  const float2 mdxi = f2(-dxi), mdyi = f2(-dyi), mdzi = f2(-dzi);
+  const float2 F1 = f2(f1), F2 = f2(f2_), F3 = f2(f3);
+  const int x = 2 * tx + 2, y = ty + 1;
+  for (int k = k0; k <= k1; ++k) {
+    commit(k + 1);
+    __syncthreads();
+    if (k + 1 <= k1) fetch(k + 2);
+    if (in) {
+      const int cm = (k - 1) % 3, c0 = k % 3, cp = (k + 1) % 3;
+      // u
+      const float *ur = su[c0][y];
+      const float2 U0 = ld2(ur, x), UL = ld2(ur, x - 2), UR = ld2(ur, x + 2);
+      const float2 Uip = mid(U0, UR), Uim = mid(UL, U0);
+      const float2 Ujp = ld2(su[c0][y + 1], x), Ujm = ld2(su[c0][y - 1], x);
+      const float2 Ukp = ld2(su[cp][y], x), Ukm = ld2(su[cm][y], x);
+      const float2 Uimjp = mid(ld2(su[c0][y + 1], x - 2), Ujp), Uimkp = mid(ld2(su[cp][y], x - 2), Ukp);
+      // v
+      const float *vr = sv[c0][y];
+      const float2 V0 = ld2(vr, x), VL = ld2(vr, x - 2), VR = ld2(vr, x + 2);
+      const float2 Vip = mid(V0, VR), Vim = mid(VL, V0);
+      const float2 Vjp = ld2(sv[c0][y + 1], x), Vjm = ld2(sv[c0][y - 1], x);
+      const float2 Vkp = ld2(sv[cp][y], x), Vkm = ld2(sv[cm][y], x);
+      const float2 Vipjm = mid(Vjm, ld2(sv[c0][y - 1], x + 2)), Vjmkp = ld2(sv[cp][y - 1], x);
+      // w
+      const float *wr = sw[c0][y];
+      const float2 W0 = ld2(wr, x), WL = ld2(wr, x - 2), WR = ld2(wr, x + 2);
+      const float2 Wip = mid(W0, WR), Wim = mid(WL, W0);
+      const float2 Wjp = ld2(sw[c0][y + 1], x), Wjm = ld2(sw[c0][y - 1], x);
+      const float2 Wkp = ld2(sw[cp][y], x), Wkm = ld2(sw[cm][y], x);
+      const float2 Wipkm = mid(Wkm, ld2(sw[cm][y], x + 2)), Wjpkm = ld2(sw[cm][y + 1], x);
+      // momxad, momyad, momzad (mom.f90:21-50, 94-123, 170-199), the terms
+      // of k_predict_tiled in packed arithmetic
+      const float2 Puv = mul2(add2(Ujp, U0), add2(Vip, V0));
+      const float2 Puw = mul2(add2(Ukp, U0), add2(Wip, W0));
+      const float2 Pvw = mul2(add2(Wjp, W0), add2(Vkp, V0));
+      auto lap = [&](float2 c, float2 xp, float2 xm, float2 yp, float2 ym, float2 zp, float2 zm) {
+        const float2 dx_ = sub2(sub2(xp, c), sub2(c, xm)), dy_ = sub2(sub2(yp, c), sub2(c, ym)),
+                     dz_ = sub2(sub2(zp, c), sub2(c, zm));
+        return fma2(vdx2, dx_, fma2(vdy2, dy_, mul2(vdz2, dz_)));
+      };
+      auto sqd = [&](float2 a, float2 b) { return fma2(a, a, mul2(f2(-1.f), mul2(b, b))); };  // a^2 - b^2
+      float2 ru_new, rv_new, rw_new;
+      {
+        const float2 sp_ = add2(Uip, U0), sm_ = add2(Uim, U0);
+        ru_new = fma2(qdxi, sqd(sm_, sp_),
+                      fma2(qdyi, sub2(mul2(add2(Ujm, U0), add2(Vipjm, Vjm)), Puv),
+                           fma2(qdzi, sub2(mul2(add2(Ukm, U0), add2(Wipkm, Wkm)), Puw),
+                                lap(U0, Uip, Uim, Ujp, Ujm, Ukp, Ukm))));
+      }
+      {
+        const float2 sp_ = add2(V0, Vjp), sm_ = add2(V0, Vjm);
+        rv_new = fma2(qdxi, sub2(mul2(add2(Uim, Uimjp), add2(V0, Vim)), Puv),
+                      fma2(qdyi, sqd(sm_, sp_),
+                           fma2(qdzi, sub2(mul2(add2(Wkm, Wjpkm), add2(Vkm, V0)), Pvw),
+                                lap(V0, Vip, Vim, Vjp, Vjm, Vkp, Vkm))));
+      }
+      {
+        const float2 sp_ = add2(W0, Wkp), sm_ = add2(W0, Wkm);
+        rw_new = fma2(qdxi, sub2(mul2(add2(W0, Wim), add2(Uim, Uimkp)), Puw),
+                      fma2(qdyi, sub2(mul2(add2(W0, Wjm), add2(Vjm, Vjmkp)), Pvw),
+                           fma2(qdzi, sqd(sm_, sp_), lap(W0, Wip, Wim, Wjp, Wjm, Wkp, Wkm))));
+      }
+      // pressure gradient (momxp/momyp/momzp)
+      const float *pr = sp[k % 2][y];
+      const float2 P0 = ld2(pr, x);
+      const float2 gx = mul2(mdxi, sub2(mid(P0, ld2(pr, x + 2)), P0));
+      const float2 gy = mul2(mdyi, sub2(ld2(sp[k % 2][y + 1], x), P0));
+      const float2 gz = mul2(mdzi, sub2(ld2(sp[(k + 1) % 2][y], x), P0));
+      const int c = k * PL + j * g.I + i;
+      if constexpr (BUOY) {
+        rw_new.x = (float)(bcoef * (cb[c] + cb[c + PL])) + rw_new.x;  // momzbuoy
+        rw_new.y = (float)(bcoef * (cb[c + 1] + cb[c + 1 + PL])) + rw_new.y;
+      }
+      float2 du = fma2(F1, gx, U0), dv = fma2(F1, gy, V0), dw = fma2(F1, gz, W0);
+      if (STAGE == 1) {
+        du = fma2(F1, ru_new, du);
+        dv = fma2(F1, rv_new, dv);
+        dw = fma2(F1, rw_new, dw);
+      } else {
+        const float2 ou = *reinterpret_cast<const float2 *>(ru + c), ov = *reinterpret_cast<const float2 *>(rv + c),
+                     ow = *reinterpret_cast<const float2 *>(rw + c);
+        du = add2(du, fma2(F2, ru_new, mul2(f2(-f3), ou)));
+        dv = add2(dv, fma2(F2, rv_new, mul2(f2(-f3), ov)));
+        dw = add2(dw, fma2(F2, rw_new, mul2(f2(-f3), ow)));
+      }
+      *reinterpret_cast<float2 *>(fu + c) = du;
+      *reinterpret_cast<float2 *>(fv + c) = dv;
+      *reinterpret_cast<float2 *>(fw + c) = dw;
+      if (STAGE != 3) {
+        *reinterpret_cast<float2 *>(ru + c) = ru_new;
+        *reinterpret_cast<float2 *>(rv + c) = rv_new;
+        *reinterpret_cast<float2 *>(rw + c) = rw_new;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
                     T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3, const double *cb,
                     double bcoef) {
   if constexpr (sizeof(T) == 4 && sizeof(TU) == 4) {
     if (g.nfield < (1L << 31)) {
-    dim3 grd((g.I + PTX - 1) / PTX, (g.J + PTY - 1) / PTY, (g.K + PKC - 1) / PKC);
     const float a = (float)f1, b = (float)f2, c = (float)f3;
+    if (g.I % 2 == 0 && predict_pairs()) {
+      dim3 grd((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + QKC - 1) / QKC);
+      auto go = [&](auto kern) {
+        kern<<<grd, QTX / 2 * QTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
+      };
+      if (cb) {
+        if (stage == 1) go(k_predict_pair<1, true>);
+        else if (stage == 2) go(k_predict_pair<2, true>);
+        else go(k_predict_pair<3, true>);
+      } else {
+        if (stage == 1) go(k_predict_pair<1, false>);
+        else if (stage == 2) go(k_predict_pair<2, false>);
+        else go(k_predict_pair<3, false>);
+      }
+      return;
+    }
+    dim3 grd((g.I + PTX - 1) / PTX, (g.J + PTY - 1) / PTY, (g.K + PKC - 1) / PKC);
     auto go = [&](auto kern) { kern<<<grd, PTX * PTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef); };
     if (cb) {
       if (stage == 1) go(k_predict_tiled<1, true>);

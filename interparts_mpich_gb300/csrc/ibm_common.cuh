@@ -64,6 +64,19 @@ __device__ __forceinline__ CompStencil load_cs(const CompStencil *p) {
   return s;
 }
 
+// Mixed form: one Lagrangian point in 16 bytes, written once per substep:
+// the fractions of its grid coordinates x dxi, y dyi, z dzi (FP32, exact
+// from FP64 floors) and the floors themselves as 10-bit offsets (+512) from
+// its particle's reference floor (the floors of the centre's coordinates).
+// Every pass recomputes a component's stencil from it (make_cs).
+struct __align__(16) PointRec {
+  float fx, fy, fz;
+  unsigned rel;  // (nx - refx + 512) | (ny - refy + 512) << 10 | (nz - refz + 512) << 20
+};
+__device__ __forceinline__ int rec_dx(unsigned r) { return (int)(r & 1023u) - 512; }
+__device__ __forceinline__ int rec_dy(unsigned r) { return (int)((r >> 10) & 1023u) - 512; }
+__device__ __forceinline__ int rec_dz(unsigned r) { return (int)((r >> 20) & 1023u) - 512; }
+
 // Constants of one context, passed by value to the kernels.
 struct Geo {
   int I, J, K, MX;            // grid, MX = I/2+1
@@ -105,6 +118,55 @@ __device__ __forceinline__ float delta3f(float r) {
   if (ar > 1.5f) return 0.f;
   if (ar > 0.5f) return (1.f / 6.f) * (5.f - 3.f * ar - sqrtf(-3.f * ((1.f - ar) * (1.f - ar)) + 1.f));
   return (1.f / 3.f) * (1.f + sqrtf(-3.f * (r * r) + 1.f));
+}
+// Stencil of velocity component c (0 u, 1 v, 2 w) of a point, as eulr2lagr
+// forms it (interp_spread.f90:60-131): tap (0,0,0) of the 3x3x3 block
+// relative to the particle's reference floor in x and y and absolute in z
+// (refz: the reference floor in z), and the component's FP32 delta weights.
+// Along the component's own axis the staggered origin (ilows, jlows, klows:
+// the nearest face, max(.,1) in z) and offsets; along the other axes the
+// cell-centred origin (ilow, jlow, klow clamped to [1, K-2], quirk Q5).
+__device__ __forceinline__ CompStencil make_cs(const PointRec &r, int c, int refz, int K) {
+  const int dx = rec_dx(r.rel), dy = rec_dy(r.rel), nz = refz + rec_dz(r.rel);
+  CompStencil s;
+  float o;
+  if (c == 0) {
+    const int ux = r.fx >= 0.5f;
+    s.b[0] = dx + ux - 2;
+    o = r.fx + (float)(1 - ux);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) s.w[m] = delta3f((float)m - o);
+  } else {
+    s.b[0] = dx - 1;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) s.w[m] = delta3f(((float)m - 0.5f) - r.fx);
+  }
+  if (c == 1) {
+    const int uy = r.fy >= 0.5f;
+    s.b[1] = dy + uy - 2;
+    o = r.fy + (float)(1 - uy);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) s.w[3 + m] = delta3f((float)m - o);
+  } else {
+    s.b[1] = dy - 1;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) s.w[3 + m] = delta3f(((float)m - 0.5f) - r.fy);
+  }
+  if (c == 2) {
+    const int uz = r.fz > 0.5f || (r.fz == 0.5f && nz >= 0);
+    const int klows = max(nz + uz - 1, 1);
+    s.b[2] = klows;
+    o = r.fz + (float)(nz - klows);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) s.w[6 + m] = delta3f((float)m - o);
+  } else {
+    const int klow = max(min(nz, K - 2), 1);
+    s.b[2] = klow;
+    o = r.fz + (float)(nz - klow);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) s.w[6 + m] = delta3f(((float)m - 0.5f) - o);
+  }
+  return s;
 }
 // Error-free FP32 transformations (Knuth two-sum, FMA two-product) for
 // double-float arithmetic: a value is carried as hi + lo (about 48 bits) on the

@@ -18,110 +18,100 @@
 
 namespace ibmk {
 
-__device__ __forceinline__ int relwrap(int d, int n) {
-  const int h = n / 2;
-  return d >= h ? d - n : (d < -h ? d + n : d);
-}
 
 // ---------------------------------------------------------------------------
-// Stencil records.  Component c of point t at cs[c*npl + t]:
-//   u: taps (ilows-1+i, jlow-1+j, klow+k),  weights phix,  phiyh, phizh
-//   v: taps (ilow-1+i,  jlows-1+j, klow+k), weights phixh, phiy,  phizh
-//   w: taps (ilow-1+i,  jlow-1+j, klows+k), weights phixh, phiyh, phiz
-// with the stencil origins and delta arguments of eulr2lagr
-// (interp_spread.f90:60-131): x, y indices unwrapped (periodic wrap at use).
+// Point records (16 bytes, PointRec): the fractions of the grid coordinates
+// and the floors relative to the particle's reference floor; make_cs turns
+// one into a component's stencil (origin of the 3x3x3 tap block and the
+// component's 9 delta weights, interp_spread.f90:60-131) whenever a pass
+// needs it, instead of reading 3 x 48-byte records per point and pass.
 // ---------------------------------------------------------------------------
-// one 48-byte record as three 16-byte stores (the layout load_cs reads)
-__device__ __forceinline__ void store_cs(CompStencil *dst, int b0, int b1, int b2, const float *wx, const float *wy,
-                                         const float *wz) {
-  float4 *q = reinterpret_cast<float4 *>(dst);
-  q[0] = make_float4(__int_as_float(b0), __int_as_float(b1), __int_as_float(b2), wx[0]);
-  q[1] = make_float4(wx[1], wx[2], wy[0], wy[1]);
-  q[2] = make_float4(wy[2], wz[0], wz[1], wz[2]);
+__device__ __forceinline__ int4 particle_ref(const Geo &g, const PartGeo &pg, const double *pf, int p) {
+  return make_int4(__double2int_rd(pf[PF_X * pg.np + p] * g.dxi), __double2int_rd(pf[PF_Y * pg.np + p] * g.dyi),
+                   __double2int_rd(pf[PF_Z * pg.np + p] * g.dzi), 0);
 }
-
-__global__ void __launch_bounds__(256) k_ibm_stencil_c(Geo g, PartGeo pg, IbmBuffers b) {
+__global__ void __launch_bounds__(256) k_ibm_points(Geo g, PartGeo pg, IbmBuffers b) {
   const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
+    const int4 ref = particle_ref(g, pg, b.pf, p);
+    if (l == 0) b.pref[p] = ref;
     if (l >= b.nla[p]) continue;
-    const double xfp = b.xfp[t], yfp = b.yfp[t], zfp = b.zfp[t];
-    // periodic image: a point within half a cell of the domain (the only
-    // case that occurs) is shifted by -1, 0 or +1 periods; any image whose
-    // coordinate stays in [0, I+1] addresses the same (wrapped) cells with
-    // the same weights, so the comparison need not agree with a rounded
-    // division at the boundary itself
-    const double sx = xfp - 0.5 * g.dx, sy = yfp - 0.5 * g.dy;
-    double coorxfp = xfp * g.dxi - (sx < 0. ? -(double)g.I : (sx >= g.lx ? (double)g.I : 0.));
-    double cooryfp = yfp * g.dyi - (sy < 0. ? -(double)g.J : (sy >= g.ly ? (double)g.J : 0.));
-    double coorzfp = zfp * g.dzi;
-    // floor n and exact fraction f = c - n of each coordinate (FP64 issues
-    // at a small fraction of the FP32 rate: the origins and range checks
-    // follow from n and f with integer and FP32 work); NINT rounds half
-    // away from zero
-    int nx = __double2int_rd(coorxfp), ny = __double2int_rd(cooryfp), nz = __double2int_rd(coorzfp);
-    double frx = coorxfp - (double)nx, fry = cooryfp - (double)ny, frz = coorzfp - (double)nz;
-    if (!(nx >= 0 && (nx <= g.I || (nx == g.I + 1 && frx == 0.))) ||
-        !(ny >= 0 && (ny <= g.J || (ny == g.J + 1 && fry == 0.))) || !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
+    const double cx = b.xfp[t] * g.dxi, cy = b.yfp[t] * g.dyi, cz = b.zfp[t] * g.dzi;
+    // floors and exact fractions; the range check as the periodic image
+    // the reference would take (a point within half a cell of the domain is
+    // shifted by one period; interp_spread.f90:60-104)
+    int nx = __double2int_rd(cx), ny = __double2int_rd(cy), nz = __double2int_rd(cz);
+    double frx = cx - (double)nx, fry = cy - (double)ny, frz = cz - (double)nz;
+    const double sx = b.xfp[t] - 0.5 * g.dx, sy = b.yfp[t] - 0.5 * g.dy;
+    const int ix = nx + (sx < 0. ? g.I : (sx >= g.lx ? -g.I : 0)), iy = ny + (sy < 0. ? g.J : (sy >= g.ly ? -g.J : 0));
+    const int ddx = nx - ref.x, ddy = ny - ref.y, ddz = nz - ref.z;
+    if (!(ix >= 0 && (ix <= g.I || (ix == g.I + 1 && frx == 0.))) ||
+        !(iy >= 0 && (iy <= g.J || (iy == g.J + 1 && fry == 0.))) || !(cz >= -1. && cz <= g.K + 0.49) ||
+        ddx < -510 || ddx > 510 || ddy < -510 || ddy > 510 || ddz < -510 || ddz > 510) {
       atomicExch(&b.err[2], 1);
-      nx = 1; ny = 1; nz = 1; frx = 0.; fry = 0.; frz = 0.5;
+      nx = ref.x; ny = ref.y; nz = max(min(ref.z, g.K - 1), 1); frx = 0.; fry = 0.; frz = 0.5;
     }
-    const int ux = frx > 0.5 || (frx == 0.5 && nx >= 0), uy = fry > 0.5 || (fry == 0.5 && ny >= 0),
-              uz = frz > 0.5 || (frz == 0.5 && nz >= 0);
-    const int ilows = nx + ux - 1, jlows = ny + uy - 1, klows = max(nz + uz - 1, 1);
-    const int ilow = nx, jlow = ny;
-    const int klow = max(min(nz, g.K - 2), 1);
-    // offsets of the point from the stencil origins: the FP32 fraction plus
-    // the small integer between floor and origin (0, 1 or 2)
-    const float fx = (float)frx, fy = (float)fry, fz = (float)frz;
-    const float ox = fx + (float)(nx - ilows), oy = fy + (float)(ny - jlows), oz = fz + (float)(nz - klows);
-    const float hx = fx, hy = fy, hz = fz + (float)(nz - klow);
-    float phix[3], phiy[3], phiz[3], phixh[3], phiyh[3], phizh[3];
-    for (int m = 0; m < 3; ++m) {
-      phix[m] = delta3f((float)m - ox);
-      phiy[m] = delta3f((float)m - oy);
-      phiz[m] = delta3f((float)m - oz);
-      phixh[m] = delta3f(((float)m - 0.5f) - hx);
-      phiyh[m] = delta3f(((float)m - 0.5f) - hy);
-      phizh[m] = delta3f(((float)m - 0.5f) - hz);
-    }
-    const long npl = (long)n;
-    store_cs(b.cs + t, ilows - 1, jlow - 1, klow, phix, phiyh, phizh);
-    store_cs(b.cs + npl + t, ilow - 1, jlows - 1, klow, phixh, phiy, phizh);
-    store_cs(b.cs + 2 * npl + t, ilow - 1, jlow - 1, klows, phixh, phiyh, phiz);
+    PointRec r;
+    r.fx = (float)frx;
+    r.fy = (float)fry;
+    r.fz = (float)frz;
+    r.rel = (unsigned)(nx - ref.x + 512) | ((unsigned)(ny - ref.y + 512) << 10) | ((unsigned)(nz - ref.z + 512) << 20);
+    b.rec[t] = r;
   }
 }
 
 // Box of the cells the stencils of particle p, component c touch:
 // bgeo[(p*3 + c)*8 + ] = {refx, refy, bmin_x, bmin_y, bmin_z, nbx, nby, nbz};
-// x, y relative to the first point's origin (periodic), box cell (cx,cy,cz)
-// = tap (refx + bmin_x + cx, refy + bmin_y + cy, bmin_z + cz).
-__global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, int I, int J) {
+// x, y relative to the particle's reference floor, box cell (cx,cy,cz) =
+// tap (refx + bmin_x + cx, refy + bmin_y + cy, bmin_z + cz).  With at most
+// IBM_BOX_ROWS rows, rowx[(p*3 + c)*IBM_BOX_ROWS + cz*nby + cy] = the x
+// extent (first, last cell) the stencils touch in that row (first > last:
+// none): a sphere's shell touches about 40 % of its box.
+__global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, int K) {
   const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
-  const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
-  const CompStencil *cs = b.cs + c * npl + t0;
+  const PointRec *rp = b.rec + (long)p * pg.nl;
   __shared__ int mn[3], mx[3];
+  __shared__ int rlo[IBM_BOX_ROWS], rhi[IBM_BOX_ROWS];
   if (threadIdx.x < 3) { mn[threadIdx.x] = 0x7fffffff; mx[threadIdx.x] = -0x7fffffff; }
+  for (int q = threadIdx.x; q < IBM_BOX_ROWS; q += blockDim.x) { rlo[q] = 0x7fff; rhi[q] = -1; }
   __syncthreads();
-  const int refx = nla > 0 ? cs[0].b[0] : 0, refy = nla > 0 ? cs[0].b[1] : 0;
+  const int4 ref = b.pref[p];
   int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
-    const int4 o = *reinterpret_cast<const int4 *>(&cs[l]);  // b[0..2] (+ w[0])
-    const int r[3] = {relwrap(o.x - refx, I), relwrap(o.y - refy, J), o.z};
-    for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], r[d]); hi[d] = max(hi[d], r[d]); }
+    const CompStencil s = make_cs(rp[l], c, ref.z, K);
+    for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], s.b[d]); hi[d] = max(hi[d], s.b[d]); }
   }
   for (int d = 0; d < 3; ++d) {
     const int wl = __reduce_min_sync(0xffffffffu, lo[d]), wh = __reduce_max_sync(0xffffffffu, hi[d]);
     if ((threadIdx.x & 31) == 0) { atomicMin(&mn[d], wl); atomicMax(&mx[d], wh); }
   }
   __syncthreads();
+  const int nby = mx[1] - mn[1] + 3, nbz = mx[2] - mn[2] + 3;
+  if (nla > 0 && nby * nbz <= IBM_BOX_ROWS) {
+    for (int l = threadIdx.x; l < nla; l += blockDim.x) {
+      const CompStencil s = make_cs(rp[l], c, ref.z, K);
+      const int x0 = s.b[0] - mn[0], y0 = s.b[1] - mn[1], z0 = s.b[2] - mn[2];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int row = (z0 + k) * nby + y0 + j;
+          atomicMin(&rlo[row], x0);
+          atomicMax(&rhi[row], x0 + 2);
+        }
+    }
+    __syncthreads();
+    short2 *rx = b.rowx + ((long)p * 3 + c) * IBM_BOX_ROWS;
+    for (int q = threadIdx.x; q < nby * nbz; q += blockDim.x) rx[q] = make_short2((short)rlo[q], (short)rhi[q]);
+  }
   if (threadIdx.x == 0) {
     int *o = b.bgeo + ((long)p * 3 + c) * 8;
-    o[0] = refx; o[1] = refy;
+    o[0] = ref.x; o[1] = ref.y;
     if (nla > 0) {
       o[2] = mn[0]; o[3] = mn[1]; o[4] = mn[2];
-      o[5] = mx[0] - mn[0] + 3; o[6] = mx[1] - mn[1] + 3; o[7] = mx[2] - mn[2] + 3;
+      o[5] = mx[0] - mn[0] + 3; o[6] = nby; o[7] = nbz;
     } else {
       o[2] = o[3] = o[4] = o[5] = o[6] = o[7] = 0;
     }
@@ -130,8 +120,8 @@ __global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, 
 
 void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b) {
   if (pg.np == 0) return;
-  k_ibm_stencil_c<<<1216, 256, 0, s>>>(g, pg, b);
-  k_ibm_box_geom<<<dim3(pg.np, 3), 256, 0, s>>>(pg, b, g.I, g.J);
+  k_ibm_points<<<1216, 256, 0, s>>>(g, pg, b);
+  k_ibm_box_geom<<<dim3(pg.np, 3), 256, 0, s>>>(pg, b, g.K);
 }
 
 // box usable in shared memory: fits cap and narrower than half the periodic
@@ -139,23 +129,30 @@ void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBu
 __device__ __forceinline__ bool box_ok(const int *bg, int cap, int I, int J) {
   return bg[5] > 0 && (long)bg[5] * bg[6] * bg[7] <= cap && bg[5] < I / 2 && bg[6] < J / 2;
 }
-// offset of tap (0,0,0) of a point in its particle's box
-__device__ __forceinline__ int box_off(const CompStencil &s, const int *bg, int I, int J) {
-  const int cx = relwrap(s.b[0] - bg[0], I) - bg[2], cy = relwrap(s.b[1] - bg[1], J) - bg[3];
-  return ((s.b[2] - bg[4]) * bg[6] + cy) * bg[5] + cx;
+// offset of tap (0,0,0) of a point (make_cs origin, relative in x and y) in
+// its particle's box
+__device__ __forceinline__ int box_off(const CompStencil &s, const int *bg) {
+  return ((s.b[2] - bg[4]) * bg[6] + (s.b[1] - bg[3])) * bg[5] + (s.b[0] - bg[2]);
 }
-__device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__ F, const int *bg, float *box) {
+__device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__ F, const int *bg, float *box,
+                                         const short2 *__restrict__ rowx) {
   const int nbx = bg[5], nby = bg[6], nxy = nbx * nby, nbox = nxy * bg[7];
   const int x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
   if ((g.I & 3) == 0) {
     // rows read as 16-byte quads of x-cells (aligned: I is a multiple of 4,
     // so a quad never straddles the periodic wrap); cells outside the row
-    // are dropped
+    // are dropped, and so are quads outside the row's recorded extent (the
+    // cells no stencil reads)
     const int a0 = x0 - (((x0 % 4) + 4) % 4);
     const int nq = (x0 + nbx - a0 + 3) >> 2, nrow = nby * bg[7];
+    const bool ext = nrow <= IBM_BOX_ROWS;
     for (int e = threadIdx.x; e < nrow * nq; e += blockDim.x) {
       const int row = e / nq, t = e - row * nq;
       const int cz = row / nby, cy = row - cz * nby, gx = a0 + 4 * t;
+      if (ext) {
+        const short2 xr = rowx[row];
+        if (gx + 3 - x0 < xr.x || gx - x0 > xr.y) continue;
+      }
       const float4 v =
           __ldg(reinterpret_cast<const float4 *>(&F[fidx(g, wrapm(gx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]));
       const float vv[4] = {v.x, v.y, v.z, v.w};
@@ -172,6 +169,17 @@ __device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__
     box[q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
   }
 }
+// Offset of a point from its particle's centre along one axis (FP64, from the
+// record: floor + FP32 fraction in grid units)
+__device__ __forceinline__ double rec_arm(int ref, int d, float fr, double h, double centre) {
+  return ((double)(ref + d) + (double)fr) * h - centre;
+}
+// rigid-body velocity component of point t: the particle's, or with rotation
+// on the per-point value (u + omega x r, updated with the points)
+__device__ __forceinline__ double point_u(const PartGeo &pg, const double *Ua, double Up, long t) {
+  return pg.rotation ? Ua[t] : Up;
+}
+
 // 27-tap interpolation of one component, k outer, j, i inner, each term
 // f * (wx_i * (wy_j * wz_k))
 template <typename TAP>
@@ -252,47 +260,57 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
   __syncthreads();
   const bool boxed = box_ok(bg, INTERP_BOX, g.I, g.J);
   if (boxed) {
-    load_box(g, F, bg, box);
+    load_box(g, F, bg, box, b.rowx + ((long)p * 3 + c) * IBM_BOX_ROWS);
     __syncthreads();
   }
   double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
-  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
+  const double *Ua = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
   double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
+  float *slip = b.slip + c * npl;
   const double *pf = b.pf;
   const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
-  const CompStencil *csp = b.cs + c * npl + t0;
+  const double Up = pf[(c == 0 ? PF_U : (c == 1 ? PF_V : PF_W)) * pg.np + p];
+  const int4 ref = b.pref[p];
+  const PointRec *rp = b.rec + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
   double sF = 0., sa = 0., sb = 0.;
   float r2 = 0.f, r0 = 0.f;
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const long t = t0 + l;
-    const CompStencil s = load_cs(csp + l);
+    const PointRec rr = rp[l];
+    const CompStencil s = make_cs(rr, c, ref.z, g.K);
     float acc;
     if (boxed) {
-      const float *B = box + box_off(s, bg, g.I, g.J);
+      const float *B = box + box_off(s, bg);
       acc = interp27(s, [&](int i, int j, int k) { return B[i + j * ys + k * zs]; });
     } else {
       acc = interp27(s, [&](int i, int j, int k) {
-        return __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
+        return __ldg(&F[fidx(g, wrapm(ref.x + s.b[0] + i, g.I), wrapm(ref.y + s.b[1] + j, g.J), s.b[2] + k)]);
       });
     }
+    const double U = point_u(pg, Ua, Up, t);
     if (first == -1) {  // residual only: sum of (U - u~)^2 of the component
-      const float e = (float)U[t] - acc;
+      const float e = (float)U - acc;
       r2 = fmaf(e, e, r2);
       continue;
     }
-    dud[t] = acc;
-    if (first < 0) continue;
+    if (first < 0) {  // the interpolation only (diagnostics)
+      dud[t] = acc;
+      continue;
+    }
+    const double sd = U - acc;
+    slip[t] = (float)sd;  // the spreading's increment (U - u~)/dt, FP32
     if (first) {  // first-pass slip, for the learned loop's gate reference
-      const float e = (float)U[t] - acc;
+      const float e = (float)sd;
       r0 = fmaf(e, e, r0);
     }
-    const double f = first ? (U[t] - acc) * dti : Fl[t] + (U[t] - acc) * dti;
+    const double f = first ? sd * dti : Fl[t] + sd * dti;
     Fl[t] = f;
     // lever arms of the torque terms of this component:
     // c=0: (rz, ry), c=1: (rz, rx), c=2: (ry, rx)
-    const double la = c == 2 ? b.yfp[t] - py : b.zfp[t] - pz;
-    const double lb = c == 0 ? b.yfp[t] - py : b.xfp[t] - px;
+    const double ry = rec_arm(ref.y, rec_dy(rr.rel), rr.fy, g.dy, py);
+    const double la = c == 2 ? ry : rec_arm(ref.z, rec_dz(rr.rel), rr.fz, g.dz, pz);
+    const double lb = c == 0 ? ry : rec_arm(ref.x, rec_dx(rr.rel), rr.fx, g.dx, px);
     sF += f;
     sa += la * f;
     sb += lb * f;
@@ -411,10 +429,10 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     for (int q = threadIdx.x; q < nbox; q += blockDim.x) box[q] = 0.f;
     __syncthreads();
   }
-  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
-  const double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
+  const float *slip = b.slip + c * npl;
   double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
-  const CompStencil *csp = b.cs + c * npl + t0;
+  const int4 ref = b.pref[p];
+  const PointRec *rp = b.rec + t0;
   double sF = 0., sa = 0., sb = 0.;
   double px = 0., py = 0., pz = 0.;
   float ysig = 0.f, ymu = 0.f;
@@ -446,29 +464,32 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
       Fl[t] = f;
       const float e0 = (float)(f0 * dt_l);  // the first pass's slip U - u~
       r0 = fmaf(e0, e0, r0);
-      const double la = c == 2 ? b.yfp[t] - py : b.zfp[t] - pz;
-      const double lb = c == 0 ? b.yfp[t] - py : b.xfp[t] - px;
+      const PointRec rr = rp[l];
+      const double ry = rec_arm(ref.y, rec_dy(rr.rel), rr.fy, g.dy, py);
+      const double la = c == 2 ? ry : rec_arm(ref.z, rec_dz(rr.rel), rr.fz, g.dz, pz);
+      const double lb = c == 0 ? ry : rec_arm(ref.x, rec_dx(rr.rel), rr.fx, g.dx, px);
       sF += f;
       sa += la * f;
       sb += lb * f;
       pre = (float)(lf.incr ? d : f) * pcoef;
     } else {
-      pre = (float)(U[t] - dud[t]) * ucoef;
+      pre = slip[t] * ucoef;
     }
     if (staged) {
       spre[l] = pre;
       asum += fabsf(pre);
       continue;
     }
-    const CompStencil s = load_cs(csp + l);
+    const CompStencil s = make_cs(rp[l], c, ref.z, g.K);
     if (boxed) {
-      spread27_box<false>(box, s, box_off(s, bg, g.I, g.J), nbx, nby, pre);
+      spread27_box<false>(box, s, box_off(s, bg), nbx, nby, pre);
     } else {
       for (int k = 0; k < 3; ++k)
         for (int j = 0; j < 3; ++j) {
           const float a = pre * s.w[3 + j] * s.w[6 + k];
-          const int y = wrapm(s.b[1] + j, g.J);
-          for (int i = 0; i < 3; ++i) atomicAdd(&F[fidx(g, wrapm(s.b[0] + i, g.I), y, s.b[2] + k)], a * s.w[i]);
+          const int y = wrapm(ref.y + s.b[1] + j, g.J);
+          for (int i = 0; i < 3; ++i)
+            atomicAdd(&F[fidx(g, wrapm(ref.x + s.b[0] + i, g.I), y, s.b[2] + k)], a * s.w[i]);
         }
     }
   }
@@ -495,8 +516,8 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     for (int m = threadIdx.x; m < 32 * nq; m += blockDim.x) {
       const int l = (m & 31) * nq + (m >> 5);
       if (l >= nla) continue;
-      const CompStencil s = load_cs(csp + l);
-      const int o = box_off(s, bg, g.I, g.J);
+      const CompStencil s = make_cs(rp[l], c, ref.z, g.K);
+      const int o = box_off(s, bg);
       if (scale > 0.f) spread27_box<true>(box, s, o, nbx, nby, spre[l] * scale);
       else spread27_box<false>(box, s, o, nbx, nby, spre[l]);
     }
@@ -559,11 +580,10 @@ void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b) {
 // network.  The interpolated velocity goes to dudtl as eulr2lagr would;
 // with first_force the first pass's point force F0 = (U - u~)/dt as well
 // (complagrforces), so the feature kernel is that pass's interpolation.
-// k_ibm_features_comp (one block per particle and component, on the
-// particle's shared-memory box) serves the learned loop; k_ibm_features_f
-// (one thread per point, all components) serves the harvest, which also
-// stores every stride-th point's raw FP32 features and index for the target
-// written after the plain passes.
+// k_ibm_features_f (one thread per point, all components) serves the
+// harvest, which also stores every stride-th point's raw FP32 features and
+// index for the target written after the plain passes; the learned loop
+// forms the same features inside the tensor-core inference kernel.
 // ---------------------------------------------------------------------------
 struct FeatSink {
   __nv_bfloat16 *x;  // row of the standardised features (or null)
@@ -600,7 +620,6 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
                                                         __nv_bfloat16 *__restrict__ X, HarvestArgs H,
                                                         int first_force) {
   const int n = pg.np * pg.nl;
-  const long npl = n;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
     if (l >= b.nla[p]) {
@@ -621,32 +640,35 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
         H.pidx[h] = t;
       }
     }
-    const CompStencil su = load_cs(b.cs + t), sv = load_cs(b.cs + npl + t), sw = load_cs(b.cs + 2 * npl + t);
+    const int4 ref = b.pref[p];
+    const PointRec rr = b.rec[t];
     auto tap = [&](const float *F, const CompStencil &s, int i, int j, int k) {
-      return __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
+      return __ldg(&F[fidx(g, wrapm(ref.x + s.b[0] + i, g.I), wrapm(ref.y + s.b[1] + j, g.J), s.b[2] + k)]);
     };
+    const double *pf = b.pf;
+    const double Up[3] = {pf[PF_U * pg.np + p], pf[PF_V * pg.np + p], pf[PF_W * pg.np + p]};
+    const double *Ua[3] = {b.ul, b.vl, b.wl};
     if (!snk.x && !snk.raw) {  // interpolation (and the first-pass force) only
-      const float iu = interp27(su, [&](int i, int j, int k) { return tap(fu, su, i, j, k); });
-      const float iv = interp27(sv, [&](int i, int j, int k) { return tap(fv, sv, i, j, k); });
-      const float iw = interp27(sw, [&](int i, int j, int k) { return tap(fw, sw, i, j, k); });
-      b.dudtl[t] = iu; b.dvdtl[t] = iv; b.dwdtl[t] = iw;
-      if (first_force) {
-        b.fxl[t] = (b.ul[t] - iu) * dti; b.fyl[t] = (b.vl[t] - iv) * dti; b.fzl[t] = (b.wl[t] - iw) * dti;
+      for (int c = 0; c < 3; ++c) {
+        const CompStencil s = make_cs(rr, c, ref.z, g.K);
+        const float a = interp27(s, [&](int i, int j, int k) { return tap(c == 0 ? fu : (c == 1 ? fv : fw), s, i, j, k); });
+        (c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl))[t] = a;
+        if (first_force) (c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl))[t] = (point_u(pg, Ua[c], Up[c], t) - a) * dti;
       }
       continue;
     }
-    const double px = b.pf[PF_X * pg.np + p], py = b.pf[PF_Y * pg.np + p], pz = b.pf[PF_Z * pg.np + p];
-    const float nrm[3] = {(float)(b.xfp[t] - px) * inv_r, (float)(b.yfp[t] - py) * inv_r,
-                          (float)(b.zfp[t] - pz) * inv_r};
-    const CompStencil *cs3[3] = {&su, &sv, &sw};
+    const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
+    const float nrm[3] = {(float)rec_arm(ref.x, rec_dx(rr.rel), rr.fx, g.dx, px) * inv_r,
+                          (float)rec_arm(ref.y, rec_dy(rr.rel), rr.fy, g.dy, py) * inv_r,
+                          (float)rec_arm(ref.z, rec_dz(rr.rel), rr.fz, g.dz, pz) * inv_r};
     const float *F3[3] = {fu, fv, fw};
-    const double *U3[3] = {b.ul, b.vl, b.wl};
     double *D3[3] = {b.dudtl, b.dvdtl, b.dwdtl};
     double *Fl3[3] = {b.fxl, b.fyl, b.fzl};
 #pragma unroll 1
     for (int c = 0; c < 3; ++c) {
-      const CompStencil &s = *cs3[c];
-      const float Uc = (float)U3[c][t];
+      const CompStencil s = make_cs(rr, c, ref.z, g.K);
+      const double Ud = point_u(pg, Ua[c], Up[c], t);
+      const float Uc = (float)Ud;
       float acc = 0.f;
 #pragma unroll
       for (int k = 0; k < 3; ++k)
@@ -661,7 +683,7 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
           }
         }
       D3[c][t] = acc;
-      if (first_force) Fl3[c][t] = (U3[c][t] - acc) * dti;
+      if (first_force) Fl3[c][t] = (Ud - acc) * dti;
       snk.put(Uc - acc);
       snk.put(Uc);
       snk.put(nrm[c]);
@@ -680,99 +702,12 @@ void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmB
                                         first_force);
 }
 
-// Features of the learned loop, one block per (particle, component) on the
-// particle's box (same values and order as k_ibm_features_f); also the first
-// pass's interpolation and point forces F0.
-__global__ void __launch_bounds__(256, 4) k_ibm_features_comp(Geo g, PartGeo pg, IbmBuffers b,
-                                                           const float *__restrict__ fu,
-                                                           const float *__restrict__ fv,
-                                                           const float *__restrict__ fw, double dt, double dti, float inv_r,
-                                                           const float *__restrict__ mu,
-                                                           const float *__restrict__ isig,
-                                                           __nv_bfloat16 *__restrict__ X) {
-  const int p = blockIdx.x, c = blockIdx.y;
-  const int nla = b.nla[p];
-  const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
-  const float *F = c == 0 ? fu : (c == 1 ? fv : fw);
-  extern __shared__ __align__(16) unsigned char ibox_sm[];
-  float *box = reinterpret_cast<float *>(ibox_sm);
-  __shared__ int bg[8];
-  __shared__ float smu[32], sis[32];
-  if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
-  if (threadIdx.x < 32) { smu[threadIdx.x] = mu[32 * c + threadIdx.x]; sis[threadIdx.x] = isig[32 * c + threadIdx.x]; }
-  __syncthreads();
-  const bool boxed = box_ok(bg, INTERP_BOX, g.I, g.J);
-  if (boxed) {
-    load_box(g, F, bg, box);
-    __syncthreads();
-  }
-  double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
-  const double *U = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
-  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
-  const double *xc = c == 0 ? b.xfp : (c == 1 ? b.yfp : b.zfp);
-  const double pc = b.pf[(c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z)) * pg.np + p];
-  const CompStencil *csp = b.cs + c * npl + t0;
-  const int ys = bg[5], zs = bg[5] * bg[6];
-  for (int l = threadIdx.x; l < pg.nl; l += blockDim.x) {
-    const long t = t0 + l;
-    __nv_bfloat16 *xr = X + t * 96 + 32 * c;
-    if (l >= nla) {
-      for (int q = 0; q < 32; q += 8) *reinterpret_cast<uint4 *>(xr + q) = make_uint4(0, 0, 0, 0);
-      continue;
-    }
-    const CompStencil s = load_cs(csp + l);
-    const float Uc = (float)U[t];
-    const float *B = boxed ? box + box_off(s, bg, g.I, g.J) : nullptr;
-    float f[32];
-    float acc = 0.f;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const float wyz = s.w[3 + j] * s.w[6 + k];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float tv = boxed ? B[i + j * ys + k * zs]
-                                 : __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), wrapm(s.b[1] + j, g.J), s.b[2] + k)]);
-          acc += tv * (s.w[i] * wyz);
-          f[(k * 3 + j) * 3 + i] = tv - Uc;
-        }
-      }
-    dud[t] = acc;
-    const double F0 = (U[t] - acc) * dti;
-    Fl[t] = F0;
-    f[27] = Uc - acc;
-    f[28] = Uc;
-    f[29] = (float)(xc[t] - pc) * inv_r;
-    f[30] = (float)F0 * (float)dt;
-    f[31] = s.w[3 * c + 1];
-#pragma unroll
-    for (int q = 0; q < 32; q += 8) {
-      __nv_bfloat162 h[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-        h[e] = __floats2bfloat162_rn((f[q + 2 * e] - smu[q + 2 * e]) * sis[q + 2 * e],
-                                     (f[q + 2 * e + 1] - smu[q + 2 * e + 1]) * sis[q + 2 * e + 1]);
-      *reinterpret_cast<uint4 *>(xr + q) = *reinterpret_cast<const uint4 *>(h);
-    }
-  }
-}
-void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
-                              const float *fv, const float *fw, double dt, const float *mu, const float *isig,
-                              __nv_bfloat16 *X) {
-  if (pg.np == 0) return;
-  k_ibm_features_comp<<<dim3(pg.np, 3), 256, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, dt, 1. / dt,
-                                                                              (float)(1. / pg.radfp), mu, isig, X);
-}
-
 int ibm_set_smem_limits() {
   cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         SPREAD_BOX * (int)sizeof(float));
   cudaError_t e2 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         INTERP_BOX * (int)sizeof(float));
-  cudaError_t e3 = cudaFuncSetAttribute(k_ibm_features_comp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        INTERP_BOX * (int)sizeof(float));
-  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
+  return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
 }
 
 }  // namespace ibmk

@@ -74,12 +74,18 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
 template <typename T> int poisson_set_smem_limits();
 
 // ibm_kernels.cu
+// rows (y, z) of a particle's box with a recorded x extent; boxes with more
+// rows are read whole
+constexpr int IBM_BOX_ROWS = 1024;
 struct IbmBuffers {
   // per-point arrays [np*nl]
   double *xfp, *yfp, *zfp, *ul, *vl, *wl, *dudtl, *dvdtl, *dwdtl, *fxl, *fyl, *fzl;
   PointStencil *st;
-  CompStencil *cs;   // mixed form: [3][np*nl] per-component stencils
+  PointRec *rec;     // mixed form: [np*nl] compact point records (make_cs)
+  int4 *pref;        // mixed form: [np] reference floors (refx, refy, refz) of the particles
+  float *slip;       // mixed form: [3][np*nl] slip U - u~ of the last pass (FP32)
   int *bgeo;         // mixed form: [np][3][8] per-particle stencil boxes
+  short2 *rowx;      // mixed form: [np][3][IBM_BOX_ROWS] x extent of every box row the stencils touch
   int *nla;          // [np]
   double *pf;        // particle scalar fields [PF_N*np]
   double *diag;      // [8] force totals etc.
@@ -130,9 +136,6 @@ struct HarvestArgs {
 void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                            const float *fv, const float *fw, double dt, const float *mu, const float *isig,
                            __nv_bfloat16 *X, const HarvestArgs &H, int first_force = 0);
-void launch_ibm_features_comp(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
-                              const float *fv, const float *fw, double dt, const float *mu, const float *isig,
-                              __nv_bfloat16 *X);
 void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs &H, double dt);
 // Residual gate from the per-(particle, component) sums of (U - u~)^2 that
 // the interpolation with first < 0 leaves in psum[p][c][0] and the sums of
@@ -172,12 +175,13 @@ struct FeatIn {
   Geo g;
   int np, nl;
   const int *nla;
-  const CompStencil *cs;
+  const PointRec *rec;
+  const int4 *pref;
+  int rotation;        // 0: U is the particle velocity; 1: read U[] (with the rotation term)
   const float *F[3];   // u, v, w (FP32 fields)
-  const double *U[3];  // rigid-body velocity at the points
-  const double *X[3];  // point coordinates
-  const double *pf;    // particle scalar fields (centres)
-  double *dud[3], *Fl[3];
+  const double *U[3];  // rigid-body velocity at the points (read with rotation on)
+  const double *pf;    // particle scalar fields (centres, velocities)
+  double *Fl[3];
   double dt, dti;
   float inv_r;
   const float *mu, *isig;  // feature standardisation

@@ -507,10 +507,10 @@ __device__ __forceinline__ void gelu2_store32(const float v[32], const uint32_t 
   }
 }
 
-// The 96 features of point t (see k_ibm_features_comp: the 27 taps minus U,
-// U - u~, U, the normal component, F0 dt and the centre weight of each
-// velocity component, standardised and rounded to BF16) into row r of the
-// K-major operand tile, with the first pass's interpolation to dudtl and
+// The 96 features of point t (as k_ibm_features_f forms them: the 27 taps
+// minus U, U - u~, U, the normal component, F0 dt and the centre weight of
+// each velocity component, standardised and rounded to BF16) into row r of
+// the K-major operand tile, with the first pass's point force
 // F0 = (U - u~)/dt to fxl.  Taps are read from the fields directly (the
 // 3-float rows of a stencil share cache lines with the tile's neighbouring
 // points).  Rows beyond the points, or points not active (l >= nla), get
@@ -524,11 +524,14 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
     return;
   }
   const Geo &g = fi.g;
+  const int4 ref = fi.pref[p];
+  const PointRec rr = fi.rec[t];
 #pragma unroll 1
   for (int c = 0; c < 3; ++c) {
-    const CompStencil s = load_cs(fi.cs + c * npl + t);
+    const CompStencil s = make_cs(rr, c, ref.z, g.K);
     const float *F = fi.F[c];
-    const double Ud = fi.U[c][t];
+    const int pc = c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z);
+    const double Ud = fi.rotation ? fi.U[c][t] : fi.pf[(PF_U + c) * fi.np + p];
     const float Uc = (float)Ud;
     float f[FEAT_PER_COMP];
     float acc = 0.f;
@@ -537,20 +540,23 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         const float wyz = s.w[3 + j] * s.w[6 + k];
-        const int y = wrapm(s.b[1] + j, g.J);
+        const int y = wrapm(ref.y + s.b[1] + j, g.J);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const float tv = __ldg(&F[fidx(g, wrapm(s.b[0] + i, g.I), y, s.b[2] + k)]);
+          const float tv = __ldg(&F[fidx(g, wrapm(ref.x + s.b[0] + i, g.I), y, s.b[2] + k)]);
           acc += tv * (s.w[i] * wyz);
           f[(k * 3 + j) * 3 + i] = tv - Uc;
         }
       }
-    fi.dud[c][t] = acc;
     const double F0 = (Ud - acc) * fi.dti;
     fi.Fl[c][t] = F0;
     f[27] = Uc - acc;
     f[28] = Uc;
-    f[29] = (float)(fi.X[c][t] - fi.pf[(c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z)) * fi.np + p]) * fi.inv_r;
+    const int dc = c == 0 ? rec_dx(rr.rel) : (c == 1 ? rec_dy(rr.rel) : rec_dz(rr.rel));
+    const float frc = c == 0 ? rr.fx : (c == 1 ? rr.fy : rr.fz);
+    const int refc = c == 0 ? ref.x : (c == 1 ? ref.y : ref.z);
+    const double hc = c == 0 ? g.dx : (c == 1 ? g.dy : g.dz);
+    f[29] = (float)(((double)(refc + dc) + (double)frc) * hc - fi.pf[pc * fi.np + p]) * fi.inv_r;
     f[30] = (float)F0 * (float)fi.dt;
     f[31] = s.w[3 * c + 1];
     const float *mu = fi.mu + FEAT_PER_COMP * c, *is = fi.isig + FEAT_PER_COMP * c;
