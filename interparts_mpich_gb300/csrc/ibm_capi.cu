@@ -424,6 +424,7 @@ int alloc_all(ibm_ctx *c) {
     if (c->mixed) {
       if ((st = dalloc(c, &c->ib.rec, npl))) return st;
       if ((st = dalloc(c, &c->ib.pref, (size_t)np))) return st;
+      if ((st = dalloc(c, &c->ib.pcen, (size_t)np))) return st;
       if ((st = dalloc(c, &c->ib.slip, 3 * npl))) return st;
       if ((st = dalloc(c, &c->ib.bgeo, (size_t)24 * np))) return st;
       if ((st = dalloc(c, &c->ib.rowx, (size_t)3 * IBM_BOX_ROWS * np))) return st;
@@ -547,6 +548,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   fi.nla = c->ib.nla;
   fi.rec = c->ib.rec;
   fi.pref = c->ib.pref;
+  fi.pcen = c->ib.pcen;
   fi.rotation = c->pg.rotation;
   fi.F[0] = c->fu32; fi.F[1] = c->fv32; fi.F[2] = c->fw32;
   fi.U[0] = c->ib.ul; fi.U[1] = c->ib.vl; fi.U[2] = c->ib.wl;
@@ -865,7 +867,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->pb.cstart, c->pb.cfill, c->pb.citem, c->pb.ccell, c->ru32, c->rv32, c->rw32, c->fu32,
-                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
+                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
                   c->cfield, c->cnext, c->crk};
   for (void *q : ptrs)

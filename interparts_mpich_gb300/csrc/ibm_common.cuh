@@ -48,21 +48,12 @@ struct PointStencil {
 
 // Mixed form: one velocity component of one Lagrangian point: index of tap
 // (0,0,0) of the 3x3x3 block (x, y unwrapped) and the component's FP32 delta
-// weights wx[3], wy[3], wz[3] (48 bytes, read as three float4)
+// weights wx[3], wy[3], wz[3], formed in registers from the point's record
+// (make_cs)
 struct __align__(16) CompStencil {
   int b[3];
   float w[9];
 };
-// one 48-byte record as three 16-byte loads
-__device__ __forceinline__ CompStencil load_cs(const CompStencil *p) {
-  const float4 *q = reinterpret_cast<const float4 *>(p);
-  const float4 a = q[0], bb = q[1], c = q[2];
-  CompStencil s;
-  s.b[0] = __float_as_int(a.x); s.b[1] = __float_as_int(a.y); s.b[2] = __float_as_int(a.z);
-  s.w[0] = a.w; s.w[1] = bb.x; s.w[2] = bb.y; s.w[3] = bb.z; s.w[4] = bb.w;
-  s.w[5] = c.x; s.w[6] = c.y; s.w[7] = c.z; s.w[8] = c.w;
-  return s;
-}
 
 // Mixed form: one Lagrangian point in 16 bytes, written once per substep:
 // the fractions of its grid coordinates x dxi, y dyi, z dzi (FP32, exact
@@ -119,6 +110,32 @@ __device__ __forceinline__ float delta3f(float r) {
   if (ar > 0.5f) return (1.f / 6.f) * (5.f - 3.f * ar - sqrtf(-3.f * ((1.f - ar) * (1.f - ar)) + 1.f));
   return (1.f / 3.f) * (1.f + sqrtf(-3.f * (r * r) + 1.f));
 }
+// Square root, approximate (relative error about 2^-22; the mixed form's
+// delta weights are FP32 approximations of the FP64 ones anyway).
+__device__ __forceinline__ float sqrt_apx(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// FP32 delta weights at three consecutive nodes m = 0, 1, 2 of a point whose
+// signed distance from node 1 is r1 = x_1 - x_point (in cells).  For r1 in
+// (-0.5, 0.5] node 1 takes the inner branch of kernel.f90:7-25 and nodes 0
+// and 2 (distances 1 - r1 and 1 + r1) the outer one, and all three share
+// sqrt(1 - 3 r1^2): w1 = (1 + s)/3, w0 = (2 + 3 r1 - s)/6,
+// w2 = (2 - 3 r1 - s)/6 (they sum to one).  Any other r1 (a wall-clamped
+// origin in z) takes the general form node by node.
+__device__ __forceinline__ void delta3w(float r1, float *w) {
+  if (r1 > -0.5f && r1 <= 0.5f) {
+    const float s = sqrt_apx(fmaf(-3.f * r1, r1, 1.f));
+    w[1] = (1.f + s) * (1.f / 3.f);
+    w[0] = (fmaf(3.f, r1, 2.f) - s) * (1.f / 6.f);
+    w[2] = (fmaf(-3.f, r1, 2.f) - s) * (1.f / 6.f);
+  } else {
+    w[0] = delta3f(r1 - 1.f);
+    w[1] = delta3f(r1);
+    w[2] = delta3f(r1 + 1.f);
+  }
+}
 // Stencil of velocity component c (0 u, 1 v, 2 w) of a point, as eulr2lagr
 // forms it (interp_spread.f90:60-131): tap (0,0,0) of the 3x3x3 block
 // relative to the particle's reference floor in x and y and absolute in z
@@ -126,47 +143,46 @@ __device__ __forceinline__ float delta3f(float r) {
 // Along the component's own axis the staggered origin (ilows, jlows, klows:
 // the nearest face, max(.,1) in z) and offsets; along the other axes the
 // cell-centred origin (ilow, jlow, klow clamped to [1, K-2], quirk Q5).
+// The delta argument of node m is m - o with o the point's offset from the
+// origin (own axis) or m - 1/2 - o (cell-centred axes); delta3w takes the
+// distance r1 of node 1.
 __device__ __forceinline__ CompStencil make_cs(const PointRec &r, int c, int refz, int K) {
   const int dx = rec_dx(r.rel), dy = rec_dy(r.rel), nz = refz + rec_dz(r.rel);
   CompStencil s;
-  float o;
   if (c == 0) {
     const int ux = r.fx >= 0.5f;
     s.b[0] = dx + ux - 2;
-    o = r.fx + (float)(1 - ux);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) s.w[m] = delta3f((float)m - o);
+    delta3w((float)ux - r.fx, s.w);  // 1 - (fx + 1 - ux)
   } else {
     s.b[0] = dx - 1;
-#pragma unroll
-    for (int m = 0; m < 3; ++m) s.w[m] = delta3f(((float)m - 0.5f) - r.fx);
+    delta3w(0.5f - r.fx, s.w);
   }
   if (c == 1) {
     const int uy = r.fy >= 0.5f;
     s.b[1] = dy + uy - 2;
-    o = r.fy + (float)(1 - uy);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) s.w[3 + m] = delta3f((float)m - o);
+    delta3w((float)uy - r.fy, s.w + 3);
   } else {
     s.b[1] = dy - 1;
-#pragma unroll
-    for (int m = 0; m < 3; ++m) s.w[3 + m] = delta3f(((float)m - 0.5f) - r.fy);
+    delta3w(0.5f - r.fy, s.w + 3);
   }
   if (c == 2) {
     const int uz = r.fz > 0.5f || (r.fz == 0.5f && nz >= 0);
     const int klows = max(nz + uz - 1, 1);
     s.b[2] = klows;
-    o = r.fz + (float)(nz - klows);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) s.w[6 + m] = delta3f((float)m - o);
+    delta3w(1.f - (r.fz + (float)(nz - klows)), s.w + 6);
   } else {
     const int klow = max(min(nz, K - 2), 1);
     s.b[2] = klow;
-    o = r.fz + (float)(nz - klow);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) s.w[6 + m] = delta3f(((float)m - 0.5f) - o);
+    delta3w(0.5f - (r.fz + (float)(nz - klow)), s.w + 6);
   }
   return s;
+}
+// Offset of a point from its particle's centre along one axis, FP32: the
+// point's floor offset d from the particle's reference floor plus its
+// fraction fr, minus the centre's position cf relative to the same floor
+// (all in cells), times the cell size h.
+__device__ __forceinline__ float rec_armf(int d, float fr, float cf, float h) {
+  return (((float)d - cf) + fr) * h;
 }
 // Error-free FP32 transformations (Knuth two-sum, FMA two-product) for
 // double-float arithmetic: a value is carried as hi + lo (about 48 bits) on the

@@ -35,7 +35,12 @@ __global__ void __launch_bounds__(256) k_ibm_points(Geo g, PartGeo pg, IbmBuffer
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
     const int4 ref = particle_ref(g, pg, b.pf, p);
-    if (l == 0) b.pref[p] = ref;
+    if (l == 0) {
+      b.pref[p] = ref;
+      b.pcen[p] = make_float4((float)(b.pf[PF_X * pg.np + p] * g.dxi - (double)ref.x),
+                              (float)(b.pf[PF_Y * pg.np + p] * g.dyi - (double)ref.y),
+                              (float)(b.pf[PF_Z * pg.np + p] * g.dzi - (double)ref.z), 0.f);
+    }
     if (l >= b.nla[p]) continue;
     const double cx = b.xfp[t] * g.dxi, cy = b.yfp[t] * g.dyi, cz = b.zfp[t] * g.dzi;
     // floors and exact fractions; the range check as the periodic image
@@ -169,10 +174,20 @@ __device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__
     box[q] = __ldg(&F[fidx(g, wrapm(x0 + cx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]);
   }
 }
-// Offset of a point from its particle's centre along one axis (FP64, from the
-// record: floor + FP32 fraction in grid units)
-__device__ __forceinline__ double rec_arm(int ref, int d, float fr, double h, double centre) {
-  return ((double)(ref + d) + (double)fr) * h - centre;
+// Lever arms of the torque terms of component c (c=0: (rz, ry), c=1:
+// (rz, rx), c=2: (ry, rx)), FP32 from the point record and the centre
+// offsets cf (cells from the reference floor)
+__device__ __forceinline__ void lever_arms(const PointRec &rr, const float4 &cf, int c, float hx, float hy, float hz,
+                                           float &la, float &lb) {
+  const float ry = rec_armf(rec_dy(rr.rel), rr.fy, cf.y, hy);
+  la = c == 2 ? ry : rec_armf(rec_dz(rr.rel), rr.fz, cf.z, hz);
+  lb = c == 0 ? ry : rec_armf(rec_dx(rr.rel), rr.fx, cf.x, hx);
+}
+// The rigid-body velocity of a point as an FP32 pair hi + lo (the slip
+// U - u~ = (hi - u~) + lo keeps the FP64 velocity's bits that FP32 u~ resolves)
+__device__ __forceinline__ float2 split_u(double U) {
+  const float hi = (float)U;
+  return make_float2(hi, (float)(U - (double)hi));
 }
 // rigid-body velocity component of point t: the particle's, or with rotation
 // on the per-point value (u + omega x r, updated with the points)
@@ -244,7 +259,7 @@ __device__ __forceinline__ float block_sum_all(float a) {
   return t;
 }
 
-__global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
+__global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
                                                            const float *__restrict__ fu, const float *__restrict__ fv,
                                                            const float *__restrict__ fw, double dti, int first,
                                                            const int *__restrict__ gate) {
@@ -267,13 +282,15 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
   const double *Ua = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
   double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
   float *slip = b.slip + c * npl;
-  const double *pf = b.pf;
-  const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
-  const double Up = pf[(c == 0 ? PF_U : (c == 1 ? PF_V : PF_W)) * pg.np + p];
+  const float2 Us = split_u(b.pf[(c == 0 ? PF_U : (c == 1 ? PF_V : PF_W)) * pg.np + p]);
   const int4 ref = b.pref[p];
+  const float4 cf = b.pcen[p];
+  const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
   const PointRec *rp = b.rec + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
-  double sF = 0., sa = 0., sb = 0.;
+  // per-thread force and lever-arm sums in FP32 (a few points per thread),
+  // the block's sums in FP64
+  float sF = 0.f, sa = 0.f, sb = 0.f;
   float r2 = 0.f, r0 = 0.f;
   for (int l = threadIdx.x; l < nla; l += blockDim.x) {
     const long t = t0 + l;
@@ -288,32 +305,26 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
         return __ldg(&F[fidx(g, wrapm(ref.x + s.b[0] + i, g.I), wrapm(ref.y + s.b[1] + j, g.J), s.b[2] + k)]);
       });
     }
-    const double U = point_u(pg, Ua, Up, t);
+    const float2 U = pg.rotation ? split_u(Ua[t]) : Us;
+    const float sd = (U.x - acc) + U.y;  // slip U - u~
     if (first == -1) {  // residual only: sum of (U - u~)^2 of the component
-      const float e = (float)U - acc;
-      r2 = fmaf(e, e, r2);
+      r2 = fmaf(sd, sd, r2);
       continue;
     }
     if (first < 0) {  // the interpolation only (diagnostics)
       dud[t] = acc;
       continue;
     }
-    const double sd = U - acc;
-    slip[t] = (float)sd;  // the spreading's increment (U - u~)/dt, FP32
-    if (first) {  // first-pass slip, for the learned loop's gate reference
-      const float e = (float)sd;
-      r0 = fmaf(e, e, r0);
-    }
-    const double f = first ? sd * dti : Fl[t] + sd * dti;
+    slip[t] = sd;  // the spreading's increment (U - u~)/dt, FP32
+    if (first) r0 = fmaf(sd, sd, r0);  // first-pass slip, for the learned loop's gate reference
+    const double f = first ? (double)sd * dti : fma((double)sd, dti, Fl[t]);
     Fl[t] = f;
-    // lever arms of the torque terms of this component:
-    // c=0: (rz, ry), c=1: (rz, rx), c=2: (ry, rx)
-    const double ry = rec_arm(ref.y, rec_dy(rr.rel), rr.fy, g.dy, py);
-    const double la = c == 2 ? ry : rec_arm(ref.z, rec_dz(rr.rel), rr.fz, g.dz, pz);
-    const double lb = c == 0 ? ry : rec_arm(ref.x, rec_dx(rr.rel), rr.fx, g.dx, px);
-    sF += f;
-    sa += la * f;
-    sb += lb * f;
+    const float ff = (float)f;
+    float la, lb;
+    lever_arms(rr, cf, c, hx, hy, hz, la, lb);
+    sF += ff;
+    sa = fmaf(la, ff, sa);
+    sb = fmaf(lb, ff, sb);
   }
   // psum[p][c]: force and lever-arm sums, or (first < 0) the residual sum in
   // slot 0 for k_ibm_res_gate
@@ -330,7 +341,7 @@ __global__ void __launch_bounds__(INTERP_THREADS) k_ibm_interp_comp_f(Geo g, Par
   __syncthreads();  // the box is dead: its first words hold the partial sums
   double *st = reinterpret_cast<double *>(ibox_sm);
   __shared__ double res[3];
-  block_sum3<INTERP_THREADS>(sF, sa, sb, st, res);
+  block_sum3<INTERP_THREADS>((double)sF, (double)sa, (double)sb, st, res);
   if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
 }
 // per-particle force and torque of updtlagrforces from the component sums
@@ -433,12 +444,15 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
   const int4 ref = b.pref[p];
   const PointRec *rp = b.rec + t0;
-  double sF = 0., sa = 0., sb = 0.;
-  double px = 0., py = 0., pz = 0.;
-  float ysig = 0.f, ymu = 0.f;
+  // per-thread force and lever-arm sums in FP32, the block's sums in FP64
+  float sF = 0.f, sa = 0.f, sb = 0.f;
+  float4 cf = make_float4(0.f, 0.f, 0.f, 0.f);
+  float ysig = 0.f, ymu = 0.f, dtif = 0.f, dtf = 0.f;
+  const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
   if (lf.Y) {
-    px = b.pf[PF_X * pg.np + p]; py = b.pf[PF_Y * pg.np + p]; pz = b.pf[PF_Z * pg.np + p];
+    cf = b.pcen[p];
     ysig = lf.tsig[c]; ymu = lf.tmu[c];
+    dtif = (float)lf.dti; dtf = (float)(1. / lf.dti);
   }
   // prefactors F coeff0 (F given) or (U - u~) dti coeff0, as FP32 products
   const float pcoef = (float)coeff0, ucoef = (float)(dti * coeff0);
@@ -449,7 +463,6 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   // (coalesced loads of the point arrays).
   const int nq = (nla + 31) >> 5;
   float asum = 0.f, r0 = 0.f;
-  const double dt_l = lf.Y ? 1. / lf.dti : 0.;
   for (int m = threadIdx.x; m < 32 * nq; m += blockDim.x) {
     const int l = staged ? m : (m & 31) * nq + (m >> 5);
     if (l >= nla) continue;
@@ -459,19 +472,18 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
       // total point force F0 + the network's correction, its sums
       // (updtlagrforces), spread once
       const double f0 = Fl[t];
-      const double d = (double)(lf.Y[3 * t + c] * ysig + ymu) * lf.dti;
-      const double f = f0 + d;
+      const float d = fmaf(lf.Y[3 * t + c], ysig, ymu) * dtif;
+      const double f = f0 + (double)d;
       Fl[t] = f;
-      const float e0 = (float)(f0 * dt_l);  // the first pass's slip U - u~
+      const float e0 = (float)f0 * dtf;  // the first pass's slip U - u~
       r0 = fmaf(e0, e0, r0);
-      const PointRec rr = rp[l];
-      const double ry = rec_arm(ref.y, rec_dy(rr.rel), rr.fy, g.dy, py);
-      const double la = c == 2 ? ry : rec_arm(ref.z, rec_dz(rr.rel), rr.fz, g.dz, pz);
-      const double lb = c == 0 ? ry : rec_arm(ref.x, rec_dx(rr.rel), rr.fx, g.dx, px);
-      sF += f;
-      sa += la * f;
-      sb += lb * f;
-      pre = (float)(lf.incr ? d : f) * pcoef;
+      const float ff = (float)f;
+      float la, lb;
+      lever_arms(rp[l], cf, c, hx, hy, hz, la, lb);
+      sF += ff;
+      sa = fmaf(la, ff, sa);
+      sb = fmaf(lb, ff, sb);
+      pre = (lf.incr ? d : ff) * pcoef;
     } else {
       pre = slip[t] * ucoef;
     }
@@ -495,7 +507,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   }
   if (lf.Y) {  // psum[p][c] for k_ibm_force_sums; rsum for the gate
     __shared__ double sred[3 * SPREAD_THREADS], res[3];
-    block_sum3<SPREAD_THREADS>(sF, sa, sb, sred, res);
+    block_sum3<SPREAD_THREADS>((double)sF, (double)sa, (double)sb, sred, res);
     if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
     if (!lf.incr) {
       const float tot = block_sum_all(r0);
@@ -657,10 +669,10 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
       }
       continue;
     }
-    const double px = pf[PF_X * pg.np + p], py = pf[PF_Y * pg.np + p], pz = pf[PF_Z * pg.np + p];
-    const float nrm[3] = {(float)rec_arm(ref.x, rec_dx(rr.rel), rr.fx, g.dx, px) * inv_r,
-                          (float)rec_arm(ref.y, rec_dy(rr.rel), rr.fy, g.dy, py) * inv_r,
-                          (float)rec_arm(ref.z, rec_dz(rr.rel), rr.fz, g.dz, pz) * inv_r};
+    const float4 cf = b.pcen[p];
+    const float nrm[3] = {rec_armf(rec_dx(rr.rel), rr.fx, cf.x, (float)g.dx) * inv_r,
+                          rec_armf(rec_dy(rr.rel), rr.fy, cf.y, (float)g.dy) * inv_r,
+                          rec_armf(rec_dz(rr.rel), rr.fz, cf.z, (float)g.dz) * inv_r};
     const float *F3[3] = {fu, fv, fw};
     double *D3[3] = {b.dudtl, b.dvdtl, b.dwdtl};
     double *Fl3[3] = {b.fxl, b.fyl, b.fzl};

@@ -83,6 +83,7 @@ struct IbmBuffers {
   PointStencil *st;
   PointRec *rec;     // mixed form: [np*nl] compact point records (make_cs)
   int4 *pref;        // mixed form: [np] reference floors (refx, refy, refz) of the particles
+  float4 *pcen;      // mixed form: [np] centre position in cells relative to the reference floor (FP32)
   float *slip;       // mixed form: [3][np*nl] slip U - u~ of the last pass (FP32)
   int *bgeo;         // mixed form: [np][3][8] per-particle stencil boxes
   short2 *rowx;      // mixed form: [np][3][IBM_BOX_ROWS] x extent of every box row the stencils touch
@@ -177,6 +178,7 @@ struct FeatIn {
   const int *nla;
   const PointRec *rec;
   const int4 *pref;
+  const float4 *pcen;
   int rotation;        // 0: U is the particle velocity; 1: read U[] (with the rotation term)
   const float *F[3];   // u, v, w (FP32 fields)
   const double *U[3];  // rigid-body velocity at the points (read with rotation on)

@@ -525,12 +525,12 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
   }
   const Geo &g = fi.g;
   const int4 ref = fi.pref[p];
+  const float4 cf = fi.pcen[p];
   const PointRec rr = fi.rec[t];
 #pragma unroll 1
   for (int c = 0; c < 3; ++c) {
     const CompStencil s = make_cs(rr, c, ref.z, g.K);
     const float *F = fi.F[c];
-    const int pc = c == 0 ? PF_X : (c == 1 ? PF_Y : PF_Z);
     const double Ud = fi.rotation ? fi.U[c][t] : fi.pf[(PF_U + c) * fi.np + p];
     const float Uc = (float)Ud;
     float f[FEAT_PER_COMP];
@@ -554,9 +554,9 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
     f[28] = Uc;
     const int dc = c == 0 ? rec_dx(rr.rel) : (c == 1 ? rec_dy(rr.rel) : rec_dz(rr.rel));
     const float frc = c == 0 ? rr.fx : (c == 1 ? rr.fy : rr.fz);
-    const int refc = c == 0 ? ref.x : (c == 1 ? ref.y : ref.z);
-    const double hc = c == 0 ? g.dx : (c == 1 ? g.dy : g.dz);
-    f[29] = (float)(((double)(refc + dc) + (double)frc) * hc - fi.pf[pc * fi.np + p]) * fi.inv_r;
+    const float cfc = c == 0 ? cf.x : (c == 1 ? cf.y : cf.z);
+    const float hc = (float)(c == 0 ? g.dx : (c == 1 ? g.dy : g.dz));
+    f[29] = rec_armf(dc, frc, cfc, hc) * fi.inv_r;
     f[30] = (float)F0 * (float)fi.dt;
     f[31] = s.w[3 * c + 1];
     const float *mu = fi.mu + FEAT_PER_COMP * c, *is = fi.isig + FEAT_PER_COMP * c;

