@@ -270,6 +270,8 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver = IBMSolver(case, mode=mode)
     if args.proj_solves and mode != 0:
         solver.set_projection_solves(args.proj_solves)
+    if mode != 0:
+        solver.set_predictor_kernel({"auto": 0, "pairs": 1, "cells": 2, "tma": 3}[args.predictor])
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
     solver.setup(case.initial_fields())
@@ -429,6 +431,9 @@ def main():
     ap.add_argument("--probe-mask", type=int, default=-1,
                     help="kernel classes timed with CUDA events inside the timed steps (bit per class; "
                          "default: the dominant class of an untimed probed step)")
+    ap.add_argument("--predictor", default="auto", choices=["auto", "pairs", "cells", "tma"],
+                    help="FP32 predictor kernel of the mixed forms (auto: planes staged by 16-byte loads; "
+                         "tma: by tensor-memory-accelerator copies)")
     ap.add_argument("--proj-solves", type=int, default=0,
                     help="FP32 Poisson solves per projection in the mixed forms (0: the library default)")
     args = ap.parse_args()

@@ -180,6 +180,22 @@ int ibm_run_adaptive(ibm_ctx *ctx, int nsteps, int ioutchk, double *dt, double *
  * is accepted there). */
 int ibm_set_projection_solves(ibm_ctx *ctx, int solves);
 
+/* Kernel of the FP32 momentum predictor of the mixed forms (rk1..rk3 +
+ * mom.f90; no counterpart in the reference, which has one CPU loop nest).
+ * Each stages the planes of u, v, w, p in shared memory tile by tile:
+ * IBM_PREDICTOR_AUTO (default): 16-byte loads through registers, where the
+ * rows are a multiple of 4 cells; otherwise, and with IBM_PREDICTOR_PAIRS,
+ * 4-byte loads; IBM_PREDICTOR_TMA: tensor-memory-accelerator copies (rows a
+ * multiple of 4 cells).  These three share their arithmetic: identical
+ * results.  IBM_PREDICTOR_CELLS: one cell per thread (FP32 terms grouped
+ * differently, results within FP32 rounding).  The FP64 form has one kernel
+ * and ignores this.  IBM_E_INVALID for any other value. */
+#define IBM_PREDICTOR_AUTO  0
+#define IBM_PREDICTOR_PAIRS 1
+#define IBM_PREDICTOR_CELLS 2
+#define IBM_PREDICTOR_TMA   3
+int ibm_set_predictor_kernel(ibm_ctx *ctx, int kind);
+
 /* --- diagnostics ----------------------------------------------------------- */
 
 /* chkdiv (chkdiv.f90:7-61): total and max |div| of (unew,vnew,wnew) and the

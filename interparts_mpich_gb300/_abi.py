@@ -22,6 +22,11 @@ IBM_E_NOT_CONVERGED = -5
 IBM_E_DIVERGENCE = -6
 IBM_E_STATE = -7
 
+IBM_PREDICTOR_AUTO = 0
+IBM_PREDICTOR_PAIRS = 1
+IBM_PREDICTOR_CELLS = 2
+IBM_PREDICTOR_TMA = 3
+
 IBM_BC_NOSLIP = 0
 IBM_BC_FREESLIP = 1
 
@@ -181,6 +186,7 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "run_adaptive": (C.c_int, [ctx, C.c_int, C.c_int, c_double_p, c_double_p]),
         "fp64_peak": (C.c_int, [c_double_p]),
         "set_projection_solves": (C.c_int, [ctx, C.c_int]),
+        "set_predictor_kernel": (C.c_int, [ctx, C.c_int]),
         "probe": (C.c_int, [ctx, C.c_uint]),
         "probe_result": (C.c_int, [ctx, c_double_p, c_int_p]),
         "harvest": (C.c_int, [ctx, C.c_int, C.c_int, C.c_int]),

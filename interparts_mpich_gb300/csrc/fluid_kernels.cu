@@ -4,9 +4,13 @@
 // One thread per interior cell; x/y neighbours by periodic wrap, z ghosts
 // stored.  All arithmetic follows the reference expression order; FP64
 // fused multiply-add contraction is allowed (differences at 1 ulp level).
-#include <algorithm>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdlib>
+#include <cstdint>
 
 #include "kernels.cuh"
 
@@ -268,16 +272,15 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
 // The same stage with two x-neighbouring cells per thread in packed FP32x2
 // arithmetic (one instruction for both cells; the x neighbours of the pair
 // come from three aligned 8-byte shared loads instead of six): 64 x 8 cells
-// per block, rows padded to an even start so that every pair is aligned.
+// per block.  Three kernels stage the planes differently and share the
+// arithmetic (pair_cells), so that they agree bit for bit:
+//   k_predict_quad  rows of 72 cells from x = i0 - 4, loaded as 16-byte
+//                   quads through registers one plane ahead (the default);
+//   k_predict_pair  rows of 66 cells, one 4-byte load per cell;
+//   k_predict_tma   the k_predict_quad rows, copied by the tensor-memory
+//                   accelerator into a ring of four planes per field.
 constexpr int QTX = 64, QTY = 8, QHY = QTY + 2, QROW = QTX + 4, QKC = 32;
-// IBM_PREDICT_SCALAR=1 selects k_predict_tiled (one cell per thread) instead
-bool predict_pairs() {
-  static const bool on = [] {
-    const char *e = std::getenv("IBM_PREDICT_SCALAR");
-    return !(e && e[0] == '1');
-  }();
-  return on;
-}
+constexpr int TBX = QTX + 8, TBY = QTY + 2;  // quad / TMA rows: 72 cells from x = i0 - 4, 10 rows from y = j0 - 1
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
@@ -285,15 +288,123 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 ld2(const float *row, int idx) { return *reinterpret_cast<const float2 *>(row + idx); }
 __device__ __forceinline__ float2 mid(float2 a, float2 b) { return make_float2(a.y, b.x); }
+
+struct PairCoef {
+  float2 qdxi, qdyi, qdzi, vdx2, vdy2, vdz2, mdxi, mdyi, mdzi, F1, F2, mF3;
+  __device__ PairCoef(const Geo &g, float f1, float f2_, float f3) {
+    const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi, visc = (float)g.visc;
+    qdxi = f2(0.25f * dxi); qdyi = f2(0.25f * dyi); qdzi = f2(0.25f * dzi);
+    vdx2 = f2(visc * dxi * dxi); vdy2 = f2(visc * dyi * dyi); vdz2 = f2(visc * dzi * dzi);
+    mdxi = f2(-dxi); mdyi = f2(-dyi); mdzi = f2(-dzi);
+    F1 = f2(f1); F2 = f2(f2_); mF3 = f2(-f3);
+  }
+};
+// Planes k-1 (m), k (0), k+1 (p) of u, v, w and k, k+1 of p in shared
+// memory, rows of RS cells; the pair's first cell at column x of row y.
+struct PairPlanes {
+  const float *um, *u0, *up, *vm, *v0, *vp, *wm, *w0, *wp, *p0, *pp;
+};
+// momxad, momyad, momzad (mom.f90:21-50, 94-123, 170-199), momxp..momzp and
+// the rk1..rk3 update of two cells (global index c, c + 1; 32-bit: the
+// tiled kernels run on fields of fewer than 2^31 cells)
+template <int STAGE, bool BUOY, int RS>
+__device__ __forceinline__ void pair_cells(const PairPlanes &P, int x, int y, int c, int PL, const PairCoef &q,
+                                           float *__restrict__ ru, float *__restrict__ rv, float *__restrict__ rw,
+                                           float *__restrict__ fu, float *__restrict__ fv, float *__restrict__ fw,
+                                           const double *__restrict__ cb, double bcoef) {
+  auto row = [&](const float *f, int yy) { return f + yy * RS; };
+  // u
+  const float *ur = row(P.u0, y);
+  const float2 U0 = ld2(ur, x), UL = ld2(ur, x - 2), UR = ld2(ur, x + 2);
+  const float2 Uip = mid(U0, UR), Uim = mid(UL, U0);
+  const float2 Ujp = ld2(row(P.u0, y + 1), x), Ujm = ld2(row(P.u0, y - 1), x);
+  const float2 Ukp = ld2(row(P.up, y), x), Ukm = ld2(row(P.um, y), x);
+  const float2 Uimjp = mid(ld2(row(P.u0, y + 1), x - 2), Ujp), Uimkp = mid(ld2(row(P.up, y), x - 2), Ukp);
+  // v
+  const float *vr = row(P.v0, y);
+  const float2 V0 = ld2(vr, x), VL = ld2(vr, x - 2), VR = ld2(vr, x + 2);
+  const float2 Vip = mid(V0, VR), Vim = mid(VL, V0);
+  const float2 Vjp = ld2(row(P.v0, y + 1), x), Vjm = ld2(row(P.v0, y - 1), x);
+  const float2 Vkp = ld2(row(P.vp, y), x), Vkm = ld2(row(P.vm, y), x);
+  const float2 Vipjm = mid(Vjm, ld2(row(P.v0, y - 1), x + 2)), Vjmkp = ld2(row(P.vp, y - 1), x);
+  // w
+  const float *wr = row(P.w0, y);
+  const float2 W0 = ld2(wr, x), WL = ld2(wr, x - 2), WR = ld2(wr, x + 2);
+  const float2 Wip = mid(W0, WR), Wim = mid(WL, W0);
+  const float2 Wjp = ld2(row(P.w0, y + 1), x), Wjm = ld2(row(P.w0, y - 1), x);
+  const float2 Wkp = ld2(row(P.wp, y), x), Wkm = ld2(row(P.wm, y), x);
+  const float2 Wipkm = mid(Wkm, ld2(row(P.wm, y), x + 2)), Wjpkm = ld2(row(P.wm, y + 1), x);
+  // the terms of k_predict_tiled in packed arithmetic
+  const float2 Puv = mul2(add2(Ujp, U0), add2(Vip, V0));
+  const float2 Puw = mul2(add2(Ukp, U0), add2(Wip, W0));
+  const float2 Pvw = mul2(add2(Wjp, W0), add2(Vkp, V0));
+  auto lap = [&](float2 cc, float2 xp, float2 xm, float2 yp, float2 ym, float2 zp, float2 zm) {
+    const float2 dx_ = sub2(sub2(xp, cc), sub2(cc, xm)), dy_ = sub2(sub2(yp, cc), sub2(cc, ym)),
+                 dz_ = sub2(sub2(zp, cc), sub2(cc, zm));
+    return fma2(q.vdx2, dx_, fma2(q.vdy2, dy_, mul2(q.vdz2, dz_)));
+  };
+  auto sqd = [&](float2 a, float2 b) { return fma2(a, a, mul2(f2(-1.f), mul2(b, b))); };  // a^2 - b^2
+  float2 ru_new, rv_new, rw_new;
+  {
+    const float2 sp_ = add2(Uip, U0), sm_ = add2(Uim, U0);
+    ru_new = fma2(q.qdxi, sqd(sm_, sp_),
+                  fma2(q.qdyi, sub2(mul2(add2(Ujm, U0), add2(Vipjm, Vjm)), Puv),
+                       fma2(q.qdzi, sub2(mul2(add2(Ukm, U0), add2(Wipkm, Wkm)), Puw),
+                            lap(U0, Uip, Uim, Ujp, Ujm, Ukp, Ukm))));
+  }
+  {
+    const float2 sp_ = add2(V0, Vjp), sm_ = add2(V0, Vjm);
+    rv_new = fma2(q.qdxi, sub2(mul2(add2(Uim, Uimjp), add2(V0, Vim)), Puv),
+                  fma2(q.qdyi, sqd(sm_, sp_),
+                       fma2(q.qdzi, sub2(mul2(add2(Wkm, Wjpkm), add2(Vkm, V0)), Pvw),
+                            lap(V0, Vip, Vim, Vjp, Vjm, Vkp, Vkm))));
+  }
+  {
+    const float2 sp_ = add2(W0, Wkp), sm_ = add2(W0, Wkm);
+    rw_new = fma2(q.qdxi, sub2(mul2(add2(W0, Wim), add2(Uim, Uimkp)), Puw),
+                  fma2(q.qdyi, sub2(mul2(add2(W0, Wjm), add2(Vjm, Vjmkp)), Pvw),
+                       fma2(q.qdzi, sqd(sm_, sp_), lap(W0, Wip, Wim, Wjp, Wjm, Wkp, Wkm))));
+  }
+  // pressure gradient (momxp/momyp/momzp)
+  const float *pr = row(P.p0, y);
+  const float2 P0 = ld2(pr, x);
+  const float2 gx = mul2(q.mdxi, sub2(mid(P0, ld2(pr, x + 2)), P0));
+  const float2 gy = mul2(q.mdyi, sub2(ld2(row(P.p0, y + 1), x), P0));
+  const float2 gz = mul2(q.mdzi, sub2(ld2(row(P.pp, y), x), P0));
+  if constexpr (BUOY) {
+    rw_new.x = (float)(bcoef * (cb[c] + cb[c + PL])) + rw_new.x;  // momzbuoy
+    rw_new.y = (float)(bcoef * (cb[c + 1] + cb[c + 1 + PL])) + rw_new.y;
+  }
+  float2 du = fma2(q.F1, gx, U0), dv = fma2(q.F1, gy, V0), dw = fma2(q.F1, gz, W0);
+  if (STAGE == 1) {
+    du = fma2(q.F1, ru_new, du);
+    dv = fma2(q.F1, rv_new, dv);
+    dw = fma2(q.F1, rw_new, dw);
+  } else {
+    const float2 ou = *reinterpret_cast<const float2 *>(ru + c), ov = *reinterpret_cast<const float2 *>(rv + c),
+                 ow = *reinterpret_cast<const float2 *>(rw + c);
+    du = add2(du, fma2(q.F2, ru_new, mul2(q.mF3, ou)));
+    dv = add2(dv, fma2(q.F2, rv_new, mul2(q.mF3, ov)));
+    dw = add2(dw, fma2(q.F2, rw_new, mul2(q.mF3, ow)));
+  }
+  *reinterpret_cast<float2 *>(fu + c) = du;
+  *reinterpret_cast<float2 *>(fv + c) = dv;
+  *reinterpret_cast<float2 *>(fw + c) = dw;
+  if (STAGE != 3) {
+    *reinterpret_cast<float2 *>(ru + c) = ru_new;
+    *reinterpret_cast<float2 *>(rv + c) = rv_new;
+    *reinterpret_cast<float2 *>(rw + c) = rw_new;
+  }
+}
+
+#define PREDICT_ARGS                                                                                          \
+  Geo g, const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,               \
+      const float *__restrict__ p, float *__restrict__ ru, float *__restrict__ rv, float *__restrict__ rw,    \
+      float *__restrict__ fu, float *__restrict__ fv, float *__restrict__ fw, float f1, float f2_, float f3,  \
+      const double *__restrict__ cb, double bcoef
+
 template <int STAGE, bool BUOY>
-__global__ void __launch_bounds__(QTX / 2 * QTY) k_predict_pair(Geo g, const float *__restrict__ u,
-                                                               const float *__restrict__ v,
-                                                               const float *__restrict__ w,
-                                                               const float *__restrict__ p, float *__restrict__ ru,
-                                                               float *__restrict__ rv, float *__restrict__ rw,
-                                                               float *__restrict__ fu, float *__restrict__ fv,
-                                                               float *__restrict__ fw, float f1, float f2_, float f3,
-                                                               const double *__restrict__ cb, double bcoef) {
+__global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_pair(PREDICT_ARGS) {
   // row layout: [pad, x = i0 - 1, x = i0 .. i0 + 63, x = i0 + 64, pad]
   __shared__ __align__(16) float su[3][QHY][QROW], sv[3][QHY][QROW], sw[3][QHY][QROW], sp[2][QHY][QROW];
   constexpr int NT = QTX / 2 * QTY, NH = QHY * (QTX + 2), HQ = (NH + NT - 1) / NT;
@@ -340,127 +451,370 @@ __global__ void __launch_bounds__(QTX / 2 * QTY) k_predict_pair(Geo g, const flo
   fetch(k0);
   commit(k0);
   fetch(k0 + 1);
-  const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi, visc = (float)g.visc;
-  const float2 qdxi = f2(0.25f * dxi), qdyi = f2(0.25f * dyi), qdzi = f2(0.25f * dzi);
-  const float2 vdx2 = f2(visc * dxi * dxi), vdy2 = f2(visc * dyi * dyi), vdz2 = f2(visc * dzi * dzi);
-  const float2 mdxi = f2(-dxi), mdyi = f2(-dyi), mdzi = f2(-dzi);
-  const float2 F1 = f2(f1), F2 = f2(f2_), F3 = f2(f3);
-  const int x = 2 * tx + 2, y = ty + 1;
+  const PairCoef cf(g, f1, f2_, f3);
   for (int k = k0; k <= k1; ++k) {
     commit(k + 1);
     __syncthreads();
     if (k + 1 <= k1) fetch(k + 2);
     if (in) {
       const int cm = (k - 1) % 3, c0 = k % 3, cp = (k + 1) % 3;
-      // u
-      const float *ur = su[c0][y];
-      const float2 U0 = ld2(ur, x), UL = ld2(ur, x - 2), UR = ld2(ur, x + 2);
-      const float2 Uip = mid(U0, UR), Uim = mid(UL, U0);
-      const float2 Ujp = ld2(su[c0][y + 1], x), Ujm = ld2(su[c0][y - 1], x);
-      const float2 Ukp = ld2(su[cp][y], x), Ukm = ld2(su[cm][y], x);
-      const float2 Uimjp = mid(ld2(su[c0][y + 1], x - 2), Ujp), Uimkp = mid(ld2(su[cp][y], x - 2), Ukp);
-      // v
-      const float *vr = sv[c0][y];
-      const float2 V0 = ld2(vr, x), VL = ld2(vr, x - 2), VR = ld2(vr, x + 2);
-      const float2 Vip = mid(V0, VR), Vim = mid(VL, V0);
-      const float2 Vjp = ld2(sv[c0][y + 1], x), Vjm = ld2(sv[c0][y - 1], x);
-      const float2 Vkp = ld2(sv[cp][y], x), Vkm = ld2(sv[cm][y], x);
-      const float2 Vipjm = mid(Vjm, ld2(sv[c0][y - 1], x + 2)), Vjmkp = ld2(sv[cp][y - 1], x);
-      // w
-      const float *wr = sw[c0][y];
-      const float2 W0 = ld2(wr, x), WL = ld2(wr, x - 2), WR = ld2(wr, x + 2);
-      const float2 Wip = mid(W0, WR), Wim = mid(WL, W0);
-      const float2 Wjp = ld2(sw[c0][y + 1], x), Wjm = ld2(sw[c0][y - 1], x);
-      const float2 Wkp = ld2(sw[cp][y], x), Wkm = ld2(sw[cm][y], x);
-      const float2 Wipkm = mid(Wkm, ld2(sw[cm][y], x + 2)), Wjpkm = ld2(sw[cm][y + 1], x);
-      // momxad, momyad, momzad (mom.f90:21-50, 94-123, 170-199), the terms
-      // of k_predict_tiled in packed arithmetic
-      const float2 Puv = mul2(add2(Ujp, U0), add2(Vip, V0));
-      const float2 Puw = mul2(add2(Ukp, U0), add2(Wip, W0));
-      const float2 Pvw = mul2(add2(Wjp, W0), add2(Vkp, V0));
-      auto lap = [&](float2 c, float2 xp, float2 xm, float2 yp, float2 ym, float2 zp, float2 zm) {
-        const float2 dx_ = sub2(sub2(xp, c), sub2(c, xm)), dy_ = sub2(sub2(yp, c), sub2(c, ym)),
-                     dz_ = sub2(sub2(zp, c), sub2(c, zm));
-        return fma2(vdx2, dx_, fma2(vdy2, dy_, mul2(vdz2, dz_)));
-      };
-      auto sqd = [&](float2 a, float2 b) { return fma2(a, a, mul2(f2(-1.f), mul2(b, b))); };  // a^2 - b^2
-      float2 ru_new, rv_new, rw_new;
-      {
-        const float2 sp_ = add2(Uip, U0), sm_ = add2(Uim, U0);
-        ru_new = fma2(qdxi, sqd(sm_, sp_),
-                      fma2(qdyi, sub2(mul2(add2(Ujm, U0), add2(Vipjm, Vjm)), Puv),
-                           fma2(qdzi, sub2(mul2(add2(Ukm, U0), add2(Wipkm, Wkm)), Puw),
-                                lap(U0, Uip, Uim, Ujp, Ujm, Ukp, Ukm))));
-      }
-      {
-        const float2 sp_ = add2(V0, Vjp), sm_ = add2(V0, Vjm);
-        rv_new = fma2(qdxi, sub2(mul2(add2(Uim, Uimjp), add2(V0, Vim)), Puv),
-                      fma2(qdyi, sqd(sm_, sp_),
-                           fma2(qdzi, sub2(mul2(add2(Wkm, Wjpkm), add2(Vkm, V0)), Pvw),
-                                lap(V0, Vip, Vim, Vjp, Vjm, Vkp, Vkm))));
-      }
-      {
-        const float2 sp_ = add2(W0, Wkp), sm_ = add2(W0, Wkm);
-        rw_new = fma2(qdxi, sub2(mul2(add2(W0, Wim), add2(Uim, Uimkp)), Puw),
-                      fma2(qdyi, sub2(mul2(add2(W0, Wjm), add2(Vjm, Vjmkp)), Pvw),
-                           fma2(qdzi, sqd(sm_, sp_), lap(W0, Wip, Wim, Wjp, Wjm, Wkp, Wkm))));
-      }
-      // pressure gradient (momxp/momyp/momzp)
-      const float *pr = sp[k % 2][y];
-      const float2 P0 = ld2(pr, x);
-      const float2 gx = mul2(mdxi, sub2(mid(P0, ld2(pr, x + 2)), P0));
-      const float2 gy = mul2(mdyi, sub2(ld2(sp[k % 2][y + 1], x), P0));
-      const float2 gz = mul2(mdzi, sub2(ld2(sp[(k + 1) % 2][y], x), P0));
-      const int c = k * PL + j * g.I + i;
-      if constexpr (BUOY) {
-        rw_new.x = (float)(bcoef * (cb[c] + cb[c + PL])) + rw_new.x;  // momzbuoy
-        rw_new.y = (float)(bcoef * (cb[c + 1] + cb[c + 1 + PL])) + rw_new.y;
-      }
-      float2 du = fma2(F1, gx, U0), dv = fma2(F1, gy, V0), dw = fma2(F1, gz, W0);
-      if (STAGE == 1) {
-        du = fma2(F1, ru_new, du);
-        dv = fma2(F1, rv_new, dv);
-        dw = fma2(F1, rw_new, dw);
-      } else {
-        const float2 ou = *reinterpret_cast<const float2 *>(ru + c), ov = *reinterpret_cast<const float2 *>(rv + c),
-                     ow = *reinterpret_cast<const float2 *>(rw + c);
-        du = add2(du, fma2(F2, ru_new, mul2(f2(-f3), ou)));
-        dv = add2(dv, fma2(F2, rv_new, mul2(f2(-f3), ov)));
-        dw = add2(dw, fma2(F2, rw_new, mul2(f2(-f3), ow)));
-      }
-      *reinterpret_cast<float2 *>(fu + c) = du;
-      *reinterpret_cast<float2 *>(fv + c) = dv;
-      *reinterpret_cast<float2 *>(fw + c) = dw;
-      if (STAGE != 3) {
-        *reinterpret_cast<float2 *>(ru + c) = ru_new;
-        *reinterpret_cast<float2 *>(rv + c) = rv_new;
-        *reinterpret_cast<float2 *>(rw + c) = rw_new;
-      }
+      const PairPlanes P{&su[cm][0][0], &su[c0][0][0], &su[cp][0][0], &sv[cm][0][0], &sv[c0][0][0],
+                         &sv[cp][0][0], &sw[cm][0][0], &sw[c0][0][0], &sw[cp][0][0], &sp[k % 2][0][0],
+                         &sp[(k + 1) % 2][0][0]};
+      pair_cells<STAGE, BUOY, QROW>(P, 2 * tx + 2, ty + 1, k * PL + j * g.I + i, PL, cf, ru, rv, rw, fu,
+                                    fv, fw, cb, bcoef);
     }
     __syncthreads();
   }
 }
 
+// Quads: the block's 18 x 10 quads of a plane (16-byte aligned with I a
+// multiple of 4, so that a quad never straddles the periodic wrap, which is
+// applied to whole quads) are read by its first 180 threads, one quad of
+// each field per thread, into registers one plane ahead.
+constexpr int QQX = TBX / 4, NQUAD = QQX * TBY;
+template <int STAGE, bool BUOY>
+__global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_quad(PREDICT_ARGS) {
+  __shared__ __align__(16) float su[3][TBY][TBX], sv[3][TBY][TBX], sw[3][TBY][TBX], sp[2][TBY][TBX];
+  const int tx = threadIdx.x % (QTX / 2), ty = threadIdx.x / (QTX / 2);
+  const int i0 = blockIdx.x * QTX, j0 = blockIdx.y * QTY;
+  const int k0 = 1 + blockIdx.z * QKC, k1 = min(g.K, k0 + QKC - 1);
+  const int i = i0 + 2 * tx, j = j0 + ty;
+  const bool in = i < g.I && j < g.J;
+  const int PL = g.I * g.J;  // 32-bit offsets: launched only for fields < 2^31 cells
+  const bool has = threadIdx.x < NQUAD;
+  const int qy = threadIdx.x / QQX, qx = threadIdx.x - qy * QQX;
+  const int gx = (((i0 - 4 + 4 * qx) % g.I) + g.I) % g.I, gy = (((j0 - 1 + qy) % g.J) + g.J) % g.J;
+  const int qoff = gy * g.I + gx, qsm = qy * TBX + 4 * qx;
+  float4 nu, nv, nw, np_;
+  auto fetch = [&](int kk) {
+    if (has) {
+      const int o = kk * PL + qoff;
+      nu = __ldg(reinterpret_cast<const float4 *>(u + o));
+      nv = __ldg(reinterpret_cast<const float4 *>(v + o));
+      nw = __ldg(reinterpret_cast<const float4 *>(w + o));
+      np_ = __ldg(reinterpret_cast<const float4 *>(p + o));
+    }
+  };
+  auto commit = [&](int kk) {
+    if (has) {
+      *reinterpret_cast<float4 *>(&su[kk % 3][0][0] + qsm) = nu;
+      *reinterpret_cast<float4 *>(&sv[kk % 3][0][0] + qsm) = nv;
+      *reinterpret_cast<float4 *>(&sw[kk % 3][0][0] + qsm) = nw;
+      *reinterpret_cast<float4 *>(&sp[kk % 2][0][0] + qsm) = np_;
+    }
+  };
+  fetch(k0 - 1);
+  commit(k0 - 1);
+  fetch(k0);
+  commit(k0);
+  fetch(k0 + 1);
+  const PairCoef cf(g, f1, f2_, f3);
+  for (int k = k0; k <= k1; ++k) {
+    commit(k + 1);
+    __syncthreads();
+    if (k + 1 <= k1) fetch(k + 2);
+    if (in) {
+      const int cm = (k - 1) % 3, c0 = k % 3, cp = (k + 1) % 3;
+      const PairPlanes P{&su[cm][0][0], &su[c0][0][0], &su[cp][0][0], &sv[cm][0][0], &sv[c0][0][0],
+                         &sv[cp][0][0], &sw[cm][0][0], &sw[c0][0][0], &sw[cp][0][0], &sp[k % 2][0][0],
+                         &sp[(k + 1) % 2][0][0]};
+      pair_cells<STAGE, BUOY, TBX>(P, 2 * tx + 4, ty + 1, k * PL + j * g.I + i, PL, cf, ru, rv, rw, fu,
+                                   fv, fw, cb, bcoef);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The quad rows staged by the tensor-memory accelerator: one
+// cp.async.bulk.tensor load per field and plane brings the block's 72 x 10
+// box (x from i0 - 4, 16-byte aligned) from HBM into shared memory,
+// completing on the slot's mbarrier.  Four slots per field hold the planes
+// k-1, k, k+1 being read and k+2 in flight; the next load is issued into the
+// slot of k-1 once the block has finished reading it.  Box cells outside the
+// domain (filled with zeros by the copy) are patched with their periodic
+// images by plain loads, fetched one plane ahead into registers.  Measured
+// at 256^3 this stages no faster than the quads through registers (the
+// waits for the copies stay on the critical path at every prefetch depth
+// tried), so it is selectable (IBM_PREDICTOR_TMA), not the default.
+// ---------------------------------------------------------------------------
+constexpr int TSLOT = ((TBX * TBY * 4 + 127) / 128) * 128 / 4;     // floats per field slot (128-byte aligned)
+constexpr int TNS = 4;                                             // slots per field
+constexpr int TPATCH = (QTX + 2) * TBY;                            // cells of the box the stencils read
+constexpr int TPQ = (TPATCH + QTX / 2 * QTY - 1) / (QTX / 2 * QTY);  // patch cells per thread
+constexpr size_t TMA_SMEM = (size_t)TNS * 4 * TSLOT * 4 + 128;
+struct TmaFields {
+  CUtensorMap u, v, w, p;
+};
+namespace {
+__device__ __forceinline__ uint32_t sm_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool tma_wait(uint64_t *bar, uint32_t parity) {
+  for (long it = 0; it < (1L << 22); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(sm_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_plane(const TmaFields &tm, float *slot, uint64_t *bar, int x, int y, int z) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sm_addr(bar)), "r"(4 * TBX * TBY * 4)
+               : "memory");
+  const CUtensorMap *m[4] = {&tm.u, &tm.v, &tm.w, &tm.p};
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(sm_addr(slot + f * TSLOT)),
+        "l"(reinterpret_cast<uint64_t>(m[f])), "r"(x), "r"(y), "r"(z), "r"(sm_addr(bar))
+        : "memory");
+}
+}  // namespace
+
+template <int STAGE, bool BUOY>
+__global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_tma(PREDICT_ARGS, const __grid_constant__ TmaFields tm,
+                                                                 int kc, int *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char tma_sm[];
+  float *sbase = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tma_sm) + 127) & ~uintptr_t(127));
+  __shared__ __align__(8) uint64_t bar[TNS];
+  constexpr int NT = QTX / 2 * QTY;
+  const int tx = threadIdx.x % (QTX / 2), ty = threadIdx.x / (QTX / 2);
+  const int i0 = blockIdx.x * QTX, j0 = blockIdx.y * QTY;
+  const int k0 = 1 + blockIdx.z * kc, k1 = min(g.K, k0 + kc - 1);
+  const int pfirst = k0 - 1, plast = k1 + 1;  // planes this block reads
+  const int i = i0 + 2 * tx, j = j0 + ty;
+  const bool in = i < g.I && j < g.J;  // I even: i + 1 < I as well
+  const int PL = g.I * g.J;  // 32-bit offsets: launched only for fields < 2^31 cells
+  auto sidx = [&](int P) { return (P - pfirst) & (TNS - 1); };
+  auto slot_of = [&](int P) { return sbase + sidx(P) * 4 * TSLOT; };
+  auto parity_of = [&](int P) { return (uint32_t)(((P - pfirst) / TNS) & 1); };
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < TNS; ++q) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sm_addr(&bar[q])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int P = pfirst; P <= min(plast, pfirst + TNS - 1); ++P)
+      tma_load_plane(tm, slot_of(P), &bar[sidx(P)], i0 - 4, j0 - 1, P);
+  // box cells outside the domain that the stencils read: their periodic
+  // images by plain loads (none in tiles away from the domain's edges).
+  // Thread cell q is e = tid + q NT of the (QTX + 2) x TBY region from x =
+  // i0 - 1; bit q of pmask marks the ones outside.
+  auto patch_cell = [&](int q, int &hyx, int &off) {
+    const int e = threadIdx.x + q * NT;
+    const int hy = e / (QTX + 2), hx = e - hy * (QTX + 2) + 3;
+    const int gx = i0 - 4 + hx, gy = j0 - 1 + hy;
+    hyx = hy * TBX + hx;
+    off = (((gy % g.J) + g.J) % g.J) * g.I + ((gx % g.I) + g.I) % g.I;
+    return e < TPATCH && (gx < 0 || gx >= g.I || gy < 0 || gy >= g.J);
+  };
+  unsigned pmask = 0;
+#pragma unroll
+  for (int q = 0; q < TPQ; ++q) {
+    int a, b;
+    if (patch_cell(q, a, b)) pmask |= 1u << q;
+  }
+  const bool edge = __syncthreads_or(pmask != 0) != 0;  // the block patches cells
+  float nu[TPQ], nv[TPQ], nw[TPQ], np_[TPQ];
+  auto fetch = [&](int P) {
+#pragma unroll
+    for (int q = 0; q < TPQ; ++q)
+      if (pmask & (1u << q)) {
+        int a, b;
+        patch_cell(q, a, b);
+        const int o = P * PL + b;
+        nu[q] = u[o]; nv[q] = v[o]; nw[q] = w[o]; np_[q] = p[o];
+      }
+  };
+  auto commit = [&](int P) {
+    float *sl = slot_of(P);
+#pragma unroll
+    for (int q = 0; q < TPQ; ++q)
+      if (pmask & (1u << q)) {
+        int a, b;
+        patch_cell(q, a, b);
+        sl[a] = nu[q];
+        sl[TSLOT + a] = nv[q];
+        sl[2 * TSLOT + a] = nw[q];
+        sl[3 * TSLOT + a] = np_[q];
+      }
+  };
+  // bounded wait on plane P, the same outcome in every thread
+  bool failed = false;
+  auto wait_plane = [&](int P) {
+    const bool ok = tma_wait(&bar[sidx(P)], parity_of(P));
+    failed = __syncthreads_or(!ok) != 0;
+  };
+  int issued = min(plast, pfirst + TNS - 1);  // last plane whose load is issued
+  int waited = pfirst - 1;                    // last plane waited for
+  fetch(pfirst);
+  wait_plane(pfirst);
+  waited = pfirst;
+  if (!failed) {
+    commit(pfirst);
+    fetch(pfirst + 1);
+    wait_plane(pfirst + 1);
+    waited = pfirst + 1;
+  }
+  if (!failed) {
+    commit(pfirst + 1);
+    fetch(pfirst + 2);
+  }
+  const PairCoef cf(g, f1, f2_, f3);
+  for (int k = k0; k <= k1 && !failed; ++k) {
+    wait_plane(k + 1);
+    if (failed) break;
+    waited = k + 1;
+    if (edge) {
+      commit(k + 1);
+      if (k + 2 <= plast) fetch(k + 2);
+      __syncthreads();
+    }
+    if (in) {
+      const float *Sm = slot_of(k - 1), *S0 = slot_of(k), *Sp = slot_of(k + 1);
+      const PairPlanes P{Sm, S0, Sp, Sm + TSLOT, S0 + TSLOT, Sp + TSLOT, Sm + 2 * TSLOT, S0 + 2 * TSLOT,
+                         Sp + 2 * TSLOT, S0 + 3 * TSLOT, Sp + 3 * TSLOT};
+      pair_cells<STAGE, BUOY, TBX>(P, 2 * tx + 4, ty + 1, k * PL + j * g.I + i, PL, cf, ru, rv, rw, fu,
+                                   fv, fw, cb, bcoef);
+    }
+    // the slot of plane k - 1 is free once every thread is past this point;
+    // the patches written into it are ordered before the next copy into it
+    if (pmask) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && issued < plast) {
+      ++issued;
+      tma_load_plane(tm, slot_of(issued), &bar[sidx(issued)], i0 - 4, j0 - 1, issued);
+    }
+  }
+  if (failed && threadIdx.x == 0) {
+    // a copy did not complete within the limit: flag it, and give the copies
+    // still in flight a bounded time to land before the block exits
+    atomicExch(err, 1);
+    for (int P = waited + 1; P <= issued; ++P) tma_wait(&bar[sidx(P)], parity_of(P));
+  }
+}
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+// 3-D map of one FP32 cell field (I, J, K + 2), box 72 x 10 x 1
+bool encode_field_map(CUtensorMap *m, const Geo &g, const float *f) {
+  auto enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(f) & 15)) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)g.I, (cuuint64_t)g.J, (cuuint64_t)(g.K + 2)};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.I * 4, (cuuint64_t)g.I * g.J * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)TBX, (cuuint32_t)TBY, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(f), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+int tma_blocks_per_sm() {
+  static int n = [] {
+    int nb = 0;
+    for (auto k : {k_predict_tma<1, false>, k_predict_tma<2, false>, k_predict_tma<3, false>,
+                   k_predict_tma<1, true>, k_predict_tma<2, true>, k_predict_tma<3, true>})
+      if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TMA_SMEM) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_predict_tma<2, false>, QTX / 2 * QTY, TMA_SMEM) !=
+        cudaSuccess)
+      return 0;
+    return nb;
+  }();
+  return n;
+}
+}  // namespace
+
+// The TMA-staged stage: false when it does not apply (rows not a multiple of
+// 4 cells, no tensor-map encoder).
+bool launch_predict_tma(cudaStream_t s, const Geo &g, int stage, const float *u, const float *v, const float *w,
+                        const float *p, float *ru, float *rv, float *rw, float *fu, float *fv, float *fw, float a,
+                        float b, float c, const double *cb, double bcoef, int *err) {
+  if (!err || g.I % 4 != 0 || g.nfield >= (1L << 31)) return false;
+  const int nbs = tma_blocks_per_sm();
+  if (nbs <= 0) return false;
+  TmaFields tm;
+  if (!encode_field_map(&tm.u, g, u) || !encode_field_map(&tm.v, g, v) || !encode_field_map(&tm.w, g, w) ||
+      !encode_field_map(&tm.p, g, p))
+    return false;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // z chunks: the split that keeps the resident-block waves fullest, net of
+  // the two halo planes each chunk reads in addition, at most 24 planes
+  // (measured fastest at 256^3)
+  const int tiles = ((g.I + QTX - 1) / QTX) * ((g.J + QTY - 1) / QTY), slots = std::max(1, nsm * nbs);
+  int kc = g.K;
+  double best = -1.;
+  for (int nz = 1; nz <= std::min(g.K, 64); ++nz) {
+    const int kcz = (g.K + nz - 1) / nz, nb = tiles * ((g.K + kcz - 1) / kcz);
+    if (kcz > 24 && nz < std::min(g.K, 64)) continue;
+    const double waves = (double)nb / slots, eff = waves / std::ceil(waves) * kcz / (kcz + 2.);
+    if (eff > best + 1e-9) { best = eff; kc = kcz; }
+  }
+  dim3 grd((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + kc - 1) / kc);
+  auto go = [&](auto kern) {
+    kern<<<grd, QTX / 2 * QTY, TMA_SMEM, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef, tm, kc, err);
+  };
+  if (cb) {
+    if (stage == 1) go(k_predict_tma<1, true>);
+    else if (stage == 2) go(k_predict_tma<2, true>);
+    else go(k_predict_tma<3, true>);
+  } else {
+    if (stage == 1) go(k_predict_tma<1, false>);
+    else if (stage == 2) go(k_predict_tma<2, false>);
+    else go(k_predict_tma<3, false>);
+  }
+  return true;
+}
+
 template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
                     T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3, const double *cb,
-                    double bcoef) {
+                    double bcoef, int kind, int *err) {
   if constexpr (sizeof(T) == 4 && sizeof(TU) == 4) {
     if (g.nfield < (1L << 31)) {
     const float a = (float)f1, b = (float)f2, c = (float)f3;
-    if (g.I % 2 == 0 && predict_pairs()) {
-      dim3 grd((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + QKC - 1) / QKC);
-      auto go = [&](auto kern) {
-        kern<<<grd, QTX / 2 * QTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
-      };
+    if (kind == IBM_PREDICTOR_TMA &&
+        launch_predict_tma(s, g, stage, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef, err))
+      return;
+    dim3 gq((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + QKC - 1) / QKC);
+    auto goq = [&](auto kern) {
+      kern<<<gq, QTX / 2 * QTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
+    };
+    if (g.I % 4 == 0 && (kind == IBM_PREDICTOR_AUTO || kind == IBM_PREDICTOR_TMA)) {
       if (cb) {
-        if (stage == 1) go(k_predict_pair<1, true>);
-        else if (stage == 2) go(k_predict_pair<2, true>);
-        else go(k_predict_pair<3, true>);
+        if (stage == 1) goq(k_predict_quad<1, true>);
+        else if (stage == 2) goq(k_predict_quad<2, true>);
+        else goq(k_predict_quad<3, true>);
       } else {
-        if (stage == 1) go(k_predict_pair<1, false>);
-        else if (stage == 2) go(k_predict_pair<2, false>);
-        else go(k_predict_pair<3, false>);
+        if (stage == 1) goq(k_predict_quad<1, false>);
+        else if (stage == 2) goq(k_predict_quad<2, false>);
+        else goq(k_predict_quad<3, false>);
+      }
+      return;
+    }
+    if (g.I % 2 == 0 && kind != IBM_PREDICTOR_CELLS) {
+      if (cb) {
+        if (stage == 1) goq(k_predict_pair<1, true>);
+        else if (stage == 2) goq(k_predict_pair<2, true>);
+        else goq(k_predict_pair<3, true>);
+      } else {
+        if (stage == 1) goq(k_predict_pair<1, false>);
+        else if (stage == 2) goq(k_predict_pair<2, false>);
+        else goq(k_predict_pair<3, false>);
       }
       return;
     }
@@ -490,10 +844,11 @@ void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const 
 template void launch_predict<double, double>(cudaStream_t, const Geo &, int, const double *, const double *,
                                              const double *, const double *, double *, double *, double *,
                                              double *, double *, double *, double, double, double, const double *,
-                                             double);
+                                             double, int, int *);
 template void launch_predict<float, float>(cudaStream_t, const Geo &, int, const float *, const float *,
                                            const float *, const float *, float *, float *, float *, float *,
-                                           float *, float *, double, double, double, const double *, double);
+                                           float *, float *, double, double, double, const double *, double, int,
+                                           int *);
 
 // ---------------------------------------------------------------------------
 // Scalar: scalad (scal.f90:11-58) fused with the dcdt update of rk1..rk3

@@ -112,6 +112,8 @@ struct ibm_ctx {
   double *cnext = nullptr;      // dcdt of the substep: cnew after the projection
   double *crk = nullptr;        // dcrkold, the scalar's stored right-hand side
   bool c_pending = false;       // cnext holds this substep's scalar
+  int pred_kind = IBM_PREDICTOR_AUTO;  // mixed forms: predictor kernel (ibm_set_predictor_kernel)
+  int *ferr = nullptr;          // [4] fluid kernels' flags: [0] a staged-plane copy did not complete
   int proj_solves = 1;          // mixed forms: FP32 Poisson solves per projection (2: defect correction)
   ibm_scalar_params sp{};
   double kappa = 0.;
@@ -414,6 +416,7 @@ int alloc_all(ibm_ctx *c) {
   }
   if ((st = dalloc(c, &c->scratch, 4096))) return st;
   if ((st = dalloc(c, &c->dout, 64))) return st;
+  if ((st = dalloc(c, &c->ferr, 4))) return st;
   CK(cudaMallocHost((void **)&c->hpin, 64 * sizeof(double)));
   const int np = c->pg.np, nl = c->pg.nl, nq = c->nq;
   if (np > 0) {
@@ -486,6 +489,12 @@ int alloc_all(ibm_ctx *c) {
 }
 
 int check_flags(ibm_ctx *c) {
+  if (c->ferr) {
+    int f = 0;
+    CK(cudaMemcpyAsync(&f, c->ferr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (f) return set_err(c, IBM_E_NOT_CONVERGED, "a staged-plane copy of the predictor did not complete in time");
+  }
   if (c->pg.np == 0) return IBM_OK;
   int h[5];
   CK(cudaMemcpyAsync(h, c->pb.err, 5 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -513,7 +522,7 @@ int predict(ibm_ctx *c, int rkiter, double dt) {
   const double bcoef = 0.5 * c->sp.beta * 9.81;
   if (c->mixed)
     PROBED(IBM_PROBE_PREDICT, launch_predict<float, float>(c->stream, g, rkiter, c->u32, c->v32, c->w32, c->p32, c->ru32, c->rv32, c->rw32,
-                                 c->fu32, c->fv32, c->fw32, f1, f2, f3, cb, bcoef));
+                                 c->fu32, c->fv32, c->fw32, f1, f2, f3, cb, bcoef, c->pred_kind, c->ferr));
   else
     PROBED(IBM_PROBE_PREDICT, launch_predict<double, double>(c->stream, g, rkiter, c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv,
                                    c->fw, f1, f2, f3, cb, bcoef));
@@ -869,7 +878,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->pb.cstart, c->pb.cfill, c->pb.citem, c->pb.ccell, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
-                  c->cfield, c->cnext, c->crk};
+                  c->cfield, c->cnext, c->crk, c->ferr};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
@@ -1567,6 +1576,15 @@ int ibm_set_projection_solves(ibm_ctx *c, int solves) {
   if (solves != 1 && solves != 2) return set_err(c, IBM_E_INVALID, "projection solves must be 1 or 2");
   if (!c->mixed) return solves == 1 ? IBM_OK : set_err(c, IBM_E_STATE, "the FP64 form solves once");
   c->proj_solves = solves;
+  return IBM_OK;
+}
+
+int ibm_set_predictor_kernel(ibm_ctx *c, int kind) {
+  if (!c) return IBM_E_INVALID;
+  if (kind != IBM_PREDICTOR_AUTO && kind != IBM_PREDICTOR_PAIRS && kind != IBM_PREDICTOR_CELLS &&
+      kind != IBM_PREDICTOR_TMA)
+    return set_err(c, IBM_E_INVALID, "predictor kernel must be IBM_PREDICTOR_AUTO, _PAIRS, _CELLS or _TMA");
+  c->pred_kind = kind;
   return IBM_OK;
 }
 

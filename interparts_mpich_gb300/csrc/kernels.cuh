@@ -15,7 +15,8 @@ namespace ibmk {
 template <typename TU, typename T>
 void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w, const TU *p,
                     T *ru, T *rv, T *rw, T *fu, T *fv, T *fw, double f1, double f2, double f3,
-                    const double *cb = nullptr, double bcoef = 0.);
+                    const double *cb = nullptr, double bcoef = 0., int kind = IBM_PREDICTOR_AUTO,
+                    int *err = nullptr);
 template <typename TU>
 void launch_scalar_stage(cudaStream_t s, const Geo &g, int stage, const TU *u, const TU *v, const TU *w,
                          const double *cf, double *rc, double *cnext, double kappa, double f1, double f2, double f3);

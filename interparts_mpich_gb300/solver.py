@@ -265,6 +265,13 @@ class IBMSolver:
         2 (the solve plus a defect-correction solve)."""
         self._chk(self.fn["set_projection_solves"](self.ctx, int(solves)))
 
+    def set_predictor_kernel(self, kind: int):
+        """Mixed forms: the FP32 predictor kernel (_abi.IBM_PREDICTOR_AUTO:
+        planes staged by 16-byte loads; _PAIRS: 4-byte loads; _TMA: tensor-
+        memory-accelerator copies; all three give identical results;
+        _CELLS: one cell per thread)."""
+        self._chk(self.fn["set_predictor_kernel"](self.ctx, int(kind)))
+
     def set_stream(self, stream_handle: int | None):
         self._chk(self.fn["set_stream"](self.ctx, C.c_void_p(stream_handle or 0)))
 
