@@ -43,6 +43,14 @@ extern "C" {
 /* boundary condition types for the z walls (param.f90:33-34, bound.f90:17-65) */
 #define IBM_BC_NOSLIP   0
 #define IBM_BC_FREESLIP 1
+/* Periodic z (no counterpart in the reference, whose z boundaries are
+ * always walls): set for both bc_top and bc_bot.  The plain FP64 form only,
+ * at most one particle (the collision pass has no images across z); no
+ * scalar transport, no plane statistics.  Ghost planes are periodic copies,
+ * the Poisson solve in z is cyclic (Sherman-Morrison around the Thomas
+ * sweep, the zero mode pinned at its last plane), the IBM stencils and the
+ * sphere integrals wrap in z, and the particle position wraps in z. */
+#define IBM_BC_PERIODIC 2
 
 /* arithmetic forms of the step */
 #define IBM_MODE_PLAIN_FP64    0   /* drop-in: FP64 everywhere                    */

@@ -29,6 +29,7 @@ IBM_PREDICTOR_TMA = 3
 
 IBM_BC_NOSLIP = 0
 IBM_BC_FREESLIP = 1
+IBM_BC_PERIODIC = 2
 
 IBM_MODE_PLAIN_FP64 = 0
 IBM_MODE_MIXED = 1

@@ -18,7 +18,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._abi import IBM_BC_FREESLIP, IBM_BC_NOSLIP, IBM_MODE_PLAIN_FP64, IbmParams, ParticleState, dptr
+from ._abi import IBM_BC_FREESLIP, IBM_BC_NOSLIP, IBM_BC_PERIODIC, IBM_MODE_PLAIN_FP64, IbmParams, ParticleState, dptr
 
 
 def derived_nl(radius: float, dxi: float) -> int:
@@ -38,15 +38,21 @@ def fibonacci_sphere(nl: int) -> tuple[np.ndarray, np.ndarray]:
 
 
 def bounduvw(u, v, w, bc_top=IBM_BC_NOSLIP, bc_bot=IBM_BC_NOSLIP):
-    """Reference ghost values (bound.f90:11-80) on (0:i1,0:j1,0:k1) arrays."""
-    s_top = -1.0 if bc_top == IBM_BC_NOSLIP else 1.0
-    s_bot = -1.0 if bc_bot == IBM_BC_NOSLIP else 1.0
-    u[:, :, -1] = s_top * u[:, :, -2]
-    v[:, :, -1] = s_top * v[:, :, -2]
-    w[:, :, -2] = 0.0
-    u[:, :, 0] = s_bot * u[:, :, 1]
-    v[:, :, 0] = s_bot * v[:, :, 1]
-    w[:, :, 0] = 0.0
+    """Reference ghost values (bound.f90:11-80) on (0:i1,0:j1,0:k1) arrays;
+    with IBM_BC_PERIODIC the z ghost planes are periodic copies."""
+    if bc_top == IBM_BC_PERIODIC:
+        for f in (u, v, w):
+            f[:, :, -1] = f[:, :, 1]
+            f[:, :, 0] = f[:, :, -2]
+    else:
+        s_top = -1.0 if bc_top == IBM_BC_NOSLIP else 1.0
+        s_bot = -1.0 if bc_bot == IBM_BC_NOSLIP else 1.0
+        u[:, :, -1] = s_top * u[:, :, -2]
+        v[:, :, -1] = s_top * v[:, :, -2]
+        w[:, :, -2] = 0.0
+        u[:, :, 0] = s_bot * u[:, :, 1]
+        v[:, :, 0] = s_bot * v[:, :, 1]
+        w[:, :, 0] = 0.0
     for f in (u, v, w):
         f[-1, :, :] = f[1, :, :]
         f[0, :, :] = f[-2, :, :]
@@ -228,14 +234,17 @@ def wide_channel_case(nx: int = 512, nz: int = 256, nspheres: int = 8000, seed: 
                 gap=0.05)
 
 
-def settling_case(n: int = 64, seed: int = 1) -> Case:
-    """Single settling sphere D = 16 dx, density ratio 1.5, Galileo 150, fluid at
-    rest, unit cube.  The reference has walls in z, so the periodic-z cube is run
-    with free-slip walls."""
+def settling_case(n: int = 64, seed: int = 1, periodic: bool = True) -> Case:
+    """Single settling sphere D = 16 dx at the centre of the unit cube,
+    density ratio 1.5, Galileo 150 (nu = sqrt((rho_r - 1) g D^3) / Ga),
+    fluid at rest.  periodic: triply periodic (IBM_BC_PERIODIC in z, a
+    variant of the method the reference, with walls in z, cannot express);
+    otherwise free-slip walls in z."""
     R = 8.0 / n
     D = 2 * R
     ga = 150.0
     visc = math.sqrt((1.5 - 1.0) * 9.81 * D ** 3) / ga
-    return Case(name=f"settling{n}", itot=n, jtot=n, ktot=n, visc=visc, radius=R, ratiorho=1.5,
-                bc_top=IBM_BC_FREESLIP, bc_bot=IBM_BC_FREESLIP, np=1, seed=seed, flow="pur", perturb=0.0,
+    bc = IBM_BC_PERIODIC if periodic else IBM_BC_FREESLIP
+    return Case(name=f"settling{n}{'p' if periodic else 'w'}", itot=n, jtot=n, ktot=n, visc=visc, radius=R,
+                ratiorho=1.5, bc_top=bc, bc_bot=bc, np=1, seed=seed, flow="pur", perturb=0.0,
                 centres=np.array([[0.5, 0.5, 0.5]]))

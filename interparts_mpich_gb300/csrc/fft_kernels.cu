@@ -548,9 +548,11 @@ __global__ void __launch_bounds__(128) k_fillps_fftx(Geo g, FftPlan plx, const T
         df_add(sh, sl, th, tl, sh, sl);
         val = (T)(sh + sl);
       } else {
-        const TA wk = (k == g.K) ? (TA)0 : (TA)fw[c];
-        const TA wkm = (TA)fw[c - g.plane];  // plane 0 holds w(0)=0
-        if (k == g.K) fw[c] = (TIn)0;
+        // walls: w(kmax) = 0 (bounduvw on dudt), plane 0 holds w(0) = 0;
+        // periodic z: w(kmax) is an unknown and w(0) = w(kmax)
+        const TA wk = (k == g.K && !g.zper) ? (TA)0 : (TA)fw[c];
+        const TA wkm = (TA)fw[(k == 1 && g.zper) ? c + (long)(g.K - 1) * g.plane : c - g.plane];
+        if (k == g.K && !g.zper) fw[c] = (TIn)0;
         const TA vjm = (TA)fv[fidx(g, i, j == 0 ? g.J - 1 : j - 1, k)];
         const TA uim = (TA)fu[fidx(g, i == 0 ? g.I - 1 : i - 1, j, k)];
         val = (T)((wk - wkm) * (TA)dtidzi + ((TA)fv[c] - vjm) * (TA)dtidyi + ((TA)fu[c] - uim) * (TA)dtidxi);
@@ -683,6 +685,92 @@ __global__ void __launch_bounds__(128) k_thomas(Geo g, typename cpx<T>::t *__res
 #pragma unroll
     for (int q = 0; q < PF; ++q)
       if (k1 - q >= 0) st(k1 - q, buf[q]);
+  }
+}
+
+// Periodic z: the cyclic tridiagonal solve of every (kx, ky) mode in FP64,
+// one thread per column: Sherman-Morrison around the Thomas sweep (diagonal
+// -2 a2 + xy, off-diagonals and corners a2; gamma = -b), the zero mode
+// (xy = 0) pinned at its last plane.  The same operation order as the
+// oracle's cyclic_solve; the two right-hand sides (the spectrum and the
+// Sherman-Morrison vector) are swept together.  xy = xrt(kx) + yrt(ky) from
+// the host tables.
+__global__ void __launch_bounds__(128) k_thomas_cyclic(Geo g, double2 *__restrict__ S, const double *__restrict__ xrt,
+                                                       const double *__restrict__ yrt, double a2, double scale,
+                                                       double *__restrict__ work) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long ncol = (long)g.MX * g.J;
+  if (t >= ncol) return;
+  const int kx = (int)(t % g.MX), ky = (int)(t / g.MX);
+  const long sstride = (long)g.J * g.MX;
+  double2 *s = S + t;
+  double *cp = work + t, *zz = work + ncol * g.K + t;  // [K][ncol] each
+  const double xy = xrt[kx] + yrt[ky];
+  const double b = -2. * a2 + xy;
+  const int K = g.K;
+  auto rd = [&](int k) { const double2 v = s[k * sstride]; return make_double2(v.x * scale, v.y * scale); };
+  if (xy == 0.) {  // rows 0..K-2 with the last unknown pinned to 0
+    const int n = K - 1;
+    double den = b;
+    cp[0] = a2 / den;
+    double2 r = rd(0);
+    r = make_double2(r.x / den, r.y / den);
+    s[0] = r;
+    for (int k = 1; k < n; ++k) {
+      den = b - a2 * cp[(long)(k - 1) * ncol];
+      cp[(long)k * ncol] = a2 / den;
+      const double2 v = rd(k);
+      r = make_double2((v.x - a2 * r.x) / den, (v.y - a2 * r.y) / den);
+      s[k * sstride] = r;
+    }
+    for (int k = n - 2; k >= 0; --k) {
+      const double2 v = s[k * sstride];
+      const double c = cp[(long)k * ncol];
+      r = make_double2(v.x - c * r.x, v.y - c * r.y);
+      s[k * sstride] = r;
+    }
+    s[(long)(K - 1) * sstride] = make_double2(0., 0.);
+    return;
+  }
+  const double gamma = -b;
+  const double b0 = b - gamma, bn = b - a2 * a2 / gamma;
+  // forward sweep of both right-hand sides: the spectrum r and u = (gamma, 0.., 0, a2)
+  double den = b0;
+  cp[0] = a2 / den;
+  double2 r = rd(0);
+  r = make_double2(r.x / den, r.y / den);
+  s[0] = r;
+  double z = gamma / den;
+  zz[0] = z;
+  for (int k = 1; k < K; ++k) {
+    const double bk = k == K - 1 ? bn : b;
+    den = bk - a2 * cp[(long)(k - 1) * ncol];
+    cp[(long)k * ncol] = a2 / den;
+    const double2 v = rd(k);
+    r = make_double2((v.x - a2 * r.x) / den, (v.y - a2 * r.y) / den);
+    s[k * sstride] = r;
+    const double uk = k == K - 1 ? a2 : 0.;
+    z = (uk - a2 * z) / den;
+    zz[(long)k * ncol] = z;
+  }
+  // back substitution of both
+  for (int k = K - 2; k >= 0; --k) {
+    const double2 v = s[k * sstride];
+    const double c = cp[(long)k * ncol];
+    r = make_double2(v.x - c * r.x, v.y - c * r.y);
+    s[k * sstride] = r;
+    z = zz[(long)k * ncol] - c * z;
+    zz[(long)k * ncol] = z;
+  }
+  // r, z hold row 0; rows K-1 from memory
+  const double2 rl = s[(long)(K - 1) * sstride];
+  const double zl = zz[(long)(K - 1) * ncol];
+  const double fdn = 1. + z + a2 * zl / gamma;
+  const double fx = (r.x + a2 * rl.x / gamma) / fdn, fy = (r.y + a2 * rl.y / gamma) / fdn;
+  for (int k = 0; k < K; ++k) {
+    const double2 v = s[k * sstride];
+    const double zk = zz[(long)k * ncol];
+    s[k * sstride] = make_double2(v.x - fx * zk, v.y - fy * zk);
   }
 }
 
@@ -891,6 +979,10 @@ void launch_poisson(cudaStream_t s, const Geo &g, const FftPlan &plx, const FftP
     k_thomas_df<<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(
         g, reinterpret_cast<float2 *>(S), thomas_df, thomas_df + (long)g.K * (g.J / 2 + 1) * g.MX, a2h, a2l,
         (float)scale);
+  } else if (g.zper) {
+    k_thomas_cyclic<<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, reinterpret_cast<double2 *>(S), zt, zt + g.MX,
+                                                                    g.dzi * g.dzi, scale,
+                                                                    const_cast<double *>(zt) + g.MX + g.J);
   } else {
     k_thomas<T><<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(g, S, zt, g.dzi * g.dzi, scale);
   }

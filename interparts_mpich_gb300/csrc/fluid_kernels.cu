@@ -941,6 +941,27 @@ __global__ void __launch_bounds__(256) k_correc(Geo g, const TF *fu, const TF *f
   const T P0 = (T)phi[c];
   const T Pip = (T)phi[fidx(g, ip, j, k)];
   const T Pjp = (T)phi[fidx(g, i, jp, k)];
+  if (g.zper) {  // periodic z: p(k1) = p(1); w(kmax) is an unknown; ghost planes are copies
+    const T Pkp = (k == g.K) ? (T)phi[c - (long)(g.K - 1) * PL] : (T)phi[c + PL];
+    const T un = (T)fu[c] - fi * (Pip - P0);
+    const T vn = (T)fv[c] - fj * (Pjp - P0);
+    const T wn = (T)fw[c] - fk * (Pkp - P0);
+    u[c] = un;
+    v[c] = vn;
+    w[c] = wn;
+    const double pnn = pn[c] + (double)phi[c];
+    pn[c] = pnn;
+    if (pn32) pn32[c] = (float)pnn;
+    const long gh = k == 1 ? c + (long)g.K * PL : (k == g.K ? c - (long)g.K * PL : -1);
+    if (gh >= 0) {  // plane 1 -> ghost k1, plane K -> ghost 0
+      u[gh] = un;
+      v[gh] = vn;
+      w[gh] = wn;
+      pn[gh] = pnn;
+      if (pn32) pn32[gh] = (float)pnn;
+    }
+    return;
+  }
   const T Pkp = (k == g.K) ? P0 : (T)phi[c + PL];
   const T un = (T)fu[c] - fi * (Pip - P0);
   const T vn = (T)fv[c] - fj * (Pjp - P0);

@@ -240,6 +240,7 @@ void derived(ibm_ctx *c) {
   g.dx = 1. / g.dxi; g.dy = 1. / g.dyi; g.dz = 1. / g.dzi;
   g.visc = P.visc;
   g.bc_top = P.bc_top; g.bc_bot = P.bc_bot;
+  g.zper = P.bc_top == IBM_BC_PERIODIC ? 1 : 0;
   c->offset = (std::sqrt(3. * (1.5 * 1.5))) / g.dxi + 0.01 / g.dxi;
   c->volp = (4. / 3.) * PI * std::pow(P.radius, 3.);
   c->mominert = (2. / 5.) * c->volp * std::pow(P.radius, 2.);
@@ -291,6 +292,7 @@ void derived(ibm_ctx *c) {
   pg.a11_ini_pw = -(1. / eps_ini_pw) + 1. / 5. * std::log(eps_ini_pw) + 1. / 21. * eps_ini_pw * std::log(eps_ini_pw) - .9713;
   pg.a11_sat_pw = -(1. / eps_sat_pw) + 1. / 5. * std::log(eps_sat_pw) + 1. / 21. * eps_sat_pw * std::log(eps_sat_pw) - .9713;
   pg.I = g.I; pg.J = g.J; pg.K = g.K;
+  pg.zper = g.zper;
   {  // collision cell list: cells >= 1.01 x 2.1 R wide
     const double w = 1.01 * 2.1 * P.radius;
     pg.ncx = std::max(1, (int)std::floor(P.lx / w));
@@ -357,6 +359,18 @@ int build_solver_tables(ibm_ctx *c) {
     yrt[k] = -4. * g.dyi * g.dyi * (s * s);
   }
   if (J % 2 == 0) yrt[J / 2] = -4. * g.dyi * g.dyi;
+  if (g.zper) {
+    // periodic z: the cyclic solve forms its pivots itself; tables xrt[MX],
+    // yrt[J] (both signs of ky) and its work space (2 K ncol)
+    const long ncol = (long)MX * J;
+    std::vector<double> tb((size_t)(MX + J), 0.);
+    for (int kx = 0; kx < MX; ++kx) tb[kx] = xrt[kx];
+    for (int ky = 0; ky < J; ++ky) tb[MX + ky] = yrt[ky <= J / 2 ? ky : J - ky];
+    if ((st = dalloc(c, &c->zt, tb.size() + (size_t)2 * K * ncol))) return st;
+    CK(cudaMemcpyAsync(c->zt, tb.data(), tb.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return IBM_OK;
+  }
   const long zst = (long)(J / 2 + 1) * MX;
   std::vector<double> z((size_t)zst * K);
   for (int ky = 0; ky <= J / 2; ++ky)
@@ -669,7 +683,7 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     PROBED(IBM_PROBE_INTERP,
            launch_ibm_interp_force<double>(c->stream, g, c->pg, c->ib, c->fu, c->fv, c->fw, dt, it == 0 ? 1 : 0));
     LAUNCHED(1);
-    if (it == 0) {  // dwdtf(:,:,k1) carries only S(F) (interp_spread.f90:267-269)
+    if (it == 0 && !g.zper) {  // dwdtf(:,:,k1) carries only S(F) (interp_spread.f90:267-269)
       launch_zero_plane<double>(c->stream, g, c->fw, g.K + 1);
       LAUNCHED(1);
     }
@@ -814,6 +828,11 @@ ibm_ctx *ibm_create(const ibm_params *P) {
   }
   if (P->mode != IBM_MODE_PLAIN_FP64 && P->mode != IBM_MODE_MIXED && P->mode != IBM_MODE_MIXED_LEARNED) {
     g_create_error = "mode must be IBM_MODE_PLAIN_FP64, IBM_MODE_MIXED or IBM_MODE_MIXED_LEARNED";
+    return nullptr;
+  }
+  if ((P->bc_top == IBM_BC_PERIODIC) != (P->bc_bot == IBM_BC_PERIODIC) ||
+      (P->bc_top == IBM_BC_PERIODIC && (P->mode != IBM_MODE_PLAIN_FP64 || P->np > 1))) {
+    g_create_error = "periodic z needs bc_top = bc_bot = IBM_BC_PERIODIC, the plain FP64 form and at most one particle";
     return nullptr;
   }
   if (P->np > 0) {
@@ -1312,6 +1331,7 @@ int ibm_run_adaptive(ibm_ctx *c, int nsteps, int ioutchk, double *dt, double *ti
 int ibm_set_scalar(ibm_ctx *c, const ibm_scalar_params *sp, const double *cf, const double *dcrk) {
   if (!c) return IBM_E_INVALID;
   if (!sp || !(sp->pran > 0.)) return set_err(c, IBM_E_INVALID, "scalar parameters need pran > 0");
+  if (c->g.zper) return set_err(c, IBM_E_STATE, "no scalar transport with periodic z");
   if ((sp->bc_c_top_type != IBM_BC_C_DIRICHLET && sp->bc_c_top_type != IBM_BC_C_NEUMANN) ||
       (sp->bc_c_bot_type != IBM_BC_C_DIRICHLET && sp->bc_c_bot_type != IBM_BC_C_NEUMANN))
     return set_err(c, IBM_E_INVALID, "scalar boundary types must be IBM_BC_C_DIRICHLET or IBM_BC_C_NEUMANN");
@@ -1395,6 +1415,7 @@ int ibm_phase_indicator(ibm_ctx *c, int itype, double *gamu, double *gamv, doubl
                         double *upart, double *vpart, double *wpart) {
   if (!c) return IBM_E_INVALID;
   if (itype != 0 && itype != 1) return set_err(c, IBM_E_INVALID, "itype must be 0 or 1");
+  if (c->g.zper) return set_err(c, IBM_E_STATE, "no plane statistics with periodic z");
   if (c->pg.np > 0 && !c->have_particles) return set_err(c, IBM_E_STATE, "no particles set");
   int st;
   if ((st = ensure_href(c))) return st;
@@ -1536,6 +1557,7 @@ static void post1d_finish(const ibm_ctx *c, const std::vector<double> &S, bool p
 int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
   if (!c) return IBM_E_INVALID;
   if (!c->have_fields) return set_err(c, IBM_E_STATE, "no fields set");
+  if (c->g.zper) return set_err(c, IBM_E_STATE, "no plane statistics with periodic z");
   const bool parts = c->pg.np > 0;
   if (parts && !c->have_particles) return set_err(c, IBM_E_STATE, "no particles set");
   int st;

@@ -74,6 +74,7 @@ struct Geo {
   long plane, nfield;         // I*J, (K+2)*I*J
   double lx, ly, lz, dxi, dyi, dzi, dx, dy, dz, visc;
   int bc_top, bc_bot;
+  int zper;  // periodic z (IBM_BC_PERIODIC): ghost planes are copies, no walls
 };
 
 struct PartGeo {
@@ -83,6 +84,7 @@ struct PartGeo {
   double kn_ss, etan_ss, kt_ss, etat_ss, muc_ss, kn_sw, etan_sw, kt_sw, etat_sw, muc_sw;
   double coeff_f, a11a_ini_pp, a11b_ini_pp, a11a_sat_pp, a11b_sat_pp, a11_ini_pw, a11_sat_pw;
   int I, J, K;
+  int zper;  // periodic z: stencils and sphere boxes wrap in z, no walls
   // uniform cell list of the collision candidate search: cells at least
   // 1.01 x the FP32 filter distance 2.1 R wide (ncx, ncy >= 3, else the
   // search scans all particles)
@@ -95,6 +97,11 @@ __host__ __device__ inline long fidx(const Geo &g, int i, int j, int k) {
 }
 __device__ __forceinline__ int wrapm(int i, int n) {  // i in [-n, 2n)
   return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+// z plane of a stencil tap: as given with walls (ghost planes stored);
+// periodic z maps planes 0, K+1, K+2 onto K, 1, 2
+__device__ __forceinline__ int zwrap(const Geo &g, int k) {
+  return g.zper ? (k < 1 ? k + g.K : (k > g.K ? k - g.K : k)) : k;
 }
 
 // Roma-Peskin 3-point regularised delta times h (kernel.f90:7-25)

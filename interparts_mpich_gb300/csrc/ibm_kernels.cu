@@ -28,21 +28,22 @@ __global__ void __launch_bounds__(256) k_ibm_stencil(Geo g, PartGeo pg, IbmBuffe
     const double xfp = b.xfp[t], yfp = b.yfp[t], zfp = b.zfp[t];
     double coorxfp = xfp * g.dxi - (double)((long)floor((xfp - 0.5 * g.dx) / g.lx) * g.I) - (1 - 1);
     double cooryfp = yfp * g.dyi - (double)((long)floor((yfp - 0.5 * g.dy) / g.ly) * g.J) - (1 - 1);
-    double coorzfp = zfp * g.dzi;
+    // periodic z: the image rule of x and y along z (no wall clamps below)
+    double coorzfp = g.zper ? zfp * g.dzi - (double)((long)floor((zfp - 0.5 * g.dz) / g.lz) * g.K) : zfp * g.dzi;
     // Guard: a point outside the grid (or a non-finite position) would index
     // outside the arrays; flag it and park the point at a safe location.
     if (!(coorxfp >= 0. && coorxfp <= g.I + 1.) || !(cooryfp >= 0. && cooryfp <= g.J + 1.) ||
-        !(coorzfp >= -1. && coorzfp <= g.K + 0.49)) {
+        !(g.zper ? (coorzfp >= 0. && coorzfp <= g.K + 1.) : (coorzfp >= -1. && coorzfp <= g.K + 0.49))) {
       atomicExch(&b.err[2], 1);
       coorxfp = 1.; cooryfp = 1.; coorzfp = 1.5;
     }
     PointStencil s;
     s.ilows = fnint(coorxfp) - 1;
     s.jlows = fnint(cooryfp) - 1;
-    s.klows = max(fnint(coorzfp) - 1, 1);
+    s.klows = g.zper ? fnint(coorzfp) - 1 : max(fnint(coorzfp) - 1, 1);
     s.ilow = (int)floor(coorxfp);
     s.jlow = (int)floor(cooryfp);
-    s.klow = max(min((int)floor(coorzfp), g.K - 2), 1);
+    s.klow = g.zper ? (int)floor(coorzfp) : max(min((int)floor(coorzfp), g.K - 2), 1);
     for (int m = 0; m < 3; ++m) {
       s.phix[m] = delta3(1. * s.ilows + m - coorxfp);
       s.phiy[m] = delta3(1. * s.jlows + m - cooryfp);
@@ -102,9 +103,14 @@ __device__ __forceinline__ void interp_point(const Geo &g, const PointStencil &s
     jy[m] = wrapm(s.jlows + m - 1, g.J);
     jyh[m] = wrapm(s.jlow + m - 1, g.J);
   }
-  interp_sep(s, [&](int i, int j, int k) { return (double)fu[fidx(g, ix[i], jyh[j], s.klow + k)]; },
-             [&](int i, int j, int k) { return (double)fv[fidx(g, ixh[i], jy[j], s.klow + k)]; },
-             [&](int i, int j, int k) { return (double)fw[fidx(g, ixh[i], jyh[j], s.klows + k)]; }, ou, ov, ow);
+  int kz[3], kzs[3];
+  for (int m = 0; m < 3; ++m) {
+    kz[m] = zwrap(g, s.klow + m);
+    kzs[m] = zwrap(g, s.klows + m);
+  }
+  interp_sep(s, [&](int i, int j, int k) { return (double)fu[fidx(g, ix[i], jyh[j], kz[k])]; },
+             [&](int i, int j, int k) { return (double)fv[fidx(g, ixh[i], jy[j], kz[k])]; },
+             [&](int i, int j, int k) { return (double)fw[fidx(g, ixh[i], jyh[j], kzs[k])]; }, ou, ov, ow);
 }
 
 // eulr2lagr + complagrforces/updtlagrforces for one particle per block:
@@ -197,17 +203,19 @@ __global__ void __launch_bounds__(256) k_ibm_spread(Geo g, PartGeo pg, IbmBuffer
       jy[m] = wrapm(s.jlows + m - 1, g.J);
       jyh[m] = wrapm(s.jlow + m - 1, g.J);
     }
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 3; ++k) {
+      const int kz = zwrap(g, s.klow + k), kzs = zwrap(g, s.klows + k);
       for (int j = 0; j < 3; ++j) {
         const double a = dfx * coeff0 * s.phiyh[j] * s.phizh[k];
         const double bb = dfy * coeff0 * s.phiy[j] * s.phizh[k];
         const double cc = dfz * coeff0 * s.phiyh[j] * s.phiz[k];
         for (int i = 0; i < 3; ++i) {
-          atomicAdd(&fu[fidx(g, ix[i], jyh[j], s.klow + k)], (T)(a * s.phix[i]));
-          atomicAdd(&fv[fidx(g, ixh[i], jy[j], s.klow + k)], (T)(bb * s.phixh[i]));
-          atomicAdd(&fw[fidx(g, ixh[i], jyh[j], s.klows + k)], (T)(cc * s.phixh[i]));
+          atomicAdd(&fu[fidx(g, ix[i], jyh[j], kz)], (T)(a * s.phix[i]));
+          atomicAdd(&fv[fidx(g, ixh[i], jy[j], kz)], (T)(bb * s.phixh[i]));
+          atomicAdd(&fw[fidx(g, ixh[i], jyh[j], kzs)], (T)(cc * s.phixh[i]));
         }
       }
+    }
   }
 }
 

@@ -177,14 +177,17 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
   float A0h = 0.f, A0l = 0.f, TAh = 0.f, TAl = 0.f, TBh = 0.f, TBl = 0.f;
   // lever arms per component: ta += la * f*w, tb += lb * f*w with
   // comp 0: (rz, -ry), comp 1: (-rz, rx), comp 2: (ry, -rx)
-  for (int nb = 0; nb <= 8; ++nb) {
+  // copies nb = 0..8 (x/y images); with periodic z each also at z -+ lz
+  const int nzs = pg.zper ? 3 : 1;
+  for (int nbz = 0; nbz < 9 * nzs; ++nbz) {
+    const int nb = nbz / nzs, zs = nbz - nb * nzs;
     if (nb > 0 && nbf[nb] != 1) continue;
     __syncthreads();  // previous copy done with the tables and the box
     if (threadIdx.x == 0) {
       int nbrecv = nb;
       if (nb > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
       double cx = PF(PF_X), cy = PF(PF_Y);
-      const double cz = PF(PF_Z);
+      const double cz = PF(PF_Z) + (zs == 1 ? -pg.lz : (zs == 2 ? pg.lz : 0.));
       if (nb > 0) copy_shift_sphere(nbrecv, g.lx, g.ly, cx, cy);
       int ilow = fnint((cx - radius) * g.dxi - 2.), ihigh = fnint((cx + radius) * g.dxi + 2.);
       int jlow = fnint((cy - radius) * g.dyi - 2.), jhigh = fnint((cy + radius) * g.dyi + 2.);
@@ -894,6 +897,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   const int qm_w = b.qmax[p];
   for (int qw_ = botw; qw_ <= topw; ++qw_) {
     const int idq = qw_;
+    if (pg.zper) break;  // periodic z: no walls
     const double deltax = 0., deltay = 0., deltaz = (qw_ - botw) * pg.lz - pz;
     const double dist = sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
     const double deltan = radius - dist;
@@ -1014,6 +1018,12 @@ __global__ void __launch_bounds__(256) k_ne_finalize(PartGeo pg, PartBuffers b, 
       if (y > pg.ly) y = y - pg.ly;
       if (y < 0.) y = y + pg.ly;
       PF(PF_X) = x; PF(PF_Y) = y;
+      if (pg.zper) {  // periodic z: the same correction along z
+        double z = PF(PF_Z);
+        if (z > pg.lz) z = z - pg.lz;
+        if (z < 0.) z = z + pg.lz;
+        PF(PF_Z) = z;
+      }
     }
     const double ro = pg.radius + pg.offset;
     const double leftb = 0., rightb = pg.lx, frontb = 0., backb = pg.ly;

@@ -169,6 +169,10 @@ struct orc_ctx {
   int itot, jtot, ktot, imax, jmax, kmax, i1, j1, k1;
   double lx, ly, lz, visc, radius, ratiorho;
   int bc_top, bc_bot, particle_rotation, np, nl, nqmax, npmax, nb_copies;
+  // periodic in z (bc_top = bc_bot = IBM_BC_PERIODIC): a variant the
+  // reference cannot express (its z boundaries are always walls, bound.f90:
+  // 17-65, initsolver.f90:26-30); see the functions marked "periodic z"
+  bool zper = false;
   // derived (init.f90:74-243)
   double dxi, dyi, dzi, dx, dy, dz, offset, volp, mominert, retrac;
   double rkcoeffab[3];
@@ -280,6 +284,17 @@ void updthalos(orc_ctx *c, Arr3 &v, int dir) {
 
 // bounduvw (bound.f90:11-80)
 void bounduvw(orc_ctx *c, Arr3 &u, Arr3 &v, Arr3 &w) {
+  if (c->zper) {  // periodic z: ghost planes are copies, w(kmax) is an unknown
+    for (int j = 0; j <= c->j1; ++j)
+      for (int i = 0; i <= c->i1; ++i)
+        for (Arr3 *f : {&u, &v, &w}) {
+          (*f)(i, j, c->k1) = (*f)(i, j, 1);
+          (*f)(i, j, 0) = (*f)(i, j, c->kmax);
+        }
+    updthalos(c, u, 1); updthalos(c, v, 1); updthalos(c, w, 1);
+    updthalos(c, u, 2); updthalos(c, v, 2); updthalos(c, w, 2);
+    return;
+  }
   for (int j = 0; j <= c->j1; ++j)
     for (int i = 0; i <= c->i1; ++i) {
       if (c->bc_top == IBM_BC_NOSLIP) {
@@ -310,8 +325,13 @@ void bounduvw(orc_ctx *c, Arr3 &u, Arr3 &v, Arr3 &w) {
 void boundp(orc_ctx *c, Arr3 &p) {
   for (int j = 0; j <= c->j1; ++j)
     for (int i = 0; i <= c->i1; ++i) {
-      p(i, j, 0) = p(i, j, 1);
-      p(i, j, c->k1) = p(i, j, c->kmax);
+      if (c->zper) {  // periodic z
+        p(i, j, 0) = p(i, j, c->kmax);
+        p(i, j, c->k1) = p(i, j, 1);
+      } else {
+        p(i, j, 0) = p(i, j, 1);
+        p(i, j, c->k1) = p(i, j, c->kmax);
+      }
     }
   updthalos(c, p, 1);
   updthalos(c, p, 2);
@@ -321,6 +341,20 @@ void boundp(orc_ctx *c, Arr3 &p) {
 // icase 1: 2-wide periodic copy; icase 2: reverse accumulation of the halos.
 void updthalos_ibm(orc_ctx *c, Arr3 &v, int dir, int icase) {
   const int imax = c->imax, jmax = c->jmax, i1 = c->i1, j1 = c->j1, k1 = c->k1;
+  if (dir == 3) {  // periodic z: the x and y patterns along k, over the full x/y halo range
+    const int kmax = c->kmax;
+    for (int j = -1; j <= j1 + 1; ++j)
+      for (int i = -1; i <= i1 + 1; ++i) {
+        if (icase == 1) {
+          v(i, j, k1) = v(i, j, 1); v(i, j, k1 + 1) = v(i, j, 2);
+          v(i, j, -1) = v(i, j, kmax - 1); v(i, j, 0) = v(i, j, kmax);
+        } else {
+          v(i, j, 1) += v(i, j, k1); v(i, j, 2) += v(i, j, k1 + 1);
+          v(i, j, kmax - 1) += v(i, j, -1); v(i, j, kmax) += v(i, j, 0);
+        }
+      }
+    return;
+  }
   if (icase == 1) {
     if (dir == 1) {
       for (int k = -1; k <= k1 + 1; ++k)
@@ -601,14 +635,21 @@ struct Stencil {
 inline void stencil(const orc_ctx *c, double xfp, double yfp, double zfp, Stencil &s) {
   const double coorxfp = xfp * c->dxi - std::floor((xfp - 0.5 * c->dx) / c->lx) * (c->itot) - (1 - 1);
   const double cooryfp = yfp * c->dyi - std::floor((yfp - 0.5 * c->dy) / c->ly) * (c->jtot) - (1 - 1);
-  const double coorzfp = zfp * c->dzi;
   const int val_k_min = 1, val_k_max = c->kmax;
   s.ilows = nint(coorxfp) - 1;
   s.jlows = nint(cooryfp) - 1;
-  s.klows = std::max(nint(coorzfp) - 1, val_k_min);
   s.ilow = ffloor(coorxfp);
   s.jlow = ffloor(cooryfp);
-  s.klow = std::max(std::min(ffloor(coorzfp), val_k_max - 2), val_k_min);
+  double coorzfp;
+  if (c->zper) {  // periodic z: the x/y image rule along z, no wall clamps
+    coorzfp = zfp * c->dzi - std::floor((zfp - 0.5 * c->dz) / c->lz) * (c->ktot);
+    s.klows = nint(coorzfp) - 1;
+    s.klow = ffloor(coorzfp);
+  } else {
+    coorzfp = zfp * c->dzi;
+    s.klows = std::max(nint(coorzfp) - 1, val_k_min);
+    s.klow = std::max(std::min(ffloor(coorzfp), val_k_max - 2), val_k_min);
+  }
   for (int m = 0; m < 3; ++m) {
     s.phix[m] = kernel(1. * s.ilows + m - coorxfp);
     s.phiy[m] = kernel(1. * s.jlows + m - cooryfp);
@@ -627,6 +668,7 @@ void eulr2lagr(orc_ctx *c) {
     }
   updthalos_ibm(c, c->dudtf, 1, 1); updthalos_ibm(c, c->dvdtf, 1, 1); updthalos_ibm(c, c->dwdtf, 1, 1);
   updthalos_ibm(c, c->dudtf, 2, 1); updthalos_ibm(c, c->dvdtf, 2, 1); updthalos_ibm(c, c->dwdtf, 2, 1);
+  if (c->zper) { updthalos_ibm(c, c->dudtf, 3, 1); updthalos_ibm(c, c->dvdtf, 3, 1); updthalos_ibm(c, c->dwdtf, 3, 1); }
 #pragma omp parallel for schedule(static)
   for (int p = 0; p < c->pmax; ++p) {
     Part &P = c->ap[p];
@@ -708,6 +750,7 @@ void lagr2eulr(orc_ctx *c, double dt) {
   }
   updthalos_ibm(c, c->dudtf, 1, 2); updthalos_ibm(c, c->dvdtf, 1, 2); updthalos_ibm(c, c->dwdtf, 1, 2);
   updthalos_ibm(c, c->dudtf, 2, 2); updthalos_ibm(c, c->dvdtf, 2, 2); updthalos_ibm(c, c->dwdtf, 2, 2);
+  if (c->zper) { updthalos_ibm(c, c->dudtf, 3, 2); updthalos_ibm(c, c->dvdtf, 3, 2); updthalos_ibm(c, c->dwdtf, 3, 2); }
   c->forceytot = c->forceytot / dt / (1. * c->itot * c->jtot * c->ktot) + c->wallshearnew;
   // iniu .ne. 'COU' always holds (lower-case values are used): add dudtold
 #pragma omp parallel for schedule(static)
@@ -753,10 +796,12 @@ void initsolver(orc_ctx *c) {
     c->c[k] = c->dzi * c->dzi;
     c->b[k] = -(c->a[k] + c->c[k]);
   }
-  c->b[1] = c->b[1] + c->a[1];
-  c->b[kmax] = c->b[kmax] + c->c[kmax];
-  c->a[1] = 0.;
-  c->c[kmax] = 0.;
+  if (!c->zper) {  // Neumann walls; periodic z keeps the cyclic corners a(1), c(kmax)
+    c->b[1] = c->b[1] + c->a[1];
+    c->b[kmax] = c->b[kmax] + c->c[kmax];
+    c->a[1] = 0.;
+    c->c[kmax] = 0.;
+  }
   std::vector<double> xrt(itot + 1), yrt(jtot + 1);
   for (int i = 3; i <= itot; i += 2) {
     xrt[i - 1] = -4. * c->dxi * c->dxi * std::pow(std::sin(double(i - 1) * PI / (2. * itot)), 2);
@@ -773,6 +818,45 @@ void initsolver(orc_ctx *c) {
   c->xyrt.assign((size_t)c->imax * c->jmax, 0.);
   for (int j = 1; j <= c->jmax; ++j)
     for (int i = 1; i <= c->imax; ++i) c->xyrt[(size_t)(i - 1) + (size_t)c->imax * (j - 1)] = xrt[i] + yrt[j];
+}
+
+// Periodic z: the cyclic tridiagonal system of one (kx, ky) mode, diagonal
+// -2 a2 + xy, off-diagonals and corners a2 (n unknowns, in place in r).
+// Sherman-Morrison around the tridiagonal part with gamma = -b: x = y -
+// f z, T y = r, T z = (gamma, 0.., 0, a2), f = (y_0 + a2 y_{n-1}/gamma) /
+// (1 + z_0 + a2 z_{n-1}/gamma), where T has b - gamma and b - a2^2/gamma in
+// its first and last diagonal entries.  The zero mode (xy = 0) is singular:
+// its last unknown is pinned to 0 and rows 0..n-2 are solved (the
+// counterpart of the reference's zero-mode guard, solver.f90:119-123).
+// w1, w2: work arrays of n.
+void tri_solve(double *r, int n, double a2, double b0, double b, double bn, double *cp) {
+  double den = b0;
+  cp[0] = a2 / den;
+  r[0] = r[0] / den;
+  for (int k = 1; k < n; ++k) {
+    const double bk = k == n - 1 ? bn : b;
+    den = bk - a2 * cp[k - 1];
+    cp[k] = a2 / den;
+    r[k] = (r[k] - a2 * r[k - 1]) / den;
+  }
+  for (int k = n - 2; k >= 0; --k) r[k] = r[k] - cp[k] * r[k + 1];
+}
+void cyclic_solve(double *r, int n, double a2, double xy, double *w1, double *w2) {
+  const double b = -2. * a2 + xy;
+  if (xy == 0.) {
+    tri_solve(r, n - 1, a2, b, b, b, w1);
+    r[n - 1] = 0.;
+    return;
+  }
+  const double gamma = -b;
+  const double b0 = b - gamma, bn = b - a2 * a2 / gamma;
+  tri_solve(r, n, a2, b0, b, bn, w1);
+  for (int k = 0; k < n; ++k) w2[k] = 0.;
+  w2[0] = gamma;
+  w2[n - 1] = a2;
+  tri_solve(w2, n, a2, b0, b, bn, w1);
+  const double f = (r[0] + a2 * r[n - 1] / gamma) / (1. + w2[0] + a2 * w2[n - 1] / gamma);
+  for (int k = 0; k < n; ++k) r[k] = r[k] - f * w2[k];
 }
 
 // solver2d (solver.f90:43-172): x-FFT, y-FFT, Thomas in k, inverse y, inverse x.
@@ -794,6 +878,18 @@ void solver2d(orc_ctx *c) {
       for (int j = 0; j < jmax; ++j) pz(i, j + 1, k) = col[j];
     }
   }
+  if (c->zper) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= jmax; ++j) {
+      std::vector<double> col(kmax), w1(kmax), w2(kmax);
+      for (int i = 1; i <= imax; ++i) {
+        for (int k = 0; k < kmax; ++k) col[k] = pz(i, j, k + 1);
+        cyclic_solve(col.data(), kmax, c->dzi * c->dzi, c->xyrt[(size_t)(i - 1) + (size_t)imax * (j - 1)],
+                     w1.data(), w2.data());
+        for (int k = 0; k < kmax; ++k) pz(i, j, k + 1) = col[k];
+      }
+    }
+  } else {
   // Thomas algorithm with the zero-mode guard (solver.f90:94-134)
 #pragma omp parallel for schedule(static)
   for (int j = 1; j <= jmax; ++j) {
@@ -817,6 +913,7 @@ void solver2d(orc_ctx *c) {
         pz(i, j, kmax) = 0.;
       for (int k = kmax - 1; k >= 1; --k) pz(i, j, k) = pz(i, j, k) - d[k] * pz(i, j, k + 1);
     }
+  }
   }
 #pragma omp parallel for schedule(static)
   for (int k = 1; k <= kmax; ++k) {
@@ -946,7 +1043,10 @@ void intgr_over_sphere(orc_ctx *c, int type) {
       if (!go) continue;
       int nbrecv = nb;
       if (nb > 0 && P.mslv > 0) { nbrecv = nb + 4; if (nbrecv > 8) nbrecv -= 8; }
-      const double cx = ax[nbrecv], cy = ay[nbrecv], cz = az[nbrecv];
+      // periodic z: the images at z -+ lz as well (clipped to the grid like
+      // the x/y copies), summed into the same copy
+      for (int zs = 0; zs < (c->zper ? 3 : 1); ++zs) {
+      const double cx = ax[nbrecv], cy = ay[nbrecv], cz = az[nbrecv] + (zs == 1 ? -c->lz : (zs == 2 ? c->lz : 0.));
       const double coorxc = cx - 0., cooryc = cy - 0., coorzc = cz;
       int ilow = nint((coorxc - radius) * c->dxi - 2.);
       int ihigh = nint((coorxc + radius) * c->dxi + 2.);
@@ -1025,6 +1125,7 @@ void intgr_over_sphere(orc_ctx *c, int type) {
             }
           }
         }
+      }
       }
     }
     double su = 0., sv = 0., sw = 0.;
@@ -1312,8 +1413,8 @@ int intgr_nwtn_eulr(orc_ctx *c, int rkiter, double dt) {
           P.qmax = qlast;
         }
       }
-      // walls (:503-603)
-      for (int q = botw; q <= topw; ++q) {
+      // walls (:503-603); none with periodic z
+      for (int q = botw; q <= (c->zper ? botw - 1 : topw); ++q) {
         const int idq = q;
         const double deltax = 0., deltay = 0., deltaz = (q - botw) * c->lz - P.z;
         const double dist = std::sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
@@ -1383,6 +1484,10 @@ int intgr_nwtn_eulr(orc_ctx *c, int rkiter, double dt) {
       if (P.x < 0.) P.x = P.x + c->lx;
       if (P.y > c->ly) P.y = P.y - c->ly;
       if (P.y < 0.) P.y = P.y + c->ly;
+      if (c->zper) {  // periodic z: the same correction along z
+        if (P.z > c->lz) P.z = P.z - c->lz;
+        if (P.z < 0.) P.z = P.z + c->lz;
+      }
     }
   }
   // re-ordering of masters (:716-1396): on one rank every particle stays
@@ -1892,6 +1997,14 @@ orc_ctx *orc_create(const ibm_params *prm) {
   c->radius = prm->radius; c->ratiorho = prm->ratiorho;
   c->bc_top = prm->bc_top; c->bc_bot = prm->bc_bot; c->particle_rotation = prm->particle_rotation;
   c->np = prm->np; c->nl = prm->nl;
+  // periodic z: both boundaries, at most one particle (no particle images
+  // across z in the collision pass)
+  if ((prm->bc_top == IBM_BC_PERIODIC) != (prm->bc_bot == IBM_BC_PERIODIC) ||
+      (prm->bc_top == IBM_BC_PERIODIC && prm->np > 1)) {
+    delete c;
+    return nullptr;
+  }
+  c->zper = prm->bc_top == IBM_BC_PERIODIC;
   c->nqmax = std::min(c->np + 2, 15);
   c->npmax = c->np;
   c->nb_copies = prm->nb_copies == 1 ? 1 : 9;
@@ -2177,6 +2290,7 @@ int orc_diagnostics(orc_ctx *c, double *wsn, double *wso, double ft[3]) {
 
 int orc_set_scalar(orc_ctx *c, const ibm_scalar_params *sp, const double *cf, const double *dcrk) {
   if (!sp || !(sp->pran > 0.)) return fail(c, IBM_E_INVALID, "scalar parameters need pran > 0");
+  if (c->zper) return fail(c, IBM_E_STATE, "no scalar transport with periodic z");
   c->kappa = c->visc / sp->pran;  // init.f90:94
   c->beta = sp->beta;
   c->bc_c_top_val = sp->bc_c_top_val; c->bc_c_bot_val = sp->bc_c_bot_val;
@@ -2195,6 +2309,7 @@ int orc_get_scalar(orc_ctx *c, double *cf, double *dcrk) {
 int orc_phase_indicator(orc_ctx *c, int itype, double *gamu, double *gamv, double *gamw, double *gamp,
                         double *upart, double *vpart, double *wpart) {
   if (itype != 0 && itype != 1) return fail(c, IBM_E_INVALID, "itype must be 0 or 1");
+  if (c->zper) return fail(c, IBM_E_STATE, "no plane statistics with periodic z");
   Arr3 a[7];
   for (auto &x : a) x.init(0, c->i1 + 1, c->j1 + 1, c->k1 + 1);
   phase_indicator(c, itype, a[0], a[1], a[2], a[3], a[4], a[5], a[6]);
@@ -2204,6 +2319,7 @@ int orc_phase_indicator(orc_ctx *c, int itype, double *gamu, double *gamv, doubl
 }
 int orc_post1d(orc_ctx *c, double *profiles, double *scalars) {
   if (!c->have_fields) return fail(c, IBM_E_STATE, "no fields set");
+  if (c->zper) return fail(c, IBM_E_STATE, "no plane statistics with periodic z");
   post1d(c, profiles, scalars);
   return IBM_OK;
 }

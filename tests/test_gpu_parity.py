@@ -153,7 +153,7 @@ def test_projection_divergence_free(gpu_lib):
 def test_settling_sphere(gpu_lib):
     """The single settling sphere (free-slip walls) for a few steps."""
     from interparts_mpich_gb300.cases import settling_case
-    case = settling_case(32)
+    case = settling_case(32, periodic=False)
     g, o, vg, vo = pair(case, gpu_lib)
     dt = 1e-3
     g.run(dt, 5)
