@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define IBM_ABI_VERSION 1
+#define IBM_ABI_VERSION 2
 
 /* status codes */
 #define IBM_OK                 0
@@ -81,6 +81,23 @@ typedef struct ibm_params {
                                   self-neighbour copies nb=0..8 (intgr_nwtn_eulr.f90:358);
                                   1: only nb=0                                 */
   int    mode;                 /* IBM_MODE_*                                   */
+  const double *radii;         /* NULL: every sphere has `radius`.  Otherwise
+                                  [np] radii (polydisperse, a variant the
+                                  reference cannot express: it has one radius
+                                  and one nl, param.f90:48, init.f90:129).
+                                  Sphere p then has nl_p = nint(pi/3*(12*((r_p-
+                                  retrac)*dxi)^2+1)) force points on the shell
+                                  r_p - retrac (retrac = 0.3/dxi); thetarc and
+                                  phirc hold the nl_p-point tables of the
+                                  spheres one after the other (sum of nl_p
+                                  entries), nl must equal the largest nl_p
+                                  (the capacity of every sphere's Lagrangian
+                                  arrays), and radius and radfp are ignored.
+                                  Pairs: contact at r_p + r_q; the spring and
+                                  dashpot of the effective mass and the
+                                  lubrication of the equivalent radius
+                                  2 r_p r_q / (r_p + r_q).  The plane
+                                  statistics reject it. */
 } ibm_params;
 
 /*

@@ -53,7 +53,7 @@ class IbmParams(C.Structure):
         ("bc_top", C.c_int), ("bc_bot", C.c_int), ("particle_rotation", C.c_int),
         ("np", C.c_int), ("nl", C.c_int),
         ("thetarc", c_double_p), ("phirc", c_double_p), ("radfp", C.c_double),
-        ("nb_copies", C.c_int), ("mode", C.c_int),
+        ("nb_copies", C.c_int), ("mode", C.c_int), ("radii", c_double_p),
     ]
 
 

@@ -94,6 +94,7 @@ class Case:
     rotation: int = 0
     centres: np.ndarray | None = None
     velocities: np.ndarray | None = None
+    radii: np.ndarray | None = None  # polydisperse: [np] radii (radius is then unused)
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -102,7 +103,16 @@ class Case:
 
     @property
     def nl(self) -> int:
-        return derived_nl(self.radius, self.dxi) if self.np > 0 else 0
+        """Points per sphere (the largest sphere's when polydisperse)."""
+        if self.np == 0:
+            return 0
+        if self.radii is not None:
+            return max(derived_nl(float(r), self.dxi) for r in self.radii)
+        return derived_nl(self.radius, self.dxi)
+
+    @property
+    def rmax(self) -> float:
+        return float(np.max(self.radii)) if self.radii is not None else self.radius
 
     @property
     def nq(self) -> int:
@@ -113,22 +123,29 @@ class Case:
         return (self.itot + 2, self.jtot + 2, self.ktot + 2)
 
     def lagrangian_table(self):
+        """(theta, phi, radfp); polydisperse: every sphere's table of its own
+        point count, one after the other (radfp unused)."""
         nl = self.nl
         if nl == 0:
             return np.zeros(1), np.zeros(1), 0.0
+        if self.radii is not None:
+            tabs = [fibonacci_sphere(derived_nl(float(r), self.dxi)) for r in self.radii]
+            return (np.ascontiguousarray(np.concatenate([t[0] for t in tabs])),
+                    np.ascontiguousarray(np.concatenate([t[1] for t in tabs])), self.rmax - 0.3 / self.dxi)
         theta, phi = fibonacci_sphere(nl)
         radfp = self.radius - 0.3 / self.dxi
         return theta, phi, radfp
 
     def params(self, mode: int = IBM_MODE_PLAIN_FP64) -> IbmParams:
         theta, phi, radfp = self.lagrangian_table()
-        self._keep = [theta, phi]
+        radii = None if self.radii is None else np.ascontiguousarray(self.radii, dtype=np.float64)
+        self._keep = [theta, phi, radii]
         return IbmParams(
             itot=self.itot, jtot=self.jtot, ktot=self.ktot, lx=self.lx, ly=self.ly, lz=self.lz,
             visc=self.visc, radius=self.radius, ratiorho=self.ratiorho,
             bc_top=self.bc_top, bc_bot=self.bc_bot, particle_rotation=self.rotation,
             np=self.np, nl=self.nl, thetarc=dptr(theta), phirc=dptr(phi), radfp=radfp,
-            nb_copies=self.nb_copies, mode=mode)
+            nb_copies=self.nb_copies, mode=mode, radii=dptr(radii) if radii is not None else None)
 
     # ---- fields -----------------------------------------------------------
     def initial_fields(self) -> dict[str, np.ndarray]:
@@ -159,10 +176,14 @@ class Case:
         return self._placed.copy()
 
     def _place_spheres(self) -> np.ndarray:
-        R = self.radius
+        """Seeded uniform centres with rejection of gaps below gap x the
+        diameter (gap x the mean of the two diameters between unequal
+        spheres) to each other and to the walls."""
+        radii = (np.asarray(self.radii, np.float64) if self.radii is not None
+                 else np.full(self.np, self.radius))
+        R = float(radii.max())
         D = 2 * R
-        zmin, zmax = R + self.gap * D, self.lz - R - self.gap * D
-        dmin = D + self.gap * D
+        dmin = D + self.gap * D  # the largest pair distance tested: cell size
         rng = np.random.default_rng(self.seed + 7919)
         out = np.zeros((self.np, 3))
         # accepted centres binned in cells at least dmin wide (periodic in x
@@ -183,7 +204,12 @@ class Case:
             tries += 1
             if tries > 2000 * max(1, self.np):
                 raise RuntimeError("could not place the spheres without overlap")
-            c = np.array([rng.uniform(0, self.lx), rng.uniform(0, self.ly), rng.uniform(zmin, zmax)])
+            rn = radii[n]
+            if self.radii is None:
+                zlo, zhi = rn + self.gap * D, self.lz - rn - self.gap * D
+            else:
+                zlo, zhi = rn * (1 + 2 * self.gap), self.lz - rn * (1 + 2 * self.gap)
+            c = np.array([rng.uniform(0, self.lx), rng.uniform(0, self.ly), rng.uniform(zlo, zhi)])
             if n:
                 ix, iy, iz = cell(c)
                 near = []
@@ -195,8 +221,14 @@ class Case:
                     d = np.abs(out[near] - c)
                     d[:, 0] = np.minimum(d[:, 0], self.lx - d[:, 0])
                     d[:, 1] = np.minimum(d[:, 1], self.ly - d[:, 1])
-                    if np.min(np.sum(d * d, axis=1)) < dmin * dmin:
-                        continue
+                    d2 = np.sum(d * d, axis=1)
+                    if self.radii is None:
+                        if np.min(d2) < dmin * dmin:
+                            continue
+                    else:
+                        lim = (radii[near] + rn) * (1 + self.gap)
+                        if np.any(d2 < lim * lim):
+                            continue
             out[n] = c
             cells.setdefault(cell(c), []).append(n)
             n += 1
@@ -248,3 +280,23 @@ def settling_case(n: int = 64, seed: int = 1, periodic: bool = True) -> Case:
     return Case(name=f"settling{n}{'p' if periodic else 'w'}", itot=n, jtot=n, ktot=n, visc=visc, radius=R,
                 ratiorho=1.5, bc_top=bc, bc_bot=bc, np=1, seed=seed, flow="pur", perturb=0.0,
                 centres=np.array([[0.5, 0.5, 0.5]]))
+
+
+def poly_case(nx: int = 768, nz: int = 384, nspheres: int = 15000, seed: int = 1234, dmin_cells: float = 12.0,
+              dmax_cells: float = 24.0) -> Case:
+    """Polydisperse settling suspension: nx x nx x nz grid on a (nx/nz,
+    nx/nz, 1) box (dx = 1/nz), periodic in x and y, no-slip walls in z; spheres
+    with D drawn uniformly from [dmin, dmax] dx (seeded), placed at random
+    without overlap (gaps >= 0.05 D); density ratio 2.0, gravity in -z,
+    Galileo number 200 on the mean diameter (nu = sqrt((rho_r - 1) g D^3) /
+    Ga); fluid at rest.  At 768 x 768 x 384 with 15000 spheres of 12..24 dx
+    the solid volume fraction is about 22 %."""
+    lx = nx / nz
+    dx = 1.0 / nz
+    rng = np.random.default_rng(seed + 104729)
+    radii = 0.5 * dx * rng.uniform(dmin_cells, dmax_cells, nspheres)
+    dmean = 0.5 * (dmin_cells + dmax_cells) * dx
+    visc = math.sqrt((2.0 - 1.0) * 9.81 * dmean ** 3) / 200.0
+    return Case(name=f"poly{nx}x{nz}_np{nspheres}", itot=nx, jtot=nx, ktot=nz, lx=lx, ly=lx, lz=1.0, visc=visc,
+                radius=float(radii.max()), ratiorho=2.0, np=nspheres, seed=seed, flow="pur", perturb=0.0, gap=0.05,
+                radii=radii)

@@ -112,6 +112,11 @@ struct ibm_ctx {
   double *cnext = nullptr;      // dcdt of the substep: cnew after the projection
   double *crk = nullptr;        // dcrkold, the scalar's stored right-hand side
   bool c_pending = false;       // cnext holds this substep's scalar
+  // polydisperse sizes (host copies; device arrays in pg)
+  std::vector<double> prad_h, pradfp_h, pdvl_h, pvol_h, pmi_h, prthr_h;
+  std::vector<int> pnl_h, ptoff_h;
+  double *psize = nullptr;      // device [6][np]: radius, shell radius, dVlagr, volume, moment of inertia, rthr
+  int *pcount = nullptr;        // device [2][np]: point count, table offset
   int pred_kind = IBM_PREDICTOR_AUTO;  // mixed forms: predictor kernel (ibm_set_predictor_kernel)
   int *ferr = nullptr;          // [4] fluid kernels' flags: [0] a staged-plane copy did not complete
   int proj_solves = 1;          // mixed forms: FP32 Poisson solves per projection (2: defect correction)
@@ -229,6 +234,18 @@ void init_mlp_params(std::vector<float> &w, unsigned seed) {
     }
 }
 
+// smallest double x with sqrt(x) >= r (sqrt is correctly rounded and
+// monotone on host and device alike)
+double sqrt_threshold(double r) {
+  double t = r * r;
+  if (std::sqrt(t) >= r) {
+    while (t > 0 && std::sqrt(std::nextafter(t, 0.)) >= r) t = std::nextafter(t, 0.);
+  } else {
+    while (!(std::sqrt(t) >= r)) t = std::nextafter(t, 1e300);
+  }
+  return t;
+}
+
 void derived(ibm_ctx *c) {
   const ibm_params &P = c->prm;
   Geo &g = c->g;
@@ -302,15 +319,59 @@ void derived(ibm_ctx *c) {
     pg.ciy = (float)(pg.ncy / P.ly);
     pg.ciz = (float)(pg.ncz / P.lz);
   }
-  // smallest double x with sqrt(x) >= radius (sqrt is correctly rounded and
-  // monotone on host and device alike)
-  double t = P.radius * P.radius;
-  if (std::sqrt(t) >= P.radius) {
-    while (t > 0 && std::sqrt(std::nextafter(t, 0.)) >= P.radius) t = std::nextafter(t, 0.);
-  } else {
-    while (!(std::sqrt(t) >= P.radius)) t = std::nextafter(t, 1e300);
+  pg.rthr = sqrt_threshold(P.radius);
+  pg.visc = P.visc;
+  pg.pc_an = PI * PI + std::pow(std::fabs(std::log(en)), 2.);
+  pg.pc_at = PI * PI + std::pow(std::fabs(std::log(et)), 2.);
+  pg.pc_b = std::pow(Nstretch * dt_estim, 2.);
+  pg.pc_en = -2. * (std::log(en));
+  pg.pc_et = -2. * (std::log(et));
+  pg.pc_ndt = Nstretch * dt_estim;
+  pg.poly = 0;
+  pg.ntab = P.nl;
+  pg.rmax = P.radius;
+  pg.box_cap = 8192;
+  if (!c->prad_h.empty()) {
+    // polydisperse: per-sphere point counts, shells, Lagrangian volumes
+    // (coordsfp.f90:84-90), volumes and moments of inertia (coordsfp.f90:
+    // 96-102) from each radius, in the oracle's expressions
+    pg.poly = 1;
+    const double retrac = 0.3 / g.dxi;
+    int off = 0;
+    double rmax = 0.;
+    c->pradfp_h.clear(); c->pdvl_h.clear(); c->pvol_h.clear(); c->pmi_h.clear(); c->prthr_h.clear();
+    c->pnl_h.clear(); c->ptoff_h.clear();
+    for (int p = 0; p < P.np; ++p) {
+      const double r = c->prad_h[p];
+      const int nlp = (int)std::lround((PI / 3.) * (12. * std::pow((r - retrac) * g.dxi, 2) + 1.));
+      const double rfp = r - retrac;
+      const double vol = (4. / 3.) * PI * std::pow(r, 3.);
+      c->pradfp_h.push_back(rfp);
+      c->pdvl_h.push_back(((4. / 3.) * PI * std::pow(rfp + 0.5 / g.dxi, 3.) -
+                           (4. / 3.) * PI * std::pow(rfp - 0.5 / g.dxi, 3.)) / (1. * nlp));
+      c->pvol_h.push_back(vol);
+      c->pmi_h.push_back((2. / 5.) * vol * std::pow(r, 2.));
+      c->prthr_h.push_back(sqrt_threshold(r));
+      c->pnl_h.push_back(nlp);
+      c->ptoff_h.push_back(off);
+      off += nlp;
+      rmax = std::max(rmax, r);
+    }
+    pg.ntab = off;
+    pg.rmax = rmax;
+    // the largest (particle, component) box of the mixed form: the shell's
+    // extent plus the 3-point stencils, per axis
+    const int ext = (int)std::ceil(2. * (rmax - retrac) * g.dxi + 6.);
+    pg.box_cap = std::min(40960, std::max(8192, ext * ext * ext));
+    // collision cell list: cells >= 1.01 x 2.1 Rmax wide
+    const double w = 1.01 * 2.1 * rmax;
+    pg.ncx = std::max(1, (int)std::floor(P.lx / w));
+    pg.ncy = std::max(1, (int)std::floor(P.ly / w));
+    pg.ncz = std::max(1, (int)std::floor(P.lz / w));
+    pg.cix = (float)(pg.ncx / P.lx);
+    pg.ciy = (float)(pg.ncy / P.ly);
+    pg.ciz = (float)(pg.ncz / P.lz);
   }
-  pg.rthr = t;
 }
 
 // twiddles and the Thomas pivots (initsolver.f90:10-66)
@@ -459,7 +520,8 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, &c->pb.nb, (size_t)np * 9))) return st;
     if ((st = dalloc(c, &c->pb.mslv, np))) return st;
     if ((st = dalloc(c, &c->pb.rkp, (size_t)RK_N * np))) return st;
-    if ((st = dalloc(c, &c->pb.sincos, (size_t)4 * nl))) return st;
+    const int nt = c->pg.ntab;  // entries of each point table (nl, or the sum of the point counts)
+    if ((st = dalloc(c, &c->pb.sincos, (size_t)4 * nt))) return st;
     if ((st = dalloc(c, &c->pb.err, 8))) return st;
     if ((st = dalloc(c, &c->pb.red, (size_t)10 * np))) return st;
     if ((st = dalloc(c, &c->pb.pos4, (size_t)np))) return st;
@@ -471,14 +533,31 @@ int alloc_all(ibm_ctx *c) {
     if ((st = dalloc(c, &c->ib.diag, 8))) return st;
     c->ib.pf = c->pb.pf;
     c->ib.err = c->pb.err;
-    std::vector<double> sc((size_t)4 * nl);
-    for (int l = 0; l < nl; ++l) {
+    std::vector<double> sc((size_t)4 * nt);
+    for (int l = 0; l < nt; ++l) {
       sc[l] = std::sin(c->thetarc[l]);
-      sc[nl + l] = std::cos(c->thetarc[l]);
-      sc[2 * nl + l] = std::sin(c->phirc[l]);
-      sc[3 * nl + l] = std::cos(c->phirc[l]);
+      sc[nt + l] = std::cos(c->thetarc[l]);
+      sc[2 * nt + l] = std::sin(c->phirc[l]);
+      sc[3 * nt + l] = std::cos(c->phirc[l]);
     }
     CK(cudaMemcpyAsync(c->pb.sincos, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (c->pg.poly) {  // per-sphere sizes on the device
+      if ((st = dalloc(c, &c->psize, (size_t)6 * np))) return st;
+      if ((st = dalloc(c, &c->pcount, (size_t)2 * np))) return st;
+      std::vector<double> ps((size_t)6 * np);
+      std::vector<int> pc((size_t)2 * np);
+      for (int p = 0; p < np; ++p) {
+        ps[p] = c->prad_h[p]; ps[np + p] = c->pradfp_h[p]; ps[2 * np + p] = c->pdvl_h[p];
+        ps[3 * np + p] = c->pvol_h[p]; ps[4 * np + p] = c->pmi_h[p]; ps[5 * np + p] = c->prthr_h[p];
+        pc[p] = c->pnl_h[p]; pc[np + p] = c->ptoff_h[p];
+      }
+      CK(cudaMemcpyAsync(c->psize, ps.data(), ps.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->pcount, pc.data(), pc.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      c->pg.prad = c->psize; c->pg.pradfp = c->psize + np; c->pg.pdvl = c->psize + 2 * np;
+      c->pg.pvol = c->psize + 3 * np; c->pg.pmi = c->psize + 4 * np; c->pg.prthr = c->psize + 5 * np;
+      c->pg.pnl = c->pcount; c->pg.ptoff = c->pcount + np;
+    }
   }
   if (c->mode == IBM_MODE_MIXED_LEARNED) {
     const int npar = mlp_nparam();
@@ -580,6 +659,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   fi.dt = dt;
   fi.dti = 1. / dt;
   fi.inv_r = (float)(1. / c->pg.radfp);
+  fi.pradfp = c->pg.poly ? c->pg.pradfp : nullptr;
   fi.mu = c->norm;
   fi.isig = c->norm + 96;
   PROBED(IBM_PROBE_MLP, c->launches += launch_mlp_features_tc(c->stream, fi, c->mt.w1b, c->mt.params, c->ly,
@@ -835,7 +915,30 @@ ibm_ctx *ibm_create(const ibm_params *P) {
     g_create_error = "periodic z needs bc_top = bc_bot = IBM_BC_PERIODIC, the plain FP64 form and at most one particle";
     return nullptr;
   }
-  if (P->np > 0) {
+  long ntab = P->nl;  // entries of the point tables
+  if (P->np > 0 && P->radii) {
+    // polydisperse: every sphere's point count from its radius; nl is their
+    // maximum, the tables hold them one after the other
+    const double dxi = P->itot / P->lx, retrac = 0.3 / dxi;
+    int nlmax = 0;
+    ntab = 0;
+    for (int p = 0; p < P->np; ++p) {
+      const double r = P->radii[p];
+      const int nlp = r > retrac ? (int)std::lround((PI / 3.) * (12. * std::pow((r - retrac) * dxi, 2) + 1.)) : 0;
+      if (!(r > retrac) || nlp < 1) {
+        g_create_error = "radii must exceed 0.3 dx (the force-point shell r - 0.3 dx)";
+        return nullptr;
+      }
+      nlmax = std::max(nlmax, nlp);
+      ntab += nlp;
+    }
+    if (nlmax != P->nl) {
+      g_create_error = "nl = " + std::to_string(P->nl) + " must equal the largest sphere's point count " +
+                       std::to_string(nlmax);
+      return nullptr;
+    }
+    if (!P->thetarc || !P->phirc) { g_create_error = "polydisperse spheres need thetarc and phirc"; return nullptr; }
+  } else if (P->np > 0) {
     // nl must equal nint(pi/3*(12*((radius-retrac)*dxi)^2+1)) (main.f90:118-132)
     const double dxi = P->itot / P->lx, retrac = 0.3 / dxi;
     const int nl = (int)std::lround((PI / 3.) * (12. * std::pow((P->radius - retrac) * dxi, 2) + 1.));
@@ -852,11 +955,13 @@ ibm_ctx *ibm_create(const ibm_params *P) {
   ibm_ctx *c = new ibm_ctx();
   c->prm = *P;
   if (P->np > 0) {
-    c->thetarc.assign(P->thetarc, P->thetarc + P->nl);
-    c->phirc.assign(P->phirc, P->phirc + P->nl);
+    c->thetarc.assign(P->thetarc, P->thetarc + ntab);
+    c->phirc.assign(P->phirc, P->phirc + ntab);
   }
+  if (P->np > 0 && P->radii) c->prad_h.assign(P->radii, P->radii + P->np);
   c->prm.thetarc = nullptr;
   c->prm.phirc = nullptr;
+  c->prm.radii = nullptr;
   c->mode = P->mode;
   c->mixed = P->mode != IBM_MODE_PLAIN_FP64;
   derived(c);
@@ -876,7 +981,7 @@ ibm_ctx *ibm_create(const ibm_params *P) {
   int st = alloc_all(c);
   if (st == IBM_OK) st = build_solver_tables(c);
   if (st == IBM_OK && (poisson_set_smem_limits<double>() != 0 || poisson_set_smem_limits<float>() != 0 ||
-                       mlp_set_smem_limits() != 0 || ibm_set_smem_limits() != 0))
+                       mlp_set_smem_limits() != 0 || ibm_set_smem_limits(c->pg.box_cap) != 0))
     st = set_err(c, IBM_E_CUDA, "cudaFuncSetAttribute failed");
   if (st == IBM_OK) st = cuda_err(c, cudaStreamSynchronize(c->stream), "create");
   if (st != IBM_OK) {
@@ -897,7 +1002,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->pb.cstart, c->pb.cfill, c->pb.citem, c->pb.ccell, c->ru32, c->rv32, c->rw32, c->fu32,
                   c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
-                  c->cfield, c->cnext, c->crk, c->ferr};
+                  c->cfield, c->cnext, c->crk, c->ferr, c->psize, c->pcount};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
@@ -1415,7 +1520,7 @@ int ibm_phase_indicator(ibm_ctx *c, int itype, double *gamu, double *gamv, doubl
                         double *upart, double *vpart, double *wpart) {
   if (!c) return IBM_E_INVALID;
   if (itype != 0 && itype != 1) return set_err(c, IBM_E_INVALID, "itype must be 0 or 1");
-  if (c->g.zper) return set_err(c, IBM_E_STATE, "no plane statistics with periodic z");
+  if (c->g.zper || c->pg.poly) return set_err(c, IBM_E_STATE, "no plane statistics with periodic z or polydisperse spheres");
   if (c->pg.np > 0 && !c->have_particles) return set_err(c, IBM_E_STATE, "no particles set");
   int st;
   if ((st = ensure_href(c))) return st;
@@ -1557,7 +1662,7 @@ static void post1d_finish(const ibm_ctx *c, const std::vector<double> &S, bool p
 int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
   if (!c) return IBM_E_INVALID;
   if (!c->have_fields) return set_err(c, IBM_E_STATE, "no fields set");
-  if (c->g.zper) return set_err(c, IBM_E_STATE, "no plane statistics with periodic z");
+  if (c->g.zper || c->pg.poly) return set_err(c, IBM_E_STATE, "no plane statistics with periodic z or polydisperse spheres");
   const bool parts = c->pg.np > 0;
   if (parts && !c->have_particles) return set_err(c, IBM_E_STATE, "no particles set");
   int st;

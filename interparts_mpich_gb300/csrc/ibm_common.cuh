@@ -85,12 +85,36 @@ struct PartGeo {
   double coeff_f, a11a_ini_pp, a11b_ini_pp, a11a_sat_pp, a11b_sat_pp, a11_ini_pw, a11_sat_pw;
   int I, J, K;
   int zper;  // periodic z: stencils and sphere boxes wrap in z, no walls
+  // polydisperse (poly = 1): per-sphere radius, force-point shell radius,
+  // Lagrangian volume, volume, moment of inertia, sphere-integral threshold
+  // (smallest double whose square root is >= the radius), point count and
+  // offset into the point table; rmax the largest radius
+  int poly;
+  double visc;
+  // host-formed factors of the pair constants: kn = (pc_an me) / pc_b,
+  // kt = (pc_at mt) / pc_b, etan = (pc_en me) / pc_ndt, etat = (pc_et mt) / pc_ndt
+  double pc_an, pc_at, pc_b, pc_en, pc_et, pc_ndt;
+  const double *prad, *pradfp, *pdvl, *pvol, *pmi, *prthr;
+  const int *pnl, *ptoff;
+  double rmax;
+  int ntab;     // entries of each of the four point tables (sum of the point counts)
+  int box_cap;  // mixed form: cells of the shared-memory box of one (particle, component)
   // uniform cell list of the collision candidate search: cells at least
   // 1.01 x the FP32 filter distance 2.1 R wide (ncx, ncy >= 3, else the
   // search scans all particles)
   int ncx, ncy, ncz;
   float cix, ciy, ciz;  // cells per unit length
 };
+
+// per-sphere sizes: the particle's own when polydisperse, else the scalars
+__device__ __forceinline__ double p_rad(const PartGeo &pg, int p) { return pg.poly ? pg.prad[p] : pg.radius; }
+__device__ __forceinline__ double p_radfp(const PartGeo &pg, int p) { return pg.poly ? pg.pradfp[p] : pg.radfp; }
+__device__ __forceinline__ double p_dvl(const PartGeo &pg, int p) { return pg.poly ? pg.pdvl[p] : pg.dVlagr; }
+__device__ __forceinline__ double p_vol(const PartGeo &pg, int p) { return pg.poly ? pg.pvol[p] : pg.volp; }
+__device__ __forceinline__ double p_mi(const PartGeo &pg, int p) { return pg.poly ? pg.pmi[p] : pg.mominert; }
+__device__ __forceinline__ double p_rthr(const PartGeo &pg, int p) { return pg.poly ? pg.prthr[p] : pg.rthr; }
+__device__ __forceinline__ int p_nl(const PartGeo &pg, int p) { return pg.poly ? pg.pnl[p] : pg.nl; }
+__device__ __forceinline__ int p_toff(const PartGeo &pg, int p) { return pg.poly ? pg.ptoff[p] : 0; }
 
 __host__ __device__ inline long fidx(const Geo &g, int i, int j, int k) {
   return ((long)k * g.J + j) * g.I + i;

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_ibm_interp_force(Geo g, PartGeo pg, Ibm
   }
   if (threadIdx.x == 0 && first >= 0) {
     double *pw = b.pf;
-    const double dV = pg.dVlagr;
+    const double dV = p_dvl(pg, p);
     const double tx = red[3][0] * dV, ty = red[4][0] * dV, tz = red[5][0] * dV;
     pw[PF_FXLTOT * pg.np + p] = red[0][0] * dV;
     pw[PF_FYLTOT * pg.np + p] = red[1][0] * dV;
@@ -187,12 +187,14 @@ template void launch_ibm_interp_force<double>(cudaStream_t, const Geo &, const P
 template <typename T>
 __global__ void __launch_bounds__(256) k_ibm_spread(Geo g, PartGeo pg, IbmBuffers b, T *__restrict__ fu,
                                                     T *__restrict__ fv, T *__restrict__ fw, double dti,
-                                                    double coeff0) {
+                                                    double coeff0_, double dt) {
   const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
     if (l >= b.nla[p]) continue;
     const PointStencil s = b.st[t];
+    // the particle's own Lagrangian volume when polydisperse
+    const double coeff0 = pg.poly ? (pg.pdvl[p] / pg.dVeul) * dt : coeff0_;
     const double dfx = (b.ul[t] - b.dudtl[t]) * dti;
     const double dfy = (b.vl[t] - b.dvdtl[t]) * dti;
     const double dfz = (b.wl[t] - b.dwdtl[t]) * dti;
@@ -267,7 +269,7 @@ void launch_ibm_spread(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffe
   (void)first;
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread<T><<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0);
+  k_ibm_spread<T><<<1216, 256, 0, s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0, dt);
 }
 template void launch_ibm_spread<double>(cudaStream_t, const Geo &, const PartGeo &, IbmBuffers, double *, double *,
                                         double *, double, int);

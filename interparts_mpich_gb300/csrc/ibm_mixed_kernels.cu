@@ -220,7 +220,8 @@ __device__ __forceinline__ float interp27(const CompStencil &s, TAP tap) {
 // (FP32: it feeds the learned loop's gate), dudtl left as it was; first ==
 // -2: the interpolation to dudtl only (the slip-residual diagnostic).
 // ---------------------------------------------------------------------------
-constexpr int INTERP_BOX = 8192;  // cells (32 KB)
+// box capacity: pg.box_cap cells (8192 = 32 KB for spheres up to about
+// D = 16 dx; polydisperse runs size it for the largest sphere)
 constexpr int INTERP_THREADS = 256;
 
 // Sums of three per-thread FP64 values over a block of NT threads (NT a
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
   __shared__ int bg[8];
   if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
   __syncthreads();
-  const bool boxed = box_ok(bg, INTERP_BOX, g.I, g.J);
+  const bool boxed = box_ok(bg, pg.box_cap, g.I, g.J);
   if (boxed) {
     load_box(g, F, bg, box, b.rowx + ((long)p * 3 + c) * IBM_BOX_ROWS);
     __syncthreads();
@@ -350,7 +351,7 @@ __global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= pg.np) return;
   const double *s = b.psum + (long)p * 9;
-  const double dV = pg.dVlagr;
+  const double dV = p_dvl(pg, p);
   double *pw = b.pf;
   const double tx = (s[7] - s[4]) * dV, ty = (s[1] - s[8]) * dV, tz = (s[5] - s[2]) * dV;
   pw[PF_FXLTOT * pg.np + p] = s[0] * dV;
@@ -365,7 +366,7 @@ __global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict
 int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                               const float *fv, const float *fw, double dt, int first, const int *gate) {
   if (pg.np == 0) return 0;
-  k_ibm_interp_comp_f<<<dim3(pg.np, 3), INTERP_THREADS, INTERP_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw,
+  k_ibm_interp_comp_f<<<dim3(pg.np, 3), INTERP_THREADS, pg.box_cap * sizeof(float), s>>>(g, pg, b, fu, fv, fw,
                                                                                          1. / dt, first, gate);
   if (first < 0) return 1;
   k_ibm_force_sums<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, gate);
@@ -387,10 +388,9 @@ int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, I
 // B / 2^28 per tap, is of the order of the FP32 rounding of the cell sums
 // it replaces (B is a few hundred times the largest prefactor).  Particles with
 // more than SPREAD_PRE points, or a bound that is zero or not finite, add
-// FP32 values into the box instead; boxes beyond SPREAD_BOX cells add per
+// FP32 values into the box instead; boxes beyond pg.box_cap cells add per
 // tap to the field.
 // ---------------------------------------------------------------------------
-constexpr int SPREAD_BOX = 8192;
 constexpr int SPREAD_PRE = 2048;
 constexpr int SPREAD_THREADS = 384;
 
@@ -414,8 +414,8 @@ __device__ __forceinline__ void spread27_box(float *box, const CompStencil &s, i
 
 __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
                                                       float *__restrict__ fv, float *__restrict__ fw, double dti,
-                                                      double coeff0, LearnedForce lf,
-                                                      const int *__restrict__ gate) {
+                                                      double coeff0_, LearnedForce lf,
+                                                      const int *__restrict__ gate, double dt) {
   if (gate && *gate == 0) return;  // learned form: plain pass not needed
   const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   __shared__ float spre[SPREAD_PRE];  // prefactors of the staged points
   if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
   __syncthreads();
-  const bool boxed = box_ok(bg, SPREAD_BOX, g.I, g.J);
+  const bool boxed = box_ok(bg, pg.box_cap, g.I, g.J);
   const bool staged = boxed && nla <= SPREAD_PRE;
   const int nbx = bg[5], nby = bg[6], nbox = nbx * nby * bg[7];
   if (boxed) {
@@ -455,6 +455,8 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     dtif = (float)lf.dti; dtf = (float)(1. / lf.dti);
   }
   // prefactors F coeff0 (F given) or (U - u~) dti coeff0, as FP32 products
+  // (coeff0 with the particle's own Lagrangian volume when polydisperse)
+  const double coeff0 = pg.poly ? (pg.pdvl[p] / pg.dVeul) * dt : coeff0_;
   const float pcoef = (float)coeff0, ucoef = (float)(dti * coeff0);
   // Taps into the box: points in transposed order, the 32 lanes of a warp
   // taking points nq apart in the particle's list (neighbouring points have
@@ -572,8 +574,8 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
                          float *fw, double dt, const LearnedForce &lf, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_f<<<dim3(pg.np, 3), SPREAD_THREADS, SPREAD_BOX * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt,
-                                                                                  coeff0, lf, gate);
+  k_ibm_spread_f<<<dim3(pg.np, 3), SPREAD_THREADS, pg.box_cap * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt,
+                                                                                    coeff0, lf, gate, dt);
 }
 void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b) {
   if (pg.np == 0) return;
@@ -670,9 +672,10 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
       continue;
     }
     const float4 cf = b.pcen[p];
-    const float nrm[3] = {rec_armf(rec_dx(rr.rel), rr.fx, cf.x, (float)g.dx) * inv_r,
-                          rec_armf(rec_dy(rr.rel), rr.fy, cf.y, (float)g.dy) * inv_r,
-                          rec_armf(rec_dz(rr.rel), rr.fz, cf.z, (float)g.dz) * inv_r};
+    const float ir = pg.poly ? (float)(1. / pg.pradfp[p]) : inv_r;  // the sphere's own shell when polydisperse
+    const float nrm[3] = {rec_armf(rec_dx(rr.rel), rr.fx, cf.x, (float)g.dx) * ir,
+                          rec_armf(rec_dy(rr.rel), rr.fy, cf.y, (float)g.dy) * ir,
+                          rec_armf(rec_dz(rr.rel), rr.fz, cf.z, (float)g.dz) * ir};
     const float *F3[3] = {fu, fv, fw};
     double *D3[3] = {b.dudtl, b.dvdtl, b.dwdtl};
     double *Fl3[3] = {b.fxl, b.fyl, b.fzl};
@@ -714,12 +717,18 @@ void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmB
                                         first_force);
 }
 
-int ibm_set_smem_limits() {
+// the box kernels' dynamic shared memory, raised (never lowered: other
+// contexts may use larger boxes) to box_cap cells
+int ibm_set_smem_limits(int box_cap) {
+  static int cur = 0;
+  if (box_cap <= cur) return 0;
   cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        SPREAD_BOX * (int)sizeof(float));
+                                        box_cap * (int)sizeof(float));
   cudaError_t e2 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        INTERP_BOX * (int)sizeof(float));
-  return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
+                                        box_cap * (int)sizeof(float));
+  if (e1 != cudaSuccess || e2 != cudaSuccess) return -1;
+  cur = box_cap;
+  return 0;
 }
 
 }  // namespace ibmk

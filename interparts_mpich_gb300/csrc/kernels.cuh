@@ -158,7 +158,7 @@ struct MlpTrainBuffers {
   __nv_bfloat16 *h1, *h2, *dz1, *dz2;         // [nb][128]
 };
 int mlp_nparam();
-int ibm_set_smem_limits();
+int ibm_set_smem_limits(int box_cap);
 int mlp_set_smem_limits();
 void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
                         const __nv_bfloat16 *w2b, const float *params, float *y, float *z1, float *z2,
@@ -187,6 +187,7 @@ struct FeatIn {
   double *Fl[3];
   double dt, dti;
   float inv_r;
+  const double *pradfp;  // polydisperse: per-sphere shell radius (the normal's scale), else null
   const float *mu, *isig;  // feature standardisation
 };
 int launch_mlp_features_tc(cudaStream_t s, const FeatIn &fi, const __nv_bfloat16 *w1b, const float *params,

@@ -556,7 +556,7 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
     const float frc = c == 0 ? rr.fx : (c == 1 ? rr.fy : rr.fz);
     const float cfc = c == 0 ? cf.x : (c == 1 ? cf.y : cf.z);
     const float hc = (float)(c == 0 ? g.dx : (c == 1 ? g.dy : g.dz));
-    f[29] = rec_armf(dc, frc, cfc, hc) * fi.inv_r;
+    f[29] = rec_armf(dc, frc, cfc, hc) * (fi.pradfp ? (float)(1. / fi.pradfp[p]) : fi.inv_r);
     f[30] = (float)F0 * (float)fi.dt;
     f[31] = s.w[3 * c + 1];
     const float *mu = fi.mu + FEAT_PER_COMP * c, *is = fi.isig + FEAT_PER_COMP * c;

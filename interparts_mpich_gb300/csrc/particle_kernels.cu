@@ -140,26 +140,29 @@ __global__ void __launch_bounds__(256) k_sphere_int(Geo g, PartGeo pg, PartBuffe
   // is computed by one thread and read from shared memory: FP64 issues at a
   // small fraction of the FP32 rate, and every thread repeating it cost more
   // than the line sums themselves.
-  __shared__ double s_radin2, s_cx, s_cy, s_cz;
+  __shared__ double s_radin2, s_cx, s_cy, s_cz, s_rad, s_rthr;
   __shared__ float s_thr[7];
   __shared__ int s_box[6];  // ilow, ni, jlow, nj, klow, nk
   if (threadIdx.x == 0) {
-    const double radin = pg.radius - 2. * g.dx;
+    const double rad = p_rad(pg, p), rth = p_rthr(pg, p);  // the particle's own when polydisperse
+    const double radin = rad - 2. * g.dx;
     const double radin2 = radin * radin;
     s_radin2 = radin2;
+    s_rad = rad;
+    s_rthr = rth;
     // sqrt(d2) >= radius  <=>  d2 >= rthr (rthr: smallest double whose
     // correctly rounded square root is >= radius)
     s_thr[0] = (float)(radin2 * (1. - 1e-5));
     s_thr[1] = (float)(radin2 * (1. + 1e-5));
-    s_thr[2] = (float)(pg.rthr * (1. - 1e-5));
-    s_thr[3] = (float)(pg.rthr * (1. + 1e-5));
+    s_thr[2] = (float)(rth * (1. - 1e-5));
+    s_thr[3] = (float)(rth * (1. + 1e-5));
     s_thr[4] = (float)radin2;
-    s_thr[5] = (float)pg.rthr;
-    s_thr[6] = (float)pg.radius;
+    s_thr[5] = (float)rth;
+    s_thr[6] = (float)rad;
   }
   __syncthreads();
-  const double radius = pg.radius, dx = g.dx, dy = g.dy, dz = g.dz;
-  const double radin2 = s_radin2, rthr = pg.rthr;
+  const double radius = s_rad, dx = g.dx, dy = g.dy, dz = g.dz;
+  const double radin2 = s_radin2, rthr = s_rthr;
   const float radin2_lo = s_thr[0], radin2_hi = s_thr[1], rthr_lo = s_thr[2], rthr_hi = s_thr[3];
   const float radin2f = s_thr[4], rthrf = s_thr[5], radiusf = s_thr[6];
   __shared__ double sxm[AX], sxp[AX], srx[AX], sym[AX], syp[AX], sry[AX], szm[AX], szp[AX], srz[AX];
@@ -454,7 +457,7 @@ template void launch_sphere_integrals<float>(cudaStream_t, const Geo &, const Pa
 // ---------------------------------------------------------------------------
 // the scalar normal lubrication force f1 of lubrication (collisions.f90:222-438)
 __device__ double d_lub_f1(const PartGeo &pg, double pu, double pv, double pw, int idq, double nx, double ny,
-                           double nz, double eps, double u_nb, double v_nb, double w_nb) {
+                           double nz, double eps, double u_nb, double v_nb, double w_nb, double coeff_f) {
   const double u1a = pu * nx + pv * ny + pw * nz;
   const double u1b = u_nb * nx + v_nb * ny + w_nb * nz;
   double f1;
@@ -463,7 +466,7 @@ __device__ double d_lub_f1(const PartGeo &pg, double pu, double pv, double pw, i
     if (eps < 0.001) a11 = pg.a11_sat_pw;
     else a11 = -(1. / eps) + 1. / 5. * log(eps) + 1. / 21. * eps * log(eps) - .9713;
     f1 = (a11 * u1a);
-    f1 = pg.coeff_f * (f1 - (pg.a11_ini_pw * u1a));
+    f1 = coeff_f * (f1 - (pg.a11_ini_pw * u1a));
   } else {
     double a11a, a11b;
     if (eps < 0.001) { a11a = pg.a11a_sat_pp; a11b = pg.a11b_sat_pp; }
@@ -473,17 +476,36 @@ __device__ double d_lub_f1(const PartGeo &pg, double pu, double pv, double pw, i
       a11b = -a11 + .350;
     }
     f1 = (a11a * u1a + a11b * u1b);
-    f1 = pg.coeff_f * (f1 - (pg.a11a_ini_pp * u1a + pg.a11b_ini_pp * u1b));
+    f1 = coeff_f * (f1 - (pg.a11a_ini_pp * u1a + pg.a11b_ini_pp * u1b));
   }
   return f1;
 }
 __device__ void d_lubrication(const PartGeo &pg, double pu, double pv, double pw, int idq, double nx, double ny,
-                              double nz, double eps, double u_nb, double v_nb, double w_nb, double &cfx, double &cfy,
-                              double &cfz) {
-  const double f1 = d_lub_f1(pg, pu, pv, pw, idq, nx, ny, nz, eps, u_nb, v_nb, w_nb);
+                              double nz, double eps, double u_nb, double v_nb, double w_nb, double coeff_f,
+                              double &cfx, double &cfy, double &cfz) {
+  const double f1 = d_lub_f1(pg, pu, pv, pw, idq, nx, ny, nz, eps, u_nb, v_nb, w_nb, coeff_f);
   cfx = cfx + f1 * nx;
   cfy = cfy + f1 * ny;
   cfz = cfz + f1 * nz;
+}
+
+// Polydisperse pair constants (init.f90:137-241 with the pair's effective
+// mass ratiorho vp vq / (vp + vq), or ratiorho vp for a wall, and the
+// lubrication prefactor 6 pi nu Re of the equivalent radius Re), as the
+// oracle's pair_consts forms them
+struct PairC {
+  double kn, kt, etan, etat, muc, coeff_f;
+};
+__device__ PairC pair_consts(const PartGeo &pg, double vp, double vq, double re) {
+  const double me = vq > 0. ? pg.ratiorho * vp * vq / (vp + vq) : pg.ratiorho * vp, mt = 2. / 7. * me;
+  PairC k;
+  k.kn = pg.pc_an * me / pg.pc_b;
+  k.kt = pg.pc_at * mt / pg.pc_b;
+  k.etan = pg.pc_en * me / pg.pc_ndt;
+  k.etat = pg.pc_et * mt / pg.pc_ndt;
+  k.muc = 0.;
+  k.coeff_f = 6. * IBM_PI * pg.visc * re;
+  return k;
 }
 
 struct PState {  // the particle's own state held in registers by the collision thread
@@ -494,20 +516,27 @@ __device__ void d_collisions(const PartGeo &pg, PartBuffers &b, int p, PState &S
                              double deltax, double deltay, double deltaz, double u_nb, double v_nb, double w_nb,
                              double omx_nb, double omy_nb, double omz_nb, double dtsub, double rkab) {
   const int np = pg.np, nq = pg.nq;
-  const double radius = pg.radius;
+  const double radius = p_rad(pg, p);
+  // polydisperse: the partner's radius in its own rotation term (a wall: 0)
+  const double rq = pg.poly ? (idq <= np ? pg.prad[idq - 1] : 0.) : radius;
   const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
   double deltan, kn, etan, kt, etat, muc;
-  if (idq <= np) {
+  if (pg.poly) {
+    const bool wall = idq > np;
+    const PairC k = pair_consts(pg, pg.pvol[p], wall ? 0. : pg.pvol[idq - 1], radius);
+    deltan = (wall ? radius : radius + rq) - dist;
+    kn = k.kn; kt = k.kt; etan = k.etan; etat = k.etat; muc = k.muc;
+  } else if (idq <= np) {
     deltan = 2 * radius - dist; kn = pg.kn_ss; kt = pg.kt_ss; etan = pg.etan_ss; etat = pg.etat_ss; muc = pg.muc_ss;
   } else {
     deltan = radius - dist; kn = pg.kn_sw; kt = pg.kt_sw; etan = pg.etan_sw; etat = pg.etat_sw; muc = pg.muc_sw;
   }
   const double dun = (S.u + (S.omy * radius * nz) - (S.omz * radius * ny)) -
-                     (u_nb + (omy_nb * radius * (-nz)) - (omz_nb * radius * (-ny)));
+                     (u_nb + (omy_nb * rq * (-nz)) - (omz_nb * rq * (-ny)));
   const double dvn = (S.v - (S.omx * radius * nz) + (S.omz * radius * nx)) -
-                     (v_nb - (omx_nb * radius * (-nz)) + (omz_nb * radius * (-nx)));
+                     (v_nb - (omx_nb * rq * (-nz)) + (omz_nb * rq * (-nx)));
   const double dwn = (S.w + (S.omx * radius * ny) - (S.omy * radius * nx)) -
-                     (w_nb + (omx_nb * radius * (-ny)) - (omy_nb * radius * (-nx)));
+                     (w_nb + (omx_nb * rq * (-ny)) - (omy_nb * rq * (-nx)));
   const double vabs = dun * nx + dvn * ny + dwn * nz;
   const double fxn = -(kn * (deltan * nx)) - etan * (vabs * nx);
   const double fyn = -(kn * (deltan * ny)) - etan * (vabs * ny);
@@ -707,12 +736,14 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   const int p = blockIdx.x * COLL_WARPS + wid;
   if (p >= np) return;
   if (lane == 0) ncand[wid] = 0;
-  const double radius = pg.radius;
+  const double radius = p_rad(pg, p);
   const int qmax0 = b.qmax[p];
   const int *fc = b.firstc + (long)p * nq;
   if (lane < qmax0 && lane < 16) fcs[wid][lane] = fc[lane];
   __syncwarp();
-  const float thr = 2.1f * (float)radius;
+  // FP32 filter distance: 2.1 R (polydisperse: 1.05 (R + Rmax), a superset
+  // of every pair's 1.05 (Rp + Rq))
+  const float thr = pg.poly ? 1.05f * (float)(radius + pg.rmax) : 2.1f * (float)radius;
   const float thr2 = thr * thr;
   const float lxf = (float)pg.lx, lyf = (float)pg.ly;
   const float4 pp = b.pos4[p];
@@ -831,11 +862,17 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
         deltay = minimg(qy - py, qy - pg.ly - py, qy + pg.ly - py);
         dist = sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
         nx = deltax / dist; ny = deltay / dist; nz = deltaz / dist;
-        const double eps = (dist - 2. * radius) / radius;
+        // polydisperse: contact at the sum of the radii, eps and the
+        // lubrication prefactor with the equivalent radius (pair_consts)
+        const double rqq = p_rad(pg, q);
+        const double rsum = pg.poly ? radius + rqq : 2. * radius;
+        const double re = pg.poly ? 2. * radius * rqq / (radius + rqq) : radius;
+        const double eps = (dist - rsum) / re;
         qu = b.pf[(long)PF_SU * np + q]; qv = b.pf[(long)PF_SV * np + q]; qw = b.pf[(long)PF_SW * np + q];
         if ((eps < 0.025) && (eps > 0.)) {
           lub = 1;
-          f1 = d_lub_f1(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, qu, qv, qw);
+          f1 = d_lub_f1(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, qu, qv, qw,
+                        pg.poly ? 6. * IBM_PI * pg.visc * re : pg.coeff_f);
         }
       }
     }
@@ -861,9 +898,10 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
       }
       int qq = 0;
       const int qm = b.qmax[p];
+      const double jrsum = pg.poly ? radius + pg.prad[jq] : 2. * radius;
       for (int i = 1; i <= qm; ++i) {
         if (jidq == fcw[i - 1]) {
-          if (jdist < (2. * radius)) {
+          if (jdist < jrsum) {
             qq = i;
             d_collisions(pg, b, p, S, qq, jidq, jdist, jdx, jdy, jdz, jqu, jqv, jqw,
                          b.pf[(long)PF_SOMX * np + jq], b.pf[(long)PF_SOMY * np + jq], b.pf[(long)PF_SOMZ * np + jq],
@@ -873,7 +911,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
           }
         }
       }
-      if (qq == 0 && jdist < (2. * radius)) {
+      if (qq == 0 && jdist < jrsum) {
         qlast = qlast + 1;
         if (qlast > nq) {  // overflow: flagged, the pair's update skipped
           atomicExch(&b.err[1], 1);
@@ -905,7 +943,8 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
     int qq = 0;
     const double eps = -deltan / radius;
     if ((eps < 0.075) && (eps > 0.))
-      d_lubrication(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, 0., 0., 0., S.colfx, S.colfy, S.colfz);
+      d_lubrication(pg, S.u, S.v, S.w, idq, nx, ny, nz, eps, 0., 0., 0.,
+                    pg.poly ? 6. * IBM_PI * pg.visc * radius : pg.coeff_f, S.colfx, S.colfy, S.colfz);
     for (int i = 1; i <= qm_w; ++i) {
       if (idq == fcw[i - 1]) {
         qq = i;
@@ -929,7 +968,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   b.qmax[p] = qlast;
   // Newton-Euler (intgr_nwtn_eulr.f90:611-667); colflg is reset to 0 first
   const double colflgx = 0., colflgy = 0., colflgz = 0.;
-  const double vol = pg.volp, rr = pg.ratiorho;  // ap%vol, ap%ratiorho (coordsfp.f90:96-102)
+  const double vol = p_vol(pg, p), rr = pg.ratiorho;  // ap%vol, ap%ratiorho (coordsfp.f90:96-102)
   const double vr = vol * rr;
   const double ou = PF(PF_OU), ov = PF(PF_OV), ow = PF(PF_OW);
   double nu = ou + (1 - colflgx) * ((-1.) * dt * (PF(PF_FXLTOT)) / vr + (PF(PF_INTU) - PF(PF_OINTU)) / vr) +
@@ -946,7 +985,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   PF(PF_COLTX) = 0.; PF(PF_COLTY) = 0.; PF(PF_COLTZ) = 0.;
   double omx, omy, omz;
   if (pg.rotation) {
-    const double mr = pg.mominert * rr;
+    const double mr = p_mi(pg, p) * rr;
     omx = PF(PF_OOMX) + (-1.) * dt * PF(PF_TQX) / mr + (PF(PF_INTOMX) - PF(PF_OINTOMX)) / mr +
           rkab * 0.5 * dt * (PF(PF_COLTX) + PF(PF_OCOLTX)) / mr;
     omy = PF(PF_OOMY) + (-1.) * dt * PF(PF_TQY) / mr + (PF(PF_INTOMY) - PF(PF_OINTOMY)) / mr +
@@ -973,7 +1012,7 @@ __global__ void __launch_bounds__(32 * COLL_WARPS) k_collide_update(PartGeo pg, 
   r[RK_TX] = r[RK_TX] + (-1.) * PF(PF_TQX) + (PF(PF_INTOMX) - PF(PF_OINTOMX)) / dt;
   r[RK_TY] = r[RK_TY] + (-1.) * PF(PF_TQY) + (PF(PF_INTOMY) - PF(PF_OINTOMY)) / dt;
   r[RK_TZ] = r[RK_TZ] + (-1.) * PF(PF_TQZ) + (PF(PF_INTOMZ) - PF(PF_OINTOMZ)) / dt;
-  r[RK_TT] = r[RK_TT] + (-1.) * (-dpdy_new * pg.dVlagr);
+  r[RK_TT] = r[RK_TT] + (-1.) * (-dpdy_new * p_dvl(pg, p));
   r[RK_CFX] = r[RK_CFX] + 0.5 * rkab * (S.colfx + PF(PF_OCOLFX));
   r[RK_CFY] = r[RK_CFY] + 0.5 * rkab * (S.colfy + PF(PF_OCOLFY));
   r[RK_CFZ] = r[RK_CFZ] + 0.5 * rkab * (S.colfz + PF(PF_OCOLFZ));
@@ -1025,7 +1064,7 @@ __global__ void __launch_bounds__(256) k_ne_finalize(PartGeo pg, PartBuffers b, 
         PF(PF_Z) = z;
       }
     }
-    const double ro = pg.radius + pg.offset;
+    const double ro = p_rad(pg, p) + pg.offset;
     const double leftb = 0., rightb = pg.lx, frontb = 0., backb = pg.ly;
     int *nbf = b.nb + (long)p * 9;
     if (init != 2) {
@@ -1053,21 +1092,25 @@ __global__ void __launch_bounds__(256) k_ne_finalize(PartGeo pg, PartBuffers b, 
     base = 0;
   }
   __syncthreads();
-  const int nl = pg.nl;
+  // nl: the per-particle capacity of the Lagrangian arrays; the sphere's
+  // own point count, table offset and shell radius when polydisperse
+  const int nl = pg.nl, nlp = p_nl(pg, p), nt = pg.ntab;
+  const double radfp = p_radfp(pg, p);
+  const double *sct = b.sincos + p_toff(pg, p);
   const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
   const float lxf = (float)pg.lx, lyf = (float)pg.ly;
-  for (int l0 = 0; l0 < nl; l0 += blockDim.x) {
+  for (int l0 = 0; l0 < nlp; l0 += blockDim.x) {
     const int l = l0 + threadIdx.x;
     bool keep = false;
     double xfploc = 0, yfploc = 0, zfploc = 0, rx = 0, ry = 0, rz = 0;
-    if (l < nl && b.mslv[p] != 0) {
-      const double st = b.sincos[l], ct = b.sincos[nl + l], sp = b.sincos[2 * nl + l], cp = b.sincos[3 * nl + l];
+    if (l < nlp && b.mslv[p] != 0) {
+      const double st = sct[l], ct = sct[nt + l], sp = sct[2 * nt + l], cp = sct[3 * nt + l];
       // offsets from the centre, radfp*st*cp etc. with the reference's
       // rounding; they also serve as (xfp - xc) in the point velocities
-      const double rst = pg.radfp * st;
+      const double rst = radfp * st;
       rx = rst * cp;
       ry = rst * sp;
-      rz = pg.radfp * ct;
+      rz = radfp * ct;
       xfploc = sx + rx;
       yfploc = sy + ry;
       zfploc = sz + rz;

@@ -173,6 +173,14 @@ struct orc_ctx {
   // reference cannot express (its z boundaries are always walls, bound.f90:
   // 17-65, initsolver.f90:26-30); see the functions marked "periodic z"
   bool zper = false;
+  // polydisperse (ibm_params.radii set): per-particle radius, force-point
+  // shell radius, point count, offset into the concatenated point table and
+  // Lagrangian volume; another variant the reference cannot express (one
+  // radius and one nl, param.f90:48, init.f90:129).  Pair constants: see
+  // pair_consts.
+  bool poly = false;
+  std::vector<double> prad, pradfp, pdvl;
+  std::vector<int> pnl, ptoff;
   // derived (init.f90:74-243)
   double dxi, dyi, dzi, dx, dy, dz, offset, volp, mominert, retrac;
   double rkcoeffab[3];
@@ -214,6 +222,17 @@ int fail(orc_ctx *c, int code, const char *msg) {
   c->err = msg;
   return code;
 }
+
+// Polydisperse pair constants: the contact spring/dashpot of init.f90:137-
+// 241 with the effective mass ratiorho vp vq / (vp + vq) of the pair (vq = 0:
+// a wall, ratiorho vp), and the lubrication prefactor 6 pi nu Re with the
+// equivalent radius Re = 2 Rp Rq / (Rp + Rq) (Rp for a wall), so that the
+// leading squeeze term 6 pi nu Re^2 / (4 gap) is the unequal-sphere one;
+// both reduce to the equal-sphere constants.
+struct PairC {
+  double kn, kt, etan, etat, muc, coeff_f;
+};
+PairC pair_consts(const orc_ctx *c, double vp, double vq, double re);
 
 // derived_parameters (init.f90:74-243), single rank
 void derived_parameters(orc_ctx *c) {
@@ -263,6 +282,21 @@ void derived_parameters(orc_ctx *c) {
   c->a11_ini_pw = -(1. / eps_ini_pw) + 1. / 5. * std::log(eps_ini_pw) + 1. / 21. * eps_ini_pw * std::log(eps_ini_pw) - .9713;
   c->a11_sat_pw = -(1. / eps_sat_pw) + 1. / 5. * std::log(eps_sat_pw) + 1. / 21. * eps_sat_pw * std::log(eps_sat_pw) - .9713;
 }
+
+PairC pair_consts(const orc_ctx *c, double vp, double vq, double re) {
+  const double Nstretch = 8, dt_estim = 0.05, en = 0.97, et = 0.10;
+  const double me = vq > 0. ? c->ratiorho * vp * vq / (vp + vq) : c->ratiorho * vp, mt = 2. / 7. * me;
+  PairC k;
+  k.kn = (PI * PI + std::pow(std::fabs(std::log(en)), 2.)) * me / std::pow(Nstretch * dt_estim, 2.);
+  k.kt = (PI * PI + std::pow(std::fabs(std::log(et)), 2.)) * mt / std::pow(Nstretch * dt_estim, 2.);
+  k.etan = -2. * (std::log(en)) * me / (Nstretch * dt_estim);
+  k.etat = -2. * (std::log(et)) * mt / (Nstretch * dt_estim);
+  k.muc = 0.;
+  k.coeff_f = 6. * PI * c->visc * re;
+  return k;
+}
+double prad(const orc_ctx *c, int p) { return c->poly ? c->prad[p] : c->radius; }
+double pdvl(const orc_ctx *c, int p) { return c->poly ? c->pdvl[p] : c->dVlagr; }
 
 // ---- boundary conditions (bound.f90) ---------------------------------------
 // updthalos (bound.f90:173-221) on one rank: periodic copy of one plane.
@@ -712,12 +746,13 @@ void lagrforces(orc_ctx *c, double dt, bool first) {
       P.torqyltot = P.torqyltot + (P.zfp[l] - P.z) * P.fxl[l] - (P.xfp[l] - P.x) * P.fzl[l];
       P.torqzltot = P.torqzltot + (P.xfp[l] - P.x) * P.fyl[l] - (P.yfp[l] - P.y) * P.fxl[l];
     }
-    P.fxltot = P.fxltot * c->dVlagr;
-    P.fyltot = P.fyltot * c->dVlagr;
-    P.fzltot = P.fzltot * c->dVlagr;
-    P.torqxltot = P.torqxltot * c->dVlagr;
-    P.torqyltot = P.torqyltot * c->dVlagr;
-    P.torqzltot = P.torqzltot * c->dVlagr;
+    const double dVl = pdvl(c, p);
+    P.fxltot = P.fxltot * dVl;
+    P.fyltot = P.fyltot * dVl;
+    P.fzltot = P.fzltot * dVl;
+    P.torqxltot = P.torqxltot * dVl;
+    P.torqyltot = P.torqyltot * dVl;
+    P.torqzltot = P.torqzltot * dVl;
     P.torqtheta = (P.torqyltot * std::cos(P.phi)) - (P.torqxltot * std::sin(P.phi));
   }
   // master/slave exchange: on one rank anb(1..8)=0 and the sum over nb=0..8
@@ -726,15 +761,19 @@ void lagrforces(orc_ctx *c, double dt, bool first) {
 
 // lagr2eulr (interp_spread.f90:230-474)
 void lagr2eulr(orc_ctx *c, double dt) {
-  const double dVlagrdVeuli = c->dVlagr / c->dVeul;
+  double dVlagrdVeuli = c->dVlagr / c->dVeul;
   std::fill(c->dudtf.d.begin(), c->dudtf.d.end(), 0.);
   std::fill(c->dvdtf.d.begin(), c->dvdtf.d.end(), 0.);
   std::fill(c->dwdtf.d.begin(), c->dwdtf.d.end(), 0.);
-  const double coeffx0 = dVlagrdVeuli * dt, coeffy0 = dVlagrdVeuli * dt, coeffz0 = dVlagrdVeuli * dt;
+  double coeffx0 = dVlagrdVeuli * dt, coeffy0 = dVlagrdVeuli * dt, coeffz0 = dVlagrdVeuli * dt;
   c->forceytot = 0.;
   for (int p = 0; p < c->pmax; ++p) {  // serial: the atomic-add order of the reference loop
     Part &P = c->ap[p];
     if (P.mslv == 0) continue;
+    if (c->poly) {  // the particle's own Lagrangian volume
+      dVlagrdVeuli = c->pdvl[p] / c->dVeul;
+      coeffx0 = coeffy0 = coeffz0 = dVlagrdVeuli * dt;
+    }
     for (int l = 0; l < c->nla[p]; ++l) {
       Stencil s;
       stencil(c, P.xfp[l], P.yfp[l], P.zfp[l], s);
@@ -955,10 +994,13 @@ void lagrangian_points(orc_ctx *c) {
     c->nla[p] = 0;
     if (P.mslv == 0) continue;
     int ll = 0;
-    for (int l = 0; l < c->nl; ++l) {
-      double xfploc = P.x + c->radfp * std::sin(P.theta * 0. + c->thetarc[l]) * std::cos(P.phi * 0. + c->phirc[l]);
-      double yfploc = P.y + c->radfp * std::sin(P.theta * 0. + c->thetarc[l]) * std::sin(P.phi * 0. + c->phirc[l]);
-      double zfploc = P.z + c->radfp * std::cos(P.theta * 0. + c->thetarc[l]);
+    const int nlp = c->poly ? c->pnl[p] : c->nl, to = c->poly ? c->ptoff[p] : 0;
+    const double radfp = c->poly ? c->pradfp[p] : c->radfp;
+    for (int l = 0; l < nlp; ++l) {
+      const double th = c->thetarc[to + l], ph = c->phirc[to + l];
+      double xfploc = P.x + radfp * std::sin(P.theta * 0. + th) * std::cos(P.phi * 0. + ph);
+      double yfploc = P.y + radfp * std::sin(P.theta * 0. + th) * std::sin(P.phi * 0. + ph);
+      double zfploc = P.z + radfp * std::cos(P.theta * 0. + th);
       double isperiodx = 0., isperiody = 0.;
       if (xfploc < 0. + 0.5 * c->dx) isperiodx = 1.;
       if (xfploc >= c->lx + 0.5 * c->dx) isperiodx = -1.;
@@ -983,7 +1025,7 @@ void lagrangian_points(orc_ctx *c) {
 
 // nb flags of a master on one rank (intgr_nwtn_eulr.f90:1051-1090, bounds 0..lx, 0..ly)
 void nb_flags(const orc_ctx *c, Part &P) {
-  const double ro = c->radius + c->offset;
+  const double ro = (c->poly ? c->prad[&P - c->ap.data()] : c->radius) + c->offset;
   const double leftb = 0. * c->lx / 1., rightb = 1. * c->lx / 1., frontb = 0. * c->ly / 1., backb = 1. * c->ly / 1.;
   for (int n = 0; n < 9; ++n) P.nb[n] = 0;
   double dist;
@@ -1021,11 +1063,12 @@ inline void copy_shift_sphere(const orc_ctx *c, int nbrecv, double &x, double &y
 // 3 read the current (unew,vnew,wnew).
 void intgr_over_sphere(orc_ctx *c, int type) {
   const double dx = 1. / c->dxi, dy = 1. / c->dyi, dz = 1. / c->dzi;
-  const double radin = c->radius - 2. * dx;
-  const double radin2 = radin * radin;
-  const double radius = c->radius, dVeul = c->dVeul;
+  const double dVeul = c->dVeul;
 #pragma omp parallel for schedule(dynamic)
   for (int p = 0; p < c->pmax; ++p) {
+    const double radius = prad(c, p);  // polydisperse: the particle's own
+    const double radin = radius - 2. * dx;
+    const double radin2 = radin * radin;
     Part &P = c->ap[p];
     double ax[9], ay[9], az[9], iu[9], iv[9], iw[9];
     for (int n = 0; n < 9; ++n) { ax[n] = 0; ay[n] = 0; az[n] = 0; iu[n] = 0; iv[n] = 0; iw[n] = 0; }
@@ -1138,7 +1181,7 @@ void intgr_over_sphere(orc_ctx *c, int type) {
 // lubrication (collisions.f90:222-438): only the normal (squeeze) force is
 // applied (collisions.f90:430-432), so only f1 is evaluated.
 void lubrication(orc_ctx *c, Part &P, int idq, double nx, double ny, double nz, double eps,
-                 double u_nb, double v_nb, double w_nb) {
+                 double u_nb, double v_nb, double w_nb, double coeff_f) {
   const double u1a = P.u * nx + P.v * ny + P.w * nz;
   const double u1b = u_nb * nx + v_nb * ny + w_nb * nz;
   double f1;
@@ -1147,7 +1190,7 @@ void lubrication(orc_ctx *c, Part &P, int idq, double nx, double ny, double nz, 
     if (eps < 0.001) a11 = c->a11_sat_pw;
     else a11 = -(1. / eps) + 1. / 5. * std::log(eps) + 1. / 21. * eps * std::log(eps) - .9713;
     f1 = (a11 * u1a);
-    f1 = c->coeff_f * (f1 - (c->a11_ini_pw * u1a));
+    f1 = coeff_f * (f1 - (c->a11_ini_pw * u1a));
   } else {
     double a11a, a11b;
     if (eps < 0.001) { a11a = c->a11a_sat_pp; a11b = c->a11b_sat_pp; }
@@ -1157,7 +1200,7 @@ void lubrication(orc_ctx *c, Part &P, int idq, double nx, double ny, double nz, 
       a11b = -a11 + .350;
     }
     f1 = (a11a * u1a + a11b * u1b);
-    f1 = c->coeff_f * (f1 - (c->a11a_ini_pp * u1a + c->a11b_ini_pp * u1b));
+    f1 = coeff_f * (f1 - (c->a11a_ini_pp * u1a + c->a11b_ini_pp * u1b));
   }
   P.colfx = P.colfx + f1 * nx;
   P.colfy = P.colfy + f1 * ny;
@@ -1170,20 +1213,27 @@ void collisions(orc_ctx *c, int p, int qq, int idq, double dist, double deltax, 
                 double omz_nb, double dtsub, int rkiter) {
   Part &P = c->ap[p];
   OldPart &O = c->op[p];
-  const double radius = c->radius;
+  const double radius = prad(c, p);
+  // polydisperse: the partner's radius in its own rotation term (a wall: 0)
+  const double rq = c->poly ? (idq <= c->np ? c->prad[idq - 1] : 0.) : radius;
   const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
   double deltan, kn, etan, kt, etat, muc;
-  if (idq <= c->np) {
+  if (c->poly) {
+    const bool wall = idq > c->np;
+    const PairC k = pair_consts(c, P.vol, wall ? 0. : c->ap[idq - 1].vol, radius);
+    deltan = (wall ? radius : radius + rq) - dist;
+    kn = k.kn; kt = k.kt; etan = k.etan; etat = k.etat; muc = k.muc;
+  } else if (idq <= c->np) {
     deltan = 2 * radius - dist; kn = c->kn_ss; kt = c->kt_ss; etan = c->etan_ss; etat = c->etat_ss; muc = c->muc_ss;
   } else {
     deltan = radius - dist; kn = c->kn_sw; kt = c->kt_sw; etan = c->etan_sw; etat = c->etat_sw; muc = c->muc_sw;
   }
   const double dun = (P.u + (P.omy * radius * nz) - (P.omz * radius * ny)) -
-                     (u_nb + (omy_nb * radius * (-nz)) - (omz_nb * radius * (-ny)));
+                     (u_nb + (omy_nb * rq * (-nz)) - (omz_nb * rq * (-ny)));
   const double dvn = (P.v - (P.omx * radius * nz) + (P.omz * radius * nx)) -
-                     (v_nb - (omx_nb * radius * (-nz)) + (omz_nb * radius * (-nx)));
+                     (v_nb - (omx_nb * rq * (-nz)) + (omz_nb * rq * (-nx)));
   const double dwn = (P.w + (P.omx * radius * ny) - (P.omy * radius * nx)) -
-                     (w_nb + (omx_nb * radius * (-ny)) - (omy_nb * radius * (-nx)));
+                     (w_nb + (omx_nb * rq * (-ny)) - (omy_nb * rq * (-nx)));
   const double vabs = dun * nx + dvn * ny + dwn * nz;
   const double fxn = -(kn * (deltan * nx)) - etan * (vabs * nx);
   const double fyn = -(kn * (deltan * ny)) - etan * (vabs * ny);
@@ -1388,12 +1438,18 @@ int intgr_nwtn_eulr(orc_ctx *c, int rkiter, double dt) {
           const double deltay = ady[minloc_abs3(ady)];
           const double dist = std::sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
           const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
-          const double eps = (dist - 2. * radius) / radius;
-          if ((eps < 0.025) && (eps > 0.)) lubrication(c, P, idq, nx, ny, nz, eps, su[q], sv[q], sw[q]);
+          // polydisperse: contact at the sum of the radii, eps and the
+          // lubrication prefactor with the equivalent radius (pair_consts)
+          const double rp = prad(c, p), rqq = prad(c, q);
+          const double rsum = c->poly ? rp + rqq : 2. * radius;
+          const double re = c->poly ? 2. * rp * rqq / (rp + rqq) : radius;
+          const double cfl = c->poly ? 6. * PI * c->visc * re : c->coeff_f;
+          const double eps = (dist - rsum) / re;
+          if ((eps < 0.025) && (eps > 0.)) lubrication(c, P, idq, nx, ny, nz, eps, su[q], sv[q], sw[q], cfl);
           int qq = 0;
           for (int i = 1; i <= P.qmax; ++i) {
             if (idq == P.firstc[i - 1]) {
-              if (dist < (2. * radius)) {
+              if (dist < rsum) {
                 qq = i;
                 collisions(c, p, qq, idq, dist, deltax, deltay, deltaz, su[q], sv[q], sw[q], sox[q], soy[q], soz[q], dt, rkiter);
               } else if (iter == itermax) {
@@ -1401,7 +1457,7 @@ int intgr_nwtn_eulr(orc_ctx *c, int rkiter, double dt) {
               }
             }
           }
-          if (qq == 0 && dist < (2. * radius)) {
+          if (qq == 0 && dist < rsum) {
             qlast = qlast + 1;
             if (qlast > c->nqmax) { status = IBM_E_CONTACT_OVERFLOW; qlast = c->nqmax; continue; }
             qq = qlast;
@@ -1416,24 +1472,26 @@ int intgr_nwtn_eulr(orc_ctx *c, int rkiter, double dt) {
       // walls (:503-603); none with periodic z
       for (int q = botw; q <= (c->zper ? botw - 1 : topw); ++q) {
         const int idq = q;
+        const double rp = prad(c, p);
         const double deltax = 0., deltay = 0., deltaz = (q - botw) * c->lz - P.z;
         const double dist = std::sqrt(deltax * deltax + deltay * deltay + deltaz * deltaz);
-        const double deltan = radius - dist;
+        const double deltan = rp - dist;
         const double nx = deltax / dist, ny = deltay / dist, nz = deltaz / dist;
         int qq = 0;
-        const double eps = -deltan / radius;
-        if ((eps < 0.075) && (eps > 0.)) lubrication(c, P, idq, nx, ny, nz, eps, 0., 0., 0.);
+        const double eps = -deltan / rp;
+        const double cfl = c->poly ? 6. * PI * c->visc * rp : c->coeff_f;
+        if ((eps < 0.075) && (eps > 0.)) lubrication(c, P, idq, nx, ny, nz, eps, 0., 0., 0., cfl);
         for (int i = 1; i <= P.qmax; ++i) {
           if (idq == P.firstc[i - 1]) {
             qq = i;
-            if (dist < radius) {
+            if (dist < rp) {
               collisions(c, p, qq, idq, dist, deltax, deltay, deltaz, 0., 0., 0., 0., 0., 0., dt, rkiter);
             } else if (iter == itermax) {
               remove_contact(P, O, i, qlast);
             }
           }
         }
-        if ((qq == 0) && (dist < radius)) {
+        if ((qq == 0) && (dist < rp)) {
           qlast = qlast + 1;
           if (qlast > c->nqmax) { status = IBM_E_CONTACT_OVERFLOW; qlast = c->nqmax; continue; }
           qq = qlast;
@@ -1533,6 +1591,22 @@ void alloc(orc_ctx *c) {
   }
   c->rkp.assign((size_t)c->npmax * RK_N, 0.);
   c->nla.assign(c->npmax, 0);
+}
+
+// per-particle volume and moment of inertia (coordsfp.f90:96-102), with the
+// particle's own radius when polydisperse
+void set_sizes(orc_ctx *c) {
+  for (size_t p = 0; p < c->ap.size(); ++p) {
+    Part &P = c->ap[p];
+    P.ratiorho = c->ratiorho;
+    if (c->poly) {
+      P.vol = (4. / 3.) * PI * std::pow(c->prad[p], 3.);
+      P.mominert = (2. / 5.) * P.vol * std::pow(c->prad[p], 2.);
+    } else {
+      P.vol = c->volp;
+      P.mominert = c->mominert;
+    }
+  }
 }
 
 // the IBM block of the driver (main.f90:286-338)
@@ -2010,7 +2084,31 @@ orc_ctx *orc_create(const ibm_params *prm) {
   c->nb_copies = prm->nb_copies == 1 ? 1 : 9;
   derived_parameters(c);
   c->radfp = prm->radfp;
-  if (c->np > 0 && c->nl > 0) {
+  if (prm->radii && c->np > 0) {
+    // polydisperse: per-sphere point counts (the nl formula of init.f90:
+    // 127-129 with the sphere's radius), shells and Lagrangian volumes
+    // (coordsfp.f90:84-90); tables concatenated in particle order
+    c->poly = true;
+    const double retrac = 0.3 / c->dxi;
+    int off = 0, nlmax = 0;
+    for (int p = 0; p < c->np; ++p) {
+      const double r = prm->radii[p];
+      const int nlp = (int)std::lround((PI / 3.) * (12. * std::pow((r - retrac) * c->dxi, 2) + 1.));
+      if (!(r > retrac) || nlp < 1) { delete c; return nullptr; }
+      const double rfp = r - retrac;
+      c->prad.push_back(r);
+      c->pradfp.push_back(rfp);
+      c->pnl.push_back(nlp);
+      c->ptoff.push_back(off);
+      c->pdvl.push_back(((4. / 3.) * PI * std::pow(rfp + 0.5 / c->dxi, 3.) -
+                         (4. / 3.) * PI * std::pow(rfp - 0.5 / c->dxi, 3.)) / (1. * nlp));
+      off += nlp;
+      nlmax = std::max(nlmax, nlp);
+    }
+    if (nlmax != c->nl) { delete c; return nullptr; }
+    c->thetarc.assign(prm->thetarc, prm->thetarc + off);
+    c->phirc.assign(prm->phirc, prm->phirc + off);
+  } else if (c->np > 0 && c->nl > 0) {
     c->thetarc.assign(prm->thetarc, prm->thetarc + c->nl);
     c->phirc.assign(prm->phirc, prm->phirc + c->nl);
   }
@@ -2087,7 +2185,7 @@ int orc_set_particles(orc_ctx *c, const ibm_particles *s) {
         P.ul[l] = s->ul[o]; P.vl[l] = s->vl[o]; P.wl[l] = s->wl[o];
         if (s->fxl) { P.fxl[l] = s->fxl[o]; P.fyl[l] = s->fyl[o]; P.fzl[l] = s->fzl[o]; }
       }
-      c->nla[p] = c->nl;
+      c->nla[p] = c->poly ? c->pnl[p] : c->nl;
     }
   } else {
     lagrangian_points(c);
@@ -2098,7 +2196,7 @@ int orc_set_particles(orc_ctx *c, const ibm_particles *s) {
   c->dVlagr = ((4. / 3.) * PI * std::pow(c->radfp + 0.5 / c->dxi, 3.) -
                (4. / 3.) * PI * std::pow(c->radfp - 0.5 / c->dxi, 3.)) / (1. * c->nl);
   c->dVeul = 1. / (c->dxi * c->dyi * c->dzi);
-  for (auto &P : c->ap) { P.vol = c->volp; P.ratiorho = c->ratiorho; P.mominert = c->mominert; }
+  set_sizes(c);
   c->have_particles = true;
   return IBM_OK;
 }
@@ -2156,7 +2254,7 @@ int orc_init_particles(orc_ctx *c, double *vol_calc) {
   c->dVlagr = ((4. / 3.) * PI * std::pow(c->radfp + 0.5 / c->dxi, 3.) -
                (4. / 3.) * PI * std::pow(c->radfp - 0.5 / c->dxi, 3.)) / (1. * c->nl);
   c->dVeul = 1. / (c->dxi * c->dyi * c->dzi);
-  for (auto &P : c->ap) { P.vol = c->volp; P.ratiorho = c->ratiorho; P.mominert = c->mominert; }
+  set_sizes(c);
   intgr_over_sphere(c, 1);
   if (vol_calc) *vol_calc = c->np > 0 ? c->ap[0].intu : 0.;
   intgr_over_sphere(c, 2);
@@ -2309,7 +2407,7 @@ int orc_get_scalar(orc_ctx *c, double *cf, double *dcrk) {
 int orc_phase_indicator(orc_ctx *c, int itype, double *gamu, double *gamv, double *gamw, double *gamp,
                         double *upart, double *vpart, double *wpart) {
   if (itype != 0 && itype != 1) return fail(c, IBM_E_INVALID, "itype must be 0 or 1");
-  if (c->zper) return fail(c, IBM_E_STATE, "no plane statistics with periodic z");
+  if (c->zper || c->poly) return fail(c, IBM_E_STATE, "no plane statistics with periodic z or polydisperse spheres");
   Arr3 a[7];
   for (auto &x : a) x.init(0, c->i1 + 1, c->j1 + 1, c->k1 + 1);
   phase_indicator(c, itype, a[0], a[1], a[2], a[3], a[4], a[5], a[6]);
@@ -2319,7 +2417,7 @@ int orc_phase_indicator(orc_ctx *c, int itype, double *gamu, double *gamv, doubl
 }
 int orc_post1d(orc_ctx *c, double *profiles, double *scalars) {
   if (!c->have_fields) return fail(c, IBM_E_STATE, "no fields set");
-  if (c->zper) return fail(c, IBM_E_STATE, "no plane statistics with periodic z");
+  if (c->zper || c->poly) return fail(c, IBM_E_STATE, "no plane statistics with periodic z or polydisperse spheres");
   post1d(c, profiles, scalars);
   return IBM_OK;
 }

@@ -17,7 +17,10 @@ values (the reference ships no golden outputs for this path):
   express): the projection leaves the field divergence-free, and the whole
   run is invariant under a shift by half the period in z (the sphere placed
   across the periodic boundary), which exercises the cyclic Poisson solve,
-  the wrapped IBM stencils and halos and the sphere integrals' z images.
+  the wrapped IBM stencils and halos and the sphere integrals' z images;
+* the polydisperse variant (another case the reference cannot express):
+  spheres given as a radius array that are all equal reproduce the
+  monodisperse run.
 """
 import ctypes as C
 import math
@@ -149,3 +152,23 @@ def test_periodic_z_shift_invariance():
         assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a), n
     assert pa.w[0] < 0 and abs(pa.w[0] - pb.w[0]) <= 1e-12 * abs(pa.w[0])
     assert abs((pa.z[0] - pb.z[0]) % 1.0 - 0.5) < 1e-12
+
+
+def test_polydisperse_equal_radii_reproduce_monodisperse():
+    r = 5.0 / 48
+    runs = []
+    for radii in (None, np.full(6, r)):
+        c = Case(name="pp", itot=48, jtot=48, ktot=48, radius=r, np=6, visc=1.0 / 800.0, seed=7, gap=0.02,
+                 radii=radii, ratiorho=1.5, flow="poi", perturb=0.05)
+        o = OracleSolver(c)
+        o.setup()
+        dt = 0.5 * o.chkdt() if not runs else runs[0][2]
+        o.run(dt, 5)
+        runs.append((o.get_fields(), o.get_particles(lagrangian=False), dt))
+        o.close()
+    (fa, pa, _), (fb, pb, _) = runs
+    for n in "uvwp":
+        a, b = fa[n][1:-1, 1:-1, 1:-1], fb[n][1:-1, 1:-1, 1:-1]
+        assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a), n
+    assert np.max(np.abs(pa.z - pb.z)) <= 1e-14
+    assert pa.contact_lists() == pb.contact_lists()
