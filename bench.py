@@ -142,14 +142,25 @@ def fp64_peak() -> float | None:
     return t.value if fn["fp64_peak"](C.byref(t)) == 0 else None
 
 
-def sphere_box(case) -> int:
-    return int(round(2 * case.radius * case.dxi + 5)) ** 3
+def _radii(case):
+    import numpy as np
+    return np.asarray(case.radii, np.float64) if case.radii is not None else np.array([case.radius])
+
+
+def sphere_box(case) -> float:
+    """Cells of the sphere-integral box (2R/dx + 5)^3, the mean over the
+    spheres when they differ."""
+    import numpy as np
+    return float(np.mean(np.round(2 * _radii(case) * case.dxi + 5) ** 3))
 
 
 def s_fp(case) -> float:
+    """Footprint cells of a sphere's force-point shell, the mean over the
+    spheres when they differ."""
     import math
-    r = (case.radius - 0.3 / case.dxi) * case.dxi
-    return 4.0 / 3.0 * math.pi * ((r + 1.5) ** 3 - (r - 1.5) ** 3)
+    import numpy as np
+    r = (_radii(case) - 0.3 / case.dxi) * case.dxi
+    return float(np.mean(4.0 / 3.0 * math.pi * ((r + 1.5) ** 3 - (r - 1.5) ** 3)))
 
 
 def algorithmic_bytes(case, w: int = 8) -> dict:
@@ -231,8 +242,10 @@ def statistics_timing(solver, case, calls: int) -> dict:
 
 
 def workload_case(args):
-    from interparts_mpich_gb300.cases import channel_case, wide_channel_case
+    from interparts_mpich_gb300.cases import channel_case, poly_case, wide_channel_case
 
+    if args.workload == "poly":
+        return poly_case(3 * args.n, 3 * args.n // 2, args.np if args.np != 1000 else 15000, seed=1234)
     if args.workload == "wide":
         return wide_channel_case(2 * args.n, args.n, args.np if args.np != 1000 else 8000, seed=1234)
     return channel_case(args.n, args.np, seed=1234)
@@ -276,10 +289,17 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver.set_stream(stream.cuda_stream)
     solver.setup(case.initial_fields())
     dt = 0.5 * solver.chkdt()  # frozen dt (0.5 dtmax at t=0, main.f90:151-154)
+    if args.workload == "poly":
+        # settling from rest: dtmax at t = 0 is the viscous limit, far above
+        # what the spheres' fall allows; CFL 0.5 on the gravitational
+        # velocity scale sqrt((rho_r - 1) g D) of the mean diameter instead
+        import math
+        dmean = 2.0 * float(case.radii.mean())
+        dt = min(dt, 0.5 / case.dxi / math.sqrt((case.ratiorho - 1.0) * 9.81 * dmean))
     learn = None
     nwarm = args.warmup
     if mode == IBM_MODE_MIXED_LEARNED:
-        if args.workload == "channel":
+        if args.workload in ("channel", "poly"):
             # the first warm-up steps: plain passes with harvesting; then GPU training
             learn = harvest_and_train(solver, case, dt, args)
             nwarm = max(1, nwarm - learn["harvest_steps"])
@@ -330,7 +350,9 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
     _, divmax, _ = solver.chkdiv()
-    stats = statistics_timing(solver, case, args.stats_calls) if args.stats_calls > 0 else None
+    # (the plane statistics are not defined for polydisperse spheres)
+    stats = (statistics_timing(solver, case, args.stats_calls)
+             if args.stats_calls > 0 and args.workload != "poly" else None)
     if learn is not None:
         st = solver.learned_stats()
         gs = solver.learned_gate_state()
@@ -412,9 +434,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="channel", choices=["channel", "wide"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "wide", "poly"],
                     help="channel: n^3, np spheres (the headline case); wide: 2n x 2n x n on a (2, 2, 1) box, "
-                         "8000 spheres, the learned network trained on the 256^3 channel")
+                         "8000 spheres, the learned network trained on the 256^3 channel; poly: 3n x 3n x 1.5n "
+                         "on a (2, 2, 1) box, 15000 settling spheres of D = 12..24 dx (rho_r 2, Ga 200), the "
+                         "network harvested and trained on the same case")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--np", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -443,9 +467,15 @@ def main():
     from interparts_mpich_gb300.cases import channel_case
 
     wl = workload_case(args)
-    config = {"workload": f"{'channel' if args.workload == 'channel' else 'wide channel'} "
-                          f"{wl.itot}x{wl.jtot}x{wl.ktot} ({wl.lx:g} x {wl.ly:g} x {wl.lz:g}), {wl.np} spheres "
-                          f"D=16dx, perturbed Poiseuille Re_b=5600, Nl=3, dt=0.5 dtmax frozen",
+    if args.workload == "poly":
+        desc = (f"polydisperse settling {wl.itot}x{wl.jtot}x{wl.ktot} ({wl.lx:g} x {wl.ly:g} x {wl.lz:g}), "
+                f"{wl.np} spheres D=12..24dx, rho_r=2, Ga=200, fluid at rest, Nl=3, "
+                f"dt=min(0.5 dtmax, 0.5 dx/sqrt((rho_r-1) g D_mean)) frozen")
+    else:
+        desc = (f"{'channel' if args.workload == 'channel' else 'wide channel'} "
+                f"{wl.itot}x{wl.jtot}x{wl.ktot} ({wl.lx:g} x {wl.ly:g} x {wl.lz:g}), {wl.np} spheres "
+                f"D=16dx, perturbed Poiseuille Re_b=5600, Nl=3, dt=0.5 dtmax frozen")
+    config = {"workload": desc,
               "grid": [wl.itot, wl.jtot, wl.ktot], "spheres": wl.np,
               "l2_policy": "inputs larger than L2 (each field >= 137 MB > 129 MB L2)"}
 

@@ -1235,6 +1235,7 @@ int ibm_set_particles(ibm_ctx *c, const ibm_particles *s) {
       CK(cudaMemcpyAsync(c->ib.fzl, s->fzl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     }
     std::vector<int> nla(np, nl);
+    if (c->pg.poly) nla = c->pnl_h;  // each sphere's own point count (the arrays' capacity is nl)
     CK(cudaMemcpyAsync(c->ib.nla, nla.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     c->particles_ready = true;
   } else {

@@ -116,3 +116,26 @@ def test_equal_radii_reproduce_monodisperse(gpu_lib):
     assert max(e.values()) <= 1e-12, e
     assert max(particle_errors(pb, pa).values()) <= 1e-12
     assert pa.contact_lists() == pb.contact_lists()
+
+
+def test_poly_state_round_trip(gpu_lib):
+    """Each sphere keeps its own point count when the state goes out through
+    ibm_get_particles with the Lagrangian arrays and back in through
+    ibm_set_particles (the arrays' capacity is the largest sphere's count)."""
+    case = poly_channel_case()
+    a, b = IBMSolver(case), IBMSolver(case)
+    a.setup()
+    b.setup()
+    dt = 0.5 * a.chkdt()
+    a.run(dt, 2)
+    b.run(dt, 2)
+    f, ps = b.get_fields(), b.get_particles(lagrangian=True)
+    b.set_fields(f["u"], f["v"], f["w"], f["p"], f["durk"], f["dvrk"], f["dwrk"])
+    b.set_particles(ps)
+    a.run(dt, 2)
+    b.run(dt, 2)
+    e = field_errors(b.get_fields(), a.get_fields())
+    assert max(e.values()) <= 1e-12, e
+    assert max(particle_errors(b.get_particles(lagrangian=False), a.get_particles(lagrangian=False)).values()) <= 1e-12
+    a.close()
+    b.close()
