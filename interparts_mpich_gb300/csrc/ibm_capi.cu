@@ -642,7 +642,7 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   const Geo &g = c->g;
   const long npts = (long)c->pg.np * c->pg.nl;
   PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
-  LAUNCHED(2);
+  LAUNCHED(3);  // reference floors, point records, boxes
   FeatIn fi;
   fi.g = g;
   fi.np = c->pg.np;
@@ -721,7 +721,7 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
     const long npts = (long)c->pg.np * c->pg.nl;
     const int npass = c->harvesting ? std::max(nl_iter, c->hv_passes) : nl_iter;
     PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
-    LAUNCHED(1);
+    LAUNCHED(3);  // reference floors, point records, boxes
     for (int it = 0; it < npass; ++it) {
       PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
                                                                              c->fv32, c->fw32, dt, it == 0 ? 1 : 0));

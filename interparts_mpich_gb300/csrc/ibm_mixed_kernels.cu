@@ -26,42 +26,49 @@ namespace ibmk {
 // component's 9 delta weights, interp_spread.f90:60-131) whenever a pass
 // needs it, instead of reading 3 x 48-byte records per point and pass.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int4 particle_ref(const Geo &g, const PartGeo &pg, const double *pf, int p) {
-  return make_int4(__double2int_rd(pf[PF_X * pg.np + p] * g.dxi), __double2int_rd(pf[PF_Y * pg.np + p] * g.dyi),
-                   __double2int_rd(pf[PF_Z * pg.np + p] * g.dzi), 0);
+// Reference floors of the particles (the floors of the centres' grid
+// coordinates) and the centres' offsets from them in cells, FP64 once per
+// particle.
+__global__ void k_ibm_pref(Geo g, PartGeo pg, IbmBuffers b) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= pg.np) return;
+  const double x = b.pf[PF_X * pg.np + p] * g.dxi, y = b.pf[PF_Y * pg.np + p] * g.dyi,
+               z = b.pf[PF_Z * pg.np + p] * g.dzi;
+  const int4 ref = make_int4(__double2int_rd(x), __double2int_rd(y), __double2int_rd(z), 0);
+  b.pref[p] = ref;
+  b.pcen[p] = make_float4((float)(x - (double)ref.x), (float)(y - (double)ref.y), (float)(z - (double)ref.z), 0.f);
 }
+// Point records: the point's position relative to its particle's reference
+// floor in cells, from its FP64 offset from the centre (exact to the FP32
+// rounding of an offset of at most the radius) plus the centre's offset;
+// the floor and the fraction of that FP32 position.  A point whose
+// absolute z lies beyond the walls' reach (or is not finite) is flagged and
+// parked at the centre, as in the FP64 form.
 __global__ void __launch_bounds__(256) k_ibm_points(Geo g, PartGeo pg, IbmBuffers b) {
   const int n = pg.np * pg.nl;  // < 2^31 points (checked at create)
+  const float dxi = (float)g.dxi, dyi = (float)g.dyi, dzi = (float)g.dzi;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int p = t / pg.nl, l = t - p * pg.nl;
-    const int4 ref = particle_ref(g, pg, b.pf, p);
-    if (l == 0) {
-      b.pref[p] = ref;
-      b.pcen[p] = make_float4((float)(b.pf[PF_X * pg.np + p] * g.dxi - (double)ref.x),
-                              (float)(b.pf[PF_Y * pg.np + p] * g.dyi - (double)ref.y),
-                              (float)(b.pf[PF_Z * pg.np + p] * g.dzi - (double)ref.z), 0.f);
-    }
     if (l >= b.nla[p]) continue;
-    const double cx = b.xfp[t] * g.dxi, cy = b.yfp[t] * g.dyi, cz = b.zfp[t] * g.dzi;
-    // floors and exact fractions; the range check as the periodic image
-    // the reference would take (a point within half a cell of the domain is
-    // shifted by one period; interp_spread.f90:60-104)
-    int nx = __double2int_rd(cx), ny = __double2int_rd(cy), nz = __double2int_rd(cz);
-    double frx = cx - (double)nx, fry = cy - (double)ny, frz = cz - (double)nz;
-    const double sx = b.xfp[t] - 0.5 * g.dx, sy = b.yfp[t] - 0.5 * g.dy;
-    const int ix = nx + (sx < 0. ? g.I : (sx >= g.lx ? -g.I : 0)), iy = ny + (sy < 0. ? g.J : (sy >= g.ly ? -g.J : 0));
-    const int ddx = nx - ref.x, ddy = ny - ref.y, ddz = nz - ref.z;
-    if (!(ix >= 0 && (ix <= g.I || (ix == g.I + 1 && frx == 0.))) ||
-        !(iy >= 0 && (iy <= g.J || (iy == g.J + 1 && fry == 0.))) || !(cz >= -1. && cz <= g.K + 0.49) ||
-        ddx < -510 || ddx > 510 || ddy < -510 || ddy > 510 || ddz < -510 || ddz > 510) {
+    const int4 ref = b.pref[p];
+    const float4 cf = b.pcen[p];
+    const float cx = fmaf((float)(b.xfp[t] - b.pf[PF_X * pg.np + p]), dxi, cf.x);
+    const float cy = fmaf((float)(b.yfp[t] - b.pf[PF_Y * pg.np + p]), dyi, cf.y);
+    const float cz = fmaf((float)(b.zfp[t] - b.pf[PF_Z * pg.np + p]), dzi, cf.z);
+    float fx = floorf(cx), fy = floorf(cy), fz = floorf(cz);
+    int dx = (int)fx, dy = (int)fy, dz = (int)fz;
+    float frx = cx - fx, fry = cy - fy, frz = cz - fz;
+    const float zabs = (float)ref.z + cz;
+    if (!(fabsf(cx) < 510.f && fabsf(cy) < 510.f && fabsf(cz) < 510.f) ||
+        !(zabs >= -1.f && zabs <= (float)g.K + 0.49f)) {  // also NaN
       atomicExch(&b.err[2], 1);
-      nx = ref.x; ny = ref.y; nz = max(min(ref.z, g.K - 1), 1); frx = 0.; fry = 0.; frz = 0.5;
+      dx = 0; dy = 0; dz = max(min(ref.z, g.K - 1), 1) - ref.z; frx = 0.f; fry = 0.f; frz = 0.5f;
     }
     PointRec r;
-    r.fx = (float)frx;
-    r.fy = (float)fry;
-    r.fz = (float)frz;
-    r.rel = (unsigned)(nx - ref.x + 512) | ((unsigned)(ny - ref.y + 512) << 10) | ((unsigned)(nz - ref.z + 512) << 20);
+    r.fx = frx;
+    r.fy = fry;
+    r.fz = frz;
+    r.rel = (unsigned)(dx + 512) | ((unsigned)(dy + 512) << 10) | ((unsigned)(dz + 512) << 20);
     b.rec[t] = r;
   }
 }
@@ -125,6 +132,7 @@ __global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, 
 
 void launch_ibm_stencil_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b) {
   if (pg.np == 0) return;
+  k_ibm_pref<<<(pg.np + 127) / 128, 128, 0, s>>>(g, pg, b);
   k_ibm_points<<<1216, 256, 0, s>>>(g, pg, b);
   k_ibm_box_geom<<<dim3(pg.np, 3), 256, 0, s>>>(pg, b, g.K);
 }
@@ -260,10 +268,16 @@ __device__ __forceinline__ float block_sum_all(float a) {
   return t;
 }
 
+// FIRST (the pass kind) and ROT (per-point rigid-body velocities) are
+// template parameters: FP64 instructions of an if-converted branch issue
+// under a false predicate and still occupy the FP64 pipe, which this GPU
+// runs at 1/64 of the FP32 rate.
+template <int FIRST, bool ROT>
 __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, PartGeo pg, IbmBuffers b,
                                                            const float *__restrict__ fu, const float *__restrict__ fv,
-                                                           const float *__restrict__ fw, double dti, int first,
+                                                           const float *__restrict__ fw, double dti,
                                                            const int *__restrict__ gate) {
+  constexpr int first = FIRST;
   if (gate && *gate == 0) return;  // learned form: plain pass not needed
   const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
@@ -306,19 +320,22 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
         return __ldg(&F[fidx(g, wrapm(ref.x + s.b[0] + i, g.I), wrapm(ref.y + s.b[1] + j, g.J), s.b[2] + k)]);
       });
     }
-    const float2 U = pg.rotation ? split_u(Ua[t]) : Us;
+    float2 U = Us;
+    if constexpr (ROT) U = split_u(Ua[t]);
     const float sd = (U.x - acc) + U.y;  // slip U - u~
-    if (first == -1) {  // residual only: sum of (U - u~)^2 of the component
+    if constexpr (FIRST == -1) {  // residual only: sum of (U - u~)^2 of the component
       r2 = fmaf(sd, sd, r2);
       continue;
     }
-    if (first < 0) {  // the interpolation only (diagnostics)
+    if constexpr (FIRST < 0) {  // the interpolation only (diagnostics)
       dud[t] = acc;
       continue;
     }
     slip[t] = sd;  // the spreading's increment (U - u~)/dt, FP32
-    if (first) r0 = fmaf(sd, sd, r0);  // first-pass slip, for the learned loop's gate reference
-    const double f = first ? (double)sd * dti : fma((double)sd, dti, Fl[t]);
+    if constexpr (FIRST == 1) r0 = fmaf(sd, sd, r0);  // first-pass slip, for the learned loop's gate reference
+    double f;
+    if constexpr (FIRST == 1) f = (double)sd * dti;
+    else f = fma((double)sd, dti, Fl[t]);
     Fl[t] = f;
     const float ff = (float)f;
     float la, lb;
@@ -366,8 +383,14 @@ __global__ void k_ibm_force_sums(PartGeo pg, IbmBuffers b, const int *__restrict
 int launch_ibm_interp_force_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuffers b, const float *fu,
                               const float *fv, const float *fw, double dt, int first, const int *gate) {
   if (pg.np == 0) return 0;
-  k_ibm_interp_comp_f<<<dim3(pg.np, 3), INTERP_THREADS, pg.box_cap * sizeof(float), s>>>(g, pg, b, fu, fv, fw,
-                                                                                         1. / dt, first, gate);
+  const dim3 grd(pg.np, 3);
+  const size_t sm = pg.box_cap * sizeof(float);
+  auto go = [&](auto kern) { kern<<<grd, INTERP_THREADS, sm, s>>>(g, pg, b, fu, fv, fw, 1. / dt, gate); };
+  const bool rot = pg.rotation != 0;
+  if (first == 1) rot ? go(k_ibm_interp_comp_f<1, true>) : go(k_ibm_interp_comp_f<1, false>);
+  else if (first == 0) rot ? go(k_ibm_interp_comp_f<0, true>) : go(k_ibm_interp_comp_f<0, false>);
+  else if (first == -1) rot ? go(k_ibm_interp_comp_f<-1, true>) : go(k_ibm_interp_comp_f<-1, false>);
+  else rot ? go(k_ibm_interp_comp_f<-2, true>) : go(k_ibm_interp_comp_f<-2, false>);
   if (first < 0) return 1;
   k_ibm_force_sums<<<(pg.np + 127) / 128, 128, 0, s>>>(pg, b, gate);
   return 2;
@@ -412,6 +435,9 @@ __device__ __forceinline__ void spread27_box(float *box, const CompStencil &s, i
     }
 }
 
+// LY: a learned (or perturbation) force is given (lf.Y), as a template
+// parameter so that the plain passes issue none of its FP64 work
+template <bool LY>
 __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartGeo pg, IbmBuffers b, float *__restrict__ fu,
                                                       float *__restrict__ fv, float *__restrict__ fw, double dti,
                                                       double coeff0_, LearnedForce lf,
@@ -420,8 +446,8 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
   if (nla <= 0) {
-    if (lf.Y && threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = 0.;
-    if (lf.Y && !lf.incr && threadIdx.x == 0) b.rsum[(long)p * 3 + c] = 0.f;
+    if (LY && threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = 0.;
+    if (LY && !lf.incr && threadIdx.x == 0) b.rsum[(long)p * 3 + c] = 0.f;
     return;
   }
   const long npl = (long)pg.np * pg.nl, t0 = (long)p * pg.nl;
@@ -449,7 +475,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   float4 cf = make_float4(0.f, 0.f, 0.f, 0.f);
   float ysig = 0.f, ymu = 0.f, dtif = 0.f, dtf = 0.f;
   const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
-  if (lf.Y) {
+  if constexpr (LY) {
     cf = b.pcen[p];
     ysig = lf.tsig[c]; ymu = lf.tmu[c];
     dtif = (float)lf.dti; dtf = (float)(1. / lf.dti);
@@ -470,7 +496,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     if (l >= nla) continue;
     const long t = t0 + l;
     float pre;
-    if (lf.Y) {
+    if constexpr (LY) {
       // total point force F0 + the network's correction, its sums
       // (updtlagrforces), spread once
       const double f0 = Fl[t];
@@ -507,7 +533,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
         }
     }
   }
-  if (lf.Y) {  // psum[p][c] for k_ibm_force_sums; rsum for the gate
+  if constexpr (LY) {  // psum[p][c] for k_ibm_force_sums; rsum for the gate
     __shared__ double sred[3 * SPREAD_THREADS], res[3];
     block_sum3<SPREAD_THREADS>((double)sF, (double)sa, (double)sb, sred, res);
     if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
@@ -574,8 +600,12 @@ void launch_ibm_spread_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmBuf
                          float *fw, double dt, const LearnedForce &lf, const int *gate) {
   if (pg.np == 0) return;
   const double coeff0 = (pg.dVlagr / pg.dVeul) * dt;
-  k_ibm_spread_f<<<dim3(pg.np, 3), SPREAD_THREADS, pg.box_cap * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt,
-                                                                                    coeff0, lf, gate, dt);
+  auto go = [&](auto kern) {
+    kern<<<dim3(pg.np, 3), SPREAD_THREADS, pg.box_cap * sizeof(float), s>>>(g, pg, b, fu, fv, fw, 1. / dt, coeff0, lf,
+                                                                          gate, dt);
+  };
+  if (lf.Y) go(k_ibm_spread_f<true>);
+  else go(k_ibm_spread_f<false>);
 }
 void launch_ibm_force_sums(cudaStream_t s, const PartGeo &pg, IbmBuffers b) {
   if (pg.np == 0) return;
@@ -722,10 +752,17 @@ void launch_ibm_features_f(cudaStream_t s, const Geo &g, const PartGeo &pg, IbmB
 int ibm_set_smem_limits(int box_cap) {
   static int cur = 0;
   if (box_cap <= cur) return 0;
-  cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e1 = cudaFuncSetAttribute(k_ibm_spread_f<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         box_cap * (int)sizeof(float));
-  cudaError_t e2 = cudaFuncSetAttribute(k_ibm_interp_comp_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        box_cap * (int)sizeof(float));
+  if (e1 == cudaSuccess)
+    e1 = cudaFuncSetAttribute(k_ibm_spread_f<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              box_cap * (int)sizeof(float));
+  cudaError_t e2 = cudaSuccess;
+  for (auto k : {k_ibm_interp_comp_f<1, false>, k_ibm_interp_comp_f<0, false>, k_ibm_interp_comp_f<-1, false>,
+                 k_ibm_interp_comp_f<-2, false>, k_ibm_interp_comp_f<1, true>, k_ibm_interp_comp_f<0, true>,
+                 k_ibm_interp_comp_f<-1, true>, k_ibm_interp_comp_f<-2, true>})
+    if (e2 == cudaSuccess)
+      e2 = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, box_cap * (int)sizeof(float));
   if (e1 != cudaSuccess || e2 != cudaSuccess) return -1;
   cur = box_cap;
   return 0;
