@@ -449,7 +449,7 @@ def main():
                     help="plain warm-up steps harvested (every stride-th point, so that the capacity spans them)")
     ap.add_argument("--harvest-passes", type=int, default=3,
                     help="plain passes of the harvested loops (3: the Nl = 3 correction the network replaces)")
-    ap.add_argument("--train-steps", type=int, default=6000)
+    ap.add_argument("--train-steps", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--stats-calls", type=int, default=3, help="post1d calls timed after the steps (0: none)")
     ap.add_argument("--probe-mask", type=int, default=-1,

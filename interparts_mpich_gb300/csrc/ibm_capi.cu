@@ -503,6 +503,10 @@ int alloc_all(ibm_ctx *c) {
       if ((st = dalloc(c, &c->ib.rec, npl))) return st;
       if ((st = dalloc(c, &c->ib.pref, (size_t)np))) return st;
       if ((st = dalloc(c, &c->ib.pcen, (size_t)np))) return st;
+      for (float **f : {&c->ib.fxs, &c->ib.fys, &c->ib.fzs})
+        if ((st = dalloc(c, f, npl))) return st;
+      if ((st = dalloc(c, &c->ib.pvh, (size_t)np))) return st;
+      if ((st = dalloc(c, &c->ib.pvl, (size_t)np))) return st;
       if ((st = dalloc(c, &c->ib.slip, 3 * npl))) return st;
       if ((st = dalloc(c, &c->ib.bgeo, (size_t)24 * np))) return st;
       if ((st = dalloc(c, &c->ib.rowx, (size_t)3 * IBM_BOX_ROWS * np))) return st;
@@ -651,11 +655,13 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   fi.rec = c->ib.rec;
   fi.pref = c->ib.pref;
   fi.pcen = c->ib.pcen;
+  fi.pvh = c->ib.pvh;
+  fi.pvl = c->ib.pvl;
   fi.rotation = c->pg.rotation;
   fi.F[0] = c->fu32; fi.F[1] = c->fv32; fi.F[2] = c->fw32;
   fi.U[0] = c->ib.ul; fi.U[1] = c->ib.vl; fi.U[2] = c->ib.wl;
   fi.pf = c->pb.pf;
-  fi.Fl[0] = c->ib.fxl; fi.Fl[1] = c->ib.fyl; fi.Fl[2] = c->ib.fzl;
+  fi.Fl[0] = c->ib.fxs; fi.Fl[1] = c->ib.fys; fi.Fl[2] = c->ib.fzs;
   fi.dt = dt;
   fi.dti = 1. / dt;
   fi.inv_r = (float)(1. / c->pg.radfp);
@@ -1000,7 +1006,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->pb.cstart, c->pb.cfill, c->pb.citem, c->pb.ccell, c->ru32, c->rv32, c->rw32, c->fu32,
-                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
+                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.fxs, c->ib.fys, c->ib.fzs, c->ib.pvh, c->ib.pvl, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
                   c->cfield, c->cnext, c->crk, c->ferr, c->psize, c->pcount};
   for (void *q : ptrs)
@@ -1233,6 +1239,12 @@ int ibm_set_particles(ibm_ctx *c, const ibm_particles *s) {
       CK(cudaMemcpyAsync(c->ib.fxl, s->fxl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemcpyAsync(c->ib.fyl, s->fyl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemcpyAsync(c->ib.fzl, s->fzl, npl * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      if (c->mixed) {  // the mixed forms carry the point forces in FP32
+        launch_d2f(c->stream, (long)npl, c->ib.fxl, c->ib.fxs);
+        launch_d2f(c->stream, (long)npl, c->ib.fyl, c->ib.fys);
+        launch_d2f(c->stream, (long)npl, c->ib.fzl, c->ib.fzs);
+        LAUNCHED(3);
+      }
     }
     std::vector<int> nla(np, nl);
     if (c->pg.poly) nla = c->pnl_h;  // each sphere's own point count (the arrays' capacity is nl)
@@ -1263,6 +1275,12 @@ int ibm_get_particles(ibm_ctx *c, ibm_particles *s) {
   if (s->nb) CK(cudaMemcpyAsync(s->nb, c->pb.nb, (size_t)np * 9 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   if (s->mslv) CK(cudaMemcpyAsync(s->mslv, c->pb.mslv, np * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   const size_t npl = (size_t)np * nl;
+  if (c->mixed && (s->fxl || s->fyl || s->fzl)) {  // the mixed forms' FP32 point forces, widened
+    launch_f2d(c->stream, (long)npl, c->ib.fxs, c->ib.fxl);
+    launch_f2d(c->stream, (long)npl, c->ib.fys, c->ib.fyl);
+    launch_f2d(c->stream, (long)npl, c->ib.fzs, c->ib.fzl);
+    LAUNCHED(3);
+  }
   const double *ls[9] = {c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl, c->ib.wl, c->ib.fxl, c->ib.fyl, c->ib.fzl};
   double *lh[9] = {s->xfp, s->yfp, s->zfp, s->ul, s->vl, s->wl, s->fxl, s->fyl, s->fzl};
   for (int f = 0; f < 9; ++f)

@@ -281,9 +281,9 @@ __global__ void k_ibm_harvest_targets(IbmBuffers b, HarvestArgs H, double dt) {
   for (int h = lo + blockIdx.x * blockDim.x + threadIdx.x; h < hi; h += gridDim.x * blockDim.x) {
     const int t = H.pidx[h];
     const float *f = H.feat + (long)h * 96 + FEAT_F0;
-    H.targ[3 * (long)h] = (float)(b.fxl[t] * dt) - f[0];
-    H.targ[3 * (long)h + 1] = (float)(b.fyl[t] * dt) - f[FEAT_PER_COMP];
-    H.targ[3 * (long)h + 2] = (float)(b.fzl[t] * dt) - f[2 * FEAT_PER_COMP];
+    H.targ[3 * (long)h] = b.fxs[t] * (float)dt - f[0];
+    H.targ[3 * (long)h + 1] = b.fys[t] * (float)dt - f[FEAT_PER_COMP];
+    H.targ[3 * (long)h + 2] = b.fzs[t] * (float)dt - f[2 * FEAT_PER_COMP];
   }
 }
 __global__ void k_ibm_harvest_close(HarvestArgs H) {

@@ -26,9 +26,15 @@ namespace ibmk {
 // component's 9 delta weights, interp_spread.f90:60-131) whenever a pass
 // needs it, instead of reading 3 x 48-byte records per point and pass.
 // ---------------------------------------------------------------------------
+// The rigid-body velocity of a point as an FP32 pair hi + lo (the slip
+// U - u~ = (hi - u~) + lo keeps the FP64 velocity's bits that FP32 u~ resolves)
+__device__ __forceinline__ float2 split_u(double U) {
+  const float hi = (float)U;
+  return make_float2(hi, (float)(U - (double)hi));
+}
 // Reference floors of the particles (the floors of the centres' grid
-// coordinates) and the centres' offsets from them in cells, FP64 once per
-// particle.
+// coordinates), the centres' offsets from them in cells and the velocities
+// as FP32 pairs, FP64 once per particle.
 __global__ void k_ibm_pref(Geo g, PartGeo pg, IbmBuffers b) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= pg.np) return;
@@ -37,6 +43,10 @@ __global__ void k_ibm_pref(Geo g, PartGeo pg, IbmBuffers b) {
   const int4 ref = make_int4(__double2int_rd(x), __double2int_rd(y), __double2int_rd(z), 0);
   b.pref[p] = ref;
   b.pcen[p] = make_float4((float)(x - (double)ref.x), (float)(y - (double)ref.y), (float)(z - (double)ref.z), 0.f);
+  const float2 u = split_u(b.pf[PF_U * pg.np + p]), v = split_u(b.pf[PF_V * pg.np + p]),
+               w = split_u(b.pf[PF_W * pg.np + p]);
+  b.pvh[p] = make_float4(u.x, v.x, w.x, 0.f);
+  b.pvl[p] = make_float4(u.y, v.y, w.y, 0.f);
 }
 // Point records: the point's position relative to its particle's reference
 // floor in cells, from its FP64 offset from the centre (exact to the FP32
@@ -191,12 +201,6 @@ __device__ __forceinline__ void lever_arms(const PointRec &rr, const float4 &cf,
   la = c == 2 ? ry : rec_armf(rec_dz(rr.rel), rr.fz, cf.z, hz);
   lb = c == 0 ? ry : rec_armf(rec_dx(rr.rel), rr.fx, cf.x, hx);
 }
-// The rigid-body velocity of a point as an FP32 pair hi + lo (the slip
-// U - u~ = (hi - u~) + lo keeps the FP64 velocity's bits that FP32 u~ resolves)
-__device__ __forceinline__ float2 split_u(double U) {
-  const float hi = (float)U;
-  return make_float2(hi, (float)(U - (double)hi));
-}
 // rigid-body velocity component of point t: the particle's, or with rotation
 // on the per-point value (u + omega x r, updated with the points)
 __device__ __forceinline__ double point_u(const PartGeo &pg, const double *Ua, double Up, long t) {
@@ -295,12 +299,14 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
   }
   double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);
   const double *Ua = c == 0 ? b.ul : (c == 1 ? b.vl : b.wl);
-  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
+  float *Fl = c == 0 ? b.fxs : (c == 1 ? b.fys : b.fzs);
   float *slip = b.slip + c * npl;
-  const float2 Us = split_u(b.pf[(c == 0 ? PF_U : (c == 1 ? PF_V : PF_W)) * pg.np + p]);
+  const float4 vh = b.pvh[p], vl = b.pvl[p];
+  const float2 Us = c == 0 ? make_float2(vh.x, vl.x) : (c == 1 ? make_float2(vh.y, vl.y) : make_float2(vh.z, vl.z));
   const int4 ref = b.pref[p];
   const float4 cf = b.pcen[p];
   const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
+  const float dtif = (float)dti;
   const PointRec *rp = b.rec + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
   // per-thread force and lever-arm sums in FP32 (a few points per thread),
@@ -333,11 +339,10 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
     }
     slip[t] = sd;  // the spreading's increment (U - u~)/dt, FP32
     if constexpr (FIRST == 1) r0 = fmaf(sd, sd, r0);  // first-pass slip, for the learned loop's gate reference
-    double f;
-    if constexpr (FIRST == 1) f = (double)sd * dti;
-    else f = fma((double)sd, dti, Fl[t]);
-    Fl[t] = f;
-    const float ff = (float)f;
+    float ff;  // the point force, FP32 (its sums below, FP64 across the block)
+    if constexpr (FIRST == 1) ff = sd * dtif;
+    else ff = fmaf(sd, dtif, Fl[t]);
+    Fl[t] = ff;
     float la, lb;
     lever_arms(rr, cf, c, hx, hy, hz, la, lb);
     sF += ff;
@@ -467,7 +472,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     __syncthreads();
   }
   const float *slip = b.slip + c * npl;
-  double *Fl = c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl);
+  float *Fl = c == 0 ? b.fxs : (c == 1 ? b.fys : b.fzs);
   const int4 ref = b.pref[p];
   const PointRec *rp = b.rec + t0;
   // per-thread force and lever-arm sums in FP32, the block's sums in FP64
@@ -499,13 +504,12 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     if constexpr (LY) {
       // total point force F0 + the network's correction, its sums
       // (updtlagrforces), spread once
-      const double f0 = Fl[t];
+      const float f0 = Fl[t];
       const float d = fmaf(lf.Y[3 * t + c], ysig, ymu) * dtif;
-      const double f = f0 + (double)d;
-      Fl[t] = f;
-      const float e0 = (float)f0 * dtf;  // the first pass's slip U - u~
+      const float ff = f0 + d;
+      Fl[t] = ff;
+      const float e0 = f0 * dtf;  // the first pass's slip U - u~
       r0 = fmaf(e0, e0, r0);
-      const float ff = (float)f;
       float la, lb;
       lever_arms(rp[l], cf, c, hx, hy, hz, la, lb);
       sF += ff;
@@ -697,7 +701,8 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
         const CompStencil s = make_cs(rr, c, ref.z, g.K);
         const float a = interp27(s, [&](int i, int j, int k) { return tap(c == 0 ? fu : (c == 1 ? fv : fw), s, i, j, k); });
         (c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl))[t] = a;
-        if (first_force) (c == 0 ? b.fxl : (c == 1 ? b.fyl : b.fzl))[t] = (point_u(pg, Ua[c], Up[c], t) - a) * dti;
+        if (first_force)
+          (c == 0 ? b.fxs : (c == 1 ? b.fys : b.fzs))[t] = (float)((point_u(pg, Ua[c], Up[c], t) - a) * dti);
       }
       continue;
     }
@@ -708,7 +713,7 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
                           rec_armf(rec_dz(rr.rel), rr.fz, cf.z, (float)g.dz) * ir};
     const float *F3[3] = {fu, fv, fw};
     double *D3[3] = {b.dudtl, b.dvdtl, b.dwdtl};
-    double *Fl3[3] = {b.fxl, b.fyl, b.fzl};
+    float *Fl3[3] = {b.fxs, b.fys, b.fzs};
 #pragma unroll 1
     for (int c = 0; c < 3; ++c) {
       const CompStencil s = make_cs(rr, c, ref.z, g.K);
@@ -728,11 +733,11 @@ __global__ void __launch_bounds__(256, 2) k_ibm_features_f(Geo g, PartGeo pg, Ib
           }
         }
       D3[c][t] = acc;
-      if (first_force) Fl3[c][t] = (Ud - acc) * dti;
+      if (first_force) Fl3[c][t] = (float)((Ud - acc) * dti);
       snk.put(Uc - acc);
       snk.put(Uc);
       snk.put(nrm[c]);
-      snk.put((float)Fl3[c][t] * (float)dt);
+      snk.put(Fl3[c][t] * (float)dt);
       snk.put(s.w[3 * c + 1]);
     }
   }

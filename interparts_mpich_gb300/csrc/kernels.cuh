@@ -83,6 +83,8 @@ struct IbmBuffers {
   double *xfp, *yfp, *zfp, *ul, *vl, *wl, *dudtl, *dvdtl, *dwdtl, *fxl, *fyl, *fzl;
   PointStencil *st;
   PointRec *rec;     // mixed form: [np*nl] compact point records (make_cs)
+  float *fxs, *fys, *fzs;  // mixed forms: [np*nl] point forces F_l (FP32; fxl.. hold FP64 copies at the boundary)
+  float4 *pvh, *pvl;       // mixed forms: [np] particle velocity u, v, w as FP32 pairs hi + lo
   int4 *pref;        // mixed form: [np] reference floors (refx, refy, refz) of the particles
   float4 *pcen;      // mixed form: [np] centre position in cells relative to the reference floor (FP32)
   float *slip;       // mixed form: [3][np*nl] slip U - u~ of the last pass (FP32)
@@ -180,11 +182,12 @@ struct FeatIn {
   const PointRec *rec;
   const int4 *pref;
   const float4 *pcen;
+  const float4 *pvh, *pvl;  // particle velocity as FP32 pairs (without rotation)
   int rotation;        // 0: U is the particle velocity; 1: read U[] (with the rotation term)
   const float *F[3];   // u, v, w (FP32 fields)
   const double *U[3];  // rigid-body velocity at the points (read with rotation on)
   const double *pf;    // particle scalar fields (centres, velocities)
-  double *Fl[3];
+  float *Fl[3];      // point forces (FP32)
   double dt, dti;
   float inv_r;
   const double *pradfp;  // polydisperse: per-sphere shell radius (the normal's scale), else null

@@ -531,8 +531,17 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
   for (int c = 0; c < 3; ++c) {
     const CompStencil s = make_cs(rr, c, ref.z, g.K);
     const float *F = fi.F[c];
-    const double Ud = fi.rotation ? fi.U[c][t] : fi.pf[(PF_U + c) * fi.np + p];
-    const float Uc = (float)Ud;
+    // the rigid-body velocity as an FP32 pair (per point with rotation)
+    float2 Us;
+    if (fi.rotation) {
+      const double Ud = fi.U[c][t];
+      Us.x = (float)Ud;
+      Us.y = (float)(Ud - (double)Us.x);
+    } else {
+      const float4 vh = fi.pvh[p], vl = fi.pvl[p];
+      Us = c == 0 ? make_float2(vh.x, vl.x) : (c == 1 ? make_float2(vh.y, vl.y) : make_float2(vh.z, vl.z));
+    }
+    const float Uc = Us.x;
     float f[FEAT_PER_COMP];
     float acc = 0.f;
 #pragma unroll
@@ -548,7 +557,7 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
           f[(k * 3 + j) * 3 + i] = tv - Uc;
         }
       }
-    const double F0 = (Ud - acc) * fi.dti;
+    const float F0 = ((Uc - acc) + Us.y) * (float)fi.dti;  // (U - u~)/dt, as the first plain pass forms it
     fi.Fl[c][t] = F0;
     f[27] = Uc - acc;
     f[28] = Uc;
