@@ -1052,10 +1052,28 @@ static int ensure_href(ibm_ctx *c) {
   return IBM_OK;
 }
 
+// A device-side alias of a caller's array: page-locked host memory is mapped
+// into the device's address space (unified addressing), so the layout
+// conversion kernels can read and write it directly over the host link, with
+// no staging copy; device and managed memory are used as they are.  nullptr
+// for pageable memory, which takes the staging buffer and cudaMemcpy.
+static const void *device_view(const void *h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) return nullptr;
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return a.devicePointer ? a.devicePointer : h;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
 static int upload_field(ibm_ctx *c, const double *h, double *d) {
   const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
   if (!h) {
     CK(cudaMemsetAsync(d, 0, (size_t)c->g.nfield * sizeof(double), c->stream));
+    return IBM_OK;
+  }
+  if (const double *dv = static_cast<const double *>(device_view(h))) {
+    launch_ref_to_dev<double>(c->stream, c->g, dv, d);
+    LAUNCHED(1);
     return IBM_OK;
   }
   CK(cudaMemcpyAsync(c->href, h, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -1063,25 +1081,27 @@ static int upload_field(ibm_ctx *c, const double *h, double *d) {
   LAUNCHED(1);
   return IBM_OK;
 }
-static int download_field(ibm_ctx *c, const double *d, double *h) {
+// the reference-layout copy of one device field into h (synchronised by the
+// caller)
+extern "C++" {
+template <typename T>
+static int download_any(ibm_ctx *c, const T *d, double *h) {
   if (!h) return IBM_OK;
   const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
-  launch_dev_to_ref<double>(c->stream, c->g, d, c->href);
+  if (double *dv = static_cast<double *>(const_cast<void *>(device_view(h)))) {
+    launch_dev_to_ref<T>(c->stream, c->g, d, dv);
+    LAUNCHED(1);
+    return IBM_OK;
+  }
+  launch_dev_to_ref<T>(c->stream, c->g, d, c->href);
   LAUNCHED(1);
   CK(cudaMemcpyAsync(h, c->href, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaStreamSynchronize(c->stream));  // href is reused by the next field
   return IBM_OK;
 }
-
-static int download_field32(ibm_ctx *c, const float *d, double *h) {
-  if (!h) return IBM_OK;
-  const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
-  launch_dev_to_ref<float>(c->stream, c->g, d, c->href);
-  LAUNCHED(1);
-  CK(cudaMemcpyAsync(h, c->href, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  return IBM_OK;
-}
+}  // extern "C++"
+static int download_field(ibm_ctx *c, const double *d, double *h) { return download_any<double>(c, d, h); }
+static int download_field32(ibm_ctx *c, const float *d, double *h) { return download_any<float>(c, d, h); }
 
 int ibm_set_fields(ibm_ctx *c, const double *u, const double *v, const double *w, const double *p, const double *durk,
                    const double *dvrk, const double *dwrk) {
@@ -1105,8 +1125,12 @@ int ibm_set_fields(ibm_ctx *c, const double *u, const double *v, const double *w
     for (int f = 0; f < 6; ++f) {
       if (h32[f]) {
         const size_t n = (size_t)(c->g.I + 2) * (c->g.J + 2) * (c->g.K + 2);
-        CK(cudaMemcpyAsync(c->href, h32[f], n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        launch_ref_to_dev<float>(c->stream, c->g, c->href, d32[f]);
+        const double *src = static_cast<const double *>(device_view(h32[f]));
+        if (!src) {
+          CK(cudaMemcpyAsync(c->href, h32[f], n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+          src = c->href;
+        }
+        launch_ref_to_dev<float>(c->stream, c->g, src, d32[f]);
         LAUNCHED(1);
       } else {
         CK(cudaMemsetAsync(d32[f], 0, (size_t)c->g.nfield * sizeof(float), c->stream));
@@ -1131,6 +1155,7 @@ int ibm_get_fields(ibm_ctx *c, double *u, double *v, double *w, double *p, doubl
   if (!c->mixed) {
     for (int f = 0; f < 7; ++f)
       if ((st = download_field(c, ds[f], hs[f]))) return st;
+    CK(cudaStreamSynchronize(c->stream));
     return IBM_OK;
   }
   if (p) {
@@ -1142,6 +1167,7 @@ int ibm_get_fields(ibm_ctx *c, double *u, double *v, double *w, double *p, doubl
   double *h32[6] = {u, v, w, durk, dvrk, dwrk};
   for (int f = 0; f < 6; ++f)
     if ((st = download_field32(c, d32[f], h32[f]))) return st;
+  CK(cudaStreamSynchronize(c->stream));
   return IBM_OK;
 }
 
