@@ -383,14 +383,14 @@ int ibm_get_forcing_model(ibm_ctx *ctx, float *params, float *norm);
  * the learned loop's residual R is held to fallback_ratio x c_s x R0, R0 its
  * own first-pass slip (rms |U - u~| before any forcing) and c_s the factor
  * by which the plain passes reduced the first-pass slip on the latest plain
- * loops measured at the same RK stage s (harvested loops and the
- * calibration loops below).  The stage is that of the last ibm_rk_predict. */
+ * loop measured at the same RK stage s (a calibration loop below, or before
+ * any, a harvested loop).  The stage is that of the last ibm_rk_predict. */
 int ibm_learned_config(ibm_ctx *ctx, int enable, double fallback_ratio, double plain_rms_ref);
-/* With the network on, every period-th forcing loop runs the plain passes
- * instead and measures c_s on the current state (default 10, which visits
- * the three stages in turn, each once every ten RK3 steps; 0: never, c_s
- * then comes from the harvest); a loop with the network on at a stage
- * without any plain loop measured yet is one. */
+/* Calibration loops: with the network on, a forcing loop at RK stage s runs
+ * the plain passes instead and measures c_s on the current state when s has
+ * none measured since the model was trained or set, and then after 1, 2, 4,
+ * 8 ... learned loops of s, at most period - 1 (default 10: one loop in ten
+ * per stage once settled; 0: the first only). */
 int ibm_learned_calibration(ibm_ctx *ctx, int period);
 /* stats[6]: rms residual of the last learned loop, the reference its gate
  * used (before any learned loop: the last plain residual measured), fallback

@@ -75,14 +75,15 @@ struct ibm_ctx {
   HarvestArgs hv{};
   int hv_passes = 0;
   bool harvesting = false, learn_on = false, model_ready = false, stats_ready = false;
-  // live plain reference of the fallback gate: every calib_period-th loop
-  // with the network on runs the plain passes and measures their reduction
-  // of the first-pass slip, per RK stage (also the first such loop of a
-  // stage when that stage has no plain loop measured yet); a period that is
-  // not a multiple of 3 visits the stages in turn
+  // live plain reference of the fallback gate: a loop with the network on
+  // at RK stage s runs the plain passes instead and measures their
+  // reduction of the first-pass slip when s has no plain loop measured
+  // since the model was set, and then after 1, 2, 4, 8 ... learned loops of
+  // s (the learned forcing's imprint on the flow changes the reduction over
+  // the first steps), at most calib_period - 1; period 0: the first only
   int calib_period = 10;
-  long long learn_calls = 0;
-  bool calibrated[3] = {false, false, false};
+  int ncal[3] = {0, 0, 0};               // plain loops measured per stage since the model was set
+  long long since[3] = {0, 0, 0};        // learned loops per stage since its last plain loop
   int stage = 0;  // RK stage of the last predictor call (0..2)
   // forcing perturbation (a test of the learned form's error budget): point
   // noise of rms noise_sigma (velocity units) after the plain passes
@@ -719,9 +720,13 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
   if (c->mixed) {
     bool calibrate = false;
     if (c->learn_on && !c->harvesting && nl_iter >= 2) {
-      const long long k = c->learn_calls++;
-      calibrate = !c->calibrated[c->stage] || (c->calib_period > 0 && k % c->calib_period == c->calib_period - 1);
-      if (!calibrate) return forcing_learned(c, dt, nl_iter);
+      const int s = c->stage;
+      const long long gap = std::min<long long>(1LL << std::min(std::max(c->ncal[s] - 1, 0), 30), c->calib_period - 1);
+      calibrate = c->ncal[s] == 0 || (c->calib_period > 0 && c->since[s] >= gap);
+      if (!calibrate) {
+        ++c->since[s];
+        return forcing_learned(c, dt, nl_iter);
+      }
     }
     const bool measure = c->harvesting || calibrate;
     const long npts = (long)c->pg.np * c->pg.nl;
@@ -752,7 +757,10 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
         PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
         launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 1, c->stage);
         LAUNCHED(2);
-        c->calibrated[c->stage] = true;
+        if (calibrate) {
+          ++c->ncal[c->stage];
+          c->since[c->stage] = 0;
+        }
       }
     }
     if (c->harvesting) {
@@ -1852,6 +1860,21 @@ int ibm_harvest(ibm_ctx *c, int capacity, int stride, int passes) {
   return IBM_OK;
 }
 
+// a new model: the live gate's plain reduction factors are measured afresh
+// per RK stage (those of the harvest come from an earlier flow)
+static int reset_gate_factors(ibm_ctx *c) {
+  for (int s = 0; s < 3; ++s) c->ncal[s] = 0, c->since[s] = 0;
+  if (!c->ls) return IBM_OK;
+  double h[IBM_LS_N];
+  CK(cudaMemcpyAsync(h, c->ls, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  h[1] = h[11] = h[12] = 0.;
+  h[13] = h[14] = h[15] = 0.;
+  CK(cudaMemcpyAsync(c->ls, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
 int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsigned seed, int reinit, double *loss) {
   if (!c) return IBM_E_INVALID;
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "training needs IBM_MODE_MIXED_LEARNED");
@@ -1927,7 +1950,7 @@ int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsign
   if (loss) *loss = l;
   c->model_ready = true;
   c->learn_on = true;
-  return IBM_OK;
+  return reset_gate_factors(c);
 }
 
 int ibm_set_forcing_model(ibm_ctx *c, const float *params, const float *norm) {
@@ -1942,7 +1965,7 @@ int ibm_set_forcing_model(ibm_ctx *c, const float *params, const float *norm) {
   CK(cudaStreamSynchronize(c->stream));
   c->train_step = 0;
   c->stats_ready = c->model_ready = c->learn_on = true;
-  return IBM_OK;
+  return reset_gate_factors(c);
 }
 
 int ibm_get_forcing_model(ibm_ctx *c, float *params, float *norm) {
@@ -1993,7 +2016,7 @@ int ibm_learned_calibration(ibm_ctx *c, int period) {
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "needs IBM_MODE_MIXED_LEARNED");
   if (period < 0) return set_err(c, IBM_E_INVALID, "period must be >= 0");
   c->calib_period = period;
-  c->learn_calls = 0;
+  for (long long &n : c->since) n = 0;
   return IBM_OK;
 }
 

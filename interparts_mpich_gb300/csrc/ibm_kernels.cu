@@ -301,7 +301,7 @@ void launch_ibm_harvest_targets(cudaStream_t s, IbmBuffers b, const HarvestArgs 
 // learned loop of stage s is held to fallback ratio x (that stage's ratio x
 // its own R0), i.e. to what the plain passes would reach from the same
 // first-pass slip.  Learn state ls (device):
-//   [0] R of the last learned loop      [1] plain R/R0 of stage 1 (running, weight 1/2)
+//   [0] R of the last learned loop      [1] plain R/R0 of stage 1 (the last measured)
 //   [2] plain loops measured            [3] fallback ratio
 //   [4] fallbacks taken                 [5] learned loops
 //   [6] R0 of the last learned loop     [7] reference of the last gate
@@ -333,8 +333,9 @@ __global__ void __launch_bounds__(1024) k_ibm_res_gate(int n, const double *__re
   const double R = npts ? sqrt(tot / (double)npts) : 0., R0 = npts ? sqrt(tot0 / (double)npts) : 0.;
   const int cs = stage == 0 ? 1 : 10 + stage, ns = 13 + stage;
   if (plain) {  // the plain passes' reduction of the slip on the current state
-    const double ci = R0 > 0. ? R / R0 : 0.;
-    ls[cs] = ls[ns] > 0. ? 0.5 * ls[cs] + 0.5 * ci : ci;
+    // the latest measurement alone: the reduction drifts as the flow (and
+    // the learned forcing's imprint on it) develops, an average lags it
+    ls[cs] = R0 > 0. ? R / R0 : 0.;
     ls[ns] += 1.;
     ls[2] += 1.;
     ls[9] = R0;

@@ -332,8 +332,9 @@ class IBMSolver:
         self._chk(self.fn["learned_config"](self.ctx, int(enable), float(fallback_ratio), float(plain_rms_ref)))
 
     def learned_calibration(self, period: int):
-        """Every period-th loop with the network on runs the plain passes and
-        refreshes the gate's reference (0: never)."""
+        """Calibration loops (plain passes that refresh the gate's per-stage
+        reduction factor): after 1, 2, 4 ... learned loops of a stage, at
+        most period - 1 (0: only the first loop of each stage)."""
         self._chk(self.fn["learned_calibration"](self.ctx, int(period)))
 
     def learned_gate_state(self) -> dict:
