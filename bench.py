@@ -319,11 +319,13 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
         solver.rk3_step(dt)
     solver.sync()
     phases = solver.timed_step(dt)
-    # one untimed step with CUDA events around every kernel class: the kernel
-    # table, and the dominant class, the only one timed inside the timed steps
-    # (events around every class cost about 0.2 ms per step)
+    # untimed steps (as many as the timed ones: the learned form's calibration
+    # loops fall on some steps only) with CUDA events around every kernel
+    # class: the kernel table, and the dominant class, the only one timed
+    # inside the timed steps (events around every class cost about 0.2 ms per step)
+    probe_steps = max(1, args.steps)
     solver.probe()
-    solver.run(dt, 1)
+    solver.run(dt, probe_steps)
     kernels_all = solver.probe_result()
     dom_class = max(kernels_all, key=lambda k: kernels_all[k][0])
     mask = args.probe_mask if args.probe_mask >= 0 else 1 << solver.PROBE_NAMES.index(dom_class)
@@ -403,7 +405,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver.close()
     return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
             "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn,
-            "kernels": kernels_all, "kernels_timed": kernels_timed, "stats": stats}
+            "kernels": kernels_all, "kernels_timed": kernels_timed, "probe_steps": probe_steps, "stats": stats}
 
 
 def cpu_baseline(args, case_fn):
@@ -532,7 +534,7 @@ def main():
     def kernel_table(x, wb, key="kernels", steps=1):
         """Per kernel class: launches and mean duration (CUDA events), the
         algorithmic bytes or flops per launch and the fraction of the peak.
-        key "kernels": the untimed probed step (every class); "kernels_timed":
+        key "kernels": the untimed probed steps (every class); "kernels_timed":
         the classes probed inside the timed steps."""
         model = kernel_model(x["case"], wb)
         out = {}
@@ -550,7 +552,7 @@ def main():
         return out
     ab = algorithmic_bytes(case, w)
     names = ["predictor", "ibm", "projection", "newton_euler"]
-    ktab = kernel_table(r, w)
+    ktab = kernel_table(r, w, "kernels", r["probe_steps"])
     # the roofline kernel: the dominant class, timed inside the timed steps
     ttab = kernel_table(r, w, "kernels_timed", args.steps)
     dom = max(ttab, key=lambda k: ttab[k]["share_of_step"])
@@ -566,7 +568,7 @@ def main():
                       "mcell_steps_per_s": round(args.gpus * x["ncell"] / (x["ms"] * 1e-3) / 1e6, 1),
                       "phases_ms": {n: round(t, 4) for n, t in zip(names, x["phases"])},
                       "chkdiv_max": x["divmax"], "gpu_launches": int(x["launches"]),
-                      "kernels": kernel_table(x, 8 if f == "plain" else 4),
+                      "kernels": kernel_table(x, 8 if f == "plain" else 4, "kernels", x["probe_steps"]),
                       **({"e2e": x["e2e"]} if x["e2e"] else {}),
                       **({"post1d": x["stats"]} if x["stats"] else {}),
                       **({"learned_forcing": x["learn"]} if x["learn"] else {})} for f, x in res.items()},

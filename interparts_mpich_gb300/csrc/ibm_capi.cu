@@ -180,22 +180,22 @@ int dalloc(ibm_ctx *c, T **ptr, size_t n) {
 }
 
 void free_mlp_batch(MlpTrainBuffers &B) {
-  void *q[] = {B.x, B.t, B.y, B.z1, B.z2, B.h1, B.h2, B.dz1, B.dz2};
+  void *q[] = {B.x, B.t, B.y, B.part, B.err};
   for (void *p : q)
     if (p) cudaFree(p);
-  B.x = nullptr; B.t = B.y = B.z1 = B.z2 = nullptr; B.h1 = B.h2 = B.dz1 = B.dz2 = nullptr;
+  B.x = nullptr; B.t = B.y = B.part = nullptr; B.err = nullptr;
 }
-// training batch buffers for nb rows (rounded up to the 64-row tile)
+// training batch buffers for nb rows: the per-tile gradients, the error
+// flag, and a batch of features, targets and outputs for the test hooks
 int alloc_mlp_batch(ibm_ctx *c, MlpTrainBuffers &B, int nb) {
-  const size_t n = ((size_t)nb + 63) / 64 * 64;
+  const size_t n = ((size_t)nb + 127) / 128 * 128;
   int st;
   if ((st = dalloc(c, &B.x, n * 96))) return st;
   for (float **f : {&B.t, &B.y})
     if ((st = dalloc(c, f, n * 3))) return st;
-  for (float **f : {&B.z1, &B.z2})
-    if ((st = dalloc(c, f, n * 128))) return st;
-  for (__nv_bfloat16 **f : {&B.h1, &B.h2, &B.dz1, &B.dz2})
-    if ((st = dalloc(c, f, n * 128))) return st;
+  if ((st = dalloc(c, &B.part, mlp_part_floats(nb)))) return st;
+  if ((st = dalloc(c, &B.err, 1))) return st;
+  CK(cudaMemsetAsync(B.err, 0, sizeof(int), c->stream));
   return IBM_OK;
 }
 // model buffers (params, moments, gradient, BF16 copies) of a scratch model
@@ -204,12 +204,12 @@ int alloc_mlp_model(ibm_ctx *c, MlpTrainBuffers &B) {
   for (float **f : {&B.params, &B.m, &B.v, &B.grad})
     if ((st = dalloc(c, f, mlp_nparam()))) return st;
   if ((st = dalloc(c, &B.loss, 4))) return st;
-  for (__nv_bfloat16 **f : {&B.w1b, &B.w2b, &B.w2tb})
+  for (__nv_bfloat16 **f : {&B.w1b, &B.w2b})
     if ((st = dalloc(c, f, 128 * 128))) return st;
   return IBM_OK;
 }
 void free_mlp_model(MlpTrainBuffers &B) {
-  void *q[] = {B.params, B.m, B.v, B.grad, B.loss, B.w1b, B.w2b, B.w2tb};
+  void *q[] = {B.params, B.m, B.v, B.grad, B.loss, B.w1b, B.w2b};
   for (void *p : q)
     if (p) cudaFree(p);
 }
@@ -569,7 +569,7 @@ int alloc_all(ibm_ctx *c) {
     for (float **f : {&c->mt.params, &c->mt.m, &c->mt.v, &c->mt.grad})
       if ((st = dalloc(c, f, npar))) return st;
     if ((st = dalloc(c, &c->mt.loss, 4))) return st;
-    for (__nv_bfloat16 **f : {&c->mt.w1b, &c->mt.w2b, &c->mt.w2tb})
+    for (__nv_bfloat16 **f : {&c->mt.w1b, &c->mt.w2b})
       if ((st = dalloc(c, f, 128 * 128))) return st;
     if ((st = dalloc(c, &c->norm, 198))) return st;
     if ((st = dalloc(c, &c->ls, IBM_LS_N))) return st;
@@ -1019,7 +1019,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->cfield, c->cnext, c->crk, c->ferr, c->psize, c->pcount};
   for (void *q : ptrs)
     if (q) cudaFree(q);
-  void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b, c->mt.w2tb,
+  void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b,
                    c->norm, c->ls, c->gate, c->ly, c->hv.feat, c->hv.pidx, c->hv.targ,
                    c->hv.count, c->tx, c->tt};
   for (void *q : lptrs)
@@ -1913,7 +1913,7 @@ int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsign
     CK(cudaMemcpy(c->mt.params, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
     CK(cudaMemsetAsync(c->mt.m, 0, w.size() * sizeof(float), c->stream));
     CK(cudaMemsetAsync(c->mt.v, 0, w.size() * sizeof(float), c->stream));
-    launch_mlp_refresh(c->stream, c->mt.params, c->mt.w1b, c->mt.w2b, c->mt.w2tb);
+    launch_mlp_refresh(c->stream, c->mt.params, c->mt.w1b, c->mt.w2b);
     LAUNCHED(1);
     c->train_step = 0;
     c->stats_ready = true;
@@ -1940,13 +1940,15 @@ int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsign
   }
   for (int q = 0; q < nsteps; ++q) {
     ++c->train_step;
-    launch_mlp_gather(c->stream, n, c->tx, c->tt, batch, seed, c->train_step, c->mt.x, c->mt.t);
-    launch_mlp_train_step(c->stream, c->mt, batch, c->train_step, (float)lr);
-    LAUNCHED(8);
+    c->launches += launch_mlp_train_step(c->stream, c->mt, c->tx, c->tt, n, batch, seed, 1, c->train_step, (float)lr,
+                                         1, nullptr);
   }
   float l = 0.f;
+  int herr = 0;
   CK(cudaMemcpyAsync(&l, c->mt.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(&herr, c->mt.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (herr) return set_err(c, IBM_E_NOT_CONVERGED, "tensor-core MMA wait timed out in training");
   if (loss) *loss = l;
   c->model_ready = true;
   c->learn_on = true;
@@ -1960,7 +1962,7 @@ int ibm_set_forcing_model(ibm_ctx *c, const float *params, const float *norm) {
   CK(cudaMemcpyAsync(c->norm, norm, 198 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->mt.m, 0, mlp_nparam() * sizeof(float), c->stream));
   CK(cudaMemsetAsync(c->mt.v, 0, mlp_nparam() * sizeof(float), c->stream));
-  launch_mlp_refresh(c->stream, c->mt.params, c->mt.w1b, c->mt.w2b, c->mt.w2tb);
+  launch_mlp_refresh(c->stream, c->mt.params, c->mt.w1b, c->mt.w2b);
   LAUNCHED(1);
   CK(cudaStreamSynchronize(c->stream));
   c->train_step = 0;
@@ -2055,7 +2057,7 @@ static int mlp_scratch(ibm_ctx *c, const float *params, const float *x, const fl
   CK(cudaMemcpyAsync(xf, x, (size_t)nb * 96 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   launch_f2bf(c->stream, (long)nb * 96, xf, B.x);
   CK(cudaMemcpyAsync(B.t, t, (size_t)nb * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  launch_mlp_refresh(c->stream, B.params, B.w1b, B.w2b, B.w2tb);
+  launch_mlp_refresh(c->stream, B.params, B.w1b, B.w2b);
   LAUNCHED(2);
   CK(cudaStreamSynchronize(c->stream));
   cudaFree(xf);
@@ -2068,16 +2070,18 @@ int ibm_mlp_gradient(ibm_ctx *c, const float *params, const float *x, const floa
   MlpTrainBuffers B{};
   int st = mlp_scratch(c, params, x, t, nb, B);
   if (st == IBM_OK) {
-    launch_mlp_grad(c->stream, B, nb);
-    c->launches += 5;
+    c->launches += launch_mlp_train_step(c->stream, B, B.x, B.t, nb, nb, 0u, 0, 1, 0.f, 0, B.y);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && grad)
       e = cudaMemcpyAsync(grad, B.grad, mlp_nparam() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, B.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && y)
       e = cudaMemcpyAsync(y, B.y, (size_t)nb * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     st = cuda_err(c, e, "ibm_mlp_gradient");
+    if (st == IBM_OK && herr) st = set_err(c, IBM_E_NOT_CONVERGED, "tensor-core MMA wait timed out");
   }
   cudaStreamSynchronize(c->stream);
   free_mlp_batch(B);
@@ -2137,15 +2141,17 @@ int ibm_mlp_fit(ibm_ctx *c, const float *params_in, const float *x, const float 
   int st = mlp_scratch(c, params_in, x, t, nb, B);
   cudaError_t e = cudaSuccess;
   for (int q = 0; st == IBM_OK && e == cudaSuccess && q < nsteps; ++q) {
-    launch_mlp_train_step(c->stream, B, nb, q + 1, (float)lr);
-    c->launches += 6;
+    c->launches += launch_mlp_train_step(c->stream, B, B.x, B.t, nb, nb, 0u, 0, q + 1, (float)lr, 1, nullptr);
     e = cudaGetLastError();
     if (e == cudaSuccess && losses) e = cudaMemcpyAsync(losses + q, B.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
   }
   if (st == IBM_OK && e == cudaSuccess && params_out)
     e = cudaMemcpyAsync(params_out, B.params, mlp_nparam() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  int herr = 0;
+  if (st == IBM_OK && e == cudaSuccess) e = cudaMemcpyAsync(&herr, B.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (st == IBM_OK && e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (st == IBM_OK) st = cuda_err(c, e, "ibm_mlp_fit");
+  if (st == IBM_OK && herr) st = set_err(c, IBM_E_NOT_CONVERGED, "tensor-core MMA wait timed out");
   cudaStreamSynchronize(c->stream);
   free_mlp_batch(B);
   free_mlp_model(B);

@@ -153,20 +153,18 @@ void launch_normal_fill(cudaStream_t s, float *y, long n, unsigned seed, unsigne
 
 // mlp_kernels.cu (learned forcing model)
 struct MlpTrainBuffers {
-  float *params, *m, *v, *grad, *loss;       // FP32 masters, Adam moments, gradient, loss accumulator
-  __nv_bfloat16 *w1b, *w2b, *w2tb;           // BF16 copies of W1, W2 and W2 transposed
-  __nv_bfloat16 *x;                           // [nb][96] batch features
-  float *t, *y, *z1, *z2;                     // targets [nb][3], outputs, pre-activations [nb][128]
-  __nv_bfloat16 *h1, *h2, *dz1, *dz2;         // [nb][128]
+  float *params, *m, *v, *grad, *loss;       // FP32 masters, Adam moments, gradient, loss
+  __nv_bfloat16 *w1b, *w2b;                  // BF16 copies of W1, W2
+  __nv_bfloat16 *x;                           // [nb][96] batch features (test hooks)
+  float *t, *y;                               // targets, outputs [nb][3] (test hooks)
+  float *part;                                // per-tile gradients and losses [mlp_part_floats(nb)]
+  int *err;                                   // MMA wait timed out
 };
 int mlp_nparam();
+size_t mlp_part_floats(int nb);
 int ibm_set_smem_limits(int box_cap);
 int mlp_set_smem_limits();
-void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
-                        const __nv_bfloat16 *w2b, const float *params, float *y, float *z1, float *z2,
-                        __nv_bfloat16 *h1, __nv_bfloat16 *h2, int train);
-void launch_mlp_refresh(cudaStream_t s, const float *params, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b,
-                        __nv_bfloat16 *w2tb);
+void launch_mlp_refresh(cudaStream_t s, const float *params, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b);
 void launch_mlp_infer(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
                       const __nv_bfloat16 *w2b, const float *params, float *y);
 int launch_mlp_infer_tc(cudaStream_t s, const __nv_bfloat16 *x, int n, const __nv_bfloat16 *w1b,
@@ -195,12 +193,13 @@ struct FeatIn {
 };
 int launch_mlp_features_tc(cudaStream_t s, const FeatIn &fi, const __nv_bfloat16 *w1b, const float *params,
                            float *y, int *err);
-void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr);
-void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb);
+// one Adam step (adam = 1) or the gradient alone on nb rows drawn from X, T
+// (n rows) by the (seed, step, row) hash (gather = 1) or rows 0..nb-1;
+// outputs to y when not null.  Returns the launches.
+int launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, const __nv_bfloat16 *X, const float *T, int n,
+                          int nb, unsigned seed, int gather, int step, float lr, int adam, float *y);
 void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,
                       const float *tmu, const float *tsig, __nv_bfloat16 *X, float *T);
-void launch_mlp_gather(cudaStream_t s, int n, const __nv_bfloat16 *X, const float *T, int nb, unsigned seed, int step,
-                       __nv_bfloat16 *bx, float *bt);
 void launch_f2bf(cudaStream_t s, long n, const float *a, __nv_bfloat16 *b);
 
 // particle_kernels.cu

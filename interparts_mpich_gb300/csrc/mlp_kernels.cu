@@ -6,11 +6,12 @@
 // velocity-unit correction that the plain passes 1 and 2 would add
 // (interp_spread.f90 / forcing.f90, Nl = 3).
 //
-// Layers 1 and 2 run on the tensor cores: mma.sync m16n8k16 with BF16
-// operands (features, weights, hidden activations) and FP32 accumulators;
-// layer 3 (128 -> 3) and GELU run on the FP32 pipes.  Training (forward,
-// backward, weight gradients, Adam) uses the same fragments; the FP32 master
-// weights live on the device and BF16 copies are refreshed after each step.
+// Training (forward, backward, weight gradients) runs on the tcgen05 tensor
+// cores with TMEM accumulators, one CTA per 128-row tile of the batch, and a
+// second kernel sums the tiles' gradients and applies Adam to the FP32
+// master weights and their BF16 copies.  Inference in the learned loop is
+// the tcgen05 kernel fused with the feature formation; an mma.sync m16n8k16
+// inference kernel with the training's rounding points is kept as a check.
 //
 // Parameter vector (FP32): W1[128][96], b1[128], W2[128][128], b2[128],
 // W3[3][128], b3[3].
@@ -89,144 +90,8 @@ __device__ __forceinline__ float gelu_grad_f(float z) {
 
 constexpr int NIN = 96, NH = 128, NOUT = 3;
 constexpr int LDX = NIN + 8, LDH = NH + 8;  // padded shared-memory rows
-constexpr int TILE = 64;                    // rows per CTA tile (4 warps x 16)
 constexpr int OFF_B1 = NH * NIN, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
               OFF_B3 = OFF_W3 + NOUT * NH, NPARAM = OFF_B3 + NOUT;
-
-// ---------------------------------------------------------------------------
-// Forward: X (N x 96, bf16) -> Y (N x 3, fp32).  Persistent CTAs keep W1, W2
-// in shared memory.  TRAIN additionally stores Z1, Z2 (fp32) and H1, H2
-// (bf16) for the backward pass.
-// ---------------------------------------------------------------------------
-struct MlpFwdArgs {
-  const bf16 *x;
-  int n;
-  const bf16 *w1b, *w2b;
-  const float *params;
-  float *y;
-  float *z1, *z2;
-  bf16 *h1, *h2;
-};
-
-template <bool TRAIN>
-__global__ void __launch_bounds__(128) k_mlp_forward(MlpFwdArgs A) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  bf16 *W1s = reinterpret_cast<bf16 *>(sm);   // [128][LDX]
-  bf16 *W2s = W1s + NH * LDX;                 // [128][LDH]
-  bf16 *Xs = W2s + NH * LDH;                  // [64][LDX]
-  bf16 *H1s = Xs + TILE * LDX;                // [64][LDH]
-  bf16 *H2s = H1s + TILE * LDH;               // [64][LDH]
-  float *bias = reinterpret_cast<float *>(H2s + TILE * LDH);  // b1, b2, W3, b3
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int t = tid; t < NH * NIN; t += blockDim.x) W1s[(t / NIN) * LDX + t % NIN] = A.w1b[t];
-  for (int t = tid; t < NH * NH; t += blockDim.x) W2s[(t / NH) * LDH + t % NH] = A.w2b[t];
-  for (int t = tid; t < NH; t += blockDim.x) { bias[t] = A.params[OFF_B1 + t]; bias[NH + t] = A.params[OFF_B2 + t]; }
-  for (int t = tid; t < NOUT * NH + NOUT; t += blockDim.x) bias[2 * NH + t] = A.params[OFF_W3 + t];
-  __syncthreads();
-  const float *b1 = bias, *b2 = bias + NH, *w3 = bias + 2 * NH, *b3 = w3 + NOUT * NH;
-  const int ntiles = (A.n + TILE - 1) / TILE;
-  const int g = lane >> 2, tq = lane & 3;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int row0 = tile * TILE;
-    // stage the feature tile (rows beyond n are zero)
-    for (int t = tid; t < TILE * NIN / 8; t += blockDim.x) {
-      const int r = t / (NIN / 8), c8 = (t % (NIN / 8)) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (row0 + r < A.n) v = *reinterpret_cast<const uint4 *>(&A.x[(long)(row0 + r) * NIN + c8]);
-      *reinterpret_cast<uint4 *>(&Xs[r * LDX + c8]) = v;
-    }
-    __syncthreads();
-    const int m0 = warp * 16;
-    // layer 1: 16 rows x 128 columns per warp
-    float acc[16][4];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-#pragma unroll
-    for (int k0 = 0; k0 < NIN; k0 += 16) {
-      uint32_t a[4];
-      load_a(a, Xs, LDX, m0, k0, lane);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        uint32_t b[2];
-        load_b(b, W1s, LDX, j * 8, k0, lane);
-        mma16816(acc[j], a, b);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const int col = j * 8 + 2 * tq;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int r = m0 + g + 8 * h;
-        const float z0 = acc[j][2 * h] + b1[col], z1 = acc[j][2 * h + 1] + b1[col + 1];
-        const bf16 h0 = __float2bfloat16(gelu_f(z0)), h1v = __float2bfloat16(gelu_f(z1));
-        H1s[r * LDH + col] = h0;
-        H1s[r * LDH + col + 1] = h1v;
-        if (TRAIN && row0 + r < A.n) {
-          const long o = (long)(row0 + r) * NH + col;
-          A.z1[o] = z0; A.z1[o + 1] = z1;
-          A.h1[o] = h0; A.h1[o + 1] = h1v;
-        }
-      }
-    }
-    __syncwarp();
-    // layer 2 (each warp reads only its own 16 rows of H1)
-#pragma unroll
-    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-#pragma unroll
-    for (int k0 = 0; k0 < NH; k0 += 16) {
-      uint32_t a[4];
-      load_a(a, H1s, LDH, m0, k0, lane);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        uint32_t b[2];
-        load_b(b, W2s, LDH, j * 8, k0, lane);
-        mma16816(acc[j], a, b);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const int col = j * 8 + 2 * tq;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int r = m0 + g + 8 * h;
-        const float z0 = acc[j][2 * h] + b2[col], z1 = acc[j][2 * h + 1] + b2[col + 1];
-        const bf16 h0 = __float2bfloat16(gelu_f(z0)), h1v = __float2bfloat16(gelu_f(z1));
-        H2s[r * LDH + col] = h0;
-        H2s[r * LDH + col + 1] = h1v;
-        if (TRAIN && row0 + r < A.n) {
-          const long o = (long)(row0 + r) * NH + col;
-          A.z2[o] = z0; A.z2[o + 1] = z1;
-          A.h2[o] = h0; A.h2[o + 1] = h1v;
-        }
-      }
-    }
-    __syncwarp();
-    // layer 3 on the FP32 pipes: 16 rows x 3 outputs per warp
-    for (int q = lane; q < 16 * NOUT; q += 32) {
-      const int r = m0 + q / NOUT, o = q % NOUT;
-      float s = b3[o];
-      for (int c = 0; c < NH; ++c) s += __bfloat162float(H2s[r * LDH + c]) * w3[o * NH + c];
-      if (row0 + r < A.n) A.y[(long)(row0 + r) * NOUT + o] = s;
-    }
-    __syncthreads();
-  }
-}
-
-size_t mlp_forward_smem() {
-  return (size_t)(NH * LDX + NH * LDH + TILE * LDX + 2 * TILE * LDH) * sizeof(bf16) +
-         (size_t)(2 * NH + NOUT * NH + NOUT) * sizeof(float);
-}
-
-void launch_mlp_forward(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, const bf16 *w2b, const float *params,
-                        float *y, float *z1, float *z2, bf16 *h1, bf16 *h2, int train) {
-  if (n <= 0) return;
-  MlpFwdArgs A{x, n, w1b, w2b, params, y, z1, z2, h1, h2};
-  const int ntiles = (n + TILE - 1) / TILE;
-  const int grid = ntiles < 2 * 152 ? ntiles : 2 * 152;
-  if (train) k_mlp_forward<true><<<grid, 128, mlp_forward_smem(), s>>>(A);
-  else k_mlp_forward<false><<<grid, 128, mlp_forward_smem(), s>>>(A);
-}
 
 // ---------------------------------------------------------------------------
 // Inference: X (N x 96, bf16) -> Y (N x 3, fp32), one warp per 16-row tile.
@@ -235,8 +100,8 @@ void launch_mlp_forward(cudaStream_t s, const bf16 *x, int n, const bf16 *w1b, c
 // A fragment of the 16-column k-block m (rows g, g+8; columns 2t, 2t+1 and
 // 2t+8, 2t+9).  Layer 3 is a per-lane partial dot product over the 32
 // columns a lane holds, summed over the 4 lanes of a row pair by shuffles.
-// Same rounding points as the training forward: BF16 inputs, weights of
-// layers 1-2 and hidden activations; FP32 accumulation; FP32 W3.
+// Same rounding points as the training's forward pass: BF16 inputs, weights
+// of layers 1-2 and hidden activations; FP32 accumulation; FP32 W3.
 // ---------------------------------------------------------------------------
 constexpr int IW = 12;  // warps per CTA (163 registers: one CTA per SM)
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
@@ -763,237 +628,460 @@ int launch_mlp_features_tc(cudaStream_t s, const FeatIn &fi, const bf16 *w1b, co
 }
 
 // ---------------------------------------------------------------------------
-// Backward through layer 3, GELU and layer 2 for a batch: dY = 2(Y-T)/B;
-// dH2 = dY W3; dZ2 = dH2 * gelu'(Z2) (bf16); dH1 = dZ2 W2 (tensor cores);
-// dZ1 = dH1 * gelu'(Z1) (bf16).  Bias and W3 gradients accumulate into grad.
+// Training on the 5th-generation tensor cores (tcgen05): one CTA per 128-row
+// tile of the batch runs the forward pass, the backward pass and the tile's
+// weight gradients; a second kernel sums the tiles' gradients in a fixed
+// order and applies Adam.  Rounding points as the CPU reference of the model
+// states them: BF16 features, W1, W2, hidden activations and back-propagated
+// pre-activation gradients; FP32 accumulation (TMEM); FP32 layer 3.
+//
+// Every operand is one shared-memory tile of 8x8 core matrices (8 rows of 16
+// bytes, row groups `sbo` bytes apart, column groups 128 bytes apart), and
+// the same tile serves as a K-major operand (rows = M or N) and, through a
+// second descriptor, as an MN-major one (rows = K): the forward products
+// read X, H1 and W1, W2 K-major; dH1 = dZ2 W2 reads W2 MN-major; the weight
+// gradients, whose K is the tile's 128 rows, read dZ2, dZ1, H1, H2, X and dY
+// MN-major.  A column of ones appended to X and to H1 turns the bias
+// gradients of layers 1 and 2 into one more output column of dW1 and dW2.
+// dY enters the layer-3 weight gradient as a BF16 pair (hi + lo), so that
+// product keeps about 16 significant bits of dY.
+//
+// TMEM (512 columns): Z1 [0,128) -> dW1|db1 [0,112) once Z1 is dead;
+// Z2 [128,256) -> dH1 [128,256); dW2|db2 [256,400); dW3^T (hi, lo) [400,416).
+// Every wait is bounded: on a timeout the CTA records err[0] and stops
+// issuing, waits (bounded) for its MMA in flight and frees its TMEM.
 // ---------------------------------------------------------------------------
-struct MlpBwdArgs {
-  int nb;
-  const float *y, *t, *z1, *z2;
-  const bf16 *h2;
-  const bf16 *w2tb;  // W2 transposed: [in][out]
+__device__ __forceinline__ unsigned mix32(unsigned x) {
+  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+  return x;
+}
+// byte offset of element (row, col) of a core-matrix tile with row groups
+// sbo bytes apart
+__host__ __device__ constexpr uint32_t cm_off(int row, int col, uint32_t sbo) {
+  return (uint32_t)((row >> 3) * sbo + (col >> 3) * 128 + (row & 7) * 16 + (col & 7) * 2);
+}
+// kind::f16 instruction descriptor: BF16 A and B, FP32 D; amn / bmn: the
+// operand is MN-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, int amn, int bmn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)amn << 15) | ((uint32_t)bmn << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// MN-major no-swizzle descriptor: K groups (8 rows of the tile) kstride
+// bytes apart (leading byte offset), MN groups 128 bytes apart (stride
+// byte offset)
+__device__ __forceinline__ uint64_t mn_desc(uint32_t saddr, uint32_t kstride) { return umma_desc(saddr, kstride, 128); }
+
+constexpr int TT_THREADS = 256;
+constexpr int TT_XK = NIN + 16;   // X, a column of ones, zeros
+constexpr int TT_HK = NH + 16;    // H1, a column of ones, zeros
+constexpr int TT_DYN = 16;        // dY hi (columns 0..2), lo (3..5), zeros
+constexpr uint32_t TT_SB_X = TT_XK / 8 * 128, TT_SB_H1 = TT_HK / 8 * 128, TT_SB_H = NH / 8 * 128,
+                   TT_SB_W1 = NIN / 8 * 128, TT_SB_DY = TT_DYN / 8 * 128;
+constexpr size_t TT_OW1 = 0, TT_OW2 = TT_OW1 + NH * NIN * 2, TT_OX = TT_OW2 + NH * NH * 2,
+                 TT_OH1 = TT_OX + 128 * TT_XK * 2, TT_OH2 = TT_OH1 + 128 * TT_HK * 2, TT_OD2 = TT_OH2 + 128 * NH * 2,
+                 TT_ODY = TT_OD2 + 128 * NH * 2, TT_OF = TT_ODY + 128 * TT_DYN * 2;
+// FP32 constants: b1, b2, W3, b3, the two column halves' layer-3 partials,
+// per-warp sums of dY and the squared error
+constexpr int TF_B1 = 0, TF_B2 = NH, TF_W3 = 2 * NH, TF_B3 = TF_W3 + NOUT * NH, TF_YP = TF_B3 + 4,
+              TF_RED = TF_YP + 2 * 128 * 4, TF_N = TF_RED + 4 * 4;
+// The CTA takes the whole 227 KB (it holds all 512 TMEM columns, one CTA per
+// SM in any case): every descriptor's reach, with its two byte offsets read
+// either way round, stays inside the allocation.
+constexpr size_t TT_OBAR = TT_OF + TF_N * 4, TT_SMEM = 227 * 1024;
+constexpr int TT_PSTRIDE = (NPARAM + 1 + 3) / 4 * 4;  // a tile's gradient, then its loss
+static_assert(TT_OBAR % 8 == 0 && TT_OBAR + 32 <= TT_SMEM, "training kernel shared memory");
+static_assert(TT_OD2 + 7 * 2 * TT_SB_H + 128 + 15 * TT_SB_H + 127 < TT_SMEM &&
+                  TT_OH1 + 7 * 2 * TT_SB_H1 + 128 + 17 * TT_SB_H1 + 127 < TT_SMEM,
+              "MN-major operand reach");
+constexpr uint32_t ID_L1 = idesc_bf16(128, NH, 0, 0), ID_L2 = idesc_bf16(128, NH, 0, 0),
+                   ID_DH1 = idesc_bf16(128, NH, 0, 1), ID_DW2 = idesc_bf16(128, TT_HK, 1, 1),
+                   ID_DW3 = idesc_bf16(128, TT_DYN, 1, 1), ID_DW1 = idesc_bf16(128, TT_XK, 1, 1);
+
+struct MlpTrainArgs {
+  const bf16 *X;    // [n][96] standardised features
+  const float *T;   // [n][3] standardised targets
+  int n, nb, gather;
+  unsigned seed;
+  int step;
+  const bf16 *w1b, *w2b;
   const float *params;
-  bf16 *dz1, *dz2;
-  float *grad;
-  float *loss;
+  float *part;      // [tiles][TT_PSTRIDE]
+  float *y;         // outputs [nb][3] or null
+  int *err;
 };
+// row `row` of the batch: drawn with replacement by a counter-based hash of
+// (seed, step, row), or the row itself
+__device__ __forceinline__ int train_src(const MlpTrainArgs &A, int row) {
+  if (!A.gather) return row;
+  const unsigned h = mix32(A.seed ^ mix32((unsigned)A.step * 0x9E3779B9U + (unsigned)row));
+  return (int)(h % (unsigned)A.n);
+}
+__device__ __forceinline__ uint32_t bf2_bits(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+__device__ __forceinline__ void st4f(float *p, const float *v) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
 
-__global__ void __launch_bounds__(128) k_mlp_backward(MlpBwdArgs A) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  bf16 *W2t = reinterpret_cast<bf16 *>(sm);  // [128][LDH]: W2t[i][o]
-  bf16 *D2 = W2t + NH * LDH;                 // [64][LDH] dZ2 tile
-  float *w3 = reinterpret_cast<float *>(D2 + TILE * LDH);  // [3][128]
-  float *dy = w3 + NOUT * NH;                              // [64][3]
-  float *red = dy + TILE * NOUT;                           // [128] bias-gradient partials
+__global__ void __launch_bounds__(TT_THREADS, 1) k_mlp_train_tc(const MlpTrainArgs A) {
+  extern __shared__ __align__(16) unsigned char tt_sm[];
+  unsigned char *W1s = tt_sm + TT_OW1, *W2s = tt_sm + TT_OW2, *Xs = tt_sm + TT_OX, *H1s = tt_sm + TT_OH1,
+                *H2s = tt_sm + TT_OH2, *D2s = tt_sm + TT_OD2, *DYs = tt_sm + TT_ODY;
+  float *fs = reinterpret_cast<float *>(tt_sm + TT_OF);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(tt_sm + TT_OBAR);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  int *bad = reinterpret_cast<int *>(tslot + 1);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int t = tid; t < NH * NH; t += blockDim.x) W2t[(t / NH) * LDH + t % NH] = A.w2tb[t];
-  for (int t = tid; t < NOUT * NH; t += blockDim.x) w3[t] = A.params[OFF_W3 + t];
-  const int row0 = blockIdx.x * TILE;
-  const float inv = 2.f / (float)A.nb;
-  float lsum = 0.f;
-  for (int q = tid; q < TILE * NOUT; q += blockDim.x) {
-    const int r = q / NOUT, o = q % NOUT;
-    float d = 0.f;
-    if (row0 + r < A.nb) {
-      const float e = A.y[(long)(row0 + r) * NOUT + o] - A.t[(long)(row0 + r) * NOUT + o];
-      d = inv * e;
-      lsum += e * e;
+  const int row0 = blockIdx.x * 128;
+  // the tile's rows of X (16-byte asynchronous copies; zero rows beyond nb),
+  // the ones column, W1 and W2 (BF16), the FP32 constants
+  for (int q = tid; q < 128 * (NIN / 8); q += TT_THREADS) {
+    const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+    const bool valid = row0 + r < A.nb;
+    cp_async16(Xs + cm_off(r, c8, TT_SB_X), valid ? A.X + (long)train_src(A, row0 + r) * NIN + c8 : A.X, valid);
+  }
+  for (int q = tid; q < 128 * 2; q += TT_THREADS) {
+    const int r = q >> 1, c8 = NIN + (q & 1) * 8;
+    const uint32_t one = (c8 == NIN && row0 + r < A.nb) ? 0x3F80u : 0u;  // BF16 1.0 in column 96
+    *reinterpret_cast<uint4 *>(Xs + cm_off(r, c8, TT_SB_X)) = make_uint4(one, 0u, 0u, 0u);
+  }
+  for (int q = tid; q < NH * NIN / 8; q += TT_THREADS) {
+    const int r = q / (NIN / 8), c8 = (q % (NIN / 8)) * 8;
+    cp_async16(W1s + cm_off(r, c8, TT_SB_W1), A.w1b + r * NIN + c8, true);
+  }
+  for (int q = tid; q < NH * NH / 8; q += TT_THREADS) {
+    const int r = q / (NH / 8), c8 = (q % (NH / 8)) * 8;
+    cp_async16(W2s + cm_off(r, c8, TT_SB_H), A.w2b + r * NH + c8, true);
+  }
+  for (int q = tid; q < NH; q += TT_THREADS) {
+    fs[TF_B1 + q] = A.params[OFF_B1 + q];
+    fs[TF_B2 + q] = A.params[OFF_B2 + q];
+  }
+  for (int q = tid; q < NOUT * NH; q += TT_THREADS) fs[TF_W3 + q] = A.params[OFF_W3 + q];
+  if (tid < NOUT) fs[TF_B3 + tid] = A.params[OFF_B3 + tid];
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+    *bad = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t T0 = *tslot;
+  const int q4 = warp & 3, hf = warp >> 2;  // TMEM lane quarter, column half
+  const int r = q4 * 32 + lane;              // this thread's row of the tile (its TMEM lane)
+  const uint32_t lb = (uint32_t)(q4 * 32) << 16;
+  const bool valid = row0 + r < A.nb;
+  const uint32_t xs = smem_u32(Xs), w1 = smem_u32(W1s), w2 = smem_u32(W2s), h1 = smem_u32(H1s), h2 = smem_u32(H2s),
+                 d2 = smem_u32(D2s), dys = smem_u32(DYs);
+  const long LIMIT = 1L << 22;
+  uint32_t phase = 0;
+  // all threads wait (bounded) for the committed MMAs, then decide together
+  auto mma_wait = [&]() -> bool {
+    if (!mbar_wait(bar, phase, LIMIT)) {
+      if (A.err) atomicExch(A.err, 1);
+      *bad = 1;
     }
-    dy[q] = d;
+    phase ^= 1u;
+    tc_fence_after();
+    __syncthreads();
+    return *bad == 0;
+  };
+  auto issued = [&]() {  // operands written by the threads, visible to the tensor cores
+    tc_fence_before();
+    fence_async_smem();
+    __syncthreads();
+  };
+
+  // ---- layer 1: Z1 = X W1^T -> TMEM [0,128)
+  if (tid == 0) {
+    tc_fence_after();
+#pragma unroll
+    for (int kk = 0; kk < NIN / 16; ++kk)
+      umma_f16(T0, umma_desc(xs + kk * 256, 128, TT_SB_X), umma_desc(w1 + kk * 256, 128, TT_SB_W1), ID_L1, kk > 0);
+    umma_commit(bar);
+  }
+  bool ok = mma_wait();
+  // H1 = bf16(gelu(Z1 + b1)), and the ones column
+  if (ok) {
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+      const int col = hf * 64 + cc * 32;
+      float v[32];
+      tmem_ld32(T0 + lb + col, v);
+#pragma unroll
+      for (int c8 = 0; c8 < 32; c8 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int c = col + c8 + 2 * e;
+          pk[e] = bf2_bits(gelu_f(v[c8 + 2 * e] + fs[TF_B1 + c]), gelu_f(v[c8 + 2 * e + 1] + fs[TF_B1 + c + 1]));
+        }
+        *reinterpret_cast<uint4 *>(H1s + cm_off(r, col + c8, TT_SB_H1)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    if (hf == 1) {
+      *reinterpret_cast<uint4 *>(H1s + cm_off(r, NH, TT_SB_H1)) = make_uint4(valid ? 0x3F80u : 0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4 *>(H1s + cm_off(r, NH + 8, TT_SB_H1)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+  issued();
+  // ---- layer 2: Z2 = H1 W2^T -> TMEM [128,256)
+  if (ok && tid == 0) {
+    tc_fence_after();
+#pragma unroll
+    for (int kk = 0; kk < NH / 16; ++kk)
+      umma_f16(T0 + 128, umma_desc(h1 + kk * 256, 128, TT_SB_H1), umma_desc(w2 + kk * 256, 128, TT_SB_H), ID_L2,
+               kk > 0);
+    umma_commit(bar);
+  }
+  if (ok) ok = mma_wait();
+  // H2 = bf16(gelu(Z2 + b2)); layer 3 on the FP32 pipes (each column half
+  // a partial dot product)
+  if (ok) {
+    float yp[NOUT] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+      const int col = hf * 64 + cc * 32;
+      float v[32];
+      tmem_ld32(T0 + 128 + lb + col, v);
+#pragma unroll
+      for (int c8 = 0; c8 < 32; c8 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int c = col + c8 + 2 * e;
+          const __nv_bfloat162 hb =
+              __floats2bfloat162_rn(gelu_f(v[c8 + 2 * e] + fs[TF_B2 + c]), gelu_f(v[c8 + 2 * e + 1] + fs[TF_B2 + c + 1]));
+          const float ha = __low2float(hb), hc = __high2float(hb);
+#pragma unroll
+          for (int o = 0; o < NOUT; ++o) yp[o] += ha * fs[TF_W3 + o * NH + c] + hc * fs[TF_W3 + o * NH + c + 1];
+          pk[e] = *reinterpret_cast<const uint32_t *>(&hb);
+        }
+        *reinterpret_cast<uint4 *>(H2s + cm_off(r, col + c8, TT_SB_H)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < NOUT; ++o) fs[TF_YP + (hf * 128 + r) * 4 + o] = yp[o];
   }
   __syncthreads();
-  // loss, W3 and b3 gradients
-  for (int q = tid; q < NOUT * NH + NOUT; q += blockDim.x) {
-    float s = 0.f;
-    if (q < NOUT * NH) {
-      const int o = q / NH, c = q % NH;
-      for (int r = 0; r < TILE && row0 + r < A.nb; ++r)
-        s += dy[r * NOUT + o] * __bfloat162float(A.h2[(long)(row0 + r) * NH + c]);
-      atomicAdd(&A.grad[OFF_W3 + q], s);
+  if (ok) {
+    // Y, dY = 2 (Y - T) / nb (zero beyond nb), the loss
+    float dy[NOUT], e[NOUT];
+    const long src = valid ? train_src(A, row0 + r) : 0;
+#pragma unroll
+    for (int o = 0; o < NOUT; ++o) {
+      const float yv = (fs[TF_YP + r * 4 + o] + fs[TF_YP + (128 + r) * 4 + o]) + fs[TF_B3 + o];
+      e[o] = valid ? yv - A.T[src * NOUT + o] : 0.f;
+      dy[o] = (2.f / (float)A.nb) * e[o];
+      if (hf == 0 && valid && A.y) A.y[(long)(row0 + r) * NOUT + o] = yv;
+    }
+    if (hf == 0) {
+      float hi[NOUT], lo[NOUT];
+#pragma unroll
+      for (int o = 0; o < NOUT; ++o) {
+        hi[o] = __bfloat162float(__float2bfloat16(dy[o]));
+        lo[o] = dy[o] - hi[o];
+      }
+      *reinterpret_cast<uint4 *>(DYs + cm_off(r, 0, TT_SB_DY)) =
+          make_uint4(bf2_bits(hi[0], hi[1]), bf2_bits(hi[2], lo[0]), bf2_bits(lo[1], lo[2]), 0u);
+      *reinterpret_cast<uint4 *>(DYs + cm_off(r, 8, TT_SB_DY)) = make_uint4(0u, 0u, 0u, 0u);
+      float s[4] = {dy[0], dy[1], dy[2], (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) / (float)A.nb};
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        for (int d = 16; d > 0; d >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], d);
+      if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) fs[TF_RED + q4 * 4 + k] = s[k];
+    }
+    // dZ2 = bf16((dY W3) gelu'(Z2 + b2)), Z2 read again
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+      const int col = hf * 64 + cc * 32;
+      float v[32];
+      tmem_ld32(T0 + 128 + lb + col, v);
+#pragma unroll
+      for (int c8 = 0; c8 < 32; c8 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int ee = 0; ee < 4; ++ee) {
+          float d[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int c = col + c8 + 2 * ee + u;
+            const float dh = dy[0] * fs[TF_W3 + c] + dy[1] * fs[TF_W3 + NH + c] + dy[2] * fs[TF_W3 + 2 * NH + c];
+            d[u] = dh * gelu_grad_f(v[c8 + 2 * ee + u] + fs[TF_B2 + c]);
+          }
+          pk[ee] = bf2_bits(d[0], d[1]);
+        }
+        *reinterpret_cast<uint4 *>(D2s + cm_off(r, col + c8, TT_SB_H)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+  }
+  issued();
+  // ---- dH1 = dZ2 W2 -> [128,256); [dW2 | db2] = dZ2^T [H1 | 1] -> [256,400);
+  //      dW3^T (hi, lo) = H2^T [dY hi | dY lo] -> [400,416)
+  if (ok && tid == 0) {
+    tc_fence_after();
+#pragma unroll
+    for (int kk = 0; kk < NH / 16; ++kk)
+      umma_f16(T0 + 128, umma_desc(d2 + kk * 256, 128, TT_SB_H), mn_desc(w2 + kk * 2 * TT_SB_H, TT_SB_H), ID_DH1,
+               kk > 0);
+#pragma unroll
+    for (int kk = 0; kk < 128 / 16; ++kk)
+      umma_f16(T0 + 256, mn_desc(d2 + kk * 2 * TT_SB_H, TT_SB_H), mn_desc(h1 + kk * 2 * TT_SB_H1, TT_SB_H1), ID_DW2,
+               kk > 0);
+#pragma unroll
+    for (int kk = 0; kk < 128 / 16; ++kk)
+      umma_f16(T0 + 400, mn_desc(h2 + kk * 2 * TT_SB_H, TT_SB_H), mn_desc(dys + kk * 2 * TT_SB_DY, TT_SB_DY), ID_DW3,
+               kk > 0);
+    umma_commit(bar);
+  }
+  if (ok) ok = mma_wait();
+  // dZ1 = bf16(dH1 gelu'(Z1 + b1)) into H2's tile (read by the completed MMAs)
+  if (ok) {
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+      const int col = hf * 64 + cc * 32;
+      float dh[32], z[32];
+      tmem_ld32(T0 + 128 + lb + col, dh);
+      tmem_ld32(T0 + lb + col, z);
+#pragma unroll
+      for (int c8 = 0; c8 < 32; c8 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int ee = 0; ee < 4; ++ee) {
+          const int c = col + c8 + 2 * ee, j = c8 + 2 * ee;
+          pk[ee] = bf2_bits(dh[j] * gelu_grad_f(z[j] + fs[TF_B1 + c]), dh[j + 1] * gelu_grad_f(z[j + 1] + fs[TF_B1 + c + 1]));
+        }
+        *reinterpret_cast<uint4 *>(H2s + cm_off(r, col + c8, TT_SB_H)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+  }
+  issued();
+  // ---- [dW1 | db1] = dZ1^T [X | 1] -> [0,112)
+  if (ok && tid == 0) {
+    tc_fence_after();
+#pragma unroll
+    for (int kk = 0; kk < 128 / 16; ++kk)
+      umma_f16(T0, mn_desc(h2 + kk * 2 * TT_SB_H, TT_SB_H), mn_desc(xs + kk * 2 * TT_SB_X, TT_SB_X), ID_DW1, kk > 0);
+    umma_commit(bar);
+  }
+  if (ok) ok = mma_wait();
+  // the tile's gradient (TMEM lane = output neuron) and loss
+  if (ok) {
+    float *P = A.part + (long)blockIdx.x * TT_PSTRIDE;
+    const int o = r;
+    float v[32];
+    if (hf == 0) {
+#pragma unroll 1
+      for (int cc = 0; cc < 2; ++cc) {
+        tmem_ld32(T0 + lb + cc * 32, v);
+#pragma unroll
+        for (int k = 0; k < 32; k += 4) st4f(P + o * NIN + cc * 32 + k, v + k);
+      }
     } else {
-      const int o = q - NOUT * NH;
-      for (int r = 0; r < TILE; ++r) s += dy[r * NOUT + o];
-      atomicAdd(&A.grad[OFF_B3 + o], s);
+      tmem_ld32(T0 + lb + 64, v);
+#pragma unroll
+      for (int k = 0; k < 32; k += 4) st4f(P + o * NIN + 64 + k, v + k);
+      float v8[8];
+      tmem_ld8(T0 + lb + NIN, v8);
+      P[OFF_B1 + o] = v8[0];
     }
-  }
-  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-  if (lane == 0) atomicAdd(A.loss, lsum / (float)A.nb);
-  // dZ2 = (dY W3) * gelu'(Z2)
-  for (int q = tid; q < TILE * NH; q += blockDim.x) {
-    const int r = q / NH, c = q % NH;
-    float v = 0.f;
-    if (row0 + r < A.nb) {
-      const float dh = dy[r * NOUT] * w3[c] + dy[r * NOUT + 1] * w3[NH + c] + dy[r * NOUT + 2] * w3[2 * NH + c];
-      v = dh * gelu_grad_f(A.z2[(long)(row0 + r) * NH + c]);
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+      const int col = hf * 64 + cc * 32;
+      tmem_ld32(T0 + 256 + lb + col, v);
+#pragma unroll
+      for (int k = 0; k < 32; k += 4) st4f(P + OFF_W2 + o * NH + col + k, v + k);
     }
-    const bf16 vb = __float2bfloat16(v);
-    D2[r * LDH + c] = vb;
-    if (row0 + r < A.nb) A.dz2[(long)(row0 + r) * NH + c] = vb;
-  }
-  __syncthreads();
-  // b2 gradient (sum of the rounded dZ2 over the tile rows)
-  for (int c = tid; c < NH; c += blockDim.x) {
-    float s = 0.f;
-    for (int r = 0; r < TILE; ++r) s += __bfloat162float(D2[r * LDH + c]);
-    atomicAdd(&A.grad[OFF_B2 + c], s);
-  }
-  // dH1 = dZ2 W2 (K = 128 outputs of layer 2), then dZ1
-  const int m0 = warp * 16, g = lane >> 2, tq = lane & 3;
-  float acc[16][4];
+    float v8[8];
+    if (hf == 1) {
+      tmem_ld8(T0 + 256 + NH + lb, v8);
+      P[OFF_B2 + o] = v8[0];
+    } else {
+      tmem_ld8(T0 + 400 + lb, v8);
 #pragma unroll
-  for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-#pragma unroll
-  for (int k0 = 0; k0 < NH; k0 += 16) {
-    uint32_t a[4];
-    load_a(a, D2, LDH, m0, k0, lane);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      uint32_t b[2];
-      load_b(b, W2t, LDH, j * 8, k0, lane);
-      mma16816(acc[j], a, b);
+      for (int k = 0; k < NOUT; ++k) P[OFF_W3 + k * NH + o] = v8[k] + v8[NOUT + k];
     }
-  }
-  __syncthreads();
-  float *colsum = red;
-  for (int c = tid; c < NH; c += blockDim.x) colsum[c] = 0.f;
-  __syncthreads();
+    if (tid == 0)
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int col = j * 8 + 2 * tq;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int r = m0 + g + 8 * h;
-      if (row0 + r < A.nb) {
-        const long o = (long)(row0 + r) * NH + col;
-        const bf16 d0 = __float2bfloat16(acc[j][2 * h] * gelu_grad_f(A.z1[o]));
-        const bf16 d1 = __float2bfloat16(acc[j][2 * h + 1] * gelu_grad_f(A.z1[o + 1]));
-        A.dz1[o] = d0;
-        A.dz1[o + 1] = d1;
-        atomicAdd(&colsum[col], __bfloat162float(d0));
-        atomicAdd(&colsum[col + 1], __bfloat162float(d1));
+      for (int k = 0; k < 4; ++k) {
+        const float s = ((fs[TF_RED + k] + fs[TF_RED + 4 + k]) + fs[TF_RED + 8 + k]) + fs[TF_RED + 12 + k];
+        if (k < NOUT) P[OFF_B3 + k] = s;
+        else P[NPARAM] = s;
       }
-    }
   }
+  // a timed-out MMA may still be running: give it a bounded time to land
+  if (*bad && tid == 0) mbar_wait(bar, phase ^ 1u, LIMIT);
+  tc_fence_before();
   __syncthreads();
-  for (int c = tid; c < NH; c += blockDim.x) atomicAdd(&A.grad[OFF_B1 + c], colsum[c]);
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(T0));
 }
 
-size_t mlp_backward_smem() {
-  return (size_t)(NH * LDH + TILE * LDH) * sizeof(bf16) + (size_t)(NOUT * NH + TILE * NOUT + NH) * sizeof(float);
-}
-
-// ---------------------------------------------------------------------------
-// Weight gradient G[o][i] += sum_r D[r][o] * H[r][i] over a chunk of batch
-// rows (tensor cores, K = batch): 8 warps, warp w owns outputs 16w..16w+15.
-// ---------------------------------------------------------------------------
-template <int NI>
-__global__ void __launch_bounds__(256) k_mlp_wgrad(int nb, const bf16 *__restrict__ D, const bf16 *__restrict__ H,
-                                                    float *__restrict__ G, int chunk) {
-  constexpr int KT = 32;            // batch rows per shared-memory stage
-  constexpr int LDK = KT + 8;
-  __shared__ __align__(16) bf16 Ds[NH * LDK];   // Ds[o][r]
-  __shared__ __align__(16) bf16 Hs[NI * LDK];   // Hs[i][r]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = lane >> 2, tq = lane & 3;
-  constexpr int NJ = NI / 8;
-  float acc[NJ][4];
-#pragma unroll
-  for (int j = 0; j < NJ; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-  const int r0 = blockIdx.x * chunk, r1 = min(nb, r0 + chunk);
-  for (int rb = r0; rb < r1; rb += KT) {
-    __syncthreads();
-    for (int t = tid; t < KT * NH; t += blockDim.x) {
-      const int r = t / NH, o = t % NH;
-      Ds[o * LDK + r] = (rb + r < r1) ? D[(long)(rb + r) * NH + o] : __float2bfloat16(0.f);
-    }
-    for (int t = tid; t < KT * NI; t += blockDim.x) {
-      const int r = t / NI, i = t % NI;
-      Hs[i * LDK + r] = (rb + r < r1) ? H[(long)(rb + r) * NI + i] : __float2bfloat16(0.f);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k0 = 0; k0 < KT; k0 += 16) {
-      uint32_t a[4];
-      load_a(a, Ds, LDK, warp * 16, k0, lane);
-#pragma unroll
-      for (int j = 0; j < NJ; ++j) {
-        uint32_t b[2];
-        load_b(b, Hs, LDK, j * 8, k0, lane);
-        mma16816(acc[j], a, b);
-      }
-    }
+// the tiles' gradients summed in tile order (deterministic) into grad and
+// the loss; with adam: one Adam step of the FP32 masters and their BF16
+// copies
+__global__ void __launch_bounds__(256) k_mlp_reduce_adam(const float *__restrict__ part, int nparts,
+                                                         float *__restrict__ grad, float *__restrict__ loss,
+                                                         float *__restrict__ p, float *__restrict__ m,
+                                                         float *__restrict__ v, bf16 *__restrict__ w1b,
+                                                         bf16 *__restrict__ w2b, int adam, float lr, float b1, float b2,
+                                                         float eps, float c1, float c2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > NPARAM) return;
+  float s = 0.f;
+#pragma unroll 8
+  for (int c = 0; c < nparts; ++c) s += part[(long)c * TT_PSTRIDE + t];
+  if (t == NPARAM) {
+    *loss = s;
+    return;
   }
-#pragma unroll
-  for (int j = 0; j < NJ; ++j) {
-    const int col = j * 8 + 2 * tq;
-    const int o0 = warp * 16 + g;
-    atomicAdd(&G[o0 * NI + col], acc[j][0]);
-    atomicAdd(&G[o0 * NI + col + 1], acc[j][1]);
-    atomicAdd(&G[(o0 + 8) * NI + col], acc[j][2]);
-    atomicAdd(&G[(o0 + 8) * NI + col + 1], acc[j][3]);
-  }
+  grad[t] = s;
+  if (!adam) return;
+  const float mm = b1 * m[t] + (1.f - b1) * s;
+  const float vv = b2 * v[t] + (1.f - b2) * s * s;
+  m[t] = mm;
+  v[t] = vv;
+  const float pn = p[t] - lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+  p[t] = pn;
+  if (t < NH * NIN) w1b[t] = __float2bfloat16(pn);
+  else if (t >= OFF_W2 && t < OFF_W2 + NH * NH) w2b[t - OFF_W2] = __float2bfloat16(pn);
 }
-
-// Adam (FP32 masters) followed by the BF16 weight copies
-__global__ void k_adam(float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m,
-                       float *__restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const float g = gr[t];
-    const float mm = b1 * m[t] + (1.f - b1) * g;
-    const float vv = b2 * v[t] + (1.f - b2) * g * g;
-    m[t] = mm;
-    v[t] = vv;
-    p[t] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
-  }
-}
-__global__ void k_refresh_bf16(const float *__restrict__ p, bf16 *__restrict__ w1b, bf16 *__restrict__ w2b,
-                               bf16 *__restrict__ w2tb) {
+__global__ void k_refresh_bf16(const float *__restrict__ p, bf16 *__restrict__ w1b, bf16 *__restrict__ w2b) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < NH * NIN + NH * NH; t += gridDim.x * blockDim.x) {
-    if (t < NH * NIN) {
-      w1b[t] = __float2bfloat16(p[t]);
-    } else {
-      const int q = t - NH * NIN, o = q / NH, i = q % NH;
-      const bf16 v = __float2bfloat16(p[OFF_W2 + q]);
-      w2b[q] = v;
-      w2tb[i * NH + o] = v;
-    }
+    if (t < NH * NIN) w1b[t] = __float2bfloat16(p[t]);
+    else w2b[t - NH * NIN] = __float2bfloat16(p[OFF_W2 + t - NH * NIN]);
   }
 }
 
 int mlp_nparam() { return NPARAM; }
+size_t mlp_part_floats(int nb) { return (size_t)((nb + 127) / 128) * TT_PSTRIDE; }
 
-void launch_mlp_refresh(cudaStream_t s, const float *params, bf16 *w1b, bf16 *w2b, bf16 *w2tb) {
-  k_refresh_bf16<<<64, 256, 0, s>>>(params, w1b, w2b, w2tb);
+void launch_mlp_refresh(cudaStream_t s, const float *params, bf16 *w1b, bf16 *w2b) {
+  k_refresh_bf16<<<64, 256, 0, s>>>(params, w1b, w2b);
 }
 
-// one optimisation step on a batch already staged in x (bf16) and t (fp32)
-void launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, int nb, int step, float lr) {
-  cudaMemsetAsync(B.grad, 0, NPARAM * sizeof(float), s);
-  cudaMemsetAsync(B.loss, 0, sizeof(float), s);
-  launch_mlp_forward(s, B.x, nb, B.w1b, B.w2b, B.params, B.y, B.z1, B.z2, B.h1, B.h2, 1);
-  MlpBwdArgs A{nb, B.y, B.t, B.z1, B.z2, B.h2, B.w2tb, B.params, B.dz1, B.dz2, B.grad, B.loss};
-  k_mlp_backward<<<(nb + TILE - 1) / TILE, 128, mlp_backward_smem(), s>>>(A);
-  const int chunk = 512;
-  const int nchunk = (nb + chunk - 1) / chunk;
-  k_mlp_wgrad<NH><<<nchunk, 256, 0, s>>>(nb, B.dz2, B.h1, B.grad + OFF_W2, chunk);
-  k_mlp_wgrad<NIN><<<nchunk, 256, 0, s>>>(nb, B.dz1, B.x, B.grad, chunk);
+// one optimisation step (adam = 1) or the gradient alone: rows drawn from
+// X, T (n rows) by the (seed, step, row) hash (gather = 1), or rows 0..nb-1
+int launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, const bf16 *X, const float *T, int n, int nb,
+                          unsigned seed, int gather, int step, float lr, int adam, float *y) {
+  const int ntile = (nb + 127) / 128;
+  const MlpTrainArgs A{X, T, n, nb, gather, seed, step, B.w1b, B.w2b, B.params, B.part, y, B.err};
+  k_mlp_train_tc<<<ntile, TT_THREADS, TT_SMEM, s>>>(A);
   const float b1 = 0.9f, b2 = 0.999f;
-  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-  k_adam<<<64, 256, 0, s>>>(B.params, B.grad, B.m, B.v, NPARAM, lr, b1, b2, 1e-8f, c1, c2);
-  k_refresh_bf16<<<64, 256, 0, s>>>(B.params, B.w1b, B.w2b, B.w2tb);
-}
-
-// gradient only (for the check against the CPU reference)
-void launch_mlp_grad(cudaStream_t s, const MlpTrainBuffers &B, int nb) {
-  cudaMemsetAsync(B.grad, 0, NPARAM * sizeof(float), s);
-  cudaMemsetAsync(B.loss, 0, sizeof(float), s);
-  launch_mlp_forward(s, B.x, nb, B.w1b, B.w2b, B.params, B.y, B.z1, B.z2, B.h1, B.h2, 1);
-  MlpBwdArgs A{nb, B.y, B.t, B.z1, B.z2, B.h2, B.w2tb, B.params, B.dz1, B.dz2, B.grad, B.loss};
-  k_mlp_backward<<<(nb + TILE - 1) / TILE, 128, mlp_backward_smem(), s>>>(A);
-  const int chunk = 512;
-  const int nchunk = (nb + chunk - 1) / chunk;
-  k_mlp_wgrad<NH><<<nchunk, 256, 0, s>>>(nb, B.dz2, B.h1, B.grad + OFF_W2, chunk);
-  k_mlp_wgrad<NIN><<<nchunk, 256, 0, s>>>(nb, B.dz1, B.x, B.grad, chunk);
+  const float c1 = adam ? 1.f - powf(b1, (float)step) : 1.f, c2 = adam ? 1.f - powf(b2, (float)step) : 1.f;
+  k_mlp_reduce_adam<<<(NPARAM + 1 + 255) / 256, 256, 0, s>>>(B.part, ntile, B.grad, B.loss, B.params, B.m, B.v, B.w1b,
+                                                             B.w2b, adam, lr, b1, b2, 1e-8f, c1, c2);
+  return 2;
 }
 
 // harvested samples -> standardised training set: X (bf16), T (fp32)
@@ -1015,30 +1103,6 @@ void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *tar
   k_mlp_stage<<<1216, 256, 0, s>>>(n, feat, targ, mu, isig, tmu, tsig, X, T);
 }
 
-// batch of nb rows drawn with replacement by a counter-based hash of
-// (seed, step, row) -- no host round trip between optimisation steps
-__device__ __forceinline__ unsigned mix32(unsigned x) {
-  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
-  return x;
-}
-__global__ void k_mlp_gather(int n, const bf16 *__restrict__ X, const float *__restrict__ T, int nb, unsigned seed,
-                             int step, bf16 *__restrict__ bx, float *__restrict__ bt) {
-  for (int r = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < nb; r += gridDim.x * (blockDim.x / 32)) {
-    const unsigned h = mix32(seed ^ mix32((unsigned)step * 0x9E3779B9U + (unsigned)r));
-    const int src = (int)(h % (unsigned)n);
-    const int lane = threadIdx.x & 31;
-    // 96 bf16 = 48 words per row
-    const uint32_t *xs = reinterpret_cast<const uint32_t *>(X + (long)src * NIN);
-    uint32_t *xd = reinterpret_cast<uint32_t *>(bx + (long)r * NIN);
-    for (int w = lane; w < NIN / 2; w += 32) xd[w] = xs[w];
-    if (lane < NOUT) bt[(long)r * NOUT + lane] = T[(long)src * NOUT + lane];
-  }
-}
-void launch_mlp_gather(cudaStream_t s, int n, const bf16 *X, const float *T, int nb, unsigned seed, int step, bf16 *bx,
-                       float *bt) {
-  k_mlp_gather<<<(nb + 7) / 8 < 1216 ? (nb + 7) / 8 : 1216, 256, 0, s>>>(n, X, T, nb, seed, step, bx, bt);
-}
-
 __global__ void k_f2bf(long n, const float *__restrict__ a, bf16 *__restrict__ b) {
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
     b[q] = __float2bfloat16(a[q]);
@@ -1046,19 +1110,14 @@ __global__ void k_f2bf(long n, const float *__restrict__ a, bf16 *__restrict__ b
 void launch_f2bf(cudaStream_t s, long n, const float *a, bf16 *b) { k_f2bf<<<608, 256, 0, s>>>(n, a, b); }
 
 int mlp_set_smem_limits() {
-  cudaError_t e1 = cudaFuncSetAttribute(k_mlp_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)mlp_forward_smem());
-  cudaError_t e2 = cudaFuncSetAttribute(k_mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)mlp_forward_smem());
-  cudaError_t e3 = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)mlp_backward_smem());
-  cudaError_t e4 = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_infer_smem());
-  cudaError_t e5 = cudaFuncSetAttribute(k_mlp_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-  if (e5 == cudaSuccess)
-    e5 = cudaFuncSetAttribute(k_mlp_infer_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-  return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && e4 == cudaSuccess && e5 == cudaSuccess)
-             ? 0
-             : -1;
+  cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_infer_smem());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mlp_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mlp_infer_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_SMEM);
+  return e == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace ibmk
