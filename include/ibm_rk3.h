@@ -367,12 +367,19 @@ int ibm_sync(ibm_ctx *ctx);
  * passes as the reference for the fallback test.  capacity = 0 stops
  * harvesting and keeps the samples. */
 int ibm_harvest(ibm_ctx *ctx, int capacity, int stride, int passes);
+/* The harvested training set to host arrays: the first min(cap, *n) samples'
+ * features [cap][IBM_NN_IN] and targets [cap][IBM_NN_OUT] (either may be
+ * NULL); *n = the number of samples kept. */
+int ibm_harvest_read(ibm_ctx *ctx, float *feat, float *targ, int cap, int *n);
 /* nsteps Adam steps (lr, betas 0.9/0.999) on batches of `batch` samples drawn
- * with replacement from the harvest, on the GPU (BF16 tensor-core forward and
- * backward, FP32 master weights).  On the first call, or with reinit, the
- * standardisation is computed from the samples and the weights start afresh
- * from `seed`.  *loss = mean squared error of the last batch (standardised
- * units).  Enables the learned correction. */
+ * with replacement from the harvest, on the GPU (forward, backward and weight
+ * gradients on the tcgen05 tensor cores with BF16 operands, FP32 master
+ * weights).  On the first call, or with reinit, the standardisation is
+ * computed from the samples (FP64 column statistics on the device) and the
+ * weights start afresh from `seed`.  *loss = mean squared error of the last
+ * batch (standardised units).  Enables the learned correction and resets the
+ * fallback gate's calibration.  IBM_E_NOT_CONVERGED: a tensor-core wait
+ * timed out. */
 int ibm_train_forcing_model(ibm_ctx *ctx, int nsteps, int batch, double lr, unsigned seed, int reinit,
                             double *loss);
 /* Model transfer: params[IBM_NN_NPARAM], norm[IBM_NN_NNORM].  set enables it. */

@@ -191,6 +191,7 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "probe": (C.c_int, [ctx, C.c_uint]),
         "probe_result": (C.c_int, [ctx, c_double_p, c_int_p]),
         "harvest": (C.c_int, [ctx, C.c_int, C.c_int, C.c_int]),
+        "harvest_read": (C.c_int, [ctx, c_float_p, c_float_p, C.c_int, c_int_p]),
         "train_forcing_model": (C.c_int, [ctx, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_int, c_double_p]),
         "set_forcing_model": (C.c_int, [ctx, c_float_p, c_float_p]),
         "get_forcing_model": (C.c_int, [ctx, c_float_p, c_float_p]),

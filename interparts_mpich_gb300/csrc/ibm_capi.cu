@@ -71,6 +71,7 @@ struct ibm_ctx {
   float *norm = nullptr;       // [198]: feature mean, 1/sigma; target mean, sigma
   float *ly = nullptr;         // [np*nl][3] network output
   double *ls = nullptr;        // learn state, see k_ibm_res_gate
+  double *nscr = nullptr;      // standardisation scratch
   int *gate = nullptr;
   HarvestArgs hv{};
   int hv_passes = 0;
@@ -1021,7 +1022,7 @@ int ibm_destroy(ibm_ctx *c) {
     if (q) cudaFree(q);
   void *lptrs[] = {c->mt.params, c->mt.m, c->mt.v, c->mt.grad, c->mt.loss, c->mt.w1b, c->mt.w2b,
                    c->norm, c->ls, c->gate, c->ly, c->hv.feat, c->hv.pidx, c->hv.targ,
-                   c->hv.count, c->tx, c->tt};
+                   c->hv.count, c->tx, c->tt, c->nscr};
   for (void *q : lptrs)
     if (q) cudaFree(q);
   free_mlp_batch(c->mt);
@@ -1833,6 +1834,21 @@ int ibm_sync(ibm_ctx *c) {
 
 /* --- learned forcing -------------------------------------------------------- */
 
+int ibm_harvest_read(ibm_ctx *c, float *feat, float *targ, int cap, int *n) {
+  if (!c || !n || cap < 0) return IBM_E_INVALID;
+  *n = 0;
+  if (!c->hv.count) return IBM_OK;
+  int cnt[2];
+  CK(cudaMemcpyAsync(cnt, c->hv.count, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *n = cnt[1];
+  const size_t m = (size_t)std::min(cap, cnt[1]);
+  if (feat && m) CK(cudaMemcpyAsync(feat, c->hv.feat, m * 96 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  if (targ && m) CK(cudaMemcpyAsync(targ, c->hv.targ, m * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IBM_OK;
+}
+
 int ibm_harvest(ibm_ctx *c, int capacity, int stride, int passes) {
   if (!c) return IBM_E_INVALID;
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "harvesting needs IBM_MODE_MIXED_LEARNED");
@@ -1886,28 +1902,11 @@ int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsign
   const int n = cnt[1];
   if (n < 1) return set_err(c, IBM_E_STATE, "no harvested samples (ibm_harvest)");
   if (reinit || !c->stats_ready) {
-    // standardisation from the samples (host, once), fresh weights and moments
-    std::vector<float> f((size_t)n * 96), t((size_t)n * 3);
-    CK(cudaMemcpy(f.data(), c->hv.feat, f.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(t.data(), c->hv.targ, t.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    std::vector<float> nrm(198);
-    for (int q = 0; q < 99; ++q) {
-      const int nc = q < 96 ? 96 : 3;
-      const float *a = q < 96 ? f.data() + q : t.data() + (q - 96);
-      double s = 0, s2 = 0;
-      for (int r = 0; r < n; ++r) s += a[(size_t)r * nc];
-      const double mu = s / n;
-      for (int r = 0; r < n; ++r) s2 += (a[(size_t)r * nc] - mu) * (a[(size_t)r * nc] - mu);
-      const double sd = std::sqrt(s2 / n);
-      if (q < 96) {
-        nrm[q] = (float)mu;
-        nrm[96 + q] = sd > 1e-30 ? (float)(1. / sd) : 0.f;
-      } else {
-        nrm[192 + (q - 96)] = (float)mu;
-        nrm[195 + (q - 96)] = sd > 1e-30 ? (float)sd : 1.f;
-      }
-    }
-    CK(cudaMemcpy(c->norm, nrm.data(), nrm.size() * sizeof(float), cudaMemcpyHostToDevice));
+    // standardisation from the samples (device reductions), fresh weights
+    // and moments
+    int st;
+    if (!c->nscr && (st = dalloc(c, &c->nscr, mlp_norm_scratch()))) return st;
+    c->launches += launch_mlp_norm(c->stream, n, c->hv.feat, c->hv.targ, c->nscr, c->norm);
     std::vector<float> w;
     init_mlp_params(w, seed);
     CK(cudaMemcpy(c->mt.params, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));

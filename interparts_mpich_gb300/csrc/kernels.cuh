@@ -201,6 +201,10 @@ int launch_mlp_train_step(cudaStream_t s, const MlpTrainBuffers &B, const __nv_b
 void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *targ, const float *mu, const float *isig,
                       const float *tmu, const float *tsig, __nv_bfloat16 *X, float *T);
 void launch_f2bf(cudaStream_t s, long n, const float *a, __nv_bfloat16 *b);
+// standardisation of n harvested samples into norm[198] (mu, 1/sd of the
+// features; mu, sd of the targets); scratch of mlp_norm_scratch() doubles
+size_t mlp_norm_scratch();
+int launch_mlp_norm(cudaStream_t s, int n, const float *feat, const float *targ, double *scratch, float *norm);
 
 // particle_kernels.cu
 struct PartBuffers {

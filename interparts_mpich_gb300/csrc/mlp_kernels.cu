@@ -1103,6 +1103,54 @@ void launch_mlp_stage(cudaStream_t s, int n, const float *feat, const float *tar
   k_mlp_stage<<<1216, 256, 0, s>>>(n, feat, targ, mu, isig, tmu, tsig, X, T);
 }
 
+// Standardisation of the harvested set: per column (96 features, 3
+// targets) the mean and the standard deviation, two passes in FP64 over
+// fixed row chunks (sums of the chunks in chunk order: deterministic).
+// norm: mu[96], 1/sd[96] (0 for a constant column), target mu[3], sd[3]
+// (1 for a constant column).
+constexpr int NORM_BLOCKS = 608, NORM_COLS = NIN + NOUT;
+__global__ void __launch_bounds__(128) k_mlp_colsum(int n, const float *__restrict__ feat,
+                                                    const float *__restrict__ targ, const double *__restrict__ mu,
+                                                    double *__restrict__ part) {
+  const int c = threadIdx.x;
+  if (c >= NORM_COLS) return;
+  const long chunk = ((long)n + gridDim.x - 1) / gridDim.x;
+  const long r0 = blockIdx.x * chunk, r1 = min((long)n, r0 + chunk);
+  const double m = mu ? mu[c] : 0.;
+  double s = 0.;
+  for (long r = r0; r < r1; ++r) {
+    const double a = c < NIN ? (double)feat[r * NIN + c] : (double)targ[r * NOUT + (c - NIN)];
+    s += mu ? (a - m) * (a - m) : a;
+  }
+  part[(long)blockIdx.x * NORM_COLS + c] = s;
+}
+__global__ void k_mlp_colfinal(int n, int nblk, const double *__restrict__ part, double *__restrict__ mu,
+                               float *__restrict__ norm, int second) {
+  const int c = threadIdx.x;
+  if (c >= NORM_COLS) return;
+  double s = 0.;
+  for (int b = 0; b < nblk; ++b) s += part[(long)b * NORM_COLS + c];
+  s /= (double)n;
+  if (!second) {
+    mu[c] = s;
+    if (c < NIN) norm[c] = (float)s;
+    else norm[2 * NIN + (c - NIN)] = (float)s;
+    return;
+  }
+  const double sd = sqrt(s);
+  if (c < NIN) norm[NIN + c] = sd > 1e-30 ? (float)(1. / sd) : 0.f;
+  else norm[2 * NIN + NOUT + (c - NIN)] = sd > 1e-30 ? (float)sd : 1.f;
+}
+size_t mlp_norm_scratch() { return (size_t)NORM_BLOCKS * NORM_COLS + NORM_COLS; }
+int launch_mlp_norm(cudaStream_t s, int n, const float *feat, const float *targ, double *scratch, float *norm) {
+  double *mu = scratch + (size_t)NORM_BLOCKS * NORM_COLS;
+  k_mlp_colsum<<<NORM_BLOCKS, 128, 0, s>>>(n, feat, targ, nullptr, scratch);
+  k_mlp_colfinal<<<1, 128, 0, s>>>(n, NORM_BLOCKS, scratch, mu, norm, 0);
+  k_mlp_colsum<<<NORM_BLOCKS, 128, 0, s>>>(n, feat, targ, mu, scratch);
+  k_mlp_colfinal<<<1, 128, 0, s>>>(n, NORM_BLOCKS, scratch, mu, norm, 1);
+  return 4;
+}
+
 __global__ void k_f2bf(long n, const float *__restrict__ a, bf16 *__restrict__ b) {
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
     b[q] = __float2bfloat16(a[q]);

@@ -309,6 +309,16 @@ class IBMSolver:
         following forcing loops; capacity=0 stops and keeps the samples."""
         self._chk(self.fn["harvest"](self.ctx, int(capacity), int(stride), int(passes)))
 
+    def harvest_read(self) -> tuple[np.ndarray, np.ndarray]:
+        """The harvested training set: features [n, 96], targets [n, 3]."""
+        n = C.c_int()
+        self._chk(self.fn["harvest_read"](self.ctx, None, None, 0, C.byref(n)))
+        f = np.zeros((n.value, 96), np.float32)
+        t = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            self._chk(self.fn["harvest_read"](self.ctx, _fp(f), _fp(t), n.value, C.byref(n)))
+        return f, t
+
     def train_forcing_model(self, nsteps: int, batch: int = 8192, lr: float = 1e-3, seed: int = 0,
                             reinit: bool = False) -> float:
         loss = C.c_double()

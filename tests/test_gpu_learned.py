@@ -145,6 +145,23 @@ def trained(gpu_lib):
     return s, dt, loss, st
 
 
+def test_standardisation_matches_numpy(trained):
+    """The device's two-pass FP64 column statistics of the harvested set
+    against numpy's on the same samples (read back through the C ABI)."""
+    s = trained[0]
+    f, t = s.harvest_read()
+    assert f.shape[0] > 10000
+    _, norm = s.get_forcing_model()
+    mu, sd = f.astype(np.float64).mean(0), f.astype(np.float64).std(0)
+    tmu, tsd = t.astype(np.float64).mean(0), t.astype(np.float64).std(0)
+    scale = np.maximum(sd, 1e-30)
+    assert np.all(np.abs(norm[:96] - mu) <= 1e-5 * scale + 1e-6 * np.abs(mu))
+    isd = np.where(sd > 1e-30, 1.0 / scale, 0.0)
+    assert np.allclose(norm[96:192], isd, rtol=1e-5, atol=0)
+    assert np.allclose(norm[192:195], tmu, rtol=1e-5, atol=1e-6 * tsd.max())
+    assert np.allclose(norm[195:198], tsd, rtol=1e-5)
+
+
 def _loop_residual(s, dt, nl):
     s.rk(1, dt)
     s.forcing_loop(dt, nl)
