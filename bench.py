@@ -177,13 +177,17 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
 # dominant kernels from one ncu capture of the same command, for the roofline's
 # `traffic` key: {(form, kernel class): bytes}
 TRAFFIC = {
-    ("learned", "predict"): 283552512 + 355950080,  # k_predict_tiled<1>
-    ("mixed", "predict"): 283552512 + 355950080,
-    ("learned", "correc"): 402452992 + 288781568,  # k_correc_mixed
-    ("mixed", "correc"): 402452992 + 288781568,
-    ("learned", "spread"): 238345472 + 39752192,   # k_ibm_spread_f (cold cache)
-    ("mixed", "spread"): 238345472 + 39752192,
-    ("learned", "mlp"): 280366848 + 35936000,      # k_mlp_infer_tc<true> (features formed in the kernel)
+    ("learned", "predict"): 284273152 + 354237696,  # k_predict_quad<1, 0>
+    ("mixed", "predict"): 284273152 + 354237696,
+    ("learned", "correc"): 402418176 + 284520704,  # k_correc_mixed4
+    ("mixed", "correc"): 402418176 + 284520704,
+    ("learned", "spread"): 125048064 + 42400256,   # k_ibm_spread_f<1> (the learned spreading)
+    ("learned", "interp"): 139406080 + 3336704,    # k_ibm_interp_comp_f<-1, 0> (the gate's residual)
+    ("learned", "mlp"): 140426752 + 11782656,      # k_mlp_infer_tc<1> (features formed in the kernel)
+    ("learned", "sphere"): 103032576 + 3572992,    # k_sphere_int<float, 1>
+    ("mixed", "sphere"): 103032576 + 3572992,
+    ("learned", "thomas"): 159725568 + 44540928,   # k_thomas_df
+    ("mixed", "thomas"): 159725568 + 44540928,
 }
 
 
@@ -212,6 +216,8 @@ def kernel_model(case, w: int) -> dict:
         "ifftx": ("hbm", 2 * n * w), "correc": ("hbm", (11 if w == 4 else 9) * n * w),
         "sphere": ("hbm", 3 * sphere_box(case) * case.np * w),
         "features": ("hbm", 3 * ibm * w + npts * 96 * 2), "mlp": ("tensor", 2 * 29184 * npts),
+        # the learned loop's plain passes 2..Nl: no work unless the gate fell back
+        "gated": ("hbm", 0),
     }
 
 
@@ -577,6 +583,11 @@ def main():
         "roofline": {"bound": dk["bound"], "kernel": dom, "achieved": dk["achieved"],
                      "peak": peak_of[dk["bound"]], "unit": dk["unit"], "frac": dk["frac"],
                      "traffic": TRAFFIC.get((head, dom)),
+                     # the DRAM bandwidth the kernel's measured traffic implies (its honest
+                     # roof when it is not bound by its own unit, e.g. the gather-bound MLP)
+                     **({"dram_gbs": round(TRAFFIC[(head, dom)] / (dk["ms_per_launch"] * 1e-3) / 1e9, 1),
+                         "dram_frac": round(TRAFFIC[(head, dom)] / (dk["ms_per_launch"] * 1e-3) / 1e9 / hbm, 4)}
+                        if (head, dom) in TRAFFIC else {}),
                      "algorithmic_per_launch": dk["algorithmic_per_launch"], "ms_per_launch": dk["ms_per_launch"],
                      "peak_source": ("ibm_fp64_peak, FMA chains on all SMs (of measured)" if dk["bound"] == "fp64"
                                      else ("MEASURED_PEAKS.json " + ("hbm_gbs" if dk["bound"] == "hbm" else "bf16_tflops")

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define IBM_ABI_VERSION 2
+#define IBM_ABI_VERSION 3
 
 /* status codes */
 #define IBM_OK                 0
@@ -445,7 +445,8 @@ int ibm_mlp_fit(ibm_ctx *ctx, const float *params_in, const float *x, const floa
 #define IBM_PROBE_MLP         11  /* learned forcing: network inference         */
 #define IBM_PROBE_PHASE       12  /* statistics: phase indicator (both passes)   */
 #define IBM_PROBE_STATS       13  /* statistics: plane sums of post1d            */
-#define IBM_PROBE_N           14
+#define IBM_PROBE_GATED       14  /* learned loop: plain passes 2..Nl, gated     */
+#define IBM_PROBE_N           15
 /* Records CUDA events on the context stream around every launch of the
  * selected classes from now on (a profiler-free per-kernel timer; the events
  * add no GPU work).  ibm_probe_result synchronises, returns per class the

@@ -666,6 +666,11 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
   fi.Fl[0] = c->ib.fxs; fi.Fl[1] = c->ib.fys; fi.Fl[2] = c->ib.fzs;
   fi.dt = dt;
   fi.dti = 1. / dt;
+  fi.dtf = (float)dt;
+  fi.dtif = (float)(1. / dt);
+  fi.hx = (float)g.dx;
+  fi.hy = (float)g.dy;
+  fi.hz = (float)g.dz;
   fi.inv_r = (float)(1. / c->pg.radfp);
   fi.pradfp = c->pg.poly ? c->pg.pradfp : nullptr;
   fi.mu = c->norm;
@@ -685,10 +690,11 @@ int forcing_learned(ibm_ctx *c, double dt, int nl_iter) {
                                                                          c->fv32, c->fw32, dt, -1));
   launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 0, c->stage);
   LAUNCHED(4);  // spreading, force sums, residual interpolation, gate
+  // (their own probe class: they return at once unless the gate fell back)
   for (int it = 1; it < nl_iter; ++it) {
-    PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
-                                                                           c->fv32, c->fw32, dt, 0, c->gate));
-    PROBED(IBM_PROBE_SPREAD,
+    PROBED(IBM_PROBE_GATED, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32,
+                                                                          c->fv32, c->fw32, dt, 0, c->gate));
+    PROBED(IBM_PROBE_GATED,
            launch_ibm_spread_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, LearnedForce{}, c->gate));
     LAUNCHED(2);
   }

@@ -236,26 +236,33 @@ __device__ __forceinline__ float interp27(const CompStencil &s, TAP tap) {
 // D = 16 dx; polydisperse runs size it for the largest sphere)
 constexpr int INTERP_THREADS = 256;
 
-// Sums of three per-thread FP64 values over a block of NT threads (NT a
-// multiple of 32, at least 96) through the [3][NT] shared buffer st: each of
-// three warps sums one value (NT/32 per lane, then across the lanes), so the
-// block spends 3 (NT/32 + 5) FP64 warp instructions instead of a shuffle tree
-// in every warp (FP64 issues at 1/64 of the FP32 rate).  The sums land in
-// res[0..2]; st and res are valid for every thread after the call.
-template <int NT>
-__device__ __forceinline__ void block_sum3(double a, double b, double c, double *st, double *res) {
-  st[threadIdx.x] = a;
-  st[NT + threadIdx.x] = b;
-  st[2 * NT + threadIdx.x] = c;
+// Sums of three per-thread FP32 values over the block in double-float
+// (error-free TwoSum steps on the FP32 pipes, about 48 significant bits, as
+// FP64 sums of the FP32 partials give at these magnitudes), widened to FP64
+// by three threads at the end: no FP64 instruction per warp.  st: 192 floats
+// of shared memory; res[0..2] valid for every thread after the call.
+__device__ __forceinline__ void block_sum3_df(float a, float b, float c, float *st, double *res) {
+  float h[3] = {a, b, c}, l[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float oh = __shfl_xor_sync(0xffffffffu, h[q], d), ol = __shfl_xor_sync(0xffffffffu, l[q], d);
+      df_add(h[q], l[q], oh, ol, h[q], l[q]);
+    }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      st[(2 * q) * 32 + w] = h[q];
+      st[(2 * q + 1) * 32 + w] = l[q];
+    }
   __syncthreads();
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (w < 3) {
-    double x = 0.;
-#pragma unroll
-    for (int q = lane; q < NT; q += 32) x += st[w * NT + q];
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
-    if (lane == 0) res[w] = x;
+  if (threadIdx.x < 3) {
+    const int q = threadIdx.x;
+    float sh = 0.f, sl = 0.f;
+    for (int k = 0; k < nw; ++k) df_add(sh, sl, st[(2 * q) * 32 + k], st[(2 * q + 1) * 32 + k], sh, sl);
+    res[q] = (double)sh + (double)sl;
   }
   __syncthreads();
 }
@@ -290,7 +297,14 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
   extern __shared__ __align__(16) unsigned char ibox_sm[];
   float *box = reinterpret_cast<float *>(ibox_sm);
   __shared__ int bg[8];
+  __shared__ float kc[4];  // FP32 1/dt and grid spacings, converted once per block
   if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
+  if (threadIdx.x == 32) {
+    kc[0] = (float)dti;
+    kc[1] = (float)g.dx;
+    kc[2] = (float)g.dy;
+    kc[3] = (float)g.dz;
+  }
   __syncthreads();
   const bool boxed = box_ok(bg, pg.box_cap, g.I, g.J);
   if (boxed) {
@@ -305,8 +319,8 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
   const float2 Us = c == 0 ? make_float2(vh.x, vl.x) : (c == 1 ? make_float2(vh.y, vl.y) : make_float2(vh.z, vl.z));
   const int4 ref = b.pref[p];
   const float4 cf = b.pcen[p];
-  const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
-  const float dtif = (float)dti;
+  const float hx = kc[1], hy = kc[2], hz = kc[3];
+  const float dtif = kc[0];
   const PointRec *rp = b.rec + t0;
   const int ys = bg[5], zs = bg[5] * bg[6];
   // per-thread force and lever-arm sums in FP32 (a few points per thread),
@@ -362,9 +376,9 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
     if (threadIdx.x == 0) b.rsum[(long)p * 3 + c] = tot;
   }
   __syncthreads();  // the box is dead: its first words hold the partial sums
-  double *st = reinterpret_cast<double *>(ibox_sm);
+  float *st = reinterpret_cast<float *>(ibox_sm);
   __shared__ double res[3];
-  block_sum3<INTERP_THREADS>((double)sF, (double)sa, (double)sb, st, res);
+  block_sum3_df(sF, sa, sb, st, res);
   if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
 }
 // per-particle force and torque of updtlagrforces from the component sums
@@ -462,7 +476,23 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   int *ibox = reinterpret_cast<int *>(spread_sm);
   __shared__ int bg[8];
   __shared__ float spre[SPREAD_PRE];  // prefactors of the staged points
+  // the block's FP32 constants, formed once by one thread (FP64 arithmetic
+  // in every thread, or issued under a false predicate, would occupy the
+  // 1/64-rate FP64 pipe): prefactors F coeff0 (F given) and (U - u~) dti
+  // coeff0 (coeff0 with the particle's own Lagrangian volume when
+  // polydisperse), 1/dt and dt of the learned force
+  __shared__ float kc[7];
   if (threadIdx.x < 8) bg[threadIdx.x] = b.bgeo[((long)p * 3 + c) * 8 + threadIdx.x];
+  if (threadIdx.x == 32) {
+    const double coeff0 = pg.poly ? (pg.pdvl[p] / pg.dVeul) * dt : coeff0_;
+    kc[0] = (float)coeff0;
+    kc[1] = (float)(dti * coeff0);
+    kc[2] = LY ? (float)lf.dti : 0.f;
+    kc[3] = LY ? (float)(1. / lf.dti) : 0.f;
+    kc[4] = (float)g.dx;
+    kc[5] = (float)g.dy;
+    kc[6] = (float)g.dz;
+  }
   __syncthreads();
   const bool boxed = box_ok(bg, pg.box_cap, g.I, g.J);
   const bool staged = boxed && nla <= SPREAD_PRE;
@@ -479,16 +509,13 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
   float sF = 0.f, sa = 0.f, sb = 0.f;
   float4 cf = make_float4(0.f, 0.f, 0.f, 0.f);
   float ysig = 0.f, ymu = 0.f, dtif = 0.f, dtf = 0.f;
-  const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
+  const float hx = kc[4], hy = kc[5], hz = kc[6];
   if constexpr (LY) {
     cf = b.pcen[p];
     ysig = lf.tsig[c]; ymu = lf.tmu[c];
-    dtif = (float)lf.dti; dtf = (float)(1. / lf.dti);
+    dtif = kc[2]; dtf = kc[3];
   }
-  // prefactors F coeff0 (F given) or (U - u~) dti coeff0, as FP32 products
-  // (coeff0 with the particle's own Lagrangian volume when polydisperse)
-  const double coeff0 = pg.poly ? (pg.pdvl[p] / pg.dVeul) * dt : coeff0_;
-  const float pcoef = (float)coeff0, ucoef = (float)(dti * coeff0);
+  const float pcoef = kc[0], ucoef = kc[1];
   // Taps into the box: points in transposed order, the 32 lanes of a warp
   // taking points nq apart in the particle's list (neighbouring points have
   // overlapping stencils, and shared-memory adds to one address in one
@@ -538,8 +565,9 @@ __global__ void __launch_bounds__(SPREAD_THREADS, 3) k_ibm_spread_f(Geo g, PartG
     }
   }
   if constexpr (LY) {  // psum[p][c] for k_ibm_force_sums; rsum for the gate
-    __shared__ double sred[3 * SPREAD_THREADS], res[3];
-    block_sum3<SPREAD_THREADS>((double)sF, (double)sa, (double)sb, sred, res);
+    __shared__ float sred[192];
+    __shared__ double res[3];
+    block_sum3_df(sF, sa, sb, sred, res);
     if (threadIdx.x < 3) b.psum[((long)p * 3 + c) * 3 + threadIdx.x] = res[threadIdx.x];
     if (!lf.incr) {
       const float tot = block_sum_all(r0);

@@ -187,6 +187,7 @@ struct FeatIn {
   const double *pf;    // particle scalar fields (centres, velocities)
   float *Fl[3];      // point forces (FP32)
   double dt, dti;
+  float dtf, dtif, hx, hy, hz;  // FP32 copies of dt, 1/dt and the grid spacings
   float inv_r;
   const double *pradfp;  // polydisperse: per-sphere shell radius (the normal's scale), else null
   const float *mu, *isig;  // feature standardisation

@@ -392,6 +392,9 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
   const int4 ref = fi.pref[p];
   const float4 cf = fi.pcen[p];
   const PointRec rr = fi.rec[t];
+  // the normal's scale (FP32 constants of the launch: no FP64 conversions
+  // per point, which this GPU issues on its 1/64-rate FP64 pipe)
+  const float inv_r = fi.pradfp ? (float)(1. / fi.pradfp[p]) : fi.inv_r;
 #pragma unroll 1
   for (int c = 0; c < 3; ++c) {
     const CompStencil s = make_cs(rr, c, ref.z, g.K);
@@ -422,16 +425,16 @@ __device__ __forceinline__ void feature_row(const FeatIn &fi, long t, unsigned c
           f[(k * 3 + j) * 3 + i] = tv - Uc;
         }
       }
-    const float F0 = ((Uc - acc) + Us.y) * (float)fi.dti;  // (U - u~)/dt, as the first plain pass forms it
+    const float F0 = ((Uc - acc) + Us.y) * fi.dtif;  // (U - u~)/dt, as the first plain pass forms it
     fi.Fl[c][t] = F0;
     f[27] = Uc - acc;
     f[28] = Uc;
     const int dc = c == 0 ? rec_dx(rr.rel) : (c == 1 ? rec_dy(rr.rel) : rec_dz(rr.rel));
     const float frc = c == 0 ? rr.fx : (c == 1 ? rr.fy : rr.fz);
     const float cfc = c == 0 ? cf.x : (c == 1 ? cf.y : cf.z);
-    const float hc = (float)(c == 0 ? g.dx : (c == 1 ? g.dy : g.dz));
-    f[29] = rec_armf(dc, frc, cfc, hc) * (fi.pradfp ? (float)(1. / fi.pradfp[p]) : fi.inv_r);
-    f[30] = (float)F0 * (float)fi.dt;
+    const float hc = c == 0 ? fi.hx : (c == 1 ? fi.hy : fi.hz);
+    f[29] = rec_armf(dc, frc, cfc, hc) * inv_r;
+    f[30] = F0 * fi.dtf;
     f[31] = s.w[3 * c + 1];
     const float *mu = fi.mu + FEAT_PER_COMP * c, *is = fi.isig + FEAT_PER_COMP * c;
 #pragma unroll

@@ -285,9 +285,9 @@ class IBMSolver:
     # --- per-kernel event timing --------------------------------------------------
 
     PROBE_NAMES = ("predict", "stencil", "interp", "spread", "fillps_fftx", "ffty", "thomas", "ifftx", "correc",
-                   "sphere", "features", "mlp", "phase", "stats")
+                   "sphere", "features", "mlp", "phase", "stats", "gated")
 
-    def probe(self, mask: int = (1 << 14) - 1):
+    def probe(self, mask: int = (1 << 15) - 1):
         """Time every launch of the selected kernel classes with CUDA events."""
         self._chk(self.fn["probe"](self.ctx, int(mask)))
 

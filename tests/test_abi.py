@@ -42,7 +42,7 @@ def test_binder_covers_header(lib):
 
 def test_abi_version(lib):
     lib.ibm_abi_version.restype = C.c_int
-    assert lib.ibm_abi_version() == 2
+    assert lib.ibm_abi_version() == 3
 
 
 def test_create_rejects_bad_params_before_touching_the_gpu(lib):

@@ -89,6 +89,7 @@ def test_bench_kernel_model_covers_probe_classes():
                 continue
             assert name in model, name
             bound, units = model[name]
-            assert bound in ("hbm", "tensor", "fp64") and units > 0
+            # the gated plain passes of the learned loop do no work unless the gate fell back
+            assert bound in ("hbm", "tensor", "fp64") and (units > 0 or name == "gated")
     for form, name in bench.TRAFFIC:
         assert form in ("mixed", "learned", "plain") and name in bench.kernel_model(case, 4)
