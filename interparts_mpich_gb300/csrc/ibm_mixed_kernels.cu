@@ -236,36 +236,6 @@ __device__ __forceinline__ float interp27(const CompStencil &s, TAP tap) {
 // D = 16 dx; polydisperse runs size it for the largest sphere)
 constexpr int INTERP_THREADS = 256;
 
-// Sums of three per-thread FP32 values over the block in double-float
-// (error-free TwoSum steps on the FP32 pipes, about 48 significant bits, as
-// FP64 sums of the FP32 partials give at these magnitudes), widened to FP64
-// by three threads at the end: no FP64 instruction per warp.  st: 192 floats
-// of shared memory; res[0..2] valid for every thread after the call.
-__device__ __forceinline__ void block_sum3_df(float a, float b, float c, float *st, double *res) {
-  float h[3] = {a, b, c}, l[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1)
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const float oh = __shfl_xor_sync(0xffffffffu, h[q], d), ol = __shfl_xor_sync(0xffffffffu, l[q], d);
-      df_add(h[q], l[q], oh, ol, h[q], l[q]);
-    }
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  if (lane == 0)
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      st[(2 * q) * 32 + w] = h[q];
-      st[(2 * q + 1) * 32 + w] = l[q];
-    }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    const int q = threadIdx.x;
-    float sh = 0.f, sl = 0.f;
-    for (int k = 0; k < nw; ++k) df_add(sh, sl, st[(2 * q) * 32 + k], st[(2 * q + 1) * 32 + k], sh, sl);
-    res[q] = (double)sh + (double)sl;
-  }
-  __syncthreads();
-}
 // FP32 sum over the block (blockDim a multiple of 32, at most 1024), to every thread
 __device__ __forceinline__ float block_sum_all(float a) {
   __shared__ float part[32];
