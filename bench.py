@@ -174,8 +174,8 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# dominant kernels from one ncu capture of the same command, for the roofline's
-# `traffic` key: {(form, kernel class): bytes}
+# dominant kernels from one ncu capture of the same command (the 256^3 channel
+# with 1000 spheres), for the roofline's `traffic` key: {(form, kernel class): bytes}
 TRAFFIC = {
     ("learned", "predict"): 284273152 + 354237696,  # k_predict_quad<1, 0>
     ("mixed", "predict"): 284273152 + 354237696,
@@ -563,6 +563,9 @@ def main():
     ttab = kernel_table(r, w, "kernels_timed", args.steps)
     dom = max(ttab, key=lambda k: ttab[k]["share_of_step"])
     dk = ttab[dom]
+    # the ncu bytes were captured on the 256^3 channel with 1000 spheres only
+    measured_case = args.workload == "channel" and args.n == 256 and args.np == 1000
+    traffic = TRAFFIC.get((head, dom)) if measured_case else None
     line = {
         "metric": METRIC, "value": round(r["ms"], 4), "unit": "ms/step", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(r["ms"], 4), "higher_is_better": False, "scaling": "weak",
@@ -582,12 +585,12 @@ def main():
         "hbm_roofline_frac_step": round(ab["total"] / (r["ms"] * 1e-3) / 1e9 / hbm, 4),
         "roofline": {"bound": dk["bound"], "kernel": dom, "achieved": dk["achieved"],
                      "peak": peak_of[dk["bound"]], "unit": dk["unit"], "frac": dk["frac"],
-                     "traffic": TRAFFIC.get((head, dom)),
+                     "traffic": traffic,
                      # the DRAM bandwidth the kernel's measured traffic implies (its honest
                      # roof when it is not bound by its own unit, e.g. the gather-bound MLP)
-                     **({"dram_gbs": round(TRAFFIC[(head, dom)] / (dk["ms_per_launch"] * 1e-3) / 1e9, 1),
-                         "dram_frac": round(TRAFFIC[(head, dom)] / (dk["ms_per_launch"] * 1e-3) / 1e9 / hbm, 4)}
-                        if (head, dom) in TRAFFIC else {}),
+                     **({"dram_gbs": round(traffic / (dk["ms_per_launch"] * 1e-3) / 1e9, 1),
+                         "dram_frac": round(traffic / (dk["ms_per_launch"] * 1e-3) / 1e9 / hbm, 4)}
+                        if traffic else {}),
                      "algorithmic_per_launch": dk["algorithmic_per_launch"], "ms_per_launch": dk["ms_per_launch"],
                      "peak_source": ("ibm_fp64_peak, FMA chains on all SMs (of measured)" if dk["bound"] == "fp64"
                                      else ("MEASURED_PEAKS.json " + ("hbm_gbs" if dk["bound"] == "hbm" else "bf16_tflops")
