@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(PTX *PTY) k_predict_tiled(Geo g, const float *
 //   k_predict_pair  rows of 66 cells, one 4-byte load per cell;
 //   k_predict_tma   the k_predict_quad rows, copied by the tensor-memory
 //                   accelerator into a ring of four planes per field.
-constexpr int QTX = 64, QTY = 8, QHY = QTY + 2, QROW = QTX + 4, QKC = 32;
+constexpr int QTX = 64, QTY = 8, QHY = QTY + 2, QROW = QTX + 4;
 constexpr int TBX = QTX + 8, TBY = QTY + 2;  // quad / TMA rows: 72 cells from x = i0 - 4, 10 rows from y = j0 - 1
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -401,7 +401,7 @@ __device__ __forceinline__ void pair_cells(const PairPlanes &P, int x, int y, in
   Geo g, const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,               \
       const float *__restrict__ p, float *__restrict__ ru, float *__restrict__ rv, float *__restrict__ rw,    \
       float *__restrict__ fu, float *__restrict__ fv, float *__restrict__ fw, float f1, float f2_, float f3,  \
-      const double *__restrict__ cb, double bcoef
+      const double *__restrict__ cb, double bcoef, int kc
 
 template <int STAGE, bool BUOY>
 __global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_pair(PREDICT_ARGS) {
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_pair(PREDICT_ARGS)
   constexpr int NT = QTX / 2 * QTY, NH = QHY * (QTX + 2), HQ = (NH + NT - 1) / NT;
   const int tx = threadIdx.x % (QTX / 2), ty = threadIdx.x / (QTX / 2);
   const int i0 = blockIdx.x * QTX, j0 = blockIdx.y * QTY;
-  const int k0 = 1 + blockIdx.z * QKC, k1 = min(g.K, k0 + QKC - 1);
+  const int k0 = 1 + blockIdx.z * kc, k1 = min(g.K, k0 + kc - 1);
   const int i = i0 + 2 * tx, j = j0 + ty;
   const bool in = i < g.I && j < g.J;  // I even: i + 1 < I as well
   const int PL = g.I * g.J;  // 32-bit offsets: launched only for fields < 2^31 cells
@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_quad(PREDICT_ARGS)
   __shared__ __align__(16) float su[3][TBY][TBX], sv[3][TBY][TBX], sw[3][TBY][TBX], sp[2][TBY][TBX];
   const int tx = threadIdx.x % (QTX / 2), ty = threadIdx.x / (QTX / 2);
   const int i0 = blockIdx.x * QTX, j0 = blockIdx.y * QTY;
-  const int k0 = 1 + blockIdx.z * QKC, k1 = min(g.K, k0 + QKC - 1);
+  const int k0 = 1 + blockIdx.z * kc, k1 = min(g.K, k0 + kc - 1);
   const int i = i0 + 2 * tx, j = j0 + ty;
   const bool in = i < g.I && j < g.J;
   const int PL = g.I * g.J;  // 32-bit offsets: launched only for fields < 2^31 cells
@@ -577,7 +577,7 @@ __device__ __forceinline__ void tma_load_plane(const TmaFields &tm, float *slot,
 
 template <int STAGE, bool BUOY>
 __global__ void __launch_bounds__(QTX / 2 * QTY, 3) k_predict_tma(PREDICT_ARGS, const __grid_constant__ TmaFields tm,
-                                                                 int kc, int *__restrict__ err) {
+                                                                 int *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char tma_sm[];
   float *sbase = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tma_sm) + 127) & ~uintptr_t(127));
   __shared__ __align__(8) uint64_t bar[TNS];
@@ -722,6 +722,36 @@ bool encode_field_map(CUtensorMap *m, const Geo &g, const float *f) {
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+// z chunks of a 2.5D predictor launch with nbs resident blocks per SM: the
+// split that keeps the block waves fullest, net of the two halo planes each
+// chunk reads in addition, chunks of at most maxkc planes
+int predict_zchunk(const Geo &g, int nbs, int maxkc) {
+  static int nsm = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
+  }();
+  const int tiles = ((g.I + QTX - 1) / QTX) * ((g.J + QTY - 1) / QTY), slots = std::max(1, nsm * nbs);
+  int kc = g.K;
+  double best = -1.;
+  for (int nz = 1; nz <= std::min(g.K, 64); ++nz) {
+    const int kcz = (g.K + nz - 1) / nz, nb = tiles * ((g.K + kcz - 1) / kcz);
+    if (kcz > maxkc && nz < std::min(g.K, 64)) continue;
+    const double waves = (double)nb / slots, eff = waves / std::ceil(waves) * kcz / (kcz + 2.);
+    if (eff > best + 1e-9) { best = eff; kc = kcz; }
+  }
+  return kc;
+}
+int quad_blocks_per_sm() {
+  static int n = [] {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_predict_quad<2, false>, QTX / 2 * QTY, 0) != cudaSuccess)
+      return 3;
+    return nb > 0 ? nb : 3;
+  }();
+  return n;
+}
 int tma_blocks_per_sm() {
   static int n = [] {
     int nb = 0;
@@ -749,24 +779,11 @@ bool launch_predict_tma(cudaStream_t s, const Geo &g, int stage, const float *u,
   if (!encode_field_map(&tm.u, g, u) || !encode_field_map(&tm.v, g, v) || !encode_field_map(&tm.w, g, w) ||
       !encode_field_map(&tm.p, g, p))
     return false;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // z chunks: the split that keeps the resident-block waves fullest, net of
-  // the two halo planes each chunk reads in addition, at most 24 planes
-  // (measured fastest at 256^3)
-  const int tiles = ((g.I + QTX - 1) / QTX) * ((g.J + QTY - 1) / QTY), slots = std::max(1, nsm * nbs);
-  int kc = g.K;
-  double best = -1.;
-  for (int nz = 1; nz <= std::min(g.K, 64); ++nz) {
-    const int kcz = (g.K + nz - 1) / nz, nb = tiles * ((g.K + kcz - 1) / kcz);
-    if (kcz > 24 && nz < std::min(g.K, 64)) continue;
-    const double waves = (double)nb / slots, eff = waves / std::ceil(waves) * kcz / (kcz + 2.);
-    if (eff > best + 1e-9) { best = eff; kc = kcz; }
-  }
+  // at most 24 planes a chunk (measured fastest at 256^3)
+  const int kc = predict_zchunk(g, nbs, 24);
   dim3 grd((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + kc - 1) / kc);
   auto go = [&](auto kern) {
-    kern<<<grd, QTX / 2 * QTY, TMA_SMEM, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef, tm, kc, err);
+    kern<<<grd, QTX / 2 * QTY, TMA_SMEM, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef, kc, tm, err);
   };
   if (cb) {
     if (stage == 1) go(k_predict_tma<1, true>);
@@ -790,9 +807,10 @@ void launch_predict(cudaStream_t s, const Geo &g, int stage, const TU *u, const 
     if (kind == IBM_PREDICTOR_TMA &&
         launch_predict_tma(s, g, stage, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef, err))
       return;
-    dim3 gq((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + QKC - 1) / QKC);
+    const int kc = predict_zchunk(g, quad_blocks_per_sm(), 64);
+    dim3 gq((g.I + QTX - 1) / QTX, (g.J + QTY - 1) / QTY, (g.K + kc - 1) / kc);
     auto goq = [&](auto kern) {
-      kern<<<gq, QTX / 2 * QTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef);
+      kern<<<gq, QTX / 2 * QTY, 0, s>>>(g, u, v, w, p, ru, rv, rw, fu, fv, fw, a, b, c, cb, bcoef, kc);
     };
     if (g.I % 4 == 0 && (kind == IBM_PREDICTOR_AUTO || kind == IBM_PREDICTOR_TMA)) {
       if (cb) {
