@@ -191,6 +191,12 @@ TRAFFIC = {
 }
 
 
+# untimed steps of the learned form between training and the timed steps:
+# the gate's calibration loops fall after 1, 2, 4 and 8 learned loops of each
+# stage after a new model, then every ninth (calib_period 10)
+LEARNED_SETTLE_STEPS = 12
+
+
 # FP64 flops per cell of the FP64 predictor (momxad/momyad/momzad 3 x 54,
 # pressure gradient 6, RK combination 12-18): the plain form's predictor is
 # bound by the FP64 pipe, not by HBM
@@ -293,6 +299,8 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
         solver.set_predictor_kernel({"auto": 0, "pairs": 1, "cells": 2, "tma": 3}[args.predictor])
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
+    if args.no_graphs:
+        solver.set_step_graphs(False)
     solver.setup(case.initial_fields())
     dt = 0.5 * solver.chkdt()  # frozen dt (0.5 dtmax at t=0, main.f90:151-154)
     if args.workload == "poly":
@@ -308,7 +316,10 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
         if args.workload in ("channel", "poly"):
             # the first warm-up steps: plain passes with harvesting; then GPU training
             learn = harvest_and_train(solver, case, dt, args)
-            nwarm = max(1, nwarm - learn["harvest_steps"])
+            # untimed steps through the gate's early calibration phase after a
+            # new model (calibration loops after 1, 2, 4, 8 learned loops of a
+            # stage), so that the timed steps hold the settled one loop in ten
+            nwarm = max(nwarm, LEARNED_SETTLE_STEPS)
         else:
             # the network is harvested and trained on the 256^3 channel, then
             # runs on this case
@@ -321,20 +332,16 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
             src.close()
             solver.set_forcing_model(p, nrm)
             solver.learned_config(enable=True, fallback_ratio=1.5)
+            nwarm = max(nwarm, LEARNED_SETTLE_STEPS)
     for _ in range(nwarm):
         solver.rk3_step(dt)
     solver.sync()
     phases = solver.timed_step(dt)
-    # untimed steps (as many as the timed ones: the learned form's calibration
-    # loops fall on some steps only) with CUDA events around every kernel
-    # class: the kernel table, and the dominant class, the only one timed
-    # inside the timed steps (events around every class cost about 0.2 ms per step)
+    # the RK stages run as CUDA graphs: capture every stage graph the timed
+    # steps replay now, so that no capture falls inside them
+    if not args.no_graphs:
+        solver.prepare_step_graphs(dt)
     probe_steps = max(1, args.steps)
-    solver.probe()
-    solver.run(dt, probe_steps)
-    kernels_all = solver.probe_result()
-    dom_class = max(kernels_all, key=lambda k: kernels_all[k][0])
-    mask = args.probe_mask if args.probe_mask >= 0 else 1 << solver.PROBE_NAMES.index(dom_class)
     torch.cuda.synchronize()
     launches0 = solver.launch_count()
     barrier(ws)
@@ -342,7 +349,8 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        solver.probe(mask)  # CUDA events around every launch of the selected kernel classes
+        if args.no_graphs:
+            solver.probe(args.probe_mask if args.probe_mask > 0 else (1 << len(solver.PROBE_NAMES)) - 1)
         with torch.cuda.stream(stream):
             torch.cuda.nvtx.range_push("timed")  # profilers select the timed steps by this range
             ev0.record(stream)
@@ -350,11 +358,18 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
             ev1.record(stream)
             torch.cuda.nvtx.range_pop()
         ev1.synchronize()
-    torch.cuda.synchronize()
-    barrier(ws)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    kernels_timed = solver.probe_result()
-    launches = solver.launch_count() - launches0
+        torch.cuda.synchronize()
+        barrier(ws)
+        ms = ev0.elapsed_time(ev1) / args.steps
+        launches = solver.launch_count() - launches0
+        if not args.no_graphs:
+            # the kernel table and the roofline kernel: CUDA events around every
+            # launch of every kernel class over as many further steps, launched
+            # directly (a replayed graph cannot record events per launch); the
+            # kernels are the same, at the same point of the run
+            solver.probe(args.probe_mask if args.probe_mask > 0 else (1 << len(solver.PROBE_NAMES)) - 1)
+            solver.run(dt, probe_steps)
+        kernels_all = solver.probe_result()
     ms_max = max_over_ranks(ms, ws)
     solver.sync()
     _, divmax, _ = solver.chkdiv()
@@ -411,7 +426,7 @@ def run_form(args, ws, rank, local, mode: int, with_e2e: bool):
     solver.close()
     return {"case": case, "dt": dt, "ms": ms_max, "phases": phases, "launches": launches, "clocks": clk.summary(),
             "e2e": e2e, "ncell": case.itot * case.jtot * case.ktot, "divmax": divmax, "learn": learn,
-            "kernels": kernels_all, "kernels_timed": kernels_timed, "probe_steps": probe_steps, "stats": stats}
+            "kernels": kernels_all, "probe_steps": probe_steps, "stats": stats}
 
 
 def cpu_baseline(args, case_fn):
@@ -461,11 +476,12 @@ def main():
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--stats-calls", type=int, default=3, help="post1d calls timed after the steps (0: none)")
     ap.add_argument("--probe-mask", type=int, default=-1,
-                    help="kernel classes timed with CUDA events inside the timed steps (bit per class; "
-                         "default: the dominant class of an untimed probed step)")
+                    help="kernel classes timed with CUDA events (bit per class; default: every class) over as "
+                         "many steps as the timed ones, run right after them (with --no-graphs: inside them)")
     ap.add_argument("--predictor", default="auto", choices=["auto", "pairs", "cells", "tma"],
                     help="FP32 predictor kernel of the mixed forms (auto: planes staged by 16-byte loads; "
                          "tma: by tensor-memory-accelerator copies)")
+    ap.add_argument("--no-graphs", action="store_true", help="issue every launch directly (no CUDA graphs of the stages)")
     ap.add_argument("--proj-solves", type=int, default=0,
                     help="FP32 Poisson solves per projection in the mixed forms (0: the library default)")
     args = ap.parse_args()
@@ -485,7 +501,8 @@ def main():
                 f"D=16dx, perturbed Poiseuille Re_b=5600, Nl=3, dt=0.5 dtmax frozen")
     config = {"workload": desc,
               "grid": [wl.itot, wl.jtot, wl.ktot], "spheres": wl.np,
-              "l2_policy": "inputs larger than L2 (each field >= 137 MB > 129 MB L2)"}
+              "l2_policy": "inputs larger than L2 (each field >= 137 MB > 129 MB L2)",
+              "launch": "per-kernel launches" if args.no_graphs else "CUDA graphs of the RK stages (captured before the timed steps)"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -540,8 +557,7 @@ def main():
     def kernel_table(x, wb, key="kernels", steps=1):
         """Per kernel class: launches and mean duration (CUDA events), the
         algorithmic bytes or flops per launch and the fraction of the peak.
-        key "kernels": the untimed probed steps (every class); "kernels_timed":
-        the classes probed inside the timed steps."""
+        key "kernels": the probed steps (every class)."""
         model = kernel_model(x["case"], wb)
         out = {}
         for name, (tot_ms, cnt) in x[key].items():
@@ -559,8 +575,8 @@ def main():
     ab = algorithmic_bytes(case, w)
     names = ["predictor", "ibm", "projection", "newton_euler"]
     ktab = kernel_table(r, w, "kernels", r["probe_steps"])
-    # the roofline kernel: the dominant class, timed inside the timed steps
-    ttab = kernel_table(r, w, "kernels_timed", args.steps)
+    # the roofline kernel: the class with the largest share of the step
+    ttab = {k: v for k, v in ktab.items() if v["algorithmic_per_launch"] > 0}
     dom = max(ttab, key=lambda k: ttab[k]["share_of_step"])
     dk = ttab[dom]
     # the ncu bytes were captured on the 256^3 channel with 1000 spheres only
@@ -592,6 +608,10 @@ def main():
                          "dram_frac": round(traffic / (dk["ms_per_launch"] * 1e-3) / 1e9 / hbm, 4)}
                         if traffic else {}),
                      "algorithmic_per_launch": dk["algorithmic_per_launch"], "ms_per_launch": dk["ms_per_launch"],
+                     "timing": ("CUDA events around every launch of every kernel class over as many steps as "
+                                "the timed ones, run directly right after them (the timed steps replay CUDA "
+                                "graphs of the RK stages, which cannot record events per launch)"
+                                if not args.no_graphs else "CUDA events around every launch inside the timed steps"),
                      "peak_source": ("ibm_fp64_peak, FMA chains on all SMs (of measured)" if dk["bound"] == "fp64"
                                      else ("MEASURED_PEAKS.json " + ("hbm_gbs" if dk["bound"] == "hbm" else "bf16_tflops")
                                            + " (of measured)") if peaks else "fallback (of fallback)")},

@@ -220,6 +220,18 @@ int ibm_set_projection_solves(ibm_ctx *ctx, int solves);
 #define IBM_PREDICTOR_CELLS 2
 #define IBM_PREDICTOR_TMA   3
 int ibm_set_predictor_kernel(ibm_ctx *ctx, int kind);
+/* CUDA graphs of the RK stages in ibm_rk3_step / ibm_run (default on): each
+ * stage (predictor, forcing loop, projection, Newton-Euler) is captured the
+ * second time it runs with a given dt and forcing kind, and replayed after;
+ * settings that change a stage's launches drop the graphs.  Not used for
+ * timed steps, while probing, harvesting or perturbing the forcing, or with
+ * scalar transport.  enable = 0: every launch issued directly. */
+int ibm_set_step_graphs(ibm_ctx *ctx, int enable);
+/* Captures now, without launching them, the stage graphs that steps with
+ * this dt and the current settings will replay (both forcing kinds of the
+ * learned form), so that no capture falls inside later steps.  Needs one
+ * step run before (launch settings initialised outside a capture). */
+int ibm_prepare_step_graphs(ibm_ctx *ctx, double dt);
 
 /* --- diagnostics ----------------------------------------------------------- */
 

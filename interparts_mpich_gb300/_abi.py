@@ -188,6 +188,8 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         "fp64_peak": (C.c_int, [c_double_p]),
         "set_projection_solves": (C.c_int, [ctx, C.c_int]),
         "set_predictor_kernel": (C.c_int, [ctx, C.c_int]),
+        "set_step_graphs": (C.c_int, [ctx, C.c_int]),
+        "prepare_step_graphs": (C.c_int, [ctx, C.c_double]),
         "probe": (C.c_int, [ctx, C.c_uint]),
         "probe_result": (C.c_int, [ctx, c_double_p, c_int_p]),
         "harvest": (C.c_int, [ctx, C.c_int, C.c_int, C.c_int]),

@@ -83,6 +83,14 @@ struct ibm_ctx {
   // s (the learned forcing's imprint on the flow changes the reduction over
   // the first steps), at most calib_period - 1; period 0: the first only
   int calib_period = 10;
+  // CUDA graphs of whole RK stages (predictor, forcing loop, projection,
+  // Newton-Euler), one per (stage, forcing kind): a stage runs directly the
+  // first time with a given dt and is captured the second, then replayed
+  bool use_graphs = true;
+  cudaGraphExec_t gexec[3][3] = {};
+  double gdt[3][3] = {};
+  long long glaunch[3][3] = {};
+  int gseen[3][3] = {};
   int ncal[3] = {0, 0, 0};               // plain loops measured per stage since the model was set
   long long since[3] = {0, 0, 0};        // learned loops per stage since its last plain loop
   int stage = 0;  // RK stage of the last predictor call (0..2)
@@ -721,21 +729,30 @@ int perturb_forces(ibm_ctx *c, double dt) {
   return IBM_OK;
 }
 
-int forcing(ibm_ctx *c, double dt, int nl_iter) {
+// The forcing loop's kind at the current RK stage, decided on the host (and
+// the calibration schedule's counters advanced): FORCING_PLAIN, the plain
+// passes (and a calibration measurement, FORCING_CALIB), or FORCING_LEARNED.
+enum { FORCING_PLAIN = 0, FORCING_CALIB = 1, FORCING_LEARNED = 2 };
+int forcing_kind(ibm_ctx *c, int nl_iter) {
+  if (!c->mixed || !c->learn_on || c->harvesting || nl_iter < 2 || c->pg.np == 0) return FORCING_PLAIN;
+  const int s = c->stage;
+  const long long gap = std::min<long long>(1LL << std::min(std::max(c->ncal[s] - 1, 0), 30), c->calib_period - 1);
+  if (c->ncal[s] == 0 || (c->calib_period > 0 && c->since[s] >= gap)) {
+    ++c->ncal[s];
+    c->since[s] = 0;
+    return FORCING_CALIB;
+  }
+  ++c->since[s];
+  return FORCING_LEARNED;
+}
+
+// the launches of one forcing loop of the given kind (no host decision)
+int forcing_run(ibm_ctx *c, double dt, int nl_iter, int kind) {
   if (c->pg.np == 0 || nl_iter <= 0) return IBM_OK;
   const Geo &g = c->g;
   if (c->mixed) {
-    bool calibrate = false;
-    if (c->learn_on && !c->harvesting && nl_iter >= 2) {
-      const int s = c->stage;
-      const long long gap = std::min<long long>(1LL << std::min(std::max(c->ncal[s] - 1, 0), 30), c->calib_period - 1);
-      calibrate = c->ncal[s] == 0 || (c->calib_period > 0 && c->since[s] >= gap);
-      if (!calibrate) {
-        ++c->since[s];
-        return forcing_learned(c, dt, nl_iter);
-      }
-    }
-    const bool measure = c->harvesting || calibrate;
+    if (kind == FORCING_LEARNED) return forcing_learned(c, dt, nl_iter);
+    const bool measure = c->harvesting || kind == FORCING_CALIB;
     const long npts = (long)c->pg.np * c->pg.nl;
     const int npass = c->harvesting ? std::max(nl_iter, c->hv_passes) : nl_iter;
     PROBED(IBM_PROBE_STENCIL, launch_ibm_stencil_f(c->stream, g, c->pg, c->ib));
@@ -764,10 +781,6 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
         PROBED(IBM_PROBE_INTERP, c->launches += -1 + launch_ibm_interp_force_f(c->stream, g, c->pg, c->ib, c->fu32, c->fv32, c->fw32, dt, -1));
         launch_ibm_residual_gate(c->stream, c->pg, c->ib, npts, c->ls, c->gate, 1, c->stage);
         LAUNCHED(2);
-        if (calibrate) {
-          ++c->ncal[c->stage];
-          c->since[c->stage] = 0;
-        }
       }
     }
     if (c->harvesting) {
@@ -793,6 +806,8 @@ int forcing(ibm_ctx *c, double dt, int nl_iter) {
   }
   return IBM_OK;
 }
+
+int forcing(ibm_ctx *c, double dt, int nl_iter) { return forcing_run(c, dt, nl_iter, forcing_kind(c, nl_iter)); }
 
 int project_fluid(ibm_ctx *c, int rkiter, double dt) {
   const Geo &g = c->g;
@@ -897,6 +912,100 @@ int newton_euler(ibm_ctx *c, int rkiter, double dt) {
   launch_ne_finalize(c->stream, c->pg, c->pb, c->ib, 0);
   LAUNCHED(1);
   return IBM_OK;
+}
+
+void drop_graphs(ibm_ctx *c) {
+  for (auto &r : c->gexec)
+    for (auto &e : r)
+      if (e) {
+        cudaGraphExecDestroy(e);
+        e = nullptr;
+      }
+  for (auto &r : c->gseen)
+    for (int &n : r) n = 0;
+}
+
+int stage_direct(ibm_ctx *c, int rkiter, double dt, int kind) {
+  int st;
+  if ((st = predict(c, rkiter, dt))) return st;
+  if ((st = forcing_run(c, dt, 3, kind))) return st;
+  if ((st = project(c, rkiter, dt))) return st;
+  return newton_euler(c, rkiter, dt);
+}
+
+// a stage's launches depend on host state only through what the graph keys
+// hold (stage, forcing kind, dt) and the settings whose setters drop the
+// graphs; these conditions change the launch sequence from step to step
+// (scalar transport swaps its buffers every stage) or add host work
+bool graphs_apply(const ibm_ctx *c) {
+  return c->use_graphs && c->probe_mask == 0 && !c->harvesting && !c->cfield &&
+         !(c->noise_sigma[0] > 0 || c->noise_sigma[1] > 0 || c->noise_sigma[2] > 0);
+}
+
+// Captures the stage into its graph (which it replaces) and, with launch,
+// launches it; without, the stage's host state is left as it was.  A failed
+// capture turns the graphs off and (with launch) runs the stage directly.
+int stage_capture(ibm_ctx *c, int rkiter, double dt, int kind, bool launch) {
+  const int s = rkiter - 1;
+  cudaGraphExec_t &ex = c->gexec[s][kind];
+  if (ex) cudaGraphExecDestroy(ex);
+  ex = nullptr;
+  const long long l0 = c->launches;
+  const int stage0 = c->stage;
+  if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGetLastError();
+    c->use_graphs = false;
+    return launch ? stage_direct(c, rkiter, dt, kind) : IBM_OK;
+  }
+  const int st = stage_direct(c, rkiter, dt, kind);
+  const long long ncap = c->launches - l0;  // the stage's launches, counted again at every replay
+  cudaGraph_t gr = nullptr;
+  const cudaError_t e1 = cudaStreamEndCapture(c->stream, &gr);
+  cudaGraphExec_t ne = nullptr;
+  const cudaError_t e2 = (st == IBM_OK && e1 == cudaSuccess) ? cudaGraphInstantiate(&ne, gr, 0) : cudaErrorUnknown;
+  if (gr) cudaGraphDestroy(gr);
+  c->launches = l0;
+  if (st != IBM_OK || e1 != cudaSuccess || e2 != cudaSuccess) {
+    // the stage was only recorded
+    cudaGetLastError();
+    if (ne) cudaGraphExecDestroy(ne);
+    c->use_graphs = false;
+    c->stage = stage0;
+    if (st != IBM_OK) return st;
+    return launch ? stage_direct(c, rkiter, dt, kind) : IBM_OK;
+  }
+  ex = ne;
+  c->gdt[s][kind] = dt;
+  c->gseen[s][kind] = 2;
+  c->glaunch[s][kind] = ncap;
+  if (!launch) {
+    c->stage = stage0;
+    return IBM_OK;
+  }
+  CK(cudaGraphLaunch(ex, c->stream));
+  c->launches += c->glaunch[s][kind];
+  return IBM_OK;
+}
+
+int stage_graph(ibm_ctx *c, int rkiter, double dt, int kind) {
+  const int s = rkiter - 1;
+  cudaGraphExec_t &ex = c->gexec[s][kind];
+  if (c->gdt[s][kind] != dt) {
+    if (ex) cudaGraphExecDestroy(ex);
+    ex = nullptr;
+    c->gdt[s][kind] = dt;
+    c->gseen[s][kind] = 0;
+  }
+  if (ex) {
+    CK(cudaGraphLaunch(ex, c->stream));
+    c->launches += c->glaunch[s][kind];
+    c->stage = s;
+    return IBM_OK;
+  }
+  // first time: directly (lazily initialised launch settings are set up
+  // outside a capture); second time: captured, then launched
+  if (c->gseen[s][kind]++ == 0) return stage_direct(c, rkiter, dt, kind);
+  return stage_capture(c, rkiter, dt, kind, true);
 }
 
 int ready(ibm_ctx *c) {
@@ -1016,6 +1125,7 @@ ibm_ctx *ibm_create(const ibm_params *P) {
 int ibm_destroy(ibm_ctx *c) {
   if (!c) return IBM_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graphs(c);
   void *ptrs[] = {c->u, c->v, c->w, c->p, c->ru, c->rv, c->rw, c->fu, c->fv, c->fw, c->phi, c->spec, c->zt, c->twM,
                   c->twN, c->twJ, c->scratch, c->dout, c->href, c->ib.xfp, c->ib.yfp, c->ib.zfp, c->ib.ul, c->ib.vl,
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
@@ -1342,6 +1452,7 @@ int ibm_get_particles(ibm_ctx *c, ibm_particles *s) {
 
 int ibm_init_particles(ibm_ctx *c, double *vol_calc) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (!c->have_fields) return set_err(c, IBM_E_STATE, "ibm_set_fields has not been called");
   if (c->pg.np == 0) { c->particles_ready = true; if (vol_calc) *vol_calc = 0.; return IBM_OK; }
   if (!c->have_particles) return set_err(c, IBM_E_STATE, "ibm_set_particles has not been called");
@@ -1390,22 +1501,27 @@ static int step_once(ibm_ctx *c, double dt, bool timed) {
   int st;
   float ms[4] = {0, 0, 0, 0};
   for (int rkiter = 1; rkiter <= 3; ++rkiter) {
-    if (timed) CK(cudaEventRecord(c->ev[0], c->stream));
+    if (!timed) {
+      c->stage = rkiter - 1;
+      const int kind = forcing_kind(c, 3);
+      if ((st = graphs_apply(c) ? stage_graph(c, rkiter, dt, kind) : stage_direct(c, rkiter, dt, kind))) return st;
+      continue;
+    }
+    // timed: directly, with events between the phases
+    CK(cudaEventRecord(c->ev[0], c->stream));
     if ((st = predict(c, rkiter, dt))) return st;
-    if (timed) CK(cudaEventRecord(c->ev[1], c->stream));
+    CK(cudaEventRecord(c->ev[1], c->stream));
     if ((st = forcing(c, dt, 3))) return st;
-    if (timed) CK(cudaEventRecord(c->ev[2], c->stream));
+    CK(cudaEventRecord(c->ev[2], c->stream));
     if ((st = project(c, rkiter, dt))) return st;
-    if (timed) CK(cudaEventRecord(c->ev[3], c->stream));
+    CK(cudaEventRecord(c->ev[3], c->stream));
     if ((st = newton_euler(c, rkiter, dt))) return st;
-    if (timed) {
-      CK(cudaEventRecord(c->ev[4], c->stream));
-      CK(cudaEventSynchronize(c->ev[4]));
-      for (int q = 0; q < 4; ++q) {
-        float t = 0;
-        cudaEventElapsedTime(&t, c->ev[q], c->ev[q + 1]);
-        ms[q] += t;
-      }
+    CK(cudaEventRecord(c->ev[4], c->stream));
+    CK(cudaEventSynchronize(c->ev[4]));
+    for (int q = 0; q < 4; ++q) {
+      float t = 0;
+      cudaEventElapsedTime(&t, c->ev[q], c->ev[q + 1]);
+      ms[q] += t;
     }
   }
   if (timed)
@@ -1495,6 +1611,7 @@ int ibm_run_adaptive(ibm_ctx *c, int nsteps, int ioutchk, double *dt, double *ti
 // ---------------------------------------------------------------------------
 int ibm_set_scalar(ibm_ctx *c, const ibm_scalar_params *sp, const double *cf, const double *dcrk) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (!sp || !(sp->pran > 0.)) return set_err(c, IBM_E_INVALID, "scalar parameters need pran > 0");
   if (c->g.zper) return set_err(c, IBM_E_STATE, "no scalar transport with periodic z");
   if ((sp->bc_c_top_type != IBM_BC_C_DIRICHLET && sp->bc_c_top_type != IBM_BC_C_NEUMANN) ||
@@ -1760,6 +1877,7 @@ int ibm_post1d(ibm_ctx *c, double *prof, double *scal) {
 
 int ibm_set_projection_solves(ibm_ctx *c, int solves) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (solves != 1 && solves != 2) return set_err(c, IBM_E_INVALID, "projection solves must be 1 or 2");
   if (!c->mixed) return solves == 1 ? IBM_OK : set_err(c, IBM_E_STATE, "the FP64 form solves once");
   c->proj_solves = solves;
@@ -1768,10 +1886,36 @@ int ibm_set_projection_solves(ibm_ctx *c, int solves) {
 
 int ibm_set_predictor_kernel(ibm_ctx *c, int kind) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (kind != IBM_PREDICTOR_AUTO && kind != IBM_PREDICTOR_PAIRS && kind != IBM_PREDICTOR_CELLS &&
       kind != IBM_PREDICTOR_TMA)
     return set_err(c, IBM_E_INVALID, "predictor kernel must be IBM_PREDICTOR_AUTO, _PAIRS, _CELLS or _TMA");
   c->pred_kind = kind;
+  return IBM_OK;
+}
+
+int ibm_set_step_graphs(ibm_ctx *c, int enable) {
+  if (!c) return IBM_E_INVALID;
+  CK(cudaStreamSynchronize(c->stream));
+  drop_graphs(c);
+  c->use_graphs = enable != 0;
+  return IBM_OK;
+}
+
+int ibm_prepare_step_graphs(ibm_ctx *c, double dt) {
+  int st;
+  if ((st = ready(c))) return st;
+  if (!(dt > 0)) return set_err(c, IBM_E_INVALID, "dt must be > 0");
+  // lazily initialised launch settings are set up by a direct step first
+  if (!graphs_apply(c) || !(c->dt_last > 0)) return IBM_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  const bool learned = c->mixed && c->learn_on && c->pg.np > 0;
+  for (int rkiter = 1; rkiter <= 3; ++rkiter)
+    for (int kind = FORCING_PLAIN; kind <= FORCING_LEARNED; ++kind) {
+      if (learned ? kind == FORCING_PLAIN : kind != FORCING_PLAIN) continue;
+      if ((st = stage_capture(c, rkiter, dt, kind, false))) return st;
+      if (!c->use_graphs) return IBM_OK;
+    }
   return IBM_OK;
 }
 
@@ -1857,6 +2001,7 @@ int ibm_harvest_read(ibm_ctx *c, float *feat, float *targ, int cap, int *n) {
 
 int ibm_harvest(ibm_ctx *c, int capacity, int stride, int passes) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "harvesting needs IBM_MODE_MIXED_LEARNED");
   if (capacity < 0 || (capacity > 0 && (stride < 1 || passes < 0))) return set_err(c, IBM_E_INVALID, "bad harvest arguments");
   if (capacity == 0) {
@@ -1899,6 +2044,7 @@ static int reset_gate_factors(ibm_ctx *c) {
 
 int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsigned seed, int reinit, double *loss) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "training needs IBM_MODE_MIXED_LEARNED");
   if (nsteps < 0 || batch < 1 || !(lr > 0)) return set_err(c, IBM_E_INVALID, "bad training arguments");
   if (!c->hv.count) return set_err(c, IBM_E_STATE, "no harvested samples (ibm_harvest)");
@@ -1962,6 +2108,7 @@ int ibm_train_forcing_model(ibm_ctx *c, int nsteps, int batch, double lr, unsign
 
 int ibm_set_forcing_model(ibm_ctx *c, const float *params, const float *norm) {
   if (!c || !params || !norm) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "a model needs IBM_MODE_MIXED_LEARNED");
   CK(cudaMemcpyAsync(c->mt.params, params, mlp_nparam() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->norm, norm, 198 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
@@ -1986,6 +2133,7 @@ int ibm_get_forcing_model(ibm_ctx *c, float *params, float *norm) {
 
 int ibm_learned_config(ibm_ctx *c, int enable, double fallback_ratio, double plain_rms_ref) {
   if (!c) return IBM_E_INVALID;
+  drop_graphs(c);  // the captured stages may depend on what this changes
   if (c->mode != IBM_MODE_MIXED_LEARNED) return set_err(c, IBM_E_STATE, "needs IBM_MODE_MIXED_LEARNED");
   if (enable && !c->model_ready) return set_err(c, IBM_E_STATE, "no model to enable");
   if (!(fallback_ratio > 0) || plain_rms_ref < 0) return set_err(c, IBM_E_INVALID, "bad learned-forcing settings");

@@ -272,6 +272,14 @@ class IBMSolver:
         _CELLS: one cell per thread)."""
         self._chk(self.fn["set_predictor_kernel"](self.ctx, int(kind)))
 
+    def set_step_graphs(self, enable: bool):
+        """CUDA graphs of the RK stages (default on); off: every launch direct."""
+        self._chk(self.fn["set_step_graphs"](self.ctx, int(bool(enable))))
+
+    def prepare_step_graphs(self, dt: float):
+        """Capture the stage graphs that steps with this dt will replay."""
+        self._chk(self.fn["prepare_step_graphs"](self.ctx, float(dt)))
+
     def set_stream(self, stream_handle: int | None):
         self._chk(self.fn["set_stream"](self.ctx, C.c_void_p(stream_handle or 0)))
 
