@@ -519,7 +519,7 @@ int alloc_all(ibm_ctx *c) {
       if ((st = dalloc(c, &c->ib.pvl, (size_t)np))) return st;
       if ((st = dalloc(c, &c->ib.slip, 3 * npl))) return st;
       if ((st = dalloc(c, &c->ib.bgeo, (size_t)24 * np))) return st;
-      if ((st = dalloc(c, &c->ib.rowx, (size_t)3 * IBM_BOX_ROWS * np))) return st;
+      if ((st = dalloc(c, &c->ib.rowm, (size_t)3 * IBM_BOX_ROWS * np))) return st;
       if ((st = dalloc(c, &c->ib.psum, (size_t)9 * np))) return st;
       if ((st = dalloc(c, &c->ib.rsum, (size_t)3 * np))) return st;
     } else {
@@ -1131,7 +1131,7 @@ int ibm_destroy(ibm_ctx *c) {
                   c->ib.wl, c->ib.dudtl, c->ib.dvdtl, c->ib.dwdtl, c->ib.fxl, c->ib.fyl, c->ib.fzl, c->ib.st,
                   c->ib.nla, c->ib.diag, c->pb.pf, c->pb.cf, c->pb.qmax, c->pb.firstc, c->pb.ofirstc, c->pb.nb,
                   c->pb.mslv, c->pb.rkp, c->pb.sincos, c->pb.err, c->pb.red, c->pb.pos4, c->pb.cstart, c->pb.cfill, c->pb.citem, c->pb.ccell, c->ru32, c->rv32, c->rw32, c->fu32,
-                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.fxs, c->ib.fys, c->ib.fzs, c->ib.pvh, c->ib.pvl, c->ib.slip, c->ib.bgeo, c->ib.rowx, c->u32, c->v32,
+                  c->fv32, c->fw32, c->phi32, c->phi32b, c->spec32, c->twM32, c->twN32, c->twJ32, c->ib.rec, c->ib.pref, c->ib.pcen, c->ib.fxs, c->ib.fys, c->ib.fzs, c->ib.pvh, c->ib.pvl, c->ib.slip, c->ib.bgeo, c->ib.rowm, c->u32, c->v32,
                   c->w32, c->p32, c->plo32, c->thomas_df, c->ib.psum, c->ib.rsum, c->noise_y, c->noise_par, c->ph.G, c->ph.W0, c->ph.W1, c->stat_part,
                   c->cfield, c->cnext, c->crk, c->ferr, c->psize, c->pcount};
   for (void *q : ptrs)

@@ -87,17 +87,18 @@ __global__ void __launch_bounds__(256) k_ibm_points(Geo g, PartGeo pg, IbmBuffer
 // bgeo[(p*3 + c)*8 + ] = {refx, refy, bmin_x, bmin_y, bmin_z, nbx, nby, nbz};
 // x, y relative to the particle's reference floor, box cell (cx,cy,cz) =
 // tap (refx + bmin_x + cx, refy + bmin_y + cy, bmin_z + cz).  With at most
-// IBM_BOX_ROWS rows, rowx[(p*3 + c)*IBM_BOX_ROWS + cz*nby + cy] = the x
-// extent (first, last cell) the stencils touch in that row (first > last:
-// none): a sphere's shell touches about 40 % of its box.
+// IBM_BOX_ROWS rows and at most 32 cells in x, rowm[(p*3 + c)*IBM_BOX_ROWS +
+// cz*nby + cy] = the cells the stencils touch in that row (bit cx): a
+// sphere's shell touches about 40 % of its box, and a row through the
+// sphere only its two ends.
 __global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, int K) {
   const int p = blockIdx.x, c = blockIdx.y;
   const int nla = b.nla[p];
   const PointRec *rp = b.rec + (long)p * pg.nl;
   __shared__ int mn[3], mx[3];
-  __shared__ int rlo[IBM_BOX_ROWS], rhi[IBM_BOX_ROWS];
+  __shared__ unsigned rm[IBM_BOX_ROWS];
   if (threadIdx.x < 3) { mn[threadIdx.x] = 0x7fffffff; mx[threadIdx.x] = -0x7fffffff; }
-  for (int q = threadIdx.x; q < IBM_BOX_ROWS; q += blockDim.x) { rlo[q] = 0x7fff; rhi[q] = -1; }
+  for (int q = threadIdx.x; q < IBM_BOX_ROWS; q += blockDim.x) rm[q] = 0u;
   __syncthreads();
   const int4 ref = b.pref[p];
   int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
@@ -110,23 +111,20 @@ __global__ void __launch_bounds__(256) k_ibm_box_geom(PartGeo pg, IbmBuffers b, 
     if ((threadIdx.x & 31) == 0) { atomicMin(&mn[d], wl); atomicMax(&mx[d], wh); }
   }
   __syncthreads();
-  const int nby = mx[1] - mn[1] + 3, nbz = mx[2] - mn[2] + 3;
-  if (nla > 0 && nby * nbz <= IBM_BOX_ROWS) {
+  const int nbx = mx[0] - mn[0] + 3, nby = mx[1] - mn[1] + 3, nbz = mx[2] - mn[2] + 3;
+  if (nla > 0 && nby * nbz <= IBM_BOX_ROWS && nbx <= 32) {
     for (int l = threadIdx.x; l < nla; l += blockDim.x) {
       const CompStencil s = make_cs(rp[l], c, ref.z, K);
       const int x0 = s.b[0] - mn[0], y0 = s.b[1] - mn[1], z0 = s.b[2] - mn[2];
+      const unsigned bits = 7u << x0;  // cells x0 .. x0 + 2 (x0 + 2 < nbx <= 32)
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const int row = (z0 + k) * nby + y0 + j;
-          atomicMin(&rlo[row], x0);
-          atomicMax(&rhi[row], x0 + 2);
-        }
+        for (int j = 0; j < 3; ++j) atomicOr(&rm[(z0 + k) * nby + y0 + j], bits);
     }
     __syncthreads();
-    short2 *rx = b.rowx + ((long)p * 3 + c) * IBM_BOX_ROWS;
-    for (int q = threadIdx.x; q < nby * nbz; q += blockDim.x) rx[q] = make_short2((short)rlo[q], (short)rhi[q]);
+    unsigned *rx = b.rowm + ((long)p * 3 + c) * IBM_BOX_ROWS;
+    for (int q = threadIdx.x; q < nby * nbz; q += blockDim.x) rx[q] = rm[q];
   }
   if (threadIdx.x == 0) {
     int *o = b.bgeo + ((long)p * 3 + c) * 8;
@@ -158,23 +156,24 @@ __device__ __forceinline__ int box_off(const CompStencil &s, const int *bg) {
   return ((s.b[2] - bg[4]) * bg[6] + (s.b[1] - bg[3])) * bg[5] + (s.b[0] - bg[2]);
 }
 __device__ __forceinline__ void load_box(const Geo &g, const float *__restrict__ F, const int *bg, float *box,
-                                         const short2 *__restrict__ rowx) {
+                                         const unsigned *__restrict__ rowm) {
   const int nbx = bg[5], nby = bg[6], nxy = nbx * nby, nbox = nxy * bg[7];
   const int x0 = bg[0] + bg[2], y0 = bg[1] + bg[3], z0 = bg[4];
   if ((g.I & 3) == 0) {
     // rows read as 16-byte quads of x-cells (aligned: I is a multiple of 4,
     // so a quad never straddles the periodic wrap); cells outside the row
-    // are dropped, and so are quads outside the row's recorded extent (the
-    // cells no stencil reads)
+    // are dropped, and so are quads holding none of the cells the stencils
+    // read (the row masks of k_ibm_box_geom, for boxes up to 32 cells wide)
     const int a0 = x0 - (((x0 % 4) + 4) % 4);
     const int nq = (x0 + nbx - a0 + 3) >> 2, nrow = nby * bg[7];
-    const bool ext = nrow <= IBM_BOX_ROWS;
+    const bool masked = nrow <= IBM_BOX_ROWS && nbx <= 32;
     for (int e = threadIdx.x; e < nrow * nq; e += blockDim.x) {
       const int row = e / nq, t = e - row * nq;
       const int cz = row / nby, cy = row - cz * nby, gx = a0 + 4 * t;
-      if (ext) {
-        const short2 xr = rowx[row];
-        if (gx + 3 - x0 < xr.x || gx - x0 > xr.y) continue;
+      if (masked) {
+        const unsigned m = rowm[row];
+        const int sh = gx - x0;  // first cell of the quad, -3 .. nbx - 1
+        if (((sh >= 0 ? m >> sh : m << -sh) & 0xFu) == 0u) continue;
       }
       const float4 v =
           __ldg(reinterpret_cast<const float4 *>(&F[fidx(g, wrapm(gx, g.I), wrapm(y0 + cy, g.J), z0 + cz)]));
@@ -278,7 +277,7 @@ __global__ void __launch_bounds__(INTERP_THREADS, 4) k_ibm_interp_comp_f(Geo g, 
   __syncthreads();
   const bool boxed = box_ok(bg, pg.box_cap, g.I, g.J);
   if (boxed) {
-    load_box(g, F, bg, box, b.rowx + ((long)p * 3 + c) * IBM_BOX_ROWS);
+    load_box(g, F, bg, box, b.rowm + ((long)p * 3 + c) * IBM_BOX_ROWS);
     __syncthreads();
   }
   double *dud = c == 0 ? b.dudtl : (c == 1 ? b.dvdtl : b.dwdtl);

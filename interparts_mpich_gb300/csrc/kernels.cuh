@@ -89,7 +89,7 @@ struct IbmBuffers {
   float4 *pcen;      // mixed form: [np] centre position in cells relative to the reference floor (FP32)
   float *slip;       // mixed form: [3][np*nl] slip U - u~ of the last pass (FP32)
   int *bgeo;         // mixed form: [np][3][8] per-particle stencil boxes
-  short2 *rowx;      // mixed form: [np][3][IBM_BOX_ROWS] x extent of every box row the stencils touch
+  unsigned *rowm;    // mixed form: [np][3][IBM_BOX_ROWS] the cells of every box row the stencils touch (bit cx)
   int *nla;          // [np]
   double *pf;        // particle scalar fields [PF_N*np]
   double *diag;      // [8] force totals etc.
