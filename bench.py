@@ -177,13 +177,13 @@ def algorithmic_bytes(case, w: int = 8) -> dict:
 # dominant kernels from one ncu capture of the same command (the 256^3 channel
 # with 1000 spheres), for the roofline's `traffic` key: {(form, kernel class): bytes}
 TRAFFIC = {
-    ("learned", "predict"): 284273152 + 354237696,  # k_predict_quad<1, 0>
-    ("mixed", "predict"): 284273152 + 354237696,
+    ("learned", "predict"): 282611200 + 352861696,  # k_predict_quad<1, 0> (37-plane z chunks)
+    ("mixed", "predict"): 282611200 + 352861696,
     ("learned", "correc"): 402418176 + 284520704,  # k_correc_mixed4
     ("mixed", "correc"): 402418176 + 284520704,
-    ("learned", "spread"): 125048064 + 42400256,   # k_ibm_spread_f<1> (the learned spreading)
-    ("learned", "interp"): 139406080 + 3336704,    # k_ibm_interp_comp_f<-1, 0> (the gate's residual)
-    ("learned", "mlp"): 140426752 + 11782656,      # k_mlp_infer_tc<1> (features formed in the kernel)
+    ("learned", "spread"): 125088000 + 42448384,   # k_ibm_spread_f<1> (the learned spreading)
+    ("learned", "interp"): 139311360 + 3998720,    # k_ibm_interp_comp_f<-1, 0> (the gate's residual)
+    ("learned", "mlp"): 140372992 + 11529984,      # k_mlp_infer_tc<1> (features formed in the kernel)
     ("learned", "sphere"): 103032576 + 3572992,    # k_sphere_int<float, 1>
     ("mixed", "sphere"): 103032576 + 3572992,
     ("learned", "thomas"): 159725568 + 44540928,   # k_thomas_df
