@@ -2,7 +2,7 @@
 give the same state as runs with every launch issued directly (to the
 rounding the IBM spreading's atomic flush order leaves: the same run is not
 bit-reproducible either), the same launch count, the same contact lists, and
-the learned form the same calibration schedule and fallbacks."""
+the learned form the same calibration schedule."""
 import numpy as np
 import pytest
 
@@ -22,7 +22,9 @@ def _run(case, mode, graphs, nsteps, model=None):
     s.set_step_graphs(graphs)
     if model is not None:
         s.set_forcing_model(*model)
-        s.learned_config(enable=True, fallback_ratio=1.5)
+        # no fallbacks: a device decision near the threshold could differ between two runs at
+        # rounding level; the calibration schedule (host-side) still runs both forcing kinds
+        s.learned_config(enable=True, fallback_ratio=1e9)
     dt = 0.5 * s.chkdt()
     l0 = s.launch_count()
     s.run(dt, nsteps)  # a stage runs directly once, is captured the second time, replayed after
@@ -65,8 +67,8 @@ def test_stage_graphs_learned_form(gpu_lib):
     direct = _run(case, IBM_MODE_MIXED_LEARNED, False, 12, model)
     graphed = _run(case, IBM_MODE_MIXED_LEARNED, True, 12, model)
     assert graphed["launches"] == direct["launches"] > 0
-    for key in ("learned_loops", "fallbacks"):
-        assert graphed["learned"][key] == direct["learned"][key], key
+    assert graphed["learned"]["learned_loops"] == direct["learned"]["learned_loops"]
+    assert graphed["learned"]["fallbacks"] == direct["learned"]["fallbacks"] == 0
     assert graphed["gate"]["plain_loops"] == direct["gate"]["plain_loops"]
     assert direct["learned"]["learned_loops"] > 0 and direct["gate"]["plain_loops"] > 0
     errs = field_errors(graphed["fields"], direct["fields"], ("u", "v", "w"))
